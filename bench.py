@@ -1,0 +1,382 @@
+"""Benchmark of the GB300 volume ray caster (one JSON line on rank 0).
+
+Default workload (the headline configuration): extinction-based shading of a
+256^3 u16 value-noise volume (4 octaves, lacunarity 2, gain 0.5, 4 nested
+shells) rendered at 1024^2 with SAT ambient occlusion (radii 2, 6, 16 voxels)
+and a directional SAT cone shadow, step 0.5 voxel.  A step is one frame.
+
+  value  : Msamples/s of the render kernel with inputs resident in HBM
+           (primary-ray steps counted by the kernel / CUDA-event time), L2
+           flushed between timed frames.
+  e2e    : the same metric through the C ABI from host buffers: per step the
+           volume is copied from pinned host memory (cvr_set_volume), the SAT
+           is rebuilt (cvr_build_sat) and the frame is rendered and read back
+           (cvr_render_host) — the Init() + Redraw() + readback sequence.
+  roofline: algorithmic gather bytes of the marcher per launch / kernel time
+           against the measured HBM copy bandwidth.
+  cpu_baseline: the FP32 CPU oracle (a restatement of the reference shaders)
+           on all host cores over a band of rows of the same frame.
+
+--impl reference times that CPU restatement alone (the reference's own GLSL
+path needs OpenGL, which neither machine has).
+With torchrun (N > 1) every rank renders its own frame on its own GPU
+(replicas; the path needs no exchange), timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD_DESC = {
+    "extinction": "extinction SAT shading: 256^3 u16 value-noise shells -> 1024^2, AO radii {2,6,16} + "
+                  "directional SAT cone shadow, step 0.5 voxel",
+    "plain": "plain ray casting: 64^3 u8 8-blob volume, unit cube -> 256^2, step 0.5 voxel",
+    "cone": "cone DOS shading: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 5-level extinction pyramid, "
+            "occlusion + point-light shadow cones",
+    "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
+                    "1 shadow ray to a point light, 1-voxel light steps",
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(values, ws):
+    """Barrier + max over ranks (gloo on host tensors); identity for one rank."""
+    if ws == 1:
+        return values
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def barrier_sum(values, ws):
+    if ws == 1:
+        return values
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor(values, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return t.tolist()
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"cvr_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = [l.split(",") for l in self.path.read_text().splitlines() if l.strip()]
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        self.path.unlink(missing_ok=True)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profile_traffic(workload):
+    """Per-launch DRAM traffic of the marcher from the committed ncu summary."""
+    for p in sorted((ROOT / "profiles").glob(f"*{workload}*.md")):
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", p.read_text())
+        if m:
+            return float(m.group(1)), p.name
+    return None, None
+
+
+def algorithmic_bytes(wl, st, abi):
+    """Algorithmic bytes of one frame: 8 voxel texels per primary sample,
+    plus per secondary fetch 64 int64 SAT texels (extinction), 8 float32
+    pyramid texels (cone) or 8 voxel texels (ground truth), plus the image."""
+    bvox = 1 if wl.dtype == abi.CVR_U8 else 2
+    per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 8, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox}[wl.method]
+    return st.samples * 8 * bvox + st.aux_fetches * per_aux + wl.width * wl.height * 16
+
+
+def cpu_baseline(wl, target_s=12.0, threads=None):
+    """FP32 oracle on all host cores over a centred band of rows."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    orc = oracle.Oracle()
+    oracle.prepare(orc, wl)
+    H = wl.height
+    band = max(1, H // 128)
+    mid = H // 2
+    t0 = time.perf_counter()
+    _, _, n0 = orc.render(wl.method, wl.cam, wl.light, wl.params, wl.width, H, precision=32,
+                          rows=(mid - band // 2, mid - band // 2 + band), threads=threads)
+    dt = time.perf_counter() - t0
+    rows = int(min(H, max(band, band * target_s / max(dt, 1e-3))))
+    y0 = max(0, mid - rows // 2)
+    t0 = time.perf_counter()
+    _, _, n = orc.render(wl.method, wl.cam, wl.light, wl.params, wl.width, H, precision=32, rows=(y0, y0 + rows),
+                         threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt / 1e6, "unit": "Msamples/s", "cores": threads, "kind": "port",
+            "sample": f"rows {y0}..{y0 + rows} of the {wl.width}x{H} frame ({n} samples, {dt:.1f} s, FP32 oracle, "
+                      f"OpenMP over rows)"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from cpp_volume_rendering_gb300 import scene
+    import oracle
+    oracle.build()
+    wl = scene.workload(args.workload)
+    threads = os.cpu_count() or 1
+    orc = oracle.Oracle()
+    oracle.prepare(orc, wl)
+    H = wl.height
+    band = max(1, H // 128)
+    mid = H // 2
+    # size each step's band of rows so the whole run stays within a few minutes
+    t0 = time.perf_counter()
+    orc.render(wl.method, wl.cam, wl.light, wl.params, wl.width, H, precision=32,
+               rows=(mid - band // 2, mid - band // 2 + band), threads=threads)
+    dt = time.perf_counter() - t0
+    per_step_s = min(20.0, 150.0 / max(1, args.steps + args.warmup))
+    rows = int(min(H, max(band, band * per_step_s / max(dt, 1e-3))))
+    y0 = max(0, mid - rows // 2)
+    for _ in range(args.warmup):
+        orc.render(wl.method, wl.cam, wl.light, wl.params, wl.width, H, precision=32, rows=(y0, y0 + rows),
+                   threads=threads)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, n = orc.render(wl.method, wl.cam, wl.light, wl.params, wl.width, H, precision=32,
+                             rows=(y0, y0 + rows), threads=threads)
+        tot_t += time.perf_counter() - t0
+        tot_n += n
+    value = tot_n / tot_t / 1e6
+    sample = f"rows {y0}..{y0 + rows} of the {wl.width}x{H} frame per step, FP32 oracle on {threads} threads"
+    print(json.dumps({
+        "impl": "reference", "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD_DESC[args.workload]},
+        "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference renders with GLSL compute shaders (OpenGL); no graphics stack exists on this box, "
+                "so its CPU-side restatement (the oracle) is what is timed"}))
+
+
+def time_frames(ctx, lib, wl, params, out_ptr, steps, warmup, flush=True):
+    import ctypes as C
+    from cpp_volume_rendering_gb300 import abi
+    cam, lt = wl.cam, wl.light
+    for _ in range(warmup):
+        abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(cam), C.byref(lt), C.byref(params), C.sizeof(params),
+                                 out_ptr, wl.width, wl.height, None, None), ctx.h)
+    abi.check(lib.cvr_sync(ctx.h), ctx.h)
+    times = []
+    ms = C.c_float()
+    for _ in range(steps):
+        if flush:
+            abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+        abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+        abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(cam), C.byref(lt), C.byref(params), C.sizeof(params),
+                                 out_ptr, wl.width, wl.height, None, None), ctx.h)
+        abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+        times.append(ms.value)
+    return times
+
+
+def run_ours(args):
+    import ctypes as C
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    from cpp_volume_rendering_gb300 import abi, build, scene
+    build.build()
+    lib = abi.load()
+    wl = scene.workload(args.workload)
+    ctx = scene.Context(local)
+    scene.prepare(ctx, wl)
+    out = C.POINTER(C.c_float)()
+    abi.check(lib.cvr_get_frame_buffer(ctx.h, wl.width, wl.height, C.byref(out)), ctx.h)
+    out_ptr = C.cast(out, C.c_void_p)
+    params = wl.params
+    # one stats frame: sample counts are deterministic for a fixed frame
+    st = abi.FrameStats()
+    abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),
+                             out_ptr, wl.width, wl.height, None, C.byref(st)), ctx.h)
+    barrier_max([0.0], ws)
+    with ClockSampler(local) as clk:
+        times = time_frames(ctx, lib, wl, params, out_ptr, args.steps, args.warmup)
+    clocks = clk.summary()
+    total_ms = sum(times)
+    total_ms, = barrier_max([total_ms], ws)
+    samples_all, = barrier_sum([float(st.samples * args.steps)], ws)
+    value = samples_all / (total_ms / 1000.0) / 1e6
+    ms_per_step = total_ms / args.steps
+    # roofline of the dominant kernel (the marcher is the only launch per frame)
+    alg = algorithmic_bytes(wl, st, abi)
+    med_ms = statistics.median(times)
+    achieved = alg / (med_ms / 1000.0) / 1e9
+    peak, peak_src = measured_peak_hbm()
+    traffic, traffic_src = profile_traffic(args.workload)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "algorithmic_bytes_per_launch": alg, "kernel_ms_median": med_ms,
+                "note": "algorithmic gather bytes (8 voxel texels per primary step + 64 int64 SAT texels per box "
+                        "query + image); the SAT and volume are L2-resident, so the effective gather rate can "
+                        "exceed the HBM line"}
+    if traffic_src:
+        roofline["traffic_source"] = f"profiles/{traffic_src}"
+    # end to end through the C ABI with host buffers
+    vol = wl.volume
+    nbytes = vol.nbytes
+    pinned = C.c_void_p()
+    abi.check(lib.cvr_host_alloc_pinned(nbytes, C.byref(pinned)))
+    img_pinned = C.c_void_p()
+    abi.check(lib.cvr_host_alloc_pinned(wl.width * wl.height * 16, C.byref(img_pinned)))
+    C.memmove(pinned, vol.ctypes.data, nbytes)
+    ext = wl.tf.ext_per_value(wl.dtype)
+    d, h, w = vol.shape
+    e2e_times = []
+    est = abi.FrameStats()
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        abi.check(lib.cvr_set_volume(ctx.h, pinned, w, h, d, wl.dtype, *wl.spacing), ctx.h)
+        if wl.method == abi.EXTINCTION:
+            abi.check(lib.cvr_build_sat(ctx.h, abi.dptr(ext), len(ext)), ctx.h)
+        if wl.method == abi.CONE_DOS:
+            ctx.build_pyramid(**wl.pyramid)
+        abi.check(lib.cvr_render_host(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
+                                      C.sizeof(params), C.cast(img_pinned, C.POINTER(C.c_float)), wl.width,
+                                      wl.height, None), ctx.h)
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    lib.cvr_host_free_pinned(pinned)
+    lib.cvr_host_free_pinned(img_pinned)
+    e2e_total, = barrier_max([sum(e2e_times)], ws)
+    e2e = {"value": samples_all / e2e_total / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": int(nbytes + ext.nbytes),
+           "d2h_bytes_per_step": int(wl.width * wl.height * 16),
+           "ms_per_step": 1000.0 * e2e_total / args.steps,
+           "includes": "cvr_set_volume from pinned host memory + cvr_build_sat + cvr_render_host readback"}
+    renderers = {}
+    if not args.quick:
+        for name in ("plain", "cone", "ground_truth"):
+            if name == args.workload:
+                continue
+            w2 = scene.workload(name)
+            scene.prepare(ctx, w2)
+            o2 = C.POINTER(C.c_float)()
+            abi.check(lib.cvr_get_frame_buffer(ctx.h, w2.width, w2.height, C.byref(o2)), ctx.h)
+            s2 = abi.FrameStats()
+            abi.check(lib.cvr_render(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
+                                     C.sizeof(w2.params), C.cast(o2, C.c_void_p), w2.width, w2.height, None,
+                                     C.byref(s2)), ctx.h)
+            tt = time_frames(ctx, lib, w2, w2.params, C.cast(o2, C.c_void_p), 3, 1)
+            m = statistics.median(tt)
+            renderers[name] = {"workload": WORKLOAD_DESC[name], "ms": m, "fps": 1000.0 / m,
+                               "msamples_s": s2.samples / (m / 1000.0) / 1e6,
+                               "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9}
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, target_s=args.cpu_seconds)
+    ctx.close()
+    if rank != 0:
+        return
+    print(json.dumps({
+        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value noise / Gaussian blobs)",
+        "config": {"workload": WORKLOAD_DESC[args.workload], "image": [wl.width, wl.height],
+                   "volume": list(wl.dims), "l2": "flushed between timed steps (cvr_flush_l2, outside the events)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "fps": 1000.0 / ms_per_step,
+        "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
+        "clocks": clocks, "renderers": renderers}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="extinction", choices=list(WORKLOAD_DESC))
+    ap.add_argument("--quick", action="store_true", help="skip the per-renderer table")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

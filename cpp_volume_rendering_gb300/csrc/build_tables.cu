@@ -1,0 +1,201 @@
+// build_tables.cu — device builders for the two illumination tables:
+//  * the extinction summed-area table of RC1PExtinctionBasedShading
+//    (GenerateExtinctionSAT3DTex, ebsrenderer.cpp:624-723, and
+//    SummedAreaTable3D<double>::BuildSAT, libs/vis_utils/summedareatable.h:218-280),
+//  * the Gaussian extinction mip pyramid of RC1PConeTracingDirOcclusionShading
+//    (ExtinctionCoefficientVolume::GenerateExtinctionCoefficientVolumeAnySize,
+//    extcoefvolumegenerator.cpp:230-408, gen_extcoefvol_anysize*.comp, backtotau.comp).
+#include "build_tables.cuh"
+
+namespace cvr {
+
+// ------------------------------------------------------------------ SAT
+// Pass 1: fill + x-scan.  One warp per SAT row (y, z).  Interior cells take
+// lut[voxel(x-1, y-1, z-1)] (the extinction of that voxel value in fixed
+// point); the one-cell border is zero (ebsrenderer.cpp:651-659).
+__global__ void k_sat_fill_xscan(const void* vox, int dtype, int nx, int ny, int nz,
+                                 const long long* __restrict__ lut, long long* __restrict__ sat) {
+  const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= sy * sz) return;
+  int y = warp % sy, z = warp / sy;
+  long long* row = sat + ((size_t)z * sy + y) * (size_t)sx;
+  bool border_row = (y == 0 || z == 0 || y == sy - 1 || z == sz - 1);
+  size_t vrow = border_row ? 0 : ((size_t)(z - 1) * ny + (y - 1)) * (size_t)nx;
+  long long carry = 0;
+  for (int base = 0; base < sx; base += 32) {
+    int x = base + lane;
+    long long v = 0;
+    if (!border_row && x > 0 && x < sx - 1) {
+      unsigned int q = (dtype == 1) ? (unsigned int)__ldg(static_cast<const uint8_t*>(vox) + vrow + (x - 1))
+                                    : (unsigned int)__ldg(static_cast<const uint16_t*>(vox) + vrow + (x - 1));
+      v = __ldg(lut + q);
+    }
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      long long n = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += n;
+    }
+    v += carry;
+    if (x < sx) row[x] = v;
+    carry = __shfl_sync(0xffffffffu, v, 31);
+  }
+}
+
+// Pass 2 / 3: inclusive scan along y (stride sx) or z (stride sx*sy).  One
+// thread per line; consecutive threads own consecutive x, so every step is a
+// coalesced 256-byte warp access.
+__global__ void k_sat_scan_lines(long long* __restrict__ sat, int sx, int n_lines_inner, int n_lines_outer,
+                                 size_t line_stride_inner, size_t line_stride_outer, size_t step, int len) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int total = sx * n_lines_inner * n_lines_outer;
+  if (t >= total) return;
+  int x = t % sx;
+  int r = t / sx;
+  int a = r % n_lines_inner, b = r / n_lines_inner;
+  long long* p = sat + (size_t)x + (size_t)a * line_stride_inner + (size_t)b * line_stride_outer;
+  long long acc = 0;
+  int i = 0;
+  for (; i + 4 <= len; i += 4) {
+    long long v0 = p[(size_t)(i + 0) * step], v1 = p[(size_t)(i + 1) * step];
+    long long v2 = p[(size_t)(i + 2) * step], v3 = p[(size_t)(i + 3) * step];
+    acc += v0; p[(size_t)(i + 0) * step] = acc;
+    acc += v1; p[(size_t)(i + 1) * step] = acc;
+    acc += v2; p[(size_t)(i + 2) * step] = acc;
+    acc += v3; p[(size_t)(i + 3) * step] = acc;
+  }
+  for (; i < len; ++i) {
+    acc += p[(size_t)i * step];
+    p[(size_t)i * step] = acc;
+  }
+}
+
+cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
+                             long long* sat, cudaStream_t st) {
+  const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
+  {
+    long long rows = (long long)sy * sz;
+    int threads = 256;
+    long long blocks = (rows * 32 + threads - 1) / threads;
+    k_sat_fill_xscan<<<(unsigned)blocks, threads, 0, st>>>(vox, dtype, nx, ny, nz, lut, sat);
+  }
+  {
+    // y-scan: lines indexed by (x, z); stride along y = sx.
+    int total = sx * sz;
+    k_sat_scan_lines<<<(total + 255) / 256, 256, 0, st>>>(sat, sx, 1, sz, 0, (size_t)sx * sy, (size_t)sx, sy);
+  }
+  {
+    // z-scan: lines indexed by (x, y); stride along z = sx*sy.
+    int total = sx * sy;
+    k_sat_scan_lines<<<(total + 255) / 256, 256, 0, st>>>(sat, sx, sy, 1, (size_t)sx, 0, (size_t)sx * sy, sz);
+  }
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------------- pyramid
+// gen_extcoefvol_anysize.comp: base level voxel (i,j,k) holds the normalised
+// 7x7x7 Gaussian average (sigma S0, taps at integer multiples of S0) of the
+// TF opacity of the trilinearly sampled volume; samples outside the grid
+// count as 0 opacity but keep their weight.
+__global__ void k_pyr_base(VolumeView vol, const float4* __restrict__ tf_rgba, int tf_n, int bx, int by, int bz,
+                           float s0, float* __restrict__ out) {
+  extern __shared__ float4 sm_tf[];
+  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tf[i] = tf_rgba[i];
+  __syncthreads();
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)bx * by * bz;
+  if (idx >= total) return;
+  int x = int(idx % bx), y = int((idx / bx) % by), z = int(idx / ((long long)bx * by));
+  float3 vs = f3(vol.grid.x / float(bx), vol.grid.y / float(by), vol.grid.z / float(bz));
+  float3 gp = f3((float(x) + 0.5f) * vs.x, (float(y) + 0.5f) * vs.y, (float(z) + 0.5f) * vs.z);
+  float sum_wc = 0.0f, sum_w = 0.0f;
+  for (int ptx = -3; ptx < 4; ++ptx) {
+    for (int pty = -3; pty < 4; ++pty) {
+      for (int ptz = -3; ptz < 4; ++ptz) {
+        float fx = float(ptx) * s0, fy = float(pty) * s0, fz = float(ptz) * s0;
+        float wk = (s0 * s0 * s0) * expf(-(fx * fx + fy * fy + fz * fz) / (2.0f * s0 * s0));
+        float3 p = gp + f3(fx, fy, fz);
+        float3 t = p / vol.grid;
+        float ck = 0.0f;
+        if (!(t.x < 0.0f || t.y < 0.0f || t.z < 0.0f || t.x > 1.0f || t.y > 1.0f || t.z > 1.0f))
+          ck = tf_alpha(sm_tf, tf_n, sample_volume(vol, p));
+        sum_wc += wk * ck;
+        sum_w += wk;
+      }
+    }
+  }
+  out[idx] = sum_wc / sum_w;
+}
+
+// gen_extcoefvol_anysize_mmlevel.comp: level l from level l-1 with sigma
+// Si = S0 * 2^l, sampling level l-1 trilinearly (textureLod at an integer lod).
+__global__ void k_pyr_level(PyramidView P, int l, float si, float* __restrict__ out) {
+  const int* d = P.dims[l];
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = (long long)d[0] * d[1] * d[2];
+  if (idx >= total) return;
+  int x = int(idx % d[0]), y = int((idx / d[0]) % d[1]), z = int(idx / ((long long)d[0] * d[1]));
+  float3 lvs = P.grid / f3(float(d[0]), float(d[1]), float(d[2]));
+  float3 gp = f3((float(x) + 0.5f) * lvs.x, (float(y) + 0.5f) * lvs.y, (float(z) + 0.5f) * lvs.z);
+  float sum_wc = 0.0f, sum_w = 0.0f;
+  for (int ptx = -3; ptx < 4; ++ptx) {
+    for (int pty = -3; pty < 4; ++pty) {
+      for (int ptz = -3; ptz < 4; ++ptz) {
+        float fx = float(ptx) * si, fy = float(pty) * si, fz = float(ptz) * si;
+        float wk = (si * si * si) * expf(-(fx * fx + fy * fy + fz * fz) / (2.0f * si * si));
+        float3 p = gp + f3(fx, fy, fz);
+        float3 t = p / P.grid;
+        float ck = 0.0f;
+        if (!(t.x < 0.0f || t.y < 0.0f || t.z < 0.0f || t.x > 1.0f || t.y > 1.0f || t.z > 1.0f))
+          ck = pyr_sample_level(P, l - 1, p);
+        sum_wc += wk * ck;
+        sum_w += wk;
+      }
+    }
+  }
+  out[idx] = sum_wc / sum_w;
+}
+
+// backtotau.comp: opacity -> extinction, -log(1 - opacity), every level.
+__global__ void k_pyr_backtotau(float* data, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) data[i] = -1.0f * logf(1.0f - data[i]);
+}
+
+cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, int tf_n, float s0,
+                                 PyramidView& P, float* data, cudaStream_t st) {
+  const int threads = 128;
+  long long n0 = (long long)P.dims[0][0] * P.dims[0][1] * P.dims[0][2];
+  size_t sm = sizeof(float4) * tf_n;
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_pyr_base, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  k_pyr_base<<<(unsigned)((n0 + threads - 1) / threads), threads, sm, st>>>(
+      vol, tf_rgba, tf_n, P.dims[0][0], P.dims[0][1], P.dims[0][2], s0, data + P.offset[0]);
+  P.data = data;
+  for (int l = 1; l < P.n_levels; ++l) {
+    long long nl = (long long)P.dims[l][0] * P.dims[l][1] * P.dims[l][2];
+    float si = s0 * powf(2.0f, float(l));
+    k_pyr_level<<<(unsigned)((nl + threads - 1) / threads), threads, 0, st>>>(P, l, si, data + P.offset[l]);
+  }
+  long long total = P.offset[P.n_levels - 1] +
+                    (long long)P.dims[P.n_levels - 1][0] * P.dims[P.n_levels - 1][1] * P.dims[P.n_levels - 1][2];
+  k_pyr_backtotau<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(data, total);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- L2 flush
+__global__ void k_fill(uint4* p, size_t n, unsigned int v) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) p[i] = make_uint4(v, v, v, v);
+}
+cudaError_t launch_fill(void* p, size_t bytes, unsigned int v, cudaStream_t st) {
+  size_t n = bytes / sizeof(uint4);
+  k_fill<<<152 * 8, 256, 0, st>>>(static_cast<uint4*>(p), n, v);
+  return cudaGetLastError();
+}
+
+}  // namespace cvr

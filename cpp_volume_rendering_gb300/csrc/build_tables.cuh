@@ -1,0 +1,19 @@
+// build_tables.cuh — launchers of the SAT / pyramid builders and utilities.
+#pragma once
+
+#include "cvr_device.cuh"
+
+namespace cvr {
+
+// Builds the (nx+2)(ny+2)(nz+2) int64 SAT of lut[voxel] with a zero border.
+cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
+                             long long* sat, cudaStream_t st);
+
+// Builds every level of P (dims/offsets/grid filled by the caller) into data.
+cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, int tf_n, float s0,
+                                 PyramidView& P, float* data, cudaStream_t st);
+
+// Grid-stride fill of a device buffer (used to flush L2 between timed frames).
+cudaError_t launch_fill(void* p, size_t bytes, unsigned int v, cudaStream_t st);
+
+}  // namespace cvr

@@ -1,0 +1,600 @@
+// context.cu — cvr_ctx and the device entry points of cvr.h.
+//
+// A context mirrors the GL state a renderer plugin owns between Init() and
+// Clean(): the volume texture, transfer-function textures, SAT / pyramid /
+// cone-table / kernel-vector textures and the output frame.  Uploads happen
+// once (Init); each cvr_render is Update() + Redraw() of one frame.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cvr.h"
+#include "build_tables.cuh"
+#include "march.cuh"
+
+using namespace cvr;
+
+struct cvr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // volume
+  void* d_vol = nullptr;
+  size_t vol_cap = 0;
+  int nx = 0, ny = 0, nz = 0, dtype = 0;
+  float sx = 1, sy = 1, sz = 1;
+  bool has_volume = false;
+  // transfer function
+  float4* d_rgbt = nullptr;
+  float4* d_rgba = nullptr;
+  int tf_n = 0, tf_cap = 0;
+  // SAT
+  long long* d_sat = nullptr;
+  size_t sat_cap = 0;
+  long long* d_lut = nullptr;
+  int sat_frac_bits = 0;
+  bool sat_ready = false;
+  // pyramid
+  float* d_pyr = nullptr;
+  size_t pyr_cap = 0;
+  PyramidView pyr{};
+  bool pyr_ready = false;
+  // cone tables
+  float4* d_occ_sec = nullptr;
+  float4* d_sdw_sec = nullptr;
+  ConeTableDev occ{}, sdw{};
+  bool cone_ready = false;
+  // GT kernel vectors
+  float3* d_occ_vec = nullptr;
+  float3* d_sdw_vec = nullptr;
+  int n_occ = 0, n_sdw = 0;
+  bool gt_ready = false;
+  // frame
+  unsigned long long* d_stats = nullptr;
+  float4* d_out = nullptr;
+  size_t out_cap = 0;
+  void* d_flush = nullptr;
+  size_t flush_bytes = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int tile_w = 16, tile_h = 8;
+};
+
+namespace {
+
+thread_local std::string g_create_err;
+
+cvr_status fail(cvr_ctx* c, cvr_status code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+cvr_status cuda_fail(cvr_ctx* c, cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a sticky launch error where possible
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(c, e == cudaErrorMemoryAllocation ? CVR_ERR_OUT_OF_MEMORY : CVR_ERR_CUDA, msg);
+}
+
+#define CK(ctx, call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+// Grows a device allocation to at least 'bytes' (contents discarded).
+template <class T>
+cudaError_t ensure(T*& p, size_t& cap, size_t bytes) {
+  if (cap >= bytes && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc((void**)&p, bytes);
+  if (e == cudaSuccess) cap = bytes;
+  return e;
+}
+
+VolumeView volume_view(const cvr_ctx* c) {
+  VolumeView v;
+  v.voxels = c->d_vol;
+  v.dtype = c->dtype;
+  v.nx = c->nx; v.ny = c->ny; v.nz = c->nz;
+  v.spacing = f3(c->sx, c->sy, c->sz);
+  v.inv_spacing = f3(1.0f / c->sx, 1.0f / c->sy, 1.0f / c->sz);
+  v.grid = f3(c->nx * c->sx, c->ny * c->sy, c->nz * c->sz);
+  v.norm = c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  return v;
+}
+
+// glm::lookAt basis in single precision (libs/vis_utils/camera.cpp:281-284).
+CameraView camera_view(const cvr_camera* cam, int w, int h) {
+  float3 eye = make3(cam->eye), ctr = make3(cam->center), up = make3(cam->up);
+  float3 fw = ctr - eye;
+  float inv = 1.0f / std::sqrt(dot3(fw, fw));
+  fw = fw * inv;
+  float3 s = cross3(fw, up);
+  inv = 1.0f / std::sqrt(dot3(s, s));
+  s = s * inv;
+  float3 u = cross3(s, fw);
+  CameraView cv;
+  cv.eye = eye; cv.s = s; cv.u = u; cv.f = fw;
+  cv.tan_half_fovy = (float)std::tan((double)cam->fovy_deg * (3.14159265358979323846 / 180.0) / 2.0);
+  cv.aspect = cam->aspect > 0.0f ? cam->aspect : (float)w / (float)h;
+  return cv;
+}
+
+bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+}  // namespace
+
+extern "C" {
+
+int cvr_abi_version(void) { return CVR_ABI_VERSION; }
+
+const char* cvr_last_error(const cvr_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_err.c_str(); }
+
+cvr_status cvr_create(cvr_ctx** out, int device) {
+  if (!out) return CVR_ERR_INVALID_ARG;
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    g_create_err = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    return CVR_ERR_CUDA;
+  }
+  if (device < 0 || device >= n) {
+    g_create_err = "device index out of range";
+    return CVR_ERR_INVALID_ARG;
+  }
+  cvr_ctx* c = new cvr_ctx();
+  c->device = device;
+  auto bail = [&](cudaError_t err, const char* what) {
+    g_create_err = std::string(what) + ": " + cudaGetErrorString(err);
+    cvr_destroy(c);
+    return err == cudaErrorMemoryAllocation ? CVR_ERR_OUT_OF_MEMORY : CVR_ERR_CUDA;
+  };
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(e, "cudaSetDevice");
+  if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(e, "cudaStreamCreate");
+  for (int i = 0; i < 4; ++i)
+    if ((e = cudaEventCreate(&c->ev[i])) != cudaSuccess) return bail(e, "cudaEventCreate");
+  if ((e = cudaMalloc((void**)&c->d_stats, 4 * sizeof(unsigned long long))) != cudaSuccess)
+    return bail(e, "cudaMalloc(stats)");
+  *out = c;
+  return CVR_OK;
+}
+
+void cvr_destroy(cvr_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  for (int i = 0; i < 4; ++i)
+    if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+cvr_status cvr_sync(cvr_ctx* c) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
+void* cvr_stream(cvr_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+static cvr_status set_volume_common(cvr_ctx* c, const void* src, bool src_device, int w, int h, int d, int dtype,
+                                    float sx, float sy, float sz) {
+  if (!c || !src || w <= 0 || h <= 0 || d <= 0 || (dtype != CVR_U8 && dtype != CVR_U16))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_volume: bad arguments");
+  if (!(sx > 0.0f && sy > 0.0f && sz > 0.0f) || !std::isfinite(sx) || !std::isfinite(sy) || !std::isfinite(sz))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_volume: spacing must be positive");
+  if ((long long)w * h * d > (1ll << 34)) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_volume: volume too large");
+  CK(c, cudaSetDevice(c->device));
+  size_t bytes = (size_t)w * h * d * (dtype == CVR_U8 ? 1 : 2);
+  CK(c, ensure(c->d_vol, c->vol_cap, bytes));
+  CK(c, cudaMemcpyAsync(c->d_vol, src, bytes, src_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                        c->stream));
+  c->nx = w; c->ny = h; c->nz = d; c->dtype = dtype;
+  c->sx = sx; c->sy = sy; c->sz = sz;
+  c->has_volume = true;
+  // Derived tables belong to the previous volume.
+  c->sat_ready = false;
+  c->pyr_ready = false;
+  return CVR_OK;
+}
+
+cvr_status cvr_set_volume(cvr_ctx* c, const void* host, int w, int h, int d, int dtype, float sx, float sy,
+                          float sz) {
+  return set_volume_common(c, host, false, w, h, d, dtype, sx, sy, sz);
+}
+
+cvr_status cvr_set_volume_device(cvr_ctx* c, const void* dev, int w, int h, int d, int dtype, float sx, float sy,
+                                 float sz) {
+  return set_volume_common(c, dev, true, w, h, d, dtype, sx, sy, sz);
+}
+
+cvr_status cvr_set_transfer_function(cvr_ctx* c, const float* rgbt, const float* rgba, int n) {
+  if (!c || !rgbt || n < 2 || n > 65536) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_transfer_function: bad arguments");
+  CK(c, cudaSetDevice(c->device));
+  std::vector<float> op;
+  if (!rgba) {
+    op.assign(rgbt, rgbt + 4 * (size_t)n);
+    for (int i = 0; i < n; ++i) op[4 * i + 3] = (float)(1.0 - std::exp(-(double)rgbt[4 * i + 3]));
+    rgba = op.data();
+  }
+  if (n > c->tf_cap) {
+    if (c->d_rgbt) cudaFree(c->d_rgbt);
+    if (c->d_rgba) cudaFree(c->d_rgba);
+    c->d_rgbt = c->d_rgba = nullptr;
+    c->tf_cap = 0;
+    CK(c, cudaMalloc((void**)&c->d_rgbt, sizeof(float4) * n));
+    CK(c, cudaMalloc((void**)&c->d_rgba, sizeof(float4) * n));
+    c->tf_cap = n;
+  }
+  CK(c, cudaMemcpyAsync(c->d_rgbt, rgbt, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(c->d_rgba, rgba, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+  // Host sources may be pageable temporaries: finish before returning.
+  CK(c, cudaStreamSynchronize(c->stream));
+  c->tf_n = n;
+  c->pyr_ready = false;
+  return CVR_OK;
+}
+
+cvr_status cvr_build_sat(cvr_ctx* c, const double* ext, int n_values) {
+  if (!c || !ext) return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_sat: bad arguments");
+  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_build_sat: no volume");
+  int need = c->dtype == CVR_U8 ? 256 : 65536;
+  if (n_values != need) return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_sat: n_values must be 256 (u8) or 65536 (u16)");
+  double maxv = 0.0;
+  for (int i = 0; i < n_values; ++i) {
+    if (!(ext[i] >= 0.0) || !std::isfinite(ext[i]))
+      return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_sat: extinction values must be finite and >= 0");
+    maxv = std::max(maxv, ext[i]);
+  }
+  // Fixed point: the largest possible entry (all voxels at the largest
+  // extinction) must stay below 2^62.
+  double nvox = (double)c->nx * c->ny * c->nz;
+  int F = 52;
+  if (maxv > 0.0) F = (int)std::floor(62.0 - std::log2(nvox * maxv));
+  F = std::min(52, std::max(0, F));
+  std::vector<long long> q(n_values);
+  double scale = std::ldexp(1.0, F);
+  for (int i = 0; i < n_values; ++i) q[i] = std::llround(ext[i] * scale);
+  CK(c, cudaSetDevice(c->device));
+  size_t lut_cap = 0;
+  if (c->d_lut) { cudaFree(c->d_lut); c->d_lut = nullptr; }
+  CK(c, ensure(c->d_lut, lut_cap, sizeof(long long) * n_values));
+  CK(c, cudaMemcpyAsync(c->d_lut, q.data(), sizeof(long long) * n_values, cudaMemcpyHostToDevice, c->stream));
+  size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+  CK(c, ensure(c->d_sat, c->sat_cap, cells * sizeof(long long)));
+  CK(c, launch_sat_build(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut, c->d_sat, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));  // q is a host temporary
+  c->sat_frac_bits = F;
+  c->sat_ready = true;
+  return CVR_OK;
+}
+
+cvr_status cvr_get_sat_info(cvr_ctx* c, int dims[3], int* frac_bits) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "SAT not built");
+  if (dims) { dims[0] = c->nx + 2; dims[1] = c->ny + 2; dims[2] = c->nz + 2; }
+  if (frac_bits) *frac_bits = c->sat_frac_bits;
+  return CVR_OK;
+}
+
+cvr_status cvr_download_sat(cvr_ctx* c, int64_t* host) {
+  if (!c || !host) return CVR_ERR_INVALID_ARG;
+  if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "SAT not built");
+  size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+  CK(c, cudaMemcpyAsync(host, c->d_sat, cells * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
+cvr_status cvr_build_ext_pyramid(cvr_ctx* c, const cvr_pyramid_params* p) {
+  if (!c || !p) return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_ext_pyramid: bad arguments");
+  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_build_ext_pyramid: no volume");
+  if (c->tf_n == 0) return fail(c, CVR_ERR_NOT_READY, "cvr_build_ext_pyramid: no transfer function");
+  if (p->base_dims[0] <= 0 || p->base_dims[1] <= 0 || p->base_dims[2] <= 0 || p->base_dims[0] > 4096 ||
+      p->base_dims[1] > 4096 || p->base_dims[2] > 4096 || !(p->sigma0 > 0.0f) || p->n_levels < 0)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_ext_pyramid: bad parameters");
+  // GL mip chain: level i has max(1, dim >> i) per axis; the chain ends after
+  // the level where every axis is 1 (extcoefvolumegenerator.cpp:321-331).
+  int maxdim = std::max(p->base_dims[0], std::max(p->base_dims[1], p->base_dims[2]));
+  int chain = 1;
+  while ((maxdim >> chain) > 0) ++chain;
+  int levels = p->n_levels > 0 ? std::min(p->n_levels, chain) : chain;
+  levels = std::min(levels, CVR_MAX_LEVELS);
+  PyramidView P{};
+  long long off = 0;
+  for (int l = 0; l < levels; ++l) {
+    for (int a = 0; a < 3; ++a) P.dims[l][a] = std::max(1, p->base_dims[a] >> l);
+    P.offset[l] = off;
+    off += (long long)P.dims[l][0] * P.dims[l][1] * P.dims[l][2];
+  }
+  P.n_levels = levels;
+  VolumeView v = volume_view(c);
+  P.grid = v.grid;
+  P.inv_grid = f3(1.0f / v.grid.x, 1.0f / v.grid.y, 1.0f / v.grid.z);
+  CK(c, cudaSetDevice(c->device));
+  CK(c, ensure(c->d_pyr, c->pyr_cap, (size_t)off * sizeof(float)));
+  CK(c, launch_pyramid_build(v, c->d_rgba, c->tf_n, p->sigma0, P, c->d_pyr, c->stream));
+  c->pyr = P;
+  c->pyr_ready = true;
+  return CVR_OK;
+}
+
+cvr_status cvr_get_pyramid_info(cvr_ctx* c, int* n_levels, int (*dims)[3], int max_levels) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (!c->pyr_ready) return fail(c, CVR_ERR_NOT_READY, "pyramid not built");
+  if (n_levels) *n_levels = c->pyr.n_levels;
+  if (dims)
+    for (int l = 0; l < c->pyr.n_levels && l < max_levels; ++l)
+      for (int a = 0; a < 3; ++a) dims[l][a] = c->pyr.dims[l][a];
+  return CVR_OK;
+}
+
+cvr_status cvr_download_pyramid_level(cvr_ctx* c, int level, float* host) {
+  if (!c || !host) return CVR_ERR_INVALID_ARG;
+  if (!c->pyr_ready) return fail(c, CVR_ERR_NOT_READY, "pyramid not built");
+  if (level < 0 || level >= c->pyr.n_levels) return fail(c, CVR_ERR_INVALID_ARG, "level out of range");
+  size_t n = (size_t)c->pyr.dims[level][0] * c->pyr.dims[level][1] * c->pyr.dims[level][2];
+  CK(c, cudaMemcpyAsync(host, c->d_pyr + c->pyr.offset[level], n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
+static cvr_status upload_cone(cvr_ctx* c, const cvr_cone_table* t, float4** d, ConeTableDev* out) {
+  if (t->n_sections < 0 || t->n_sections > CVR_MAX_CONE_SECTIONS)
+    return fail(c, CVR_ERR_INVALID_ARG, "cone table: bad section count");
+  int n1 = t->integration_samples[0], n3 = t->integration_samples[1], n7 = t->integration_samples[2];
+  if (n1 < 0 || n3 < 0 || n7 < 0 || n1 + n3 + n7 > t->n_sections)
+    return fail(c, CVR_ERR_INVALID_ARG, "cone table: integration counts exceed the section count");
+  if (*d) { cudaFree(*d); *d = nullptr; }
+  size_t bytes = sizeof(float4) * std::max(1, t->n_sections);
+  CK(c, cudaMalloc((void**)d, bytes));
+  if (t->n_sections) CK(c, cudaMemcpy(*d, t->sections, sizeof(float4) * t->n_sections, cudaMemcpyHostToDevice));
+  out->n_sections = t->n_sections;
+  out->n1 = n1; out->n3 = n3; out->n7 = n7;
+  for (int i = 0; i < 10; ++i) out->axes[i] = make3(t->axes[i]);
+  out->initial_step = t->initial_step;
+  out->w7 = t->ray7_adj_weight;
+  out->ui_weight = t->ui_weight;
+  return CVR_OK;
+}
+
+cvr_status cvr_set_cone_tables(cvr_ctx* c, const cvr_cone_table* occ, const cvr_cone_table* sdw) {
+  if (!c || !occ || !sdw) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_cone_tables: bad arguments");
+  CK(c, cudaSetDevice(c->device));
+  cvr_status s = upload_cone(c, occ, &c->d_occ_sec, &c->occ);
+  if (s != CVR_OK) return s;
+  s = upload_cone(c, sdw, &c->d_sdw_sec, &c->sdw);
+  if (s != CVR_OK) return s;
+  c->cone_ready = true;
+  return CVR_OK;
+}
+
+cvr_status cvr_set_gt_kernels(cvr_ctx* c, const float* occ, int n_occ, const float* sdw, int n_sdw) {
+  if (!c || n_occ < 0 || n_sdw < 0 || n_occ > CVR_MAX_GT_RAYS || n_sdw > CVR_MAX_GT_RAYS || (n_occ && !occ) ||
+      (n_sdw && !sdw))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_gt_kernels: bad arguments (at most 256 rays per cone)");
+  CK(c, cudaSetDevice(c->device));
+  if (c->d_occ_vec) { cudaFree(c->d_occ_vec); c->d_occ_vec = nullptr; }
+  if (c->d_sdw_vec) { cudaFree(c->d_sdw_vec); c->d_sdw_vec = nullptr; }
+  CK(c, cudaMalloc((void**)&c->d_occ_vec, sizeof(float3) * std::max(1, n_occ)));
+  CK(c, cudaMalloc((void**)&c->d_sdw_vec, sizeof(float3) * std::max(1, n_sdw)));
+  if (n_occ) CK(c, cudaMemcpy(c->d_occ_vec, occ, sizeof(float3) * n_occ, cudaMemcpyHostToDevice));
+  if (n_sdw) CK(c, cudaMemcpy(c->d_sdw_vec, sdw, sizeof(float3) * n_sdw, cudaMemcpyHostToDevice));
+  c->n_occ = n_occ;
+  c->n_sdw = n_sdw;
+  c->gt_ready = true;
+  return CVR_OK;
+}
+
+static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
+                              const void* params, size_t params_size, float* out, int w, int h, uint32_t* counts,
+                              cvr_frame_stats* stats) {
+  if (!c || !cam || !params || !out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: bad arguments");
+  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_render: no volume loaded");
+  if (c->tf_n == 0) return fail(c, CVR_ERR_NOT_READY, "cvr_render: no transfer function");
+  if (!finite3(cam->eye) || !finite3(cam->center) || !finite3(cam->up))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: non-finite camera");
+  CK(c, cudaSetDevice(c->device));
+  FrameArgs f;
+  f.vol = volume_view(c);
+  f.cam = camera_view(cam, w, h);
+  f.tf = c->d_rgbt;
+  f.tf_n = c->tf_n;
+  f.W = w; f.H = h;
+  f.tile_w = c->tile_w; f.tile_h = c->tile_h;
+  f.out = reinterpret_cast<float4*>(out);
+  f.counts = counts;
+  f.stats = c->d_stats;
+  if (c->tf_n * sizeof(float4) > 48 * 1024) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: TF larger than 3072 entries");
+  // Steps below 1e-6 of the diagonal would not advance a single-precision
+  // ray parameter; they are rejected rather than marched.
+  const float min_step = 1.0e-6f * std::sqrt(dot3(f.vol.grid, f.vol.grid));
+  {
+    float step = *static_cast<const float*>(params);  // every params struct starts with step_size
+    if (!(step >= min_step) || !std::isfinite(step))
+      return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: step_size must be finite and >= 1e-6 * diagonal");
+  }
+  CK(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
+  cvr_light dl{};
+  if (!light) { light = &dl; }
+  cudaError_t e = cudaSuccess;
+  if (stats) CK(c, cudaEventRecord(c->ev[2], c->stream));
+  switch (method) {
+    case CVR_METHOD_PLAIN: {
+      if (params_size != sizeof(cvr_plain_params)) return fail(c, CVR_ERR_INVALID_ARG, "plain params size");
+      const cvr_plain_params* p = static_cast<const cvr_plain_params*>(params);
+      if (!(p->step_size > 0.0f)) return fail(c, CVR_ERR_INVALID_ARG, "step_size must be > 0");
+      f.step = p->step_size;
+      e = launch_plain(f, c->stream);
+      break;
+    }
+    case CVR_METHOD_EXTINCTION: {
+      if (params_size != sizeof(cvr_ext_params)) return fail(c, CVR_ERR_INVALID_ARG, "extinction params size");
+      const cvr_ext_params* p = static_cast<const cvr_ext_params*>(params);
+      if (!(p->step_size > 0.0f)) return fail(c, CVR_ERR_INVALID_ARG, "step_size must be > 0");
+      if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: extinction SAT not built");
+      if (p->apply_occlusion && (p->ao_n_shells < 1 || p->ao_n_shells > CVR_MAX_AO_SHELLS))
+        return fail(c, CVR_ERR_INVALID_ARG, "ao_n_shells must be in [1, 32]");
+      if (p->apply_shadow && !(p->sdw_sample_interval >= 1.0e-3f))
+        return fail(c, CVR_ERR_INVALID_ARG, "sdw_sample_interval must be >= 1e-3 voxels");
+      f.step = p->step_size;
+      ExtArgs a{};
+      a.sat.sat = c->d_sat;
+      a.sat.sx = c->nx + 2; a.sat.sy = c->ny + 2; a.sat.sz = c->nz + 2;
+      a.sat.inv_scale = (float)std::ldexp(1.0, -c->sat_frac_bits);
+      a.sat.inv_spacing = f.vol.inv_spacing;
+      a.sat.min_pos = f.vol.spacing * 0.5f;
+      a.sat.max_pos = f.vol.grid + f.vol.spacing * 1.5f;
+      a.apply_occ = p->apply_occlusion; a.apply_sdw = p->apply_shadow;
+      a.n_shells = p->apply_occlusion ? p->ao_n_shells : 1;
+      for (int i = 0; i < CVR_MAX_AO_SHELLS; ++i) a.radii[i] = p->ao_radii[i];
+      a.cone_angle = p->sdw_cone_angle_rad; a.interval = p->sdw_sample_interval;
+      a.initial = p->sdw_initial_step; a.ui_weight = p->sdw_ui_weight; a.max_dist = p->sdw_max_distance;
+      a.shadow_type = p->shadow_type;
+      a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
+      a.ka = p->ka; a.kd = p->kd;
+      e = launch_extinction(f, a, c->stream);
+      break;
+    }
+    case CVR_METHOD_CONE_DOS: {
+      if (params_size != sizeof(cvr_dos_params)) return fail(c, CVR_ERR_INVALID_ARG, "dos params size");
+      const cvr_dos_params* p = static_cast<const cvr_dos_params*>(params);
+      if (!(p->step_size > 0.0f)) return fail(c, CVR_ERR_INVALID_ARG, "step_size must be > 0");
+      if (!c->pyr_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: extinction pyramid not built");
+      if (!c->cone_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: cone tables not set");
+      f.step = p->step_size;
+      DosArgs a{};
+      a.pyr = c->pyr;
+      a.pyr.data = c->d_pyr;
+      a.occ_sections = c->d_occ_sec; a.sdw_sections = c->d_sdw_sec;
+      a.occ = c->occ; a.sdw = c->sdw;
+      a.apply_occ = p->apply_occlusion; a.apply_sdw = p->apply_shadow; a.shadow_type = p->shadow_type;
+      a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
+      a.light_up = make3(light->up); a.light_right = make3(light->right);
+      a.spot_cos_max = light->spot_cos_max;
+      a.ka = p->ka; a.kd = p->kd;
+      e = launch_dos(f, a, c->stream);
+      break;
+    }
+    case CVR_METHOD_GROUND_TRUTH: {
+      if (params_size != sizeof(cvr_gt_params)) return fail(c, CVR_ERR_INVALID_ARG, "gt params size");
+      const cvr_gt_params* p = static_cast<const cvr_gt_params*>(params);
+      if (!(p->step_size > 0.0f) || !(p->light_ray_step_size >= min_step))
+        return fail(c, CVR_ERR_INVALID_ARG, "step sizes must be >= 1e-6 * diagonal");
+      if (!c->gt_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: GT kernel vectors not set");
+      f.step = p->step_size;
+      GtArgs a{};
+      a.occ_vec = c->d_occ_vec; a.sdw_vec = c->d_sdw_vec;
+      a.n_occ = c->n_occ; a.n_sdw = c->n_sdw;
+      a.gap = p->light_ray_initial_gap; a.lstep = p->light_ray_step_size;
+      a.apply_occ = p->apply_occlusion; a.apply_sdw = p->apply_shadow; a.shadow_type = p->shadow_type;
+      a.occ_dist = p->occ_distance; a.sdw_dist = p->sdw_distance;
+      a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
+      a.light_up = make3(light->up); a.light_right = make3(light->right);
+      a.ka = p->ka; a.kd = p->kd;
+      e = launch_gt(f, a, c->stream);
+      break;
+    }
+    default:
+      return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: unknown method");
+  }
+  if (e != cudaSuccess) return cuda_fail(c, e, "render launch");
+  if (stats) {
+    CK(c, cudaEventRecord(c->ev[3], c->stream));
+    unsigned long long hs[3];
+    CK(c, cudaMemcpyAsync(hs, c->d_stats, sizeof hs, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    float ms = 0.0f;
+    CK(c, cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]));
+    stats->samples = hs[0];
+    stats->shaded_samples = hs[1];
+    stats->aux_fetches = hs[2];
+    stats->kernel_ms = ms;
+  }
+  return CVR_OK;
+}
+
+cvr_status cvr_render(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light, const void* params,
+                      size_t params_size, float* out_dev, int w, int h, uint32_t* counts, cvr_frame_stats* stats) {
+  return render_impl(c, method, cam, light, params, params_size, out_dev, w, h, counts, stats);
+}
+
+cvr_status cvr_render_host(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light, const void* params,
+                           size_t params_size, float* out_host, int w, int h, cvr_frame_stats* stats) {
+  if (!c || !out_host || w <= 0 || h <= 0) return fail(c, CVR_ERR_INVALID_ARG, "cvr_render_host: bad arguments");
+  CK(c, cudaSetDevice(c->device));
+  size_t bytes = (size_t)w * h * sizeof(float4);
+  CK(c, ensure(c->d_out, c->out_cap, bytes));
+  cvr_status s = render_impl(c, method, cam, light, params, params_size, reinterpret_cast<float*>(c->d_out), w, h,
+                             nullptr, stats);
+  if (s != CVR_OK) return s;
+  CK(c, cudaMemcpyAsync(out_host, c->d_out, bytes, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
+cvr_status cvr_get_frame_buffer(cvr_ctx* c, int w, int h, float** dev_out) {
+  if (!c || !dev_out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_get_frame_buffer: bad arguments");
+  CK(c, cudaSetDevice(c->device));
+  CK(c, ensure(c->d_out, c->out_cap, (size_t)w * h * sizeof(float4)));
+  *dev_out = reinterpret_cast<float*>(c->d_out);
+  return CVR_OK;
+}
+
+cvr_status cvr_timer_start(cvr_ctx* c) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  CK(c, cudaEventRecord(c->ev[0], c->stream));
+  return CVR_OK;
+}
+
+cvr_status cvr_timer_stop(cvr_ctx* c, float* ms) {
+  if (!c || !ms) return CVR_ERR_INVALID_ARG;
+  CK(c, cudaEventRecord(c->ev[1], c->stream));
+  CK(c, cudaEventSynchronize(c->ev[1]));
+  CK(c, cudaEventElapsedTime(ms, c->ev[0], c->ev[1]));
+  return CVR_OK;
+}
+
+cvr_status cvr_flush_l2(cvr_ctx* c) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  CK(c, cudaSetDevice(c->device));
+  if (!c->d_flush) {
+    int l2 = 0;
+    CK(c, cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, c->device));
+    size_t bytes = std::max<size_t>((size_t)l2 * 2, 256u << 20);
+    CK(c, cudaMalloc(&c->d_flush, bytes));
+    c->flush_bytes = bytes;
+  }
+  CK(c, launch_fill(c->d_flush, c->flush_bytes, 0x5a5a5a5au, c->stream));
+  return CVR_OK;
+}
+
+cvr_status cvr_host_alloc_pinned(size_t bytes, void** out) {
+  if (!out || bytes == 0) return CVR_ERR_INVALID_ARG;
+  cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    g_create_err = std::string("cudaHostAlloc: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? CVR_ERR_OUT_OF_MEMORY : CVR_ERR_CUDA;
+  }
+  return CVR_OK;
+}
+
+void cvr_host_free_pinned(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,258 @@
+// cvr_device.cuh — device-side building blocks shared by every marcher.
+//
+// Each function states the reference shader code it restates.  All sampling
+// follows OpenGL texture() semantics on normalised coordinates: texel centres
+// at (i + 0.5) / n, clamp-to-edge, (tri)linear weights computed exactly in
+// FP32 (the reference's FP16 texture storage is not reproduced: voxels are
+// read as exact u8/u16 values and normalised by 255 / 65535).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cvr {
+
+// ---------------------------------------------------------------- float3 math
+__host__ __device__ __forceinline__ float3 f3(float x, float y, float z) { return make_float3(x, y, z); }
+__host__ __device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__host__ __device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__host__ __device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(a.x * s, a.y * s, a.z * s); }
+__host__ __device__ __forceinline__ float3 operator/(float3 a, float3 b) { return f3(a.x / b.x, a.y / b.y, a.z / b.z); }
+__host__ __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 normalize3(float3 a) {
+  float inv = rsqrtf(dot3(a, a));
+  return a * inv;
+}
+__device__ __forceinline__ float3 fmin3(float3 a, float3 b) { return f3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
+__device__ __forceinline__ float3 fmax3(float3 a, float3 b) { return f3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)); }
+__device__ __forceinline__ float3 clamp3(float3 v, float3 lo, float3 hi) { return fmin3(fmax3(v, lo), hi); }
+__device__ __forceinline__ float3 abs3(float3 a) { return f3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+__host__ __device__ __forceinline__ float3 make3(const float* p) { return f3(p[0], p[1], p[2]); }
+
+// ---------------------------------------------------------------- state
+// Volume as uploaded by cvr_set_volume: u8/u16, x fastest.
+struct VolumeView {
+  const void* voxels;
+  int dtype;            // 1 = u8, 2 = u16
+  int nx, ny, nz;
+  float3 spacing;       // VolumeScales
+  float3 inv_spacing;
+  float3 grid;          // VolumeGridSize = dims * spacing
+  float norm;           // 1/255 or 1/65535
+};
+
+// Per-frame camera frame (glm::lookAt rows s, u, f) and projection terms.
+struct CameraView {
+  float3 eye;
+  float3 s, u, f;       // right, up, forward
+  float tan_half_fovy;
+  float aspect;
+};
+
+// ---------------------------------------------------------------- camera ray
+// ray_marching_1p.comp:160-170: VerPos = ((x+0.5)/W, (y+0.5)/H)*2-1,
+// camera_dir = normalize(vec3(X*tan*aspect, Y*tan, -1) * mat3(LookAt)).
+// Row-vector times the lookAt 3x3 equals X*tan*aspect*s + Y*tan*u + f.
+__device__ __forceinline__ float3 primary_dir(const CameraView& c, int px, int py, int W, int H) {
+  float vx = ((float(px) + 0.5f) / float(W)) * 2.0f - 1.0f;
+  float vy = ((float(py) + 0.5f) / float(H)) * 2.0f - 1.0f;
+  float a = vx * c.tan_half_fovy * c.aspect;
+  float b = vy * c.tan_half_fovy;
+  return normalize3(c.s * a + c.u * b + c.f);
+}
+
+// ray_bbox_intersection.comp:18-52 (IntersectBox + RayAABBIntersection):
+// slab test against [-S/2, S/2], tnear clamped to 0, hit iff tfar > tnear.
+__device__ __forceinline__ bool ray_aabb(float3 origin, float3 dir, float3 grid, float& tnear, float& tfar) {
+  float3 bmin = grid * -0.5f;
+  float3 bmax = grid * 0.5f;
+  float3 inv = f3(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+  float3 t0 = inv * (bmin - origin);
+  float3 t1 = inv * (bmax - origin);
+  float3 tmin = fmin3(t0, t1);
+  float3 tmax = fmax3(t0, t1);
+  tnear = fmaxf(fmaxf(tmin.x, tmin.y), tmin.z);
+  tfar = fminf(fminf(tmax.x, tmax.y), tmax.z);
+  bool hit = tfar > tnear;
+  tnear = fmaxf(tnear, 0.0f);
+  return hit;
+}
+
+// ---------------------------------------------------------------- sampling
+__device__ __forceinline__ float voxel(const VolumeView& v, int x, int y, int z) {
+  size_t i = (size_t)x + (size_t)v.nx * ((size_t)y + (size_t)v.ny * (size_t)z);
+  if (v.dtype == 1) return float(__ldg(static_cast<const uint8_t*>(v.voxels) + i));
+  return float(__ldg(static_cast<const uint16_t*>(v.voxels) + i));
+}
+
+// One axis of a GL_LINEAR clamp-to-edge lookup at texel coordinate u.
+struct Tap {
+  int i0, i1;
+  float t;
+};
+__device__ __forceinline__ Tap axis_tap(float u, int n) {
+  float fl = floorf(u);
+  int i = int(fl);
+  Tap r;
+  r.t = u - fl;
+  r.i0 = min(max(i, 0), n - 1);
+  r.i1 = min(max(i + 1, 0), n - 1);
+  return r;
+}
+
+// texture(TexVolume, tex_pos / VolumeGridSize).r with tex_pos in [0, S]:
+// texel coordinate = tex_pos / spacing - 0.5.
+__device__ __forceinline__ float sample_volume(const VolumeView& v, float3 tex_pos) {
+  Tap tx = axis_tap(fmaf(tex_pos.x, v.inv_spacing.x, -0.5f), v.nx);
+  Tap ty = axis_tap(fmaf(tex_pos.y, v.inv_spacing.y, -0.5f), v.ny);
+  Tap tz = axis_tap(fmaf(tex_pos.z, v.inv_spacing.z, -0.5f), v.nz);
+  float c000 = voxel(v, tx.i0, ty.i0, tz.i0), c100 = voxel(v, tx.i1, ty.i0, tz.i0);
+  float c010 = voxel(v, tx.i0, ty.i1, tz.i0), c110 = voxel(v, tx.i1, ty.i1, tz.i0);
+  float c001 = voxel(v, tx.i0, ty.i0, tz.i1), c101 = voxel(v, tx.i1, ty.i0, tz.i1);
+  float c011 = voxel(v, tx.i0, ty.i1, tz.i1), c111 = voxel(v, tx.i1, ty.i1, tz.i1);
+  float c00 = fmaf(tx.t, c100 - c000, c000), c10 = fmaf(tx.t, c110 - c010, c010);
+  float c01 = fmaf(tx.t, c101 - c001, c001), c11 = fmaf(tx.t, c111 - c011, c011);
+  float c0 = fmaf(ty.t, c10 - c00, c00), c1 = fmaf(ty.t, c11 - c01, c01);
+  return fmaf(tz.t, c1 - c0, c0) * v.norm;
+}
+
+// texture(TexTransferFunc, density): 1D GL_LINEAR, clamp-to-edge over n entries.
+__device__ __forceinline__ float4 tf_lookup(const float4* tf, int n, float density) {
+  Tap t = axis_tap(fmaf(density, float(n), -0.5f), n);
+  float4 a = tf[t.i0], b = tf[t.i1];
+  return make_float4(fmaf(t.t, b.x - a.x, a.x), fmaf(t.t, b.y - a.y, a.y),
+                     fmaf(t.t, b.z - a.z, a.z), fmaf(t.t, b.w - a.w, a.w));
+}
+__device__ __forceinline__ float tf_alpha(const float4* tf, int n, float density) {
+  Tap t = axis_tap(fmaf(density, float(n), -0.5f), n);
+  float a = tf[t.i0].w, b = tf[t.i1].w;
+  return fmaf(t.t, b - a, a);
+}
+
+// ---------------------------------------------------------------- SAT query
+// The extinction SAT is stored as exact int64 fixed point (value * 2^F).
+// The reference evaluates a box as V1-V2-V3+V4-V5+V6+V7-V8 over eight
+// trilinear SAT fetches (ebs_ray_bbox_marching.comp:74-100).  That is the
+// tensor product, over the three axes, of the 1-D functional
+//   L(S) = [(1-th) S[b0] + th S[b1]] - [(1-tl) S[a0] + tl S[a1]]
+// which equals (1-th)(S[b0]-S[a0]) + th (S[b1]-S[a1]) + (th-tl)(S[a1]-S[a0]).
+// Applying the three integer differences along every axis gives 27 exact
+// small box sums; only those are converted to float and weighted, so the
+// query has no cancellation however large the SAT entries are.
+struct SatView {
+  const long long* sat;  // (nx+2)(ny+2)(nz+2), x fastest
+  int sx, sy, sz;        // SAT dims = volume dims + 2
+  float inv_scale;       // 2^-F
+  float3 inv_spacing;
+  float3 min_pos;        // MinSATPosition = spacing*0.5
+  float3 max_pos;        // MaxSATPosition = grid + spacing*1.5
+};
+
+struct BoxAxis {
+  int a0, a1, b0, b1;  // texel indices of the low and high corner taps
+  float c0, c1, c2;    // weights of D0=S[b0]-S[a0], D1=S[b1]-S[a1], D2=S[a1]-S[a0]
+};
+__device__ __forceinline__ BoxAxis box_axis(float lo, float hi, int n) {
+  Tap l = axis_tap(lo, n), h = axis_tap(hi, n);
+  BoxAxis b;
+  b.a0 = l.i0; b.a1 = l.i1; b.b0 = h.i0; b.b1 = h.i1;
+  b.c0 = 1.0f - h.t; b.c1 = h.t; b.c2 = h.t - l.t;
+  return b;
+}
+
+// Three x-differences of one SAT row segment.
+struct D3 { long long d0, d1, d2; };
+__device__ __forceinline__ D3 x_diffs(const long long* row, const BoxAxis& X) {
+  long long va0 = __ldg(row + X.a0), va1 = __ldg(row + X.a1);
+  long long vb0 = __ldg(row + X.b0), vb1 = __ldg(row + X.b1);
+  D3 r; r.d0 = vb0 - va0; r.d1 = vb1 - va1; r.d2 = va1 - va0;
+  return r;
+}
+struct D9 { D3 y0, y1, y2; };  // y-differences (D0, D1, D2) of x-differenced rows
+__device__ __forceinline__ D9 yx_diffs(const SatView& S, int z, const BoxAxis& X, const BoxAxis& Y) {
+  const long long* plane = S.sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
+  D3 ra0 = x_diffs(plane + (size_t)Y.a0 * S.sx, X);
+  D3 ra1 = x_diffs(plane + (size_t)Y.a1 * S.sx, X);
+  D3 rb0 = x_diffs(plane + (size_t)Y.b0 * S.sx, X);
+  D3 rb1 = x_diffs(plane + (size_t)Y.b1 * S.sx, X);
+  D9 r;
+  r.y0.d0 = rb0.d0 - ra0.d0; r.y0.d1 = rb0.d1 - ra0.d1; r.y0.d2 = rb0.d2 - ra0.d2;
+  r.y1.d0 = rb1.d0 - ra1.d0; r.y1.d1 = rb1.d1 - ra1.d1; r.y1.d2 = rb1.d2 - ra1.d2;
+  r.y2.d0 = ra1.d0 - ra0.d0; r.y2.d1 = ra1.d1 - ra0.d1; r.y2.d2 = ra1.d2 - ra0.d2;
+  return r;
+}
+__device__ __forceinline__ float weigh9(const D9& a, const D9& b, const BoxAxis& X, const BoxAxis& Y) {
+  // sum over y-op and x-op of cy*cx*(a-b)
+  auto w3 = [&](const D3& p, const D3& q) {
+    return X.c0 * float(p.d0 - q.d0) + X.c1 * float(p.d1 - q.d1) + X.c2 * float(p.d2 - q.d2);
+  };
+  return Y.c0 * w3(a.y0, b.y0) + Y.c1 * w3(a.y1, b.y1) + Y.c2 * w3(a.y2, b.y2);
+}
+
+// EvaluateSAT3D(p1, p2) on already offset + clamped world positions.
+__device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2) {
+  BoxAxis X = box_axis(fmaf(p1.x, S.inv_spacing.x, -0.5f), fmaf(p2.x, S.inv_spacing.x, -0.5f), S.sx);
+  BoxAxis Y = box_axis(fmaf(p1.y, S.inv_spacing.y, -0.5f), fmaf(p2.y, S.inv_spacing.y, -0.5f), S.sy);
+  BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
+  D9 za0 = yx_diffs(S, Z.a0, X, Y);
+  D9 za1 = yx_diffs(S, Z.a1, X, Y);
+  float acc = Z.c2 * weigh9(za1, za0, X, Y);
+  D9 zb0 = yx_diffs(S, Z.b0, X, Y);
+  acc = fmaf(Z.c0, weigh9(zb0, za0, X, Y), acc);
+  D9 zb1 = yx_diffs(S, Z.b1, X, Y);
+  acc = fmaf(Z.c1, weigh9(zb1, za1, X, Y), acc);
+  return acc * S.inv_scale;
+}
+
+// ---------------------------------------------------------------- pyramid
+// Gaussian extinction pyramid, float32 levels concatenated, x fastest.
+#define CVR_MAX_LEVELS 16
+struct PyramidView {
+  const float* data;
+  int n_levels;
+  int dims[CVR_MAX_LEVELS][3];
+  long long offset[CVR_MAX_LEVELS];
+  float3 grid;         // VolumeScaledSizes
+  float3 inv_grid;
+};
+
+__device__ __forceinline__ float pyr_fetch(const PyramidView& P, int l, int x, int y, int z) {
+  const int* d = P.dims[l];
+  return __ldg(P.data + P.offset[l] + (long long)x + (long long)d[0] * ((long long)y + (long long)d[1] * z));
+}
+// textureLod(pyr, tex_pos / S, level) at an integer level: trilinear in that level.
+__device__ __forceinline__ float pyr_sample_level(const PyramidView& P, int l, float3 tex_pos) {
+  const int* d = P.dims[l];
+  Tap tx = axis_tap(fmaf(tex_pos.x * P.inv_grid.x, float(d[0]), -0.5f), d[0]);
+  Tap ty = axis_tap(fmaf(tex_pos.y * P.inv_grid.y, float(d[1]), -0.5f), d[1]);
+  Tap tz = axis_tap(fmaf(tex_pos.z * P.inv_grid.z, float(d[2]), -0.5f), d[2]);
+  float c000 = pyr_fetch(P, l, tx.i0, ty.i0, tz.i0), c100 = pyr_fetch(P, l, tx.i1, ty.i0, tz.i0);
+  float c010 = pyr_fetch(P, l, tx.i0, ty.i1, tz.i0), c110 = pyr_fetch(P, l, tx.i1, ty.i1, tz.i0);
+  float c001 = pyr_fetch(P, l, tx.i0, ty.i0, tz.i1), c101 = pyr_fetch(P, l, tx.i1, ty.i0, tz.i1);
+  float c011 = pyr_fetch(P, l, tx.i0, ty.i1, tz.i1), c111 = pyr_fetch(P, l, tx.i1, ty.i1, tz.i1);
+  float c00 = fmaf(tx.t, c100 - c000, c000), c10 = fmaf(tx.t, c110 - c010, c010);
+  float c01 = fmaf(tx.t, c101 - c001, c001), c11 = fmaf(tx.t, c111 - c011, c011);
+  float c0 = fmaf(ty.t, c10 - c00, c00), c1 = fmaf(ty.t, c11 - c01, c01);
+  return fmaf(tz.t, c1 - c0, c0);
+}
+// GL_LINEAR_MIPMAP_LINEAR with an explicit lod: levels clamped to the
+// pyramid, fractional lods blend the two neighbouring levels.
+__device__ __forceinline__ float pyr_sample(const PyramidView& P, float lod, float3 tex_pos) {
+  float maxl = float(P.n_levels - 1);
+  lod = fminf(fmaxf(lod, 0.0f), maxl);
+  float fl = floorf(lod);
+  int l0 = int(fl);
+  float t = lod - fl;
+  float a = pyr_sample_level(P, l0, tex_pos);
+  if (t == 0.0f) return a;
+  float b = pyr_sample_level(P, min(l0 + 1, P.n_levels - 1), tex_pos);
+  return fmaf(t, b - a, a);
+}
+
+}  // namespace cvr

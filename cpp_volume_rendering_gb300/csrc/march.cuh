@@ -1,0 +1,71 @@
+// march.cuh — kernel argument blocks shared by march.cu and the context code.
+#pragma once
+
+#include "cvr_device.cuh"
+
+namespace cvr {
+
+#define CVR_MAX_GT_RAYS 256
+
+// Launch geometry: each CTA covers a tile_w x tile_h block of pixels; each
+// warp covers an 8x4 sub-tile so the 32 rays of a warp stay spatially
+// coherent (they walk neighbouring voxels, which keeps gathers in L1).
+struct FrameArgs {
+  VolumeView vol;
+  CameraView cam;
+  const float4* tf;      // RGBt table (alpha = extinction)
+  int tf_n;
+  float step;            // StepSize
+  int W, H;
+  int tile_w, tile_h;    // pixels per CTA (multiples of 8 and 4)
+  float4* out;
+  uint32_t* counts;                // per-pixel step count, nullable
+  unsigned long long* stats;       // [0] samples, [1] shaded samples, [2] secondary fetches
+};
+
+struct ExtArgs {
+  SatView sat;
+  int apply_occ, apply_sdw;
+  int n_shells;
+  float radii[32];
+  float cone_angle, interval, initial, ui_weight, max_dist;
+  int shadow_type;
+  float3 light_pos, light_fwd;
+  float ka, kd;
+};
+
+struct ConeTableDev {
+  int n_sections;
+  int n1, n3, n7;
+  float3 axes[10];
+  float initial_step, w7, ui_weight;
+};
+
+struct DosArgs {
+  PyramidView pyr;
+  const float4* occ_sections;  // device, n_sections entries
+  const float4* sdw_sections;
+  ConeTableDev occ, sdw;
+  int apply_occ, apply_sdw, shadow_type;
+  float3 light_pos, light_fwd, light_up, light_right;
+  float spot_cos_max;
+  float ka, kd;
+};
+
+struct GtArgs {
+  const float3* occ_vec;  // device
+  const float3* sdw_vec;
+  int n_occ, n_sdw;
+  float gap, lstep;
+  int apply_occ, apply_sdw, shadow_type;
+  float occ_dist, sdw_dist;
+  float3 light_pos, light_fwd, light_up, light_right;
+  float ka, kd;
+};
+
+cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
+cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, cudaStream_t st);
+cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, cudaStream_t st);
+cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st);
+
+}  // namespace cvr

@@ -1,0 +1,400 @@
+"""Scenes for tests and the benchmark, built through the C ABI of libcvr.so.
+
+* TransferFunction: control points -> the RGBt / RGBA tables and the per-voxel
+  extinction (host code of the library, restating TransferFunction1D).
+* Context: a cvr_ctx (device state of one renderer: volume, tables, frames).
+* configuration(): the five seeded synthetic workloads (volume, transfer
+  function, camera, light, method parameters).
+
+World units follow the reference: a volume of dims N and spacing s spans
+[-N*s/2, N*s/2].  The plain-casting workload uses the unit cube (s = 1/64);
+the illumination workloads use 1 world unit per voxel, the spacing the
+reference's .raw / .syn readers set, because their cone, SAT and pyramid
+parameters are expressed in those units.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import abi
+from .abi import check
+
+# ---------------------------------------------------------------- TF
+
+
+@dataclass
+class TransferFunction:
+    rgb: list  # (r, g, b, iso)
+    alpha: list  # (a, iso)
+    max_density: int = 255
+    extinction_input: bool = False
+
+    def _pts(self):
+        rgb = np.ascontiguousarray(np.array(self.rgb, dtype=np.float64).reshape(-1, 4))
+        al = np.ascontiguousarray(np.array(self.alpha, dtype=np.float64).reshape(-1, 2))
+        return rgb, al
+
+    def tables(self) -> tuple[np.ndarray, np.ndarray]:
+        """(rgbt, rgba) tables, (max_density+1) x 4 float32."""
+        rgb, al = self._pts()
+        n = self.max_density + 1
+        rgbt = np.zeros((n, 4), np.float32)
+        rgba = np.zeros((n, 4), np.float32)
+        check(abi.load().cvr_tf_build_linear(self.max_density, len(rgb), abi.dptr(rgb), len(al), abi.dptr(al),
+                                             int(self.extinction_input), abi.fptr(rgbt), abi.fptr(rgba)))
+        return rgbt, rgba
+
+    def ext_per_value(self, dtype: int) -> np.ndarray:
+        rgb, al = self._pts()
+        out = np.zeros(256 if dtype == abi.CVR_U8 else 65536, np.float64)
+        check(abi.load().cvr_tf_ext_per_value(self.max_density, len(rgb), abi.dptr(rgb), len(al), abi.dptr(al),
+                                              int(self.extinction_input), dtype, abi.dptr(out)))
+        return out
+
+    @staticmethod
+    def read_tf1d(path: str) -> "TransferFunction":
+        md, ext, nr, na = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        rgb = np.zeros((4096, 4), np.float64)
+        al = np.zeros((4096, 2), np.float64)
+        check(abi.load().cvr_read_tf1d(path.encode(), C.byref(md), C.byref(ext), C.byref(nr), abi.dptr(rgb), 4096,
+                                       C.byref(na), abi.dptr(al), 4096))
+        return TransferFunction([tuple(r) for r in rgb[:nr.value]], [tuple(a) for a in al[:na.value]],
+                                md.value, bool(ext.value))
+
+
+# The benchmark transfer function: 4 piecewise-linear RGBA points at
+# 0/80/160/255 with opacity 0/0.05/0.4/0.9 and a fixed colour ramp.
+BENCH_TF = TransferFunction(
+    rgb=[(0.20, 0.30, 0.90, 0), (0.30, 0.80, 0.40, 80), (0.90, 0.70, 0.20, 160), (1.00, 0.95, 0.90, 255)],
+    alpha=[(0.0, 0), (0.05, 80), (0.4, 160), (0.9, 255)],
+)
+
+# ---------------------------------------------------------------- volumes
+
+
+def synth_blobs(w, h, d, dtype, n_blobs, seed, noise_max=0.0) -> np.ndarray:
+    out = np.empty((d, h, w), np.uint8 if dtype == abi.CVR_U8 else np.uint16)
+    check(abi.load().cvr_synth_blobs(abi.vptr(out), w, h, d, dtype, n_blobs, seed, noise_max))
+    return out
+
+
+def synth_value_noise(w, h, d, dtype, seed, octaves=4, lacunarity=2.0, gain=0.5, shells=4) -> np.ndarray:
+    out = np.empty((d, h, w), np.uint8 if dtype == abi.CVR_U8 else np.uint16)
+    check(abi.load().cvr_synth_value_noise(abi.vptr(out), w, h, d, dtype, octaves, lacunarity, gain, shells, seed))
+    return out
+
+
+def cone_table(half_angle, packing, covered, initial_step, ui_weight, min_sigma) -> abi.ConeTable:
+    t = abi.ConeTable()
+    check(abi.load().cvr_cone_sampler_build(half_angle, packing, covered, initial_step, ui_weight, min_sigma,
+                                            C.byref(t)))
+    return t
+
+
+def gt_vectors(n_occ, occ_aperture, n_sdw, sdw_aperture, seed=1):
+    occ = np.zeros((max(n_occ, 1), 3), np.float32)
+    sdw = np.zeros((max(n_sdw, 1), 3), np.float32)
+    check(abi.load().cvr_gt_kernel_vectors(n_occ, occ_aperture, n_sdw, sdw_aperture, seed, abi.fptr(occ),
+                                           abi.fptr(sdw)))
+    return occ[:n_occ].copy(), sdw[:n_sdw].copy()
+
+
+# ---------------------------------------------------------------- camera / light
+
+
+def camera(eye, center=(0, 0, 0), up=(0, 1, 0), fovy=30.0, aspect=0.0) -> abi.Camera:
+    c = abi.Camera()
+    c.eye[:] = [float(v) for v in eye]
+    c.center[:] = [float(v) for v in center]
+    c.up[:] = [float(v) for v in up]
+    c.fovy_deg = fovy
+    c.aspect = aspect
+    return c
+
+
+def orbit_eye(distance, azimuth_deg, elevation_deg):
+    a, e = math.radians(azimuth_deg), math.radians(elevation_deg)
+    return (distance * math.cos(e) * math.sin(a), distance * math.sin(e), distance * math.cos(e) * math.cos(a))
+
+
+def _norm(v):
+    v = np.asarray(v, np.float64)
+    return v / np.linalg.norm(v)
+
+
+def light(kind, position=(0, 0, 0), forward=(0, 0, 1), up=(0, 1, 0), right=(1, 0, 0), spot_cos=0.0) -> abi.Light:
+    L = abi.Light()
+    L.type = kind
+    L.position[:] = [float(v) for v in position]
+    L.forward[:] = [float(v) for v in forward]
+    L.up[:] = [float(v) for v in up]
+    L.right[:] = [float(v) for v in right]
+    L.spot_cos_max = spot_cos
+    return L
+
+
+def light_frame(direction):
+    """Orthonormal (forward, up, right) light-camera vectors for a direction."""
+    f = _norm(direction)
+    ref = np.array([0.0, 1.0, 0.0]) if abs(f[1]) < 0.9 else np.array([1.0, 0.0, 0.0])
+    r = _norm(np.cross(ref, f))
+    u = _norm(np.cross(f, r))
+    return tuple(f), tuple(u), tuple(r)
+
+
+# ---------------------------------------------------------------- params
+
+
+def default_step(spacing) -> float:
+    """Init(): 0.5 * |spacing| / sqrt(3) (rc1prenderer.cpp:63) = half a voxel."""
+    s = np.asarray(spacing, np.float64)
+    return float((0.5 / math.sqrt(3.0)) * math.sqrt(float((s * s).sum())))
+
+
+def ext_params(step, diag, ao_radii=(2, 6, 16), shadow_type=1, apply_occ=True, apply_sdw=True,
+               cone_angle_deg=1.0, interval=2.0, initial=2.0, ui_weight=1.0) -> abi.ExtParams:
+    p = abi.ExtParams()
+    p.step_size = step
+    p.apply_occlusion = int(apply_occ)
+    p.apply_shadow = int(apply_sdw)
+    p.ao_n_shells = len(ao_radii)
+    for i, r in enumerate(ao_radii):
+        p.ao_radii[i] = float(r)
+    p.sdw_cone_angle_rad = float(cone_angle_deg * math.pi / 180.0)
+    p.sdw_sample_interval = interval
+    p.sdw_initial_step = initial
+    p.sdw_ui_weight = ui_weight
+    p.sdw_max_distance = 0.75 * diag
+    p.shadow_type = shadow_type
+    p.ka, p.kd = 0.5, 0.5
+    return p
+
+
+def dos_params(step, apply_occ=True, apply_sdw=False, shadow_type=0) -> abi.DosParams:
+    p = abi.DosParams()
+    p.step_size = step
+    p.apply_occlusion = int(apply_occ)
+    p.apply_shadow = int(apply_sdw)
+    p.shadow_type = shadow_type
+    p.ka, p.kd = 0.5, 0.5
+    return p
+
+
+def gt_params(step, diag, occ_distance=None, sdw_distance=None, light_step=0.5, gap=1.0, apply_occ=True,
+              apply_sdw=True, shadow_type=0) -> abi.GtParams:
+    p = abi.GtParams()
+    p.step_size = step
+    p.light_ray_initial_gap = gap
+    p.light_ray_step_size = light_step
+    p.apply_occlusion = int(apply_occ)
+    p.occ_distance = occ_distance if occ_distance is not None else 0.5 * diag
+    p.apply_shadow = int(apply_sdw)
+    p.sdw_distance = sdw_distance if sdw_distance is not None else 0.75 * diag
+    p.shadow_type = shadow_type
+    p.ka, p.kd = 0.5, 0.5
+    return p
+
+
+# ---------------------------------------------------------------- context
+
+
+class Context:
+    """One cvr_ctx: the device state a renderer plugin builds in Init()."""
+
+    def __init__(self, device: int = 0):
+        self.lib = abi.load()
+        h = C.c_void_p()
+        code = self.lib.cvr_create(C.byref(h), device)
+        if code != abi.CVR_OK:
+            raise abi.CvrError(code, self.lib.cvr_last_error(None).decode())
+        self.h = h
+        self.dims = None
+        self.dtype = None
+        self.spacing = None
+
+    def close(self):
+        if self.h:
+            self.lib.cvr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, code):
+        check(code, self.h)
+
+    def set_volume(self, vol: np.ndarray, spacing=(1.0, 1.0, 1.0)):
+        vol = np.ascontiguousarray(vol)
+        d, h, w = vol.shape
+        dtype = abi.CVR_U8 if vol.dtype == np.uint8 else abi.CVR_U16
+        self._ck(self.lib.cvr_set_volume(self.h, abi.vptr(vol), w, h, d, dtype, *[float(s) for s in spacing]))
+        self.dims, self.dtype, self.spacing = (w, h, d), dtype, tuple(float(s) for s in spacing)
+
+    def set_transfer_function(self, tf: TransferFunction):
+        rgbt, rgba = tf.tables()
+        self._ck(self.lib.cvr_set_transfer_function(self.h, abi.fptr(rgbt), abi.fptr(rgba), len(rgbt)))
+
+    def build_sat(self, ext_per_value: np.ndarray):
+        ext = np.ascontiguousarray(ext_per_value, np.float64)
+        self._ck(self.lib.cvr_build_sat(self.h, abi.dptr(ext), len(ext)))
+
+    def sat(self) -> tuple[np.ndarray, int]:
+        dims = (C.c_int * 3)()
+        fb = C.c_int()
+        self._ck(self.lib.cvr_get_sat_info(self.h, dims, C.byref(fb)))
+        out = np.zeros((dims[2], dims[1], dims[0]), np.int64)
+        self._ck(self.lib.cvr_download_sat(self.h, out.ctypes.data_as(C.POINTER(C.c_int64))))
+        return out, fb.value
+
+    def build_pyramid(self, base_dims=(128, 128, 128), sigma0=1.0, n_levels=0):
+        p = abi.PyramidParams()
+        p.base_dims[:] = list(base_dims)
+        p.sigma0 = sigma0
+        p.n_levels = n_levels
+        self._ck(self.lib.cvr_build_ext_pyramid(self.h, C.byref(p)))
+
+    def pyramid(self) -> list[np.ndarray]:
+        n = C.c_int()
+        dims = (C.c_int * 48)()
+        self._ck(self.lib.cvr_get_pyramid_info(self.h, C.byref(n), dims, 16))
+        levels = []
+        for l in range(n.value):
+            w, h, d = dims[3 * l], dims[3 * l + 1], dims[3 * l + 2]
+            a = np.zeros((d, h, w), np.float32)
+            self._ck(self.lib.cvr_download_pyramid_level(self.h, l, abi.fptr(a)))
+            levels.append(a)
+        return levels
+
+    def set_cone_tables(self, occ: abi.ConeTable, sdw: abi.ConeTable):
+        self._ck(self.lib.cvr_set_cone_tables(self.h, C.byref(occ), C.byref(sdw)))
+
+    def set_gt_kernels(self, occ: np.ndarray, sdw: np.ndarray):
+        occ = np.ascontiguousarray(occ, np.float32).reshape(-1, 3)
+        sdw = np.ascontiguousarray(sdw, np.float32).reshape(-1, 3)
+        if len(occ) == 0:
+            occ = np.zeros((1, 3), np.float32)[:0]
+        self._ck(self.lib.cvr_set_gt_kernels(self.h, abi.fptr(np.ascontiguousarray(occ)), len(occ),
+                                             abi.fptr(np.ascontiguousarray(sdw)), len(sdw)))
+
+    def render(self, method, cam, lt, params, w, h, stats=True):
+        """Renders into host memory; returns (H x W x 4 float32 image, FrameStats)."""
+        out = np.zeros((h, w, 4), np.float32)
+        st = abi.FrameStats()
+        self._ck(self.lib.cvr_render_host(self.h, method, C.byref(cam), C.byref(lt) if lt is not None else None,
+                                          C.byref(params), C.sizeof(params), abi.fptr(out), w, h,
+                                          C.byref(st) if stats else None))
+        return out, st
+
+
+# ---------------------------------------------------------------- workloads
+
+
+@dataclass
+class Workload:
+    name: str
+    method: int
+    volume: np.ndarray
+    spacing: tuple
+    tf: TransferFunction
+    cam: abi.Camera
+    light: abi.Light
+    params: object
+    width: int
+    height: int
+    pyramid: dict = field(default_factory=dict)
+    cones: tuple = ()
+    gt: tuple = ()
+
+    @property
+    def dims(self):
+        d, h, w = self.volume.shape
+        return (w, h, d)
+
+    @property
+    def diagonal(self):
+        w, h, d = self.dims
+        s = self.spacing
+        return math.sqrt((w * s[0]) ** 2 + (h * s[1]) ** 2 + (d * s[2]) ** 2)
+
+    @property
+    def dtype(self):
+        return abi.CVR_U8 if self.volume.dtype == np.uint8 else abi.CVR_U16
+
+
+def workload(name: str, n: int | None = None, image: int | None = None) -> Workload:
+    """The seeded synthetic workloads.  n / image shrink the volume side and
+    image side for fast parity tests (same generator, same parameters).
+
+    plain      : 64^3 u8, 8 Gaussian blobs, unit cube, 256^2, step 0.5 voxel
+    extinction : 256^3 u16 4-octave value noise in 4 nested shells, SAT AO
+                 (radii 2, 6, 16 voxels) + directional SAT cone shadow, 1024^2
+    ground_truth / cone : 256^3 u8, 32 blobs + U[0,20] background; GT with 16
+                 occlusion rays (90 deg, 32 voxels) and 1 shadow ray to a point
+                 light at 1-voxel steps; cone method on a 5-level pyramid, 512^2
+    """
+    if name == "plain":
+        n = n or 64
+        image = image or 256
+        vol = synth_blobs(n, n, n, abi.CVR_U8, 8, seed=1000)
+        sp = (1.0 / n,) * 3
+        cam = camera(orbit_eye(3.0, 35.0, 25.0), fovy=30.0)
+        p = abi.PlainParams()
+        p.step_size = 0.5 / n
+        return Workload(name, abi.PLAIN, vol, sp, BENCH_TF, cam, light(abi.LIGHT_POINT), p, image, image)
+    if name == "extinction":
+        n = n or 256
+        image = image or 1024
+        vol = synth_value_noise(n, n, n, abi.CVR_U16, seed=2000)
+        sp = (1.0, 1.0, 1.0)
+        cam = camera(orbit_eye(3.0 * n, 35.0, 25.0), fovy=30.0)
+        fwd, up, right = light_frame((0.35, 0.8, 0.45))
+        lt = light(abi.LIGHT_DIRECTIONAL, position=tuple(3.0 * n * np.array(fwd)), forward=fwd, up=up, right=right)
+        wl = Workload(name, abi.EXTINCTION, vol, sp, BENCH_TF, cam, lt, None, image, image)
+        wl.params = ext_params(default_step(sp), wl.diagonal, ao_radii=(2, 6, 16), shadow_type=1)
+        return wl
+    if name in ("ground_truth", "cone"):
+        n = n or 256
+        image = image or 512
+        vol = synth_blobs(n, n, n, abi.CVR_U8, 32, seed=3000, noise_max=20.0)
+        sp = (1.0, 1.0, 1.0)
+        cam = camera(orbit_eye(3.0 * n, -30.0, 20.0), fovy=30.0)
+        lpos = tuple(2.0 * n * _norm((-0.5, 1.0, 0.4)))
+        fwd, up, right = light_frame(lpos)
+        lt = light(abi.LIGHT_POINT, position=lpos, forward=fwd, up=up, right=right)
+        wl = Workload(name, abi.GROUND_TRUTH, vol, sp, BENCH_TF, cam, lt, None, image, image)
+        diag = wl.diagonal
+        if name == "ground_truth":
+            wl.params = gt_params(default_step(sp), diag, occ_distance=32.0, light_step=1.0, gap=1.0,
+                                  shadow_type=0)
+            wl.gt = gt_vectors(16, 90.0, 1, 0.0, seed=1)
+        else:
+            wl.method = abi.CONE_DOS
+            wl.params = dos_params(default_step(sp), apply_occ=True, apply_sdw=True, shadow_type=0)
+            # RC1PConeTracingDirOcclusionShading defaults (dosrcrenderer.cpp:47-59,112-113):
+            # occlusion 20 deg, packing 3, weight 0.35, 0.5*diag; shadow 0.5 deg, packing 1, weight 1, 0.75*diag.
+            wl.cones = (cone_table(20.0, 1, 0.5 * diag, 3.0, 0.35, 1.0),
+                        cone_table(0.5, 0, 0.75 * diag, 3.0, 1.0, 1.0))
+            base = max(1, n // 2)
+            wl.pyramid = dict(base_dims=(base, base, base), sigma0=1.0, n_levels=5)
+        return wl
+    raise KeyError(name)
+
+
+def prepare(ctx: Context, wl: Workload):
+    """Init(): uploads the volume and every table the workload's method needs."""
+    ctx.set_volume(wl.volume, wl.spacing)
+    ctx.set_transfer_function(wl.tf)
+    if wl.method == abi.EXTINCTION:
+        ctx.build_sat(wl.tf.ext_per_value(wl.dtype))
+    if wl.method == abi.CONE_DOS:
+        ctx.build_pyramid(**wl.pyramid)
+        ctx.set_cone_tables(*wl.cones)
+    if wl.method == abi.GROUND_TRUTH:
+        ctx.set_gt_kernels(*wl.gt)

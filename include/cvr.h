@@ -1,0 +1,297 @@
+/*
+ * cvr.h — C ABI of the GB300-native structured volume ray caster (libcvr.so).
+ *
+ * This is the device boundary that replaces the reference's GLSL compute
+ * dispatch.  In the reference every renderer plugin reaches the GPU through
+ *   BaseVolumeRenderer::Redraw()            (cppvolrend/volrenderbase.h:49)
+ *     -> gl::ComputeShader::Dispatch()      (libs/gl_utils/computeshader.cpp:120-126)
+ *       -> glDispatchCompute of a *.comp shader, 8x8 work groups
+ * with all state passed as uniforms / textures in Init() and Update()
+ * (e.g. RayCasting1Pass::Init/Update, cppvolrend/structured/rc1pass/rc1prenderer.cpp:50-138).
+ * Here the same state is uploaded once through cvr_set_* calls (the Init()
+ * half) and each frame is one cvr_render call (the Update()+Redraw() half).
+ *
+ * Conventions
+ *  - Every entry point returns cvr_status: 0 on success, a negative code on
+ *    failure.  Nothing in the library calls exit(); the reference's
+ *    gl::ExitOnGLError / loader exit() paths become error codes.
+ *  - Handles are opaque.  The library owns every device buffer it allocates;
+ *    the caller owns host buffers and any device output buffer it passes in.
+ *  - A context is bound to one CUDA device and one CUDA stream.  Rendering is
+ *    asynchronous on that stream unless a call says otherwise.  Contexts are
+ *    thread-compatible, not thread-safe: one context per host thread.
+ *  - Images are RGBA32F, row 0 = bottom row (OpenGL image convention used by
+ *    imageStore in the reference shaders); pixels whose ray misses the volume
+ *    are (0,0,0,0) as after RenderFrameToScreen::ClearTexture.
+ *  - World space: the volume occupies the axis-aligned box
+ *    [-S/2, S/2] with S = dims * spacing (ray_bbox_intersection.comp:34-52).
+ */
+#ifndef CVR_H
+#define CVR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CVR_ABI_VERSION 1
+
+typedef int cvr_status;
+
+enum cvr_status_codes {
+  CVR_OK = 0,
+  CVR_ERR_INVALID_ARG = -1,  /* bad pointer, size or enum value */
+  CVR_ERR_NO_VOLUME = -2,    /* Init() returns false without a volume (rc1prenderer.cpp:54) */
+  CVR_ERR_NOT_READY = -3,    /* a table the method needs (SAT, pyramid, cone or kernel tables) is missing */
+  CVR_ERR_CUDA = -4,         /* CUDA runtime / launch error; see cvr_last_error() */
+  CVR_ERR_OUT_OF_MEMORY = -5,
+  CVR_ERR_IO = -6,           /* file could not be opened / was short (rawloader.cpp:16-35) */
+  CVR_ERR_FORMAT = -7,       /* file content malformed */
+  CVR_ERR_TIMEOUT = -8,      /* a bounded device-side wait gave up */
+  CVR_ERR_UNSUPPORTED = -9
+};
+
+typedef enum cvr_dtype {
+  CVR_U8 = 1,   /* DataStorageSize::_8_BITS,  normalised by 255   (structuredgridvolume.cpp:121-151) */
+  CVR_U16 = 2   /* DataStorageSize::_16_BITS, normalised by 65535 */
+} cvr_dtype;
+
+typedef enum cvr_method {
+  CVR_METHOD_PLAIN = 0,       /* rc1pass    : ray_marching_1p.comp */
+  CVR_METHOD_EXTINCTION = 1,  /* rc1pextbsd : ebs_ray_bbox_marching.comp */
+  CVR_METHOD_CONE_DOS = 2,    /* rc1pdosct  : ray_bbox_marching.comp */
+  CVR_METHOD_GROUND_TRUTH = 3 /* rc1pcrtgt  : gt_ray_marching.comp (single pass) */
+} cvr_method;
+
+typedef struct cvr_ctx cvr_ctx;
+
+/* Camera state: vis::CameraData (libs/vis_utils/camera.cpp:17-54) reduced to
+ * what the shaders consume: eye, LookAt = glm::lookAt(eye, center, up)
+ * (camera.cpp:281-284), tan(fovy/2) and aspect ratio. */
+typedef struct cvr_camera {
+  float eye[3];
+  float center[3];
+  float up[3];
+  float fovy_deg;  /* reference default 45 */
+  float aspect;    /* <= 0: use image width / height (Camera::UpdateAspectRatio) */
+} cvr_camera;
+
+typedef enum cvr_light_type {
+  CVR_LIGHT_POINT = 0,
+  CVR_LIGHT_SPOT = 1,
+  CVR_LIGHT_DIRECTIONAL = 2
+} cvr_light_type;
+
+/* Light state: vis::LightSourceData (libs/volvis_utils/lightsourcelist.h:17-50).
+ * forward/up/right are the light camera vectors as the renderer's shader
+ * receives them (LightCamForward / LightCamUp / LightCamRight uniforms). */
+typedef struct cvr_light {
+  int type;            /* cvr_light_type */
+  float position[3];   /* WorldLightingPos / LightSourcePosition */
+  float forward[3];    /* LightCamForward: for directional lights the direction towards the light */
+  float up[3];         /* LightCamUp */
+  float right[3];      /* LightCamRight */
+  float spot_cos_max;  /* SpotLightMaxAngle uniform (a cosine), spot lights only */
+} cvr_light;
+
+/* ---- per-method parameters (the renderers' uniforms) ------------------- */
+
+/* RayCasting1Pass (rc1prenderer.cpp:72-138, ray_marching_1p.comp:85-178). */
+typedef struct cvr_plain_params {
+  float step_size;  /* StepSize, world units; Init default 0.5*|spacing|/sqrt(3) (rc1prenderer.cpp:63) */
+} cvr_plain_params;
+
+/* RC1PExtinctionBasedShading (ebsrenderer.cpp:19-247, ebs_ray_bbox_marching.comp). */
+#define CVR_MAX_AO_SHELLS 32
+typedef struct cvr_ext_params {
+  float step_size;
+  int apply_occlusion;           /* ApplyOcclusion */
+  int apply_shadow;              /* ApplyShadow */
+  int ao_n_shells;               /* AmbOccShells (reference default 15) */
+  float ao_radii[CVR_MAX_AO_SHELLS]; /* shell radius i in voxels; reference: AmbOccRadius*(i+1) */
+  float sdw_cone_angle_rad;      /* DirSdwConeAngle (default 1 degree) */
+  float sdw_sample_interval;     /* DirSdwSampleInterval, voxels (default 2) */
+  float sdw_initial_step;        /* DirSdwInitialStep, voxels (default 2) */
+  float sdw_ui_weight;           /* DirSdwUserInterfaceWeight (default 1) */
+  float sdw_max_distance;        /* DirSdwConeMaxDistance, world (default 0.75*diagonal) */
+  int shadow_type;               /* TypeOfShadow: 0 point light (position), 1 directional (forward) */
+  float ka, kd;                  /* Kambient, Kdiffuse (RenderingParameters defaults 0.5, 0.5) */
+} cvr_ext_params;
+
+/* RC1PConeTracingDirOcclusionShading (dosrcrenderer.cpp:134-247, ray_bbox_marching.comp). */
+typedef struct cvr_dos_params {
+  float step_size;
+  int apply_occlusion;  /* default true */
+  int apply_shadow;     /* default false (dosrcrenderer.cpp:53) */
+  int shadow_type;      /* TypeOfShadow: 0 point, 1 spot, 2 directional */
+  float ka, kd;
+} cvr_dos_params;
+
+/* RC1PConeLightGroundTruthSteps (crtgtrenderer.cpp:23-260, gt_ray_marching.comp). */
+typedef struct cvr_gt_params {
+  float step_size;
+  float light_ray_initial_gap;  /* LightRayInitialGap (default 1) */
+  float light_ray_step_size;    /* LightRayStepSize (default 0.5) */
+  int apply_occlusion;          /* ApplyConeOcclusion */
+  float occ_distance;           /* OccConeDistanceEvaluation (default 0.5*diagonal) */
+  int apply_shadow;             /* ApplyConeShadow */
+  float sdw_distance;           /* SdwConeDistanceEvaluation (default 0.75*diagonal) */
+  int shadow_type;              /* SdwShadowType: 0 point, 1 spot, 2 directional */
+  float ka, kd;
+} cvr_gt_params;
+
+/* Cone section table of one ConeGaussianSampler
+ * (cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp:179-205, 212-386).
+ * sections[i] = (interval distance, mip level, d_integral, amplitude). */
+#define CVR_MAX_CONE_SECTIONS 512
+typedef struct cvr_cone_table {
+  int n_sections;
+  float sections[CVR_MAX_CONE_SECTIONS][4];
+  int integration_samples[3];   /* gaussian_samples_1 / _3 / _7 */
+  float axes[10][3];            /* ray3_axis[0..2], ray7_axis[0..6] */
+  float initial_step;           /* OccInitialStep / SdwInitialStep */
+  float ray7_adj_weight;        /* OccRay7AdjWeight / SdwRay7AdjWeight */
+  float ui_weight;              /* OccUIWeight / SdwUIWeight */
+} cvr_cone_table;
+
+/* Extinction pyramid parameters (ExtinctionCoefficientVolume,
+ * cppvolrend/structured/rc1pdosct/extcoefvolumegenerator.cpp:20-408). */
+typedef struct cvr_pyramid_params {
+  int base_dims[3];   /* custom base resolution (reference default 128^3) */
+  float sigma0;       /* S0, world units (reference default 1) */
+  int n_levels;       /* 0 = until a level would have size 0 (reference behaviour) */
+} cvr_pyramid_params;
+
+typedef struct cvr_frame_stats {
+  uint64_t samples;         /* executed primary-ray steps (volume fetches) */
+  uint64_t shaded_samples;  /* steps with extinction > 0 that went through ShadeSample */
+  uint64_t aux_fetches;     /* secondary lookups: SAT box queries (extinction), pyramid
+                               taps (cone), light-ray volume samples (ground truth) */
+  float kernel_ms;          /* device time of the render kernel (CUDA events) */
+} cvr_frame_stats;
+
+/* ---- context ------------------------------------------------------------ */
+cvr_status cvr_create(cvr_ctx** out, int device);
+void cvr_destroy(cvr_ctx* ctx);
+/* Last error message of this context (or of the last failed cvr_create when ctx == NULL). */
+const char* cvr_last_error(const cvr_ctx* ctx);
+int cvr_abi_version(void);
+/* Blocks until all work queued on the context stream has finished. */
+cvr_status cvr_sync(cvr_ctx* ctx);
+/* The CUDA stream (cudaStream_t) the context launches on. */
+void* cvr_stream(cvr_ctx* ctx);
+
+/* ---- Init() state ------------------------------------------------------- */
+/* Volume upload; replaces DataManager::GenerateStructuredVolumeTexture +
+ * vis::GenerateRTexture (libs/volvis_utils/utils.cpp:20-56).  Voxels stay
+ * u8/u16 on the device (x fastest: x + W*y + W*H*z). */
+cvr_status cvr_set_volume(cvr_ctx* ctx, const void* host_voxels, int w, int h, int d,
+                          int dtype, float sx, float sy, float sz);
+/* Same, from device memory already resident on this context's device. */
+cvr_status cvr_set_volume_device(cvr_ctx* ctx, const void* dev_voxels, int w, int h, int d,
+                                 int dtype, float sx, float sy, float sz);
+
+/* Transfer function tables (TransferFunction1D::GenerateTexture_1D_RGBt and
+ * GenerateTexture_1D_RGBA, transferfunction1d.cpp:58-118): n entries of RGBA.
+ * rgbt alpha = extinction; rgba alpha = opacity (may be NULL: derived as 1-exp(-t)). */
+cvr_status cvr_set_transfer_function(cvr_ctx* ctx, const float* rgbt, const float* rgba, int n);
+
+/* Extinction SAT (GenerateExtinctionSAT3DTex, ebsrenderer.cpp:624-723).
+ * ext_per_value[v] = extinction of voxel value v (TransferFunction1D::GetExtN of
+ * the normalised value), n_values = 256 (u8) or 65536 (u16).  The SAT is
+ * (W+2)(H+2)(D+2), zero border, built on the device by exact int64
+ * fixed-point prefix sums. */
+cvr_status cvr_build_sat(cvr_ctx* ctx, const double* ext_per_value, int n_values);
+/* Fixed-point scale of the SAT: entry = round(sum * 2^frac_bits). */
+cvr_status cvr_get_sat_info(cvr_ctx* ctx, int dims[3], int* frac_bits);
+/* Copies the SAT to host memory (dims[0]*dims[1]*dims[2] int64). Synchronous. */
+cvr_status cvr_download_sat(cvr_ctx* ctx, int64_t* host_out);
+
+/* Gaussian extinction mip pyramid (gen_extcoefvol_anysize*.comp + backtotau.comp). */
+cvr_status cvr_build_ext_pyramid(cvr_ctx* ctx, const cvr_pyramid_params* params);
+/* Level count and per-level dims (level_dims is [max_levels][3]). */
+cvr_status cvr_get_pyramid_info(cvr_ctx* ctx, int* n_levels, int (*level_dims)[3], int max_levels);
+/* Copies one level (float32, x fastest) to host memory. Synchronous. */
+cvr_status cvr_download_pyramid_level(cvr_ctx* ctx, int level, float* host_out);
+
+/* Cone tables of the occlusion and shadow samplers (BindConeOcclusionUniforms /
+ * BindConeShadowUniforms, dosrcrenderer.cpp:823-990). */
+cvr_status cvr_set_cone_tables(cvr_ctx* ctx, const cvr_cone_table* occlusion, const cvr_cone_table* shadow);
+
+/* Ground-truth kernel vectors (TexOccRaysSampledVectors / TexSdwRaysSampledVectors,
+ * crtgtrenderer.cpp:131-187): n x 3 floats, in the (right, up, dir) frame. */
+cvr_status cvr_set_gt_kernels(cvr_ctx* ctx, const float* occ_vectors, int n_occ,
+                              const float* sdw_vectors, int n_sdw);
+
+/* ---- Update() + Redraw() ---------------------------------------------- */
+/* Renders one w x h RGBA32F frame into out_rgba_dev (device memory, 16*w*h bytes).
+ * params points to the method's cvr_*_params struct, params_size = sizeof it.
+ * sample_counts_dev (nullable) receives the per-pixel primary step count.
+ * stats (nullable): when given, the call synchronises and fills it. */
+cvr_status cvr_render(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
+                      const void* params, size_t params_size, float* out_rgba_dev, int w, int h,
+                      uint32_t* sample_counts_dev, cvr_frame_stats* stats);
+/* Same as cvr_render but the image lands in host memory (synchronous): the
+ * RenderFrameToScreen readback path (renderingmanager.cpp:638-639). */
+cvr_status cvr_render_host(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
+                           const void* params, size_t params_size, float* out_rgba_host, int w, int h,
+                           cvr_frame_stats* stats);
+
+/* Library-owned device frame buffer of at least w*h RGBA32F pixels (the
+ * headless counterpart of GetScreenTextureID, volrenderbase.h:73-75).  The
+ * pointer stays valid until the next call with a larger size or cvr_destroy. */
+cvr_status cvr_get_frame_buffer(cvr_ctx* ctx, int w, int h, float** dev_out);
+
+/* ---- device timing on the context stream --------------------------------- */
+cvr_status cvr_timer_start(cvr_ctx* ctx);
+/* Records the stop event, synchronises and returns elapsed milliseconds. */
+cvr_status cvr_timer_stop(cvr_ctx* ctx, float* ms);
+/* Writes a device buffer larger than L2 (flushes the L2 cache) on the stream. */
+cvr_status cvr_flush_l2(cvr_ctx* ctx);
+
+/* ---- host-side helpers (no GPU needed) ------------------------------------ */
+/* TransferFunction1D::BuildLinear over control points (transferfunction1d.cpp:319-358)
+ * followed by GenerateTexture_1D_RGBt / _RGBA; tables hold max_density+1 entries. */
+cvr_status cvr_tf_build_linear(int max_density, int n_rgb, const double* rgb_points /* r,g,b,iso */,
+                               int n_alpha, const double* alpha_points /* a,iso */,
+                               int extinction_input, float* rgbt_out, float* rgba_out);
+/* TransferFunction1D::GetExtN for every voxel value of a dtype (the SAT input). */
+cvr_status cvr_tf_ext_per_value(int max_density, int n_rgb, const double* rgb_points,
+                                int n_alpha, const double* alpha_points, int extinction_input,
+                                int dtype, double* out /* 256 or 65536 */);
+/* .tf1d reader (readtf1d, libs/volvis_utils/reader.cpp:744-814): returns control points. */
+cvr_status cvr_read_tf1d(const char* path, int* max_density, int* extinction_input,
+                         int* n_rgb, double* rgb_points, int max_rgb,
+                         int* n_alpha, double* alpha_points, int max_alpha);
+/* .raw / .syn reader header: dims and dtype from the file (readraw name convention
+ * "name.<bytes>.<W>x<H>x<D>.raw", reader.cpp:162-225; readsyn, reader.cpp:283-371). */
+cvr_status cvr_read_volume_info(const char* path, int dims[3], int* dtype, float spacing[3]);
+/* Reads the voxels into host_out (W*H*D*bytes). */
+cvr_status cvr_read_volume(const char* path, void* host_out, size_t out_bytes);
+/* ConeGaussianSampler::ComputeConeIntegrationSteps (conegaussiansampler.cpp:212-386). */
+cvr_status cvr_cone_sampler_build(float cone_half_angle_deg, int max_packing /* 0:1, 1:3, 2:7 */,
+                                  float covered_distance, float initial_step, float ui_weight,
+                                  double min_sigma, cvr_cone_table* out);
+/* GT kernel vectors (crtgtrenderer.cpp:131-187): one std::default_random_engine
+ * (libstdc++ minstd_rand0, seeded with 'seed'; the reference uses the default
+ * seed 1) draws the n_occ occlusion vectors and then the n_sdw shadow vectors. */
+cvr_status cvr_gt_kernel_vectors(int n_occ, float occ_aperture_deg, int n_sdw, float sdw_aperture_deg,
+                                 unsigned int seed, float* occ_xyz, float* sdw_xyz);
+
+/* Page-locked host memory for asynchronous copies (cudaHostAlloc / cudaFreeHost). */
+cvr_status cvr_host_alloc_pinned(size_t bytes, void** out);
+void cvr_host_free_pinned(void* p);
+
+/* Seeded synthetic volumes used by the benchmark configurations. */
+cvr_status cvr_synth_blobs(void* host_out, int w, int h, int d, int dtype, int n_blobs,
+                           uint64_t seed, float noise_max);
+cvr_status cvr_synth_value_noise(void* host_out, int w, int h, int d, int dtype, int octaves,
+                                 float lacunarity, float gain, int shells, uint64_t seed);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CVR_H */

@@ -1,0 +1,182 @@
+"""TEST INFRASTRUCTURE ONLY — Python binding of the CPU oracle (liboracle.so)
+and of the reference's own table builders (oracle/_ref/libcvr_ref.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+legs may use this package; the product (libcvr.so and its package) never
+imports it.  Parity status: the table builders are pinned against the
+reference's own C++ (see build_ref.py) and committed golden vectors; the
+marching loops are restatements of GLSL that cannot run on these machines.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from cpp_volume_rendering_gb300 import abi
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libcvr_ref.so"
+
+_lib = None
+_ref = None
+
+
+def build():
+    import importlib
+    return importlib.import_module("oracle.build").build()
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            build()
+        lib = C.CDLL(str(LIB))
+        P, I, D = C.c_void_p, C.c_int, C.c_double
+        sig = {
+            "oracle_create": (P, []),
+            "oracle_destroy": (None, [P]),
+            "oracle_set_volume": (I, [P, P, I, I, I, I, D, D, D]),
+            "oracle_set_tf": (I, [P, P, P, I]),
+            "oracle_build_sat": (I, [P, P, I]),
+            "oracle_get_sat": (I, [P, P]),
+            "oracle_sat_i64": (I, [P, I, I, I, I, P, P]),
+            "oracle_build_pyramid": (I, [P, C.POINTER(abi.PyramidParams)]),
+            "oracle_get_pyramid_level": (I, [P, I, I, P]),
+            "oracle_set_cone_tables": (I, [P, C.POINTER(abi.ConeTable), C.POINTER(abi.ConeTable)]),
+            "oracle_set_gt_kernels": (I, [P, P, I, P, I]),
+            "oracle_render": (I, [P, I, I, C.POINTER(abi.Camera), C.POINTER(abi.Light), P, I, I, I, I, P, P,
+                                  C.POINTER(C.c_uint64), I]),
+        }
+        for k, (r, a) in sig.items():
+            f = getattr(lib, k)
+            f.restype, f.argtypes = r, a
+        _lib = lib
+    return _lib
+
+
+def ref_available() -> bool:
+    if REF_LIB.exists():
+        return True
+    try:
+        import importlib
+        return importlib.import_module("oracle.build_ref").build() is not None
+    except Exception:
+        return False
+
+
+def load_ref():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise FileNotFoundError("reference pieces are not built (needs the reference checkout)")
+        _ref = C.CDLL(str(REF_LIB))
+    return _ref
+
+
+def _p(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Oracle:
+    """CPU renderer: FP64 (precision=64) is the parity oracle, FP32 the baseline."""
+
+    def __init__(self):
+        self.lib = load()
+        self.h = C.c_void_p(self.lib.oracle_create())
+
+    def __del__(self):
+        try:
+            self.lib.oracle_destroy(self.h)
+        except Exception:
+            pass
+
+    def _ck(self, r):
+        if r < 0:
+            raise RuntimeError(f"oracle error {r}")
+        return r
+
+    def set_volume(self, vol, spacing):
+        vol = np.ascontiguousarray(vol)
+        d, h, w = vol.shape
+        dt = abi.CVR_U8 if vol.dtype == np.uint8 else abi.CVR_U16
+        self._ck(self.lib.oracle_set_volume(self.h, _p(vol), w, h, d, dt, *[float(s) for s in spacing]))
+        self.vol = vol
+
+    def set_tf(self, rgbt, rgba):
+        rgbt = np.ascontiguousarray(rgbt, np.float32)
+        rgba = np.ascontiguousarray(rgba, np.float32)
+        self._ck(self.lib.oracle_set_tf(self.h, _p(rgbt), _p(rgba), len(rgbt)))
+
+    def build_sat(self, ext):
+        ext = np.ascontiguousarray(ext, np.float64)
+        self._ck(self.lib.oracle_build_sat(self.h, _p(ext), len(ext)))
+
+    def sat(self):
+        d, h, w = self.vol.shape
+        out = np.zeros((d + 2, h + 2, w + 2), np.float64)
+        self._ck(self.lib.oracle_get_sat(self.h, _p(out)))
+        return out
+
+    def build_pyramid(self, base_dims, sigma0, n_levels):
+        p = abi.PyramidParams()
+        p.base_dims[:] = list(base_dims)
+        p.sigma0 = sigma0
+        p.n_levels = n_levels
+        self.n_levels = self._ck(self.lib.oracle_build_pyramid(self.h, C.byref(p)))
+        self.base_dims = tuple(base_dims)
+        return self.n_levels
+
+    def pyramid_level(self, level, precision=64):
+        w, h, d = [max(1, b >> level) for b in self.base_dims]
+        out = np.zeros((d, h, w), np.float64)
+        self._ck(self.lib.oracle_get_pyramid_level(self.h, precision, level, _p(out)))
+        return out
+
+    def set_cone_tables(self, occ, sdw):
+        self._ck(self.lib.oracle_set_cone_tables(self.h, C.byref(occ), C.byref(sdw)))
+
+    def set_gt_kernels(self, occ, sdw):
+        occ = np.ascontiguousarray(occ, np.float32)
+        sdw = np.ascontiguousarray(sdw, np.float32)
+        self._ck(self.lib.oracle_set_gt_kernels(self.h, _p(occ), len(occ), _p(sdw), len(sdw)))
+
+    def render(self, method, cam, lt, params, w, h, precision=64, rows=None, threads=0):
+        """Returns (image rows [y0,y1) x W x 4 float64, per-pixel step counts, total steps)."""
+        import os
+        y0, y1 = rows if rows else (0, h)
+        out = np.zeros((y1 - y0, w, 4), np.float64)
+        counts = np.zeros((y1 - y0, w), np.uint32)
+        total = C.c_uint64()
+        threads = threads or os.cpu_count() or 1
+        self._ck(self.lib.oracle_render(self.h, precision, method, C.byref(cam), C.byref(lt) if lt else None,
+                                        C.c_void_p(C.addressof(params)), w, h, y0, y1, _p(out), _p(counts),
+                                        C.byref(total), threads))
+        return out, counts, total.value
+
+
+def sat_i64(vol, q):
+    vol = np.ascontiguousarray(vol)
+    d, h, w = vol.shape
+    dt = abi.CVR_U8 if vol.dtype == np.uint8 else abi.CVR_U16
+    q = np.ascontiguousarray(q, np.int64)
+    out = np.zeros((d + 2, h + 2, w + 2), np.int64)
+    load().oracle_sat_i64(_p(vol), w, h, d, dt, _p(q), _p(out))
+    return out
+
+
+def prepare(orc: Oracle, wl):
+    """Oracle-side Init() for a scene.Workload."""
+    rgbt, rgba = wl.tf.tables()
+    orc.set_volume(wl.volume, wl.spacing)
+    orc.set_tf(rgbt, rgba)
+    if wl.method == abi.EXTINCTION:
+        orc.build_sat(wl.tf.ext_per_value(wl.dtype))
+    if wl.method == abi.CONE_DOS:
+        orc.build_pyramid(wl.pyramid["base_dims"], wl.pyramid["sigma0"], wl.pyramid["n_levels"])
+        orc.set_cone_tables(*wl.cones)
+    if wl.method == abi.GROUND_TRUTH:
+        orc.set_gt_kernels(*wl.gt)

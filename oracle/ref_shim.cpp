@@ -1,0 +1,138 @@
+// ref_shim.cpp — TEST INFRASTRUCTURE ONLY.  Compiled by oracle/build_ref.py
+// together with the reference's own, unmodified C++ sources (read in place
+// from the reference checkout; nothing is copied) into oracle/_ref/.  It
+// exposes the reference's CPU table builders through a C interface so the
+// oracle and the product's host code can be pinned against them:
+//   * vis::SummedAreaTable3D<double>::BuildSAT   (libs/vis_utils/summedareatable.h:218-280)
+//   * vis::TransferFunction1D::Get / GetExtN     (libs/volvis_utils/transferfunction1d.cpp:132-197)
+//   * ConeGaussianSampler::ComputeConeIntegrationSteps
+//                                                (cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp:212-386)
+//   * RodriguesRotation                          (libs/math_utils/utils.cpp:149-156)
+// The GL texture classes those headers mention are stubbed below; no GL code
+// runs.  Private members of ConeGaussianSampler are read through the access
+// macro below (the interval list feeds the shader table but has no getter).
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include <glm/gtc/constants.hpp>
+#include <vis_utils/summedareatable.h>
+#include <volvis_utils/transferfunction1d.h>
+#include <math_utils/utils.h>
+#define private public
+#include "structured/rc1pdosct/conegaussiansampler.h"
+#undef private
+
+// Stubs for the GL texture wrappers referenced by the reference headers.
+namespace gl {
+Texture1D::Texture1D(unsigned int) {}
+Texture1D::~Texture1D() {}
+void Texture1D::GenerateTexture(GLint, GLint, GLint) {}
+bool Texture1D::SetData(GLvoid*, GLint, GLenum, GLenum) { return true; }
+GLuint Texture1D::GetTextureID() { return 0; }
+unsigned int Texture1D::GetLength() { return 0; }
+void ExitOnGLError(const char*) {}
+}  // namespace gl
+
+namespace {
+vis::TransferFunction1D* make_tf(int max_density, int n_rgb, const double* rgb, int n_alpha, const double* alpha,
+                                 int ext_input) {
+  vis::TransferFunction1D* tf = new vis::TransferFunction1D(max_density);
+  tf->SetExtinctionCoefficientInput(ext_input != 0);
+  for (int i = 0; i < n_rgb; ++i)
+    tf->AddRGBControlPoint(vis::TransferControlPoint(rgb[4 * i], rgb[4 * i + 1], rgb[4 * i + 2], (int)rgb[4 * i + 3]));
+  for (int i = 0; i < n_alpha; ++i) tf->AddAlphaControlPoint(vis::TransferControlPoint(alpha[2 * i], (int)alpha[2 * i + 1]));
+  return tf;
+}
+}  // namespace
+
+extern "C" {
+
+// SAT of a full (W x H x D) grid given cell values (x fastest).
+int ref_sat_build(int w, int h, int d, const double* cells, double* out) {
+  vis::SummedAreaTable3D<double> sat(w, h, d);
+  for (int z = 0; z < d; ++z)
+    for (int y = 0; y < h; ++y)
+      for (int x = 0; x < w; ++x) sat.SetValue(cells[(size_t)x + (size_t)w * ((size_t)y + (size_t)h * z)], x, y, z);
+  sat.BuildSAT();
+  std::memcpy(out, sat.GetData(), sizeof(double) * (size_t)w * h * d);
+  return 0;
+}
+
+// GenerateTexture_1D_RGBt / _RGBA contents, reconstructed from Get(i) (which
+// returns the float-rounded table entry at integer i) and the reference's
+// opacity <-> extinction conversions, exactly as those two functions do.
+int ref_tf_tables(int max_density, int n_rgb, const double* rgb, int n_alpha, const double* alpha, int ext_input,
+                  float* rgbt, float* rgba) {
+  vis::TransferFunction1D* tf = make_tf(max_density, n_rgb, rgb, n_alpha, alpha, ext_input);
+  for (int i = 0; i <= max_density; ++i) {
+    glm::vec4 v = tf->Get((double)i);
+    for (int c = 0; c < 3; ++c) { rgbt[4 * i + c] = v[c]; rgba[4 * i + c] = v[c]; }
+    float a = v.w;
+    rgbt[4 * i + 3] = ext_input ? a : (float)tf->MaterialOpacityToExtinction(a);
+    rgba[4 * i + 3] = ext_input ? (float)tf->ExtinctionToMaterialOpacity(a) : a;
+  }
+  delete tf;
+  return 0;
+}
+
+// tf->GetExtN(vol->GetNormalizedSample(...)) for every u8 / u16 value.
+int ref_tf_ext_per_value(int max_density, int n_rgb, const double* rgb, int n_alpha, const double* alpha,
+                         int ext_input, int bytes_per_voxel, double* out) {
+  vis::TransferFunction1D* tf = make_tf(max_density, n_rgb, rgb, n_alpha, alpha, ext_input);
+  int n = bytes_per_voxel == 1 ? 256 : 65536;
+  double denom = bytes_per_voxel == 1 ? (256.0 - 1.0) : (65536.0 - 1.0);
+  for (int v = 0; v < n; ++v) out[v] = (double)tf->GetExtN((double)v / denom);
+  delete tf;
+  return 0;
+}
+
+// ConeGaussianSampler tables: sections as (interval distance, mip level,
+// d_integral, amplitude) in double, counts, axes, adjacent weight.
+int ref_cone_sampler(float half_angle, int packing, float covered, float initial_step, double min_sigma,
+                     int max_sections, double* sections, int* counts, float* axes, double* w7) {
+  ConeGaussianSampler s;
+  s.SetConeHalfAngle(half_angle);
+  s.SetMaxGaussianPacking(packing);
+  s.covered_distance = covered;  // the setter clamps to >= 10 world units
+  s.SetInitialStep(initial_step);
+  s.ComputeConeIntegrationSteps(min_sigma);
+  int n = (int)s.data_cone_sectionsinfo.size();
+  if (n > max_sections) return -1;
+  for (int i = 0; i < n; ++i) {
+    sections[4 * i + 0] = s.data_cone_intervalsinfo[i].s_distance;
+    sections[4 * i + 1] = s.data_cone_sectionsinfo[i].mip_map_level;
+    sections[4 * i + 2] = s.data_cone_sectionsinfo[i].d_integral;
+    sections[4 * i + 3] = s.data_cone_sectionsinfo[i].amplitude;
+  }
+  counts[0] = s.gaussian_samples_1; counts[1] = s.gaussian_samples_3; counts[2] = s.gaussian_samples_7;
+  for (int i = 0; i < 3; ++i) { axes[3 * i] = s.ray3_axis[i].x; axes[3 * i + 1] = s.ray3_axis[i].y; axes[3 * i + 2] = s.ray3_axis[i].z; }
+  for (int i = 0; i < 7; ++i) { axes[9 + 3 * i] = s.ray7_axis[i].x; axes[9 + 3 * i + 1] = s.ray7_axis[i].y; axes[9 + 3 * i + 2] = s.ray7_axis[i].z; }
+  *w7 = s.GetRay7AdjacentWeight();
+  return n;
+}
+
+// The GT kernel-vector loop of crtgtrenderer.cpp:131-187 written against the
+// reference's RodriguesRotation (that renderer's Update() itself needs GL).
+int ref_gt_vectors(int n_occ, float occ_ap, int n_sdw, float sdw_ap, unsigned seed, float* occ, float* sdw) {
+  std::default_random_engine generator(seed);
+  std::uniform_real_distribution<float> distribution(0.0, 1.0);
+  glm::vec3 gtray(0, 0, 1);
+  for (int i = 0; i < n_occ; ++i) {
+    float theta = distribution(generator) * (glm::pi<float>() * (occ_ap / 180.f));
+    float phi = distribution(generator) * (glm::pi<float>() * (360.f / 180.f));
+    glm::vec3 v = RodriguesRotation(gtray, theta, glm::vec3(0, 1, 0));
+    v = RodriguesRotation(v, phi, gtray);
+    occ[3 * i] = v.x; occ[3 * i + 1] = v.y; occ[3 * i + 2] = v.z;
+  }
+  for (int i = 0; i < n_sdw; ++i) {
+    float theta = distribution(generator) * (glm::pi<float>() * (sdw_ap / 180.f));
+    float phi = distribution(generator) * (glm::pi<float>() * (360.f / 180.f));
+    glm::vec3 v = RodriguesRotation(gtray, theta, glm::vec3(0, 1, 0));
+    v = RodriguesRotation(v, phi, gtray);
+    sdw[3 * i] = v.x; sdw[3 * i + 1] = v.y; sdw[3 * i + 2] = v.z;
+  }
+  return 0;
+}
+
+}  // extern "C"

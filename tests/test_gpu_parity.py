@@ -1,0 +1,185 @@
+"""GPU parity: every CUDA path through the C ABI against the CPU oracle.
+
+Tolerances (stated by the specification of this project): images within
+max per-channel |error| <= 1/255 and PSNR >= 50 dB of the FP64 oracle; the
+extinction SAT bit-exact against the oracle's integer SAT and within relative
+error 1e-5 of the reference's FP64 builder; pyramid levels within 1e-4
+relative (FP32 sums of 343 taps).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from cpp_volume_rendering_gb300 import abi, scene
+
+pytestmark = pytest.mark.gpu
+
+MAX_ABS = 1.0 / 255.0
+MIN_PSNR = 50.0
+
+
+def psnr(a, b):
+    mse = float(np.mean((np.asarray(a, np.float64) - np.asarray(b, np.float64)) ** 2))
+    return float("inf") if mse == 0 else 10.0 * math.log10(1.0 / mse)
+
+
+def compare(img_gpu, img_ref, what):
+    err = np.abs(img_gpu.astype(np.float64) - img_ref)
+    p = psnr(img_gpu, img_ref)
+    assert np.isfinite(img_gpu).all(), f"{what}: non-finite pixels"
+    assert err.max() <= MAX_ABS, f"{what}: max abs {err.max():.3e} at {np.unravel_index(err.argmax(), err.shape)}"
+    assert p >= MIN_PSNR, f"{what}: PSNR {p:.1f} dB"
+    return err.max(), p
+
+
+def run_both(ctx, wl, rows=None):
+    scene.prepare(ctx, wl)
+    img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+    orc = oracle.Oracle()
+    oracle.prepare(orc, wl)
+    ref, counts, total = orc.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height, precision=64,
+                                    rows=rows)
+    if rows:
+        img = img[rows[0]:rows[1]]
+    return img, st, ref, total
+
+
+@pytest.mark.parametrize("name,n,image", [("plain", 64, 256), ("plain", 33, 61), ("extinction", 40, 96),
+                                          ("cone", 40, 80), ("ground_truth", 32, 64)])
+def test_workload_parity(ctx, name, n, image):
+    wl = scene.workload(name, n=n, image=image)
+    img, st, ref, total = run_both(ctx, wl)
+    compare(img, ref, f"{name} n={n}")
+    # the primary-ray step count is the Msamples numerator: GPU and oracle must agree
+    assert abs(int(st.samples) - int(total)) <= max(2, total // 2000), (st.samples, total)
+
+
+def test_plain_full_config_parity(ctx):
+    """The plain workload at its benchmark size (64^3 -> 256^2) in full."""
+    wl = scene.workload("plain")
+    img, st, ref, total = run_both(ctx, wl)
+    compare(img, ref, "plain 64^3 256^2")
+
+
+def test_extinction_u8_point_light_and_shells(ctx):
+    """u8 volume, point-light shadow (TypeOfShadow 0), the reference's
+    uniform AO shells (radius R*(i+1), K = 5)."""
+    vol = scene.synth_blobs(36, 30, 28, abi.CVR_U8, 6, seed=11)
+    wl = scene.workload("extinction", n=8, image=8)
+    wl.volume = vol
+    lp = (50.0, 70.0, -40.0)
+    wl.light = scene.light(abi.LIGHT_POINT, position=lp)
+    wl.params = scene.ext_params(scene.default_step(wl.spacing), wl.diagonal, ao_radii=(1, 2, 3, 4, 5),
+                                 shadow_type=0)
+    wl.cam = scene.camera(scene.orbit_eye(110.0, 200.0, -30.0), fovy=35.0)
+    wl.width, wl.height = 72, 56
+    img, st, ref, total = run_both(ctx, wl)
+    compare(img, ref, "extinction u8 point light")
+
+
+def test_extinction_anisotropic_spacing_and_aspect(ctx):
+    vol = scene.synth_value_noise(40, 24, 32, abi.CVR_U16, seed=9)
+    wl = scene.workload("extinction", n=8, image=8)
+    wl.volume = vol
+    wl.spacing = (1.0, 1.5, 0.75)
+    wl.params = scene.ext_params(scene.default_step(wl.spacing), wl.diagonal, ao_radii=(2, 4))
+    wl.cam = scene.camera(scene.orbit_eye(120.0, 60.0, 35.0), fovy=40.0)
+    wl.width, wl.height = 80, 48
+    img, st, ref, total = run_both(ctx, wl)
+    compare(img, ref, "extinction anisotropic")
+
+
+def test_sat_bit_exact_and_relative_error(ctx):
+    vol = scene.synth_value_noise(48, 40, 36, abi.CVR_U16, seed=4)
+    ext = scene.BENCH_TF.ext_per_value(abi.CVR_U16)
+    ctx.set_volume(vol, (1.0, 1.0, 1.0))
+    ctx.set_transfer_function(scene.BENCH_TF)
+    ctx.build_sat(ext)
+    sat, F = ctx.sat()
+    q = np.floor(ext * 2.0 ** F + 0.5).astype(np.int64)
+    assert np.array_equal(sat, oracle.sat_i64(vol, q))
+    orc = oracle.Oracle()
+    orc.set_volume(vol, (1, 1, 1))
+    orc.build_sat(ext)
+    ref = orc.sat()
+    got = sat.astype(np.float64) * 2.0 ** -F
+    big = ref > 1e-3 * ref.max()
+    rel = np.abs(got - ref)[big] / ref[big]
+    assert rel.max() <= 1e-5, rel.max()
+    assert np.abs(got - ref).max() / ref.max() <= 1e-9
+
+
+def test_pyramid_levels_match_oracle(ctx):
+    wl = scene.workload("cone", n=32, image=8)
+    scene.prepare(ctx, wl)
+    levels = ctx.pyramid()
+    orc = oracle.Oracle()
+    oracle.prepare(orc, wl)
+    assert len(levels) == orc.n_levels == 5
+    for l, lev in enumerate(levels):
+        ref = orc.pyramid_level(l, 64)
+        assert lev.shape == ref.shape
+        err = np.abs(lev - ref) / np.maximum(np.abs(ref), 1e-3)
+        assert err.max() <= 1e-4, (l, err.max())
+
+
+def test_rays_missing_the_volume_are_zero(ctx):
+    wl = scene.workload("plain", n=16, image=32)
+    wl.cam = scene.camera((0.0, 0.0, 3.0), center=(0.0, 0.0, 6.0))  # looking away
+    scene.prepare(ctx, wl)
+    img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, 32, 32)
+    assert (img == 0).all() and st.samples == 0
+
+
+def test_camera_inside_volume_and_tiny_images(ctx):
+    wl = scene.workload("plain", n=24, image=8)
+    wl.cam = scene.camera((0.05, -0.1, 0.12), center=(0.4, 0.3, -0.2), fovy=70.0)
+    for w, h in [(1, 1), (7, 3), (37, 23)]:
+        wl.width, wl.height = w, h
+        img, st, ref, total = run_both(ctx, wl)
+        compare(img, ref, f"inside camera {w}x{h}")
+
+
+def test_single_voxel_and_flat_volumes(ctx):
+    for shape in [(1, 1, 1), (1, 9, 13), (17, 1, 5)]:
+        vol = (np.arange(np.prod(shape)) * 37 % 256).astype(np.uint8).reshape(shape)
+        wl = scene.workload("plain", n=4, image=8)
+        wl.volume = vol
+        wl.spacing = (0.1, 0.1, 0.1)
+        wl.params.step_size = 0.05
+        wl.cam = scene.camera((1.0, 0.7, 2.0), fovy=30.0)
+        wl.width, wl.height = 24, 24
+        img, st, ref, total = run_both(ctx, wl)
+        compare(img, ref, f"volume {shape}")
+
+
+def test_errors_are_reported_not_crashing(ctx):
+    import ctypes as C
+    lib = abi.load()
+    img = np.zeros((4, 4, 4), np.float32)
+    p = abi.PlainParams()
+    p.step_size = 0.0
+    cam = scene.camera((0, 0, 3))
+    scene.prepare(ctx, scene.workload("plain", n=8, image=4))
+    r = lib.cvr_render_host(ctx.h, abi.PLAIN, C.byref(cam), None, C.byref(p), C.sizeof(p), abi.fptr(img), 4, 4, None)
+    assert r == abi.CVR_ERR_INVALID_ARG
+    p.step_size = 0.01
+    r = lib.cvr_render_host(ctx.h, 99, C.byref(cam), None, C.byref(p), C.sizeof(p), abi.fptr(img), 4, 4, None)
+    assert r == abi.CVR_ERR_INVALID_ARG
+    # method tables missing -> NOT_READY, context stays usable
+    fresh = scene.Context(0)
+    fresh.set_volume(np.zeros((4, 4, 4), np.uint8))
+    fresh.set_transfer_function(scene.BENCH_TF)
+    ep = scene.ext_params(0.5, 7.0)
+    r = lib.cvr_render_host(fresh.h, abi.EXTINCTION, C.byref(cam), None, C.byref(ep), C.sizeof(ep), abi.fptr(img),
+                            4, 4, None)
+    assert r == abi.CVR_ERR_NOT_READY
+    r = lib.cvr_render_host(fresh.h, abi.PLAIN, C.byref(cam), None, C.byref(p), C.sizeof(p), abi.fptr(img), 4, 4, None)
+    assert r == abi.CVR_OK
+    fresh.close()
+    empty = scene.Context(0)
+    r = lib.cvr_render_host(empty.h, abi.PLAIN, C.byref(cam), None, C.byref(p), C.sizeof(p), abi.fptr(img), 4, 4, None)
+    assert r == abi.CVR_ERR_NO_VOLUME
+    empty.close()
