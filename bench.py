@@ -190,7 +190,7 @@ def run_reference(args):
     from cpp_volume_rendering_gb300 import scene
     import oracle
     oracle.build()
-    wl = scene.workload(args.workload)
+    wl = scene.workload(args.workload, n=args.size, image=args.image)
     threads = os.cpu_count() or 1
     orc = oracle.Oracle()
     oracle.prepare(orc, wl)
@@ -259,7 +259,7 @@ def run_ours(args):
     from cpp_volume_rendering_gb300 import abi, build, scene
     build.build()
     lib = abi.load()
-    wl = scene.workload(args.workload)
+    wl = scene.workload(args.workload, n=args.size, image=args.image)
     ctx = scene.Context(local)
     scene.prepare(ctx, wl)
     out = C.POINTER(C.c_float)()
@@ -371,6 +371,8 @@ def main():
     ap.add_argument("--quick", action="store_true", help="skip the per-renderer table")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--size", type=int, default=None, help="volume side override (profiling / small cases)")
+    ap.add_argument("--image", type=int, default=None, help="image side override (profiling / small cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -115,6 +115,7 @@ SIGNATURES = {
     "cvr_render_host": (_I, [_P, _I, C.POINTER(Camera), C.POINTER(Light), _P, C.c_size_t, _FP, _I, _I,
                              C.POINTER(FrameStats)]),
     "cvr_get_frame_buffer": (_I, [_P, _I, _I, C.POINTER(_FP)]),
+    "cvr_download_frame": (_I, [_P, _P, _I, _I, _FP]),
     "cvr_timer_start": (_I, [_P]),
     "cvr_timer_stop": (_I, [_P, _FP]),
     "cvr_flush_l2": (_I, [_P]),

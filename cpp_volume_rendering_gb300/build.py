@@ -18,6 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libcvr.so"
+TOOL = BUILD / "cvr_headless"
 
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CXX = os.environ.get("CXX", "g++")
@@ -74,6 +75,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     if tasks or _stale(LIB, objs):
         _run([NVCC] + ARCH + ["-shared", "-o", str(LIB)] + [str(o) for o in objs] +
              ["-Xcompiler", "-fopenmp", "-lgomp"])
+    # the headless driver links the library through an rpath next to it
+    tool_src = CSRC / "tools" / "cvr_headless.cpp"
+    if _stale(TOOL, [tool_src, LIB] + headers):
+        _run([CXX] + CXX_FLAGS + [str(tool_src), "-o", str(TOOL), f"-L{BUILD}", "-lcvr",
+                                  "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

@@ -553,6 +553,14 @@ cvr_status cvr_get_frame_buffer(cvr_ctx* c, int w, int h, float** dev_out) {
   return CVR_OK;
 }
 
+cvr_status cvr_download_frame(cvr_ctx* c, const float* dev, int w, int h, float* host) {
+  if (!c || !dev || !host || w <= 0 || h <= 0) return fail(c, CVR_ERR_INVALID_ARG, "cvr_download_frame: bad arguments");
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpyAsync(host, dev, (size_t)w * h * sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
 cvr_status cvr_timer_start(cvr_ctx* c) {
   if (!c) return CVR_ERR_INVALID_ARG;
   CK(c, cudaEventRecord(c->ev[0], c->stream));

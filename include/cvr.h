@@ -243,6 +243,9 @@ cvr_status cvr_render_host(cvr_ctx* ctx, int method, const cvr_camera* camera, c
  * headless counterpart of GetScreenTextureID, volrenderbase.h:73-75).  The
  * pointer stays valid until the next call with a larger size or cvr_destroy. */
 cvr_status cvr_get_frame_buffer(cvr_ctx* ctx, int w, int h, float** dev_out);
+/* Copies w*h RGBA32F pixels of a device frame (e.g. the frame buffer above)
+ * to host memory; synchronous (the glGetTexImage readback of the reference). */
+cvr_status cvr_download_frame(cvr_ctx* ctx, const float* dev_frame, int w, int h, float* host_out);
 
 /* ---- device timing on the context stream --------------------------------- */
 cvr_status cvr_timer_start(cvr_ctx* ctx);

@@ -127,10 +127,23 @@ def test_pyramid_levels_match_oracle(ctx):
 
 def test_rays_missing_the_volume_are_zero(ctx):
     wl = scene.workload("plain", n=16, image=32)
-    wl.cam = scene.camera((0.0, 0.0, 3.0), center=(0.0, 0.0, 6.0))  # looking away
+    # camera beside the volume looking parallel to it: every slab test fails
+    wl.cam = scene.camera((3.0, 0.0, 0.0), center=(3.0, 0.0, 5.0), fovy=10.0)
     scene.prepare(ctx, wl)
     img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, 32, 32)
     assert (img == 0).all() and st.samples == 0
+
+
+def test_box_behind_camera_matches_reference_quirk(ctx):
+    """RayAABBIntersection tests tfar > tnear before clamping tnear to 0
+    (ray_bbox_intersection.comp:44-46), so a box entirely behind the camera
+    counts as hit and the ray marches |tfar| forward through clamp-to-edge
+    samples.  The GPU path keeps that behaviour; it must agree with the oracle."""
+    wl = scene.workload("plain", n=16, image=32)
+    wl.cam = scene.camera((0.0, 0.0, 3.0), center=(0.0, 0.0, 6.0))  # looking away
+    img, st, ref, total = run_both(ctx, wl)
+    compare(img, ref, "box behind camera")
+    assert st.samples == total > 0
 
 
 def test_camera_inside_volume_and_tiny_images(ctx):

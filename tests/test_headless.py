@@ -1,0 +1,75 @@
+"""The headless RenderingManager driver (cvr_headless): data loading and error
+reporting run on the host before any device call, so they are tested on CPU;
+the rendering path is compared with the C ABI render on the GPU."""
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from cpp_volume_rendering_gb300 import abi, build, scene
+
+TOOL = build.TOOL
+
+
+@pytest.fixture(scope="module")
+def data(tmp_path_factory, lib):
+    d = tmp_path_factory.mktemp("headless")
+    vol = scene.synth_blobs(24, 20, 16, abi.CVR_U8, 5, seed=21)
+    vp = d / "blobs.1.24x20x16.raw"
+    vol.tofile(vp)
+    tp = d / "ramp.tf1d"
+    tp.write_text("linear\n0\n4\n0.2 0.3 0.9 0\n0.3 0.8 0.4 80\n0.9 0.7 0.2 160\n1.0 0.95 0.9 255\n"
+                  "4\n0.0 0\n0.05 80\n0.4 160\n0.9 255\n")
+    cp = d / "cameras"
+    cp.write_text("Front\nARCBALL\n 10.0 20.0 60.0\n 0.0 0.0 0.0\n 0.0 1.0 0.0\n"
+                  "Side\nARCBALL\n-55.0 10.0 5.0\n 0.0 0.0 0.0\n 0.0 1.0 0.0\n")
+    lp = d / "lights"
+    lp.write_text("One light\n1\n-40.0 60.0 30.0\n-0.5 0.75 0.4\n0.0 1.0 0.0\n1.0 0.0 0.0\n20\n")
+    return dict(vol=vol, vp=vp, tp=tp, cp=cp, lp=lp, dir=d)
+
+
+def run(*args):
+    return subprocess.run([str(TOOL), *map(str, args)], capture_output=True, text=True, timeout=300)
+
+
+def test_usage_errors(data):
+    assert run().returncode == 1
+    assert run("--volume", data["vp"]).returncode == 1
+    assert run("--bogus").returncode == 1
+
+
+def test_data_errors_before_any_device_call(data, tmp_path):
+    r = run("--volume", tmp_path / "missing.1.4x4x4.raw", "--tf", data["tp"], "--renderer", "s_1rc")
+    assert r.returncode == 2 and "opening .raw" in r.stderr
+    short = tmp_path / "short.1.8x8x8.raw"
+    short.write_bytes(b"\1" * 100)
+    r = run("--volume", short, "--tf", data["tp"], "--renderer", "s_1rc")
+    assert r.returncode == 2 and "short .raw" in r.stderr
+    badtf = tmp_path / "bad.tf1d"
+    badtf.write_text("linear\n0\n3\n1 1 1 0\n")
+    r = run("--volume", data["vp"], "--tf", badtf, "--renderer", "s_1rc")
+    assert r.returncode == 2 and "tf1d" in r.stderr
+    r = run("--volume", data["vp"], "--tf", data["tp"], "--renderer", "s_1rc", "--cameras", data["cp"],
+            "--camera-index", "7")
+    assert r.returncode == 2 and "camera" in r.stderr
+    badl = tmp_path / "lights"
+    badl.write_text("Broken\n2\n1 2 3\n")
+    r = run("--volume", data["vp"], "--tf", data["tp"], "--renderer", "s_1rc", "--lights", badl)
+    assert r.returncode == 2 and "light" in r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("abbr,method", [("s_1rc", abi.PLAIN), ("s_1pebs", abi.EXTINCTION),
+                                         ("s_1pdosct", abi.CONE_DOS), ("s_1pcrtgt", abi.GROUND_TRUTH)])
+def test_headless_frames(data, abbr, method, tmp_path):
+    out = tmp_path / f"{abbr}.pfm"
+    r = run("--volume", data["vp"], "--tf", data["tp"], "--renderer", abbr, "--width", "40", "--height", "32",
+            "--cameras", data["cp"], "--camera-index", "1", "--lights", data["lp"], "--out", out)
+    assert r.returncode == 0, r.stderr
+    assert f"renderer={abbr}" in r.stdout
+    raw = out.read_bytes()
+    header_end = raw.index(b"-1.0\n") + 5
+    assert raw[:header_end].split()[:3] == [b"PF", b"40", b"32"]
+    img = np.frombuffer(raw[header_end:], np.float32).reshape(32, 40, 3)
+    assert np.isfinite(img).all() and img.max() > 0.0
