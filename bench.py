@@ -266,6 +266,12 @@ def run_ours(args):
     abi.check(lib.cvr_get_frame_buffer(ctx.h, wl.width, wl.height, C.byref(out)), ctx.h)
     out_ptr = C.cast(out, C.c_void_p)
     params = wl.params
+    # autotuner (part of set-up, outside the timed region): tile shape x register variant
+    tw, th, tv, tms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+    abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
+                               C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
+                               C.byref(tms)), ctx.h)
+    tuning = {"tile": [tw.value, th.value], "variant": tv.value, "autotune_ms": tms.value}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),
@@ -354,7 +360,7 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value noise / Gaussian blobs)",
         "config": {"workload": WORKLOAD_DESC[args.workload], "image": [wl.width, wl.height],
                    "volume": list(wl.dims), "l2": "flushed between timed steps (cvr_flush_l2, outside the events)",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU", "tuning": tuning},
         "fps": 1000.0 / ms_per_step,
         "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,

@@ -114,6 +114,10 @@ SIGNATURES = {
                         C.POINTER(FrameStats)]),
     "cvr_render_host": (_I, [_P, _I, C.POINTER(Camera), C.POINTER(Light), _P, C.c_size_t, _FP, _I, _I,
                              C.POINTER(FrameStats)]),
+    "cvr_set_tuning": (_I, [_P, _I, _I, _I]),
+    "cvr_get_tuning": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "cvr_autotune": (_I, [_P, _I, C.POINTER(Camera), C.POINTER(Light), _P, C.c_size_t, _I, _I, _I,
+                          C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _FP]),
     "cvr_get_frame_buffer": (_I, [_P, _I, _I, C.POINTER(_FP)]),
     "cvr_download_frame": (_I, [_P, _P, _I, _I, _FP]),
     "cvr_timer_start": (_I, [_P]),

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -58,7 +59,8 @@ struct cvr_ctx {
   void* d_flush = nullptr;
   size_t flush_bytes = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-  int tile_w = 16, tile_h = 8;
+  int tile_w = 16, tile_h = 8, variant = 0;
+  std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
 };
 
 namespace {
@@ -124,6 +126,85 @@ CameraView camera_view(const cvr_camera* cam, int w, int h) {
 }
 
 bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+// The boxes ConeZAxis / ConeYAxis / ConeXAxis (ebs_ray_bbox_marching.comp:190-430)
+// walk for a fixed cone direction, evaluated once per frame in double
+// precision.  Returns false when the walk has more boxes than the table holds
+// (the kernel then evaluates the geometry per sample).
+bool build_shadow_table(const cvr_ext_params* p, const float fwd[3], float3 spacing, float3 grid, ShadowBoxTable* t) {
+  double c[3] = {fwd[0], fwd[1], fwd[2]};
+  double n = std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+  for (double& v : c) v /= n;
+  double a[3] = {std::fabs(c[0]), std::fabs(c[1]), std::fabs(c[2])};
+  int ax = (a[2] > a[0] && a[2] > a[1]) ? 2 : (a[1] > a[0] ? 1 : 0);
+  const double ang = p->sdw_cone_angle_rad;
+  const double p_cs = std::cos(ang), p_sn = std::sin(ang), n_cs = std::cos(-ang), n_sn = std::sin(-ang);
+  auto nrm = [](double x, double y, double z, double* o) {
+    double l = std::sqrt(x * x + y * y + z * z);
+    o[0] = x / l; o[1] = y / l; o[2] = z / l;
+  };
+  double pa1[3], pa2[3], pb1[3], pb2[3], q1[3], q2[3];
+  int sa, sb;
+  if (ax == 2) {  // ConeZAxis: secondary axes x (proj_x) and y (proj_y)
+    sa = 0; sb = 1;
+    nrm(0, c[1], c[2], q1);  // proj_y
+    nrm(c[0], 0, c[2], q2);  // proj_x
+    nrm(q2[0] * n_cs - q2[2] * n_sn, 0, q2[0] * n_sn + q2[2] * n_cs, pa1);
+    nrm(q2[0] * p_cs - q2[2] * p_sn, 0, q2[0] * p_sn + q2[2] * p_cs, pa2);
+    nrm(0, q1[1] * n_cs - q1[2] * n_sn, q1[1] * n_sn + q1[2] * n_cs, pb1);
+    nrm(0, q1[1] * p_cs - q1[2] * p_sn, q1[1] * p_sn + q1[2] * p_cs, pb2);
+  } else if (ax == 1) {  // ConeYAxis: secondary axes x (proj_x) and z (proj_z)
+    sa = 0; sb = 2;
+    nrm(c[0], c[1], 0, q1);  // proj_x
+    nrm(0, c[1], c[2], q2);  // proj_z
+    nrm(q1[0] * n_cs - q1[1] * n_sn, q1[0] * n_sn + q1[1] * n_cs, 0, pa1);
+    nrm(q1[0] * p_cs - q1[1] * p_sn, q1[0] * p_sn + q1[1] * p_cs, 0, pa2);
+    nrm(0, q2[2] * n_sn + q2[1] * n_cs, q2[2] * n_cs - q2[1] * n_sn, pb1);
+    nrm(0, q2[2] * p_sn + q2[1] * p_cs, q2[2] * p_cs - q2[1] * p_sn, pb2);
+  } else {  // ConeXAxis: secondary axes y (proj_y) and z (proj_z)
+    sa = 1; sb = 2;
+    nrm(c[0], c[1], 0, q1);  // proj_y
+    nrm(c[0], 0, c[2], q2);  // proj_z
+    nrm(q1[1] * n_sn + q1[0] * n_cs, q1[1] * n_cs - q1[0] * n_sn, 0, pa1);
+    nrm(q1[1] * p_sn + q1[0] * p_cs, q1[1] * p_cs - q1[0] * p_sn, 0, pa2);
+    nrm(q2[2] * n_sn + q2[0] * n_cs, 0, q2[2] * n_cs - q2[0] * n_sn, pb1);
+    nrm(q2[2] * p_sn + q2[0] * p_cs, 0, q2[2] * p_cs - q2[0] * p_sn, pb2);
+  }
+  const double sc[3] = {spacing.x, spacing.y, spacing.z};
+  const double gr[3] = {grid.x, grid.y, grid.z};
+  const double signal = c[ax] < 0.0 ? -1.0 : 1.0;
+  const double iw = (double)p->sdw_sample_interval * signal * sc[ax];
+  double mp = (double)p->sdw_initial_step * signal * sc[ax];
+  int k = 0;
+  while ((mp / c[ax]) < (double)p->sdw_max_distance) {
+    if (k == CVR_MAX_SDW_BOXES) return false;
+    double mean = std::fabs(mp + iw * 0.5);
+    double a1 = pa1[sa] * (mean / std::fabs(pa1[ax])), a2 = pa2[sa] * (mean / std::fabs(pa2[ax]));
+    double b1 = pb1[sb] * (mean / std::fabs(pb1[ax])), b2 = pb2[sb] * (mean / std::fabs(pb2[ax]));
+    double lo_a = std::min(a1, a2), hi_a = std::max(a1, a2);
+    double lo_b = std::min(b1, b2), hi_b = std::max(b1, b2);
+    double ad = std::fabs(hi_a - lo_a), bd = std::fabs(hi_b - lo_b);
+    double as = (std::ceil(ad / sc[sa]) - (ad / sc[sa])) * 0.5;
+    double bs = (std::ceil(bd / sc[sb]) - (bd / sc[sb])) * 0.5;
+    lo_a -= as * sc[sa]; hi_a += as * sc[sa];
+    lo_b -= bs * sc[sb]; hi_b += bs * sc[sb];
+    double lo[3], hi[3];
+    lo[ax] = std::min(mp, mp + iw); hi[ax] = std::max(mp, mp + iw);
+    lo[sa] = lo_a; hi[sa] = hi_a; lo[sb] = lo_b; hi[sb] = hi_b;
+    double volq = (std::fabs(hi[0] - lo[0]) / sc[0]) * (std::fabs(hi[1] - lo[1]) / sc[1]) *
+                  (std::fabs(hi[2] - lo[2]) / sc[2]);
+    t->lo[k] = make_float4((float)lo[0], (float)lo[1], (float)lo[2], (float)mp);
+    t->hi[k] = make_float4((float)hi[0], (float)hi[1], (float)hi[2], (float)((double)p->sdw_ui_weight / volq));
+    mp = mp + iw;
+    ++k;
+  }
+  t->n = k;
+  t->axis = ax;
+  t->interval = (float)iw;
+  t->vmin = (float)(sc[ax] * 0.5);
+  t->vmax = (float)(gr[ax] - sc[ax] * 0.5);
+  return true;
+}
 
 }  // namespace
 
@@ -413,6 +494,7 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
   f.tf_n = c->tf_n;
   f.W = w; f.H = h;
   f.tile_w = c->tile_w; f.tile_h = c->tile_h;
+  f.variant = c->variant;
   f.out = reinterpret_cast<float4*>(out);
   f.counts = counts;
   f.stats = c->d_stats;
@@ -464,7 +546,13 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
       a.shadow_type = p->shadow_type;
       a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
       a.ka = p->ka; a.kd = p->kd;
-      e = launch_extinction(f, a, c->stream);
+      const ShadowBoxTable* table = nullptr;
+      if (p->apply_shadow && p->shadow_type == 1) {
+        if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
+        if (build_shadow_table(p, light->forward, f.vol.spacing, f.vol.grid, c->sdw_table.get()))
+          table = c->sdw_table.get();
+      }
+      e = launch_extinction(f, a, table, c->stream);
       break;
     }
     case CVR_METHOD_CONE_DOS: {
@@ -541,6 +629,70 @@ cvr_status cvr_render_host(cvr_ctx* c, int method, const cvr_camera* cam, const 
   if (s != CVR_OK) return s;
   CK(c, cudaMemcpyAsync(out_host, c->d_out, bytes, cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
+cvr_status cvr_set_tuning(cvr_ctx* c, int tile_w, int tile_h, int variant) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (tile_w <= 0 || tile_h <= 0 || tile_w % 8 || tile_h % 4 || (tile_w / 8) * (tile_h / 4) != 4 || variant < 0 ||
+      variant > 2)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_tuning: tile must be 128 threads of 8x4-pixel warps, variant 0..2");
+  c->tile_w = tile_w;
+  c->tile_h = tile_h;
+  c->variant = variant;
+  return CVR_OK;
+}
+
+cvr_status cvr_get_tuning(cvr_ctx* c, int* tile_w, int* tile_h, int* variant) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (tile_w) *tile_w = c->tile_w;
+  if (tile_h) *tile_h = c->tile_h;
+  if (variant) *variant = c->variant;
+  return CVR_OK;
+}
+
+cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light, const void* params,
+                        size_t params_size, int w, int h, int reps, int* btw, int* bth, int* bv, float* bms) {
+  if (!c || reps <= 0 || reps > 100) return fail(c, CVR_ERR_INVALID_ARG, "cvr_autotune: bad arguments");
+  static const int tiles[3][2] = {{16, 8}, {32, 4}, {8, 16}};
+  float* frame = nullptr;
+  cvr_status s = cvr_get_frame_buffer(c, w, h, &frame);
+  if (s != CVR_OK) return s;
+  int keep_w = c->tile_w, keep_h = c->tile_h, keep_v = c->variant;
+  float best = 1e30f;
+  int bw = keep_w, bh = keep_h, bvar = keep_v;
+  for (int t = 0; t < 3; ++t) {
+    for (int v = 0; v < 3; ++v) {
+      c->tile_w = tiles[t][0]; c->tile_h = tiles[t][1]; c->variant = v;
+      // one untimed frame (first launch of the variant), then the timed ones
+      s = render_impl(c, method, cam, light, params, params_size, frame, w, h, nullptr, nullptr);
+      if (s != CVR_OK) break;
+      float total = 0.0f;
+      for (int r = 0; r < reps && s == CVR_OK; ++r) {
+        if ((s = cvr_flush_l2(c)) != CVR_OK) break;
+        if ((s = cvr_timer_start(c)) != CVR_OK) break;
+        if ((s = render_impl(c, method, cam, light, params, params_size, frame, w, h, nullptr, nullptr)) != CVR_OK) break;
+        float ms = 0.0f;
+        if ((s = cvr_timer_stop(c, &ms)) != CVR_OK) break;
+        total += ms;
+      }
+      if (s != CVR_OK) break;
+      if (total / reps < best) {
+        best = total / reps;
+        bw = tiles[t][0]; bh = tiles[t][1]; bvar = v;
+      }
+    }
+    if (s != CVR_OK) break;
+  }
+  if (s != CVR_OK) {
+    c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v;
+    return s;
+  }
+  c->tile_w = bw; c->tile_h = bh; c->variant = bvar;
+  if (btw) *btw = bw;
+  if (bth) *bth = bh;
+  if (bv) *bv = bvar;
+  if (bms) *bms = best;
   return CVR_OK;
 }
 

@@ -141,10 +141,14 @@ __device__ __forceinline__ float tf_alpha(const float4* tf, int n, float density
 // trilinear SAT fetches (ebs_ray_bbox_marching.comp:74-100).  That is the
 // tensor product, over the three axes, of the 1-D functional
 //   L(S) = [(1-th) S[b0] + th S[b1]] - [(1-tl) S[a0] + tl S[a1]]
-// which equals (1-th)(S[b0]-S[a0]) + th (S[b1]-S[a1]) + (th-tl)(S[a1]-S[a0]).
+// over the taps a0, a1 (low corner, weight tl) and b0, b1 (high corner, th).
+// Written as consecutive differences along the tap sequence (a0, a1, b0, b1),
+//   L(S) = (1-tl) (S[a1]-S[a0]) + (S[b0]-S[a1]) + th (S[b1]-S[b0]).
 // Applying the three integer differences along every axis gives 27 exact
-// small box sums; only those are converted to float and weighted, so the
-// query has no cancellation however large the SAT entries are.
+// sub-box sums (a 3x3x3 split of the filtered box into faces, edges, corners
+// and core); only those are converted to float and weighted, so the query has
+// no cancellation however large the SAT entries are.  Planes are streamed in
+// tap order, so one previous plane (9 int64) is live at a time.
 struct SatView {
   const long long* sat;  // (nx+2)(ny+2)(nz+2), x fastest
   int sx, sy, sz;        // SAT dims = volume dims + 2
@@ -155,44 +159,50 @@ struct SatView {
 };
 
 struct BoxAxis {
-  int a0, a1, b0, b1;  // texel indices of the low and high corner taps
-  float c0, c1, c2;    // weights of D0=S[b0]-S[a0], D1=S[b1]-S[a1], D2=S[a1]-S[a0]
+  int s[4];    // tap sequence a0, a1, b0, b1
+  float w[3];  // weights of the consecutive differences: 1-tl, 1, th
 };
 __device__ __forceinline__ BoxAxis box_axis(float lo, float hi, int n) {
   Tap l = axis_tap(lo, n), h = axis_tap(hi, n);
   BoxAxis b;
-  b.a0 = l.i0; b.a1 = l.i1; b.b0 = h.i0; b.b1 = h.i1;
-  b.c0 = 1.0f - h.t; b.c1 = h.t; b.c2 = h.t - l.t;
+  b.s[0] = l.i0; b.s[1] = l.i1; b.s[2] = h.i0; b.s[3] = h.i1;
+  b.w[0] = 1.0f - l.t; b.w[1] = 1.0f; b.w[2] = h.t;
   return b;
 }
 
-// Three x-differences of one SAT row segment.
-struct D3 { long long d0, d1, d2; };
-__device__ __forceinline__ D3 x_diffs(const long long* row, const BoxAxis& X) {
-  long long va0 = __ldg(row + X.a0), va1 = __ldg(row + X.a1);
-  long long vb0 = __ldg(row + X.b0), vb1 = __ldg(row + X.b1);
-  D3 r; r.d0 = vb0 - va0; r.d1 = vb1 - va1; r.d2 = va1 - va0;
+struct D3 { long long d[3]; };  // consecutive x-differences of one row
+__device__ __forceinline__ D3 row_diffs(const long long* row, const BoxAxis& X) {
+  long long v0 = __ldg(row + X.s[0]), v1 = __ldg(row + X.s[1]);
+  long long v2 = __ldg(row + X.s[2]), v3 = __ldg(row + X.s[3]);
+  D3 r;
+  r.d[0] = v1 - v0; r.d[1] = v2 - v1; r.d[2] = v3 - v2;
   return r;
 }
-struct D9 { D3 y0, y1, y2; };  // y-differences (D0, D1, D2) of x-differenced rows
-__device__ __forceinline__ D9 yx_diffs(const SatView& S, int z, const BoxAxis& X, const BoxAxis& Y) {
+struct D9 { D3 y[3]; };  // consecutive y-differences of x-differenced rows
+__device__ __forceinline__ D9 plane_diffs(const SatView& S, int z, const BoxAxis& X, const BoxAxis& Y) {
   const long long* plane = S.sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
-  D3 ra0 = x_diffs(plane + (size_t)Y.a0 * S.sx, X);
-  D3 ra1 = x_diffs(plane + (size_t)Y.a1 * S.sx, X);
-  D3 rb0 = x_diffs(plane + (size_t)Y.b0 * S.sx, X);
-  D3 rb1 = x_diffs(plane + (size_t)Y.b1 * S.sx, X);
   D9 r;
-  r.y0.d0 = rb0.d0 - ra0.d0; r.y0.d1 = rb0.d1 - ra0.d1; r.y0.d2 = rb0.d2 - ra0.d2;
-  r.y1.d0 = rb1.d0 - ra1.d0; r.y1.d1 = rb1.d1 - ra1.d1; r.y1.d2 = rb1.d2 - ra1.d2;
-  r.y2.d0 = ra1.d0 - ra0.d0; r.y2.d1 = ra1.d1 - ra0.d1; r.y2.d2 = ra1.d2 - ra0.d2;
+  D3 prev = row_diffs(plane + (size_t)Y.s[0] * S.sx, X);
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    D3 cur = row_diffs(plane + (size_t)Y.s[b + 1] * S.sx, X);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r.y[b].d[a] = cur.d[a] - prev.d[a];
+    prev = cur;
+  }
   return r;
 }
-__device__ __forceinline__ float weigh9(const D9& a, const D9& b, const BoxAxis& X, const BoxAxis& Y) {
-  // sum over y-op and x-op of cy*cx*(a-b)
-  auto w3 = [&](const D3& p, const D3& q) {
-    return X.c0 * float(p.d0 - q.d0) + X.c1 * float(p.d1 - q.d1) + X.c2 * float(p.d2 - q.d2);
-  };
-  return Y.c0 * w3(a.y0, b.y0) + Y.c1 * w3(a.y1, b.y1) + Y.c2 * w3(a.y2, b.y2);
+// sum over y-op and x-op of wy * wx * (cur - prev), the z-difference of two planes
+__device__ __forceinline__ float weigh9(const D9& cur, const D9& prev, const BoxAxis& X, const BoxAxis& Y) {
+  float acc = 0.0f;
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    float row = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) row = fmaf(X.w[a], float(cur.y[b].d[a] - prev.y[b].d[a]), row);
+    acc = fmaf(Y.w[b], row, acc);
+  }
+  return acc;
 }
 
 // EvaluateSAT3D(p1, p2) on already offset + clamped world positions.
@@ -200,13 +210,14 @@ __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2)
   BoxAxis X = box_axis(fmaf(p1.x, S.inv_spacing.x, -0.5f), fmaf(p2.x, S.inv_spacing.x, -0.5f), S.sx);
   BoxAxis Y = box_axis(fmaf(p1.y, S.inv_spacing.y, -0.5f), fmaf(p2.y, S.inv_spacing.y, -0.5f), S.sy);
   BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
-  D9 za0 = yx_diffs(S, Z.a0, X, Y);
-  D9 za1 = yx_diffs(S, Z.a1, X, Y);
-  float acc = Z.c2 * weigh9(za1, za0, X, Y);
-  D9 zb0 = yx_diffs(S, Z.b0, X, Y);
-  acc = fmaf(Z.c0, weigh9(zb0, za0, X, Y), acc);
-  D9 zb1 = yx_diffs(S, Z.b1, X, Y);
-  acc = fmaf(Z.c1, weigh9(zb1, za1, X, Y), acc);
+  float acc = 0.0f;
+  D9 prev = plane_diffs(S, Z.s[0], X, Y);
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    D9 cur = plane_diffs(S, Z.s[g + 1], X, Y);
+    acc = fmaf(Z.w[g], weigh9(cur, prev, X, Y), acc);
+    prev = cur;
+  }
   return acc * S.inv_scale;
 }
 

@@ -114,6 +114,9 @@ class BaseVolumeRenderer {
   virtual void Reshape(int w, int h);
   virtual int GetDataTypeSupport() { return 0; }  // structured grid
   virtual void FillParameterSpace(ParameterSpace& ps) { ps.ClearParameterDimensions(); }
+  // The occlusion / shadow check boxes of the illumination renderers' UI
+  // (SetImGuiComponents); a no-op for renderers without illumination.
+  virtual void SetIllumination(bool occlusion, bool shadow) { (void)occlusion; (void)shadow; }
 
   // volrenderbase.cpp:77-84: Update only when outdated.
   bool PrepareRender(const vis::Camera& camera);
@@ -173,6 +176,7 @@ class RC1PExtinctionBasedShading : public BaseVolumeRenderer {
   bool Init(int w, int h) override;
   bool Update(const vis::Camera& camera) override;
   void FillParameterSpace(ParameterSpace& ps) override;
+  void SetIllumination(bool o, bool s) override { apply_ambient_occlusion = o; apply_directional_shadows = s; SetOutdated(); }
 
   float m_u_step_size = 0.5f;
   bool apply_ambient_occlusion = true;
@@ -201,6 +205,7 @@ class RC1PConeTracingDirOcclusionShading : public BaseVolumeRenderer {
   const char* GetAbbreviationName() override { return "s_1pdosct"; }
   bool Init(int w, int h) override;
   bool Update(const vis::Camera& camera) override;
+  void SetIllumination(bool o, bool s) override { glsl_apply_occlusion = o; glsl_apply_shadow = s; SetOutdated(); }
 
   float m_u_step_size = 0.5f;
   bool glsl_apply_occlusion = true, glsl_apply_shadow = false;
@@ -225,6 +230,7 @@ class RC1PConeLightGroundTruthSteps : public BaseVolumeRenderer {
   const char* GetAbbreviationName() override { return "s_1pcrtgt"; }
   bool Init(int w, int h) override;
   bool Update(const vis::Camera& camera) override;
+  void SetIllumination(bool o, bool s) override { m_apply_occlusion = o; m_apply_shadows = s; SetOutdated(); }
 
   float m_u_step_size = 0.5f;
   float m_u_light_ray_initial_step = 1.0f, m_u_light_ray_step_size = 0.5f;

@@ -27,6 +27,11 @@ struct PlainShade {
 // ====================================================== extinction (rc1pextbsd)
 struct ExtShade {
   const ExtArgs* e;
+  // Per-frame box table of a directional light (shared memory), or nullptr.
+  const float4* tlo = nullptr;
+  const float4* thi = nullptr;
+  int tn = 0, tax = 0;
+  float tiw = 0.0f, tvmin = 0.0f, tvmax = 0.0f;
   struct Ray {};
   __device__ __forceinline__ void begin(Ray&, float3) const {}
 
@@ -175,6 +180,26 @@ struct ExtShade {
     return st;
   }
 
+  // The Cone*Axis walk over the precomputed boxes of a directional light:
+  // same boxes, same CUT_WHEN_AWAY_FROM_VOLUME test, same sum.
+  __device__ float shadow_table(float3 tx, const FrameArgs& f, unsigned& aux) const {
+    const SatView& S = e->sat;
+    const float3 sc = f.vol.spacing;
+    const float pm = tax == 0 ? tx.x : (tax == 1 ? tx.y : tx.z);
+    float st = 0.0f;
+    for (int k = 0; k < tn; ++k) {
+      const float4 lo = tlo[k];
+      const float nxt = pm + (lo.w + tiw);
+      if (!(nxt > tvmin && nxt < tvmax)) break;
+      const float4 hi = thi[k];
+      float3 p1 = clamp3(tx + f3(lo.x, lo.y, lo.z) + sc, S.min_pos, S.max_pos);
+      float3 p2 = clamp3(tx + f3(hi.x, hi.y, hi.z) + sc, S.min_pos, S.max_pos);
+      st = fmaf(sat_box(S, p1, p2), hi.w, st);
+      ++aux;
+    }
+    return expf(-st);
+  }
+
   // ExtinctionDirectionalShadows (ebs_ray_bbox_marching.comp:432-456).
   __device__ float shadow(float3 tx, const FrameArgs& f, unsigned& aux) const {
     float3 realpos = tx - f.vol.grid * 0.5f;
@@ -191,7 +216,7 @@ struct ExtShade {
   __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray&, const FrameArgs& f, unsigned& aux) const {
     float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
     if (e->apply_occ) { ka = e->ka; io = ambient_occlusion(tx, f); aux += e->n_shells; }
-    if (e->apply_sdw) { kd = e->kd; is = shadow(tx, f, aux); }
+    if (e->apply_sdw) { kd = e->kd; is = tlo ? shadow_table(tx, f, aux) : shadow(tx, f, aux); }
     float k = 1.0f / (ka + kd);
     src.x = k * (src.x * io * ka + src.x * is * kd);
     src.y = k * (src.y * io * ka + src.y * is * kd);
@@ -503,11 +528,34 @@ __global__ void __launch_bounds__(128) k_march_plain(FrameArgs f) {
   march_pixel(f, tf, PlainShade{});
 }
 
-__global__ void __launch_bounds__(128) k_march_extinction(FrameArgs f, ExtArgs e) {
+// MINB: minimum resident CTAs per SM requested from the register allocator
+// (1: no cap, 4: <= 128 registers, 6: <= 80 registers); chosen by the tuner.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_march_extinction(FrameArgs f, ExtArgs e) {
   extern __shared__ float4 sm_tf[];
   const float4* tf = stage_tf(f, sm_tf);
   __syncthreads();
   ExtShade sh{&e};
+  march_pixel(f, tf, sh);
+}
+
+// Directional light: the shadow boxes come from the per-frame table, staged
+// in shared memory after the transfer function.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_march_extinction_dir(FrameArgs f, ExtArgs e,
+                                                                    const __grid_constant__ ShadowBoxTable t) {
+  extern __shared__ float4 sm_tf[];
+  const float4* tf = stage_tf(f, sm_tf);
+  float4* lo = sm_tf + f.tf_n;
+  float4* hi = lo + t.n;
+  for (int i = threadIdx.x; i < t.n; i += blockDim.x) {
+    lo[i] = t.lo[i];
+    hi[i] = t.hi[i];
+  }
+  __syncthreads();
+  ExtShade sh{&e};
+  sh.tlo = lo; sh.thi = hi; sh.tn = t.n; sh.tax = t.axis;
+  sh.tiw = t.interval; sh.tvmin = t.vmin; sh.tvmax = t.vmax;
   march_pixel(f, tf, sh);
 }
 
@@ -548,9 +596,23 @@ cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, cudaStream_t st) {
-  size_t sm = sizeof(float4) * f.tf_n;
-  k_march_extinction<<<grid_of(f), threads_of(f), sm, st>>>(f, e);
+template <int MINB>
+static void launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+  if (table) {
+    size_t sm = sizeof(float4) * (f.tf_n + 2 * table->n);
+    k_march_extinction_dir<MINB><<<grid_of(f), threads_of(f), sm, st>>>(f, e, *table);
+  } else {
+    size_t sm = sizeof(float4) * f.tf_n;
+    k_march_extinction<MINB><<<grid_of(f), threads_of(f), sm, st>>>(f, e);
+  }
+}
+
+cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+  switch (f.variant) {
+    case 1: launch_extinction_t<4>(f, e, table, st); break;
+    case 2: launch_extinction_t<6>(f, e, table, st); break;
+    default: launch_extinction_t<1>(f, e, table, st); break;
+  }
   return cudaGetLastError();
 }
 

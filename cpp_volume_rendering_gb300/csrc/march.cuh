@@ -17,7 +17,8 @@ struct FrameArgs {
   int tf_n;
   float step;            // StepSize
   int W, H;
-  int tile_w, tile_h;    // pixels per CTA (multiples of 8 and 4)
+  int tile_w, tile_h;    // pixels per CTA: 128 threads as (tile_w/8) x (tile_h/4) warps
+  int variant;           // register / occupancy variant of the kernel (0, 1, 2)
   float4* out;
   uint32_t* counts;                // per-pixel step count, nullable
   unsigned long long* stats;       // [0] samples, [1] shaded samples, [2] secondary fetches
@@ -32,6 +33,21 @@ struct ExtArgs {
   int shadow_type;
   float3 light_pos, light_fwd;
   float ka, kd;
+};
+
+// Boxes of the SAT shadow cone of a directional light.  The cone direction is
+// the same for every sample, so the box offsets of ConeZAxis / ConeYAxis /
+// ConeXAxis (ebs_ray_bbox_marching.comp:190-430) depend only on the box index
+// and are computed once per frame; each sample keeps its own
+// CUT_WHEN_AWAY_FROM_VOLUME test.
+#define CVR_MAX_SDW_BOXES 512
+struct ShadowBoxTable {
+  int n;           // boxes passing the max-distance test
+  int axis;        // dominant axis of the light direction
+  float interval;  // signed box step along the axis (world units)
+  float vmin, vmax;
+  float4 lo[CVR_MAX_SDW_BOXES];  // xyz: low corner offset, w: position along the axis
+  float4 hi[CVR_MAX_SDW_BOXES];  // xyz: high corner offset, w: UI weight / box volume in voxels
 };
 
 struct ConeTableDev {
@@ -64,7 +80,8 @@ struct GtArgs {
 };
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
-cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, cudaStream_t st);
+// table == nullptr: per-sample cone geometry (point lights, or too many boxes).
+cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st);
 cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, cudaStream_t st);
 cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st);
 

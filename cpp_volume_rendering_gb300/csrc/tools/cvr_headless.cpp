@@ -7,7 +7,8 @@
 //   cvr_headless --volume V.raw|V.syn --tf T.tf1d --renderer s_1pebs
 //                [--width 768 --height 768] [--frames 1]
 //                [--cameras LIST --camera-index i] [--lights LIST --light-index i]
-//                [--eye x y z] [--fovy deg] [--out frame.pfm]
+//                [--eye x y z] [--fovy deg] [--occlusion 0|1] [--shadow 0|1]
+//                [--out frame.pfm]
 // Exit code 0 on success, 1 on a usage error, 2 on a data error, 3 on a
 // rendering error; messages go to stderr.
 #include <chrono>
@@ -22,7 +23,7 @@ static int usage() {
   std::fprintf(stderr,
                "usage: cvr_headless --volume FILE --tf FILE --renderer ABBR [--width W --height H] [--frames N]\n"
                "       [--cameras FILE --camera-index I] [--lights FILE --light-index I] [--eye X Y Z]\n"
-               "       [--fovy DEG] [--out FILE.pfm]\n"
+               "       [--fovy DEG] [--occlusion 0|1] [--shadow 0|1] [--out FILE.pfm]\n"
                "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt\n");
   return 1;
 }
@@ -31,6 +32,7 @@ int main(int argc, char** argv) {
   std::string vol, tf, rend, out, cams, lights;
   int w = 768, h = 768, frames = 1, cam_i = 0, light_i = 0;
   bool have_eye = false;
+  int occlusion = -1, shadow = -1;
   float eye[3] = {0, 0, 0}, fovy = 45.0f;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
@@ -48,6 +50,8 @@ int main(int argc, char** argv) {
     else if (a == "--lights" && (v = next())) lights = v;
     else if (a == "--light-index" && (v = next())) light_i = std::atoi(v);
     else if (a == "--fovy" && (v = next())) fovy = (float)std::atof(v);
+    else if (a == "--occlusion" && (v = next())) occlusion = std::atoi(v);
+    else if (a == "--shadow" && (v = next())) shadow = std::atoi(v);
     else if (a == "--eye" && i + 3 < argc) {
       for (int k = 0; k < 3; ++k) eye[k] = (float)std::atof(argv[++i]);
       have_eye = true;
@@ -102,6 +106,11 @@ int main(int argc, char** argv) {
   if (!mgr.SetCurrentVolumeRenderer(rend)) {
     std::fprintf(stderr, "cvr_headless: %s\n", mgr.LastError().c_str());
     return 3;
+  }
+  if (occlusion >= 0 || shadow >= 0) {
+    // Defaults of the renderer stay where a switch is not given.
+    BaseVolumeRenderer* r = mgr.GetCurrentVolumeRenderer();
+    r->SetIllumination(occlusion != 0, shadow != 0);
   }
   auto t0 = std::chrono::steady_clock::now();
   for (int f = 0; f < frames; ++f) {

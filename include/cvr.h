@@ -247,6 +247,21 @@ cvr_status cvr_get_frame_buffer(cvr_ctx* ctx, int w, int h, float** dev_out);
  * to host memory; synchronous (the glGetTexImage readback of the reference). */
 cvr_status cvr_download_frame(cvr_ctx* ctx, const float* dev_frame, int w, int h, float* host_out);
 
+/* Launch configuration of the marchers (no reference counterpart: the
+ * reference always dispatches 8x8 work groups, computeshader.h:37).  A CTA
+ * is 128 threads whose warps each cover an 8x4 pixel block, arranged as
+ * (tile_w/8) x (tile_h/4) warps: tiles 16x8, 32x4 or 8x16.  variant selects the
+ * register budget of the kernel (0: compiler's choice, 1: <= 128, 2: <= 80
+ * registers per thread).  Results do not depend on the choice. */
+cvr_status cvr_set_tuning(cvr_ctx* ctx, int tile_w, int tile_h, int variant);
+cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
+/* Autotuner: renders the given frame with every tile shape x variant
+ * (reps timed frames each, CUDA events, L2 flushed before each), keeps the
+ * fastest on the context and reports it.  best_ms may be NULL. */
+cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
+                        const void* params, size_t params_size, int w, int h, int reps,
+                        int* best_tile_w, int* best_tile_h, int* best_variant, float* best_ms);
+
 /* ---- device timing on the context stream --------------------------------- */
 cvr_status cvr_timer_start(cvr_ctx* ctx);
 /* Records the stop event, synchronises and returns elapsed milliseconds. */

@@ -196,3 +196,39 @@ def test_errors_are_reported_not_crashing(ctx):
     r = lib.cvr_render_host(empty.h, abi.PLAIN, C.byref(cam), None, C.byref(p), C.sizeof(p), abi.fptr(img), 4, 4, None)
     assert r == abi.CVR_ERR_NO_VOLUME
     empty.close()
+
+
+def test_tuning_does_not_change_results(ctx):
+    """Every tile shape / register variant renders the same bits."""
+    import ctypes as C
+    lib = abi.load()
+    wl = scene.workload("extinction", n=48, image=72)
+    scene.prepare(ctx, wl)
+    images = []
+    for tw, th in [(16, 8), (32, 4), (8, 16)]:
+        for v in (0, 1, 2):
+            abi.check(lib.cvr_set_tuning(ctx.h, tw, th, v), ctx.h)
+            img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+            images.append(img)
+    for im in images[1:]:
+        assert np.array_equal(im, images[0])
+    assert lib.cvr_set_tuning(ctx.h, 16, 16, 0) == abi.CVR_ERR_INVALID_ARG
+    tw, th, v = C.c_int(), C.c_int(), C.c_int()
+    ms = C.c_float()
+    abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                               C.sizeof(wl.params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(v),
+                               C.byref(ms)), ctx.h)
+    assert (tw.value, th.value) in [(16, 8), (32, 4), (8, 16)] and v.value in (0, 1, 2) and ms.value > 0
+    abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
+
+
+def test_directional_shadow_table_matches_per_sample_geometry(ctx):
+    """The per-frame box table of a directional light equals the per-sample
+    cone walk: render the same light once as directional (table) and compare
+    with the oracle, which walks the cone per sample."""
+    wl = scene.workload("extinction", n=40, image=64)
+    for fwd in [(0.2, 0.3, 0.93), (-0.8, 0.1, 0.3), (0.1, -0.95, -0.2), (0.5, 0.5, 0.5)]:
+        f, u, r = scene.light_frame(fwd)
+        wl.light = scene.light(abi.LIGHT_DIRECTIONAL, forward=f, up=u, right=r)
+        img, st, ref, total = run_both(ctx, wl)
+        compare(img, ref, f"directional light {fwd}")

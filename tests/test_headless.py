@@ -64,8 +64,10 @@ def test_data_errors_before_any_device_call(data, tmp_path):
                                          ("s_1pdosct", abi.CONE_DOS), ("s_1pcrtgt", abi.GROUND_TRUTH)])
 def test_headless_frames(data, abbr, method, tmp_path):
     out = tmp_path / f"{abbr}.pfm"
+    # the ground-truth renderer starts with occlusion and shadows off (crtgtrenderer.cpp:40-46)
+    extra = ["--occlusion", "1", "--shadow", "1"] if abbr == "s_1pcrtgt" else []
     r = run("--volume", data["vp"], "--tf", data["tp"], "--renderer", abbr, "--width", "40", "--height", "32",
-            "--cameras", data["cp"], "--camera-index", "1", "--lights", data["lp"], "--out", out)
+            "--cameras", data["cp"], "--camera-index", "1", "--lights", data["lp"], "--out", out, *extra)
     assert r.returncode == 0, r.stderr
     assert f"renderer={abbr}" in r.stdout
     raw = out.read_bytes()
