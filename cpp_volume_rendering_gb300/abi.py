@@ -32,6 +32,7 @@ PLAIN, EXTINCTION, CONE_DOS, GROUND_TRUTH = 0, 1, 2, 3
 LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL = 0, 1, 2
 
 MAX_AO_SHELLS = 32
+MLP_PARAMS = 7362
 MAX_CONE_SECTIONS = 512
 
 F3 = C.c_float * 3
@@ -134,6 +135,15 @@ SIGNATURES = {
     "cvr_host_alloc_pinned": (_I, [C.c_size_t, C.POINTER(_P)]),
     "cvr_host_free_pinned": (None, [_P]),
     "cvr_synth_blobs": (_I, [_P, _I, _I, _I, _I, _I, C.c_uint64, _F]),
+    "cvr_mlp_init": (_I, [_P, C.c_uint64]),
+    "cvr_mlp_set_params": (_I, [_P, _FP, _I]),
+    "cvr_mlp_get_params": (_I, [_P, _FP, _I]),
+    "cvr_mlp_forward": (_I, [_P, _FP, _I, _FP]),
+    "cvr_mlp_gradients": (_I, [_P, _FP, _FP, _I, _FP, _FP]),
+    "cvr_mlp_set_training_data": (_I, [_P, _FP, _FP, _I]),
+    "cvr_mlp_get_training_data": (_I, [_P, _FP, _FP, _I]),
+    "cvr_mlp_training_size": (_I, [_P]),
+    "cvr_mlp_train": (_I, [_P, _I, _I, _F, C.c_uint64, _FP]),
     "cvr_synth_value_noise": (_I, [_P, _I, _I, _I, _I, _I, _F, _F, _I, C.c_uint64]),
 }
 

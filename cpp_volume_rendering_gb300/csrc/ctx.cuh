@@ -1,0 +1,164 @@
+// ctx.cuh — the cvr_ctx object shared by the translation units of the C ABI
+// (context.cu: volume, tables and rendering; mlp_host.cu: the surrogate
+// network) and their common error / allocation helpers.
+#pragma once
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/cvr.h"
+#include "build_tables.cuh"
+#include "march.cuh"
+
+using namespace cvr;
+
+// Device state of the surrogate network: FP32 master parameters, Adam
+// moments, the packed BF16 image, per-CTA gradient partials, the training set.
+struct MlpState {
+  float* params = nullptr;
+  float* m = nullptr;
+  float* v = nullptr;
+  uint8_t* packed = nullptr;
+  float* partials = nullptr;
+  size_t partials_cap = 0;
+  float* grad = nullptr;     // reduced gradient (+ loss) of the last batch
+  float* loss_acc = nullptr; // loss accumulated over an epoch
+  int* err = nullptr;        // set by a kernel whose bounded wait gave up
+  int* step = nullptr;       // Adam step counter
+  float* x = nullptr;        // training features, n x 48
+  float* t = nullptr;        // training targets, n x 2
+  size_t data_cap = 0;       // points
+  int n = 0;
+  int* idx = nullptr;        // epoch permutation
+  size_t idx_cap = 0;
+  float* io_x = nullptr;     // staging of host batches (forward / gradients)
+  float* io_y = nullptr;
+  size_t io_cap = 0;
+  cudaGraphExec_t epoch_graph = nullptr;
+  int graph_batch = 0, graph_n = 0;
+  bool ready = false;
+  ~MlpState() {
+    void* bufs[] = {params, m, v, packed, partials, grad, loss_acc, err, step, x, t, idx, io_x, io_y};
+    for (void* p : bufs)
+      if (p) cudaFree(p);
+    if (epoch_graph) cudaGraphExecDestroy(epoch_graph);
+  }
+};
+
+struct cvr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // volume
+  void* d_vol = nullptr;
+  size_t vol_cap = 0;
+  int nx = 0, ny = 0, nz = 0, dtype = 0;
+  float sx = 1, sy = 1, sz = 1;
+  bool has_volume = false;
+  // transfer function
+  float4* d_rgbt = nullptr;
+  float4* d_rgba = nullptr;
+  int tf_n = 0, tf_cap = 0;
+  // SAT
+  long long* d_sat = nullptr;
+  size_t sat_cap = 0;
+  long long* d_lut = nullptr;
+  int sat_frac_bits = 0;
+  bool sat_ready = false;
+  // pyramid
+  float* d_pyr = nullptr;
+  size_t pyr_cap = 0;
+  PyramidView pyr{};
+  bool pyr_ready = false;
+  // cone tables
+  float4* d_occ_sec = nullptr;
+  float4* d_sdw_sec = nullptr;
+  ConeTableDev occ{}, sdw{};
+  bool cone_ready = false;
+  // GT kernel vectors
+  float3* d_occ_vec = nullptr;
+  float3* d_sdw_vec = nullptr;
+  int n_occ = 0, n_sdw = 0;
+  bool gt_ready = false;
+  // frame
+  unsigned long long* d_stats = nullptr;
+  float4* d_out = nullptr;
+  size_t out_cap = 0;
+  void* d_flush = nullptr;
+  size_t flush_bytes = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  int tile_w = 16, tile_h = 8, variant = 0;
+  std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
+  std::unique_ptr<MlpState> mlp;             // surrogate network (created by cvr_mlp_init)
+};
+
+namespace cvr {
+namespace ctxutil {
+
+extern thread_local std::string g_create_err;
+
+inline cvr_status fail(cvr_ctx* c, cvr_status code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+inline cvr_status cuda_fail(cvr_ctx* c, cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a sticky launch error where possible
+  std::string msg = std::string(what) + ": " + cudaGetErrorString(e);
+  return fail(c, e == cudaErrorMemoryAllocation ? CVR_ERR_OUT_OF_MEMORY : CVR_ERR_CUDA, msg);
+}
+
+#define CK(ctx, call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+  } while (0)
+
+// Grows a device allocation to at least 'bytes' (contents discarded).
+template <class T>
+cudaError_t ensure(T*& p, size_t& cap, size_t bytes) {
+  if (cap >= bytes && p) return cudaSuccess;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMalloc((void**)&p, bytes);
+  if (e == cudaSuccess) cap = bytes;
+  return e;
+}
+
+inline VolumeView volume_view(const cvr_ctx* c) {
+  VolumeView v;
+  v.voxels = c->d_vol;
+  v.dtype = c->dtype;
+  v.nx = c->nx; v.ny = c->ny; v.nz = c->nz;
+  v.spacing = f3(c->sx, c->sy, c->sz);
+  v.inv_spacing = f3(1.0f / c->sx, 1.0f / c->sy, 1.0f / c->sz);
+  v.grid = f3(c->nx * c->sx, c->ny * c->sy, c->nz * c->sz);
+  v.norm = c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  return v;
+}
+
+// glm::lookAt basis in single precision (libs/vis_utils/camera.cpp:281-284).
+inline CameraView camera_view(const cvr_camera* cam, int w, int h) {
+  float3 eye = make3(cam->eye), ctr = make3(cam->center), up = make3(cam->up);
+  float3 fw = ctr - eye;
+  float inv = 1.0f / std::sqrt(dot3(fw, fw));
+  fw = fw * inv;
+  float3 s = cross3(fw, up);
+  inv = 1.0f / std::sqrt(dot3(s, s));
+  s = s * inv;
+  float3 u = cross3(s, fw);
+  CameraView cv;
+  cv.eye = eye; cv.s = s; cv.u = u; cv.f = fw;
+  cv.tan_half_fovy = (float)std::tan((double)cam->fovy_deg * (3.14159265358979323846 / 180.0) / 2.0);
+  cv.aspect = cam->aspect > 0.0f ? cam->aspect : (float)w / (float)h;
+  return cv;
+}
+
+
+}  // namespace ctxutil
+}  // namespace cvr

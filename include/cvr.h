@@ -269,6 +269,36 @@ cvr_status cvr_timer_stop(cvr_ctx* ctx, float* ms);
 /* Writes a device buffer larger than L2 (flushes the L2 cache) on the stream. */
 cvr_status cvr_flush_l2(cvr_ctx* ctx);
 
+/* ---- learned occlusion / shadow surrogate ---------------------------------
+ * No reference counterpart: a small MLP that stands in for the ray-traced
+ * ground-truth integrator (RC1PConeLightGroundTruthSteps).  48 inputs ->
+ * 64 -> 64 -> 2 outputs (ambient occlusion, shadow), ReLU hidden layers, BF16
+ * operands with FP32 accumulation on the tensor cores.  Parameter vector
+ * (FP32, CVR_MLP_PARAMS floats): W1[64][48], b1[64], W2[64][64], b2[64],
+ * W3[2][64], b3[2] with W[out][in]. */
+#define CVR_MLP_INPUTS 48
+#define CVR_MLP_HIDDEN 64
+#define CVR_MLP_OUTPUTS 2
+#define CVR_MLP_PARAMS 7362
+
+/* He-uniform weights from a seed, zero biases, fresh Adam state. */
+cvr_status cvr_mlp_init(cvr_ctx* ctx, uint64_t seed);
+cvr_status cvr_mlp_set_params(cvr_ctx* ctx, const float* params, int n);
+cvr_status cvr_mlp_get_params(cvr_ctx* ctx, float* params, int n);
+/* Batch inference of n points (host buffers: x n*48, y n*2). Synchronous. */
+cvr_status cvr_mlp_forward(cvr_ctx* ctx, const float* x, int n, float* y);
+/* Gradient of L = 1/(2n) sum (y - t)^2 over n points w.r.t. every parameter,
+ * without updating them (grad: CVR_MLP_PARAMS floats).  Synchronous. */
+cvr_status cvr_mlp_gradients(cvr_ctx* ctx, const float* x, const float* t, int n, float* grad, float* loss);
+/* Training set from host memory (features n*48, targets n*2). */
+cvr_status cvr_mlp_set_training_data(cvr_ctx* ctx, const float* x, const float* t, int n);
+cvr_status cvr_mlp_get_training_data(cvr_ctx* ctx, float* x, float* t, int n);
+int cvr_mlp_training_size(cvr_ctx* ctx);
+/* Adam over the training set: epochs x ceil(n/batch) steps (batch a multiple
+ * of 128); each epoch is one replay of a captured CUDA graph.
+ * loss_per_epoch (nullable) receives the mean batch loss of every epoch. */
+cvr_status cvr_mlp_train(cvr_ctx* ctx, int epochs, int batch, float lr, uint64_t seed, float* loss_per_epoch);
+
 /* ---- host-side helpers (no GPU needed) ------------------------------------ */
 /* TransferFunction1D::BuildLinear over control points (transferfunction1d.cpp:319-358)
  * followed by GenerateTexture_1D_RGBt / _RGBA; tables hold max_density+1 entries. */
