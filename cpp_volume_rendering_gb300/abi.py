@@ -32,7 +32,7 @@ PLAIN, EXTINCTION, CONE_DOS, GROUND_TRUTH = 0, 1, 2, 3
 LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL = 0, 1, 2
 
 MAX_AO_SHELLS = 32
-MLP_PARAMS = 7362
+MLP_PARAMS = 7426
 MAX_CONE_SECTIONS = 512
 
 F3 = C.c_float * 3

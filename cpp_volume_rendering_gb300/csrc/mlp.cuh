@@ -16,7 +16,7 @@ constexpr int kMlpIn = 48;
 constexpr int kMlpHidden = 64;
 constexpr int kMlpOut = 2;
 constexpr int kMlpK = 64;  // input width padded to a multiple of 16
-constexpr int kMlpParams = 64 * 48 + 64 + 64 * 64 + 64 + 2 * 64 + 2;  // 7362
+constexpr int kMlpParams = 64 * 48 + 64 + 64 * 64 + 64 + 2 * 64 + 2;  // 7426
 constexpr int kOffW1 = 0, kOffB1 = 64 * 48, kOffW2 = kOffB1 + 64, kOffB2 = kOffW2 + 64 * 64, kOffW3 = kOffB2 + 64,
               kOffB3 = kOffW3 + 2 * 64;
 

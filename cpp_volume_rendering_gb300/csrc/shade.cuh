@@ -1,0 +1,524 @@
+// shade.cuh — the shading policies of the four renderers and the shared
+// primary-ray loop (ShadeSample and main() of each reference shader).
+// Included by march.cu (the marchers) and surrogate.cu (training targets and
+// the surrogate-shaded marcher reuse the ground-truth light rays).
+#pragma once
+
+#include "march.cuh"
+
+namespace cvr {
+
+// Iteration bounds of the secondary loops.  Validated parameters stay far
+// below them (a cone walk has at most 0.75*diagonal/interval boxes, a light
+// ray distance/step samples); they only stop a loop whose position stopped
+// advancing from spinning forever.
+constexpr int kMaxConeBoxes = 1 << 16;
+constexpr int kMaxLightSteps = 1 << 20;
+
+// ============================================================ plain (rc1pass)
+struct PlainShade {
+  struct Ray {};
+  __device__ __forceinline__ void begin(Ray&, float3) const {}
+  // Gradient Blinn-Phong is off by default (m_apply_gradient_shading=false,
+  // rc1prenderer.cpp:22), so ShadeSample is the identity here.
+  __device__ __forceinline__ float4 shade(float4 src, float3, const Ray&, const FrameArgs&, unsigned&) const { return src; }
+};
+
+// ====================================================== extinction (rc1pextbsd)
+struct ExtShade {
+  const ExtArgs* e;
+  // Per-frame box table of a directional light (shared memory), or nullptr.
+  const float4* tlo = nullptr;
+  const float4* thi = nullptr;
+  int tn = 0, tax = 0;
+  float tiw = 0.0f, tvmin = 0.0f, tvmax = 0.0f;
+  struct Ray {};
+  __device__ __forceinline__ void begin(Ray&, float3) const {}
+
+  // EvaluateAmbientOcclusionSAT3D (ebs_ray_bbox_marching.comp:102-110).
+  __device__ __forceinline__ float ao_box(float3 p1, float3 p2, const FrameArgs& f) const {
+    const SatView& S = e->sat;
+    p1 = clamp3(p1 + f.vol.spacing, S.min_pos, S.max_pos);
+    p2 = clamp3(p2 + f.vol.spacing, S.min_pos, S.max_pos);
+    return sat_box(S, p1, p2);
+  }
+
+  // ExtinctionAmbientOcclusion (ebs_ray_bbox_marching.comp:112-146), with the
+  // shell radii taken from a list (reference: AmbOccRadius * (i + 1)).
+  __device__ float ambient_occlusion(float3 tx, const FrameArgs& f) const {
+    float3 sc = f.vol.spacing;
+    float r0 = e->radii[0];
+    float sat0 = ao_box(tx - sc * r0, tx + sc * r0, f);
+    float t = sat0 * (1.0f / (r0 * r0));
+    float sat_i = sat0;
+    for (int i = 1; i < e->n_shells; ++i) {
+      float ri = e->radii[i];
+      float sat_n = ao_box(tx - sc * ri, tx + sc * ri, f);
+      t = t + (sat_n - sat_i) * (1.0f / (ri * ri));
+      sat_i = sat_n;
+    }
+    float rk = e->radii[e->n_shells - 1];
+    float wa = 1.0f / (rk * rk);
+    return expf(-(wa * t));
+  }
+
+  // EvaluateShadowSAT3D, texture() branch (ebs_ray_bbox_marching.comp:173-187).
+  __device__ __forceinline__ float shadow_box(float3 p1, float3 p2, const FrameArgs& f) const {
+    float3 sc = f.vol.spacing;
+    float volq = (fabsf(p1.x - p2.x) / sc.x) * (fabsf(p1.y - p2.y) / sc.y) * (fabsf(p1.z - p2.z) / sc.z);
+    const SatView& S = e->sat;
+    p1 = clamp3(p1 + sc, S.min_pos, S.max_pos);
+    p2 = clamp3(p2 + sc, S.min_pos, S.max_pos);
+    return (sat_box(S, p1, p2) / volq) * e->ui_weight;
+  }
+
+  // ConeZAxis (ebs_ray_bbox_marching.comp:190-270).
+  __device__ float cone_z(float3 pos, float3 c, const FrameArgs& f, unsigned& aux) const {
+    float3 sc = f.vol.spacing;
+    float st = 0.0f;
+    float signal = c.z < 0.0f ? -1.0f : 1.0f;
+    float3 proj_y = normalize3(f3(0.0f, c.y, c.z));
+    float3 proj_x = normalize3(f3(c.x, 0.0f, c.z));
+    float p_cs = cosf(e->cone_angle), p_sn = sinf(e->cone_angle);
+    float n_cs = cosf(-e->cone_angle), n_sn = sinf(-e->cone_angle);
+    float3 pj_x1 = normalize3(f3(proj_x.x * n_cs - proj_x.z * n_sn, 0.0f, proj_x.x * n_sn + proj_x.z * n_cs));
+    float3 pj_x2 = normalize3(f3(proj_x.x * p_cs - proj_x.z * p_sn, 0.0f, proj_x.x * p_sn + proj_x.z * p_cs));
+    float3 pj_y1 = normalize3(f3(0.0f, proj_y.y * n_cs - proj_y.z * n_sn, proj_y.y * n_sn + proj_y.z * n_cs));
+    float3 pj_y2 = normalize3(f3(0.0f, proj_y.y * p_cs - proj_y.z * p_sn, proj_y.y * p_sn + proj_y.z * p_cs));
+    float interval = e->interval * signal * sc.z;
+    float zp = e->initial * signal * sc.z;
+    float vmin = sc.z * 0.5f, vmax = f.vol.grid.z - sc.z * 0.5f;
+    for (int guard = 0; guard < kMaxConeBoxes && (zp / c.z) < e->max_dist &&
+                        (pos.z + (zp + interval) > vmin && pos.z + (zp + interval) < vmax); ++guard) {
+      float zm = fabsf(zp + interval * 0.5f);
+      float px1 = pj_x1.x * (zm / fabsf(pj_x1.z)), px2 = pj_x2.x * (zm / fabsf(pj_x2.z));
+      float py1 = pj_y1.y * (zm / fabsf(pj_y1.z)), py2 = pj_y2.y * (zm / fabsf(pj_y2.z));
+      float x1 = fminf(px1, px2), x2 = fmaxf(px1, px2);
+      float y1 = fminf(py1, py2), y2 = fmaxf(py1, py2);
+      float xd = fabsf(x2 - x1), yd = fabsf(y2 - y1);
+      float xs = (ceilf(xd / sc.x) - (xd / sc.x)) * 0.5f;
+      float ys = (ceilf(yd / sc.y) - (yd / sc.y)) * 0.5f;
+      x1 = x1 - xs * sc.x; x2 = x2 + xs * sc.x;
+      y1 = y1 - ys * sc.y; y2 = y2 + ys * sc.y;
+      float z1 = fminf(zp, zp + interval), z2 = fmaxf(zp, zp + interval);
+      st += shadow_box(pos + f3(x1, y1, z1), pos + f3(x2, y2, z2), f);
+      ++aux;
+      zp = zp + interval;
+    }
+    return st;
+  }
+
+  // ConeYAxis (ebs_ray_bbox_marching.comp:272-350).
+  __device__ float cone_y(float3 pos, float3 c, const FrameArgs& f, unsigned& aux) const {
+    float3 sc = f.vol.spacing;
+    float st = 0.0f;
+    float signal = c.y < 0.0f ? -1.0f : 1.0f;
+    float3 proj_x = normalize3(f3(c.x, c.y, 0.0f));
+    float3 proj_z = normalize3(f3(0.0f, c.y, c.z));
+    float p_cs = cosf(e->cone_angle), p_sn = sinf(e->cone_angle);
+    float n_cs = cosf(-e->cone_angle), n_sn = sinf(-e->cone_angle);
+    float3 pj_x1 = normalize3(f3(proj_x.x * n_cs - proj_x.y * n_sn, proj_x.x * n_sn + proj_x.y * n_cs, 0.0f));
+    float3 pj_x2 = normalize3(f3(proj_x.x * p_cs - proj_x.y * p_sn, proj_x.x * p_sn + proj_x.y * p_cs, 0.0f));
+    float3 pj_z1 = normalize3(f3(0.0f, proj_z.z * n_sn + proj_z.y * n_cs, proj_z.z * n_cs - proj_z.y * n_sn));
+    float3 pj_z2 = normalize3(f3(0.0f, proj_z.z * p_sn + proj_z.y * p_cs, proj_z.z * p_cs - proj_z.y * p_sn));
+    float interval = e->interval * signal * sc.y;
+    float yp = e->initial * signal * sc.y;
+    float vmin = sc.y * 0.5f, vmax = f.vol.grid.y - sc.y * 0.5f;
+    for (int guard = 0; guard < kMaxConeBoxes && (yp / c.y) < e->max_dist &&
+                        (pos.y + (yp + interval) > vmin && pos.y + (yp + interval) < vmax); ++guard) {
+      float ym = fabsf(yp + interval * 0.5f);
+      float px1 = pj_x1.x * (ym / fabsf(pj_x1.y)), px2 = pj_x2.x * (ym / fabsf(pj_x2.y));
+      float pz1 = pj_z1.z * (ym / fabsf(pj_z1.y)), pz2 = pj_z2.z * (ym / fabsf(pj_z2.y));
+      float x1 = fminf(px1, px2), x2 = fmaxf(px1, px2);
+      float z1 = fminf(pz1, pz2), z2 = fmaxf(pz1, pz2);
+      float xd = fabsf(x2 - x1), zd = fabsf(z2 - z1);
+      float xs = (ceilf(xd / sc.x) - (xd / sc.x)) * 0.5f;
+      float zs = (ceilf(zd / sc.z) - (zd / sc.z)) * 0.5f;
+      x1 = x1 - xs * sc.x; x2 = x2 + xs * sc.x;
+      z1 = z1 - zs * sc.z; z2 = z2 + zs * sc.z;
+      float y1 = fminf(yp, yp + interval), y2 = fmaxf(yp, yp + interval);
+      st += shadow_box(pos + f3(x1, y1, z1), pos + f3(x2, y2, z2), f);
+      ++aux;
+      yp = yp + interval;
+    }
+    return st;
+  }
+
+  // ConeXAxis (ebs_ray_bbox_marching.comp:352-430).
+  __device__ float cone_x(float3 pos, float3 c, const FrameArgs& f, unsigned& aux) const {
+    float3 sc = f.vol.spacing;
+    float st = 0.0f;
+    float signal = c.x < 0.0f ? -1.0f : 1.0f;
+    float3 proj_y = normalize3(f3(c.x, c.y, 0.0f));
+    float3 proj_z = normalize3(f3(c.x, 0.0f, c.z));
+    float p_cs = cosf(e->cone_angle), p_sn = sinf(e->cone_angle);
+    float n_cs = cosf(-e->cone_angle), n_sn = sinf(-e->cone_angle);
+    float3 pj_y1 = normalize3(f3(proj_y.y * n_sn + proj_y.x * n_cs, proj_y.y * n_cs - proj_y.x * n_sn, 0.0f));
+    float3 pj_y2 = normalize3(f3(proj_y.y * p_sn + proj_y.x * p_cs, proj_y.y * p_cs - proj_y.x * p_sn, 0.0f));
+    float3 pj_z1 = normalize3(f3(proj_z.z * n_sn + proj_z.x * n_cs, 0.0f, proj_z.z * n_cs - proj_z.x * n_sn));
+    float3 pj_z2 = normalize3(f3(proj_z.z * p_sn + proj_z.x * p_cs, 0.0f, proj_z.z * p_cs - proj_z.x * p_sn));
+    float interval = e->interval * signal * sc.x;
+    float xp = e->initial * signal * sc.x;
+    float vmin = sc.x * 0.5f, vmax = f.vol.grid.x - sc.x * 0.5f;
+    for (int guard = 0; guard < kMaxConeBoxes && (xp / c.x) < e->max_dist &&
+                        (pos.x + (xp + interval) > vmin && pos.x + (xp + interval) < vmax); ++guard) {
+      float xm = fabsf(xp + interval * 0.5f);
+      float py1 = pj_y1.y * (xm / fabsf(pj_y1.x)), py2 = pj_y2.y * (xm / fabsf(pj_y2.x));
+      float pz1 = pj_z1.z * (xm / fabsf(pj_z1.x)), pz2 = pj_z2.z * (xm / fabsf(pj_z2.x));
+      float y1 = fminf(py1, py2), y2 = fmaxf(py1, py2);
+      float z1 = fminf(pz1, pz2), z2 = fmaxf(pz1, pz2);
+      float yd = fabsf(y2 - y1), zd = fabsf(z2 - z1);
+      float ys = (ceilf(yd / sc.y) - (yd / sc.y)) * 0.5f;
+      float zs = (ceilf(zd / sc.z) - (zd / sc.z)) * 0.5f;
+      y1 = y1 - ys * sc.y; y2 = y2 + ys * sc.y;
+      z1 = z1 - zs * sc.z; z2 = z2 + zs * sc.z;
+      float x1 = fminf(xp, xp + interval), x2 = fmaxf(xp, xp + interval);
+      st += shadow_box(pos + f3(x1, y1, z1), pos + f3(x2, y2, z2), f);
+      ++aux;
+      xp = xp + interval;
+    }
+    return st;
+  }
+
+  // The Cone*Axis walk over the precomputed boxes of a directional light:
+  // same boxes, same CUT_WHEN_AWAY_FROM_VOLUME test, same sum.
+  __device__ float shadow_table(float3 tx, const FrameArgs& f, unsigned& aux) const {
+    const SatView& S = e->sat;
+    const float3 sc = f.vol.spacing;
+    const float pm = tax == 0 ? tx.x : (tax == 1 ? tx.y : tx.z);
+    float st = 0.0f;
+    for (int k = 0; k < tn; ++k) {
+      const float4 lo = tlo[k];
+      const float nxt = pm + (lo.w + tiw);
+      if (!(nxt > tvmin && nxt < tvmax)) break;
+      const float4 hi = thi[k];
+      float3 p1 = clamp3(tx + f3(lo.x, lo.y, lo.z) + sc, S.min_pos, S.max_pos);
+      float3 p2 = clamp3(tx + f3(hi.x, hi.y, hi.z) + sc, S.min_pos, S.max_pos);
+      st = fmaf(sat_box(S, p1, p2), hi.w, st);
+      ++aux;
+    }
+    return expf(-st);
+  }
+
+  // ExtinctionDirectionalShadows (ebs_ray_bbox_marching.comp:432-456).
+  __device__ float shadow(float3 tx, const FrameArgs& f, unsigned& aux) const {
+    float3 realpos = tx - f.vol.grid * 0.5f;
+    float3 c = (e->shadow_type == 0) ? normalize3(e->light_pos - realpos) : normalize3(e->light_fwd);
+    float3 a = abs3(c);
+    float st;
+    if (a.z > a.x && a.z > a.y) st = cone_z(tx, c, f, aux);
+    else if (a.y > a.x) st = cone_y(tx, c, f, aux);
+    else st = cone_x(tx, c, f, aux);
+    return expf(-st);
+  }
+
+  // ShadeSample, non-gradient branch (ebs_ray_bbox_marching.comp:500-551).
+  __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray&, const FrameArgs& f, unsigned& aux) const {
+    float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
+    if (e->apply_occ) { ka = e->ka; io = ambient_occlusion(tx, f); aux += e->n_shells; }
+    if (e->apply_sdw) { kd = e->kd; is = tlo ? shadow_table(tx, f, aux) : shadow(tx, f, aux); }
+    float k = 1.0f / (ka + kd);
+    src.x = k * (src.x * io * ka + src.x * is * kd);
+    src.y = k * (src.y * io * ka + src.y * is * kd);
+    src.z = k * (src.z * io * ka + src.z * is * kd);
+    return src;
+  }
+};
+
+// ==================================================== cone DOS (rc1pdosct)
+struct DosShade {
+  const DosArgs* d;
+  const float4* occ_tab;  // shared-memory copies of the section tables
+  const float4* sdw_tab;
+  struct Ray { float3 v_up, v_right; };
+
+  // main(), ray_bbox_marching.comp:682-684.
+  __device__ __forceinline__ void begin(Ray& r, float3 dir) const {
+    r.v_right = normalize3(cross3(dir, f3(0.0f, 1.0f, 0.0f)));
+    r.v_up = normalize3(cross3(-dir, r.v_right));
+  }
+
+  // GetGaussianExtinction with CONSIDER_BORDERS (ray_bbox_marching.comp:92-112).
+  __device__ __forceinline__ float gauss_ext(float3 p, float level, const FrameArgs& f) const {
+    float rg = pyr_sample(d->pyr, level, p);
+    float3 S = f.vol.grid;
+    if (p.x < 0.0f || p.x > S.x || p.y < 0.0f || p.y > S.y || p.z < 0.0f || p.z > S.z) {
+      float sg = exp2f(level);
+      float3 c = clamp3(p, f3(0.0f, 0.0f, 0.0f), S) - p;
+      float dist = c.x * c.x + c.y * c.y + c.z * c.z;
+      rg = rg * expf(-(dist) / (2.0f * sg * sg));
+    }
+    return rg;
+  }
+
+  // Cone1/3/7Ray{Occlusion,Shadow} (ray_bbox_marching.comp:124-322, 345-531):
+  // the same three-stage integration for both cones, parameterised by table.
+  __device__ float cone(const float4* tab, const ConeTableDev& T, float3 pos, float3 k, float3 u, float3 v,
+                        const FrameArgs& f, unsigned& aux) const {
+    aux += T.n1 + 3 * T.n3 + 7 * T.n7;
+    float rays[7], last[7];
+    float track = T.initial_step;
+    rays[0] = 0.0f; last[0] = 0.0f;
+    // Cone1Ray*: one sample per section.
+    for (int i = 0; i < T.n1; ++i) {
+      float4 s = tab[i];
+      float tau = gauss_ext(pos + k * track, s.y, f);
+      float amptau = tau * s.w;
+      rays[0] += (last[0] + amptau) * s.z * T.ui_weight;
+      last[0] = amptau;
+      track += s.x;
+    }
+    if (T.n3 + T.n7 == 0) return expf(-rays[0]);
+    // Cone3Ray*: transform 1 -> 3.
+    rays[2] = rays[0]; rays[1] = rays[0];
+    last[2] = last[0]; last[1] = last[0];
+    {
+      float3 vk[3];
+#pragma unroll
+      for (int r = 0; r < 3; ++r) vk[r] = k * T.axes[r].z + u * T.axes[r].y + v * T.axes[r].x;
+      for (int i = 0; i < T.n3; ++i) {
+        float4 s = tab[T.n1 + i];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+          float tau = gauss_ext(pos + vk[r] * track, s.y, f);
+          float amptau = tau * s.w;
+          rays[r] += (last[r] + amptau) * s.z * T.ui_weight;
+          last[r] = amptau;
+        }
+        track += s.x;
+      }
+    }
+    if (T.n7 == 0) return (expf(-rays[0]) + expf(-rays[1]) + expf(-rays[2])) / 3.0f;
+    // Cone7Ray*: transform 3 -> 7.
+    rays[6] = rays[5] = rays[2];
+    rays[4] = rays[3] = rays[1];
+    float avg = (rays[2] + rays[1] + rays[0]) / 3.0f;
+    rays[2] = rays[1] = rays[0];
+    rays[0] = avg;
+    last[6] = last[5] = last[2];
+    last[4] = last[3] = last[1];
+    float avgt = (last[2] + last[1] + last[0]) / 3.0f;
+    last[2] = last[1] = last[0];
+    last[0] = avgt;
+    float3 vk[7];
+#pragma unroll
+    for (int r = 0; r < 7; ++r) vk[r] = k * T.axes[3 + r].z + u * T.axes[3 + r].y + v * T.axes[3 + r].x;
+    int step0 = T.n1 + T.n3;
+    for (int i = 0; i < T.n7; ++i) {
+      float4 s = tab[step0 + i];
+#pragma unroll
+      for (int r = 0; r < 7; ++r) {
+        float tau = gauss_ext(pos + vk[r] * track, s.y, f);
+        float amptau = tau * s.w;
+        rays[r] += (last[r] + amptau) * s.z * T.ui_weight;
+        last[r] = amptau;
+      }
+      track += s.x;
+    }
+    return (expf(-rays[0]) + (expf(-rays[1]) + expf(-rays[2]) + expf(-rays[3]) + expf(-rays[4]) +
+                              expf(-rays[5]) + expf(-rays[6])) * T.w7) / (1.0f + T.w7 * 6.0f);
+  }
+
+  // OcclusionEvaluationKernel (ray_bbox_marching.comp:324-333).
+  __device__ __forceinline__ float occlusion(float3 tx, const Ray& r, const FrameArgs& f, unsigned& aux) const {
+    float3 realpos = tx - f.vol.grid * 0.5f;
+    float3 k = normalize3(f.cam.eye - realpos);
+    return cone(occ_tab, d->occ, tx, k, r.v_up, r.v_right, f, aux);
+  }
+
+  // ShadowEvaluationKernel (ray_bbox_marching.comp:533-562).  Cone1RayShadow
+  // declares its parameters as (pos, k, v, u) and is called with (pos, k, u, v),
+  // so the shadow cone works in the swapped frame; that is kept.
+  __device__ __forceinline__ float shadow(float3 tx, const FrameArgs& f, unsigned& aux) const {
+    float3 k, u, v;
+    if (d->shadow_type == 0 || d->shadow_type == 1) {
+      k = normalize3(d->light_pos - (tx - f.vol.grid * 0.5f));
+      u = normalize3(cross3(k, d->light_right));
+      v = normalize3(cross3(k, u));
+      if (d->shadow_type == 1 && dot3(k, d->light_fwd) < d->spot_cos_max) return 0.0f;
+    } else {
+      k = d->light_fwd; v = d->light_up; u = d->light_right;
+    }
+    return cone(sdw_tab, d->sdw, tx, k, v, u, f, aux);
+  }
+
+  // ShadeSample, non-gradient branch (ray_bbox_marching.comp:607-656).
+  __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray& r, const FrameArgs& f, unsigned& aux) const {
+    float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
+    if (d->apply_occ) { ka = d->ka; io = occlusion(tx, r, f, aux); }
+    if (d->apply_sdw) { kd = d->kd; is = shadow(tx, f, aux); }
+    float kk = 1.0f / (ka + kd);
+    src.x = kk * (src.x * io * ka + src.x * is * kd);
+    src.y = kk * (src.y * io * ka + src.y * is * kd);
+    src.z = kk * (src.z * io * ka + src.z * is * kd);
+    return src;
+  }
+};
+
+// ================================================= ground truth (rc1pcrtgt)
+struct GtShade {
+  const GtArgs* g;
+  const float4* tf;
+  int tf_n;
+  const float3* occ_vec;  // shared-memory copies
+  const float3* sdw_vec;
+  struct Ray { float3 dir, v_up, v_right; };
+
+  // main(), gt_ray_marching.comp:396-399.
+  __device__ __forceinline__ void begin(Ray& r, float3 dir) const {
+    r.dir = dir;
+    r.v_right = normalize3(cross3(dir, f3(0.0f, 1.0f, 0.0f)));
+    r.v_up = normalize3(cross3(-dir, r.v_right));
+  }
+
+  // One light ray of ConeOcclusion/ShadowsEvaluationRayCasting
+  // (gt_ray_marching.comp:125-159 and 209-242): trapezoidal transmittance.
+  __device__ float light_ray(float3 tx, float3 w, float dist, const FrameArgs& f, unsigned& aux) const {
+    float vt = 1.0f;
+    ++aux;
+    float s = g->gap;
+    float3 S = f.vol.grid;
+    float st0 = tf_alpha(tf, tf_n, sample_volume(f.vol, tx + w * s));
+    for (int guard = 0; guard < kMaxLightSteps && s < dist; ++guard) {
+      float h = fminf(g->lstep, dist - s);
+      float3 at = tx + w * (s + h);
+      if (at.x < 0.0f || at.x > S.x || at.y < 0.0f || at.y > S.y || at.z < 0.0f || at.z > S.z) break;
+      float st1 = tf_alpha(tf, tf_n, sample_volume(f.vol, at));
+      ++aux;
+      vt *= expf(-((st0 + st1) * 0.5f) * h);
+      if ((1.0f - vt) > 0.99f) break;
+      st0 = st1;
+      s = s + h;
+    }
+    return vt;
+  }
+
+  // ConeOcclusionEvaluationRayCasting (gt_ray_marching.comp:109-169).
+  __device__ float occlusion(float3 tx, const Ray& r, const FrameArgs& f, unsigned& aux) const {
+    float socc = 0.0f, swgt = 0.0f;
+    float3 vd = normalize3(-r.dir);
+    for (int i = 0; i < g->n_occ; ++i) {
+      float3 c = occ_vec[i];
+      float3 w = normalize3(r.v_right * c.x + r.v_up * c.y + vd * c.z);
+      float vt = light_ray(tx, w, g->occ_dist, f, aux);
+      float rw = dot3(vd, w);
+      socc += vt * rw;
+      swgt += rw;
+    }
+    return socc / swgt;
+  }
+
+  // ConeShadowsEvaluationRayCasting (gt_ray_marching.comp:171-252).
+  __device__ float shadow(float3 tx, const FrameArgs& f, unsigned& aux) const {
+    float3 wpos = tx - f.vol.grid * 0.5f;
+    float3 vd, vu, vr;
+    if (g->shadow_type == 0 || g->shadow_type == 1) {
+      vd = normalize3(g->light_pos - wpos);
+      vu = normalize3(cross3(vd, g->light_right));
+      vr = normalize3(cross3(vd, vu));
+      // The reference compares a cosine against 30.0 here, so spot lights always return 0.
+      if (g->shadow_type == 1 && dot3(vd, g->light_fwd) < 30.0f) return 0.0f;
+    } else {
+      vd = g->light_fwd; vu = g->light_up; vr = g->light_right;
+    }
+    float ssdw = 0.0f, swgt = 0.0f;
+    for (int i = 0; i < g->n_sdw; ++i) {
+      float3 c = sdw_vec[i];
+      float3 w = normalize3(vr * c.x + vu * c.y + vd * c.z);
+      float vt = light_ray(tx, w, g->sdw_dist, f, aux);
+      float rw = dot3(vd, w);
+      ssdw += vt * rw;
+      swgt += rw;
+    }
+    return ssdw / swgt;
+  }
+
+  // ShadeSample, non-gradient branch (gt_ray_marching.comp:254-303).
+  __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray& r, const FrameArgs& f, unsigned& aux) const {
+    float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
+    if (g->apply_occ) { ka = g->ka; io = occlusion(tx, r, f, aux); }
+    if (g->apply_sdw) { kd = g->kd; is = shadow(tx, f, aux); }
+    float kk = 1.0f / (ka + kd);
+    src.x = kk * (src.x * io * ka + src.x * is * kd);
+    src.y = kk * (src.y * io * ka + src.y * is * kd);
+    src.z = kk * (src.z * io * ka + src.z * is * kd);
+    return src;
+  }
+};
+
+// ============================================================ primary loop
+__device__ __forceinline__ void pixel_of(const FrameArgs& f, int& px, int& py) {
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int warps_x = f.tile_w >> 3;
+  px = blockIdx.x * f.tile_w + (warp % warps_x) * 8 + (lane & 7);
+  py = blockIdx.y * f.tile_h + (warp / warps_x) * 4 + (lane >> 3);
+}
+
+__device__ __forceinline__ void add_stats(const FrameArgs& f, unsigned int n, unsigned int shaded, unsigned int aux) {
+  unsigned long long a = n, b = shaded, c = aux;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0 && f.stats) {
+    atomicAdd(f.stats + 0, a);
+    atomicAdd(f.stats + 1, b);
+    atomicAdd(f.stats + 2, c);
+  }
+}
+
+// The a5 loop (ray_marching_1p.comp:170-247): h = min(StepSize, D - s),
+// sample at s + h/2, skip transparent samples, alpha = 1 - exp(-sigma h),
+// front-to-back composite, stop once alpha > 0.99.
+template <class Shade>
+__device__ __forceinline__ void march_pixel(const FrameArgs& f, const float4* tf, const Shade& sh) {
+  int px, py;
+  pixel_of(f, px, py);
+  bool inside = px < f.W && py < f.H;
+  unsigned int n = 0, shaded = 0, aux = 0;
+  if (inside) {
+    float3 dir = primary_dir(f.cam, px, py, f.W, f.H);
+    float tnear, tfar;
+    float4 dst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (ray_aabb(f.cam.eye, dir, f.vol.grid, tnear, tfar)) {
+      typename Shade::Ray ray;
+      sh.begin(ray, dir);
+      float D = fabsf(tfar - tnear);
+      float3 tex0 = f.cam.eye + dir * tnear + f.vol.grid * 0.5f;
+      // Bound on the step count (never reached for validated step sizes):
+      // keeps a loop whose s stops advancing from spinning forever.
+      const unsigned max_iter = (unsigned)fminf(D / f.step, 1.0e9f) + 4u;
+      for (float s = 0.0f; s < D && n < max_iter;) {
+        float h = fminf(f.step, D - s);
+        float3 p = tex0 + dir * (s + h * 0.5f);
+        float density = sample_volume(f.vol, p);
+        float4 src = tf_lookup(tf, f.tf_n, density);
+        ++n;
+        if (src.w > 0.0f) {
+          ++shaded;
+          src = sh.shade(src, p, ray, f, aux);
+          src.w = 1.0f - expf(-src.w * h);
+          src.x *= src.w; src.y *= src.w; src.z *= src.w;
+          float r = 1.0f - dst.w;
+          dst.x += r * src.x; dst.y += r * src.y; dst.z += r * src.z; dst.w += r * src.w;
+          if (dst.w > 0.99f) break;
+        }
+        s = s + h;
+      }
+    }
+    size_t o = (size_t)py * f.W + px;
+    f.out[o] = dst;
+    if (f.counts) f.counts[o] = n;
+  }
+  add_stats(f, n, shaded, aux);
+}
+
+// Loads the RGBt table into shared memory (n <= tf_smem_cap) and returns it.
+__device__ __forceinline__ const float4* stage_tf(const FrameArgs& f, float4* smem) {
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) smem[i] = f.tf[i];
+  return smem;
+}
+
+}  // namespace cvr

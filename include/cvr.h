@@ -279,7 +279,7 @@ cvr_status cvr_flush_l2(cvr_ctx* ctx);
 #define CVR_MLP_INPUTS 48
 #define CVR_MLP_HIDDEN 64
 #define CVR_MLP_OUTPUTS 2
-#define CVR_MLP_PARAMS 7362
+#define CVR_MLP_PARAMS 7426
 
 /* He-uniform weights from a seed, zero biases, fresh Adam state. */
 cvr_status cvr_mlp_init(cvr_ctx* ctx, uint64_t seed);

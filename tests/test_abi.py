@@ -134,3 +134,11 @@ def test_create_without_gpu_reports_cuda_error(lib):
     assert r in (abi.CVR_OK, abi.CVR_ERR_CUDA)
     if r == abi.CVR_ERR_CUDA:
         assert "CUDA" in code.stdout or "device" in code.stdout
+
+
+def test_mlp_parameter_count_matches_layout():
+    from oracle import mlp_ref
+    assert abi.MLP_PARAMS == mlp_ref.N_PARAMS == 64 * 48 + 64 + 64 * 64 + 64 + 2 * 64 + 2
+    import re
+    h = (abi.PKG.parent / "include" / "cvr.h").read_text()
+    assert int(re.search(r"#define CVR_MLP_PARAMS (\d+)", h).group(1)) == abi.MLP_PARAMS

@@ -45,9 +45,8 @@ def test_gradients_match_reference(ctx):
     ref, ref_loss = mlp_ref.gradients(p, X, T, bf=True)
     exact, exact_loss = mlp_ref.gradients(p, X, T, bf=False)
     assert abs(loss.value - ref_loss) <= 1e-3 * ref_loss
-    groups = {"W1": (0, 3072), "b1": (3072, 3136), "W2": (3136, 7232), "b2": (7232, 7296), "W3": (7296, 7424 - 0),
-              "b3": (7360, 7362)}
-    groups["W3"] = (7296, 7360)
+    groups = {"W1": (0, 3072), "b1": (3072, 3136), "W2": (3136, 7232), "b2": (7232, 7296), "W3": (7296, 7424),
+              "b3": (7424, 7426)}
     for name, (a, b) in groups.items():
         rel = np.linalg.norm(g[a:b] - ref[a:b]) / max(np.linalg.norm(ref[a:b]), 1e-12)
         assert rel <= 1e-2, (name, rel)
