@@ -58,7 +58,7 @@ def test_training_reduces_loss(ctx):
     lib = abi.load()
     abi.check(lib.cvr_mlp_init(ctx.h, 3), ctx.h)
     rng = np.random.default_rng(5)
-    n = 8192
+    n = 65536
     X = rng.normal(0, 1, size=(n, 48)).astype(np.float32)
     # a smooth target in [0, 1] of a few input features
     T = np.stack([1.0 / (1.0 + np.exp(-(X[:, 0] - 0.5 * X[:, 3]))), np.exp(-0.25 * X[:, 1] ** 2)], 1)
@@ -75,4 +75,5 @@ def test_training_reduces_loss(ctx):
     Yv = np.zeros((512, 2), np.float32)
     abi.check(lib.cvr_mlp_forward(ctx.h, abi.fptr(Xv), 512, abi.fptr(Yv)), ctx.h)
     rmse = float(np.sqrt(np.mean((Yv - Tv) ** 2)))
-    assert rmse < 0.1, rmse
+    baseline = float(np.sqrt(np.mean((Tv - T.mean(0)) ** 2)))  # predicting the training mean
+    assert rmse < 0.35 * baseline, (rmse, baseline)
