@@ -28,11 +28,13 @@ CVR_ERR_UNSUPPORTED = -9
 CVR_U8 = 1
 CVR_U16 = 2
 
-PLAIN, EXTINCTION, CONE_DOS, GROUND_TRUTH = 0, 1, 2, 3
+PLAIN, EXTINCTION, CONE_DOS, GROUND_TRUTH, SURROGATE = 0, 1, 2, 3, 4
 LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL = 0, 1, 2
 
 MAX_AO_SHELLS = 32
 MLP_PARAMS = 7426
+MLP_INPUTS = 48
+SURROGATE_LEVELS = 6
 MAX_CONE_SECTIONS = 512
 
 F3 = C.c_float * 3
@@ -85,7 +87,8 @@ class FrameStats(C.Structure):
                 ("kernel_ms", C.c_float)]
 
 
-PARAMS_OF_METHOD = {PLAIN: PlainParams, EXTINCTION: ExtParams, CONE_DOS: DosParams, GROUND_TRUTH: GtParams}
+PARAMS_OF_METHOD = {PLAIN: PlainParams, EXTINCTION: ExtParams, CONE_DOS: DosParams, GROUND_TRUTH: GtParams,
+                    SURROGATE: GtParams}
 
 _P = C.c_void_p
 _I = C.c_int
@@ -144,6 +147,15 @@ SIGNATURES = {
     "cvr_mlp_get_training_data": (_I, [_P, _FP, _FP, _I]),
     "cvr_mlp_training_size": (_I, [_P]),
     "cvr_mlp_train": (_I, [_P, _I, _I, _F, C.c_uint64, _FP]),
+    "cvr_mlp_save": (_I, [_P, C.c_char_p]),
+    "cvr_mlp_load": (_I, [_P, C.c_char_p]),
+    "cvr_surrogate_collect": (_I, [_P, C.POINTER(Camera), _I, _I, _F, _F, C.c_uint64, _I, C.POINTER(C.c_int)]),
+    "cvr_surrogate_clear_points": (_I, [_P]),
+    "cvr_surrogate_point_count": (_I, [_P]),
+    "cvr_surrogate_set_points": (_I, [_P, _FP, _I]),
+    "cvr_surrogate_get_points": (_I, [_P, _FP, _I]),
+    "cvr_surrogate_label": (_I, [_P, C.POINTER(Light), C.POINTER(GtParams), _I, _FP, _FP, _I]),
+    "cvr_surrogate_evaluate": (_I, [_P, C.POINTER(Light), C.POINTER(GtParams), C.POINTER(DosParams), _D]),
     "cvr_synth_value_noise": (_I, [_P, _I, _I, _I, _I, _I, _F, _F, _I, C.c_uint64]),
 }
 

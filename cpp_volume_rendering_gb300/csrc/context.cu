@@ -157,7 +157,7 @@ void cvr_destroy(cvr_ctx* c) {
 cvr_status cvr_sync(cvr_ctx* c) {
   if (!c) return CVR_ERR_INVALID_ARG;
   CK(c, cudaStreamSynchronize(c->stream));
-  return CVR_OK;
+  return mlp_check_err(c);  // a surrogate frame whose tensor-core wait gave up
 }
 
 void* cvr_stream(cvr_ctx* c) { return c ? (void*)c->stream : nullptr; }
@@ -488,6 +488,14 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
       e = launch_gt(f, a, c->stream);
       break;
     }
+    case CVR_METHOD_SURROGATE: {
+      if (params_size != sizeof(cvr_gt_params)) return fail(c, CVR_ERR_INVALID_ARG, "surrogate params size");
+      const cvr_gt_params* p = static_cast<const cvr_gt_params*>(params);
+      f.step = p->step_size;
+      cvr_status s = render_surrogate(c, f, p, light);
+      if (s != CVR_OK) return s;
+      break;
+    }
     default:
       return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: unknown method");
   }
@@ -503,6 +511,7 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
     stats->shaded_samples = hs[1];
     stats->aux_fetches = hs[2];
     stats->kernel_ms = ms;
+    if (method == CVR_METHOD_SURROGATE) return mlp_check_err(c);
   }
   return CVR_OK;
 }

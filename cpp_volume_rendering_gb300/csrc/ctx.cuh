@@ -40,12 +40,32 @@ struct MlpState {
   size_t io_cap = 0;
   cudaGraphExec_t epoch_graph = nullptr;
   int graph_batch = 0, graph_n = 0;
+  float graph_lr = 0.0f;
   bool ready = false;
   ~MlpState() {
     void* bufs[] = {params, m, v, packed, partials, grad, loss_acc, err, step, x, t, idx, io_x, io_y};
     for (void* p : bufs)
       if (p) cudaFree(p);
     if (epoch_graph) cudaGraphExecDestroy(epoch_graph);
+  }
+};
+
+// Shading points of the surrogate (training / evaluation) and its scratch.
+struct SurState {
+  float4* pts = nullptr;         // 2 float4 per point: position, direction
+  size_t pts_cap = 0;            // points
+  int n_pts = 0;
+  unsigned int* counter = nullptr;  // collection count / marcher ray counter
+  float* cx = nullptr;           // per-chunk features, targets, predictions, cone values
+  float* ct = nullptr;
+  float* cy = nullptr;
+  float* cd = nullptr;
+  size_t chunk_cap = 0;
+  double* acc = nullptr;         // error sums of cvr_surrogate_evaluate
+  ~SurState() {
+    void* bufs[] = {pts, counter, cx, ct, cy, cd, acc};
+    for (void* p : bufs)
+      if (p) cudaFree(p);
   }
 };
 
@@ -94,6 +114,7 @@ struct cvr_ctx {
   int tile_w = 16, tile_h = 8, variant = 0;
   std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
   std::unique_ptr<MlpState> mlp;             // surrogate network (created by cvr_mlp_init)
+  std::unique_ptr<SurState> sur;             // surrogate shading points
 };
 
 namespace cvr {
@@ -159,6 +180,14 @@ inline CameraView camera_view(const cvr_camera* cam, int w, int h) {
   return cv;
 }
 
+// Surrogate pieces shared between translation units.
+// Training-set slots for 'extra' more points (contents kept); *x / *t point
+// at the first new slot.  The caller bumps mlp->n once they are written.
+cvr_status mlp_reserve_training(cvr_ctx* c, size_t extra, float** x, float** t);
+// Reads and clears the network's device error flag (bounded tensor-core waits).
+cvr_status mlp_check_err(cvr_ctx* c);
+// The CVR_METHOD_SURROGATE launch of cvr_render.
+cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params* p, const cvr_light* light);
 
 }  // namespace ctxutil
 }  // namespace cvr

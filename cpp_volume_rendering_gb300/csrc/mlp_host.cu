@@ -192,8 +192,16 @@ cvr_status cvr_mlp_gradients(cvr_ctx* c, const float* x, const float* t, int n, 
 cvr_status cvr_mlp_set_training_data(cvr_ctx* c, const float* x, const float* t, int n) {
   cvr_status st = need_mlp(c);
   if (st != CVR_OK) return st;
-  if (!x || !t || n <= 0) return fail(c, CVR_ERR_INVALID_ARG, "cvr_mlp_set_training_data: bad arguments");
+  if (n < 0 || (n > 0 && (!x || !t))) return fail(c, CVR_ERR_INVALID_ARG, "cvr_mlp_set_training_data: bad arguments");
   MlpState& s = *c->mlp;
+  if (n == 0) {  // clears the training set
+    s.n = 0;
+    if (s.epoch_graph) {
+      cudaGraphExecDestroy(s.epoch_graph);
+      s.epoch_graph = nullptr;
+    }
+    return CVR_OK;
+  }
   if ((size_t)n > s.data_cap) {
     if (s.x) cudaFree(s.x);
     if (s.t) cudaFree(s.t);
@@ -238,8 +246,8 @@ cvr_status cvr_mlp_train(cvr_ctx* c, int epochs, int batch, float lr, uint64_t s
   const int n_batches = (n + batch - 1) / batch;
   CK(c, grow(s.idx, s.idx_cap, (size_t)n));
   CK(c, grow(s.partials, s.partials_cap, (size_t)(batch / 128) * (kMlpParams + 1)));
-  // (Re)capture the epoch when the batch structure changed.
-  if (!s.epoch_graph || s.graph_batch != batch || s.graph_n != n) {
+  // (Re)capture the epoch when the batch structure or the rate changed.
+  if (!s.epoch_graph || s.graph_batch != batch || s.graph_n != n || s.graph_lr != lr) {
     if (s.epoch_graph) {
       cudaGraphExecDestroy(s.epoch_graph);
       s.epoch_graph = nullptr;
@@ -262,6 +270,7 @@ cvr_status cvr_mlp_train(cvr_ctx* c, int epochs, int batch, float lr, uint64_t s
     if (e != cudaSuccess) return cuda_fail(c, e, "cvr_mlp_train: graph instantiate");
     s.graph_batch = batch;
     s.graph_n = n;
+    s.graph_lr = lr;
   }
   std::mt19937_64 rng(seed);
   std::vector<int> perm(n);
@@ -278,4 +287,103 @@ cvr_status cvr_mlp_train(cvr_ctx* c, int epochs, int batch, float lr, uint64_t s
   return check_err(c);
 }
 
+static const char kCkptMagic[8] = {'C', 'V', 'R', 'M', 'L', 'P', '0', '1'};
+
+cvr_status cvr_mlp_save(cvr_ctx* c, const char* path) {
+  cvr_status st = need_mlp(c);
+  if (st != CVR_OK) return st;
+  if (!path) return fail(c, CVR_ERR_INVALID_ARG, "cvr_mlp_save: null path");
+  MlpState& s = *c->mlp;
+  std::vector<float> buf(3 * (size_t)kMlpParams);
+  int step = 0;
+  CK(c, cudaMemcpyAsync(buf.data(), s.params, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(buf.data() + kMlpParams, s.m, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaMemcpyAsync(buf.data() + 2 * kMlpParams, s.v, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost,
+                        c->stream));
+  CK(c, cudaMemcpyAsync(&step, s.step, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return fail(c, CVR_ERR_IO, std::string("cvr_mlp_save: cannot open ") + path);
+  const uint32_t hdr[2] = {1u, (uint32_t)kMlpParams};
+  bool ok = std::fwrite(kCkptMagic, 1, 8, fp) == 8 && std::fwrite(hdr, sizeof hdr, 1, fp) == 1 &&
+            std::fwrite(buf.data(), sizeof(float), buf.size(), fp) == buf.size() &&
+            std::fwrite(&step, sizeof step, 1, fp) == 1;
+  ok = (std::fclose(fp) == 0) && ok;
+  return ok ? CVR_OK : fail(c, CVR_ERR_IO, std::string("cvr_mlp_save: write failed: ") + path);
+}
+
+cvr_status cvr_mlp_load(cvr_ctx* c, const char* path) {
+  if (!c || !path) return fail(c, CVR_ERR_INVALID_ARG, "cvr_mlp_load: bad arguments");
+  FILE* fp = std::fopen(path, "rb");
+  if (!fp) return fail(c, CVR_ERR_IO, std::string("cvr_mlp_load: cannot open ") + path);
+  char magic[8];
+  uint32_t hdr[2] = {0, 0};
+  std::vector<float> buf(3 * (size_t)kMlpParams);
+  int step = 0;
+  bool ok = std::fread(magic, 1, 8, fp) == 8 && std::fread(hdr, sizeof hdr, 1, fp) == 1;
+  if (ok && (std::memcmp(magic, kCkptMagic, 8) != 0 || hdr[0] != 1u || hdr[1] != (uint32_t)kMlpParams)) {
+    std::fclose(fp);
+    return fail(c, CVR_ERR_FORMAT, std::string("cvr_mlp_load: not a version-1 checkpoint of this network: ") + path);
+  }
+  ok = ok && std::fread(buf.data(), sizeof(float), buf.size(), fp) == buf.size() &&
+       std::fread(&step, sizeof step, 1, fp) == 1;
+  std::fclose(fp);
+  if (!ok) return fail(c, CVR_ERR_FORMAT, std::string("cvr_mlp_load: truncated checkpoint: ") + path);
+  cvr_status st = cvr_mlp_set_params(c, buf.data(), kMlpParams);  // also resets the optimiser
+  if (st != CVR_OK) return st;
+  MlpState& s = *c->mlp;
+  CK(c, cudaMemcpyAsync(s.m, buf.data() + kMlpParams, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaMemcpyAsync(s.v, buf.data() + 2 * kMlpParams, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice,
+                        c->stream));
+  CK(c, cudaMemcpyAsync(s.step, &step, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  return CVR_OK;
+}
+
 }  // extern "C"
+
+namespace cvr {
+namespace ctxutil {
+
+cvr_status mlp_check_err(cvr_ctx* c) { return (c && c->mlp && c->mlp->err) ? check_err(c) : CVR_OK; }
+
+cvr_status mlp_reserve_training(cvr_ctx* c, size_t extra, float** x, float** t) {
+  cvr_status st = need_mlp(c);
+  if (st != CVR_OK) return st;
+  MlpState& s = *c->mlp;
+  size_t need = (size_t)s.n + extra;
+  if (need > (size_t)0x7fffffff) return fail(c, CVR_ERR_INVALID_ARG, "training set larger than 2^31 points");
+  if (need > s.data_cap) {
+    size_t cap = std::max(need, s.data_cap + s.data_cap / 2);
+    float* nx = nullptr;
+    float* nt = nullptr;
+    cudaError_t e = cudaMalloc((void**)&nx, sizeof(float) * 48 * cap);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&nt, sizeof(float) * 2 * cap);
+    if (e == cudaSuccess && s.n > 0) {
+      e = cudaMemcpyAsync(nx, s.x, sizeof(float) * 48 * (size_t)s.n, cudaMemcpyDeviceToDevice, c->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(nt, s.t, sizeof(float) * 2 * (size_t)s.n, cudaMemcpyDeviceToDevice, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    }
+    if (e != cudaSuccess) {
+      if (nx) cudaFree(nx);
+      if (nt) cudaFree(nt);
+      return cuda_fail(c, e, "training set allocation");
+    }
+    if (s.x) cudaFree(s.x);
+    if (s.t) cudaFree(s.t);
+    s.x = nx;
+    s.t = nt;
+    s.data_cap = cap;
+  }
+  if (s.epoch_graph) {  // the graph captured the old buffers
+    cudaGraphExecDestroy(s.epoch_graph);
+    s.epoch_graph = nullptr;
+  }
+  *x = s.x + 48 * (size_t)s.n;
+  *t = s.t + 2 * (size_t)s.n;
+  return CVR_OK;
+}
+
+}  // namespace ctxutil
+}  // namespace cvr

@@ -74,7 +74,7 @@ __device__ __forceinline__ void sync_tiles() {
 
 // Forward of the 128-point tile whose input rows are in s.x; returns this
 // thread's two outputs.  Must be called by all 128 threads.
-__device__ bool mlp_forward_tile(MlpSmem& s, float y[2]) {
+__device__ __forceinline__ bool mlp_forward_tile(MlpSmem& s, float y[2]) {
   const float* bias = reinterpret_cast<const float*>(s.w + kPkBias);
   bool ok = true;
   float h[64];

@@ -1,0 +1,281 @@
+// surrogate.cu — shading-point collection, feature/target labelling and the
+// surrogate-shaded marcher (network inference fused into the ray loop).
+#include "mlp_tile.cuh"
+#include "shade.cuh"
+#include "surrogate.cuh"
+
+namespace cvr {
+
+// ---------------------------------------------------------------- collection
+__device__ __forceinline__ float keep_hash(unsigned long long seed, unsigned pixel, unsigned step) {
+  unsigned long long z = seed + 0x9E3779B97F4A7C15ull * ((unsigned long long)pixel * 0x100000001ull + step + 1ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// The a5 loop of march_pixel with the opacity composite only (shading does
+// not change alpha, so the same samples are reached and the same ray stops).
+__global__ void __launch_bounds__(128) k_sur_collect(FrameArgs f, float rate, unsigned long long seed, float4* pts,
+                                                     int cap, unsigned int* count) {
+  extern __shared__ float4 sm_col[];
+  float4* tf = sm_col;
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
+  __syncthreads();
+  int px, py;
+  pixel_of(f, px, py);
+  if (px >= f.W || py >= f.H) return;
+  float3 dir = primary_dir(f.cam, px, py, f.W, f.H);
+  float tnear, tfar;
+  if (!ray_aabb(f.cam.eye, dir, f.vol.grid, tnear, tfar)) return;
+  const unsigned pixel = (unsigned)(py * f.W + px);
+  float D = fabsf(tfar - tnear);
+  float3 tex0 = f.cam.eye + dir * tnear + f.vol.grid * 0.5f;
+  const unsigned max_iter = (unsigned)fminf(D / f.step, 1.0e9f) + 4u;
+  float dw = 0.0f;
+  unsigned n = 0;
+  for (float s = 0.0f; s < D && n < max_iter;) {
+    float h = fminf(f.step, D - s);
+    float3 p = tex0 + dir * (s + h * 0.5f);
+    float4 src = tf_lookup(tf, f.tf_n, sample_volume(f.vol, p));
+    ++n;
+    if (src.w > 0.0f) {
+      if (keep_hash(seed, pixel, n) < rate) {
+        unsigned idx = atomicAdd(count, 1u);
+        if (idx < (unsigned)cap) {
+          pts[2 * (size_t)idx] = make_float4(p.x, p.y, p.z, 0.0f);
+          pts[2 * (size_t)idx + 1] = make_float4(dir.x, dir.y, dir.z, 0.0f);
+        }
+      }
+      float a = 1.0f - expf(-src.w * h);
+      float r = 1.0f - dw;
+      dw += r * a;
+      if (dw > 0.99f) break;
+    }
+    s = s + h;
+  }
+}
+
+cudaError_t launch_sur_collect(const FrameArgs& f, float rate, unsigned long long seed, float4* pts, int cap,
+                               unsigned int* count, cudaStream_t st) {
+  dim3 grid((f.W + f.tile_w - 1) / f.tile_w, (f.H + f.tile_h - 1) / f.tile_h, 1);
+  k_sur_collect<<<grid, 128, sizeof(float4) * f.tf_n, st>>>(f, rate, seed, pts, cap, count);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- labelling
+__global__ void __launch_bounds__(128) k_sur_label(const float4* __restrict__ pts, int n, FrameArgs f, SurArgs a,
+                                                   GtArgs g, DosArgs d, int want_gt, int want_dos,
+                                                   float* __restrict__ x_out, float* __restrict__ t_out,
+                                                   float* __restrict__ dos_out) {
+  extern __shared__ float4 sm_lab[];
+  float4* tf = sm_lab;
+  float4* occ_tab = tf + f.tf_n;
+  float4* sdw_tab = occ_tab + (want_dos ? d.occ.n_sections : 0);
+  float3* ov = reinterpret_cast<float3*>(sdw_tab + (want_dos ? d.sdw.n_sections : 0));
+  float3* sv = ov + (want_gt ? g.n_occ : 0);
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
+  if (want_dos) {
+    for (int i = threadIdx.x; i < d.occ.n_sections; i += blockDim.x) occ_tab[i] = d.occ_sections[i];
+    for (int i = threadIdx.x; i < d.sdw.n_sections; i += blockDim.x) sdw_tab[i] = d.sdw_sections[i];
+  }
+  if (want_gt) {
+    for (int i = threadIdx.x; i < g.n_occ; i += blockDim.x) ov[i] = g.occ_vec[i];
+    for (int i = threadIdx.x; i < g.n_sdw; i += blockDim.x) sv[i] = g.sdw_vec[i];
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float4 P = pts[2 * (size_t)i], Q = pts[2 * (size_t)i + 1];
+  float3 tx = f3(P.x, P.y, P.z), dir = f3(Q.x, Q.y, Q.z);
+  if (x_out) {
+    float x[kMlpIn];
+    sur_features(a, f.vol, tf, f.tf_n, tx, dir, x);
+    float4* o = reinterpret_cast<float4*>(x_out + (size_t)i * kMlpIn);
+#pragma unroll
+    for (int k = 0; k < kMlpIn / 4; ++k) o[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+  }
+  unsigned aux = 0;
+  if (want_gt) {
+    GtShade sh{&g, tf, f.tf_n, ov, sv};
+    GtShade::Ray r;
+    sh.begin(r, dir);
+    t_out[2 * (size_t)i] = sh.occlusion(tx, r, f, aux);
+    t_out[2 * (size_t)i + 1] = sh.shadow(tx, f, aux);
+  }
+  if (want_dos) {
+    // The cone method aims its occlusion cone at the eye; any eye on the ray
+    // behind the point gives the same axis.
+    FrameArgs fl = f;
+    fl.cam.eye = (tx - f.vol.grid * 0.5f) - dir;
+    DosShade ds{&d, occ_tab, sdw_tab};
+    DosShade::Ray r;
+    ds.begin(r, dir);
+    dos_out[2 * (size_t)i] = ds.occlusion(tx, r, fl, aux);
+    dos_out[2 * (size_t)i + 1] = ds.shadow(tx, fl, aux);
+  }
+}
+
+cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const SurArgs& a, const GtArgs* g,
+                             const DosArgs* d, float* x_out, float* t_out, float* dos_out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  GtArgs gg = g ? *g : GtArgs{};
+  DosArgs dd = d ? *d : DosArgs{};
+  const int want_gt = g && t_out ? 1 : 0, want_dos = d && dos_out ? 1 : 0;
+  size_t sm = sizeof(float4) * f.tf_n;
+  if (want_dos) sm += sizeof(float4) * (dd.occ.n_sections + dd.sdw.n_sections);
+  if (want_gt) sm += sizeof(float3) * (gg.n_occ + gg.n_sdw);
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_sur_label, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  k_sur_label<<<(n + 127) / 128, 128, sm, st>>>(pts, n, f, a, gg, dd, want_gt, want_dos, x_out, t_out, dos_out);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------- fused marcher
+// Next ray index for every active lane of a warp with one atomic.
+__device__ __forceinline__ unsigned take_ray(unsigned int* work) {
+  const unsigned m = __activemask();
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(work, (unsigned)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + (unsigned)__popc(m & ((1u << lane) - 1u));
+}
+
+struct SurRay {
+  float3 dir, tex0;
+  float D, s;
+  float4 dst;
+  unsigned n, max_iter;
+  int px, py;
+};
+
+__device__ __forceinline__ void sur_finish(const FrameArgs& f, const SurRay& r, unsigned& n_all) {
+  size_t o = (size_t)r.py * f.W + r.px;
+  f.out[o] = r.dst;
+  if (f.counts) f.counts[o] = r.n;
+  n_all += r.n;
+}
+
+__global__ void __launch_bounds__(128, 3) k_march_surrogate(FrameArgs f, SurArgs a, unsigned int* work, int* err) {
+  extern __shared__ __align__(1024) uint8_t sm_sur[];
+  uint8_t* w = sm_sur;
+  uint8_t* xt = w + kPkBytes;
+  uint8_t* ht = xt + kRowTile;
+  float4* tf = reinterpret_cast<float4*>(ht + kRowTile);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tf + f.tf_n);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  mlp_cta_begin(w, a.packed, bar, tslot);
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
+  fence_async_smem();
+  __syncthreads();
+  MlpSmem ms{w, xt, ht, bar, *tslot, 0u};
+
+  const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2;
+  const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
+  SurRay ray{};
+  bool has_ray = false, pending = false, no_work = false;
+  float4 src = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  float3 p = f3(0.0f, 0.0f, 0.0f);
+  float h = 0.0f;
+  unsigned n_all = 0, shaded = 0;
+  while (true) {
+    // Advance this thread's ray to its next shaded sample, taking new rays
+    // as rays end, until a sample is pending or the frame has no rays left.
+    while (!pending && !no_work) {
+      if (!has_ray) {
+        unsigned idx = take_ray(work);
+        if (idx >= total) { no_work = true; break; }
+        int tile = (int)(idx >> 5), within = (int)(idx & 31u);
+        ray.px = (tile % tiles_x) * 8 + (within & 7);
+        ray.py = (tile / tiles_x) * 4 + (within >> 3);
+        if (ray.px >= f.W || ray.py >= f.H) continue;
+        ray.dir = primary_dir(f.cam, ray.px, ray.py, f.W, f.H);
+        ray.dst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        ray.n = 0;
+        float tnear, tfar;
+        if (!ray_aabb(f.cam.eye, ray.dir, f.vol.grid, tnear, tfar)) {
+          sur_finish(f, ray, n_all);
+          continue;
+        }
+        ray.D = fabsf(tfar - tnear);
+        ray.tex0 = f.cam.eye + ray.dir * tnear + f.vol.grid * 0.5f;
+        ray.s = 0.0f;
+        ray.max_iter = (unsigned)fminf(ray.D / f.step, 1.0e9f) + 4u;
+        has_ray = true;
+      }
+      while (ray.s < ray.D && ray.n < ray.max_iter) {
+        h = fminf(f.step, ray.D - ray.s);
+        p = ray.tex0 + ray.dir * (ray.s + h * 0.5f);
+        src = tf_lookup(tf, f.tf_n, sample_volume(f.vol, p));
+        ++ray.n;
+        if (src.w > 0.0f) { pending = true; break; }
+        ray.s = ray.s + h;
+      }
+      if (!pending) {
+        sur_finish(f, ray, n_all);
+        has_ray = false;
+      }
+    }
+    if (!__syncthreads_or(pending)) break;
+    {
+      float x[kMlpIn];
+      if (pending) {
+        sur_features(a, f.vol, tf, f.tf_n, p, ray.dir, x);
+      } else {
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) x[k] = 0.0f;
+      }
+      store_row64(xt, threadIdx.x, x, kMlpIn);
+    }
+    sync_tiles();
+    float y[2];
+    bool ok = mlp_forward_tile(ms, y);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) atomicExch(err, 1);
+      break;
+    }
+    if (pending) {
+      ++shaded;
+      pending = false;
+      src = sur_shade(a, src, y[0], y[1]);
+      src.w = 1.0f - expf(-src.w * h);
+      src.x *= src.w; src.y *= src.w; src.z *= src.w;
+      float r = 1.0f - ray.dst.w;
+      ray.dst.x += r * src.x; ray.dst.y += r * src.y; ray.dst.z += r * src.z; ray.dst.w += r * src.w;
+      if (ray.dst.w > 0.99f) {
+        sur_finish(f, ray, n_all);
+        has_ray = false;
+      } else {
+        ray.s = ray.s + h;
+      }
+    }
+  }
+  add_stats(f, n_all, shaded, shaded * (unsigned)(kSurTapFeatures + 6));
+  mlp_cta_end(ms.tmem);
+}
+
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, unsigned int* work, int* err, cudaStream_t st) {
+  const size_t smem = kPkBytes + 2 * kRowTile + sizeof(float4) * f.tf_n + 16;
+  cudaError_t e = cudaFuncSetAttribute(k_march_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_surrogate, 128, smem)) != cudaSuccess)
+    return e;
+  // TMEM: 128 columns per CTA, 512 per SM.
+  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+  long long groups = ((long long)((f.W + 7) / 8) * ((f.H + 3) / 4) * 32 + 127) / 128;
+  long long ctas = (long long)sms * per_sm;
+  if (ctas > groups) ctas = groups;
+  if (ctas < 1) ctas = 1;
+  k_march_surrogate<<<(unsigned)ctas, 128, smem, st>>>(f, a, work, err);
+  return cudaGetLastError();
+}
+
+}  // namespace cvr

@@ -1,0 +1,130 @@
+// surrogate.cuh — the learned stand-in for the ground-truth light integrals of
+// RC1PConeLightGroundTruthSteps (gt_ray_marching.comp:109-252): a feature
+// vector of multi-level extinction samples around a shading point, the light
+// direction and the local extinction gradient, mapped by the MLP of mlp.cuh
+// to (ambient occlusion, shadow).
+//
+// Features at a shading point tx (texture-space position in [0, S]) of a
+// primary ray with direction dir:
+//   frame  n = -dir, r = normalize(dir x (0,1,0)), u = normalize(-dir x r)
+//          (the (v_right, v_up, -dir) frame of the ground-truth occlusion
+//          kernel, gt_ray_marching.comp:396-399)
+//   light  L = normalize(light_pos - world(tx)) for point and spot lights,
+//          L = light forward vector for directional lights
+//   taps   for level l = 0..5, d_l = unit * 2^(l+1) (unit = mean voxel
+//          spacing), offsets {0, L, 3L, n, 3n, r, u} * d_l:
+//          x[7l + k] = 1 - exp(-sigma_l(tx + offset_k) * d_l), where sigma_l
+//          is level l of the Gaussian extinction pyramid (trilinear within
+//          the level) and 0 outside the volume box
+//   x[42..44] = (L.r, L.u, L.n)
+//   x[45..47] = (g.r, g.u, g.n), g = central differences of the transfer
+//               function extinction at +-1 voxel (per voxel)
+// The same routine produces training inputs and the marcher's inputs.
+#pragma once
+
+#include "march.cuh"
+#include "mlp.cuh"
+
+namespace cvr {
+
+constexpr int kSurLevels = 6;
+constexpr int kSurTaps = 7;
+constexpr int kSurTapFeatures = kSurLevels * kSurTaps;  // 42
+
+struct SurArgs {
+  PyramidView pyr;  // at least kSurLevels levels
+  const uint8_t* packed;  // packed network image (mlp.cuh)
+  int apply_occ, apply_sdw, shadow_type;
+  float3 light_pos, light_fwd;
+  float ka, kd;
+  float unit;  // world length of one voxel (mean spacing)
+};
+
+struct SurFrame { float3 n, r, u, L; };
+
+__device__ __forceinline__ SurFrame sur_frame(const SurArgs& a, float3 tx, float3 dir, float3 grid) {
+  SurFrame F;
+  F.n = normalize3(-dir);
+  float3 c = cross3(dir, f3(0.0f, 1.0f, 0.0f));
+  // A ray parallel to y has no right vector; any perpendicular frame will do.
+  if (dot3(c, c) < 1.0e-12f) c = f3(1.0f, 0.0f, 0.0f);
+  F.r = normalize3(c);
+  F.u = normalize3(cross3(-dir, F.r));
+  F.L = a.shadow_type == 2 ? a.light_fwd : normalize3(a.light_pos - (tx - grid * 0.5f));
+  return F;
+}
+
+// Segment opacity 1 - exp(-sigma_l(q) d) of one tap; 0 outside the box.
+__device__ __forceinline__ float sur_tap(const PyramidView& P, int l, float3 q, float d, float3 S) {
+  if (q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) return 0.0f;
+  return 1.0f - expf(-pyr_sample_level(P, l, q) * d);
+}
+
+// The 48 features of one shading point (layout above).
+__device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView& vol, const float4* tf, int tf_n,
+                                             float3 tx, float3 dir, float* x) {
+  const float3 S = vol.grid;
+  SurFrame F = sur_frame(a, tx, dir, S);
+  float d = a.unit * 2.0f;
+#pragma unroll
+  for (int l = 0; l < kSurLevels; ++l) {
+    x[7 * l + 0] = sur_tap(a.pyr, l, tx, d, S);
+    x[7 * l + 1] = sur_tap(a.pyr, l, tx + F.L * d, d, S);
+    x[7 * l + 2] = sur_tap(a.pyr, l, tx + F.L * (3.0f * d), d, S);
+    x[7 * l + 3] = sur_tap(a.pyr, l, tx + F.n * d, d, S);
+    x[7 * l + 4] = sur_tap(a.pyr, l, tx + F.n * (3.0f * d), d, S);
+    x[7 * l + 5] = sur_tap(a.pyr, l, tx + F.r * d, d, S);
+    x[7 * l + 6] = sur_tap(a.pyr, l, tx + F.u * d, d, S);
+    d *= 2.0f;
+  }
+  x[42] = dot3(F.L, F.r);
+  x[43] = dot3(F.L, F.u);
+  x[44] = dot3(F.L, F.n);
+  const float3 sp = vol.spacing;
+  float3 g;
+  g.x = 0.5f * (tf_alpha(tf, tf_n, sample_volume(vol, tx + f3(sp.x, 0.0f, 0.0f))) -
+                tf_alpha(tf, tf_n, sample_volume(vol, tx - f3(sp.x, 0.0f, 0.0f))));
+  g.y = 0.5f * (tf_alpha(tf, tf_n, sample_volume(vol, tx + f3(0.0f, sp.y, 0.0f))) -
+                tf_alpha(tf, tf_n, sample_volume(vol, tx - f3(0.0f, sp.y, 0.0f))));
+  g.z = 0.5f * (tf_alpha(tf, tf_n, sample_volume(vol, tx + f3(0.0f, 0.0f, sp.z))) -
+                tf_alpha(tf, tf_n, sample_volume(vol, tx - f3(0.0f, 0.0f, sp.z))));
+  x[45] = dot3(g, F.r);
+  x[46] = dot3(g, F.u);
+  x[47] = dot3(g, F.n);
+}
+
+// Shading of the ground-truth renderer with the network's outputs in place of
+// the light integrals (ShadeSample, gt_ray_marching.comp:254-303).  Spot
+// lights shadow everything there (the cosine is compared against 30.0), so
+// the shadow term is 0 for them here as well.
+__device__ __forceinline__ float4 sur_shade(const SurArgs& a, float4 src, float ao, float sdw) {
+  float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
+  if (a.apply_occ) { ka = a.ka; io = fminf(fmaxf(ao, 0.0f), 1.0f); }
+  if (a.apply_sdw) { kd = a.kd; is = a.shadow_type == 1 ? 0.0f : fminf(fmaxf(sdw, 0.0f), 1.0f); }
+  float kk = 1.0f / (ka + kd);
+  src.x = kk * (src.x * io * ka + src.x * is * kd);
+  src.y = kk * (src.y * io * ka + src.y * is * kd);
+  src.z = kk * (src.z * io * ka + src.z * is * kd);
+  return src;
+}
+
+// Shading points of primary rays: each shaded sample (the samples that reach
+// ShadeSample) is kept with probability 'rate' (a hash of seed, pixel and step),
+// appended as {position, 0}, {direction, 0}.  *count is the number kept
+// (it may exceed cap; only the first cap are written).
+cudaError_t launch_sur_collect(const FrameArgs& f, float rate, unsigned long long seed, float4* pts, int cap,
+                               unsigned int* count, cudaStream_t st);
+
+// Features (n x 48), ground-truth targets (n x 2: GtShade occlusion and
+// shadow) and, when dos_out is given, the cone method's (occlusion, shadow)
+// of n points.  f supplies the volume and transfer function.
+cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const SurArgs& a, const GtArgs* g,
+                             const DosArgs* d, float* x_out, float* t_out, float* dos_out, cudaStream_t st);
+
+// The surrogate-shaded marcher: persistent CTAs take 8x4-pixel blocks of rays
+// from *work (zeroed before the launch); every round, each thread advances
+// its ray to the next shaded sample, the CTA evaluates the network for its
+// 128 samples on the tensor cores, and each thread composites its sample.
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, unsigned int* work, int* err, cudaStream_t st);
+
+}  // namespace cvr

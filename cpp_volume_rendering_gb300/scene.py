@@ -283,6 +283,60 @@ class Context:
         self._ck(self.lib.cvr_set_gt_kernels(self.h, abi.fptr(np.ascontiguousarray(occ)), len(occ),
                                              abi.fptr(np.ascontiguousarray(sdw)), len(sdw)))
 
+    # ---- surrogate network and shading points
+    def mlp_init(self, seed: int):
+        self._ck(self.lib.cvr_mlp_init(self.h, seed))
+
+    def mlp_params(self) -> np.ndarray:
+        p = np.zeros(abi.MLP_PARAMS, np.float32)
+        self._ck(self.lib.cvr_mlp_get_params(self.h, abi.fptr(p), abi.MLP_PARAMS))
+        return p
+
+    def mlp_set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, np.float32)
+        self._ck(self.lib.cvr_mlp_set_params(self.h, abi.fptr(p), len(p)))
+
+    def collect_points(self, cam, w, h, step, rate, seed, max_points) -> int:
+        n = C.c_int()
+        self._ck(self.lib.cvr_surrogate_collect(self.h, C.byref(cam), w, h, step, rate, seed, max_points,
+                                                C.byref(n)))
+        return n.value
+
+    def clear_points(self):
+        self._ck(self.lib.cvr_surrogate_clear_points(self.h))
+
+    def point_count(self) -> int:
+        return self.lib.cvr_surrogate_point_count(self.h)
+
+    def points(self) -> np.ndarray:
+        n = self.point_count()
+        out = np.zeros((n, 6), np.float32)
+        self._ck(self.lib.cvr_surrogate_get_points(self.h, abi.fptr(out), n))
+        return out
+
+    def set_points(self, pts: np.ndarray):
+        pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 6)
+        self._ck(self.lib.cvr_surrogate_set_points(self.h, abi.fptr(pts), len(pts)))
+
+    def label_points(self, lt, gt_params, append_training=False, download=True):
+        """Features (n x 48) and GT targets (n x 2) of the point list."""
+        n = self.point_count()
+        x = np.zeros((n, 48), np.float32) if download else None
+        t = np.zeros((n, 2), np.float32) if download else None
+        self._ck(self.lib.cvr_surrogate_label(self.h, C.byref(lt), C.byref(gt_params), int(append_training),
+                                              abi.fptr(x) if download else None, abi.fptr(t) if download else None,
+                                              n))
+        return x, t
+
+    def evaluate_points(self, lt, gt_params, cone_params=None) -> dict:
+        out = np.zeros(8, np.float64)
+        self._ck(self.lib.cvr_surrogate_evaluate(self.h, C.byref(lt), C.byref(gt_params),
+                                                 C.byref(cone_params) if cone_params is not None else None,
+                                                 abi.dptr(out)))
+        keys = ("rmse_ao", "rmse_shadow", "cone_rmse_ao", "cone_rmse_shadow", "points", "mean_ao",
+                "mean_shadow", "max_err_ao")
+        return dict(zip(keys, out.tolist()))
+
     def render(self, method, cam, lt, params, w, h, stats=True):
         """Renders into host memory; returns (H x W x 4 float32 image, FrameStats)."""
         out = np.zeros((h, w, 4), np.float32)
@@ -338,6 +392,9 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     ground_truth / cone : 256^3 u8, 32 blobs + U[0,20] background; GT with 16
                  occlusion rays (90 deg, 32 voxels) and 1 shadow ray to a point
                  light at 1-voxel steps; cone method on a 5-level pyramid, 512^2
+    surrogate  : held-out 512^3 u8 of the same blob generator (seed 4020), the
+                 ground-truth camera, light and integrator parameters, network
+                 inputs on a 6-level pyramid of base n/2, 1024^2
     """
     if name == "plain":
         n = n or 64
@@ -384,6 +441,12 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
             base = max(1, n // 2)
             wl.pyramid = dict(base_dims=(base, base, base), sigma0=1.0, n_levels=5)
         return wl
+    if name == "surrogate":
+        n = n or 512
+        image = image or 1024
+        vol = synth_blobs(n, n, n, abi.CVR_U8, 32, seed=SURROGATE_SEED + SURROGATE_VOLUMES, noise_max=20.0)
+        wl = surrogate_workload(vol, image)
+        return wl
     raise KeyError(name)
 
 
@@ -398,3 +461,126 @@ def prepare(ctx: Context, wl: Workload):
         ctx.set_cone_tables(*wl.cones)
     if wl.method == abi.GROUND_TRUTH:
         ctx.set_gt_kernels(*wl.gt)
+    if wl.method == abi.SURROGATE:
+        ctx.build_pyramid(**wl.pyramid)
+        ctx.set_gt_kernels(*wl.gt)
+        ctx.set_cone_tables(*wl.cones)
+
+
+# ---------------------------------------------------------------- surrogate
+# Training data: shading points of random views of SURROGATE_VOLUMES seeded
+# blob volumes (the ground-truth workload's generator, seeds 4000..4019),
+# labelled by the ground-truth integrator with the ground-truth workload's
+# parameters (16 occlusion rays of 32 voxels over 90 degrees, 1 shadow ray,
+# 1-voxel light steps); half the views use a point light, half a directional.
+SURROGATE_SEED = 4000
+SURROGATE_VOLUMES = 20
+
+
+def surrogate_workload(vol: np.ndarray, image: int, spacing=(1.0, 1.0, 1.0)) -> Workload:
+    """Surrogate shading of a blob volume with the ground-truth workload's camera,
+    point light and integrator parameters; the pyramid (base n/2, 6 levels),
+    GT kernel vectors and cone tables (for the comparison) it needs."""
+    d, h, w = vol.shape
+    n = max(w, h, d)
+    cam = camera(orbit_eye(3.0 * n, -30.0, 20.0), fovy=30.0)
+    lpos = tuple(2.0 * n * _norm((-0.5, 1.0, 0.4)))
+    fwd, up, right = light_frame(lpos)
+    lt = light(abi.LIGHT_POINT, position=lpos, forward=fwd, up=up, right=right)
+    wl = Workload("surrogate", abi.SURROGATE, vol, tuple(spacing), BENCH_TF, cam, lt, None, image, image)
+    diag = wl.diagonal
+    wl.params = gt_params(default_step(spacing), diag, occ_distance=32.0, light_step=1.0, gap=1.0, shadow_type=0)
+    wl.gt = gt_vectors(16, 90.0, 1, 0.0, seed=1)
+    wl.pyramid = dict(base_dims=(max(1, w // 2), max(1, h // 2), max(1, d // 2)), sigma0=1.0,
+                      n_levels=abi.SURROGATE_LEVELS)
+    wl.cones = (cone_table(20.0, 1, 0.5 * diag, 3.0, 0.35, 1.0), cone_table(0.5, 0, 0.75 * diag, 3.0, 1.0, 1.0))
+    return wl
+
+
+def cone_params_of(wl: Workload, shadow_type=None) -> abi.DosParams:
+    """The cone method's parameters for the same scene (the comparison)."""
+    st = wl.params.shadow_type if shadow_type is None else shadow_type
+    return dos_params(wl.params.step_size, apply_occ=True, apply_sdw=True, shadow_type=st)
+
+
+def random_view(rng: np.random.Generator, n: int, directional: bool):
+    """A camera on the sphere of radius U[2.2, 3.2] n looking at the centre
+    (30 degree field of view) and a light from a uniform random direction:
+    a point light at 2 n, or a directional light."""
+    v = rng.normal(size=3)
+    eye = tuple(float(rng.uniform(2.2, 3.2)) * n * _norm(v))
+    up = (0.0, 1.0, 0.0) if abs(_norm(v)[1]) < 0.95 else (1.0, 0.0, 0.0)
+    cam = camera(eye, up=up, fovy=30.0)
+    ldir = _norm(rng.normal(size=3))
+    fwd, lup, right = light_frame(ldir)
+    if directional:
+        lt = light(abi.LIGHT_DIRECTIONAL, position=tuple(3.0 * n * ldir), forward=fwd, up=lup, right=right)
+    else:
+        lt = light(abi.LIGHT_POINT, position=tuple(2.0 * n * ldir), forward=fwd, up=lup, right=right)
+    return cam, lt
+
+
+def shaded_sample_count(ctx: Context, cam, w, h, step) -> int:
+    """Shaded samples of a frame's primary rays (a plain render's statistics)."""
+    p = abi.PlainParams()
+    p.step_size = step
+    _, st = ctx.render(abi.PLAIN, cam, None, p, w, h)
+    return int(st.shaded_samples)
+
+
+def build_surrogate_training_set(ctx: Context, n_volumes=SURROGATE_VOLUMES, size=256, points=4_000_000,
+                                 views=4, image=256, seed=SURROGATE_SEED, log=None) -> int:
+    """Appends ~points labelled shading points to the context's training set
+    (the network must exist: cvr_mlp_init first).  Returns the points added."""
+    rng = np.random.default_rng(seed)
+    per_view = max(1, points // (n_volumes * views))
+    added = 0
+    for v in range(n_volumes):
+        vol = synth_blobs(size, size, size, abi.CVR_U8, 32, seed=seed + v, noise_max=20.0)
+        wl = surrogate_workload(vol, image)
+        prepare(ctx, wl)
+        step = wl.params.step_size
+        for k in range(views):
+            directional = (k % 2) == 1
+            cam, lt = random_view(rng, size, directional)
+            shaded = shaded_sample_count(ctx, cam, image, image, step)
+            if shaded == 0:
+                continue
+            rate = min(1.0, per_view / shaded)
+            ctx.clear_points()
+            got = ctx.collect_points(cam, image, image, step, rate, int(rng.integers(1 << 62)), per_view)
+            gp = gt_params(step, wl.diagonal, occ_distance=32.0, light_step=1.0, gap=1.0,
+                           shadow_type=2 if directional else 0)
+            ctx.label_points(lt, gp, append_training=True, download=False)
+            added += got
+        if log:
+            log(f"volume {v}: {added} points")
+    return added
+
+
+# Adam schedule: (epochs, learning rate) phases.
+SURROGATE_SCHEDULE = ((12, 2e-3), (8, 7e-4), (6, 2e-4), (4, 5e-5))
+
+
+def train_surrogate(ctx: Context, batch=4096, schedule=SURROGATE_SCHEDULE, seed=SURROGATE_SEED) -> list:
+    """Adam over the context's training set; returns the per-epoch losses."""
+    losses = []
+    for i, (epochs, lr) in enumerate(schedule):
+        out = np.zeros(epochs, np.float32)
+        ctx._ck(ctx.lib.cvr_mlp_train(ctx.h, epochs, batch, lr, seed + i, abi.fptr(out)))
+        losses.extend(out.tolist())
+    return losses
+
+
+def evaluate_surrogate(ctx: Context, wl: Workload, points=2_000_000, seed=7) -> dict:
+    """RMSE of the network and of the cone method against the ground-truth
+    integrator over a uniform sample of the shading points of wl's frame
+    (wl prepared on ctx, the network trained)."""
+    step = wl.params.step_size
+    shaded = shaded_sample_count(ctx, wl.cam, wl.width, wl.height, step)
+    rate = min(1.0, points / max(shaded, 1))
+    ctx.clear_points()
+    ctx.collect_points(wl.cam, wl.width, wl.height, step, rate, seed, points)
+    r = ctx.evaluate_points(wl.light, wl.params, cone_params_of(wl))
+    r["shaded_samples"] = shaded
+    return r

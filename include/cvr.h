@@ -62,7 +62,9 @@ typedef enum cvr_method {
   CVR_METHOD_PLAIN = 0,       /* rc1pass    : ray_marching_1p.comp */
   CVR_METHOD_EXTINCTION = 1,  /* rc1pextbsd : ebs_ray_bbox_marching.comp */
   CVR_METHOD_CONE_DOS = 2,    /* rc1pdosct  : ray_bbox_marching.comp */
-  CVR_METHOD_GROUND_TRUTH = 3 /* rc1pcrtgt  : gt_ray_marching.comp (single pass) */
+  CVR_METHOD_GROUND_TRUTH = 3, /* rc1pcrtgt  : gt_ray_marching.comp (single pass) */
+  CVR_METHOD_SURROGATE = 4     /* no reference counterpart: rc1pcrtgt with the light integrals
+                                  replaced by the learned network (see the surrogate section) */
 } cvr_method;
 
 typedef struct cvr_ctx cvr_ctx;
@@ -290,7 +292,7 @@ cvr_status cvr_mlp_forward(cvr_ctx* ctx, const float* x, int n, float* y);
 /* Gradient of L = 1/(2n) sum (y - t)^2 over n points w.r.t. every parameter,
  * without updating them (grad: CVR_MLP_PARAMS floats).  Synchronous. */
 cvr_status cvr_mlp_gradients(cvr_ctx* ctx, const float* x, const float* t, int n, float* grad, float* loss);
-/* Training set from host memory (features n*48, targets n*2). */
+/* Training set from host memory (features n*48, targets n*2); n = 0 clears it. */
 cvr_status cvr_mlp_set_training_data(cvr_ctx* ctx, const float* x, const float* t, int n);
 cvr_status cvr_mlp_get_training_data(cvr_ctx* ctx, float* x, float* t, int n);
 int cvr_mlp_training_size(cvr_ctx* ctx);
@@ -298,6 +300,60 @@ int cvr_mlp_training_size(cvr_ctx* ctx);
  * of 128); each epoch is one replay of a captured CUDA graph.
  * loss_per_epoch (nullable) receives the mean batch loss of every epoch. */
 cvr_status cvr_mlp_train(cvr_ctx* ctx, int epochs, int batch, float lr, uint64_t seed, float* loss_per_epoch);
+/* Checkpoint: parameters, Adam moments and step in a versioned binary file
+ * ("CVRMLP01", u32 version 1, u32 CVR_MLP_PARAMS, params, m, v as FP32, i32 step). */
+cvr_status cvr_mlp_save(cvr_ctx* ctx, const char* path);
+cvr_status cvr_mlp_load(cvr_ctx* ctx, const char* path);
+
+/* ---- surrogate shading ----------------------------------------------------
+ * CVR_METHOD_SURROGATE renders the image of RC1PConeLightGroundTruthSteps
+ * (method params: cvr_gt_params; step_size, apply_occlusion, apply_shadow,
+ * shadow_type, ka, kd are used, the light-ray fields describe the integrator
+ * the network was trained against) with the per-sample occlusion and shadow
+ * integrals replaced by the network, evaluated on the tensor cores inside the
+ * marcher.  It needs a network (cvr_mlp_init / _set_params / _load / _train)
+ * and an extinction pyramid with at least CVR_SURROGATE_LEVELS levels whose
+ * base is half the volume resolution (the configuration the features are
+ * defined on).
+ *
+ * Network inputs at a shading point (texture-space position p, primary ray
+ * direction dir), in the frame n = -dir, r = normalize(dir x (0,1,0)),
+ * u = normalize(-dir x r) of the ground-truth occlusion kernel:
+ *   x[7l+k], l = 0..5, k = 0..6: 1 - exp(-sigma_l(p + o_k d_l) d_l), with
+ *     d_l = 2^(l+1) voxels, o = {0, L, 3L, n, 3n, r, u}, sigma_l pyramid level l
+ *     (0 outside the volume), L the direction towards the light;
+ *   x[42..44] = L in (r, u, n); x[45..47] = extinction gradient (central
+ *     differences at +-1 voxel) in (r, u, n).
+ * Outputs: (ambient occlusion, shadow) as the ground-truth integrator defines
+ * them (gt_ray_marching.comp:109-252), clamped to [0, 1] when shading. */
+#define CVR_SURROGATE_LEVELS 6
+
+/* Shading points of one frame: every shaded sample of the primary rays (the
+ * samples that reach ShadeSample) is kept with probability rate and appended
+ * to the context's point list (position in texture space [0, S], primary ray
+ * direction), which holds at most max_points.  n_added (nullable) receives
+ * the number appended. */
+cvr_status cvr_surrogate_collect(cvr_ctx* ctx, const cvr_camera* camera, int w, int h, float step_size,
+                                 float rate, uint64_t seed, int max_points, int* n_added);
+cvr_status cvr_surrogate_clear_points(cvr_ctx* ctx);
+int cvr_surrogate_point_count(cvr_ctx* ctx);
+/* Point list from / to host memory: n x 6 floats (px, py, pz, dx, dy, dz). */
+cvr_status cvr_surrogate_set_points(cvr_ctx* ctx, const float* points, int n);
+cvr_status cvr_surrogate_get_points(cvr_ctx* ctx, float* points, int n);
+/* Network inputs (n x 48) and ground-truth targets (n x 2: occlusion and
+ * shadow of the GT integrator with the context's kernel vectors, whatever the
+ * apply flags say) of the n points of the list.  x_host / t_host (nullable)
+ * receive them; append_training != 0 appends them to the network's training
+ * set on the device. */
+cvr_status cvr_surrogate_label(cvr_ctx* ctx, const cvr_light* light, const cvr_gt_params* params,
+                               int append_training, float* x_host, float* t_host, int n);
+/* Error against the ground-truth integrator over the point list.
+ * out[0], out[1]: RMSE of the network's (occlusion, shadow) as used in shading;
+ * out[2], out[3]: RMSE of the cone method (cvr_dos_params; needs cone tables)
+ * when cone != NULL, else 0; out[4]: points; out[5], out[6]: mean GT
+ * occlusion and shadow; out[7]: largest absolute occlusion error of the network. */
+cvr_status cvr_surrogate_evaluate(cvr_ctx* ctx, const cvr_light* light, const cvr_gt_params* params,
+                                  const cvr_dos_params* cone, double out[8]);
 
 /* ---- host-side helpers (no GPU needed) ------------------------------------ */
 /* TransferFunction1D::BuildLinear over control points (transferfunction1d.cpp:319-358)

@@ -50,6 +50,9 @@ def load():
             "oracle_set_gt_kernels": (I, [P, P, I, P, I]),
             "oracle_render": (I, [P, I, I, C.POINTER(abi.Camera), C.POINTER(abi.Light), P, I, I, I, I, P, P,
                                   C.POINTER(C.c_uint64), I]),
+            "oracle_set_mlp": (I, [P, P, I]),
+            "oracle_sur_features": (I, [P, I, C.POINTER(abi.Light), I, P, I, P, P]),
+            "oracle_gt_points": (I, [P, C.POINTER(abi.Light), C.POINTER(abi.GtParams), P, I, P]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -144,6 +147,28 @@ class Oracle:
         sdw = np.ascontiguousarray(sdw, np.float32)
         self._ck(self.lib.oracle_set_gt_kernels(self.h, _p(occ), len(occ), _p(sdw), len(sdw)))
 
+    def set_mlp(self, params):
+        params = np.ascontiguousarray(params, np.float32)
+        self._ck(self.lib.oracle_set_mlp(self.h, _p(params), len(params)))
+
+    def sur_features(self, lt, shadow_type, pts, precision=64, with_outputs=False):
+        """Surrogate inputs (n x 48) of points (n x 6) and, optionally, the
+        BF16 network's outputs (n x 2) on them."""
+        pts = np.ascontiguousarray(pts, np.float32)
+        n = len(pts)
+        x = np.zeros((n, 48), np.float64)
+        y = np.zeros((n, 2), np.float64) if with_outputs else None
+        self._ck(self.lib.oracle_sur_features(self.h, precision, C.byref(lt), shadow_type, _p(pts), n, _p(x),
+                                              _p(y) if y is not None else None))
+        return (x, y) if with_outputs else x
+
+    def gt_points(self, lt, params, pts):
+        """Ground-truth (occlusion, shadow) of points (n x 6), FP64."""
+        pts = np.ascontiguousarray(pts, np.float32)
+        out = np.zeros((len(pts), 2), np.float64)
+        self._ck(self.lib.oracle_gt_points(self.h, C.byref(lt), C.byref(params), _p(pts), len(pts), _p(out)))
+        return out
+
     def render(self, method, cam, lt, params, w, h, precision=64, rows=None, threads=0):
         """Returns (image rows [y0,y1) x W x 4 float64, per-pixel step counts, total steps)."""
         import os
@@ -180,3 +205,7 @@ def prepare(orc: Oracle, wl):
         orc.set_cone_tables(*wl.cones)
     if wl.method == abi.GROUND_TRUTH:
         orc.set_gt_kernels(*wl.gt)
+    if wl.method == abi.SURROGATE:
+        orc.build_pyramid(wl.pyramid["base_dims"], wl.pyramid["sigma0"], wl.pyramid["n_levels"])
+        orc.set_gt_kernels(*wl.gt)
+        orc.set_cone_tables(*wl.cones)

@@ -73,6 +73,7 @@ struct Scene {
   bool cone_ready = false;
   std::vector<float> occ_vec, sdw_vec;
   bool gt_ready = false;
+  std::vector<float> mlp;  // surrogate network parameters (CVR_MLP_PARAMS floats)
 
   double vox_norm(size_t i) const {
     if (dtype == CVR_U8) return (double)vox[i] / 255.0;
@@ -510,6 +511,91 @@ template <class T> T gt_shadow(const Frame<T>& f, const Gt<T>& g, V3<T> tx) {
   return ssdw / swgt;
 }
 
+// ------------------------------------------------------------ surrogate
+// The network's inputs (no reference counterpart; definition in cvr.h): six
+// pyramid levels x seven taps of segment opacity around the shading point in
+// the ground-truth occlusion frame (gt_ray_marching.comp:396-399), the light
+// direction and the extinction gradient in that frame.
+template <class T>
+void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, int shadow_type, V3<T> light_pos,
+                  V3<T> light_fwd, V3<T> tx, V3<T> dir, T* x) {
+  Dos<T> d{};
+  d.s = &s;
+  d.pyr = &pyr;
+  const V3<T> S = f.grid;
+  V3<T> n = normalize(-dir);
+  V3<T> c = cross(dir, v3<T>(0, 1, 0));
+  if (dot(c, c) < T(1e-12)) c = v3<T>(1, 0, 0);
+  V3<T> r = normalize(c);
+  V3<T> u = normalize(cross(-dir, r));
+  V3<T> L = shadow_type == 2 ? light_fwd : normalize(light_pos - (tx - S * T(0.5)));
+  auto tap = [&](int l, V3<T> q, T dl) -> T {
+    if (q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) return T(0);
+    return T(1) - std::exp(-pyr_level(f, d, l, q) * dl);
+  };
+  T dl = T((s.sx + s.sy + s.sz) / 3.0) * T(2);
+  for (int l = 0; l < 6; ++l) {
+    x[7 * l + 0] = tap(l, tx, dl);
+    x[7 * l + 1] = tap(l, tx + L * dl, dl);
+    x[7 * l + 2] = tap(l, tx + L * (T(3) * dl), dl);
+    x[7 * l + 3] = tap(l, tx + n * dl, dl);
+    x[7 * l + 4] = tap(l, tx + n * (T(3) * dl), dl);
+    x[7 * l + 5] = tap(l, tx + r * dl, dl);
+    x[7 * l + 6] = tap(l, tx + u * dl, dl);
+    dl = dl * T(2);
+  }
+  x[42] = dot(L, r);
+  x[43] = dot(L, u);
+  x[44] = dot(L, n);
+  auto sg = [&](V3<T> q) { return tf_alpha<T>(s, sample_volume<T>(s, q)); };
+  V3<T> g;
+  g.x = T(0.5) * (sg(tx + v3<T>(f.spacing.x, 0, 0)) - sg(tx - v3<T>(f.spacing.x, 0, 0)));
+  g.y = T(0.5) * (sg(tx + v3<T>(0, f.spacing.y, 0)) - sg(tx - v3<T>(0, f.spacing.y, 0)));
+  g.z = T(0.5) * (sg(tx + v3<T>(0, 0, f.spacing.z)) - sg(tx - v3<T>(0, 0, f.spacing.z)));
+  x[45] = dot(g, r);
+  x[46] = dot(g, u);
+  x[47] = dot(g, n);
+}
+
+// Round to nearest even BF16 (the operand format of the tensor-core GEMMs).
+inline double bf16(double v) {
+  float f = (float)v;
+  uint32_t b;
+  std::memcpy(&b, &f, 4);
+  b += 0x7FFFu + ((b >> 16) & 1u);
+  b &= 0xFFFF0000u;
+  std::memcpy(&f, &b, 4);
+  return (double)f;
+}
+
+// 48 -> 64 -> 64 -> 2 with BF16 operands (inputs, weights, hidden
+// activations) and exact accumulation; biases in FP32.
+inline void mlp_forward_bf16(const std::vector<float>& P, const double* x, double* y) {
+  const float* W1 = P.data();
+  const float* b1 = W1 + 64 * 48;
+  const float* W2 = b1 + 64;
+  const float* b2 = W2 + 64 * 64;
+  const float* W3 = b2 + 64;
+  const float* b3 = W3 + 2 * 64;
+  double xb[48], h1[64], h2[64];
+  for (int k = 0; k < 48; ++k) xb[k] = bf16(x[k]);
+  for (int o = 0; o < 64; ++o) {
+    double a = 0;
+    for (int k = 0; k < 48; ++k) a += xb[k] * bf16(W1[o * 48 + k]);
+    h1[o] = bf16(std::max(a + (double)b1[o], 0.0));
+  }
+  for (int o = 0; o < 64; ++o) {
+    double a = 0;
+    for (int k = 0; k < 64; ++k) a += h1[k] * bf16(W2[o * 64 + k]);
+    h2[o] = bf16(std::max(a + (double)b2[o], 0.0));
+  }
+  for (int o = 0; o < 2; ++o) {
+    double a = 0;
+    for (int k = 0; k < 64; ++k) a += h2[k] * bf16(W3[o * 64 + k]);
+    y[o] = a + (double)b3[o];
+  }
+}
+
 // ------------------------------------------------------------ primary loop
 // ray_marching_1p.comp:160-247 and the identical loops of the other shaders.
 template <class T, class ShadeFn>
@@ -650,6 +736,29 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                       V3<T> v_up = normalize(cross(-dir, v_right));
                       T io = p->apply_occlusion ? gt_occlusion(f, g, tx, v_up, v_right, dir) : T(0);
                       T is = p->apply_shadow ? gt_shadow(f, g, tx) : T(0);
+                      return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
+                    });
+      return 0;
+    }
+    case CVR_METHOD_SURROGATE: {
+      // The ground-truth ShadeSample (gt_ray_marching.comp:254-303) fed by the
+      // network's (occlusion, shadow), clamped to [0, 1]; spot lights give
+      // shadow 0 as the ground truth does.
+      if (!s.pyr_ready || s.n_levels < 6 || s.mlp.size() != (size_t)CVR_MLP_PARAMS) return CVR_ERR_NOT_READY;
+      const cvr_gt_params* p = (const cvr_gt_params*)params;
+      const std::vector<T>* pyr;
+      if constexpr (sizeof(T) == 8) pyr = &s.pyr64;
+      else pyr = &s.pyr32;
+      V3<T> lpos = from<T>(light.position), lfwd = from<T>(light.forward);
+      march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
+                    [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T> dir) {
+                      T x[48];
+                      sur_features(f, s, *pyr, p->shadow_type, lpos, lfwd, tx, dir, x);
+                      double xd[48], y[2];
+                      for (int k = 0; k < 48; ++k) xd[k] = (double)x[k];
+                      mlp_forward_bf16(s.mlp, xd, y);
+                      T io = T(std::min(std::max(y[0], 0.0), 1.0));
+                      T is = p->shadow_type == 1 ? T(0) : T(std::min(std::max(y[1], 0.0), 1.0));
                       return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
                     });
       return 0;
@@ -852,6 +961,71 @@ int oracle_set_gt_kernels(void* h, const float* occ, int n_occ, const float* sdw
   s.occ_vec.assign(occ, occ + 3 * (size_t)n_occ);
   s.sdw_vec.assign(sdw, sdw + 3 * (size_t)n_sdw);
   s.gt_ready = true;
+  return 0;
+}
+
+int oracle_set_mlp(void* h, const float* params, int n) {
+  Scene& s = *(Scene*)h;
+  if (!params || n != CVR_MLP_PARAMS) return CVR_ERR_INVALID_ARG;
+  s.mlp.assign(params, params + n);
+  return 0;
+}
+
+// Network inputs (n x 48) of n points (n x 6: texture-space position, primary
+// direction) and, when y_out is given and parameters are set, the network's
+// outputs (n x 2) on the FP64 features.
+int oracle_sur_features(void* h, int precision, const cvr_light* light, int shadow_type, const float* pts, int n,
+                        double* x_out, double* y_out) {
+  Scene& s = *(Scene*)h;
+  if (!light || !pts || !x_out || n < 0) return CVR_ERR_INVALID_ARG;
+  if (!s.pyr_ready || s.n_levels < 6) return CVR_ERR_NOT_READY;
+  if (y_out && s.mlp.size() != (size_t)CVR_MLP_PARAMS) return CVR_ERR_NOT_READY;
+  auto run = [&](auto zero) {
+    using T = decltype(zero);
+    Frame<T> f;
+    f.s = &s;
+    f.spacing = v3<T>(T(s.sx), T(s.sy), T(s.sz));
+    f.grid = v3<T>(T(s.nx * s.sx), T(s.ny * s.sy), T(s.nz * s.sz));
+    const std::vector<T>* pyr;
+    if constexpr (sizeof(T) == 8) pyr = &s.pyr64;
+    else pyr = &s.pyr32;
+    for (int i = 0; i < n; ++i) {
+      const float* q = pts + 6 * (size_t)i;
+      T x[48];
+      sur_features<T>(f, s, *pyr, shadow_type, from<T>(light->position), from<T>(light->forward), from<T>(q),
+                      from<T>(q + 3), x);
+      double* xo = x_out + 48 * (size_t)i;
+      for (int k = 0; k < 48; ++k) xo[k] = (double)x[k];
+      if (y_out) mlp_forward_bf16(s.mlp, xo, y_out + 2 * (size_t)i);
+    }
+  };
+  if (precision == 64) run(0.0);
+  else run(0.0f);
+  return 0;
+}
+
+// Ground-truth (occlusion, shadow) of n points (n x 6), the integrator of
+// gt_ray_marching.comp:109-252 with the scene's kernel vectors.
+int oracle_gt_points(void* h, const cvr_light* light, const cvr_gt_params* p, const float* pts, int n, double* out) {
+  Scene& s = *(Scene*)h;
+  if (!light || !p || !pts || !out || n < 0) return CVR_ERR_INVALID_ARG;
+  if (!s.gt_ready) return CVR_ERR_NOT_READY;
+  Frame<double> f;
+  f.s = &s;
+  f.spacing = v3<double>(s.sx, s.sy, s.sz);
+  f.grid = v3<double>(s.nx * s.sx, s.ny * s.sy, s.nz * s.sz);
+  Gt<double> g;
+  g.p = p; g.s = &s;
+  g.light_pos = from<double>(light->position); g.light_fwd = from<double>(light->forward);
+  g.light_up = from<double>(light->up); g.light_right = from<double>(light->right);
+  for (int i = 0; i < n; ++i) {
+    const float* q = pts + 6 * (size_t)i;
+    V3<double> tx = from<double>(q), dir = from<double>(q + 3);
+    V3<double> v_right = normalize(cross(dir, v3<double>(0, 1, 0)));
+    V3<double> v_up = normalize(cross(-dir, v_right));
+    out[2 * (size_t)i] = gt_occlusion(f, g, tx, v_up, v_right, dir);
+    out[2 * (size_t)i + 1] = gt_shadow(f, g, tx);
+  }
   return 0;
 }
 
