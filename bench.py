@@ -46,7 +46,11 @@ WORKLOAD_DESC = {
             "occlusion + point-light shadow cones",
     "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
                     "1 shadow ray to a point light, 1-voxel light steps",
+    "surrogate": "learned occlusion/shadow surrogate: MLP 48-64-64-2 (BF16 tcgen05) trained on 4M GT-labelled "
+                 "points of 20 seeded 256^3 blob volumes; held-out 512^3 u8 blobs -> 1024^2, point light",
 }
+
+MLP_FLOP_PER_SAMPLE = 2 * (48 * 64 + 64 * 64 + 64 * 2)  # 14,592
 
 
 def dist_env():
@@ -155,6 +159,8 @@ def algorithmic_bytes(wl, st, abi):
     plus per secondary fetch 64 int64 SAT texels (extinction), 8 float32
     pyramid texels (cone) or 8 voxel texels (ground truth), plus the image."""
     bvox = 1 if wl.dtype == abi.CVR_U8 else 2
+    if wl.method == abi.SURROGATE:  # per shaded sample: 42 pyramid taps (8 float32) + 6 volume taps
+        return st.samples * 8 * bvox + st.shaded_samples * (42 * 8 * 4 + 6 * 8 * bvox) + wl.width * wl.height * 16
     per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 8, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox}[wl.method]
     return st.samples * 8 * bvox + st.aux_fetches * per_aux + wl.width * wl.height * 16
 
@@ -249,6 +255,70 @@ def time_frames(ctx, lib, wl, params, out_ptr, steps, warmup, flush=True):
     return times
 
 
+def measured_peak_bf16():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["bf16_tflops"]), "measured"
+        except Exception:
+            pass
+    return 1900.0, "fallback"
+
+
+def surrogate_section(ctx, lib, args, log=print):
+    """Trains the surrogate from scratch (cfg: 4M GT-labelled points of 20
+    seeded 256^3 blob volumes), then on the held-out 512^3 volume at 1024^2
+    measures its RMSE and the cone method's against the ground-truth
+    integrator, and the GT and surrogate frame times.  Leaves the surrogate
+    workload prepared on ctx."""
+    import ctypes as C
+    from cpp_volume_rendering_gb300 import abi, scene
+    t0 = time.perf_counter()
+    ctx.mlp_init(scene.SURROGATE_SEED)
+    abi.check(lib.cvr_mlp_set_training_data(ctx.h, None, None, 0), ctx.h)
+    pts = scene.build_surrogate_training_set(ctx, points=args.surrogate_points)
+    own = args.workload == "surrogate"
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    losses = scene.train_surrogate(ctx)
+    t_train = time.perf_counter() - t0
+    wl = scene.workload("surrogate", n=args.size if own else None, image=args.image if own else None)
+    scene.prepare(ctx, wl)
+    err = scene.evaluate_surrogate(ctx, wl)
+    out = C.POINTER(C.c_float)()
+    abi.check(lib.cvr_get_frame_buffer(ctx.h, wl.width, wl.height, C.byref(out)), ctx.h)
+    optr = C.cast(out, C.c_void_p)
+    st_s, st_g = abi.FrameStats(), abi.FrameStats()
+    for method, st in ((abi.SURROGATE, st_s), (abi.GROUND_TRUTH, st_g)):
+        abi.check(lib.cvr_render(ctx.h, method, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                                 C.sizeof(wl.params), optr, wl.width, wl.height, None, C.byref(st)), ctx.h)
+    wl.method = abi.SURROGATE
+    ts = time_frames(ctx, lib, wl, wl.params, optr, 5, 2)
+    wl.method = abi.GROUND_TRUTH
+    tg = time_frames(ctx, lib, wl, wl.params, optr, 2, 1)
+    wl.method = abi.SURROGATE
+    ms_s, ms_g = statistics.median(ts), statistics.median(tg)
+    peak, src = measured_peak_bf16()
+    tflops = st_s.shaded_samples * MLP_FLOP_PER_SAMPLE / (ms_s / 1000.0) / 1e12
+    return {
+        "workload": WORKLOAD_DESC["surrogate"], "volume": list(wl.dims), "image": [wl.width, wl.height],
+        "training": {"points": pts, "volumes": scene.SURROGATE_VOLUMES, "epochs": len(losses),
+                     "schedule": [list(x) for x in scene.SURROGATE_SCHEDULE], "batch": 4096,
+                     "final_loss": losses[-1], "first_loss": losses[0], "data_s": t_data, "train_s": t_train},
+        "heldout": {k: err[k] for k in ("rmse_ao", "rmse_shadow", "cone_rmse_ao", "cone_rmse_shadow", "points",
+                                        "mean_ao", "mean_shadow", "max_err_ao", "shaded_samples")},
+        "gt_ms": ms_g, "surrogate_ms": ms_s, "speedup_vs_gt": ms_g / ms_s,
+        "surrogate_fps": 1000.0 / ms_s, "surrogate_msamples_s": st_s.samples / (ms_s / 1000.0) / 1e6,
+        "gt_msamples_s": st_g.samples / (ms_g / 1000.0) / 1e6,
+        "mlp_tensor": {"achieved_tflops": tflops, "peak_tflops": peak, "frac": tflops / peak,
+                       "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops)",
+                       "flop_per_inference": MLP_FLOP_PER_SAMPLE,
+                       "note": "network FLOPs of the fused frame / frame time; the marcher is gather-bound, "
+                               "the tensor pipe is far from its roofline by design"},
+        "frame": {"samples": st_s.samples, "shaded_samples": st_s.shaded_samples},
+    }
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -259,8 +329,11 @@ def run_ours(args):
     from cpp_volume_rendering_gb300 import abi, build, scene
     build.build()
     lib = abi.load()
-    wl = scene.workload(args.workload, n=args.size, image=args.image)
     ctx = scene.Context(local)
+    surrogate = None
+    if args.workload == "surrogate":
+        surrogate = surrogate_section(ctx, lib, args)
+    wl = scene.workload(args.workload, n=args.size, image=args.image)
     scene.prepare(ctx, wl)
     out = C.POINTER(C.c_float)()
     abi.check(lib.cvr_get_frame_buffer(ctx.h, wl.width, wl.height, C.byref(out)), ctx.h)
@@ -316,7 +389,7 @@ def run_ours(args):
         abi.check(lib.cvr_set_volume(ctx.h, pinned, w, h, d, wl.dtype, *wl.spacing), ctx.h)
         if wl.method == abi.EXTINCTION:
             abi.check(lib.cvr_build_sat(ctx.h, abi.dptr(ext), len(ext)), ctx.h)
-        if wl.method == abi.CONE_DOS:
+        if wl.method in (abi.CONE_DOS, abi.SURROGATE):
             ctx.build_pyramid(**wl.pyramid)
         abi.check(lib.cvr_render_host(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
                                       C.sizeof(params), C.cast(img_pinned, C.POINTER(C.c_float)), wl.width,
@@ -326,12 +399,15 @@ def run_ours(args):
     lib.cvr_host_free_pinned(pinned)
     lib.cvr_host_free_pinned(img_pinned)
     e2e_total, = barrier_max([sum(e2e_times)], ws)
-    e2e = {"value": samples_all / e2e_total / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": int(nbytes + ext.nbytes),
+    e2e = {"value": samples_all / e2e_total / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": int(nbytes + (ext.nbytes if wl.method == abi.EXTINCTION else 0)),
            "d2h_bytes_per_step": int(wl.width * wl.height * 16),
            "ms_per_step": 1000.0 * e2e_total / args.steps,
-           "includes": "cvr_set_volume from pinned host memory + cvr_build_sat + cvr_render_host readback"}
+           "includes": "cvr_set_volume from pinned host memory + the method's table build (SAT or pyramid) + "
+                       "cvr_render_host readback"}
     renderers = {}
     if not args.quick:
+        if surrogate is None and not args.no_surrogate:
+            surrogate = surrogate_section(ctx, lib, args)
         for name in ("plain", "cone", "ground_truth"):
             if name == args.workload:
                 continue
@@ -364,7 +440,7 @@ def run_ours(args):
         "fps": 1000.0 / ms_per_step,
         "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-        "clocks": clocks, "renderers": renderers}))
+        "clocks": clocks, "renderers": renderers, "surrogate": surrogate}))
 
 
 def main():
@@ -376,6 +452,8 @@ def main():
     ap.add_argument("--workload", default="extinction", choices=list(WORKLOAD_DESC))
     ap.add_argument("--quick", action="store_true", help="skip the per-renderer table")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the surrogate")
+    ap.add_argument("--surrogate-points", type=int, default=4_000_000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--size", type=int, default=None, help="volume side override (profiling / small cases)")
     ap.add_argument("--image", type=int, default=None, help="image side override (profiling / small cases)")

@@ -35,6 +35,7 @@ MAX_AO_SHELLS = 32
 MLP_PARAMS = 7426
 MLP_INPUTS = 48
 SURROGATE_LEVELS = 6
+SAMPLING_TEX_FEATURES = 1
 MAX_CONE_SECTIONS = 512
 
 F3 = C.c_float * 3
@@ -147,6 +148,8 @@ SIGNATURES = {
     "cvr_mlp_get_training_data": (_I, [_P, _FP, _FP, _I]),
     "cvr_mlp_training_size": (_I, [_P]),
     "cvr_mlp_train": (_I, [_P, _I, _I, _F, C.c_uint64, _FP]),
+    "cvr_set_sampling": (_I, [_P, _I]),
+    "cvr_get_sampling": (_I, [_P]),
     "cvr_mlp_save": (_I, [_P, C.c_char_p]),
     "cvr_mlp_load": (_I, [_P, C.c_char_p]),
     "cvr_surrogate_collect": (_I, [_P, C.POINTER(Camera), _I, _I, _F, _F, C.c_uint64, _I, C.POINTER(C.c_int)]),

@@ -180,6 +180,8 @@ static cvr_status set_volume_common(cvr_ctx* c, const void* src, bool src_device
   // Derived tables belong to the previous volume.
   c->sat_ready = false;
   c->pyr_ready = false;
+  c->tex.vol_valid = false;
+  c->tex.pyr_valid = false;
   return CVR_OK;
 }
 
@@ -217,6 +219,7 @@ cvr_status cvr_set_transfer_function(cvr_ctx* c, const float* rgbt, const float*
   CK(c, cudaStreamSynchronize(c->stream));
   c->tf_n = n;
   c->pyr_ready = false;
+  c->tex.pyr_valid = false;
   return CVR_OK;
 }
 
@@ -301,6 +304,7 @@ cvr_status cvr_build_ext_pyramid(cvr_ctx* c, const cvr_pyramid_params* p) {
   CK(c, launch_pyramid_build(v, c->d_rgba, c->tf_n, p->sigma0, P, c->d_pyr, c->stream));
   c->pyr = P;
   c->pyr_ready = true;
+  c->tex.pyr_valid = false;
   return CVR_OK;
 }
 

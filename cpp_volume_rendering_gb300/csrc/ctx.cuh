@@ -50,6 +50,30 @@ struct MlpState {
   }
 };
 
+// Texture-unit copies of the volume and of the pyramid levels (hardware
+// trilinear filtering), made on first use after the source changed.
+struct TexImage {
+  cudaArray_t arr = nullptr;
+  cudaTextureObject_t tex = 0;
+  void release() {
+    if (tex) cudaDestroyTextureObject(tex);
+    if (arr) cudaFreeArray(arr);
+    tex = 0;
+    arr = nullptr;
+  }
+};
+struct TexState {
+  TexImage vol;
+  bool vol_valid = false;
+  TexImage pyr[CVR_MAX_LEVELS];
+  int n_pyr = 0;
+  bool pyr_valid = false;
+  ~TexState() {
+    vol.release();
+    for (auto& t : pyr) t.release();
+  }
+};
+
 // Shading points of the surrogate (training / evaluation) and its scratch.
 struct SurState {
   float4* pts = nullptr;         // 2 float4 per point: position, direction
@@ -115,6 +139,8 @@ struct cvr_ctx {
   std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
   std::unique_ptr<MlpState> mlp;             // surrogate network (created by cvr_mlp_init)
   std::unique_ptr<SurState> sur;             // surrogate shading points
+  TexState tex;                              // texture-unit copies (volume, pyramid)
+  int sampling = CVR_SAMPLING_TEX_FEATURES;  // cvr_set_sampling flags
 };
 
 namespace cvr {
@@ -186,6 +212,9 @@ inline CameraView camera_view(const cvr_camera* cam, int w, int h) {
 cvr_status mlp_reserve_training(cvr_ctx* c, size_t extra, float** x, float** t);
 // Reads and clears the network's device error flag (bounded tensor-core waits).
 cvr_status mlp_check_err(cvr_ctx* c);
+// Texture objects of the volume / pyramid levels, (re)made when stale.
+cvr_status ensure_volume_texture(cvr_ctx* c);
+cvr_status ensure_pyramid_textures(cvr_ctx* c);
 // The CVR_METHOD_SURROGATE launch of cvr_render.
 cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params* p, const cvr_light* light);
 

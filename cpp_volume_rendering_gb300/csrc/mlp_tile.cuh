@@ -30,11 +30,36 @@ __device__ __forceinline__ void store_row64(uint8_t* tile, int r, const float* v
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       int k0 = c * 8 + 2 * j;
-      uint32_t lo = k0 < n ? to_bf16(v[k0]) : 0u, hi = k0 + 1 < n ? to_bf16(v[k0 + 1]) : 0u;
-      w[j] = lo | (hi << 16);
+      w[j] = k0 + 1 < n ? pack_bf16(v[k0], v[k0 + 1]) : (k0 < n ? pack_bf16(v[k0], 0.0f) : 0u);
     }
     *reinterpret_cast<uint4*>(tile + (uint32_t)(r >> 3) * kRowSbo + (uint32_t)c * 128u + (uint32_t)(r & 7) * 16u) =
         make_uint4(w[0], w[1], w[2], w[3]);
+  }
+}
+
+// One 16-byte chunk (k = 8c .. 8c+7) of row r of a K = 64 row tile.
+__device__ __forceinline__ void store_chunk(uint8_t* tile, int r, int c, uint32_t w0, uint32_t w1, uint32_t w2,
+                                            uint32_t w3) {
+  *reinterpret_cast<uint4*>(tile + (uint32_t)(r >> 3) * kRowSbo + (uint32_t)c * 128u + (uint32_t)(r & 7) * 16u) =
+      make_uint4(w0, w1, w2, w3);
+}
+
+// Hidden layer epilogue: TMEM columns col..col+63 of this thread's row, plus
+// bias, ReLU, to BF16 row r of tile; 16 columns at a time.
+__device__ __forceinline__ void epilogue_relu64(uint32_t tmem, int col, const float* bias, uint8_t* tile, int r) {
+  const uint32_t lane = (uint32_t)(threadIdx.x & ~31);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    float v[16];
+    tmem_ld16(taddr(tmem, lane, (uint32_t)(col + 16 * q)), v);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 16 * q + 8 * h;
+      store_chunk(tile, r, 2 * q + h, pack_bf16_relu(v[8 * h + 0] + bias[k + 0], v[8 * h + 1] + bias[k + 1]),
+                  pack_bf16_relu(v[8 * h + 2] + bias[k + 2], v[8 * h + 3] + bias[k + 3]),
+                  pack_bf16_relu(v[8 * h + 4] + bias[k + 4], v[8 * h + 5] + bias[k + 5]),
+                  pack_bf16_relu(v[8 * h + 6] + bias[k + 6], v[8 * h + 7] + bias[k + 7]));
+    }
   }
 }
 
@@ -73,30 +98,26 @@ __device__ __forceinline__ void sync_tiles() {
 }
 
 // Forward of the 128-point tile whose input rows are in s.x; returns this
-// thread's two outputs.  Must be called by all 128 threads.
+// thread's two outputs.  Must be called by all 128 threads.  Every layer
+// accumulates into TMEM columns 0..63 (a layer's result is read out before
+// the next is issued), and the hidden activations go to s.h, which may be
+// the same buffer as s.x (the input is dead once layer 1 has completed).
 __device__ __forceinline__ bool mlp_forward_tile(MlpSmem& s, float y[2]) {
   const float* bias = reinterpret_cast<const float*>(s.w + kPkBias);
   bool ok = true;
-  float h[64];
   if (threadIdx.x == 0) {
     fence_after_sync();
     issue_k64(s.tmem, s.x, s.w + kPkW1, idesc_bf16(128, 64));
   }
   ok &= complete(s.bar, s.phase);
-  ld_row64(s.tmem, 0, h);
-#pragma unroll
-  for (int j = 0; j < 64; ++j) h[j] = fmaxf(h[j] + bias[j], 0.0f);
-  store_row64(s.h, threadIdx.x, h, 64);
+  epilogue_relu64(s.tmem, 0, bias, s.h, threadIdx.x);
   sync_tiles();
   if (threadIdx.x == 0) {
     fence_after_sync();
-    issue_k64(s.tmem + 64, s.h, s.w + kPkW2, idesc_bf16(128, 64));
+    issue_k64(s.tmem, s.h, s.w + kPkW2, idesc_bf16(128, 64));
   }
   ok &= complete(s.bar, s.phase);
-  ld_row64(s.tmem, 64, h);
-#pragma unroll
-  for (int j = 0; j < 64; ++j) h[j] = fmaxf(h[j] + bias[64 + j], 0.0f);
-  store_row64(s.h, threadIdx.x, h, 64);
+  epilogue_relu64(s.tmem, 0, bias + 64, s.h, threadIdx.x);
   sync_tiles();
   if (threadIdx.x == 0) {
     fence_after_sync();
@@ -112,8 +133,9 @@ __device__ __forceinline__ bool mlp_forward_tile(MlpSmem& s, float y[2]) {
 }
 
 // Shared set-up of an MLP CTA: TMEM allocation, mbarrier, weight image.
-__device__ __forceinline__ void mlp_cta_begin(uint8_t* w, const uint8_t* packed, uint64_t* bar, uint32_t* tslot) {
-  if (threadIdx.x < 32) tmem_alloc(tslot, 128);
+__device__ __forceinline__ void mlp_cta_begin(uint8_t* w, const uint8_t* packed, uint64_t* bar, uint32_t* tslot,
+                                              uint32_t tmem_cols = 128) {
+  if (threadIdx.x < 32) tmem_alloc(tslot, tmem_cols);
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -123,12 +145,12 @@ __device__ __forceinline__ void mlp_cta_begin(uint8_t* w, const uint8_t* packed,
   for (int i = threadIdx.x; i < (int)(kPkBytes / 16); i += blockDim.x) dst[i] = src[i];
 }
 
-__device__ __forceinline__ void mlp_cta_end(uint32_t tmem) {
+__device__ __forceinline__ void mlp_cta_end(uint32_t tmem, uint32_t tmem_cols = 128) {
   fence_before_sync();
   __syncthreads();
   if (threadIdx.x < 32) {
     fence_after_sync();
-    tmem_dealloc(tmem, 128);
+    tmem_dealloc(tmem, tmem_cols);
   }
 }
 

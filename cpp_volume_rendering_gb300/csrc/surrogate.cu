@@ -65,6 +65,13 @@ cudaError_t launch_sur_collect(const FrameArgs& f, float rate, unsigned long lon
 }
 
 // ---------------------------------------------------------------- labelling
+// Writes feature k of one point as FP32 to global memory.
+struct GlobalSink {
+  float* row;
+  __device__ __forceinline__ void operator()(int k, float v) { row[k] = v; }
+};
+
+template <bool TEX>
 __global__ void __launch_bounds__(128) k_sur_label(const float4* __restrict__ pts, int n, FrameArgs f, SurArgs a,
                                                    GtArgs g, DosArgs d, int want_gt, int want_dos,
                                                    float* __restrict__ x_out, float* __restrict__ t_out,
@@ -90,11 +97,8 @@ __global__ void __launch_bounds__(128) k_sur_label(const float4* __restrict__ pt
   float4 P = pts[2 * (size_t)i], Q = pts[2 * (size_t)i + 1];
   float3 tx = f3(P.x, P.y, P.z), dir = f3(Q.x, Q.y, Q.z);
   if (x_out) {
-    float x[kMlpIn];
-    sur_features(a, f.vol, tf, f.tf_n, tx, dir, x);
-    float4* o = reinterpret_cast<float4*>(x_out + (size_t)i * kMlpIn);
-#pragma unroll
-    for (int k = 0; k < kMlpIn / 4; ++k) o[k] = make_float4(x[4 * k], x[4 * k + 1], x[4 * k + 2], x[4 * k + 3]);
+    GlobalSink out{x_out + (size_t)i * kMlpIn};
+    sur_features<TEX>(a, f.vol, tf, f.tf_n, tx, dir, out);
   }
   unsigned aux = 0;
   if (want_gt) {
@@ -117,8 +121,9 @@ __global__ void __launch_bounds__(128) k_sur_label(const float4* __restrict__ pt
   }
 }
 
-cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const SurArgs& a, const GtArgs* g,
-                             const DosArgs* d, float* x_out, float* t_out, float* dos_out, cudaStream_t st) {
+cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const SurArgs& a, bool tex,
+                             const GtArgs* g, const DosArgs* d, float* x_out, float* t_out, float* dos_out,
+                             cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   GtArgs gg = g ? *g : GtArgs{};
   DosArgs dd = d ? *d : DosArgs{};
@@ -126,11 +131,12 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
   size_t sm = sizeof(float4) * f.tf_n;
   if (want_dos) sm += sizeof(float4) * (dd.occ.n_sections + dd.sdw.n_sections);
   if (want_gt) sm += sizeof(float3) * (gg.n_occ + gg.n_sdw);
+  auto kern = tex ? k_sur_label<true> : k_sur_label<false>;
   if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_sur_label, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_sur_label<<<(n + 127) / 128, 128, sm, st>>>(pts, n, f, a, gg, dd, want_gt, want_dos, x_out, t_out, dos_out);
+  kern<<<(n + 127) / 128, 128, sm, st>>>(pts, n, f, a, gg, dd, want_gt, want_dos, x_out, t_out, dos_out);
   return cudaGetLastError();
 }
 
@@ -161,19 +167,38 @@ __device__ __forceinline__ void sur_finish(const FrameArgs& f, const SurRay& r, 
   n_all += r.n;
 }
 
-__global__ void __launch_bounds__(128, 3) k_march_surrogate(FrameArgs f, SurArgs a, unsigned int* work, int* err) {
+// Packs features pairwise to BF16 and stores each 8-feature chunk of this
+// thread's row of the input tile as soon as it is complete.
+struct TileSink {
+  uint8_t* tile;
+  int row;
+  uint32_t w[4];
+  float lo;
+  __device__ __forceinline__ void operator()(int k, float v) {
+    if (k & 1) {
+      w[(k >> 1) & 3] = pack_bf16(lo, v);
+      if ((k & 7) == 7) store_chunk(tile, row, k >> 3, w[0], w[1], w[2], w[3]);
+    } else {
+      lo = v;
+    }
+  }
+};
+
+constexpr uint32_t kSurTmemCols = 64;
+
+template <bool TEX>
+__global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs a, unsigned int* work, int* err) {
   extern __shared__ __align__(1024) uint8_t sm_sur[];
   uint8_t* w = sm_sur;
-  uint8_t* xt = w + kPkBytes;
-  uint8_t* ht = xt + kRowTile;
-  float4* tf = reinterpret_cast<float4*>(ht + kRowTile);
+  uint8_t* xt = w + kPkBytes;  // input tile, then the hidden activations of the same tile
+  float4* tf = reinterpret_cast<float4*>(xt + kRowTile);
   uint64_t* bar = reinterpret_cast<uint64_t*>(tf + f.tf_n);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
-  mlp_cta_begin(w, a.packed, bar, tslot);
+  mlp_cta_begin(w, a.packed, bar, tslot, kSurTmemCols);
   for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
   fence_async_smem();
   __syncthreads();
-  MlpSmem ms{w, xt, ht, bar, *tslot, 0u};
+  MlpSmem ms{w, xt, xt, bar, *tslot, 0u};
 
   const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2;
   const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
@@ -222,16 +247,16 @@ __global__ void __launch_bounds__(128, 3) k_march_surrogate(FrameArgs f, SurArgs
       }
     }
     if (!__syncthreads_or(pending)) break;
-    {
-      float x[kMlpIn];
-      if (pending) {
-        sur_features(a, f.vol, tf, f.tf_n, p, ray.dir, x);
-      } else {
+    if (pending) {
+      TileSink out{xt, (int)threadIdx.x};
+      sur_features<TEX>(a, f.vol, tf, f.tf_n, p, ray.dir, out);
+    } else {
 #pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) x[k] = 0.0f;
-      }
-      store_row64(xt, threadIdx.x, x, kMlpIn);
+      for (int c = 0; c < 6; ++c) store_chunk(xt, threadIdx.x, c, 0u, 0u, 0u, 0u);
     }
+    // K padding (inputs 48..63): the previous round's hidden layers wrote there
+    store_chunk(xt, threadIdx.x, 6, 0u, 0u, 0u, 0u);
+    store_chunk(xt, threadIdx.x, 7, 0u, 0u, 0u, 0u);
     sync_tiles();
     float y[2];
     bool ok = mlp_forward_tile(ms, y);
@@ -256,25 +281,29 @@ __global__ void __launch_bounds__(128, 3) k_march_surrogate(FrameArgs f, SurArgs
     }
   }
   add_stats(f, n_all, shaded, shaded * (unsigned)(kSurTapFeatures + 6));
-  mlp_cta_end(ms.tmem);
+  mlp_cta_end(ms.tmem, kSurTmemCols);
 }
 
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, unsigned int* work, int* err, cudaStream_t st) {
-  const size_t smem = kPkBytes + 2 * kRowTile + sizeof(float4) * f.tf_n + 16;
-  cudaError_t e = cudaFuncSetAttribute(k_march_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, unsigned int* work, int* err,
+                             cudaStream_t st) {
+  const size_t smem = kPkBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
+  auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_surrogate, 128, smem)) != cudaSuccess)
-    return e;
-  // TMEM: 128 columns per CTA, 512 per SM.
-  per_sm = per_sm < 1 ? 1 : (per_sm > 4 ? 4 : per_sm);
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem)) != cudaSuccess) return e;
+  // TMEM: 64 columns per CTA of the SM's 512.  Work is taken from the ray
+  // counter, so any grid size is correct; this one keeps every SM full.
+  per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
   long long groups = ((long long)((f.W + 7) / 8) * ((f.H + 3) / 4) * 32 + 127) / 128;
   long long ctas = (long long)sms * per_sm;
   if (ctas > groups) ctas = groups;
   if (ctas < 1) ctas = 1;
-  k_march_surrogate<<<(unsigned)ctas, 128, smem, st>>>(f, a, work, err);
+  kern<<<(unsigned)ctas, 128, smem, st>>>(f, a, work, err);
   return cudaGetLastError();
 }
 

@@ -33,6 +33,8 @@ constexpr int kSurTapFeatures = kSurLevels * kSurTaps;  // 42
 
 struct SurArgs {
   PyramidView pyr;  // at least kSurLevels levels
+  cudaTextureObject_t ptex[kSurLevels];  // texture-unit copies of the first levels (tex sampling)
+  cudaTextureObject_t vtex;              // texture-unit copy of the volume (tex sampling)
   const uint8_t* packed;  // packed network image (mlp.cuh)
   int apply_occ, apply_sdw, shadow_type;
   float3 light_pos, light_fwd;
@@ -54,43 +56,70 @@ __device__ __forceinline__ SurFrame sur_frame(const SurArgs& a, float3 tx, float
   return F;
 }
 
-// Segment opacity 1 - exp(-sigma_l(q) d) of one tap; 0 outside the box.
-__device__ __forceinline__ float sur_tap(const PyramidView& P, int l, float3 q, float d, float3 S) {
-  if (q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) return 0.0f;
-  return 1.0f - expf(-pyr_sample_level(P, l, q) * d);
+// Extinction of pyramid level l at texture-space q: FP32 trilinear, or the
+// texture unit's trilinear (8-bit interpolation weights).
+template <bool TEX>
+__device__ __forceinline__ float sur_sigma(const SurArgs& a, int l, float3 q) {
+  if constexpr (TEX) {
+    return tex3D<float>(a.ptex[l], q.x * a.pyr.inv_grid.x, q.y * a.pyr.inv_grid.y, q.z * a.pyr.inv_grid.z);
+  } else {
+    return pyr_sample_level(a.pyr, l, q);
+  }
 }
 
-// The 48 features of one shading point (layout above).
+// Transfer-function extinction of the volume at q.
+template <bool TEX>
+__device__ __forceinline__ float sur_ext(const SurArgs& a, const VolumeView& vol, const float4* tf, int tf_n,
+                                         float3 q) {
+  float v;
+  if constexpr (TEX) {
+    v = tex3D<float>(a.vtex, q.x * a.pyr.inv_grid.x, q.y * a.pyr.inv_grid.y, q.z * a.pyr.inv_grid.z);
+  } else {
+    v = sample_volume(vol, q);
+  }
+  return tf_alpha(tf, tf_n, v);
+}
+
+// Segment opacity 1 - exp(-sigma_l(q) d) of one tap; 0 outside the box.
+template <bool TEX>
+__device__ __forceinline__ float sur_tap(const SurArgs& a, int l, float3 q, float d, float3 S) {
+  if (q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) return 0.0f;
+  return 1.0f - __expf(-sur_sigma<TEX>(a, l, q) * d);
+}
+
+// The 48 features of one shading point (layout above), handed to out(k, v)
+// in order k = 0..47.
+template <bool TEX, class Sink>
 __device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView& vol, const float4* tf, int tf_n,
-                                             float3 tx, float3 dir, float* x) {
+                                             float3 tx, float3 dir, Sink& out) {
   const float3 S = vol.grid;
   SurFrame F = sur_frame(a, tx, dir, S);
   float d = a.unit * 2.0f;
 #pragma unroll
   for (int l = 0; l < kSurLevels; ++l) {
-    x[7 * l + 0] = sur_tap(a.pyr, l, tx, d, S);
-    x[7 * l + 1] = sur_tap(a.pyr, l, tx + F.L * d, d, S);
-    x[7 * l + 2] = sur_tap(a.pyr, l, tx + F.L * (3.0f * d), d, S);
-    x[7 * l + 3] = sur_tap(a.pyr, l, tx + F.n * d, d, S);
-    x[7 * l + 4] = sur_tap(a.pyr, l, tx + F.n * (3.0f * d), d, S);
-    x[7 * l + 5] = sur_tap(a.pyr, l, tx + F.r * d, d, S);
-    x[7 * l + 6] = sur_tap(a.pyr, l, tx + F.u * d, d, S);
+    out(7 * l + 0, sur_tap<TEX>(a, l, tx, d, S));
+    out(7 * l + 1, sur_tap<TEX>(a, l, tx + F.L * d, d, S));
+    out(7 * l + 2, sur_tap<TEX>(a, l, tx + F.L * (3.0f * d), d, S));
+    out(7 * l + 3, sur_tap<TEX>(a, l, tx + F.n * d, d, S));
+    out(7 * l + 4, sur_tap<TEX>(a, l, tx + F.n * (3.0f * d), d, S));
+    out(7 * l + 5, sur_tap<TEX>(a, l, tx + F.r * d, d, S));
+    out(7 * l + 6, sur_tap<TEX>(a, l, tx + F.u * d, d, S));
     d *= 2.0f;
   }
-  x[42] = dot3(F.L, F.r);
-  x[43] = dot3(F.L, F.u);
-  x[44] = dot3(F.L, F.n);
+  out(42, dot3(F.L, F.r));
+  out(43, dot3(F.L, F.u));
+  out(44, dot3(F.L, F.n));
   const float3 sp = vol.spacing;
   float3 g;
-  g.x = 0.5f * (tf_alpha(tf, tf_n, sample_volume(vol, tx + f3(sp.x, 0.0f, 0.0f))) -
-                tf_alpha(tf, tf_n, sample_volume(vol, tx - f3(sp.x, 0.0f, 0.0f))));
-  g.y = 0.5f * (tf_alpha(tf, tf_n, sample_volume(vol, tx + f3(0.0f, sp.y, 0.0f))) -
-                tf_alpha(tf, tf_n, sample_volume(vol, tx - f3(0.0f, sp.y, 0.0f))));
-  g.z = 0.5f * (tf_alpha(tf, tf_n, sample_volume(vol, tx + f3(0.0f, 0.0f, sp.z))) -
-                tf_alpha(tf, tf_n, sample_volume(vol, tx - f3(0.0f, 0.0f, sp.z))));
-  x[45] = dot3(g, F.r);
-  x[46] = dot3(g, F.u);
-  x[47] = dot3(g, F.n);
+  g.x = 0.5f * (sur_ext<TEX>(a, vol, tf, tf_n, tx + f3(sp.x, 0.0f, 0.0f)) -
+                sur_ext<TEX>(a, vol, tf, tf_n, tx - f3(sp.x, 0.0f, 0.0f)));
+  g.y = 0.5f * (sur_ext<TEX>(a, vol, tf, tf_n, tx + f3(0.0f, sp.y, 0.0f)) -
+                sur_ext<TEX>(a, vol, tf, tf_n, tx - f3(0.0f, sp.y, 0.0f)));
+  g.z = 0.5f * (sur_ext<TEX>(a, vol, tf, tf_n, tx + f3(0.0f, 0.0f, sp.z)) -
+                sur_ext<TEX>(a, vol, tf, tf_n, tx - f3(0.0f, 0.0f, sp.z)));
+  out(45, dot3(g, F.r));
+  out(46, dot3(g, F.u));
+  out(47, dot3(g, F.n));
 }
 
 // Shading of the ground-truth renderer with the network's outputs in place of
@@ -118,13 +147,15 @@ cudaError_t launch_sur_collect(const FrameArgs& f, float rate, unsigned long lon
 // Features (n x 48), ground-truth targets (n x 2: GtShade occlusion and
 // shadow) and, when dos_out is given, the cone method's (occlusion, shadow)
 // of n points.  f supplies the volume and transfer function.
-cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const SurArgs& a, const GtArgs* g,
-                             const DosArgs* d, float* x_out, float* t_out, float* dos_out, cudaStream_t st);
+cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const SurArgs& a, bool tex,
+                             const GtArgs* g, const DosArgs* d, float* x_out, float* t_out, float* dos_out,
+                             cudaStream_t st);
 
 // The surrogate-shaded marcher: persistent CTAs take 8x4-pixel blocks of rays
 // from *work (zeroed before the launch); every round, each thread advances
 // its ray to the next shaded sample, the CTA evaluates the network for its
 // 128 samples on the tensor cores, and each thread composites its sample.
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, unsigned int* work, int* err, cudaStream_t st);
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, unsigned int* work, int* err,
+                             cudaStream_t st);
 
 }  // namespace cvr

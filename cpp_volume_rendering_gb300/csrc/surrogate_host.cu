@@ -79,7 +79,19 @@ SurArgs sur_args(cvr_ctx* c, const cvr_light* light, int apply_occ, int apply_sd
   a.ka = ka;
   a.kd = kd;
   a.unit = (c->sx + c->sy + c->sz) / 3.0f;
+  for (int l = 0; l < kSurLevels; ++l) a.ptex[l] = c->tex.pyr_valid ? c->tex.pyr[l].tex : 0;
+  a.vtex = c->tex.vol_valid ? c->tex.vol.tex : 0;
   return a;
+}
+
+// Texture-unit sampling of the network inputs (cvr_set_sampling).
+bool use_tex(cvr_ctx* c) { return (c->sampling & CVR_SAMPLING_TEX_FEATURES) != 0; }
+
+cvr_status prepare_textures(cvr_ctx* c) {
+  if (!use_tex(c)) return CVR_OK;
+  cvr_status st = ensure_volume_texture(c);
+  if (st == CVR_OK) st = ensure_pyramid_textures(c);
+  return st;
 }
 
 GtArgs gt_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light) {
@@ -180,10 +192,11 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   if (c->tf_n * sizeof(float4) > 24 * 1024) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: TF larger than 1536 entries");
   if (p->shadow_type < 0 || p->shadow_type > 2) return fail(c, CVR_ERR_INVALID_ARG, "shadow_type must be 0, 1 or 2");
   st = need_sur(c);
+  if (st == CVR_OK) st = prepare_textures(c);
   if (st != CVR_OK) return st;
   SurArgs a = sur_args(c, light, p->apply_occlusion, p->apply_shadow, p->shadow_type, p->ka, p->kd);
   CK(c, cudaMemsetAsync(c->sur->counter, 0, sizeof(unsigned int), c->stream));
-  CK(c, launch_surrogate(f, a, c->sur->counter, c->mlp->err, c->stream));
+  CK(c, launch_surrogate(f, a, use_tex(c), c->sur->counter, c->mlp->err, c->stream));
   return CVR_OK;
 }
 
@@ -276,6 +289,7 @@ cvr_status cvr_surrogate_label(cvr_ctx* c, const cvr_light* light, const cvr_gt_
   if (st == CVR_OK) st = need_pyramid(c, "cvr_surrogate_label");
   if (st == CVR_OK) st = need_gt(c, p, "cvr_surrogate_label");
   if (st == CVR_OK) st = need_sur(c);
+  if (st == CVR_OK) st = prepare_textures(c);
   if (st != CVR_OK) return st;
   SurState& s = *c->sur;
   if ((x_host || t_host) && n != s.n_pts)
@@ -298,7 +312,7 @@ cvr_status cvr_surrogate_label(cvr_ctx* c, const cvr_light* light, const cvr_gt_
     int cnt = (int)std::min(kChunk, (size_t)np - off);
     float* xo = append_training ? tx + kMlpIn * off : s.cx;
     float* to = append_training ? tt + 2 * off : s.ct;
-    CK(c, launch_sur_label(s.pts + 2 * off, cnt, f, a, &g, nullptr, xo, to, nullptr, c->stream));
+    CK(c, launch_sur_label(s.pts + 2 * off, cnt, f, a, use_tex(c), &g, nullptr, xo, to, nullptr, c->stream));
     if (x_host)
       CK(c, cudaMemcpyAsync(x_host + kMlpIn * off, xo, sizeof(float) * kMlpIn * cnt, cudaMemcpyDeviceToHost, c->stream));
     if (t_host) CK(c, cudaMemcpyAsync(t_host + 2 * off, to, sizeof(float) * 2 * cnt, cudaMemcpyDeviceToHost, c->stream));
@@ -318,6 +332,7 @@ cvr_status cvr_surrogate_evaluate(cvr_ctx* c, const cvr_light* light, const cvr_
   if (st == CVR_OK && cone && !c->cone_ready)
     st = fail(c, CVR_ERR_NOT_READY, "cvr_surrogate_evaluate: cone tables not set");
   if (st == CVR_OK) st = need_sur(c);
+  if (st == CVR_OK) st = prepare_textures(c);
   if (st != CVR_OK) return st;
   if (p->shadow_type < 0 || p->shadow_type > 2 || (cone && (cone->shadow_type < 0 || cone->shadow_type > 2)))
     return fail(c, CVR_ERR_INVALID_ARG, "shadow_type must be 0, 1 or 2");
@@ -333,8 +348,8 @@ cvr_status cvr_surrogate_evaluate(cvr_ctx* c, const cvr_light* light, const cvr_
   CK(c, cudaMemsetAsync(s.acc, 0, sizeof(double) * 8, c->stream));
   for (size_t off = 0; off < (size_t)np; off += kChunk) {
     int cnt = (int)std::min(kChunk, (size_t)np - off);
-    CK(c, launch_sur_label(s.pts + 2 * off, cnt, f, a, &g, cone ? &d : nullptr, s.cx, s.ct, cone ? s.cd : nullptr,
-                           c->stream));
+    CK(c, launch_sur_label(s.pts + 2 * off, cnt, f, a, use_tex(c), &g, cone ? &d : nullptr, s.cx, s.ct,
+                           cone ? s.cd : nullptr, c->stream));
     CK(c, launch_mlp_infer(c->mlp->packed, s.cx, cnt, s.cy, c->mlp->err, c->stream));
     k_sur_errors<<<std::min(1024, (cnt + 255) / 256), 256, 0, c->stream>>>(s.cy, s.ct, cone ? s.cd : nullptr, cnt,
                                                                             s.acc);

@@ -124,5 +124,19 @@ __device__ __forceinline__ uint16_t to_bf16(float x) {
 }
 __device__ __forceinline__ float from_bf16(uint16_t h) { return __uint_as_float((uint32_t)h << 16); }
 
+// Two floats to a packed BF16 pair (lo in bits 0-15), round to nearest even:
+// one cvt instruction, the same rounding as to_bf16 for finite inputs.
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+// Same with ReLU: negative inputs become +0.
+__device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
 }  // namespace tc
 }  // namespace cvr

@@ -1,0 +1,87 @@
+// textures.cu — texture-unit copies of the volume and of the extinction
+// pyramid levels: 3D CUDA arrays sampled with hardware trilinear filtering,
+// normalised coordinates and clamp-to-edge addressing (the OpenGL
+// GL_LINEAR / GL_CLAMP_TO_EDGE sampling of the reference's textures).
+#include "ctx.cuh"
+
+using namespace cvr::ctxutil;
+
+namespace {
+
+cudaError_t make_texture(cvr_ctx* c, TexImage& t, const void* src, size_t elem, cudaChannelFormatDesc desc, int w,
+                         int h, int d, cudaTextureReadMode mode) {
+  t.release();
+  cudaExtent ext = make_cudaExtent((size_t)w, (size_t)h, (size_t)d);
+  cudaError_t e = cudaMalloc3DArray(&t.arr, &desc, ext);
+  if (e != cudaSuccess) return e;
+  cudaMemcpy3DParms cp{};
+  cp.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), (size_t)w * elem, (size_t)w, (size_t)h);
+  cp.dstArray = t.arr;
+  cp.extent = ext;
+  cp.kind = cudaMemcpyDeviceToDevice;
+  if ((e = cudaMemcpy3DAsync(&cp, c->stream)) != cudaSuccess) return e;
+  cudaResourceDesc rd{};
+  rd.resType = cudaResourceTypeArray;
+  rd.res.array.array = t.arr;
+  cudaTextureDesc td{};
+  td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+  td.filterMode = cudaFilterModeLinear;
+  td.readMode = mode;
+  td.normalizedCoords = 1;
+  return cudaCreateTextureObject(&t.tex, &rd, &td, nullptr);
+}
+
+}  // namespace
+
+namespace cvr {
+namespace ctxutil {
+
+cvr_status ensure_volume_texture(cvr_ctx* c) {
+  if (c->tex.vol_valid) return CVR_OK;
+  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "volume texture: no volume");
+  cudaChannelFormatDesc desc = c->dtype == CVR_U8 ? cudaCreateChannelDesc<unsigned char>()
+                                                  : cudaCreateChannelDesc<unsigned short>();
+  cudaError_t e = make_texture(c, c->tex.vol, c->d_vol, c->dtype == CVR_U8 ? 1 : 2, desc, c->nx, c->ny, c->nz,
+                               cudaReadModeNormalizedFloat);
+  if (e != cudaSuccess) {
+    c->tex.vol.release();
+    return cuda_fail(c, e, "volume texture");
+  }
+  c->tex.vol_valid = true;
+  return CVR_OK;
+}
+
+cvr_status ensure_pyramid_textures(cvr_ctx* c) {
+  if (c->tex.pyr_valid) return CVR_OK;
+  if (!c->pyr_ready) return fail(c, CVR_ERR_NOT_READY, "pyramid textures: no pyramid");
+  for (auto& t : c->tex.pyr) t.release();
+  c->tex.n_pyr = 0;
+  for (int l = 0; l < c->pyr.n_levels; ++l) {
+    const int* d = c->pyr.dims[l];
+    cudaError_t e = make_texture(c, c->tex.pyr[l], c->d_pyr + c->pyr.offset[l], sizeof(float),
+                                 cudaCreateChannelDesc<float>(), d[0], d[1], d[2], cudaReadModeElementType);
+    if (e != cudaSuccess) {
+      for (auto& t : c->tex.pyr) t.release();
+      return cuda_fail(c, e, "pyramid texture");
+    }
+    c->tex.n_pyr = l + 1;
+  }
+  c->tex.pyr_valid = true;
+  return CVR_OK;
+}
+
+}  // namespace ctxutil
+}  // namespace cvr
+
+extern "C" {
+
+cvr_status cvr_set_sampling(cvr_ctx* c, int flags) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (flags & ~CVR_SAMPLING_TEX_FEATURES) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_sampling: unknown flags");
+  c->sampling = flags;
+  return CVR_OK;
+}
+
+int cvr_get_sampling(cvr_ctx* c) { return c ? c->sampling : 0; }
+
+}  // extern "C"

@@ -283,6 +283,9 @@ class Context:
         self._ck(self.lib.cvr_set_gt_kernels(self.h, abi.fptr(np.ascontiguousarray(occ)), len(occ),
                                              abi.fptr(np.ascontiguousarray(sdw)), len(sdw)))
 
+    def set_sampling(self, flags: int):
+        self._ck(self.lib.cvr_set_sampling(self.h, flags))
+
     # ---- surrogate network and shading points
     def mlp_init(self, seed: int):
         self._ck(self.lib.cvr_mlp_init(self.h, seed))

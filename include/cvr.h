@@ -264,6 +264,18 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
                         const void* params, size_t params_size, int w, int h, int reps,
                         int* best_tile_w, int* best_tile_h, int* best_variant, float* best_ms);
 
+/* Sampling of secondary lookups (no reference counterpart; the reference's GL
+ * texture() fetches are hardware-filtered, the FP32 hand-written trilinear is
+ * this project's exact form).  CVR_SAMPLING_TEX_FEATURES: the surrogate
+ * network's inputs (pyramid taps and the volume taps of the gradient) go
+ * through the texture unit (trilinear filtering with 8-bit interpolation
+ * weights, |input error| below 3e-2) instead of the FP32 trilinear; the
+ * default, since the network's inputs dominate a surrogate frame.  A network
+ * is best used with the flags it was trained with. */
+#define CVR_SAMPLING_TEX_FEATURES 1
+cvr_status cvr_set_sampling(cvr_ctx* ctx, int flags);
+int cvr_get_sampling(cvr_ctx* ctx);
+
 /* ---- device timing on the context stream --------------------------------- */
 cvr_status cvr_timer_start(cvr_ctx* ctx);
 /* Records the stop event, synchronises and returns elapsed milliseconds. */

@@ -3,12 +3,14 @@ labels of shading points against the CPU oracle, the fused tensor-core marcher
 against the oracle's surrogate renderer, checkpoints, and the trained
 network against the ground-truth integrator and the cone method.
 
-Tolerances: inputs within 2e-4 absolute of the FP64 restatement (FP32
-trilinear taps and exponentials); ground-truth labels within 2e-4; network
-outputs within 1e-2 of the BF16-emulating FP64 forward (a BF16 operand that
-rounds the other way moves an output by ~1e-3); surrogate images within
-2/255 max per channel and PSNR >= 45 dB of the FP64 oracle fed the same
-network (the BF16 operand rounding, not the marcher, sets this bound)."""
+Tolerances: with FP32 hand-written trilinear sampling, inputs within 2e-4
+absolute of the FP64 restatement (FP32 taps and exponentials), surrogate
+images within 1/255 max per channel and PSNR >= 50 dB of the FP64 oracle fed
+the same network; with texture-unit sampling (8-bit interpolation weights,
+the default) inputs within 3e-2 and images within 8/255, PSNR >= 40 dB.
+Ground-truth labels within 2e-4; network outputs within 1e-2 of the
+BF16-emulating FP64 forward (a BF16 operand that rounds the other way moves
+an output by ~1e-3)."""
 import math
 
 import numpy as np
@@ -29,7 +31,9 @@ def small_scene(ctx, n=64, image=64, seed=4100):
     return wl, orc
 
 
-def test_inputs_and_labels_match_oracle(ctx):
+@pytest.mark.parametrize("sampling,tol", [(0, 2e-4), (abi.SAMPLING_TEX_FEATURES, 3e-2)])
+def test_inputs_and_labels_match_oracle(ctx, sampling, tol):
+    ctx.set_sampling(sampling)
     wl, orc = small_scene(ctx)
     ctx.clear_points()
     got = ctx.collect_points(wl.cam, 64, 64, wl.params.step_size, 0.05, 11, 4096)
@@ -47,16 +51,20 @@ def test_inputs_and_labels_match_oracle(ctx):
         x, t = ctx.label_points(lt, gp)
         xr = orc.sur_features(lt, shadow_type, pts)
         err = np.abs(x - xr)
-        print(f"inputs shadow_type={shadow_type}: max err {err.max():.2e}, labels {np.abs(t - orc.gt_points(lt, gp, pts)).max():.2e}")
-        assert err.max() <= 2e-4, (shadow_type, err.max(), np.unravel_index(err.argmax(), err.shape))
+        print(f"inputs sampling={sampling} shadow_type={shadow_type}: max err {err.max():.2e} "
+              f"(taps {err[:, :42].max():.2e}, gradient {err[:, 45:].max():.2e}), "
+              f"labels {np.abs(t - orc.gt_points(lt, gp, pts)).max():.2e}")
+        assert err.max() <= tol, (shadow_type, err.max(), np.unravel_index(err.argmax(), err.shape))
         assert (x[:, :42] >= 0).all() and (x[:, :42] < 1).all()
         assert np.allclose(np.linalg.norm(x[:, 42:45], axis=1), 1.0, atol=1e-4)
         tr = orc.gt_points(lt, gp, pts)
         assert np.abs(t - tr).max() <= 2e-4, np.abs(t - tr).max()
         assert (t >= 0).all() and (t <= 1 + 1e-6).all()
+    ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
 
 
 def test_network_outputs_on_points_match_oracle(ctx, lib):
+    ctx.set_sampling(0)
     wl, orc = small_scene(ctx, seed=4101)
     ctx.mlp_init(21)
     ctx.clear_points()
@@ -69,11 +77,12 @@ def test_network_outputs_on_points_match_oracle(ctx, lib):
     _, yr = orc.sur_features(wl.light, 0, pts, with_outputs=True)
     scale = max(1.0, float(np.abs(yr).max()))
     print(f"network outputs: max err {np.abs(y - yr).max():.2e} (scale {scale:.2f})")
+    ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
     assert np.abs(y - yr).max() <= 1e-2 * scale, np.abs(y - yr).max()
 
 
-@pytest.mark.parametrize("n,image,shadow_type", [(64, 64, 0), (64, 40, 2)])
-def test_surrogate_image_matches_oracle(ctx, n, image, shadow_type):
+@pytest.mark.parametrize("n,image,shadow_type,sampling", [(64, 64, 0, 0), (64, 40, 2, 0), (64, 64, 0, 1)])
+def test_surrogate_image_matches_oracle(ctx, n, image, shadow_type, sampling):
     vol = scene.synth_blobs(n, n, n, abi.CVR_U8, 32, seed=4102, noise_max=20.0)
     wl = scene.surrogate_workload(vol, image)
     if shadow_type == 2:
@@ -87,7 +96,9 @@ def test_surrogate_image_matches_oracle(ctx, n, image, shadow_type):
     p[abi.MLP_PARAMS - 2:] = 0.5
     p[64 * 48 + 64 + 64 * 64 + 64:abi.MLP_PARAMS - 2] *= 0.05
     ctx.mlp_set_params(p)
+    ctx.set_sampling(sampling)
     img, st = ctx.render(abi.SURROGATE, wl.cam, wl.light, wl.params, image, image)
+    ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
     orc = oracle.Oracle()
     oracle.prepare(orc, wl)
     orc.set_mlp(p)
@@ -96,9 +107,10 @@ def test_surrogate_image_matches_oracle(ctx, n, image, shadow_type):
     err = np.abs(img.astype(np.float64) - ref)
     mse = float(np.mean(err ** 2))
     psnr = float("inf") if mse == 0 else 10 * math.log10(1.0 / mse)
-    print(f"surrogate image n={n} {image}^2: max err {err.max():.2e} psnr {psnr:.1f} dB")
-    assert err.max() <= 2.0 / 255.0, err.max()
-    assert psnr >= 45.0, psnr
+    print(f"surrogate image n={n} {image}^2 sampling={sampling}: max err {err.max():.2e} psnr {psnr:.1f} dB")
+    max_abs, min_psnr = (1.0 / 255.0, 50.0) if sampling == 0 else (8.0 / 255.0, 40.0)
+    assert err.max() <= max_abs, err.max()
+    assert psnr >= min_psnr, psnr
     assert abs(int(st.samples) - int(total)) <= max(2, total // 2000)
     assert st.shaded_samples > 0 and st.aux_fetches == 48 * st.shaded_samples
 
