@@ -47,7 +47,7 @@ WORKLOAD_DESC = {
     "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
                     "1 shadow ray to a point light, 1-voxel light steps",
     "surrogate": "learned occlusion/shadow surrogate: MLP 48-64-64-2 (BF16 tcgen05) trained on 4M GT-labelled "
-                 "points of 20 seeded 256^3 blob volumes; held-out 512^3 u8 blobs -> 1024^2, point light",
+                 "points of 20 seeded blob volumes (160^3..448^3); held-out 512^3 u8 blobs -> 1024^2, point light",
 }
 
 MLP_FLOP_PER_SAMPLE = 2 * (48 * 64 + 64 * 64 + 64 * 2)  # 14,592

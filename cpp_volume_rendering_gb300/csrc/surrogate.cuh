@@ -15,7 +15,10 @@
 //          spacing), offsets {0, L, 3L, n, 3n, r, u} * d_l:
 //          x[7l + k] = 1 - exp(-sigma_l(tx + offset_k) * d_l), where sigma_l
 //          is level l of the Gaussian extinction pyramid (trilinear within
-//          the level) and 0 outside the volume box
+//          the level) and 0 outside the volume box; except x[35] (level 5,
+//          centre): the far light path, 1 - exp(-sum_j sigma_5(tx + L s_j) d_5)
+//          over s_j = (4 + j) d_5, j = 0..7, while s_j <= the shadow-ray
+//          length and tx + L s_j is inside the box
 //   x[42..44] = (L.r, L.u, L.n)
 //   x[45..47] = (g.r, g.u, g.n), g = central differences of the transfer
 //               function extinction at +-1 voxel (per voxel)
@@ -39,7 +42,8 @@ struct SurArgs {
   int apply_occ, apply_sdw, shadow_type;
   float3 light_pos, light_fwd;
   float ka, kd;
-  float unit;  // world length of one voxel (mean spacing)
+  float unit;      // world length of one voxel (mean spacing)
+  float sdw_dist;  // shadow-ray length of the integrator the network stands in for
 };
 
 struct SurFrame { float3 n, r, u, L; };
@@ -87,6 +91,20 @@ __device__ __forceinline__ float sur_tap(const SurArgs& a, int l, float3 q, floa
   return 1.0f - __expf(-sur_sigma<TEX>(a, l, q) * d);
 }
 
+// Far light path: level-5 optical depth of the shadow ray beyond the taps.
+template <bool TEX>
+__device__ __forceinline__ float sur_far(const SurArgs& a, float3 tx, float3 L, float d5, float3 S) {
+  float tau = 0.0f;
+#pragma unroll 1
+  for (int j = 0; j < 8; ++j) {
+    float s = (4.0f + (float)j) * d5;
+    float3 q = tx + L * s;
+    if (s > a.sdw_dist || q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) break;
+    tau += sur_sigma<TEX>(a, kSurLevels - 1, q) * d5;
+  }
+  return 1.0f - __expf(-tau);
+}
+
 // The 48 features of one shading point (layout above), handed to out(k, v)
 // in order k = 0..47.
 template <bool TEX, class Sink>
@@ -97,7 +115,7 @@ __device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView&
   float d = a.unit * 2.0f;
 #pragma unroll
   for (int l = 0; l < kSurLevels; ++l) {
-    out(7 * l + 0, sur_tap<TEX>(a, l, tx, d, S));
+    out(7 * l + 0, l == kSurLevels - 1 ? sur_far<TEX>(a, tx, F.L, d, S) : sur_tap<TEX>(a, l, tx, d, S));
     out(7 * l + 1, sur_tap<TEX>(a, l, tx + F.L * d, d, S));
     out(7 * l + 2, sur_tap<TEX>(a, l, tx + F.L * (3.0f * d), d, S));
     out(7 * l + 3, sur_tap<TEX>(a, l, tx + F.n * d, d, S));

@@ -65,9 +65,11 @@ FrameArgs base_frame(cvr_ctx* c) {
   return f;
 }
 
-SurArgs sur_args(cvr_ctx* c, const cvr_light* light, int apply_occ, int apply_sdw, int shadow_type, float ka,
-                 float kd) {
+SurArgs sur_args(cvr_ctx* c, const cvr_light* light, const cvr_gt_params* p, int apply_occ, int apply_sdw) {
+  const int shadow_type = p->shadow_type;
+  const float ka = p->ka, kd = p->kd;
   SurArgs a{};
+  a.sdw_dist = p->sdw_distance;
   a.pyr = c->pyr;
   a.pyr.data = c->d_pyr;
   a.packed = c->mlp ? c->mlp->packed : nullptr;
@@ -194,7 +196,7 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   st = need_sur(c);
   if (st == CVR_OK) st = prepare_textures(c);
   if (st != CVR_OK) return st;
-  SurArgs a = sur_args(c, light, p->apply_occlusion, p->apply_shadow, p->shadow_type, p->ka, p->kd);
+  SurArgs a = sur_args(c, light, p, p->apply_occlusion, p->apply_shadow);
   CK(c, cudaMemsetAsync(c->sur->counter, 0, sizeof(unsigned int), c->stream));
   CK(c, launch_surrogate(f, a, use_tex(c), c->sur->counter, c->mlp->err, c->stream));
   return CVR_OK;
@@ -298,7 +300,7 @@ cvr_status cvr_surrogate_label(cvr_ctx* c, const cvr_light* light, const cvr_gt_
   const int np = s.n_pts;
   if (np == 0) return CVR_OK;
   FrameArgs f = base_frame(c);
-  SurArgs a = sur_args(c, light, 1, 1, p->shadow_type, p->ka, p->kd);
+  SurArgs a = sur_args(c, light, p, 1, 1);
   GtArgs g = gt_args(c, p, light);
   float* tx = nullptr;
   float* tt = nullptr;
@@ -341,7 +343,7 @@ cvr_status cvr_surrogate_evaluate(cvr_ctx* c, const cvr_light* light, const cvr_
   SurState& s = *c->sur;
   const int np = s.n_pts;
   FrameArgs f = base_frame(c);
-  SurArgs a = sur_args(c, light, 1, 1, p->shadow_type, p->ka, p->kd);
+  SurArgs a = sur_args(c, light, p, 1, 1);
   GtArgs g = gt_args(c, p, light);
   DosArgs d{};
   if (cone) d = dos_args(c, cone, light);

@@ -472,12 +472,15 @@ def prepare(ctx: Context, wl: Workload):
 
 # ---------------------------------------------------------------- surrogate
 # Training data: shading points of random views of SURROGATE_VOLUMES seeded
-# blob volumes (the ground-truth workload's generator, seeds 4000..4019),
+# blob volumes (the ground-truth workload's generator, seeds 4000..4019) with
+# sides from 160 to 448 voxels (the blob generator works in the unit cube, so
+# the side sets the scale of the structures and light paths in voxels),
 # labelled by the ground-truth integrator with the ground-truth workload's
 # parameters (16 occlusion rays of 32 voxels over 90 degrees, 1 shadow ray,
 # 1-voxel light steps); half the views use a point light, half a directional.
 SURROGATE_SEED = 4000
 SURROGATE_VOLUMES = 20
+SURROGATE_SIZES = (160, 192, 224, 256, 288, 320, 352, 384, 416, 448)
 
 
 def surrogate_workload(vol: np.ndarray, image: int, spacing=(1.0, 1.0, 1.0)) -> Workload:
@@ -531,21 +534,23 @@ def shaded_sample_count(ctx: Context, cam, w, h, step) -> int:
     return int(st.shaded_samples)
 
 
-def build_surrogate_training_set(ctx: Context, n_volumes=SURROGATE_VOLUMES, size=256, points=4_000_000,
+def build_surrogate_training_set(ctx: Context, n_volumes=SURROGATE_VOLUMES, size=None, points=4_000_000,
                                  views=4, image=256, seed=SURROGATE_SEED, log=None) -> int:
     """Appends ~points labelled shading points to the context's training set
-    (the network must exist: cvr_mlp_init first).  Returns the points added."""
+    (the network must exist: cvr_mlp_init first).  size=None cycles through
+    SURROGATE_SIZES.  Returns the points added."""
     rng = np.random.default_rng(seed)
     per_view = max(1, points // (n_volumes * views))
     added = 0
     for v in range(n_volumes):
-        vol = synth_blobs(size, size, size, abi.CVR_U8, 32, seed=seed + v, noise_max=20.0)
+        size_v = size or SURROGATE_SIZES[v % len(SURROGATE_SIZES)]
+        vol = synth_blobs(size_v, size_v, size_v, abi.CVR_U8, 32, seed=seed + v, noise_max=20.0)
         wl = surrogate_workload(vol, image)
         prepare(ctx, wl)
         step = wl.params.step_size
         for k in range(views):
             directional = (k % 2) == 1
-            cam, lt = random_view(rng, size, directional)
+            cam, lt = random_view(rng, size_v, directional)
             shaded = shaded_sample_count(ctx, cam, image, image, step)
             if shaded == 0:
                 continue

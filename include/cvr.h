@@ -333,7 +333,9 @@ cvr_status cvr_mlp_load(cvr_ctx* ctx, const char* path);
  * u = normalize(-dir x r) of the ground-truth occlusion kernel:
  *   x[7l+k], l = 0..5, k = 0..6: 1 - exp(-sigma_l(p + o_k d_l) d_l), with
  *     d_l = 2^(l+1) voxels, o = {0, L, 3L, n, 3n, r, u}, sigma_l pyramid level l
- *     (0 outside the volume), L the direction towards the light;
+ *     (0 outside the volume), L the direction towards the light; except
+ *     x[35]: 1 - exp(-sum_j sigma_5(p + L s_j) d_5), s_j = (4+j) d_5, j < 8,
+ *     over the s_j within sdw_distance and the volume (the far light path);
  *   x[42..44] = L in (r, u, n); x[45..47] = extinction gradient (central
  *     differences at +-1 voxel) in (r, u, n).
  * Outputs: (ambient occlusion, shadow) as the ground-truth integrator defines

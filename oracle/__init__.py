@@ -51,7 +51,7 @@ def load():
             "oracle_render": (I, [P, I, I, C.POINTER(abi.Camera), C.POINTER(abi.Light), P, I, I, I, I, P, P,
                                   C.POINTER(C.c_uint64), I]),
             "oracle_set_mlp": (I, [P, P, I]),
-            "oracle_sur_features": (I, [P, I, C.POINTER(abi.Light), I, P, I, P, P]),
+            "oracle_sur_features": (I, [P, I, C.POINTER(abi.Light), I, D, P, I, P, P]),
             "oracle_gt_points": (I, [P, C.POINTER(abi.Light), C.POINTER(abi.GtParams), P, I, P]),
         }
         for k, (r, a) in sig.items():
@@ -151,14 +151,15 @@ class Oracle:
         params = np.ascontiguousarray(params, np.float32)
         self._ck(self.lib.oracle_set_mlp(self.h, _p(params), len(params)))
 
-    def sur_features(self, lt, shadow_type, pts, precision=64, with_outputs=False):
+    def sur_features(self, lt, gt_params, pts, precision=64, with_outputs=False):
         """Surrogate inputs (n x 48) of points (n x 6) and, optionally, the
         BF16 network's outputs (n x 2) on them."""
         pts = np.ascontiguousarray(pts, np.float32)
         n = len(pts)
         x = np.zeros((n, 48), np.float64)
         y = np.zeros((n, 2), np.float64) if with_outputs else None
-        self._ck(self.lib.oracle_sur_features(self.h, precision, C.byref(lt), shadow_type, _p(pts), n, _p(x),
+        self._ck(self.lib.oracle_sur_features(self.h, precision, C.byref(lt), gt_params.shadow_type,
+                                              float(gt_params.sdw_distance), _p(pts), n, _p(x),
                                               _p(y) if y is not None else None))
         return (x, y) if with_outputs else x
 

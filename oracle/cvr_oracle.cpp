@@ -518,7 +518,7 @@ template <class T> T gt_shadow(const Frame<T>& f, const Gt<T>& g, V3<T> tx) {
 // direction and the extinction gradient in that frame.
 template <class T>
 void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, int shadow_type, V3<T> light_pos,
-                  V3<T> light_fwd, V3<T> tx, V3<T> dir, T* x) {
+                  V3<T> light_fwd, T sdw_dist, V3<T> tx, V3<T> dir, T* x) {
   Dos<T> d{};
   d.s = &s;
   d.pyr = &pyr;
@@ -533,9 +533,19 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
     if (q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) return T(0);
     return T(1) - std::exp(-pyr_level(f, d, l, q) * dl);
   };
+  auto far = [&](T d5) -> T {  // the far light path of x[35]
+    T tau = 0;
+    for (int j = 0; j < 8; ++j) {
+      T sj = (T(4) + T(j)) * d5;
+      V3<T> q = tx + L * sj;
+      if (sj > sdw_dist || q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) break;
+      tau += pyr_level(f, d, 5, q) * d5;
+    }
+    return T(1) - std::exp(-tau);
+  };
   T dl = T((s.sx + s.sy + s.sz) / 3.0) * T(2);
   for (int l = 0; l < 6; ++l) {
-    x[7 * l + 0] = tap(l, tx, dl);
+    x[7 * l + 0] = l == 5 ? far(dl) : tap(l, tx, dl);
     x[7 * l + 1] = tap(l, tx + L * dl, dl);
     x[7 * l + 2] = tap(l, tx + L * (T(3) * dl), dl);
     x[7 * l + 3] = tap(l, tx + n * dl, dl);
@@ -753,7 +763,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
       march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
                     [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T> dir) {
                       T x[48];
-                      sur_features(f, s, *pyr, p->shadow_type, lpos, lfwd, tx, dir, x);
+                      sur_features(f, s, *pyr, p->shadow_type, lpos, lfwd, T(p->sdw_distance), tx, dir, x);
                       double xd[48], y[2];
                       for (int k = 0; k < 48; ++k) xd[k] = (double)x[k];
                       mlp_forward_bf16(s.mlp, xd, y);
@@ -974,8 +984,8 @@ int oracle_set_mlp(void* h, const float* params, int n) {
 // Network inputs (n x 48) of n points (n x 6: texture-space position, primary
 // direction) and, when y_out is given and parameters are set, the network's
 // outputs (n x 2) on the FP64 features.
-int oracle_sur_features(void* h, int precision, const cvr_light* light, int shadow_type, const float* pts, int n,
-                        double* x_out, double* y_out) {
+int oracle_sur_features(void* h, int precision, const cvr_light* light, int shadow_type, double sdw_dist,
+                        const float* pts, int n, double* x_out, double* y_out) {
   Scene& s = *(Scene*)h;
   if (!light || !pts || !x_out || n < 0) return CVR_ERR_INVALID_ARG;
   if (!s.pyr_ready || s.n_levels < 6) return CVR_ERR_NOT_READY;
@@ -992,8 +1002,8 @@ int oracle_sur_features(void* h, int precision, const cvr_light* light, int shad
     for (int i = 0; i < n; ++i) {
       const float* q = pts + 6 * (size_t)i;
       T x[48];
-      sur_features<T>(f, s, *pyr, shadow_type, from<T>(light->position), from<T>(light->forward), from<T>(q),
-                      from<T>(q + 3), x);
+      sur_features<T>(f, s, *pyr, shadow_type, from<T>(light->position), from<T>(light->forward), T(sdw_dist),
+                      from<T>(q), from<T>(q + 3), x);
       double* xo = x_out + 48 * (size_t)i;
       for (int k = 0; k < 48; ++k) xo[k] = (double)x[k];
       if (y_out) mlp_forward_bf16(s.mlp, xo, y_out + 2 * (size_t)i);

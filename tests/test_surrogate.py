@@ -49,7 +49,7 @@ def test_inputs_and_labels_match_oracle(ctx, sampling, tol):
         gp = scene.gt_params(wl.params.step_size, wl.diagonal, occ_distance=32.0, light_step=1.0, gap=1.0,
                              shadow_type=shadow_type)
         x, t = ctx.label_points(lt, gp)
-        xr = orc.sur_features(lt, shadow_type, pts)
+        xr = orc.sur_features(lt, gp, pts)
         err = np.abs(x - xr)
         print(f"inputs sampling={sampling} shadow_type={shadow_type}: max err {err.max():.2e} "
               f"(taps {err[:, :42].max():.2e}, gradient {err[:, 45:].max():.2e}), "
@@ -74,7 +74,7 @@ def test_network_outputs_on_points_match_oracle(ctx, lib):
     y = np.zeros((len(x), 2), np.float32)
     abi.check(lib.cvr_mlp_forward(ctx.h, abi.fptr(x), len(x), abi.fptr(y)), ctx.h)
     orc.set_mlp(ctx.mlp_params())
-    _, yr = orc.sur_features(wl.light, 0, pts, with_outputs=True)
+    _, yr = orc.sur_features(wl.light, wl.params, pts, with_outputs=True)
     scale = max(1.0, float(np.abs(yr).max()))
     print(f"network outputs: max err {np.abs(y - yr).max():.2e} (scale {scale:.2f})")
     ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
