@@ -80,6 +80,8 @@ struct SurState {
   size_t pts_cap = 0;            // points
   int n_pts = 0;
   unsigned int* counter = nullptr;  // collection count / marcher ray counter
+  unsigned int* order = nullptr;    // marcher block order (+ 64 bucket counters)
+  size_t order_cap = 0;             // blocks
   float* cx = nullptr;           // per-chunk features, targets, predictions, cone values
   float* ct = nullptr;
   float* cy = nullptr;
@@ -87,7 +89,7 @@ struct SurState {
   size_t chunk_cap = 0;
   double* acc = nullptr;         // error sums of cvr_surrogate_evaluate
   ~SurState() {
-    void* bufs[] = {pts, counter, cx, ct, cy, cd, acc};
+    void* bufs[] = {pts, counter, order, cx, ct, cy, cd, acc};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }

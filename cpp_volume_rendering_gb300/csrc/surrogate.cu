@@ -140,6 +140,62 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- block order
+// The marcher takes 8x4-pixel blocks in the order of a permutation that puts
+// long rays first (a longest-processing-time-first schedule: the frame ends
+// when the last block taken is done, so short blocks should come last).  The
+// key of a block is the box chord of its centre ray, in 64 buckets; blocks
+// are counting-sorted by bucket.  The image does not depend on the order.
+constexpr int kOrderBuckets = 64;
+
+__device__ __forceinline__ int block_bucket(const FrameArgs& f, int b, int tiles_x) {
+  int px = (b % tiles_x) * 8 + 4, py = (b / tiles_x) * 4 + 2;
+  px = min(px, f.W - 1);
+  py = min(py, f.H - 1);
+  float3 dir = primary_dir(f.cam, px, py, f.W, f.H);
+  float tnear, tfar;
+  if (!ray_aabb(f.cam.eye, dir, f.vol.grid, tnear, tfar)) return kOrderBuckets - 1;
+  float diag = sqrtf(dot3(f.vol.grid, f.vol.grid));
+  int k = (int)(fabsf(tfar - tnear) / diag * (float)kOrderBuckets);
+  return kOrderBuckets - 1 - min(max(k, 0), kOrderBuckets - 1);  // longest first
+}
+
+__global__ void k_order_count(FrameArgs f, int tiles_x, int n_blocks, unsigned int* counts) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < n_blocks) atomicAdd(counts + block_bucket(f, b, tiles_x), 1u);
+}
+
+// Exclusive scan of the bucket counts (one warp).
+__global__ void k_order_scan(unsigned int* counts) {
+  unsigned int run = 0;
+  const int lane = threadIdx.x;
+  for (int base = 0; base < kOrderBuckets; base += 32) {
+    unsigned int v = counts[base + lane], x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    counts[base + lane] = run + x - v;
+    run += __shfl_sync(0xffffffffu, x, 31);
+  }
+}
+
+__global__ void k_order_scatter(FrameArgs f, int tiles_x, int n_blocks, unsigned int* offsets, unsigned int* perm) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < n_blocks) perm[atomicAdd(offsets + block_bucket(f, b, tiles_x), 1u)] = (unsigned int)b;
+}
+
+cudaError_t launch_block_order(const FrameArgs& f, unsigned int* scratch, unsigned int* perm, cudaStream_t st) {
+  const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2, n = tiles_x * tiles_y;
+  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned int) * kOrderBuckets, st);
+  if (e != cudaSuccess) return e;
+  k_order_count<<<(n + 255) / 256, 256, 0, st>>>(f, tiles_x, n, scratch);
+  k_order_scan<<<1, 32, 0, st>>>(scratch);
+  k_order_scatter<<<(n + 255) / 256, 256, 0, st>>>(f, tiles_x, n, scratch, perm);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------- fused marcher
 // Next ray index for every active lane of a warp with one atomic.
 __device__ __forceinline__ unsigned take_ray(unsigned int* work) {
@@ -187,7 +243,8 @@ struct TileSink {
 constexpr uint32_t kSurTmemCols = 64;
 
 template <bool TEX>
-__global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs a, unsigned int* work, int* err) {
+__global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs a, const unsigned int* __restrict__ order,
+                                                            unsigned int* work, int* err) {
   extern __shared__ __align__(1024) uint8_t sm_sur[];
   uint8_t* w = sm_sur;
   uint8_t* xt = w + kPkBytes;  // input tile, then the hidden activations of the same tile
@@ -215,7 +272,7 @@ __global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs
       if (!has_ray) {
         unsigned idx = take_ray(work);
         if (idx >= total) { no_work = true; break; }
-        int tile = (int)(idx >> 5), within = (int)(idx & 31u);
+        int tile = (int)__ldg(order + (idx >> 5)), within = (int)(idx & 31u);
         ray.px = (tile % tiles_x) * 8 + (within & 7);
         ray.py = (tile / tiles_x) * 4 + (within >> 3);
         if (ray.px >= f.W || ray.py >= f.H) continue;
@@ -284,26 +341,35 @@ __global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs
   mlp_cta_end(ms.tmem, kSurTmemCols);
 }
 
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, unsigned int* work, int* err,
-                             cudaStream_t st) {
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const unsigned int* order,
+                             unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
   auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, smem)) != cudaSuccess) return e;
-  // TMEM: 64 columns per CTA of the SM's 512.  Work is taken from the ray
-  // counter, so any grid size is correct; this one keeps every SM full.
-  per_sm = per_sm < 1 ? 1 : (per_sm > 8 ? 8 : per_sm);
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return e;
+  cudaFuncAttributes fa{};
+  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
+  // Resident CTAs per SM from shared memory, registers (allocated per warp
+  // in units of 8 per thread) and TMEM (64 of 512 columns per CTA).  Work is
+  // taken from the ray counter, so any grid size is correct; this one keeps
+  // every SM full without queued CTAs.
+  const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * 128;
+  int per_sm = smem_sm / (int)(smem + (size_t)reserved + fa.sharedSizeBytes);
+  if (regs_cta > 0) per_sm = min(per_sm, regs_sm / regs_cta);
+  per_sm = max(1, min(per_sm, (int)(512 / kSurTmemCols)));
   long long groups = ((long long)((f.W + 7) / 8) * ((f.H + 3) / 4) * 32 + 127) / 128;
   long long ctas = (long long)sms * per_sm;
   if (ctas > groups) ctas = groups;
   if (ctas < 1) ctas = 1;
-  kern<<<(unsigned)ctas, 128, smem, st>>>(f, a, work, err);
+  kern<<<(unsigned)ctas, 128, smem, st>>>(f, a, order, work, err);
   return cudaGetLastError();
 }
 

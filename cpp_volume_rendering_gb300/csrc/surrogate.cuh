@@ -169,11 +169,16 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
                              const GtArgs* g, const DosArgs* d, float* x_out, float* t_out, float* dos_out,
                              cudaStream_t st);
 
-// The surrogate-shaded marcher: persistent CTAs take 8x4-pixel blocks of rays
-// from *work (zeroed before the launch); every round, each thread advances
-// its ray to the next shaded sample, the CTA evaluates the network for its
-// 128 samples on the tensor cores, and each thread composites its sample.
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, unsigned int* work, int* err,
-                             cudaStream_t st);
+// Longest-first order of the frame's 8x4-pixel blocks: perm receives
+// ceil(W/8) * ceil(H/4) block indices; scratch holds 64 counters.
+cudaError_t launch_block_order(const FrameArgs& f, unsigned int* scratch, unsigned int* perm, cudaStream_t st);
+
+// The surrogate-shaded marcher: persistent CTAs take rays from *work (zeroed
+// before the launch) in 8x4-pixel blocks in the given block order; every
+// round, each thread advances its ray to the next shaded sample, the CTA
+// evaluates the network for its 128 samples on the tensor cores, and each
+// thread composites its sample.
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const unsigned int* order,
+                             unsigned int* work, int* err, cudaStream_t st);
 
 }  // namespace cvr

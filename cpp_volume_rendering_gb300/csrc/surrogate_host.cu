@@ -197,8 +197,18 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   if (st == CVR_OK) st = prepare_textures(c);
   if (st != CVR_OK) return st;
   SurArgs a = sur_args(c, light, p, p->apply_occlusion, p->apply_shadow);
-  CK(c, cudaMemsetAsync(c->sur->counter, 0, sizeof(unsigned int), c->stream));
-  CK(c, launch_surrogate(f, a, use_tex(c), c->sur->counter, c->mlp->err, c->stream));
+  SurState& s = *c->sur;
+  const size_t blocks = (size_t)((f.W + 7) / 8) * ((f.H + 3) / 4);
+  if (s.order_cap < blocks) {
+    if (s.order) cudaFree(s.order);
+    s.order = nullptr;
+    s.order_cap = 0;
+    CK(c, cudaMalloc((void**)&s.order, sizeof(unsigned int) * (blocks + 64)));
+    s.order_cap = blocks;
+  }
+  CK(c, launch_block_order(f, s.order + blocks, s.order, c->stream));
+  CK(c, cudaMemsetAsync(s.counter, 0, sizeof(unsigned int), c->stream));
+  CK(c, launch_surrogate(f, a, use_tex(c), s.order, s.counter, c->mlp->err, c->stream));
   return CVR_OK;
 }
 
