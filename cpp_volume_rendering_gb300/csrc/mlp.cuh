@@ -20,14 +20,16 @@ constexpr int kMlpParams = 64 * 48 + 64 + 64 * 64 + 64 + 2 * 64 + 2;  // 7426
 constexpr int kOffW1 = 0, kOffB1 = 64 * 48, kOffW2 = kOffB1 + 64, kOffB2 = kOffW2 + 64 * 64, kOffW3 = kOffB2 + 64,
               kOffB3 = kOffW3 + 2 * 64;
 
-// Packed image byte offsets (all multiples of 128).
+// Packed image byte offsets (all multiples of 128).  The forward operands
+// and the biases come first, so a forward-only CTA copies kPkFwdBytes.
 constexpr uint32_t kPkW1 = 0;        // 64 rows x K 64, lbo 128, sbo 1024
 constexpr uint32_t kPkW2 = 8192;     // 64 x 64
 constexpr uint32_t kPkW3 = 16384;    // 16 rows (2 used) x 64
-constexpr uint32_t kPkW2T = 18432;   // W2^T: 64 (in) x 64 (out)
-constexpr uint32_t kPkW3T = 26624;   // W3^T: 64 (hidden) x K 16 (2 used), lbo 128, sbo 256
-constexpr uint32_t kPkBias = 28672;  // b1[64], b2[64], b3[2] as FP32
-constexpr uint32_t kPkBytes = 28672 + 1024;
+constexpr uint32_t kPkBias = 18432;  // b1[64], b2[64], b3[2] as FP32
+constexpr uint32_t kPkFwdBytes = 18432 + 1024;
+constexpr uint32_t kPkW2T = 19456;   // W2^T: 64 (in) x 64 (out)
+constexpr uint32_t kPkW3T = 27648;   // W3^T: 64 (hidden) x K 16 (2 used), lbo 128, sbo 256
+constexpr uint32_t kPkBytes = 27648 + 2048;
 
 // One 128-point tile of the forward pass on the tensor cores.  Used by the
 // batch inference kernel and fused into the surrogate marcher.

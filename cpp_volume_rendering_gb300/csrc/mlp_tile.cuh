@@ -132,9 +132,10 @@ __device__ __forceinline__ bool mlp_forward_tile(MlpSmem& s, float y[2]) {
   return ok;
 }
 
-// Shared set-up of an MLP CTA: TMEM allocation, mbarrier, weight image.
+// Shared set-up of an MLP CTA: TMEM allocation, mbarrier, the first 'bytes'
+// of the weight image (kPkBytes, or kPkFwdBytes for the forward pass only).
 __device__ __forceinline__ void mlp_cta_begin(uint8_t* w, const uint8_t* packed, uint64_t* bar, uint32_t* tslot,
-                                              uint32_t tmem_cols = 128) {
+                                              uint32_t tmem_cols = 128, uint32_t bytes = kPkBytes) {
   if (threadIdx.x < 32) tmem_alloc(tslot, tmem_cols);
   if (threadIdx.x == 0) {
     mbar_init(bar, 1);
@@ -142,7 +143,7 @@ __device__ __forceinline__ void mlp_cta_begin(uint8_t* w, const uint8_t* packed,
   }
   const uint4* src = reinterpret_cast<const uint4*>(packed);
   uint4* dst = reinterpret_cast<uint4*>(w);
-  for (int i = threadIdx.x; i < (int)(kPkBytes / 16); i += blockDim.x) dst[i] = src[i];
+  for (int i = threadIdx.x; i < (int)(bytes / 16); i += blockDim.x) dst[i] = src[i];
 }
 
 __device__ __forceinline__ void mlp_cta_end(uint32_t tmem, uint32_t tmem_cols = 128) {

@@ -243,15 +243,15 @@ struct TileSink {
 constexpr uint32_t kSurTmemCols = 64;
 
 template <bool TEX>
-__global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs a, const unsigned int* __restrict__ order,
+__global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs a, const unsigned int* __restrict__ order,
                                                             unsigned int* work, int* err) {
   extern __shared__ __align__(1024) uint8_t sm_sur[];
   uint8_t* w = sm_sur;
-  uint8_t* xt = w + kPkBytes;  // input tile, then the hidden activations of the same tile
+  uint8_t* xt = w + kPkFwdBytes;  // input tile, then the hidden activations of the same tile
   float4* tf = reinterpret_cast<float4*>(xt + kRowTile);
   uint64_t* bar = reinterpret_cast<uint64_t*>(tf + f.tf_n);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
-  mlp_cta_begin(w, a.packed, bar, tslot, kSurTmemCols);
+  mlp_cta_begin(w, a.packed, bar, tslot, kSurTmemCols, kPkFwdBytes);
   for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
   fence_async_smem();
   __syncthreads();
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(128, 4) k_march_surrogate(FrameArgs f, SurArgs
 
 cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const unsigned int* order,
                              unsigned int* work, int* err, cudaStream_t st) {
-  const size_t smem = kPkBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
+  const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
   auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
