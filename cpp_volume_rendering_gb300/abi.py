@@ -36,6 +36,7 @@ MLP_PARAMS = 7426
 MLP_INPUTS = 48
 SURROGATE_LEVELS = 6
 SAMPLING_TEX_FEATURES = 1
+MLP_NOALLOC_MAX_POINTS = 8192
 MAX_CONE_SECTIONS = 512
 
 F3 = C.c_float * 3
@@ -148,6 +149,7 @@ SIGNATURES = {
     "cvr_mlp_get_training_data": (_I, [_P, _FP, _FP, _I]),
     "cvr_mlp_training_size": (_I, [_P]),
     "cvr_mlp_train": (_I, [_P, _I, _I, _F, C.c_uint64, _FP]),
+    "cvr_mlp_gradients_noalloc": (_I, [_P, _P, _P, _I, _P, _P]),
     "cvr_set_sampling": (_I, [_P, _I]),
     "cvr_get_sampling": (_I, [_P]),
     "cvr_mlp_save": (_I, [_P, C.c_char_p]),

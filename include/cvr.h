@@ -304,6 +304,21 @@ cvr_status cvr_mlp_forward(cvr_ctx* ctx, const float* x, int n, float* y);
 /* Gradient of L = 1/(2n) sum (y - t)^2 over n points w.r.t. every parameter,
  * without updating them (grad: CVR_MLP_PARAMS floats).  Synchronous. */
 cvr_status cvr_mlp_gradients(cvr_ctx* ctx, const float* x, const float* t, int n, float* grad, float* loss);
+/* The same gradient from device buffers without allocating any memory (no
+ * counterpart in the reference).  x_dev: n*48 floats, t_dev: n*2, grad_dev:
+ * CVR_MLP_PARAMS floats, loss_dev: 1 float (nullable); all device memory of
+ * the context's device.  Asynchronous on the context stream.  For callers that
+ * must not allocate device memory inside their loop (memory held by another
+ * allocator, or loops where an allocation's synchronisation would stall).
+ * The scratch is one fixed array per device of about 1.9 MB shared by every
+ * context on that device, so calls that overlap in time (other threads or
+ * streams) race on it.  The first call on a device sets the scratch up (its
+ * address, an index list written by a kernel) and synchronises the context
+ * stream, so make that first call before any stream capture begins.  n above
+ * CVR_MLP_NOALLOC_MAX_POINTS is an invalid argument. */
+#define CVR_MLP_NOALLOC_MAX_POINTS 8192
+cvr_status cvr_mlp_gradients_noalloc(cvr_ctx* ctx, const float* x_dev, const float* t_dev, int n, float* grad_dev,
+                                     float* loss_dev);
 /* Training set from host memory (features n*48, targets n*2); n = 0 clears it. */
 cvr_status cvr_mlp_set_training_data(cvr_ctx* ctx, const float* x, const float* t, int n);
 cvr_status cvr_mlp_get_training_data(cvr_ctx* ctx, float* x, float* t, int n);
