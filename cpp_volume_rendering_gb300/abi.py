@@ -37,6 +37,7 @@ MLP_INPUTS = 48
 SURROGATE_LEVELS = 6
 SAMPLING_TEX_FEATURES = 1
 MLP_NOALLOC_MAX_POINTS = 8192
+MAX_VOLUMES = 16
 MAX_CONE_SECTIONS = 512
 
 F3 = C.c_float * 3
@@ -87,6 +88,12 @@ class PyramidParams(C.Structure):
 class FrameStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64), ("aux_fetches", C.c_uint64),
                 ("kernel_ms", C.c_float)]
+
+
+class Job(C.Structure):
+    _fields_ = [("volume", C.c_int), ("method", C.c_int), ("params", C.c_void_p), ("params_size", C.c_size_t),
+                ("camera", Camera), ("light", Light), ("width", C.c_int), ("height", C.c_int),
+                ("out_rgba_dev", C.c_void_p)]
 
 
 PARAMS_OF_METHOD = {PLAIN: PlainParams, EXTINCTION: ExtParams, CONE_DOS: DosParams, GROUND_TRUTH: GtParams,
@@ -150,6 +157,12 @@ SIGNATURES = {
     "cvr_mlp_training_size": (_I, [_P]),
     "cvr_mlp_train": (_I, [_P, _I, _I, _F, C.c_uint64, _FP]),
     "cvr_mlp_gradients_noalloc": (_I, [_P, _P, _P, _I, _P, _P]),
+    "cvr_select_volume": (_I, [_P, _I]),
+    "cvr_current_volume": (_I, [_P]),
+    "cvr_batch_create": (_I, [_P, C.POINTER(Job), _I, C.POINTER(_P)]),
+    "cvr_batch_run": (_I, [_P]),
+    "cvr_batch_job_stats": (_I, [_P, _I, C.POINTER(FrameStats)]),
+    "cvr_batch_destroy": (None, [_P]),
     "cvr_set_sampling": (_I, [_P, _I]),
     "cvr_get_sampling": (_I, [_P]),
     "cvr_mlp_save": (_I, [_P, C.c_char_p]),

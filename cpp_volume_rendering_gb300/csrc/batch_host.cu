@@ -1,0 +1,222 @@
+// batch_host.cu — resident volume slots and batched rendering: a fixed list
+// of frames over the resident volumes, one persistent launch per method,
+// captured with the resets of its counters in one CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "ctx.cuh"
+
+using namespace cvr::ctxutil;
+
+struct cvr_batch {
+  cvr_ctx* ctx = nullptr;
+  int n_jobs = 0;
+  BatchExtJob* d_ext = nullptr;
+  int n_ext = 0;
+  unsigned ext_blocks = 0;
+  int ext_max_table = 0;
+  int ext_variant = 0;
+  float4* d_tables = nullptr;
+  SurJob* d_sur = nullptr;
+  int n_sur = 0;
+  unsigned sur_rays = 0;
+  bool sur_tex = false;
+  unsigned int* d_counters = nullptr;  // [0] extinction tiles, [1] surrogate rays
+  unsigned long long* d_stats = nullptr;  // 3 per job, in the caller's job order
+  cudaGraphExec_t graph = nullptr;
+  ~cvr_batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+    void* bufs[] = {d_ext, d_tables, d_sur, d_counters, d_stats};
+    for (void* p : bufs)
+      if (p) cudaFree(p);
+  }
+};
+
+namespace {
+
+// Makes slot s current; returns the slot that was.
+int select_slot(cvr_ctx* c, int s) {
+  int prev = c->cur_slot;
+  if (s != prev) {
+    swap_volume(c, c->slots[prev]);
+    swap_volume(c, c->slots[s]);
+    c->cur_slot = s;
+  }
+  return prev;
+}
+
+double job_cost(const cvr_job& j, const cvr_ctx* c) {
+  const VolSlot& v = c->slots[j.volume];
+  int nx = j.volume == c->cur_slot ? c->nx : v.nx, ny = j.volume == c->cur_slot ? c->ny : v.ny,
+      nz = j.volume == c->cur_slot ? c->nz : v.nz;
+  return (double)j.width * j.height * std::sqrt((double)nx * nx + (double)ny * ny + (double)nz * nz);
+}
+
+}  // namespace
+
+extern "C" {
+
+cvr_status cvr_select_volume(cvr_ctx* c, int slot) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (slot < 0 || slot >= CVR_MAX_VOLUMES) return fail(c, CVR_ERR_INVALID_ARG, "cvr_select_volume: slot out of range");
+  select_slot(c, slot);
+  return CVR_OK;
+}
+
+int cvr_current_volume(cvr_ctx* c) { return c ? c->cur_slot : -1; }
+
+cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_batch** out) {
+  if (!c || !jobs || n_jobs <= 0 || !out) return fail(c, CVR_ERR_INVALID_ARG, "cvr_batch_create: bad arguments");
+  *out = nullptr;
+  for (int i = 0; i < n_jobs; ++i) {
+    const cvr_job& j = jobs[i];
+    if (j.volume < 0 || j.volume >= CVR_MAX_VOLUMES || !j.params)
+      return fail(c, CVR_ERR_INVALID_ARG, "cvr_batch_create: bad job (volume slot or params)");
+    if (j.method == CVR_METHOD_EXTINCTION ? j.params_size != sizeof(cvr_ext_params)
+                                          : (j.method == CVR_METHOD_SURROGATE ? j.params_size != sizeof(cvr_gt_params)
+                                                                              : true))
+      return fail(c, CVR_ERR_INVALID_ARG, "cvr_batch_create: jobs must be extinction or surrogate with their params");
+  }
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaStreamSynchronize(c->stream));
+  std::unique_ptr<cvr_batch> b(new cvr_batch());
+  b->ctx = c;
+  b->n_jobs = n_jobs;
+  // longest jobs first within each method group
+  std::vector<int> order(n_jobs);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return job_cost(jobs[x], c) > job_cost(jobs[y], c); });
+  CK(c, cudaMalloc((void**)&b->d_stats, sizeof(unsigned long long) * 3 * n_jobs));
+  CK(c, cudaMalloc((void**)&b->d_counters, sizeof(unsigned int) * 2));
+  std::vector<BatchExtJob> ext;
+  std::vector<std::vector<float4>> tables;
+  std::vector<SurJob> sur;
+  const int keep = c->cur_slot;
+  cvr_status st = CVR_OK;
+  for (int oi = 0; oi < n_jobs && st == CVR_OK; ++oi) {
+    const int i = order[oi];
+    const cvr_job& j = jobs[i];
+    select_slot(c, j.volume);
+    FrameArgs f;
+    st = frame_args(c, &j.camera, j.params, j.out_rgba_dev, j.width, j.height, &f);
+    if (st != CVR_OK) break;
+    f.stats = b->d_stats + 3 * (size_t)i;
+    if (j.method == CVR_METHOD_EXTINCTION) {
+      if (f.tile_w * f.tile_h != 128) { st = fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: tile must be 128 pixels"); break; }
+      BatchExtJob J{};
+      const ShadowBoxTable* table = nullptr;
+      st = ext_args(c, static_cast<const cvr_ext_params*>(j.params), &j.light, f, &J.e, &table);
+      if (st != CVR_OK) break;
+      J.f = f;
+      J.blocks_x = (unsigned)((j.width + f.tile_w - 1) / f.tile_w);
+      J.first_block = b->ext_blocks;
+      b->ext_blocks += J.blocks_x * (unsigned)((j.height + f.tile_h - 1) / f.tile_h);
+      std::vector<float4> t;
+      if (table) {
+        J.tn = table->n; J.tax = table->axis; J.tiw = table->interval; J.tvmin = table->vmin; J.tvmax = table->vmax;
+        t.assign(table->lo, table->lo + table->n);
+        t.insert(t.end(), table->hi, table->hi + table->n);
+        b->ext_max_table = std::max(b->ext_max_table, table->n);
+      }
+      tables.push_back(std::move(t));
+      ext.push_back(J);
+    } else {
+      SurJob J{};
+      bool tex = false;
+      st = sur_job_args(c, static_cast<const cvr_gt_params*>(j.params), &j.light, &J.a, &tex);
+      if (st != CVR_OK) break;
+      if (!sur.empty() && tex != b->sur_tex) { st = fail(c, CVR_ERR_INVALID_ARG, "cvr_batch_create: mixed sampling"); break; }
+      b->sur_tex = tex;
+      J.f = f;
+      J.tiles_x = (j.width + 7) / 8;
+      J.first_tile = b->sur_rays / 32u;
+      b->sur_rays += (unsigned)J.tiles_x * (unsigned)((j.height + 3) / 4) * 32u;
+      sur.push_back(J);
+    }
+  }
+  select_slot(c, keep);
+  if (st != CVR_OK) return st;
+  if (!sur.empty() && (!c->mlp || !c->mlp->err)) return fail(c, CVR_ERR_NOT_READY, "cvr_batch_create: no network");
+  b->ext_variant = c->variant;
+  b->n_ext = (int)ext.size();
+  b->n_sur = (int)sur.size();
+  if (b->n_ext) {
+    // shadow tables: one region per job, pointers patched in
+    size_t total = 0;
+    for (auto& t : tables) total += t.size();
+    if (total) {
+      CK(c, cudaMalloc((void**)&b->d_tables, sizeof(float4) * total));
+      size_t off = 0;
+      for (size_t k = 0; k < ext.size(); ++k) {
+        if (tables[k].empty()) continue;
+        CK(c, cudaMemcpy(b->d_tables + off, tables[k].data(), sizeof(float4) * tables[k].size(), cudaMemcpyHostToDevice));
+        ext[k].tlo = b->d_tables + off;
+        ext[k].thi = b->d_tables + off + ext[k].tn;
+        off += tables[k].size();
+      }
+    }
+    CK(c, cudaMalloc((void**)&b->d_ext, sizeof(BatchExtJob) * ext.size()));
+    CK(c, cudaMemcpy(b->d_ext, ext.data(), sizeof(BatchExtJob) * ext.size(), cudaMemcpyHostToDevice));
+  }
+  if (b->n_sur) {
+    CK(c, cudaMalloc((void**)&b->d_sur, sizeof(SurJob) * sur.size()));
+    CK(c, cudaMemcpy(b->d_sur, sur.data(), sizeof(SurJob) * sur.size(), cudaMemcpyHostToDevice));
+  }
+  // capture: counter and statistics resets, then the persistent launches
+  cudaGraph_t g = nullptr;
+  CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * 2, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stats, 0, sizeof(unsigned long long) * 3 * n_jobs, c->stream);
+  if (e == cudaSuccess && b->n_ext)
+    e = launch_batch_extinction(b->d_ext, b->n_ext, b->ext_blocks, b->d_counters, c->tf_n, b->ext_max_table,
+                                b->ext_variant, c->stream);
+  if (e == cudaSuccess && b->n_sur)
+    e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->d_counters + 1, c->mlp->err,
+                               c->stream);
+  cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(c, e != cudaSuccess ? e : e2, "cvr_batch_create: capture");
+  }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cvr_batch_create: graph instantiate");
+  *out = b.release();
+  return CVR_OK;
+}
+
+cvr_status cvr_batch_run(cvr_batch* b) {
+  if (!b || !b->ctx) return CVR_ERR_INVALID_ARG;
+  cvr_ctx* c = b->ctx;
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaGraphLaunch(b->graph, c->stream));
+  return CVR_OK;
+}
+
+cvr_status cvr_batch_job_stats(cvr_batch* b, int job, cvr_frame_stats* out) {
+  if (!b || !b->ctx || !out || job < 0 || job >= b->n_jobs) return CVR_ERR_INVALID_ARG;
+  cvr_ctx* c = b->ctx;
+  CK(c, cudaSetDevice(c->device));
+  unsigned long long h[3];
+  CK(c, cudaMemcpyAsync(h, b->d_stats + 3 * (size_t)job, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  out->samples = h[0];
+  out->shaded_samples = h[1];
+  out->aux_fetches = h[2];
+  out->kernel_ms = 0.0f;
+  return mlp_check_err(c);
+}
+
+void cvr_batch_destroy(cvr_batch* b) {
+  if (!b) return;
+  if (b->ctx) {
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+  }
+  delete b;
+}
+
+}  // extern "C"

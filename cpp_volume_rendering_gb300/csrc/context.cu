@@ -102,6 +102,74 @@ bool build_shadow_table(const cvr_ext_params* p, const float fwd[3], float3 spac
 
 }  // namespace
 
+namespace cvr {
+namespace ctxutil {
+
+cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,
+                      FrameArgs* fo) {
+  if (!c || !cam || !params || !out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: bad arguments");
+  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_render: no volume loaded");
+  if (c->tf_n == 0) return fail(c, CVR_ERR_NOT_READY, "cvr_render: no transfer function");
+  if (!finite3(cam->eye) || !finite3(cam->center) || !finite3(cam->up))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: non-finite camera");
+  FrameArgs f;
+  f.vol = volume_view(c);
+  f.cam = camera_view(cam, w, h);
+  f.tf = c->d_rgbt;
+  f.tf_n = c->tf_n;
+  f.W = w; f.H = h;
+  f.tile_w = c->tile_w; f.tile_h = c->tile_h;
+  f.variant = c->variant;
+  f.out = reinterpret_cast<float4*>(out);
+  f.counts = nullptr;
+  f.stats = c->d_stats;
+  f.step = *static_cast<const float*>(params);  // every params struct starts with step_size
+  if (c->tf_n * sizeof(float4) > 48 * 1024) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: TF larger than 3072 entries");
+  // Steps below 1e-6 of the diagonal would not advance a single-precision
+  // ray parameter; they are rejected rather than marched.
+  const float min_step = 1.0e-6f * std::sqrt(dot3(f.vol.grid, f.vol.grid));
+  if (!(f.step >= min_step) || !std::isfinite(f.step))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: step_size must be finite and >= 1e-6 * diagonal");
+  *fo = f;
+  return CVR_OK;
+}
+
+cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light, const FrameArgs& f, ExtArgs* eo,
+                    const ShadowBoxTable** table) {
+  if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: extinction SAT not built");
+  if (p->apply_occlusion && (p->ao_n_shells < 1 || p->ao_n_shells > CVR_MAX_AO_SHELLS))
+    return fail(c, CVR_ERR_INVALID_ARG, "ao_n_shells must be in [1, 32]");
+  if (p->apply_shadow && !(p->sdw_sample_interval >= 1.0e-3f))
+    return fail(c, CVR_ERR_INVALID_ARG, "sdw_sample_interval must be >= 1e-3 voxels");
+  ExtArgs a{};
+  a.sat.sat = c->d_sat;
+  a.sat.sx = c->nx + 2; a.sat.sy = c->ny + 2; a.sat.sz = c->nz + 2;
+  a.sat.inv_scale = (float)std::ldexp(1.0, -c->sat_frac_bits);
+  a.sat.inv_spacing = f.vol.inv_spacing;
+  a.sat.min_pos = f.vol.spacing * 0.5f;
+  a.sat.max_pos = f.vol.grid + f.vol.spacing * 1.5f;
+  a.apply_occ = p->apply_occlusion; a.apply_sdw = p->apply_shadow;
+  a.n_shells = p->apply_occlusion ? p->ao_n_shells : 1;
+  for (int i = 0; i < CVR_MAX_AO_SHELLS; ++i) a.radii[i] = p->ao_radii[i];
+  a.cone_angle = p->sdw_cone_angle_rad; a.interval = p->sdw_sample_interval;
+  a.initial = p->sdw_initial_step; a.ui_weight = p->sdw_ui_weight; a.max_dist = p->sdw_max_distance;
+  a.shadow_type = p->shadow_type;
+  a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
+  a.ka = p->ka; a.kd = p->kd;
+  *table = nullptr;
+  if (p->apply_shadow && p->shadow_type == 1) {
+    if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
+    if (build_shadow_table(p, light->forward, f.vol.spacing, f.vol.grid, c->sdw_table.get()))
+      *table = c->sdw_table.get();
+  }
+  *eo = a;
+  return CVR_OK;
+}
+
+}  // namespace ctxutil
+}  // namespace cvr
+
 extern "C" {
 
 int cvr_abi_version(void) { return CVR_ABI_VERSION; }
@@ -375,36 +443,16 @@ cvr_status cvr_set_gt_kernels(cvr_ctx* c, const float* occ, int n_occ, const flo
   return CVR_OK;
 }
 
+
 static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
                               const void* params, size_t params_size, float* out, int w, int h, uint32_t* counts,
                               cvr_frame_stats* stats) {
-  if (!c || !cam || !params || !out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
-    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: bad arguments");
-  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_render: no volume loaded");
-  if (c->tf_n == 0) return fail(c, CVR_ERR_NOT_READY, "cvr_render: no transfer function");
-  if (!finite3(cam->eye) || !finite3(cam->center) || !finite3(cam->up))
-    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: non-finite camera");
+  if (!c) return CVR_ERR_INVALID_ARG;
   CK(c, cudaSetDevice(c->device));
   FrameArgs f;
-  f.vol = volume_view(c);
-  f.cam = camera_view(cam, w, h);
-  f.tf = c->d_rgbt;
-  f.tf_n = c->tf_n;
-  f.W = w; f.H = h;
-  f.tile_w = c->tile_w; f.tile_h = c->tile_h;
-  f.variant = c->variant;
-  f.out = reinterpret_cast<float4*>(out);
+  cvr_status fs = frame_args(c, cam, params, out, w, h, &f);
+  if (fs != CVR_OK) return fs;
   f.counts = counts;
-  f.stats = c->d_stats;
-  if (c->tf_n * sizeof(float4) > 48 * 1024) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: TF larger than 3072 entries");
-  // Steps below 1e-6 of the diagonal would not advance a single-precision
-  // ray parameter; they are rejected rather than marched.
-  const float min_step = 1.0e-6f * std::sqrt(dot3(f.vol.grid, f.vol.grid));
-  {
-    float step = *static_cast<const float*>(params);  // every params struct starts with step_size
-    if (!(step >= min_step) || !std::isfinite(step))
-      return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: step_size must be finite and >= 1e-6 * diagonal");
-  }
   CK(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
   cvr_light dl{};
   if (!light) { light = &dl; }
@@ -423,33 +471,10 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
       if (params_size != sizeof(cvr_ext_params)) return fail(c, CVR_ERR_INVALID_ARG, "extinction params size");
       const cvr_ext_params* p = static_cast<const cvr_ext_params*>(params);
       if (!(p->step_size > 0.0f)) return fail(c, CVR_ERR_INVALID_ARG, "step_size must be > 0");
-      if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: extinction SAT not built");
-      if (p->apply_occlusion && (p->ao_n_shells < 1 || p->ao_n_shells > CVR_MAX_AO_SHELLS))
-        return fail(c, CVR_ERR_INVALID_ARG, "ao_n_shells must be in [1, 32]");
-      if (p->apply_shadow && !(p->sdw_sample_interval >= 1.0e-3f))
-        return fail(c, CVR_ERR_INVALID_ARG, "sdw_sample_interval must be >= 1e-3 voxels");
-      f.step = p->step_size;
       ExtArgs a{};
-      a.sat.sat = c->d_sat;
-      a.sat.sx = c->nx + 2; a.sat.sy = c->ny + 2; a.sat.sz = c->nz + 2;
-      a.sat.inv_scale = (float)std::ldexp(1.0, -c->sat_frac_bits);
-      a.sat.inv_spacing = f.vol.inv_spacing;
-      a.sat.min_pos = f.vol.spacing * 0.5f;
-      a.sat.max_pos = f.vol.grid + f.vol.spacing * 1.5f;
-      a.apply_occ = p->apply_occlusion; a.apply_sdw = p->apply_shadow;
-      a.n_shells = p->apply_occlusion ? p->ao_n_shells : 1;
-      for (int i = 0; i < CVR_MAX_AO_SHELLS; ++i) a.radii[i] = p->ao_radii[i];
-      a.cone_angle = p->sdw_cone_angle_rad; a.interval = p->sdw_sample_interval;
-      a.initial = p->sdw_initial_step; a.ui_weight = p->sdw_ui_weight; a.max_dist = p->sdw_max_distance;
-      a.shadow_type = p->shadow_type;
-      a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
-      a.ka = p->ka; a.kd = p->kd;
       const ShadowBoxTable* table = nullptr;
-      if (p->apply_shadow && p->shadow_type == 1) {
-        if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
-        if (build_shadow_table(p, light->forward, f.vol.spacing, f.vol.grid, c->sdw_table.get()))
-          table = c->sdw_table.get();
-      }
+      cvr_status es = ext_args(c, p, light, f, &a, &table);
+      if (es != CVR_OK) return es;
       e = launch_extinction(f, a, table, c->stream);
       break;
     }
@@ -476,6 +501,7 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
     case CVR_METHOD_GROUND_TRUTH: {
       if (params_size != sizeof(cvr_gt_params)) return fail(c, CVR_ERR_INVALID_ARG, "gt params size");
       const cvr_gt_params* p = static_cast<const cvr_gt_params*>(params);
+      const float min_step = 1.0e-6f * std::sqrt(dot3(f.vol.grid, f.vol.grid));
       if (!(p->step_size > 0.0f) || !(p->light_ray_step_size >= min_step))
         return fail(c, CVR_ERR_INVALID_ARG, "step sizes must be >= 1e-6 * diagonal");
       if (!c->gt_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: GT kernel vectors not set");

@@ -8,11 +8,13 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/cvr.h"
 #include "build_tables.cuh"
 #include "march.cuh"
+#include "surrogate.cuh"
 
 using namespace cvr;
 
@@ -71,6 +73,40 @@ struct TexState {
   ~TexState() {
     vol.release();
     for (auto& t : pyr) t.release();
+  }
+};
+
+inline void swap_tex(TexState& a, TexState& b) {
+  std::swap(a.vol, b.vol);
+  std::swap(a.vol_valid, b.vol_valid);
+  for (int l = 0; l < CVR_MAX_LEVELS; ++l) std::swap(a.pyr[l], b.pyr[l]);
+  std::swap(a.n_pyr, b.n_pyr);
+  std::swap(a.pyr_valid, b.pyr_valid);
+}
+
+// A resident volume that is not the current one (cvr_select_volume): the
+// volume, its SAT, pyramid and texture copies.  The current volume lives in
+// the cvr_ctx fields of the same names.
+struct VolSlot {
+  void* d_vol = nullptr;
+  size_t vol_cap = 0;
+  int nx = 0, ny = 0, nz = 0, dtype = 0;
+  float sx = 1, sy = 1, sz = 1;
+  bool has_volume = false;
+  long long* d_sat = nullptr;
+  size_t sat_cap = 0;
+  long long* d_lut = nullptr;
+  int sat_frac_bits = 0;
+  bool sat_ready = false;
+  float* d_pyr = nullptr;
+  size_t pyr_cap = 0;
+  PyramidView pyr{};
+  bool pyr_ready = false;
+  TexState tex;
+  ~VolSlot() {
+    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr};
+    for (void* p : bufs)
+      if (p) cudaFree(p);
   }
 };
 
@@ -143,7 +179,29 @@ struct cvr_ctx {
   std::unique_ptr<SurState> sur;             // surrogate shading points
   TexState tex;                              // texture-unit copies (volume, pyramid)
   int sampling = CVR_SAMPLING_TEX_FEATURES;  // cvr_set_sampling flags
+  VolSlot slots[CVR_MAX_VOLUMES];            // the other resident volumes
+  int cur_slot = 0;
 };
+
+// Exchanges the current-volume fields of c with slot s.
+inline void swap_volume(cvr_ctx* c, VolSlot& s) {
+  std::swap(c->d_vol, s.d_vol);
+  std::swap(c->vol_cap, s.vol_cap);
+  std::swap(c->nx, s.nx); std::swap(c->ny, s.ny); std::swap(c->nz, s.nz);
+  std::swap(c->dtype, s.dtype);
+  std::swap(c->sx, s.sx); std::swap(c->sy, s.sy); std::swap(c->sz, s.sz);
+  std::swap(c->has_volume, s.has_volume);
+  std::swap(c->d_sat, s.d_sat);
+  std::swap(c->sat_cap, s.sat_cap);
+  std::swap(c->d_lut, s.d_lut);
+  std::swap(c->sat_frac_bits, s.sat_frac_bits);
+  std::swap(c->sat_ready, s.sat_ready);
+  std::swap(c->d_pyr, s.d_pyr);
+  std::swap(c->pyr_cap, s.pyr_cap);
+  std::swap(c->pyr, s.pyr);
+  std::swap(c->pyr_ready, s.pyr_ready);
+  swap_tex(c->tex, s.tex);
+}
 
 namespace cvr {
 namespace ctxutil {
@@ -217,6 +275,16 @@ cvr_status mlp_check_err(cvr_ctx* c);
 // Texture objects of the volume / pyramid levels, (re)made when stale.
 cvr_status ensure_volume_texture(cvr_ctx* c);
 cvr_status ensure_pyramid_textures(cvr_ctx* c);
+// Frame arguments of a render of the current volume (validated; f.step from
+// the params struct's leading step_size, f.counts null, f.stats the context's).
+cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,
+                      FrameArgs* f);
+// Extinction arguments of the current volume; *table: the directional
+// shadow-box table (context-owned staging, valid until the next call) or null.
+cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light, const FrameArgs& f, ExtArgs* e,
+                    const ShadowBoxTable** table);
+// Surrogate arguments of the current volume (pyramid, textures, network).
+cvr_status sur_job_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light, SurArgs* a, bool* tex);
 // The CVR_METHOD_SURROGATE launch of cvr_render.
 cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params* p, const cvr_light* light);
 

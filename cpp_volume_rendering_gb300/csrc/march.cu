@@ -83,6 +83,79 @@ cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Batched extinction frames: persistent CTAs take tiles of all jobs from one
+// counter; the job descriptor, transfer function and shadow table are staged
+// in shared memory whenever a CTA moves to another job.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_batch_extinction(const BatchExtJob* __restrict__ jobs, int n_jobs,
+                                                                unsigned total, unsigned* counter) {
+  __shared__ BatchExtJob J;
+  __shared__ unsigned s_blk;
+  __shared__ int s_job;
+  extern __shared__ float4 sm_bt[];
+  int cur = -1;
+  while (true) {
+    if (threadIdx.x == 0) {
+      const unsigned b = atomicAdd(counter, 1u);
+      s_blk = b;
+      if (b < total) {
+        int lo = 0, hi = n_jobs - 1;  // last job whose first tile is <= b
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (jobs[mid].first_block <= b) lo = mid;
+          else hi = mid - 1;
+        }
+        s_job = lo;
+      }
+    }
+    __syncthreads();
+    const unsigned b = s_blk;
+    if (b >= total) break;
+    const int j = s_job;
+    if (j != cur) {
+      const int* src = reinterpret_cast<const int*>(jobs + j);
+      int* dst = reinterpret_cast<int*>(&J);
+      for (int i = threadIdx.x; i < (int)(sizeof(BatchExtJob) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+      __syncthreads();
+      for (int i = threadIdx.x; i < J.f.tf_n; i += blockDim.x) sm_bt[i] = J.f.tf[i];
+      for (int i = threadIdx.x; i < J.tn; i += blockDim.x) {
+        sm_bt[J.f.tf_n + i] = J.tlo[i];
+        sm_bt[J.f.tf_n + J.tn + i] = J.thi[i];
+      }
+      cur = j;
+      __syncthreads();
+    }
+    const unsigned local = b - J.first_block;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps_x = J.f.tile_w >> 3;
+    const int px = (int)(local % J.blocks_x) * J.f.tile_w + (warp % warps_x) * 8 + (lane & 7);
+    const int py = (int)(local / J.blocks_x) * J.f.tile_h + (warp / warps_x) * 4 + (lane >> 3);
+    ExtShade sh{&J.e};
+    if (J.tn > 0) {
+      sh.tlo = sm_bt + J.f.tf_n; sh.thi = sm_bt + J.f.tf_n + J.tn; sh.tn = J.tn; sh.tax = J.tax;
+      sh.tiw = J.tiw; sh.tvmin = J.tvmin; sh.tvmax = J.tvmax;
+    }
+    march_ray(J.f, sm_bt, sh, px, py);
+    __syncthreads();  // J and the staged tables are reused by the next tile
+  }
+}
+
+cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
+                                    int tf_n, int max_table, int variant, cudaStream_t st) {
+  const size_t smem = sizeof(float4) * (tf_n + 2 * max_table);
+  auto kern = variant == 1 ? k_batch_extinction<4> : (variant == 2 ? k_batch_extinction<6> : k_batch_extinction<1>);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = resident_ctas(kern, 128, smem, &per_sm)) != cudaSuccess) return e;
+  unsigned ctas = (unsigned)sms * (unsigned)per_sm;
+  if (ctas > total_blocks) ctas = total_blocks;
+  if (ctas == 0) return cudaSuccess;
+  kern<<<ctas, 128, smem, st>>>(jobs, n_jobs, total_blocks, counter);
+  return cudaGetLastError();
+}
+
 template <int MINB>
 static void launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
   if (table) {

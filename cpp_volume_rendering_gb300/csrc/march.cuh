@@ -79,6 +79,47 @@ struct GtArgs {
   float ka, kd;
 };
 
+// CTAs of kern that fit on one SM at once, from its shared memory (dynamic +
+// static + the per-block reservation) and registers (allocated per warp in
+// units of 8 per thread).  Persistent launches size their grids with it.
+template <class K>
+cudaError_t resident_ctas(K kern, int threads, size_t dyn_smem, int* out) {
+  int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0, threads_sm = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev)) != cudaSuccess) return e;
+  cudaFuncAttributes fa{};
+  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
+  int n = smem_sm / (int)(dyn_smem + fa.sharedSizeBytes + (size_t)reserved);
+  const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * threads;
+  if (regs_cta > 0) n = n < regs_sm / regs_cta ? n : regs_sm / regs_cta;
+  n = n < threads_sm / threads ? n : threads_sm / threads;
+  *out = n < 1 ? 1 : n;
+  return cudaSuccess;
+}
+
+// One job of a batch of extinction frames (device table entry).  f.stats
+// points at the job's three counters; f.tile_w / tile_h are the batch's tile.
+struct BatchExtJob {
+  FrameArgs f;
+  ExtArgs e;
+  const float4* tlo;  // directional shadow-box table in global memory, or null
+  const float4* thi;
+  int tn, tax;
+  float tiw, tvmin, tvmax;
+  unsigned first_block;  // first batch-wide tile index of the job
+  unsigned blocks_x;     // tiles per image row
+};
+
+// Persistent launch over all tiles of all jobs (jobs ordered by first_block):
+// each CTA takes tiles from *counter (zeroed before the launch).  variant as
+// in FrameArgs; max_table = the largest shadow table of the jobs.
+cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
+                                    int tf_n, int max_table, int variant, cudaStream_t st);
+
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
 // table == nullptr: per-sample cone geometry (point lights, or too many boxes).
 cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st);

@@ -473,9 +473,7 @@ __device__ __forceinline__ void add_stats(const FrameArgs& f, unsigned int n, un
 // sample at s + h/2, skip transparent samples, alpha = 1 - exp(-sigma h),
 // front-to-back composite, stop once alpha > 0.99.
 template <class Shade>
-__device__ __forceinline__ void march_pixel(const FrameArgs& f, const float4* tf, const Shade& sh) {
-  int px, py;
-  pixel_of(f, px, py);
+__device__ __forceinline__ void march_ray(const FrameArgs& f, const float4* tf, const Shade& sh, int px, int py) {
   bool inside = px < f.W && py < f.H;
   unsigned int n = 0, shaded = 0, aux = 0;
   if (inside) {
@@ -513,6 +511,14 @@ __device__ __forceinline__ void march_pixel(const FrameArgs& f, const float4* tf
     if (f.counts) f.counts[o] = n;
   }
   add_stats(f, n, shaded, aux);
+}
+
+// One CTA-tile pixel per thread (pixel_of).
+template <class Shade>
+__device__ __forceinline__ void march_pixel(const FrameArgs& f, const float4* tf, const Shade& sh) {
+  int px, py;
+  pixel_of(f, px, py);
+  march_ray(f, tf, sh, px, py);
 }
 
 // Loads the RGBt table into shared memory (n <= tf_smem_cap) and returns it.

@@ -214,13 +214,69 @@ struct SurRay {
   float4 dst;
   unsigned n, max_iter;
   int px, py;
+  int job;
 };
 
-__device__ __forceinline__ void sur_finish(const FrameArgs& f, const SurRay& r, unsigned& n_all) {
+// Where a marcher thread's rays come from.  SingleSource: one frame, rays in
+// the longest-first block order.  BatchSource: the jobs of a batch, each a
+// run of 8x4-pixel tiles of one counter (jobs ordered by first tile).
+struct SingleSource {
+  const FrameArgs& f0;
+  const SurArgs& a0;
+  const unsigned int* order;
+  int tiles_x;
+  unsigned total;
+  __device__ __forceinline__ const FrameArgs& f(int) const { return f0; }
+  __device__ __forceinline__ const SurArgs& a(int) const { return a0; }
+  __device__ __forceinline__ void locate(unsigned idx, SurRay& r) const {
+    const int tile = (int)__ldg(order + (idx >> 5)), within = (int)(idx & 31u);
+    r.job = 0;
+    r.px = (tile % tiles_x) * 8 + (within & 7);
+    r.py = (tile / tiles_x) * 4 + (within >> 3);
+  }
+};
+
+struct BatchSource {
+  const SurJob* jobs;
+  int n_jobs;
+  unsigned total;
+  __device__ __forceinline__ const FrameArgs& f(int j) const { return jobs[j].f; }
+  __device__ __forceinline__ const SurArgs& a(int j) const { return jobs[j].a; }
+  __device__ __forceinline__ void locate(unsigned idx, SurRay& r) const {
+    const unsigned tile = idx >> 5;
+    int lo = 0, hi = n_jobs - 1;  // last job whose first tile is <= tile
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (jobs[mid].first_tile <= tile) lo = mid;
+      else hi = mid - 1;
+    }
+    const unsigned local = tile - jobs[lo].first_tile;
+    const int tx = jobs[lo].tiles_x, within = (int)(idx & 31u);
+    r.job = lo;
+    r.px = (int)(local % (unsigned)tx) * 8 + (within & 7);
+    r.py = (int)(local / (unsigned)tx) * 4 + (within >> 3);
+  }
+};
+
+// Step counts of the rays a thread finished, flushed to the job's counters
+// when the thread moves to another job and at the end.
+struct SurCounts {
+  int job = -1;
+  unsigned n = 0, shaded = 0;
+  __device__ __forceinline__ void flush(unsigned long long* stats) {
+    if (job >= 0 && stats && (n | shaded)) {
+      atomicAdd(stats + 0, (unsigned long long)n);
+      atomicAdd(stats + 1, (unsigned long long)shaded);
+      atomicAdd(stats + 2, (unsigned long long)shaded * (unsigned long long)(kSurTapFeatures + 6));
+    }
+    n = shaded = 0;
+  }
+};
+
+__device__ __forceinline__ void sur_finish(const FrameArgs& f, const SurRay& r) {
   size_t o = (size_t)r.py * f.W + r.px;
   f.out[o] = r.dst;
   if (f.counts) f.counts[o] = r.n;
-  n_all += r.n;
 }
 
 // Packs features pairwise to BF16 and stores each 8-feature chunk of this
@@ -242,46 +298,50 @@ struct TileSink {
 
 constexpr uint32_t kSurTmemCols = 64;
 
-template <bool TEX>
-__global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs a, const unsigned int* __restrict__ order,
-                                                            unsigned int* work, int* err) {
+// The marcher body for either source.  tf_src / tf_n: the transfer function
+// (shared by all jobs), packed: the network image.
+template <bool TEX, bool BATCH, class Src>
+__device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_src, int tf_n, const uint8_t* packed,
+                                          unsigned int* work, int* err) {
   extern __shared__ __align__(1024) uint8_t sm_sur[];
   uint8_t* w = sm_sur;
   uint8_t* xt = w + kPkFwdBytes;  // input tile, then the hidden activations of the same tile
   float4* tf = reinterpret_cast<float4*>(xt + kRowTile);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tf + f.tf_n);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tf + tf_n);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
-  mlp_cta_begin(w, a.packed, bar, tslot, kSurTmemCols, kPkFwdBytes);
-  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
+  mlp_cta_begin(w, packed, bar, tslot, kSurTmemCols, kPkFwdBytes);
+  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) tf[i] = tf_src[i];
   fence_async_smem();
   __syncthreads();
   MlpSmem ms{w, xt, xt, bar, *tslot, 0u};
 
-  const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2;
-  const unsigned total = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
+  const unsigned total = src_rays.total;
   SurRay ray{};
   bool has_ray = false, pending = false, no_work = false;
   float4 src = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   float3 p = f3(0.0f, 0.0f, 0.0f);
   float h = 0.0f;
-  unsigned n_all = 0, shaded = 0;
+  SurCounts cnt;
   while (true) {
     // Advance this thread's ray to its next shaded sample, taking new rays
-    // as rays end, until a sample is pending or the frame has no rays left.
+    // as rays end, until a sample is pending or no rays are left.
     while (!pending && !no_work) {
       if (!has_ray) {
         unsigned idx = take_ray(work);
         if (idx >= total) { no_work = true; break; }
-        int tile = (int)__ldg(order + (idx >> 5)), within = (int)(idx & 31u);
-        ray.px = (tile % tiles_x) * 8 + (within & 7);
-        ray.py = (tile / tiles_x) * 4 + (within >> 3);
+        src_rays.locate(idx, ray);
+        const FrameArgs& f = src_rays.f(ray.job);
         if (ray.px >= f.W || ray.py >= f.H) continue;
+        if (ray.job != cnt.job) {
+          if (BATCH) cnt.flush(src_rays.f(cnt.job < 0 ? 0 : cnt.job).stats);
+          cnt.job = ray.job;
+        }
         ray.dir = primary_dir(f.cam, ray.px, ray.py, f.W, f.H);
         ray.dst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         ray.n = 0;
         float tnear, tfar;
         if (!ray_aabb(f.cam.eye, ray.dir, f.vol.grid, tnear, tfar)) {
-          sur_finish(f, ray, n_all);
+          sur_finish(f, ray);
           continue;
         }
         ray.D = fabsf(tfar - tnear);
@@ -290,23 +350,27 @@ __global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs
         ray.max_iter = (unsigned)fminf(ray.D / f.step, 1.0e9f) + 4u;
         has_ray = true;
       }
-      while (ray.s < ray.D && ray.n < ray.max_iter) {
-        h = fminf(f.step, ray.D - ray.s);
-        p = ray.tex0 + ray.dir * (ray.s + h * 0.5f);
-        src = tf_lookup(tf, f.tf_n, sample_volume(f.vol, p));
-        ++ray.n;
-        if (src.w > 0.0f) { pending = true; break; }
-        ray.s = ray.s + h;
-      }
-      if (!pending) {
-        sur_finish(f, ray, n_all);
-        has_ray = false;
+      {
+        const FrameArgs& f = src_rays.f(ray.job);
+        while (ray.s < ray.D && ray.n < ray.max_iter) {
+          h = fminf(f.step, ray.D - ray.s);
+          p = ray.tex0 + ray.dir * (ray.s + h * 0.5f);
+          src = tf_lookup(tf, tf_n, sample_volume(f.vol, p));
+          ++ray.n;
+          if (src.w > 0.0f) { pending = true; break; }
+          ray.s = ray.s + h;
+        }
+        if (!pending) {
+          sur_finish(f, ray);
+          cnt.n += ray.n;
+          has_ray = false;
+        }
       }
     }
     if (!__syncthreads_or(pending)) break;
     if (pending) {
       TileSink out{xt, (int)threadIdx.x};
-      sur_features<TEX>(a, f.vol, tf, f.tf_n, p, ray.dir, out);
+      sur_features<TEX>(src_rays.a(ray.job), src_rays.f(ray.job).vol, tf, tf_n, p, ray.dir, out);
     } else {
 #pragma unroll
       for (int c = 0; c < 6; ++c) store_chunk(xt, threadIdx.x, c, 0u, 0u, 0u, 0u);
@@ -322,54 +386,84 @@ __global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs
       break;
     }
     if (pending) {
-      ++shaded;
+      ++cnt.shaded;
       pending = false;
-      src = sur_shade(a, src, y[0], y[1]);
+      src = sur_shade(src_rays.a(ray.job), src, y[0], y[1]);
       src.w = 1.0f - expf(-src.w * h);
       src.x *= src.w; src.y *= src.w; src.z *= src.w;
       float r = 1.0f - ray.dst.w;
       ray.dst.x += r * src.x; ray.dst.y += r * src.y; ray.dst.z += r * src.z; ray.dst.w += r * src.w;
       if (ray.dst.w > 0.99f) {
-        sur_finish(f, ray, n_all);
+        sur_finish(src_rays.f(ray.job), ray);
+        cnt.n += ray.n;
         has_ray = false;
       } else {
         ray.s = ray.s + h;
       }
     }
   }
-  add_stats(f, n_all, shaded, shaded * (unsigned)(kSurTapFeatures + 6));
+  if (BATCH) {
+    cnt.flush(src_rays.f(cnt.job < 0 ? 0 : cnt.job).stats);
+  } else {
+    add_stats(src_rays.f(0), cnt.n, cnt.shaded, cnt.shaded * (unsigned)(kSurTapFeatures + 6));
+  }
   mlp_cta_end(ms.tmem, kSurTmemCols);
+}
+
+template <bool TEX>
+__global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs a, const unsigned int* __restrict__ order,
+                                                            unsigned int* work, int* err) {
+  const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2;
+  SingleSource s{f, a, order, tiles_x, (unsigned)tiles_x * (unsigned)tiles_y * 32u};
+  sur_march<TEX, false>(s, f.tf, f.tf_n, a.packed, work, err);
+}
+
+template <bool TEX>
+__global__ void __launch_bounds__(128, 5) k_batch_surrogate(const SurJob* __restrict__ jobs, int n_jobs,
+                                                            unsigned total_rays, unsigned int* work, int* err) {
+  BatchSource s{jobs, n_jobs, total_rays};
+  sur_march<TEX, true>(s, jobs[0].f.tf, jobs[0].f.tf_n, jobs[0].a.packed, work, err);
+}
+
+// Persistent grid: every SM full (resident CTAs from shared memory and
+// registers, at most 512 / 64 by TMEM), no more CTAs than 128-ray groups.
+template <class K>
+static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, unsigned* ctas) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = resident_ctas(kern, 128, smem, &per_sm)) != cudaSuccess) return e;
+  per_sm = per_sm > (int)(512 / kSurTmemCols) ? (int)(512 / kSurTmemCols) : per_sm;
+  unsigned long long n = (unsigned long long)sms * (unsigned long long)per_sm, groups = (rays + 127ull) / 128ull;
+  if (n > groups) n = groups;
+  *ctas = n < 1 ? 1u : (unsigned)n;
+  return cudaSuccess;
+}
+
+cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
+                                   unsigned int* work, int* err, cudaStream_t st) {
+  const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * tf_n + 16;
+  auto kern = tex ? k_batch_surrogate<true> : k_batch_surrogate<false>;
+  unsigned ctas = 0;
+  cudaError_t e = surrogate_grid(kern, smem, total_rays, &ctas);
+  if (e != cudaSuccess) return e;
+  kern<<<ctas, 128, smem, st>>>(jobs, n_jobs, total_rays, work, err);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const unsigned int* order,
                              unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
   auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const unsigned rays = (unsigned)((f.W + 7) / 8) * (unsigned)((f.H + 3) / 4) * 32u;
+  unsigned ctas = 0;
+  cudaError_t e = surrogate_grid(kern, smem, rays, &ctas);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev)) != cudaSuccess) return e;
-  cudaFuncAttributes fa{};
-  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
-  // Resident CTAs per SM from shared memory, registers (allocated per warp
-  // in units of 8 per thread) and TMEM (64 of 512 columns per CTA).  Work is
-  // taken from the ray counter, so any grid size is correct; this one keeps
-  // every SM full without queued CTAs.
-  const int regs_cta = ((fa.numRegs + 7) / 8) * 8 * 128;
-  int per_sm = smem_sm / (int)(smem + (size_t)reserved + fa.sharedSizeBytes);
-  if (regs_cta > 0) per_sm = min(per_sm, regs_sm / regs_cta);
-  per_sm = max(1, min(per_sm, (int)(512 / kSurTmemCols)));
-  long long groups = ((long long)((f.W + 7) / 8) * ((f.H + 3) / 4) * 32 + 127) / 128;
-  long long ctas = (long long)sms * per_sm;
-  if (ctas > groups) ctas = groups;
-  if (ctas < 1) ctas = 1;
-  kern<<<(unsigned)ctas, 128, smem, st>>>(f, a, order, work, err);
+  kern<<<ctas, 128, smem, st>>>(f, a, order, work, err);
   return cudaGetLastError();
 }
 

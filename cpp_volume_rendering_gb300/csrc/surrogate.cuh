@@ -169,6 +169,20 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
                              const GtArgs* g, const DosArgs* d, float* x_out, float* t_out, float* dos_out,
                              cudaStream_t st);
 
+// One job of a batch of surrogate frames (device table entry).  f.stats points
+// at the job's three counters; f.tf / f.tf_n and a.packed of job 0 serve all.
+struct SurJob {
+  FrameArgs f;
+  SurArgs a;
+  unsigned first_tile;  // batch-wide index of the job's first 8x4-pixel tile
+  int tiles_x;
+};
+
+// Persistent launch over all rays of all jobs (jobs ordered by first_tile;
+// total_rays = 32 x all tiles), rays taken from *work (zeroed before).
+cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
+                                   unsigned int* work, int* err, cudaStream_t st);
+
 // Longest-first order of the frame's 8x4-pixel blocks: perm receives
 // ceil(W/8) * ceil(H/4) block indices; scratch holds 64 counters.
 cudaError_t launch_block_order(const FrameArgs& f, unsigned int* scratch, unsigned int* perm, cudaStream_t st);

@@ -187,7 +187,7 @@ __global__ void k_sur_errors(const float* __restrict__ y, const float* __restric
 namespace cvr {
 namespace ctxutil {
 
-cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params* p, const cvr_light* light) {
+cvr_status sur_job_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light, SurArgs* a, bool* tex) {
   if (!c->mlp || !c->mlp->ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: surrogate network not initialised");
   cvr_status st = need_pyramid(c, "cvr_render");
   if (st != CVR_OK) return st;
@@ -196,7 +196,16 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   st = need_sur(c);
   if (st == CVR_OK) st = prepare_textures(c);
   if (st != CVR_OK) return st;
-  SurArgs a = sur_args(c, light, p, p->apply_occlusion, p->apply_shadow);
+  *a = sur_args(c, light, p, p->apply_occlusion, p->apply_shadow);
+  *tex = use_tex(c);
+  return CVR_OK;
+}
+
+cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params* p, const cvr_light* light) {
+  SurArgs a{};
+  bool tex = false;
+  cvr_status st = sur_job_args(c, p, light, &a, &tex);
+  if (st != CVR_OK) return st;
   SurState& s = *c->sur;
   const size_t blocks = (size_t)((f.W + 7) / 8) * ((f.H + 3) / 4);
   if (s.order_cap < blocks) {
@@ -208,7 +217,7 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   }
   CK(c, launch_block_order(f, s.order + blocks, s.order, c->stream));
   CK(c, cudaMemsetAsync(s.counter, 0, sizeof(unsigned int), c->stream));
-  CK(c, launch_surrogate(f, a, use_tex(c), s.order, s.counter, c->mlp->err, c->stream));
+  CK(c, launch_surrogate(f, a, tex, s.order, s.counter, c->mlp->err, c->stream));
   return CVR_OK;
 }
 

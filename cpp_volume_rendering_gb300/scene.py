@@ -283,6 +283,9 @@ class Context:
         self._ck(self.lib.cvr_set_gt_kernels(self.h, abi.fptr(np.ascontiguousarray(occ)), len(occ),
                                              abi.fptr(np.ascontiguousarray(sdw)), len(sdw)))
 
+    def select_volume(self, slot: int):
+        self._ck(self.lib.cvr_select_volume(self.h, slot))
+
     def set_sampling(self, flags: int):
         self._ck(self.lib.cvr_set_sampling(self.h, flags))
 
@@ -592,3 +595,94 @@ def evaluate_surrogate(ctx: Context, wl: Workload, points=2_000_000, seed=7) -> 
     r = ctx.evaluate_points(wl.light, wl.params, cone_params_of(wl))
     r["shaded_samples"] = shaded
     return r
+
+
+# ---------------------------------------------------------------- batches
+# The batched workload: 4 volumes of uneven size (128^3 u8, 192x256x160 u16,
+# 256^3 u8, 384^3 u16, seeded value noise, seeds 5000..5003) x 16 views on a
+# sphere x 4 directional lights, 512^2 images, extinction shading (SAT AO
+# radii 2, 6, 16 + directional SAT cone shadow) and surrogate shading (the
+# same views and lights, directional shadow), one job list.
+BATCH_VOLUMES = ((128, 128, 128, abi.CVR_U8), (192, 256, 160, abi.CVR_U16), (256, 256, 256, abi.CVR_U8),
+                 (384, 384, 384, abi.CVR_U16))
+BATCH_LIGHTS = ((0.35, 0.8, 0.45), (-0.6, 0.5, 0.3), (0.2, 0.4, -0.9), (-0.3, 0.9, -0.2))
+
+
+def sphere_views(n_views: int):
+    """n_views unit directions on a Fibonacci sphere (elevation within +-60 deg)."""
+    out = []
+    golden = math.pi * (3.0 - math.sqrt(5.0))
+    for i in range(n_views):
+        y = 0.85 * (1.0 - 2.0 * (i + 0.5) / n_views)
+        r = math.sqrt(max(0.0, 1.0 - y * y))
+        out.append((r * math.cos(golden * i), y, r * math.sin(golden * i)))
+    return out
+
+
+@dataclass
+class Batch:
+    volumes: list            # (array, spacing)
+    jobs: list               # abi.Job
+    params: list             # kept alive: the params structs the jobs point at
+    width: int
+    height: int
+
+
+def batch_volumes(scale: float = 1.0):
+    """The batch's four volumes (value noise, 4 octaves, shells), optionally scaled down."""
+    vols = []
+    for i, (w, h, d, dt) in enumerate(BATCH_VOLUMES):
+        w, h, d = max(8, int(w * scale)), max(8, int(h * scale)), max(8, int(d * scale))
+        vols.append(synth_value_noise(w, h, d, dt, seed=5000 + i))
+    return vols
+
+
+def prepare_batch_volumes(ctx: Context, vols, pyramid=True):
+    """Uploads each volume into its slot with its SAT and (for the surrogate)
+    its pyramid of base n/2 and 6 levels; leaves slot 0 current."""
+    for slot, vol in enumerate(vols):
+        ctx.select_volume(slot)
+        ctx.set_volume(vol, (1.0, 1.0, 1.0))
+        if slot == 0:
+            ctx.set_transfer_function(BENCH_TF)
+        dtype = abi.CVR_U8 if vol.dtype == np.uint8 else abi.CVR_U16
+        ctx.build_sat(BENCH_TF.ext_per_value(dtype))
+        if pyramid:
+            d, h, w = vol.shape
+            ctx.build_pyramid(base_dims=(max(1, w // 2), max(1, h // 2), max(1, d // 2)), sigma0=1.0,
+                              n_levels=abi.SURROGATE_LEVELS)
+    ctx.select_volume(0)
+
+
+def batch_jobs(vols, n_views=16, lights=BATCH_LIGHTS, image=512, methods=(abi.EXTINCTION, abi.SURROGATE),
+               out_ptrs=None) -> Batch:
+    """Job list: volume x view x light x method (in that nesting order).
+    out_ptrs: device pointers, one per job, in the same order."""
+    jobs, keep = [], []
+    k = 0
+    for slot, vol in enumerate(vols):
+        d, h, w = vol.shape
+        n = max(w, h, d)
+        diag = math.sqrt(w * w + h * h + d * d)
+        for v in sphere_views(n_views):
+            cam = camera(tuple(2.6 * n * np.asarray(v)), fovy=30.0)
+            for ldir in lights:
+                fwd, up, right = light_frame(ldir)
+                lt = light(abi.LIGHT_DIRECTIONAL, position=tuple(3.0 * n * np.asarray(fwd)), forward=fwd, up=up,
+                           right=right)
+                for m in methods:
+                    if m == abi.EXTINCTION:
+                        p = ext_params(default_step((1.0, 1.0, 1.0)), diag, ao_radii=(2, 6, 16), shadow_type=1)
+                    else:
+                        p = gt_params(default_step((1.0, 1.0, 1.0)), diag, occ_distance=32.0, light_step=1.0,
+                                      gap=1.0, shadow_type=2)
+                    keep.append(p)
+                    j = abi.Job()
+                    j.volume, j.method = slot, m
+                    j.params, j.params_size = C.addressof(p), C.sizeof(p)
+                    j.camera, j.light = cam, lt
+                    j.width = j.height = image
+                    j.out_rgba_dev = out_ptrs[k] if out_ptrs is not None else None
+                    jobs.append(j)
+                    k += 1
+    return Batch(list(vols), jobs, keep, image, image)

@@ -195,6 +195,17 @@ cvr_status cvr_set_volume(cvr_ctx* ctx, const void* host_voxels, int w, int h, i
 cvr_status cvr_set_volume_device(cvr_ctx* ctx, const void* dev_voxels, int w, int h, int d,
                                  int dtype, float sx, float sy, float sz);
 
+/* Resident volumes (no reference counterpart: the reference's DataManager
+ * holds one volume).  A context keeps up to CVR_MAX_VOLUMES volumes, each
+ * with its own SAT, pyramid and texture copies; cvr_select_volume makes slot
+ * s current, and the volume calls above, cvr_build_sat, cvr_build_ext_pyramid
+ * and cvr_render act on the current slot.  Slot 0 is current at creation.
+ * The transfer function, cone tables, GT kernel vectors and the network are
+ * shared by all slots.  Batches (cvr_batch_create) name slots per job. */
+#define CVR_MAX_VOLUMES 16
+cvr_status cvr_select_volume(cvr_ctx* ctx, int slot);
+int cvr_current_volume(cvr_ctx* ctx);
+
 /* Transfer function tables (TransferFunction1D::GenerateTexture_1D_RGBt and
  * GenerateTexture_1D_RGBA, transferfunction1d.cpp:58-118): n entries of RGBA.
  * rgbt alpha = extinction; rgba alpha = opacity (may be NULL: derived as 1-exp(-t)). */
@@ -275,6 +286,36 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
 #define CVR_SAMPLING_TEX_FEATURES 1
 cvr_status cvr_set_sampling(cvr_ctx* ctx, int flags);
 int cvr_get_sampling(cvr_ctx* ctx);
+
+/* ---- batched rendering ------------------------------------------------------
+ * No reference counterpart (the reference renders one view per Redraw()).
+ * A batch is a fixed list of frames over the resident volumes, views and
+ * lights, rendered by one persistent launch per method (CVR_METHOD_EXTINCTION
+ * and CVR_METHOD_SURROGATE; other methods are rejected) whose CTAs take
+ * ray tiles of all jobs from one work counter, longest jobs first.  The
+ * launches, with the resets of their counters, are captured in one CUDA
+ * graph at creation; cvr_batch_run replays it.  Every image equals the image
+ * of the same job rendered alone by cvr_render with the context's tuning at
+ * creation.  Jobs keep pointers to their output buffers; the volumes, tables
+ * and network they use must not change while the batch exists (re-create it). */
+typedef struct cvr_job {
+  int volume;           /* volume slot */
+  int method;           /* CVR_METHOD_EXTINCTION or CVR_METHOD_SURROGATE */
+  const void* params;   /* cvr_ext_params or cvr_gt_params, copied at creation */
+  size_t params_size;
+  cvr_camera camera;
+  cvr_light light;
+  int width, height;
+  float* out_rgba_dev;  /* device frame of 16 * width * height bytes */
+} cvr_job;
+
+typedef struct cvr_batch cvr_batch;
+cvr_status cvr_batch_create(cvr_ctx* ctx, const cvr_job* jobs, int n_jobs, cvr_batch** out);
+/* One replay of the batch's graph on the context stream (asynchronous). */
+cvr_status cvr_batch_run(cvr_batch* batch);
+/* Step counts of job j from the last run (synchronises). */
+cvr_status cvr_batch_job_stats(cvr_batch* batch, int job, cvr_frame_stats* out);
+void cvr_batch_destroy(cvr_batch* batch);
 
 /* ---- device timing on the context stream --------------------------------- */
 cvr_status cvr_timer_start(cvr_ctx* ctx);

@@ -1,0 +1,102 @@
+"""Batched rendering: resident volume slots and one graph-captured persistent
+launch per method over many (volume, view, light) jobs.  Every image of a
+batch must equal, bit for bit, the same job rendered alone by cvr_render with
+the same tile configuration, and replays must repeat it."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from cpp_volume_rendering_gb300 import abi, scene
+from tests.devmem import DeviceMemory
+
+pytestmark = pytest.mark.gpu
+
+
+def small_network(ctx):
+    ctx.mlp_init(5)
+    p = ctx.mlp_params()
+    p[abi.MLP_PARAMS - 2:] = 0.5
+    p[64 * 48 + 64 + 64 * 64 + 64:abi.MLP_PARAMS - 2] *= 0.05
+    ctx.mlp_set_params(p)
+
+
+def test_volume_slots_keep_their_tables(ctx):
+    a = scene.synth_blobs(24, 24, 24, abi.CVR_U8, 8, seed=5100)
+    b = scene.synth_value_noise(20, 28, 16, abi.CVR_U16, seed=5101)
+    wl_a = scene.workload("extinction", n=24, image=32)
+    ctx.select_volume(3)
+    assert ctx.lib.cvr_current_volume(ctx.h) == 3
+    ctx.set_volume(a)
+    ctx.set_transfer_function(scene.BENCH_TF)
+    ctx.build_sat(scene.BENCH_TF.ext_per_value(abi.CVR_U8))
+    img_a, _ = ctx.render(abi.EXTINCTION, wl_a.cam, wl_a.light, wl_a.params, 32, 32)
+    ctx.select_volume(5)
+    ctx.set_volume(b)
+    ctx.build_sat(scene.BENCH_TF.ext_per_value(abi.CVR_U16))
+    img_b, _ = ctx.render(abi.EXTINCTION, wl_a.cam, wl_a.light, wl_a.params, 32, 32)
+    ctx.select_volume(3)
+    again, _ = ctx.render(abi.EXTINCTION, wl_a.cam, wl_a.light, wl_a.params, 32, 32)
+    assert np.array_equal(again, img_a) and not np.array_equal(img_a, img_b)
+    assert ctx.lib.cvr_select_volume(ctx.h, abi.MAX_VOLUMES) == abi.CVR_ERR_INVALID_ARG
+    ctx.select_volume(0)
+
+
+@pytest.mark.parametrize("sampling", [abi.SAMPLING_TEX_FEATURES, 0])
+def test_batch_equals_single_renders(ctx, sampling):
+    ctx.set_sampling(sampling)
+    vols = scene.batch_volumes(0.5)  # 64^3 u8, 96x128x80 u16, 128^3 u8, 192^3 u16
+    scene.prepare_batch_volumes(ctx, vols)
+    small_network(ctx)
+    W, H = 48, 40
+    mem = DeviceMemory()
+    try:
+        probe = scene.batch_jobs(vols, n_views=2, lights=scene.BATCH_LIGHTS[:2], image=W)
+        n = len(probe.jobs)
+        outs = [mem.alloc(W * H * 16, fill=0) for _ in range(n)]
+        b = scene.batch_jobs(vols, n_views=2, lights=scene.BATCH_LIGHTS[:2], image=W, out_ptrs=outs)
+        for j in b.jobs:
+            j.height = H
+        arr = (abi.Job * n)(*b.jobs)
+        bh = C.c_void_p()
+        abi.check(ctx.lib.cvr_batch_create(ctx.h, arr, n, C.byref(bh)), ctx.h)
+        try:
+            abi.check(ctx.lib.cvr_batch_run(bh), ctx.h)
+            abi.check(ctx.lib.cvr_sync(ctx.h), ctx.h)
+            first = [mem.download(p, (H, W, 4)) for p in outs]
+            stats = []
+            for k in range(n):
+                st = abi.FrameStats()
+                abi.check(ctx.lib.cvr_batch_job_stats(bh, k, C.byref(st)), ctx.h)
+                stats.append((st.samples, st.shaded_samples))
+            abi.check(ctx.lib.cvr_batch_run(bh), ctx.h)  # graph replay
+            abi.check(ctx.lib.cvr_sync(ctx.h), ctx.h)
+            second = [mem.download(p, (H, W, 4)) for p in outs]
+        finally:
+            ctx.lib.cvr_batch_destroy(bh)
+        mismatches = []
+        for k, j in enumerate(b.jobs):
+            assert np.array_equal(first[k], second[k]), f"job {k}: replay differs"
+            ctx.select_volume(j.volume)
+            params = b.params[k]
+            img, st = ctx.render(j.method, j.camera, j.light, params, W, H)
+            if not np.array_equal(img, first[k]):
+                mismatches.append((k, j.method, float(np.abs(img - first[k]).max())))
+            assert (st.samples, st.shaded_samples) == stats[k], (k, stats[k], st.samples)
+            assert np.isfinite(img).all() and img[..., 3].max() > 0
+        assert not mismatches, mismatches
+    finally:
+        ctx.select_volume(0)
+        ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+        mem.close()
+
+
+def test_batch_rejects_other_methods(ctx):
+    p = abi.PlainParams()
+    p.step_size = 0.5
+    j = abi.Job()
+    j.volume, j.method, j.params, j.params_size = 0, abi.PLAIN, C.addressof(p), C.sizeof(p)
+    j.width = j.height = 8
+    bh = C.c_void_p()
+    arr = (abi.Job * 1)(j)
+    assert ctx.lib.cvr_batch_create(ctx.h, arr, 1, C.byref(bh)) == abi.CVR_ERR_INVALID_ARG
