@@ -319,6 +319,80 @@ def surrogate_section(ctx, lib, args, log=print):
     }
 
 
+def batch_section(ctx, lib, args, log=print):
+    """The batched workload: 4 volumes of uneven size x 16 views x 4 directional
+    lights at 512^2, extinction and surrogate shading (512 images), one CUDA
+    graph of two persistent launches; against the same jobs as 512 cvr_render
+    calls.  Uses the network on ctx (trained by the surrogate section when it ran)."""
+    import ctypes as C
+    from cpp_volume_rendering_gb300 import abi, scene
+    t0 = time.perf_counter()
+    vols = scene.batch_volumes(1.0)
+    scene.prepare_batch_volumes(ctx, vols)
+    t_prep = time.perf_counter() - t0
+    if not ctx.lib.cvr_mlp_training_size(ctx.h):  # no trained network on ctx: timing only
+        ctx.mlp_init(7)
+    W = 512
+    probe = scene.batch_jobs(vols, image=W)
+    n = len(probe.jobs)
+    frames = C.POINTER(C.c_float)()
+    fb_w = 32768  # one library-owned buffer holding all n frames
+    abi.check(lib.cvr_get_frame_buffer(ctx.h, fb_w, (n * W * W + fb_w - 1) // fb_w, C.byref(frames)), ctx.h)
+    base = C.cast(frames, C.c_void_p).value
+    outs = [C.c_void_p(base + k * W * W * 16) for k in range(n)]
+    b = scene.batch_jobs(vols, image=W, out_ptrs=outs)
+    # tuner: tile shape x register variant on the largest volume's first extinction job
+    big = max(range(n), key=lambda k: (b.jobs[k].method == abi.EXTINCTION, vols[b.jobs[k].volume].size))
+    jb = b.jobs[big]
+    ctx.select_volume(jb.volume)
+    tw, th, tv, tms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+    abi.check(lib.cvr_autotune(ctx.h, jb.method, C.byref(jb.camera), C.byref(jb.light), C.c_void_p(jb.params),
+                               jb.params_size, W, W, 2, C.byref(tw), C.byref(th), C.byref(tv), C.byref(tms)), ctx.h)
+    ctx.select_volume(0)
+    arr = (abi.Job * n)(*b.jobs)
+    bh = C.c_void_p()
+    abi.check(lib.cvr_batch_create(ctx.h, arr, n, C.byref(bh)), ctx.h)
+    try:
+        for _ in range(2):
+            abi.check(lib.cvr_batch_run(bh), ctx.h)
+        abi.check(lib.cvr_sync(ctx.h), ctx.h)
+        times = []
+        ms = C.c_float()
+        for _ in range(3):
+            abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+            abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+            abi.check(lib.cvr_batch_run(bh), ctx.h)
+            abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+            times.append(ms.value)
+        samples = {abi.EXTINCTION: 0, abi.SURROGATE: 0}
+        for k in range(n):
+            st = abi.FrameStats()
+            abi.check(lib.cvr_batch_job_stats(bh, k, C.byref(st)), ctx.h)
+            samples[b.jobs[k].method] += st.samples
+    finally:
+        lib.cvr_batch_destroy(bh)
+    # the same jobs as single cvr_render calls (one pass, device-timed as a whole)
+    abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+    abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+    for k, j in enumerate(b.jobs):
+        abi.check(lib.cvr_select_volume(ctx.h, j.volume), ctx.h)
+        abi.check(lib.cvr_render(ctx.h, j.method, C.byref(j.camera), C.byref(j.light), C.c_void_p(j.params),
+                                 j.params_size, outs[k], W, W, None, None), ctx.h)
+    abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+    seq_ms = ms.value
+    abi.check(lib.cvr_select_volume(ctx.h, 0), ctx.h)
+    med = statistics.median(times)
+    tot = samples[abi.EXTINCTION] + samples[abi.SURROGATE]
+    return {"workload": "4 volumes (128^3 u8, 192x256x160 u16, 256^3 u8, 384^3 u16 value noise) x 16 views x "
+                        "4 directional lights x {extinction, surrogate} = 512 images of 512^2",
+            "jobs": n, "batch_ms": med, "images_per_s": n / (med / 1000.0),
+            "msamples_s": tot / (med / 1000.0) / 1e6, "samples": {"extinction": samples[abi.EXTINCTION],
+                                                                  "surrogate": samples[abi.SURROGATE]},
+            "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
+            "tuning": {"tile": [tw.value, th.value], "variant": tv.value}, "prepare_s": t_prep,
+            "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -405,9 +479,12 @@ def run_ours(args):
            "includes": "cvr_set_volume from pinned host memory + the method's table build (SAT or pyramid) + "
                        "cvr_render_host readback"}
     renderers = {}
+    batch = None
     if not args.quick:
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)
+        if not args.no_batch:
+            batch = batch_section(ctx, lib, args)
         for name in ("plain", "cone", "ground_truth"):
             if name == args.workload:
                 continue
@@ -440,7 +517,7 @@ def run_ours(args):
         "fps": 1000.0 / ms_per_step,
         "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-        "clocks": clocks, "renderers": renderers, "surrogate": surrogate}))
+        "clocks": clocks, "renderers": renderers, "surrogate": surrogate, "batch": batch}))
 
 
 def main():
@@ -454,6 +531,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the surrogate")
     ap.add_argument("--surrogate-points", type=int, default=4_000_000)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--size", type=int, default=None, help="volume side override (profiling / small cases)")
     ap.add_argument("--image", type=int, default=None, help="image side override (profiling / small cases)")
