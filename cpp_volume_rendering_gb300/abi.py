@@ -163,6 +163,8 @@ SIGNATURES = {
     "cvr_batch_run": (_I, [_P]),
     "cvr_batch_job_stats": (_I, [_P, _I, C.POINTER(FrameStats)]),
     "cvr_batch_destroy": (None, [_P]),
+    "cvr_set_brick_size": (_I, [_P, _I]),
+    "cvr_get_brick_size": (_I, [_P]),
     "cvr_set_sampling": (_I, [_P, _I]),
     "cvr_get_sampling": (_I, [_P]),
     "cvr_mlp_save": (_I, [_P, C.c_char_p]),

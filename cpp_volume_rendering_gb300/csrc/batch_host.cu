@@ -18,6 +18,7 @@ struct cvr_batch {
   unsigned ext_blocks = 0;
   int ext_max_table = 0;
   int ext_variant = 0;
+  int ext_threads = 128;
   float4* d_tables = nullptr;
   SurJob* d_sur = nullptr;
   int n_sur = 0;
@@ -105,7 +106,6 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
     if (st != CVR_OK) break;
     f.stats = b->d_stats + 3 * (size_t)i;
     if (j.method == CVR_METHOD_EXTINCTION) {
-      if (f.tile_w * f.tile_h != 128) { st = fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: tile must be 128 pixels"); break; }
       BatchExtJob J{};
       const ShadowBoxTable* table = nullptr;
       st = ext_args(c, static_cast<const cvr_ext_params*>(j.params), &j.light, f, &J.e, &table);
@@ -141,6 +141,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   if (st != CVR_OK) return st;
   if (!sur.empty() && (!c->mlp || !c->mlp->err)) return fail(c, CVR_ERR_NOT_READY, "cvr_batch_create: no network");
   b->ext_variant = c->variant;
+  b->ext_threads = (c->tile_w / 8) * (c->tile_h / 4) * 32;
   b->n_ext = (int)ext.size();
   b->n_sur = (int)sur.size();
   if (b->n_ext) {
@@ -172,7 +173,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stats, 0, sizeof(unsigned long long) * 3 * n_jobs, c->stream);
   if (e == cudaSuccess && b->n_ext)
     e = launch_batch_extinction(b->d_ext, b->n_ext, b->ext_blocks, b->d_counters, c->tf_n, b->ext_max_table,
-                                b->ext_variant, c->stream);
+                                b->ext_threads, b->ext_variant, c->stream);
   if (e == cudaSuccess && b->n_sur)
     e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->d_counters + 1, c->mlp->err,
                                c->stream);

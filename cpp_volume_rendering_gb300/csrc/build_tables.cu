@@ -187,6 +187,42 @@ cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, i
 }
 
 // ----------------------------------------------------------- L2 flush
+// ---------------------------------------------------------------- bricks
+// Copies a plain x-fastest volume into bricks of 2^bs voxels per edge
+// (brick-local x fastest, bricks x fastest); voxels past the volume's edge
+// inside the last bricks are zero and never read.
+template <class T>
+__global__ void k_brick(const T* __restrict__ src, T* __restrict__ dst, int nx, int ny, int nz, int bs,
+                        long long total) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= total) return;
+  const int m = (1 << bs) - 1;
+  const int local = (int)(e & ((1ll << (3 * bs)) - 1));
+  const long long brick = e >> (3 * bs);
+  const int bx = (nx + m) >> bs, by = (ny + m) >> bs;
+  const int x = (int)(brick % bx) * (m + 1) + (local & m);
+  const int y = (int)((brick / bx) % by) * (m + 1) + ((local >> bs) & m);
+  const int z = (int)(brick / ((long long)bx * by)) * (m + 1) + (local >> (2 * bs));
+  dst[e] = (x < nx && y < ny && z < nz) ? src[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)] : T(0);
+}
+
+long long brick_elements(int nx, int ny, int nz, int bs) {
+  const int m = (1 << bs) - 1;
+  return (long long)((nx + m) >> bs) * ((ny + m) >> bs) * ((nz + m) >> bs) << (3 * bs);
+}
+
+cudaError_t launch_brick_volume(const void* src, void* dst, int dtype, int nx, int ny, int nz, int bs,
+                                cudaStream_t st) {
+  const long long total = brick_elements(nx, ny, nz, bs);
+  const unsigned blocks = (unsigned)((total + 255) / 256);
+  if (dtype == 1)
+    k_brick<<<blocks, 256, 0, st>>>(static_cast<const uint8_t*>(src), static_cast<uint8_t*>(dst), nx, ny, nz, bs, total);
+  else
+    k_brick<<<blocks, 256, 0, st>>>(static_cast<const uint16_t*>(src), static_cast<uint16_t*>(dst), nx, ny, nz, bs,
+                                    total);
+  return cudaGetLastError();
+}
+
 __global__ void k_fill(uint4* p, size_t n, unsigned int v) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   size_t stride = (size_t)gridDim.x * blockDim.x;

@@ -15,5 +15,10 @@ cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, i
 
 // Grid-stride fill of a device buffer (used to flush L2 between timed frames).
 cudaError_t launch_fill(void* p, size_t bytes, unsigned int v, cudaStream_t st);
+// Bricked copy of a plain volume (bricks of 2^bs voxels per edge); the copy
+// holds brick_elements(...) elements.
+long long brick_elements(int nx, int ny, int nz, int bs);
+cudaError_t launch_brick_volume(const void* src, void* dst, int dtype, int nx, int ny, int nz, int bs,
+                                cudaStream_t st);
 
 }  // namespace cvr

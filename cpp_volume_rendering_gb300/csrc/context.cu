@@ -105,6 +105,27 @@ bool build_shadow_table(const cvr_ext_params* p, const float fwd[3], float3 spac
 namespace cvr {
 namespace ctxutil {
 
+cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
+  VolumeView v = volume_view(c);
+  if (c->brick_bs > 0) {
+    if (c->vbrick_bs != c->brick_bs) {
+      const long long n = brick_elements(c->nx, c->ny, c->nz, c->brick_bs);
+      CK(c, ensure(c->d_vbrick, c->vbrick_cap, (size_t)n * (c->dtype == CVR_U8 ? 1 : 2)));
+      CK(c, launch_brick_volume(c->d_vol, c->d_vbrick, c->dtype, c->nx, c->ny, c->nz, c->brick_bs, c->stream));
+      c->vbrick_bs = c->brick_bs;
+    }
+    const int B = 1 << c->brick_bs;
+    const long long bx = (c->nx + B - 1) / B, by = (c->ny + B - 1) / B;
+    v.voxels = c->d_vbrick;
+    v.bs = c->brick_bs;
+    v.stride[0] = (long long)B * B * B;
+    v.stride[1] = bx * v.stride[0];
+    v.stride[2] = by * v.stride[1];
+  }
+  *out = v;
+  return CVR_OK;
+}
+
 cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,
                       FrameArgs* fo) {
   if (!c || !cam || !params || !out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
@@ -114,7 +135,8 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
   if (!finite3(cam->eye) || !finite3(cam->center) || !finite3(cam->up))
     return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: non-finite camera");
   FrameArgs f;
-  f.vol = volume_view(c);
+  cvr_status vs = render_volume_view(c, &f.vol);
+  if (vs != CVR_OK) return vs;
   f.cam = camera_view(cam, w, h);
   f.tf = c->d_rgbt;
   f.tf_n = c->tf_n;
@@ -213,7 +235,7 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush};
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -250,6 +272,7 @@ static cvr_status set_volume_common(cvr_ctx* c, const void* src, bool src_device
   c->pyr_ready = false;
   c->tex.vol_valid = false;
   c->tex.pyr_valid = false;
+  c->vbrick_bs = -1;
   return CVR_OK;
 }
 
@@ -565,11 +588,17 @@ cvr_status cvr_render_host(cvr_ctx* c, int method, const cvr_camera* cam, const 
   return CVR_OK;
 }
 
+static bool tile_ok(int tile_w, int tile_h) {
+  if (tile_w <= 0 || tile_h <= 0 || tile_w % 8 || tile_h % 4) return false;
+  const int warps = (tile_w / 8) * (tile_h / 4);
+  return warps == 2 || warps == 4 || warps == 8;
+}
+
 cvr_status cvr_set_tuning(cvr_ctx* c, int tile_w, int tile_h, int variant) {
   if (!c) return CVR_ERR_INVALID_ARG;
-  if (tile_w <= 0 || tile_h <= 0 || tile_w % 8 || tile_h % 4 || (tile_w / 8) * (tile_h / 4) != 4 || variant < 0 ||
-      variant > 2)
-    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_tuning: tile must be 128 threads of 8x4-pixel warps, variant 0..2");
+  if (!tile_ok(tile_w, tile_h) || variant < 0 || variant > 2)
+    return fail(c, CVR_ERR_INVALID_ARG,
+                "cvr_set_tuning: tile must be 2, 4 or 8 warps of 8x4 pixels (8x8 ... 32x8), variant 0..2");
   c->tile_w = tile_w;
   c->tile_h = tile_h;
   c->variant = variant;
@@ -584,44 +613,75 @@ cvr_status cvr_get_tuning(cvr_ctx* c, int* tile_w, int* tile_h, int* variant) {
   return CVR_OK;
 }
 
+cvr_status cvr_set_brick_size(cvr_ctx* c, int edge) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  int bs = edge == 0 ? 0 : (edge == 4 ? 2 : (edge == 8 ? 3 : (edge == 16 ? 4 : (edge == 32 ? 5 : -1))));
+  if (bs < 0) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_brick_size: edge must be 0, 4, 8, 16 or 32");
+  c->brick_bs = bs;
+  return CVR_OK;
+}
+
+int cvr_get_brick_size(cvr_ctx* c) { return (c && c->brick_bs > 0) ? (1 << c->brick_bs) : 0; }
+
+// Mean device time of reps frames of the current tuning (one untimed frame
+// first, L2 flushed before each timed one).
+static cvr_status time_config(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
+                              const void* params, size_t params_size, float* frame, int w, int h, int reps,
+                              float* mean_ms) {
+  cvr_status s = render_impl(c, method, cam, light, params, params_size, frame, w, h, nullptr, nullptr);
+  float total = 0.0f;
+  for (int r = 0; r < reps && s == CVR_OK; ++r) {
+    if ((s = cvr_flush_l2(c)) != CVR_OK) break;
+    if ((s = cvr_timer_start(c)) != CVR_OK) break;
+    if ((s = render_impl(c, method, cam, light, params, params_size, frame, w, h, nullptr, nullptr)) != CVR_OK) break;
+    float ms = 0.0f;
+    if ((s = cvr_timer_stop(c, &ms)) != CVR_OK) break;
+    total += ms;
+  }
+  *mean_ms = total / (float)reps;
+  return s;
+}
+
 cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light, const void* params,
                         size_t params_size, int w, int h, int reps, int* btw, int* bth, int* bv, float* bms) {
   if (!c || reps <= 0 || reps > 100) return fail(c, CVR_ERR_INVALID_ARG, "cvr_autotune: bad arguments");
-  static const int tiles[3][2] = {{16, 8}, {32, 4}, {8, 16}};
+  // ray tiles from 8x8 to 32x8 (2, 4 and 8 warps) x register variants, then
+  // the volume's brick size at the best of those (plain layout, 8^3, 16^3, 32^3)
+  static const int tiles[6][2] = {{8, 8}, {16, 8}, {32, 4}, {8, 16}, {32, 8}, {16, 16}};
+  static const int bricks[4] = {0, 3, 4, 5};
   float* frame = nullptr;
   cvr_status s = cvr_get_frame_buffer(c, w, h, &frame);
   if (s != CVR_OK) return s;
-  int keep_w = c->tile_w, keep_h = c->tile_h, keep_v = c->variant;
+  const int keep_w = c->tile_w, keep_h = c->tile_h, keep_v = c->variant, keep_b = c->brick_bs;
   float best = 1e30f;
-  int bw = keep_w, bh = keep_h, bvar = keep_v;
-  for (int t = 0; t < 3; ++t) {
-    for (int v = 0; v < 3; ++v) {
+  int bw = keep_w, bh = keep_h, bvar = keep_v, bb = 0;
+  c->brick_bs = 0;
+  for (int t = 0; t < 6 && s == CVR_OK; ++t) {
+    for (int v = 0; v < 3 && s == CVR_OK; ++v) {
       c->tile_w = tiles[t][0]; c->tile_h = tiles[t][1]; c->variant = v;
-      // one untimed frame (first launch of the variant), then the timed ones
-      s = render_impl(c, method, cam, light, params, params_size, frame, w, h, nullptr, nullptr);
-      if (s != CVR_OK) break;
-      float total = 0.0f;
-      for (int r = 0; r < reps && s == CVR_OK; ++r) {
-        if ((s = cvr_flush_l2(c)) != CVR_OK) break;
-        if ((s = cvr_timer_start(c)) != CVR_OK) break;
-        if ((s = render_impl(c, method, cam, light, params, params_size, frame, w, h, nullptr, nullptr)) != CVR_OK) break;
-        float ms = 0.0f;
-        if ((s = cvr_timer_stop(c, &ms)) != CVR_OK) break;
-        total += ms;
-      }
-      if (s != CVR_OK) break;
-      if (total / reps < best) {
-        best = total / reps;
+      float ms = 0.0f;
+      s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
+      if (s == CVR_OK && ms < best) {
+        best = ms;
         bw = tiles[t][0]; bh = tiles[t][1]; bvar = v;
       }
     }
-    if (s != CVR_OK) break;
-  }
-  if (s != CVR_OK) {
-    c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v;
-    return s;
   }
   c->tile_w = bw; c->tile_h = bh; c->variant = bvar;
+  for (int k = 1; k < 4 && s == CVR_OK; ++k) {
+    c->brick_bs = bricks[k];
+    float ms = 0.0f;
+    s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
+    if (s == CVR_OK && ms < best) {
+      best = ms;
+      bb = bricks[k];
+    }
+  }
+  if (s != CVR_OK) {
+    c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b;
+    return s;
+  }
+  c->brick_bs = bb;
   if (btw) *btw = bw;
   if (bth) *bth = bh;
   if (bv) *bv = bvar;

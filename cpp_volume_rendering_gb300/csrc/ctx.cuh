@@ -103,8 +103,11 @@ struct VolSlot {
   PyramidView pyr{};
   bool pyr_ready = false;
   TexState tex;
+  void* d_vbrick = nullptr;
+  size_t vbrick_cap = 0;
+  int vbrick_bs = -1;
   ~VolSlot() {
-    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr};
+    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }
@@ -181,6 +184,11 @@ struct cvr_ctx {
   int sampling = CVR_SAMPLING_TEX_FEATURES;  // cvr_set_sampling flags
   VolSlot slots[CVR_MAX_VOLUMES];            // the other resident volumes
   int cur_slot = 0;
+  // bricked copy of the current volume for the marchers (cvr_set_brick_size)
+  int brick_bs = 0;                          // tuning: 0 plain layout, else log2 of the brick edge
+  void* d_vbrick = nullptr;
+  size_t vbrick_cap = 0;
+  int vbrick_bs = -1;                        // layout of d_vbrick's contents (-1: stale)
 };
 
 // Exchanges the current-volume fields of c with slot s.
@@ -201,6 +209,9 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->pyr, s.pyr);
   std::swap(c->pyr_ready, s.pyr_ready);
   swap_tex(c->tex, s.tex);
+  std::swap(c->d_vbrick, s.d_vbrick);
+  std::swap(c->vbrick_cap, s.vbrick_cap);
+  std::swap(c->vbrick_bs, s.vbrick_bs);
 }
 
 namespace cvr {
@@ -246,6 +257,10 @@ inline VolumeView volume_view(const cvr_ctx* c) {
   v.inv_spacing = f3(1.0f / c->sx, 1.0f / c->sy, 1.0f / c->sz);
   v.grid = f3(c->nx * c->sx, c->ny * c->sy, c->nz * c->sz);
   v.norm = c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  v.bs = 0;
+  v.stride[0] = 1;
+  v.stride[1] = c->nx;
+  v.stride[2] = (long long)c->nx * c->ny;
   return v;
 }
 
@@ -275,6 +290,9 @@ cvr_status mlp_check_err(cvr_ctx* c);
 // Texture objects of the volume / pyramid levels, (re)made when stale.
 cvr_status ensure_volume_texture(cvr_ctx* c);
 cvr_status ensure_pyramid_textures(cvr_ctx* c);
+// The volume as the marchers read it: the plain layout, or the bricked copy
+// of the context's brick size (made on first use after the volume changed).
+cvr_status render_volume_view(cvr_ctx* c, VolumeView* v);
 // Frame arguments of a render of the current volume (validated; f.step from
 // the params struct's leading step_size, f.counts null, f.stats the context's).
 cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,

@@ -45,6 +45,12 @@ struct VolumeView {
   float3 inv_spacing;
   float3 grid;          // VolumeGridSize = dims * spacing
   float norm;           // 1/255 or 1/65535
+  // Storage: bricks of B = 2^bs voxels per edge, each brick x-fastest inside,
+  // bricks x-fastest; bs = 0 is the plain x-fastest layout.  stride[a] is the
+  // element distance between neighbouring bricks along axis a (plain layout:
+  // 1, nx, nx*ny).
+  int bs;
+  long long stride[3];
 };
 
 // Per-frame camera frame (glm::lookAt rows s, u, f) and projection terms.
@@ -85,10 +91,17 @@ __device__ __forceinline__ bool ray_aabb(float3 origin, float3 dir, float3 grid,
 }
 
 // ---------------------------------------------------------------- sampling
-__device__ __forceinline__ float voxel(const VolumeView& v, int x, int y, int z) {
-  size_t i = (size_t)x + (size_t)v.nx * ((size_t)y + (size_t)v.ny * (size_t)z);
+// Element offset of coordinate i along axis a (offsets of the three axes add).
+__device__ __forceinline__ long long voxel_term(const VolumeView& v, int a, int i) {
+  const int m = (1 << v.bs) - 1;
+  return (long long)(i >> v.bs) * v.stride[a] + (long long)((i & m) << (a * v.bs));
+}
+__device__ __forceinline__ float voxel_at(const VolumeView& v, long long i) {
   if (v.dtype == 1) return float(__ldg(static_cast<const uint8_t*>(v.voxels) + i));
   return float(__ldg(static_cast<const uint16_t*>(v.voxels) + i));
+}
+__device__ __forceinline__ float voxel(const VolumeView& v, int x, int y, int z) {
+  return voxel_at(v, voxel_term(v, 0, x) + voxel_term(v, 1, y) + voxel_term(v, 2, z));
 }
 
 // One axis of a GL_LINEAR clamp-to-edge lookup at texel coordinate u.
@@ -112,10 +125,13 @@ __device__ __forceinline__ float sample_volume(const VolumeView& v, float3 tex_p
   Tap tx = axis_tap(fmaf(tex_pos.x, v.inv_spacing.x, -0.5f), v.nx);
   Tap ty = axis_tap(fmaf(tex_pos.y, v.inv_spacing.y, -0.5f), v.ny);
   Tap tz = axis_tap(fmaf(tex_pos.z, v.inv_spacing.z, -0.5f), v.nz);
-  float c000 = voxel(v, tx.i0, ty.i0, tz.i0), c100 = voxel(v, tx.i1, ty.i0, tz.i0);
-  float c010 = voxel(v, tx.i0, ty.i1, tz.i0), c110 = voxel(v, tx.i1, ty.i1, tz.i0);
-  float c001 = voxel(v, tx.i0, ty.i0, tz.i1), c101 = voxel(v, tx.i1, ty.i0, tz.i1);
-  float c011 = voxel(v, tx.i0, ty.i1, tz.i1), c111 = voxel(v, tx.i1, ty.i1, tz.i1);
+  const long long x0 = voxel_term(v, 0, tx.i0), x1 = voxel_term(v, 0, tx.i1);
+  const long long y0 = voxel_term(v, 1, ty.i0), y1 = voxel_term(v, 1, ty.i1);
+  const long long z0 = voxel_term(v, 2, tz.i0), z1 = voxel_term(v, 2, tz.i1);
+  float c000 = voxel_at(v, x0 + y0 + z0), c100 = voxel_at(v, x1 + y0 + z0);
+  float c010 = voxel_at(v, x0 + y1 + z0), c110 = voxel_at(v, x1 + y1 + z0);
+  float c001 = voxel_at(v, x0 + y0 + z1), c101 = voxel_at(v, x1 + y0 + z1);
+  float c011 = voxel_at(v, x0 + y1 + z1), c111 = voxel_at(v, x1 + y1 + z1);
   float c00 = fmaf(tx.t, c100 - c000, c000), c10 = fmaf(tx.t, c110 - c010, c010);
   float c01 = fmaf(tx.t, c101 - c001, c001), c11 = fmaf(tx.t, c111 - c011, c011);
   float c0 = fmaf(ty.t, c10 - c00, c00), c1 = fmaf(ty.t, c11 - c01, c01);

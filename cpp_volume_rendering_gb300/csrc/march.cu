@@ -8,17 +8,20 @@
 
 namespace cvr {
 
-__global__ void __launch_bounds__(128) k_march_plain(FrameArgs f) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_march_plain(FrameArgs f) {
   extern __shared__ float4 sm_tf[];
   const float4* tf = stage_tf(f, sm_tf);
   __syncthreads();
   march_pixel(f, tf, PlainShade{});
 }
 
-// MINB: minimum resident CTAs per SM requested from the register allocator
-// (1: no cap, 4: <= 128 registers, 6: <= 80 registers); chosen by the tuner.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) k_march_extinction(FrameArgs f, ExtArgs e) {
+// NT: threads per CTA (64, 128 or 256: tiles of 2, 4 or 8 warps of 8x4
+// pixels).  MINB: minimum resident CTAs per SM requested from the register
+// allocator, from the tuner's register variant (0: no cap, 1: <= 128, 2: <= 80
+// registers per thread).
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_march_extinction(FrameArgs f, ExtArgs e) {
   extern __shared__ float4 sm_tf[];
   const float4* tf = stage_tf(f, sm_tf);
   __syncthreads();
@@ -28,8 +31,8 @@ __global__ void __launch_bounds__(128, MINB) k_march_extinction(FrameArgs f, Ext
 
 // Directional light: the shadow boxes come from the per-frame table, staged
 // in shared memory after the transfer function.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) k_march_extinction_dir(FrameArgs f, ExtArgs e,
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_march_extinction_dir(FrameArgs f, ExtArgs e,
                                                                     const __grid_constant__ ShadowBoxTable t) {
   extern __shared__ float4 sm_tf[];
   const float4* tf = stage_tf(f, sm_tf);
@@ -46,7 +49,8 @@ __global__ void __launch_bounds__(128, MINB) k_march_extinction_dir(FrameArgs f,
   march_pixel(f, tf, sh);
 }
 
-__global__ void __launch_bounds__(128) k_march_dos(DosArgs d, FrameArgs f) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_march_dos(DosArgs d, FrameArgs f) {
   extern __shared__ float4 sm[];
   float4* tf = sm;
   float4* occ = sm + f.tf_n;
@@ -59,7 +63,8 @@ __global__ void __launch_bounds__(128) k_march_dos(DosArgs d, FrameArgs f) {
   march_pixel(f, tf, sh);
 }
 
-__global__ void __launch_bounds__(128) k_march_gt(GtArgs g, FrameArgs f) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_march_gt(GtArgs g, FrameArgs f) {
   extern __shared__ float4 sm[];
   float4* tf = sm;
   float3* ov = reinterpret_cast<float3*>(sm + f.tf_n);
@@ -79,15 +84,19 @@ static int threads_of(const FrameArgs& f) { return (f.tile_w / 8) * (f.tile_h / 
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
   size_t sm = sizeof(float4) * f.tf_n;
-  k_march_plain<<<grid_of(f), threads_of(f), sm, st>>>(f);
+  switch (threads_of(f)) {
+    case 64: k_march_plain<64><<<grid_of(f), 64, sm, st>>>(f); break;
+    case 256: k_march_plain<256><<<grid_of(f), 256, sm, st>>>(f); break;
+    default: k_march_plain<128><<<grid_of(f), 128, sm, st>>>(f); break;
+  }
   return cudaGetLastError();
 }
 
 // Batched extinction frames: persistent CTAs take tiles of all jobs from one
 // counter; the job descriptor, transfer function and shadow table are staged
 // in shared memory whenever a CTA moves to another job.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) k_batch_extinction(const BatchExtJob* __restrict__ jobs, int n_jobs,
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob* __restrict__ jobs, int n_jobs,
                                                                 unsigned total, unsigned* counter) {
   __shared__ BatchExtJob J;
   __shared__ unsigned s_blk;
@@ -139,61 +148,109 @@ __global__ void __launch_bounds__(128, MINB) k_batch_extinction(const BatchExtJo
   }
 }
 
-cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
-                                    int tf_n, int max_table, int variant, cudaStream_t st) {
-  const size_t smem = sizeof(float4) * (tf_n + 2 * max_table);
-  auto kern = variant == 1 ? k_batch_extinction<4> : (variant == 2 ? k_batch_extinction<6> : k_batch_extinction<1>);
+template <int NT, int MINB>
+static cudaError_t launch_batch_t(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
+                                  size_t smem, cudaStream_t st) {
+  auto kern = k_batch_extinction<NT, MINB>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  if ((e = resident_ctas(kern, 128, smem, &per_sm)) != cudaSuccess) return e;
+  if ((e = resident_ctas(kern, NT, smem, &per_sm)) != cudaSuccess) return e;
   unsigned ctas = (unsigned)sms * (unsigned)per_sm;
   if (ctas > total_blocks) ctas = total_blocks;
   if (ctas == 0) return cudaSuccess;
-  kern<<<ctas, 128, smem, st>>>(jobs, n_jobs, total_blocks, counter);
+  kern<<<ctas, NT, smem, st>>>(jobs, n_jobs, total_blocks, counter);
   return cudaGetLastError();
 }
 
-template <int MINB>
+// Register variants as minimum resident CTAs: caps of 128 and 80 registers.
+template <int NT>
+constexpr int minb_of(int variant) {
+  return variant == 1 ? 65536 / (NT * 128) : (variant == 2 ? 65536 / (NT * 80) : 1);
+}
+
+cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
+                                    int tf_n, int max_table, int tile_threads, int variant, cudaStream_t st) {
+  const size_t smem = sizeof(float4) * (tf_n + 2 * max_table);
+#define CVR_BATCH(NT)                                                                                          \
+  switch (variant) {                                                                                          \
+    case 1: return launch_batch_t<NT, minb_of<NT>(1)>(jobs, n_jobs, total_blocks, counter, smem, st);        \
+    case 2: return launch_batch_t<NT, minb_of<NT>(2)>(jobs, n_jobs, total_blocks, counter, smem, st);        \
+    default: return launch_batch_t<NT, 1>(jobs, n_jobs, total_blocks, counter, smem, st);                    \
+  }
+  if (tile_threads == 64) { CVR_BATCH(64) }
+  if (tile_threads == 256) { CVR_BATCH(256) }
+  CVR_BATCH(128)
+#undef CVR_BATCH
+}
+
+template <int NT, int MINB>
 static void launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
   if (table) {
     size_t sm = sizeof(float4) * (f.tf_n + 2 * table->n);
-    k_march_extinction_dir<MINB><<<grid_of(f), threads_of(f), sm, st>>>(f, e, *table);
+    k_march_extinction_dir<NT, MINB><<<grid_of(f), NT, sm, st>>>(f, e, *table);
   } else {
     size_t sm = sizeof(float4) * f.tf_n;
-    k_march_extinction<MINB><<<grid_of(f), threads_of(f), sm, st>>>(f, e);
+    k_march_extinction<NT, MINB><<<grid_of(f), NT, sm, st>>>(f, e);
+  }
+}
+
+template <int NT>
+static void launch_extinction_nt(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+  switch (f.variant) {
+    case 1: launch_extinction_t<NT, minb_of<NT>(1)>(f, e, table, st); break;
+    case 2: launch_extinction_t<NT, minb_of<NT>(2)>(f, e, table, st); break;
+    default: launch_extinction_t<NT, 1>(f, e, table, st); break;
   }
 }
 
 cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
-  switch (f.variant) {
-    case 1: launch_extinction_t<4>(f, e, table, st); break;
-    case 2: launch_extinction_t<6>(f, e, table, st); break;
-    default: launch_extinction_t<1>(f, e, table, st); break;
+  switch (threads_of(f)) {
+    case 64: launch_extinction_nt<64>(f, e, table, st); break;
+    case 256: launch_extinction_nt<256>(f, e, table, st); break;
+    default: launch_extinction_nt<128>(f, e, table, st); break;
   }
+  return cudaGetLastError();
+}
+
+template <int NT>
+static cudaError_t launch_dos_t(const FrameArgs& f, const DosArgs& d, size_t sm, cudaStream_t st) {
+  if (sm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_march_dos<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+  }
+  k_march_dos<NT><<<grid_of(f), NT, sm, st>>>(d, f);
   return cudaGetLastError();
 }
 
 cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, cudaStream_t st) {
   size_t sm = sizeof(float4) * (f.tf_n + d.occ.n_sections + d.sdw.n_sections);
+  switch (threads_of(f)) {
+    case 64: return launch_dos_t<64>(f, d, sm, st);
+    case 256: return launch_dos_t<256>(f, d, sm, st);
+    default: return launch_dos_t<128>(f, d, sm, st);
+  }
+}
+
+template <int NT>
+static cudaError_t launch_gt_t(const FrameArgs& f, const GtArgs& g, size_t sm, cudaStream_t st) {
   if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_march_dos, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_march_gt<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_march_dos<<<grid_of(f), threads_of(f), sm, st>>>(d, f);
+  k_march_gt<NT><<<grid_of(f), NT, sm, st>>>(g, f);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st) {
   size_t sm = sizeof(float4) * f.tf_n + sizeof(float3) * (g.n_occ + g.n_sdw);
-  if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_march_gt, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
+  switch (threads_of(f)) {
+    case 64: return launch_gt_t<64>(f, g, sm, st);
+    case 256: return launch_gt_t<256>(f, g, sm, st);
+    default: return launch_gt_t<128>(f, g, sm, st);
   }
-  k_march_gt<<<grid_of(f), threads_of(f), sm, st>>>(g, f);
-  return cudaGetLastError();
 }
 
 }  // namespace cvr

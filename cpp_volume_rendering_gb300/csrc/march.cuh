@@ -17,7 +17,7 @@ struct FrameArgs {
   int tf_n;
   float step;            // StepSize
   int W, H;
-  int tile_w, tile_h;    // pixels per CTA: 128 threads as (tile_w/8) x (tile_h/4) warps
+  int tile_w, tile_h;    // pixels per CTA: (tile_w/8) x (tile_h/4) warps of 8x4 pixels (2, 4 or 8 warps)
   int variant;           // register / occupancy variant of the kernel (0, 1, 2)
   float4* out;
   uint32_t* counts;                // per-pixel step count, nullable
@@ -118,7 +118,7 @@ struct BatchExtJob {
 // each CTA takes tiles from *counter (zeroed before the launch).  variant as
 // in FrameArgs; max_table = the largest shadow table of the jobs.
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
-                                    int tf_n, int max_table, int variant, cudaStream_t st);
+                                    int tf_n, int max_table, int tile_threads, int variant, cudaStream_t st);
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
 // table == nullptr: per-sample cone geometry (point lights, or too many boxes).

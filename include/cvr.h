@@ -261,16 +261,25 @@ cvr_status cvr_get_frame_buffer(cvr_ctx* ctx, int w, int h, float** dev_out);
 cvr_status cvr_download_frame(cvr_ctx* ctx, const float* dev_frame, int w, int h, float* host_out);
 
 /* Launch configuration of the marchers (no reference counterpart: the
- * reference always dispatches 8x8 work groups, computeshader.h:37).  A CTA
- * is 128 threads whose warps each cover an 8x4 pixel block, arranged as
- * (tile_w/8) x (tile_h/4) warps: tiles 16x8, 32x4 or 8x16.  variant selects the
- * register budget of the kernel (0: compiler's choice, 1: <= 128, 2: <= 80
- * registers per thread).  Results do not depend on the choice. */
+ * reference always dispatches 8x8 work groups, computeshader.h:37).  A CTA is
+ * 2, 4 or 8 warps, each covering an 8x4 pixel block, arranged as
+ * (tile_w/8) x (tile_h/4) warps: tiles 8x8, 16x8, 32x4, 8x16, 32x8 or 16x16.
+ * variant selects the register budget of the kernel (0: compiler's choice,
+ * 1: <= 128, 2: <= 80 registers per thread).  Results do not depend on the
+ * choice. */
 cvr_status cvr_set_tuning(cvr_ctx* ctx, int tile_w, int tile_h, int variant);
 cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
-/* Autotuner: renders the given frame with every tile shape x variant
- * (reps timed frames each, CUDA events, L2 flushed before each), keeps the
- * fastest on the context and reports it.  best_ms may be NULL. */
+/* Storage of the volume the marchers read: 0 = the plain x-fastest array,
+ * else bricks of edge^3 voxels (edge 4, 8, 16 or 32; bricks x-fastest, voxels
+ * x-fastest inside a brick), a copy made on the first frame after the volume
+ * or the size changed.  Results do not depend on it. */
+cvr_status cvr_set_brick_size(cvr_ctx* ctx, int edge);
+int cvr_get_brick_size(cvr_ctx* ctx);
+/* Autotuner: renders the given frame with every tile shape x register variant
+ * (reps timed frames each, CUDA events, L2 flushed before each), then every
+ * brick size at the best of those; keeps the fastest configuration on the
+ * context and reports it (cvr_get_brick_size reports the brick).  best_ms may
+ * be NULL. */
 cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
                         const void* params, size_t params_size, int w, int h, int reps,
                         int* best_tile_w, int* best_tile_h, int* best_variant, float* best_ms);

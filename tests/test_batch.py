@@ -42,9 +42,14 @@ def test_volume_slots_keep_their_tables(ctx):
     ctx.select_volume(0)
 
 
-@pytest.mark.parametrize("sampling", [abi.SAMPLING_TEX_FEATURES, 0])
-def test_batch_equals_single_renders(ctx, sampling):
+@pytest.mark.parametrize("sampling,tile,variant,brick", [(abi.SAMPLING_TEX_FEATURES, (16, 8), 0, 0),
+                                                         (0, (16, 8), 0, 0),
+                                                         (abi.SAMPLING_TEX_FEATURES, (32, 8), 1, 8),
+                                                         (abi.SAMPLING_TEX_FEATURES, (8, 8), 2, 16)])
+def test_batch_equals_single_renders(ctx, sampling, tile, variant, brick):
     ctx.set_sampling(sampling)
+    abi.check(ctx.lib.cvr_set_tuning(ctx.h, tile[0], tile[1], variant), ctx.h)
+    abi.check(ctx.lib.cvr_set_brick_size(ctx.h, brick), ctx.h)
     vols = scene.batch_volumes(0.5)  # 64^3 u8, 96x128x80 u16, 128^3 u8, 192^3 u16
     scene.prepare_batch_volumes(ctx, vols)
     small_network(ctx)
@@ -88,6 +93,8 @@ def test_batch_equals_single_renders(ctx, sampling):
     finally:
         ctx.select_volume(0)
         ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+        abi.check(ctx.lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
+        abi.check(ctx.lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
         mem.close()
 
 

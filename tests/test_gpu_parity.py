@@ -198,28 +198,54 @@ def test_errors_are_reported_not_crashing(ctx):
     empty.close()
 
 
-def test_tuning_does_not_change_results(ctx):
-    """Every tile shape / register variant renders the same bits."""
+TILES = [(8, 8), (16, 8), (32, 4), (8, 16), (32, 8), (16, 16)]
+
+
+@pytest.mark.parametrize("name,n,image", [("extinction", 48, 72), ("plain", 40, 56), ("cone", 40, 48),
+                                          ("ground_truth", 24, 40)])
+def test_tuning_does_not_change_results(ctx, name, n, image):
+    """Every tile shape / register variant / brick size renders the same bits."""
+    import ctypes as C
+    lib = abi.load()
+    wl = scene.workload(name, n=n, image=image)
+    scene.prepare(ctx, wl)
+    images = []
+    for tw, th in TILES:
+        for v in ((0, 1, 2) if name == "extinction" else (0,)):
+            abi.check(lib.cvr_set_tuning(ctx.h, tw, th, v), ctx.h)
+            img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+            images.append(img)
+    abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
+    for edge in (4, 8, 16, 32):
+        abi.check(lib.cvr_set_brick_size(ctx.h, edge), ctx.h)
+        assert lib.cvr_get_brick_size(ctx.h) == edge
+        img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+        images.append(img)
+    abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
+    for im in images[1:]:
+        assert np.array_equal(im, images[0])
+    assert lib.cvr_set_tuning(ctx.h, 24, 8, 0) == abi.CVR_ERR_INVALID_ARG  # 6 warps
+    assert lib.cvr_set_tuning(ctx.h, 12, 8, 0) == abi.CVR_ERR_INVALID_ARG  # not whole warps
+    assert lib.cvr_set_brick_size(ctx.h, 12) == abi.CVR_ERR_INVALID_ARG
+
+
+def test_autotune_picks_a_valid_configuration(ctx):
     import ctypes as C
     lib = abi.load()
     wl = scene.workload("extinction", n=48, image=72)
     scene.prepare(ctx, wl)
-    images = []
-    for tw, th in [(16, 8), (32, 4), (8, 16)]:
-        for v in (0, 1, 2):
-            abi.check(lib.cvr_set_tuning(ctx.h, tw, th, v), ctx.h)
-            img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
-            images.append(img)
-    for im in images[1:]:
-        assert np.array_equal(im, images[0])
-    assert lib.cvr_set_tuning(ctx.h, 16, 16, 0) == abi.CVR_ERR_INVALID_ARG
     tw, th, v = C.c_int(), C.c_int(), C.c_int()
     ms = C.c_float()
     abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
                                C.sizeof(wl.params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(v),
                                C.byref(ms)), ctx.h)
-    assert (tw.value, th.value) in [(16, 8), (32, 4), (8, 16)] and v.value in (0, 1, 2) and ms.value > 0
+    assert (tw.value, th.value) in TILES and v.value in (0, 1, 2) and ms.value > 0
+    assert lib.cvr_get_brick_size(ctx.h) in (0, 8, 16, 32)
+    img, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
     abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
+    abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
+    ref, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+    assert np.array_equal(img, ref)
 
 
 def test_directional_shadow_table_matches_per_sample_geometry(ctx):
