@@ -288,15 +288,28 @@ def surrogate_section(ctx, lib, args, log=print):
     out = C.POINTER(C.c_float)()
     abi.check(lib.cvr_get_frame_buffer(ctx.h, wl.width, wl.height, C.byref(out)), ctx.h)
     optr = C.cast(out, C.c_void_p)
+    # Both renderers tuned before timing: the ground truth by the autotuner (tile x
+    # registers x brick, on a 256^2 frame of the same view), the surrogate over the
+    # brick sizes (its persistent launch does not use tiles).
+    tw, th, tv = C.c_int(), C.c_int(), C.c_int()
+    abi.check(lib.cvr_autotune(ctx.h, abi.GROUND_TRUTH, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                               C.sizeof(wl.params), 256, 256, 1, C.byref(tw), C.byref(th), C.byref(tv), None), ctx.h)
+    gt_tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h)}
     st_s, st_g = abi.FrameStats(), abi.FrameStats()
-    for method, st in ((abi.SURROGATE, st_s), (abi.GROUND_TRUTH, st_g)):
-        abi.check(lib.cvr_render(ctx.h, method, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
-                                 C.sizeof(wl.params), optr, wl.width, wl.height, None, C.byref(st)), ctx.h)
-    wl.method = abi.SURROGATE
-    ts = time_frames(ctx, lib, wl, wl.params, optr, 5, 2)
+    abi.check(lib.cvr_render(ctx.h, abi.GROUND_TRUTH, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                             C.sizeof(wl.params), optr, wl.width, wl.height, None, C.byref(st_g)), ctx.h)
     wl.method = abi.GROUND_TRUTH
     tg = time_frames(ctx, lib, wl, wl.params, optr, 2, 1)
     wl.method = abi.SURROGATE
+    best_brick, ts = 0, None
+    for edge in (0, 8, 16, 32):
+        abi.check(lib.cvr_set_brick_size(ctx.h, edge), ctx.h)
+        t = time_frames(ctx, lib, wl, wl.params, optr, 3, 1)
+        if ts is None or statistics.median(t) < statistics.median(ts):
+            ts, best_brick = t, edge
+    abi.check(lib.cvr_set_brick_size(ctx.h, best_brick), ctx.h)
+    abi.check(lib.cvr_render(ctx.h, abi.SURROGATE, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                             C.sizeof(wl.params), optr, wl.width, wl.height, None, C.byref(st_s)), ctx.h)
     ms_s, ms_g = statistics.median(ts), statistics.median(tg)
     peak, src = measured_peak_bf16()
     tflops = st_s.shaded_samples * MLP_FLOP_PER_SAMPLE / (ms_s / 1000.0) / 1e12
@@ -308,6 +321,7 @@ def surrogate_section(ctx, lib, args, log=print):
         "heldout": {k: err[k] for k in ("rmse_ao", "rmse_shadow", "cone_rmse_ao", "cone_rmse_shadow", "points",
                                         "mean_ao", "mean_shadow", "max_err_ao", "shaded_samples")},
         "gt_ms": ms_g, "surrogate_ms": ms_s, "speedup_vs_gt": ms_g / ms_s,
+        "gt_tuning": gt_tuning, "surrogate_brick": best_brick,
         "surrogate_fps": 1000.0 / ms_s, "surrogate_msamples_s": st_s.samples / (ms_s / 1000.0) / 1e6,
         "gt_msamples_s": st_g.samples / (ms_g / 1000.0) / 1e6,
         "mlp_tensor": {"achieved_tflops": tflops, "peak_tflops": peak, "frac": tflops / peak,
@@ -389,7 +403,8 @@ def batch_section(ctx, lib, args, log=print):
             "msamples_s": tot / (med / 1000.0) / 1e6, "samples": {"extinction": samples[abi.EXTINCTION],
                                                                   "surrogate": samples[abi.SURROGATE]},
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
-            "tuning": {"tile": [tw.value, th.value], "variant": tv.value}, "prepare_s": t_prep,
+            "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h)},
+            "prepare_s": t_prep,
             "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
 
 
@@ -418,7 +433,8 @@ def run_ours(args):
     abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
                                C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
                                C.byref(tms)), ctx.h)
-    tuning = {"tile": [tw.value, th.value], "variant": tv.value, "autotune_ms": tms.value}
+    tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
+              "autotune_ms": tms.value}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),

@@ -36,6 +36,7 @@ MLP_PARAMS = 7426
 MLP_INPUTS = 48
 SURROGATE_LEVELS = 6
 SAMPLING_TEX_FEATURES = 1
+SAMPLING_TEX_VOLUME = 2
 MLP_NOALLOC_MAX_POINTS = 8192
 MAX_VOLUMES = 16
 MAX_CONE_SECTIONS = 512

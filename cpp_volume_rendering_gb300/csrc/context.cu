@@ -122,6 +122,11 @@ cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
     v.stride[1] = bx * v.stride[0];
     v.stride[2] = by * v.stride[1];
   }
+  if (c->sampling & CVR_SAMPLING_TEX_VOLUME) {
+    cvr_status st = ensure_volume_texture(c);
+    if (st != CVR_OK) return st;
+    v.tex = c->tex.vol.tex;
+  }
   *out = v;
   return CVR_OK;
 }

@@ -119,8 +119,6 @@ struct SurState {
   size_t pts_cap = 0;            // points
   int n_pts = 0;
   unsigned int* counter = nullptr;  // collection count / marcher ray counter
-  unsigned int* order = nullptr;    // marcher block order (+ 64 bucket counters)
-  size_t order_cap = 0;             // blocks
   float* cx = nullptr;           // per-chunk features, targets, predictions, cone values
   float* ct = nullptr;
   float* cy = nullptr;
@@ -128,7 +126,7 @@ struct SurState {
   size_t chunk_cap = 0;
   double* acc = nullptr;         // error sums of cvr_surrogate_evaluate
   ~SurState() {
-    void* bufs[] = {pts, counter, order, cx, ct, cy, cd, acc};
+    void* bufs[] = {pts, counter, cx, ct, cy, cd, acc};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }
@@ -257,6 +255,8 @@ inline VolumeView volume_view(const cvr_ctx* c) {
   v.inv_spacing = f3(1.0f / c->sx, 1.0f / c->sy, 1.0f / c->sz);
   v.grid = f3(c->nx * c->sx, c->ny * c->sy, c->nz * c->sz);
   v.norm = c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f;
+  v.tex = 0;
+  v.inv_grid = f3(1.0f / v.grid.x, 1.0f / v.grid.y, 1.0f / v.grid.z);
   v.bs = 0;
   v.stride[0] = 1;
   v.stride[1] = c->nx;

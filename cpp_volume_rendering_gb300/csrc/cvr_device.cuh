@@ -51,6 +51,10 @@ struct VolumeView {
   // 1, nx, nx*ny).
   int bs;
   long long stride[3];
+  // Texture-unit copy (hardware trilinear, 8-bit weights), or 0: when set,
+  // sample_volume reads it instead of the array (CVR_SAMPLING_TEX_VOLUME).
+  cudaTextureObject_t tex;
+  float3 inv_grid;
 };
 
 // Per-frame camera frame (glm::lookAt rows s, u, f) and projection terms.
@@ -122,6 +126,7 @@ __device__ __forceinline__ Tap axis_tap(float u, int n) {
 // texture(TexVolume, tex_pos / VolumeGridSize).r with tex_pos in [0, S]:
 // texel coordinate = tex_pos / spacing - 0.5.
 __device__ __forceinline__ float sample_volume(const VolumeView& v, float3 tex_pos) {
+  if (v.tex) return tex3D<float>(v.tex, tex_pos.x * v.inv_grid.x, tex_pos.y * v.inv_grid.y, tex_pos.z * v.inv_grid.z);
   Tap tx = axis_tap(fmaf(tex_pos.x, v.inv_spacing.x, -0.5f), v.nx);
   Tap ty = axis_tap(fmaf(tex_pos.y, v.inv_spacing.y, -0.5f), v.ny);
   Tap tz = axis_tap(fmaf(tex_pos.z, v.inv_spacing.z, -0.5f), v.nz);

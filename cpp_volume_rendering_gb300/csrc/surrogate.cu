@@ -140,62 +140,6 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
   return cudaGetLastError();
 }
 
-// ---------------------------------------------------------------- block order
-// The marcher takes 8x4-pixel blocks in the order of a permutation that puts
-// long rays first (a longest-processing-time-first schedule: the frame ends
-// when the last block taken is done, so short blocks should come last).  The
-// key of a block is the box chord of its centre ray, in 64 buckets; blocks
-// are counting-sorted by bucket.  The image does not depend on the order.
-constexpr int kOrderBuckets = 64;
-
-__device__ __forceinline__ int block_bucket(const FrameArgs& f, int b, int tiles_x) {
-  int px = (b % tiles_x) * 8 + 4, py = (b / tiles_x) * 4 + 2;
-  px = min(px, f.W - 1);
-  py = min(py, f.H - 1);
-  float3 dir = primary_dir(f.cam, px, py, f.W, f.H);
-  float tnear, tfar;
-  if (!ray_aabb(f.cam.eye, dir, f.vol.grid, tnear, tfar)) return kOrderBuckets - 1;
-  float diag = sqrtf(dot3(f.vol.grid, f.vol.grid));
-  int k = (int)(fabsf(tfar - tnear) / diag * (float)kOrderBuckets);
-  return kOrderBuckets - 1 - min(max(k, 0), kOrderBuckets - 1);  // longest first
-}
-
-__global__ void k_order_count(FrameArgs f, int tiles_x, int n_blocks, unsigned int* counts) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < n_blocks) atomicAdd(counts + block_bucket(f, b, tiles_x), 1u);
-}
-
-// Exclusive scan of the bucket counts (one warp).
-__global__ void k_order_scan(unsigned int* counts) {
-  unsigned int run = 0;
-  const int lane = threadIdx.x;
-  for (int base = 0; base < kOrderBuckets; base += 32) {
-    unsigned int v = counts[base + lane], x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    counts[base + lane] = run + x - v;
-    run += __shfl_sync(0xffffffffu, x, 31);
-  }
-}
-
-__global__ void k_order_scatter(FrameArgs f, int tiles_x, int n_blocks, unsigned int* offsets, unsigned int* perm) {
-  int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < n_blocks) perm[atomicAdd(offsets + block_bucket(f, b, tiles_x), 1u)] = (unsigned int)b;
-}
-
-cudaError_t launch_block_order(const FrameArgs& f, unsigned int* scratch, unsigned int* perm, cudaStream_t st) {
-  const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2, n = tiles_x * tiles_y;
-  cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned int) * kOrderBuckets, st);
-  if (e != cudaSuccess) return e;
-  k_order_count<<<(n + 255) / 256, 256, 0, st>>>(f, tiles_x, n, scratch);
-  k_order_scan<<<1, 32, 0, st>>>(scratch);
-  k_order_scatter<<<(n + 255) / 256, 256, 0, st>>>(f, tiles_x, n, scratch, perm);
-  return cudaGetLastError();
-}
-
 // ---------------------------------------------------------------- fused marcher
 // Next ray index for every active lane of a warp with one atomic.
 __device__ __forceinline__ unsigned take_ray(unsigned int* work) {
@@ -220,19 +164,44 @@ struct SurRay {
 // Where a marcher thread's rays come from.  SingleSource: one frame, rays in
 // the longest-first block order.  BatchSource: the jobs of a batch, each a
 // run of 8x4-pixel tiles of one counter (jobs ordered by first tile).
+// Square spiral of 8x4-pixel tiles around the tile (cx, cy): sequence number
+// k -> ring r = ceil((sqrt(k+1) - 1) / 2), then the position on that ring.
+// Tiles near the projected volume centre (the longest rays) come first and
+// consecutive tiles are neighbours, so the CTAs' working sets overlap.
+__device__ __forceinline__ void spiral_tile(unsigned k, int& dx, int& dy) {
+  if (k == 0) { dx = dy = 0; return; }
+  int r = (int)((sqrtf((float)k + 1.0f) - 1.0f) * 0.5f);
+  while ((unsigned)(2 * r + 1) * (unsigned)(2 * r + 1) <= k) ++r;  // fix float rounding
+  while (r > 0 && (unsigned)(2 * r - 1) * (unsigned)(2 * r - 1) > k) --r;
+  const int m = (int)(k - (unsigned)(2 * r - 1) * (unsigned)(2 * r - 1));
+  const int side = m / (2 * r), off = m % (2 * r);
+  switch (side) {
+    case 0: dx = r; dy = -r + 1 + off; break;
+    case 1: dx = r - 1 - off; dy = r; break;
+    case 2: dx = -r; dy = r - 1 - off; break;
+    default: dx = -r + 1 + off; dy = -r; break;
+  }
+}
+
+// Where a marcher thread's rays come from.  SingleSource: one frame, tiles
+// in the square spiral around (cx, cy) (positions outside the image are
+// skipped: px = -1).  BatchSource: the jobs of a batch, each a run of
+// 8x4-pixel tiles of one counter (jobs ordered by first tile).
 struct SingleSource {
   const FrameArgs& f0;
   const SurArgs& a0;
-  const unsigned int* order;
-  int tiles_x;
+  int cx, cy, tiles_x, tiles_y;
   unsigned total;
   __device__ __forceinline__ const FrameArgs& f(int) const { return f0; }
   __device__ __forceinline__ const SurArgs& a(int) const { return a0; }
   __device__ __forceinline__ void locate(unsigned idx, SurRay& r) const {
-    const int tile = (int)__ldg(order + (idx >> 5)), within = (int)(idx & 31u);
+    int dx, dy;
+    spiral_tile(idx >> 5, dx, dy);
+    const int tx = cx + dx, ty = cy + dy, within = (int)(idx & 31u);
     r.job = 0;
-    r.px = (tile % tiles_x) * 8 + (within & 7);
-    r.py = (tile / tiles_x) * 4 + (within >> 3);
+    if (tx < 0 || ty < 0 || tx >= tiles_x || ty >= tiles_y) { r.px = -1; r.py = -1; return; }
+    r.px = tx * 8 + (within & 7);
+    r.py = ty * 4 + (within >> 3);
   }
 };
 
@@ -331,7 +300,7 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
         if (idx >= total) { no_work = true; break; }
         src_rays.locate(idx, ray);
         const FrameArgs& f = src_rays.f(ray.job);
-        if (ray.px >= f.W || ray.py >= f.H) continue;
+        if (ray.px < 0 || ray.px >= f.W || ray.py >= f.H) continue;
         if (ray.job != cnt.job) {
           if (BATCH) cnt.flush(src_rays.f(cnt.job < 0 ? 0 : cnt.job).stats);
           cnt.job = ray.job;
@@ -411,10 +380,9 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
 }
 
 template <bool TEX>
-__global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs a, const unsigned int* __restrict__ order,
+__global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs a, int cx, int cy, unsigned total,
                                                             unsigned int* work, int* err) {
-  const int tiles_x = (f.W + 7) >> 3, tiles_y = (f.H + 3) >> 2;
-  SingleSource s{f, a, order, tiles_x, (unsigned)tiles_x * (unsigned)tiles_y * 32u};
+  SingleSource s{f, a, cx, cy, (f.W + 7) >> 3, (f.H + 3) >> 2, total};
   sur_march<TEX, false>(s, f.tf, f.tf_n, a.packed, work, err);
 }
 
@@ -455,15 +423,20 @@ cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned tota
   return cudaGetLastError();
 }
 
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const unsigned int* order,
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, int center_x, int center_y,
                              unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
   auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
-  const unsigned rays = (unsigned)((f.W + 7) / 8) * (unsigned)((f.H + 3) / 4) * 32u;
+  const int tiles_x = (f.W + 7) / 8, tiles_y = (f.H + 3) / 4;
+  const int cx = min(max(center_x / 8, 0), tiles_x - 1), cy = min(max(center_y / 4, 0), tiles_y - 1);
+  const int R = max(max(cx, tiles_x - 1 - cx), max(cy, tiles_y - 1 - cy));
+  const unsigned long long spiral = (unsigned long long)(2 * R + 1) * (unsigned long long)(2 * R + 1) * 32ull;
+  if (spiral > 0xFFFFFFF0ull) return cudaErrorInvalidValue;
+  const unsigned rays = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
   unsigned ctas = 0;
   cudaError_t e = surrogate_grid(kern, smem, rays, &ctas);
   if (e != cudaSuccess) return e;
-  kern<<<ctas, 128, smem, st>>>(f, a, order, work, err);
+  kern<<<ctas, 128, smem, st>>>(f, a, cx, cy, (unsigned)spiral, work, err);
   return cudaGetLastError();
 }
 

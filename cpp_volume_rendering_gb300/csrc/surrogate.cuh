@@ -183,16 +183,13 @@ struct SurJob {
 cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
                                    unsigned int* work, int* err, cudaStream_t st);
 
-// Longest-first order of the frame's 8x4-pixel blocks: perm receives
-// ceil(W/8) * ceil(H/4) block indices; scratch holds 64 counters.
-cudaError_t launch_block_order(const FrameArgs& f, unsigned int* scratch, unsigned int* perm, cudaStream_t st);
-
 // The surrogate-shaded marcher: persistent CTAs take rays from *work (zeroed
-// before the launch) in 8x4-pixel blocks in the given block order; every
-// round, each thread advances its ray to the next shaded sample, the CTA
-// evaluates the network for its 128 samples on the tensor cores, and each
-// thread composites its sample.
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const unsigned int* order,
+// before the launch) in 8x4-pixel tiles, in a square spiral around the tile
+// of pixel (center_x, center_y) (the projected volume centre: long rays
+// first, neighbouring tiles together); every round, each thread advances its
+// ray to the next shaded sample, the CTA evaluates the network for its 128
+// samples on the tensor cores, and each thread composites its sample.
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, int center_x, int center_y,
                              unsigned int* work, int* err, cudaStream_t st);
 
 }  // namespace cvr

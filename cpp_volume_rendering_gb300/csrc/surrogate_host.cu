@@ -206,18 +206,20 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   bool tex = false;
   cvr_status st = sur_job_args(c, p, light, &a, &tex);
   if (st != CVR_OK) return st;
-  SurState& s = *c->sur;
-  const size_t blocks = (size_t)((f.W + 7) / 8) * ((f.H + 3) / 4);
-  if (s.order_cap < blocks) {
-    if (s.order) cudaFree(s.order);
-    s.order = nullptr;
-    s.order_cap = 0;
-    CK(c, cudaMalloc((void**)&s.order, sizeof(unsigned int) * (blocks + 64)));
-    s.order_cap = blocks;
+  // pixel of the projected volume centre (the box is centred on the origin)
+  const float3 d = f3(0.0f, 0.0f, 0.0f) - f.cam.eye;
+  const float zf = dot3(d, f.cam.f);
+  int cx = f.W / 2, cy = f.H / 2;
+  if (zf > 1e-6f) {
+    const float xn = dot3(d, f.cam.s) / (zf * f.cam.tan_half_fovy * f.cam.aspect);
+    const float yn = dot3(d, f.cam.u) / (zf * f.cam.tan_half_fovy);
+    if (std::isfinite(xn) && std::isfinite(yn) && std::fabs(xn) < 4.0f && std::fabs(yn) < 4.0f) {
+      cx = (int)((xn * 0.5f + 0.5f) * (float)f.W);
+      cy = (int)((yn * 0.5f + 0.5f) * (float)f.H);
+    }
   }
-  CK(c, launch_block_order(f, s.order + blocks, s.order, c->stream));
-  CK(c, cudaMemsetAsync(s.counter, 0, sizeof(unsigned int), c->stream));
-  CK(c, launch_surrogate(f, a, tex, s.order, s.counter, c->mlp->err, c->stream));
+  CK(c, cudaMemsetAsync(c->sur->counter, 0, sizeof(unsigned int), c->stream));
+  CK(c, launch_surrogate(f, a, tex, cx, cy, c->sur->counter, c->mlp->err, c->stream));
   return CVR_OK;
 }
 

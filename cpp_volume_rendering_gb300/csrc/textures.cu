@@ -2,11 +2,25 @@
 // pyramid levels: 3D CUDA arrays sampled with hardware trilinear filtering,
 // normalised coordinates and clamp-to-edge addressing (the OpenGL
 // GL_LINEAR / GL_CLAMP_TO_EDGE sampling of the reference's textures).
+#include <algorithm>
+
+#include <cuda_fp16.h>
+
 #include "ctx.cuh"
 
 using namespace cvr::ctxutil;
 
 namespace {
+
+__global__ void k_to_half(const float* __restrict__ src, __half* __restrict__ dst, long long n) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = __float2half_rn(src[i]);
+}
+
+cudaError_t launch_to_half(const float* src, __half* dst, long long n, cudaStream_t st) {
+  k_to_half<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst, n);
+  return cudaGetLastError();
+}
 
 cudaError_t make_texture(cvr_ctx* c, TexImage& t, const void* src, size_t elem, cudaChannelFormatDesc desc, int w,
                          int h, int d, cudaTextureReadMode mode) {
@@ -51,20 +65,34 @@ cvr_status ensure_volume_texture(cvr_ctx* c) {
   return CVR_OK;
 }
 
+// Pyramid levels as FP16 textures (the reference keeps the pyramid in R16F,
+// extcoefvolumegenerator.cpp:246-252): half the bytes of the texture reads.
 cvr_status ensure_pyramid_textures(cvr_ctx* c) {
   if (c->tex.pyr_valid) return CVR_OK;
   if (!c->pyr_ready) return fail(c, CVR_ERR_NOT_READY, "pyramid textures: no pyramid");
   for (auto& t : c->tex.pyr) t.release();
   c->tex.n_pyr = 0;
-  for (int l = 0; l < c->pyr.n_levels; ++l) {
+  long long total = 0;
+  for (int l = 0; l < c->pyr.n_levels; ++l)
+    total = std::max(total, (long long)c->pyr.dims[l][0] * c->pyr.dims[l][1] * c->pyr.dims[l][2]);
+  __half* tmp = nullptr;
+  CK(c, cudaMalloc((void**)&tmp, sizeof(__half) * (size_t)total));
+  cudaError_t e = cudaSuccess;
+  for (int l = 0; l < c->pyr.n_levels && e == cudaSuccess; ++l) {
     const int* d = c->pyr.dims[l];
-    cudaError_t e = make_texture(c, c->tex.pyr[l], c->d_pyr + c->pyr.offset[l], sizeof(float),
-                                 cudaCreateChannelDesc<float>(), d[0], d[1], d[2], cudaReadModeElementType);
-    if (e != cudaSuccess) {
-      for (auto& t : c->tex.pyr) t.release();
-      return cuda_fail(c, e, "pyramid texture");
-    }
-    c->tex.n_pyr = l + 1;
+    const long long n = (long long)d[0] * d[1] * d[2];
+    e = launch_to_half(c->d_pyr + c->pyr.offset[l], tmp, n, c->stream);
+    if (e == cudaSuccess)
+      e = make_texture(c, c->tex.pyr[l], tmp, sizeof(__half), cudaCreateChannelDescHalf(), d[0], d[1], d[2],
+                       cudaReadModeElementType);
+    // the array copy reads tmp on the stream: finish before the next level reuses it
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) c->tex.n_pyr = l + 1;
+  }
+  cudaFree(tmp);
+  if (e != cudaSuccess) {
+    for (auto& t : c->tex.pyr) t.release();
+    return cuda_fail(c, e, "pyramid texture");
   }
   c->tex.pyr_valid = true;
   return CVR_OK;
@@ -77,7 +105,8 @@ extern "C" {
 
 cvr_status cvr_set_sampling(cvr_ctx* c, int flags) {
   if (!c) return CVR_ERR_INVALID_ARG;
-  if (flags & ~CVR_SAMPLING_TEX_FEATURES) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_sampling: unknown flags");
+  if (flags & ~(CVR_SAMPLING_TEX_FEATURES | CVR_SAMPLING_TEX_VOLUME))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_sampling: unknown flags");
   c->sampling = flags;
   return CVR_OK;
 }

@@ -290,9 +290,14 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
  * network's inputs (pyramid taps and the volume taps of the gradient) go
  * through the texture unit (trilinear filtering with 8-bit interpolation
  * weights, |input error| below 3e-2) instead of the FP32 trilinear; the
- * default, since the network's inputs dominate a surrogate frame.  A network
- * is best used with the flags it was trained with. */
+ * default, since the network's inputs dominate a surrogate frame; the
+ * pyramid is read as FP16 there, as the reference stores it).
+ * CVR_SAMPLING_TEX_VOLUME: the primary volume samples of every marcher (and
+ * the ground truth's light rays) through the texture unit; images within
+ * 1/255 of the FP32 path.  A network is best used with the flags it was
+ * trained with. */
 #define CVR_SAMPLING_TEX_FEATURES 1
+#define CVR_SAMPLING_TEX_VOLUME 2
 cvr_status cvr_set_sampling(cvr_ctx* ctx, int flags);
 int cvr_get_sampling(cvr_ctx* ctx);
 

@@ -198,6 +198,27 @@ def test_errors_are_reported_not_crashing(ctx):
     empty.close()
 
 
+@pytest.mark.parametrize("name,n,image", [("plain", 64, 128), ("extinction", 40, 96), ("cone", 40, 80),
+                                          ("ground_truth", 32, 64)])
+def test_texture_variant_parity(ctx, name, n, image):
+    """The hardware-texture variant of the volume samples (8-bit filter
+    weights) stays within 1/255 max-abs of the FP64 oracle, PSNR >= 45 dB;
+    for the cone method 2/255: a ray whose opacity crosses the 0.99 cut one
+    step earlier or later moves its pixel by up to 1% of its colour."""
+    wl = scene.workload(name, n=n, image=image)
+    ctx.set_sampling(abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)
+    try:
+        img, st, ref, total = run_both(ctx, wl)
+    finally:
+        ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+    err = np.abs(img.astype(np.float64) - ref)
+    p = psnr(img, ref)
+    print(f"texture variant {name}: max abs {err.max():.2e}, PSNR {p:.1f} dB, samples {st.samples} vs {total}")
+    assert np.isfinite(img).all()
+    assert err.max() <= (2.0 / 255.0 if name == "cone" else MAX_ABS), err.max()
+    assert p >= 45.0, p
+
+
 TILES = [(8, 8), (16, 8), (32, 4), (8, 16), (32, 8), (16, 16)]
 
 
