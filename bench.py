@@ -288,28 +288,42 @@ def surrogate_section(ctx, lib, args, log=print):
     out = C.POINTER(C.c_float)()
     abi.check(lib.cvr_get_frame_buffer(ctx.h, wl.width, wl.height, C.byref(out)), ctx.h)
     optr = C.cast(out, C.c_void_p)
-    # Both renderers tuned before timing: the ground truth by the autotuner (tile x
-    # registers x brick, on a 256^2 frame of the same view), the surrogate over the
-    # brick sizes (its persistent launch does not use tiles).
-    tw, th, tv = C.c_int(), C.c_int(), C.c_int()
-    abi.check(lib.cvr_autotune(ctx.h, abi.GROUND_TRUTH, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
-                               C.sizeof(wl.params), 256, 256, 1, C.byref(tw), C.byref(th), C.byref(tv), None), ctx.h)
-    gt_tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h)}
+    # Both renderers tuned before timing, each over the sampling modes (FP32
+    # volume samples, or texture-unit samples) and the autotuner's space (tile x
+    # registers x brick for the ground truth on a 256^2 frame of the same view;
+    # CTAs per SM x brick for the surrogate, whose persistent launch ignores the
+    # tile, on a 512^2 frame).  The fastest configuration of each is timed.
+    def tuned(method, size, flags_list):
+        best = None
+        for flags in flags_list:
+            ctx.set_sampling(flags)
+            tw, th, tv = C.c_int(), C.c_int(), C.c_int()
+            abi.check(lib.cvr_autotune(ctx.h, method, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                                       C.sizeof(wl.params), size, size, 1, C.byref(tw), C.byref(th), C.byref(tv),
+                                       None), ctx.h)
+            cfg = {"sampling": flags, "tile": [tw.value, th.value], "variant": tv.value,
+                   "brick": lib.cvr_get_brick_size(ctx.h)}
+            wl.method = method
+            t = time_frames(ctx, lib, wl, wl.params, optr, 2 if method == abi.GROUND_TRUTH else 3, 1)
+            if best is None or statistics.median(t) < statistics.median(best[1]):
+                best = (cfg, t)
+        cfg = best[0]
+        ctx.set_sampling(cfg["sampling"])
+        abi.check(lib.cvr_set_tuning(ctx.h, cfg["tile"][0], cfg["tile"][1], cfg["variant"]), ctx.h)
+        abi.check(lib.cvr_set_brick_size(ctx.h, cfg["brick"]), ctx.h)
+        return best
+    sampling_modes = (abi.SAMPLING_TEX_FEATURES, abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)
+    gt_tuning, tg = tuned(abi.GROUND_TRUTH, 256, sampling_modes)
     st_s, st_g = abi.FrameStats(), abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, abi.GROUND_TRUTH, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
                              C.sizeof(wl.params), optr, wl.width, wl.height, None, C.byref(st_g)), ctx.h)
-    wl.method = abi.GROUND_TRUTH
-    tg = time_frames(ctx, lib, wl, wl.params, optr, 2, 1)
-    wl.method = abi.SURROGATE
-    best_brick, ts = 0, None
-    for edge in (0, 8, 16, 32):
-        abi.check(lib.cvr_set_brick_size(ctx.h, edge), ctx.h)
-        t = time_frames(ctx, lib, wl, wl.params, optr, 3, 1)
-        if ts is None or statistics.median(t) < statistics.median(ts):
-            ts, best_brick = t, edge
-    abi.check(lib.cvr_set_brick_size(ctx.h, best_brick), ctx.h)
+    # the exact (FP32 volume samples) ground truth at its best tuning, for reference
+    ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+    gt_fp32_tuning, tg32 = tuned(abi.GROUND_TRUTH, 256, (abi.SAMPLING_TEX_FEATURES,))
+    sur_tuning, ts = tuned(abi.SURROGATE, 512, sampling_modes)
     abi.check(lib.cvr_render(ctx.h, abi.SURROGATE, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
                              C.sizeof(wl.params), optr, wl.width, wl.height, None, C.byref(st_s)), ctx.h)
+    wl.method = abi.SURROGATE
     ms_s, ms_g = statistics.median(ts), statistics.median(tg)
     peak, src = measured_peak_bf16()
     tflops = st_s.shaded_samples * MLP_FLOP_PER_SAMPLE / (ms_s / 1000.0) / 1e12
@@ -321,7 +335,9 @@ def surrogate_section(ctx, lib, args, log=print):
         "heldout": {k: err[k] for k in ("rmse_ao", "rmse_shadow", "cone_rmse_ao", "cone_rmse_shadow", "points",
                                         "mean_ao", "mean_shadow", "max_err_ao", "shaded_samples")},
         "gt_ms": ms_g, "surrogate_ms": ms_s, "speedup_vs_gt": ms_g / ms_s,
-        "gt_tuning": gt_tuning, "surrogate_brick": best_brick,
+        "gt_tuning": gt_tuning, "surrogate_tuning": sur_tuning,
+        "gt_fp32_ms": statistics.median(tg32), "gt_fp32_tuning": gt_fp32_tuning,
+        "speedup_vs_gt_fp32": statistics.median(tg32) / ms_s,
         "surrogate_fps": 1000.0 / ms_s, "surrogate_msamples_s": st_s.samples / (ms_s / 1000.0) / 1e6,
         "gt_msamples_s": st_g.samples / (ms_g / 1000.0) / 1e6,
         "mlp_tensor": {"achieved_tflops": tflops, "peak_tflops": peak, "frac": tflops / peak,

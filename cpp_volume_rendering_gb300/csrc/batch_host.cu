@@ -175,8 +175,8 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
     e = launch_batch_extinction(b->d_ext, b->n_ext, b->ext_blocks, b->d_counters, c->tf_n, b->ext_max_table,
                                 b->ext_threads, b->ext_variant, c->stream);
   if (e == cudaSuccess && b->n_sur)
-    e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->d_counters + 1, c->mlp->err,
-                               c->stream);
+    e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->ext_variant,
+                               b->d_counters + 1, c->mlp->err, c->stream);
   cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
     if (g) cudaGraphDestroy(g);

@@ -393,19 +393,30 @@ __global__ void __launch_bounds__(128, 5) k_batch_surrogate(const SurJob* __rest
   sur_march<TEX, true>(s, jobs[0].f.tf, jobs[0].f.tf_n, jobs[0].a.packed, work, err);
 }
 
-// Persistent grid: every SM full (resident CTAs from shared memory and
-// registers, at most 512 / 64 by TMEM), no more CTAs than 128-ray groups.
+// Persistent grid.  CTAs per SM: at most 4 for variant 0, the most that fit
+// (shared memory, registers, at most 512 / 64 by TMEM) for variant 1, at most
+// 3 for variant 2.  The shared-memory carveout is sized to those CTAs,
+// so the rest of the SM's 256 KB serves as L1 / texture cache for the
+// network inputs (fewer CTAs: less latency hiding, more cache).
 template <class K>
-static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, unsigned* ctas) {
+static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, int variant, unsigned* ctas) {
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
+  int dev = 0, sms = 0, per_sm = 0, smem_sm = 0, reserved = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
   if ((e = resident_ctas(kern, 128, smem, &per_sm)) != cudaSuccess) return e;
   per_sm = per_sm > (int)(512 / kSurTmemCols) ? (int)(512 / kSurTmemCols) : per_sm;
+  if (variant == 0 && per_sm > 4) per_sm = 4;
+  if (variant == 2 && per_sm > 3) per_sm = 3;
+  cudaFuncAttributes fa{};
+  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
+  const size_t need = (size_t)per_sm * (smem + fa.sharedSizeBytes + (size_t)reserved);
+  int pct = (int)((need * 100 + (size_t)smem_sm - 1) / (size_t)smem_sm);
+  pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+  if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
   unsigned long long n = (unsigned long long)sms * (unsigned long long)per_sm, groups = (rays + 127ull) / 128ull;
   if (n > groups) n = groups;
   *ctas = n < 1 ? 1u : (unsigned)n;
@@ -413,11 +424,11 @@ static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, unsigned* 
 }
 
 cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
-                                   unsigned int* work, int* err, cudaStream_t st) {
+                                   int variant, unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * tf_n + 16;
   auto kern = tex ? k_batch_surrogate<true> : k_batch_surrogate<false>;
   unsigned ctas = 0;
-  cudaError_t e = surrogate_grid(kern, smem, total_rays, &ctas);
+  cudaError_t e = surrogate_grid(kern, smem, total_rays, variant, &ctas);
   if (e != cudaSuccess) return e;
   kern<<<ctas, 128, smem, st>>>(jobs, n_jobs, total_rays, work, err);
   return cudaGetLastError();
@@ -434,7 +445,7 @@ cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, int
   if (spiral > 0xFFFFFFF0ull) return cudaErrorInvalidValue;
   const unsigned rays = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
   unsigned ctas = 0;
-  cudaError_t e = surrogate_grid(kern, smem, rays, &ctas);
+  cudaError_t e = surrogate_grid(kern, smem, rays, f.variant, &ctas);
   if (e != cudaSuccess) return e;
   kern<<<ctas, 128, smem, st>>>(f, a, cx, cy, (unsigned)spiral, work, err);
   return cudaGetLastError();

@@ -20,8 +20,9 @@
 //          over s_j = (4 + j) d_5, j = 0..7, while s_j <= the shadow-ray
 //          length and tx + L s_j is inside the box
 //   x[42..44] = (L.r, L.u, L.n)
-//   x[45..47] = (g.r, g.u, g.n), g = central differences of the transfer
-//               function extinction at +-1 voxel (per voxel)
+//   x[45..47] = (g.r, g.u, g.n), g = central differences of pyramid level 0
+//               at +-1 voxel, times the voxel length (the level-0 taps are
+//               in cache: no second copy of the volume is read)
 // The same routine produces training inputs and the marcher's inputs.
 #pragma once
 
@@ -37,7 +38,6 @@ constexpr int kSurTapFeatures = kSurLevels * kSurTaps;  // 42
 struct SurArgs {
   PyramidView pyr;  // at least kSurLevels levels
   cudaTextureObject_t ptex[kSurLevels];  // texture-unit copies of the first levels (tex sampling)
-  cudaTextureObject_t vtex;              // texture-unit copy of the volume (tex sampling)
   const uint8_t* packed;  // packed network image (mlp.cuh)
   int apply_occ, apply_sdw, shadow_type;
   float3 light_pos, light_fwd;
@@ -69,19 +69,6 @@ __device__ __forceinline__ float sur_sigma(const SurArgs& a, int l, float3 q) {
   } else {
     return pyr_sample_level(a.pyr, l, q);
   }
-}
-
-// Transfer-function extinction of the volume at q.
-template <bool TEX>
-__device__ __forceinline__ float sur_ext(const SurArgs& a, const VolumeView& vol, const float4* tf, int tf_n,
-                                         float3 q) {
-  float v;
-  if constexpr (TEX) {
-    v = tex3D<float>(a.vtex, q.x * a.pyr.inv_grid.x, q.y * a.pyr.inv_grid.y, q.z * a.pyr.inv_grid.z);
-  } else {
-    v = sample_volume(vol, q);
-  }
-  return tf_alpha(tf, tf_n, v);
 }
 
 // Segment opacity 1 - exp(-sigma_l(q) d) of one tap; 0 outside the box.
@@ -129,12 +116,9 @@ __device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView&
   out(44, dot3(F.L, F.n));
   const float3 sp = vol.spacing;
   float3 g;
-  g.x = 0.5f * (sur_ext<TEX>(a, vol, tf, tf_n, tx + f3(sp.x, 0.0f, 0.0f)) -
-                sur_ext<TEX>(a, vol, tf, tf_n, tx - f3(sp.x, 0.0f, 0.0f)));
-  g.y = 0.5f * (sur_ext<TEX>(a, vol, tf, tf_n, tx + f3(0.0f, sp.y, 0.0f)) -
-                sur_ext<TEX>(a, vol, tf, tf_n, tx - f3(0.0f, sp.y, 0.0f)));
-  g.z = 0.5f * (sur_ext<TEX>(a, vol, tf, tf_n, tx + f3(0.0f, 0.0f, sp.z)) -
-                sur_ext<TEX>(a, vol, tf, tf_n, tx - f3(0.0f, 0.0f, sp.z)));
+  g.x = 0.5f * sp.x * (sur_sigma<TEX>(a, 0, tx + f3(sp.x, 0.0f, 0.0f)) - sur_sigma<TEX>(a, 0, tx - f3(sp.x, 0.0f, 0.0f)));
+  g.y = 0.5f * sp.y * (sur_sigma<TEX>(a, 0, tx + f3(0.0f, sp.y, 0.0f)) - sur_sigma<TEX>(a, 0, tx - f3(0.0f, sp.y, 0.0f)));
+  g.z = 0.5f * sp.z * (sur_sigma<TEX>(a, 0, tx + f3(0.0f, 0.0f, sp.z)) - sur_sigma<TEX>(a, 0, tx - f3(0.0f, 0.0f, sp.z)));
   out(45, dot3(g, F.r));
   out(46, dot3(g, F.u));
   out(47, dot3(g, F.n));
@@ -181,7 +165,7 @@ struct SurJob {
 // Persistent launch over all rays of all jobs (jobs ordered by first_tile;
 // total_rays = 32 x all tiles), rays taken from *work (zeroed before).
 cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
-                                   unsigned int* work, int* err, cudaStream_t st);
+                                   int variant, unsigned int* work, int* err, cudaStream_t st);
 
 // The surrogate-shaded marcher: persistent CTAs take rays from *work (zeroed
 // before the launch) in 8x4-pixel tiles, in a square spiral around the tile

@@ -82,7 +82,6 @@ SurArgs sur_args(cvr_ctx* c, const cvr_light* light, const cvr_gt_params* p, int
   a.kd = kd;
   a.unit = (c->sx + c->sy + c->sz) / 3.0f;
   for (int l = 0; l < kSurLevels; ++l) a.ptex[l] = c->tex.pyr_valid ? c->tex.pyr[l].tex : 0;
-  a.vtex = c->tex.vol_valid ? c->tex.vol.tex : 0;
   return a;
 }
 
@@ -91,9 +90,7 @@ bool use_tex(cvr_ctx* c) { return (c->sampling & CVR_SAMPLING_TEX_FEATURES) != 0
 
 cvr_status prepare_textures(cvr_ctx* c) {
   if (!use_tex(c)) return CVR_OK;
-  cvr_status st = ensure_volume_texture(c);
-  if (st == CVR_OK) st = ensure_pyramid_textures(c);
-  return st;
+  return ensure_pyramid_textures(c);
 }
 
 GtArgs gt_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light) {

@@ -265,8 +265,10 @@ cvr_status cvr_download_frame(cvr_ctx* ctx, const float* dev_frame, int w, int h
  * 2, 4 or 8 warps, each covering an 8x4 pixel block, arranged as
  * (tile_w/8) x (tile_h/4) warps: tiles 8x8, 16x8, 32x4, 8x16, 32x8 or 16x16.
  * variant selects the register budget of the kernel (0: compiler's choice,
- * 1: <= 128, 2: <= 80 registers per thread).  Results do not depend on the
- * choice. */
+ * 1: <= 128, 2: <= 80 registers per thread); for CVR_METHOD_SURROGATE, whose
+ * persistent launch ignores the tile, it selects the CTAs per SM (0: 4,
+ * 1: as many as fit, 2: 3), the rest of the SM's shared memory serving as
+ * cache.  Results do not depend on the choice. */
 cvr_status cvr_set_tuning(cvr_ctx* ctx, int tile_w, int tile_h, int variant);
 cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
 /* Storage of the volume the marchers read: 0 = the plain x-fastest array,
@@ -287,7 +289,7 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
 /* Sampling of secondary lookups (no reference counterpart; the reference's GL
  * texture() fetches are hardware-filtered, the FP32 hand-written trilinear is
  * this project's exact form).  CVR_SAMPLING_TEX_FEATURES: the surrogate
- * network's inputs (pyramid taps and the volume taps of the gradient) go
+ * network's inputs (the pyramid taps) go
  * through the texture unit (trilinear filtering with 8-bit interpolation
  * weights, |input error| below 3e-2) instead of the FP32 trilinear; the
  * default, since the network's inputs dominate a surrogate frame; the
@@ -406,8 +408,8 @@ cvr_status cvr_mlp_load(cvr_ctx* ctx, const char* path);
  *     (0 outside the volume), L the direction towards the light; except
  *     x[35]: 1 - exp(-sum_j sigma_5(p + L s_j) d_5), s_j = (4+j) d_5, j < 8,
  *     over the s_j within sdw_distance and the volume (the far light path);
- *   x[42..44] = L in (r, u, n); x[45..47] = extinction gradient (central
- *     differences at +-1 voxel) in (r, u, n).
+ *   x[42..44] = L in (r, u, n); x[45..47] = gradient of pyramid level 0
+ *     (central differences at +-1 voxel, times the voxel length) in (r, u, n).
  * Outputs: (ambient occlusion, shadow) as the ground-truth integrator defines
  * them (gt_ray_marching.comp:109-252), clamped to [0, 1] when shading. */
 #define CVR_SURROGATE_LEVELS 6

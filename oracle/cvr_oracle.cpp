@@ -515,7 +515,7 @@ template <class T> T gt_shadow(const Frame<T>& f, const Gt<T>& g, V3<T> tx) {
 // The network's inputs (no reference counterpart; definition in cvr.h): six
 // pyramid levels x seven taps of segment opacity around the shading point in
 // the ground-truth occlusion frame (gt_ray_marching.comp:396-399), the light
-// direction and the extinction gradient in that frame.
+// direction and the gradient of pyramid level 0 in that frame.
 template <class T>
 void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, int shadow_type, V3<T> light_pos,
                   V3<T> light_fwd, T sdw_dist, V3<T> tx, V3<T> dir, T* x) {
@@ -557,11 +557,11 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
   x[42] = dot(L, r);
   x[43] = dot(L, u);
   x[44] = dot(L, n);
-  auto sg = [&](V3<T> q) { return tf_alpha<T>(s, sample_volume<T>(s, q)); };
+  auto sg = [&](V3<T> q) { return pyr_level(f, d, 0, q); };  // level 0 of the pyramid
   V3<T> g;
-  g.x = T(0.5) * (sg(tx + v3<T>(f.spacing.x, 0, 0)) - sg(tx - v3<T>(f.spacing.x, 0, 0)));
-  g.y = T(0.5) * (sg(tx + v3<T>(0, f.spacing.y, 0)) - sg(tx - v3<T>(0, f.spacing.y, 0)));
-  g.z = T(0.5) * (sg(tx + v3<T>(0, 0, f.spacing.z)) - sg(tx - v3<T>(0, 0, f.spacing.z)));
+  g.x = T(0.5) * f.spacing.x * (sg(tx + v3<T>(f.spacing.x, 0, 0)) - sg(tx - v3<T>(f.spacing.x, 0, 0)));
+  g.y = T(0.5) * f.spacing.y * (sg(tx + v3<T>(0, f.spacing.y, 0)) - sg(tx - v3<T>(0, f.spacing.y, 0)));
+  g.z = T(0.5) * f.spacing.z * (sg(tx + v3<T>(0, 0, f.spacing.z)) - sg(tx - v3<T>(0, 0, f.spacing.z)));
   x[45] = dot(g, r);
   x[46] = dot(g, u);
   x[47] = dot(g, n);
