@@ -42,6 +42,7 @@ WORKLOAD_DESC = {
     "extinction": "extinction SAT shading: 256^3 u16 value-noise shells -> 1024^2, AO radii {2,6,16} + "
                   "directional SAT cone shadow, step 0.5 voxel",
     "plain": "plain ray casting: 64^3 u8 8-blob volume, unit cube -> 256^2, step 0.5 voxel",
+    "plain_large": "plain ray casting: 256^3 u8 8-blob volume, unit cube -> 1024^2, step 0.5 voxel",
     "cone": "cone DOS shading: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 5-level extinction pyramid, "
             "occlusion + point-light shadow cones",
     "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
@@ -513,26 +514,45 @@ def run_ours(args):
     renderers = {}
     batch = None
     if not args.quick:
+        def reset_tuning():
+            ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+            abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
+            abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)
+        reset_tuning()
         if not args.no_batch:
             batch = batch_section(ctx, lib, args)
-        for name in ("plain", "cone", "ground_truth"):
+        reset_tuning()
+        # every renderer tuned on its own frame (tile x registers x brick), with
+        # FP32 volume samples and with the texture-unit variant
+        for name in ("plain", "plain_large", "cone", "ground_truth"):
             if name == args.workload:
                 continue
             w2 = scene.workload(name)
             scene.prepare(ctx, w2)
             o2 = C.POINTER(C.c_float)()
             abi.check(lib.cvr_get_frame_buffer(ctx.h, w2.width, w2.height, C.byref(o2)), ctx.h)
-            s2 = abi.FrameStats()
-            abi.check(lib.cvr_render(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
-                                     C.sizeof(w2.params), C.cast(o2, C.c_void_p), w2.width, w2.height, None,
-                                     C.byref(s2)), ctx.h)
-            tt = time_frames(ctx, lib, w2, w2.params, C.cast(o2, C.c_void_p), 3, 1)
-            m = statistics.median(tt)
-            renderers[name] = {"workload": WORKLOAD_DESC[name], "ms": m, "fps": 1000.0 / m,
-                               "msamples_s": s2.samples / (m / 1000.0) / 1e6,
-                               "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9}
+            entry = {"workload": WORKLOAD_DESC[name]}
+            for key, flags in (("", abi.SAMPLING_TEX_FEATURES),
+                               ("tex_", abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)):
+                ctx.set_sampling(flags)
+                tw, th, tv = C.c_int(), C.c_int(), C.c_int()
+                abi.check(lib.cvr_autotune(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
+                                           C.sizeof(w2.params), w2.width, w2.height, 1, C.byref(tw), C.byref(th),
+                                           C.byref(tv), None), ctx.h)
+                s2 = abi.FrameStats()
+                abi.check(lib.cvr_render(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
+                                         C.sizeof(w2.params), C.cast(o2, C.c_void_p), w2.width, w2.height, None,
+                                         C.byref(s2)), ctx.h)
+                tt = time_frames(ctx, lib, w2, w2.params, C.cast(o2, C.c_void_p), 3, 1)
+                m = statistics.median(tt)
+                entry.update({key + "ms": m, key + "fps": 1000.0 / m, key + "msamples_s": s2.samples / (m / 1000.0) / 1e6,
+                              key + "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9,
+                              key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
+                                               "brick": lib.cvr_get_brick_size(ctx.h)}})
+            ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+            renderers[name] = entry
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, target_s=args.cpu_seconds)

@@ -393,6 +393,7 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     image side for fast parity tests (same generator, same parameters).
 
     plain      : 64^3 u8, 8 Gaussian blobs, unit cube, 256^2, step 0.5 voxel
+    plain_large: the same generator at 256^3 -> 1024^2
     extinction : 256^3 u16 4-octave value noise in 4 nested shells, SAT AO
                  (radii 2, 6, 16 voxels) + directional SAT cone shadow, 1024^2
     ground_truth / cone : 256^3 u8, 32 blobs + U[0,20] background; GT with 16
@@ -402,9 +403,9 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
                  ground-truth camera, light and integrator parameters, network
                  inputs on a 6-level pyramid of base n/2, 1024^2
     """
-    if name == "plain":
-        n = n or 64
-        image = image or 256
+    if name in ("plain", "plain_large"):
+        n = n or (64 if name == "plain" else 256)
+        image = image or (256 if name == "plain" else 1024)
         vol = synth_blobs(n, n, n, abi.CVR_U8, 8, seed=1000)
         sp = (1.0 / n,) * 3
         cam = camera(orbit_eye(3.0, 35.0, 25.0), fovy=30.0)
