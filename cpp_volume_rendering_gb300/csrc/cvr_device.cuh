@@ -191,6 +191,20 @@ __device__ __forceinline__ BoxAxis box_axis(float lo, float hi, int n) {
   return b;
 }
 
+// int64 -> float without the FP64 pipe (where the hardware converts 64-bit
+// integers, at the FP64 rate, which is low on this part): |v| split into
+// 23-bit chunks, each made exact as (2^23 + c) - 2^23 from its bit pattern,
+// recombined with two FMAs (at most one extra rounding step).
+__device__ __forceinline__ float ll_to_float(long long v) {
+  const unsigned long long s = (unsigned long long)(v >> 63);  // 0 or all ones
+  const unsigned long long a = ((unsigned long long)v ^ s) - s;
+  const float f0 = __uint_as_float(0x4B000000u | (unsigned)(a & 0x7FFFFFull)) - 8388608.0f;
+  const float f1 = __uint_as_float(0x4B000000u | (unsigned)((a >> 23) & 0x7FFFFFull)) - 8388608.0f;
+  const float f2 = __uint_as_float(0x4B000000u | (unsigned)(a >> 46)) - 8388608.0f;
+  const float f = fmaf(f2, 70368744177664.0f, fmaf(f1, 8388608.0f, f0));  // 2^46, 2^23
+  return __uint_as_float(__float_as_uint(f) | ((unsigned)s & 0x80000000u));
+}
+
 struct D3 { long long d[3]; };  // consecutive x-differences of one row
 __device__ __forceinline__ D3 row_diffs(const long long* row, const BoxAxis& X) {
   long long v0 = __ldg(row + X.s[0]), v1 = __ldg(row + X.s[1]);
@@ -220,7 +234,7 @@ __device__ __forceinline__ float weigh9(const D9& cur, const D9& prev, const Box
   for (int b = 0; b < 3; ++b) {
     float row = 0.0f;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) row = fmaf(X.w[a], float(cur.y[b].d[a] - prev.y[b].d[a]), row);
+    for (int a = 0; a < 3; ++a) row = fmaf(X.w[a], ll_to_float(cur.y[b].d[a] - prev.y[b].d[a]), row);
     acc = fmaf(Y.w[b], row, acc);
   }
   return acc;
