@@ -192,16 +192,13 @@ __device__ __forceinline__ BoxAxis box_axis(float lo, float hi, int n) {
 }
 
 // int64 -> float without the FP64 pipe (where the hardware converts 64-bit
-// integers, at the FP64 rate, which is low on this part): |v| split into
-// 23-bit chunks, each made exact as (2^23 + c) - 2^23 from its bit pattern,
-// recombined with two FMAs (at most one extra rounding step).
+// integers, at the FP64 rate, which is low on this part): |v| as two 32-bit
+// halves converted on the FP32 side, recombined by one FMA (at most one
+// rounding step more than a direct conversion), then the sign.
 __device__ __forceinline__ float ll_to_float(long long v) {
   const unsigned long long s = (unsigned long long)(v >> 63);  // 0 or all ones
   const unsigned long long a = ((unsigned long long)v ^ s) - s;
-  const float f0 = __uint_as_float(0x4B000000u | (unsigned)(a & 0x7FFFFFull)) - 8388608.0f;
-  const float f1 = __uint_as_float(0x4B000000u | (unsigned)((a >> 23) & 0x7FFFFFull)) - 8388608.0f;
-  const float f2 = __uint_as_float(0x4B000000u | (unsigned)(a >> 46)) - 8388608.0f;
-  const float f = fmaf(f2, 70368744177664.0f, fmaf(f1, 8388608.0f, f0));  // 2^46, 2^23
+  const float f = fmaf(__uint2float_rn((unsigned)(a >> 32)), 4294967296.0f, __uint2float_rn((unsigned)a));
   return __uint_as_float(__float_as_uint(f) | ((unsigned)s & 0x80000000u));
 }
 
