@@ -384,6 +384,29 @@ const void* RC1PConeLightGroundTruthSteps::Params(size_t* size) {
   return &m_p;
 }
 
+bool RC1PSurrogateShading::Init(int w, int h) {
+  if (!RC1PConeLightGroundTruthSteps::Init(w, h)) return false;
+  vr_built = false;
+  vis::StructuredGridVolume* v = m_ext_data_manager->GetCurrentStructuredVolume();
+  cvr_pyramid_params pp{};
+  pp.base_dims[0] = std::max(1, v->GetWidth() / 2);
+  pp.base_dims[1] = std::max(1, v->GetHeight() / 2);
+  pp.base_dims[2] = std::max(1, v->GetDepth() / 2);
+  pp.sigma0 = 1.0f;
+  pp.n_levels = CVR_SURROGATE_LEVELS;
+  if (!CheckABI(cvr_build_ext_pyramid(m_ctx, &pp), "Init: extinction pyramid")) return false;
+  if (!m_weights_path.empty()) {
+    if (!CheckABI(cvr_mlp_load(m_ctx, m_weights_path.c_str()), "Init: network checkpoint")) return false;
+  } else {
+    float probe = 0.0f;
+    if (cvr_mlp_get_params(m_ctx, &probe, 1) == CVR_ERR_NOT_READY)
+      return Fail("Init: no network (set m_weights_path to a cvr_mlp_save checkpoint)");
+  }
+  vr_built = true;
+  SetOutdated();
+  return true;
+}
+
 // ------------------------------------------------------------ manager
 RenderingManager::RenderingManager() {}
 RenderingManager::~RenderingManager() { m_renderers.clear(); }

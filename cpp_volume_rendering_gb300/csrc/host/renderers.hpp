@@ -250,6 +250,22 @@ class RC1PConeLightGroundTruthSteps : public BaseVolumeRenderer {
   cvr_gt_params m_p{};
 };
 
+// No reference counterpart: the ground-truth renderer with its light
+// integrals replaced by the learned network (CVR_METHOD_SURROGATE), same
+// parameters.  Init builds the 6-level pyramid of base n/2 the network's
+// inputs are defined on and loads the network from m_weights_path (a
+// cvr_mlp_save checkpoint) unless the context already holds one.
+class RC1PSurrogateShading : public RC1PConeLightGroundTruthSteps {
+ public:
+  const char* GetName() override { return "1-Pass - Learned Occlusion Surrogate"; }
+  const char* GetAbbreviationName() override { return "s_1psurr"; }
+  bool Init(int w, int h) override;
+  std::string m_weights_path;
+
+ protected:
+  int Method() const override { return CVR_METHOD_SURROGATE; }
+};
+
 // Headless RenderingManager (cppvolrend/renderingmanager.cpp:119-319): owns the
 // renderers, keeps the data / parameters, and runs the per-frame sequence
 // PrepareRender -> Redraw, with readback in place of the on-screen blit.

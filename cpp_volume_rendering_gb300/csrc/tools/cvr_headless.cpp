@@ -23,13 +23,13 @@ static int usage() {
   std::fprintf(stderr,
                "usage: cvr_headless --volume FILE --tf FILE --renderer ABBR [--width W --height H] [--frames N]\n"
                "       [--cameras FILE --camera-index I] [--lights FILE --light-index I] [--eye X Y Z]\n"
-               "       [--fovy DEG] [--occlusion 0|1] [--shadow 0|1] [--out FILE.pfm]\n"
-               "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt\n");
+               "       [--fovy DEG] [--occlusion 0|1] [--shadow 0|1] [--weights FILE] [--out FILE.pfm]\n"
+               "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt s_1psurr (needs --weights)\n");
   return 1;
 }
 
 int main(int argc, char** argv) {
-  std::string vol, tf, rend, out, cams, lights;
+  std::string vol, tf, rend, out, cams, lights, weights;
   int w = 768, h = 768, frames = 1, cam_i = 0, light_i = 0;
   bool have_eye = false;
   int occlusion = -1, shadow = -1;
@@ -42,6 +42,7 @@ int main(int argc, char** argv) {
     else if (a == "--tf" && (v = next())) tf = v;
     else if (a == "--renderer" && (v = next())) rend = v;
     else if (a == "--out" && (v = next())) out = v;
+    else if (a == "--weights" && (v = next())) weights = v;
     else if (a == "--width" && (v = next())) w = std::atoi(v);
     else if (a == "--height" && (v = next())) h = std::atoi(v);
     else if (a == "--frames" && (v = next())) frames = std::atoi(v);
@@ -66,6 +67,9 @@ int main(int argc, char** argv) {
   mgr.AddVolumeRenderer(new RC1PExtinctionBasedShading());
   mgr.AddVolumeRenderer(new RC1PConeTracingDirOcclusionShading());
   mgr.AddVolumeRenderer(new RC1PConeLightGroundTruthSteps());
+  RC1PSurrogateShading* surr = new RC1PSurrogateShading();  // no reference counterpart
+  surr->m_weights_path = weights;
+  mgr.AddVolumeRenderer(surr);
 
   std::string err;
   if (!mgr.data.ReadVolume(vol, &err) || !mgr.data.ReadTransferFunction(tf, &err)) {

@@ -75,3 +75,28 @@ def test_headless_frames(data, abbr, method, tmp_path):
     assert raw[:header_end].split()[:3] == [b"PF", b"40", b"32"]
     img = np.frombuffer(raw[header_end:], np.float32).reshape(32, 40, 3)
     assert np.isfinite(img).all() and img.max() > 0.0
+
+
+@pytest.mark.gpu
+def test_headless_surrogate_renderer(ctx, tmp_path):
+    """The surrogate plugin (no reference counterpart) loads a network
+    checkpoint and renders; without one it reports the missing network."""
+    vol = scene.synth_blobs(64, 64, 64, abi.CVR_U8, 16, seed=22, noise_max=20.0)
+    vp = tmp_path / "blobs.1.64x64x64.raw"
+    vol.tofile(vp)
+    tp = tmp_path / "ramp.tf1d"
+    tp.write_text("linear\n0\n4\n0.2 0.3 0.9 0\n0.3 0.8 0.4 80\n0.9 0.7 0.2 160\n1.0 0.95 0.9 255\n"
+                  "4\n0.0 0\n0.05 80\n0.4 160\n0.9 255\n")
+    ckpt = tmp_path / "net.cvrmlp"
+    ctx.mlp_init(9)
+    abi.check(ctx.lib.cvr_mlp_save(ctx.h, str(ckpt).encode()), ctx.h)
+    out = tmp_path / "surr.pfm"
+    r = run("--volume", vp, "--tf", tp, "--renderer", "s_1psurr", "--width", "48", "--height", "40",
+            "--occlusion", "1", "--shadow", "1", "--weights", ckpt, "--out", out)
+    assert r.returncode == 0, r.stderr
+    assert "renderer=s_1psurr" in r.stdout
+    raw = out.read_bytes()
+    img = np.frombuffer(raw[raw.index(b"-1.0\n") + 5:], np.float32).reshape(40, 48, 3)
+    assert np.isfinite(img).all() and img.max() > 0.0
+    r = run("--volume", vp, "--tf", tp, "--renderer", "s_1psurr", "--width", "16", "--height", "16")
+    assert r.returncode != 0 and "network" in (r.stdout + r.stderr)
