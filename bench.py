@@ -225,10 +225,10 @@ def run_reference(args):
     value = tot_n / tot_t / 1e6
     sample = f"rows {y0}..{y0 + rows} of the {wl.width}x{H} frame per step, FP32 oracle on {threads} threads"
     print(json.dumps({
-        "impl": "reference", "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD_DESC[args.workload]},
+        "config": {"workload": WORKLOAD_DESC[args.workload], "image": [wl.width, wl.height], "volume": list(wl.dims)},
         "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference renders with GLSL compute shaders (OpenGL); no graphics stack exists on this box, "
