@@ -164,6 +164,8 @@ SIGNATURES = {
     "cvr_batch_run": (_I, [_P]),
     "cvr_batch_job_stats": (_I, [_P, _I, C.POINTER(FrameStats)]),
     "cvr_batch_destroy": (None, [_P]),
+    "cvr_set_light_cache": (_I, [_P, _I, _I, _I]),
+    "cvr_download_light_cache": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_brick_size": (_I, [_P, _I]),
     "cvr_get_brick_size": (_I, [_P]),
     "cvr_set_sampling": (_I, [_P, _I]),

@@ -80,6 +80,8 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
                                                                               : true))
       return fail(c, CVR_ERR_INVALID_ARG, "cvr_batch_create: jobs must be extinction or surrogate with their params");
   }
+  if (c->lc_dims[0] > 0)
+    return fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: the light cache is per frame, not batched (turn it off)");
   CK(c, cudaSetDevice(c->device));
   CK(c, cudaStreamSynchronize(c->stream));
   std::unique_ptr<cvr_batch> b(new cvr_batch());

@@ -240,7 +240,7 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick};
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -503,7 +503,17 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
       const ShadowBoxTable* table = nullptr;
       cvr_status es = ext_args(c, p, light, f, &a, &table);
       if (es != CVR_OK) return es;
-      e = launch_extinction(f, a, table, c->stream);
+      if (c->lc_dims[0] > 0) {  // object-space light cache, then the object-space marcher
+        if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
+        const size_t cells = (size_t)c->lc_dims[0] * c->lc_dims[1] * c->lc_dims[2];
+        CK(c, ensure(c->d_lcache, c->lcache_cap, cells * sizeof(float2)));
+        e = launch_cache_extinction(f, a, table, *c->sdw_table, c->lc_dims, c->d_lcache, c->stream);
+        if (e == cudaSuccess)
+          e = launch_march_cached(f, c->d_lcache, c->lc_dims, p->apply_occlusion, p->apply_shadow, p->ka, p->kd,
+                                  c->stream);
+      } else {
+        e = launch_extinction(f, a, table, c->stream);
+      }
       break;
     }
     case CVR_METHOD_CONE_DOS: {
@@ -523,7 +533,16 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
       a.light_up = make3(light->up); a.light_right = make3(light->right);
       a.spot_cos_max = light->spot_cos_max;
       a.ka = p->ka; a.kd = p->kd;
-      e = launch_dos(f, a, c->stream);
+      if (c->lc_dims[0] > 0) {  // object-space light cache, then the object-space marcher
+        const size_t cells = (size_t)c->lc_dims[0] * c->lc_dims[1] * c->lc_dims[2];
+        CK(c, ensure(c->d_lcache, c->lcache_cap, cells * sizeof(float2)));
+        e = launch_cache_dos(f, a, c->lc_dims, c->d_lcache, c->stream);
+        if (e == cudaSuccess)
+          e = launch_march_cached(f, c->d_lcache, c->lc_dims, p->apply_occlusion, p->apply_shadow, p->ka, p->kd,
+                                  c->stream);
+      } else {
+        e = launch_dos(f, a, c->stream);
+      }
       break;
     }
     case CVR_METHOD_GROUND_TRUTH: {
@@ -615,6 +634,26 @@ cvr_status cvr_get_tuning(cvr_ctx* c, int* tile_w, int* tile_h, int* variant) {
   if (tile_w) *tile_w = c->tile_w;
   if (tile_h) *tile_h = c->tile_h;
   if (variant) *variant = c->variant;
+  return CVR_OK;
+}
+
+cvr_status cvr_set_light_cache(cvr_ctx* c, int w, int h, int d) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  const bool off = w == 0 && h == 0 && d == 0;
+  if (!off && (w < 1 || h < 1 || d < 1 || w > 1024 || h > 1024 || d > 1024))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_light_cache: dims must be 0,0,0 (off) or 1..1024 each");
+  c->lc_dims[0] = w; c->lc_dims[1] = h; c->lc_dims[2] = d;
+  return CVR_OK;
+}
+
+cvr_status cvr_download_light_cache(cvr_ctx* c, float* host, size_t n_floats) {
+  if (!c || !host) return CVR_ERR_INVALID_ARG;
+  const size_t cells = (size_t)c->lc_dims[0] * c->lc_dims[1] * c->lc_dims[2];
+  if (cells == 0 || !c->d_lcache) return fail(c, CVR_ERR_NOT_READY, "cvr_download_light_cache: no light cache");
+  if (n_floats != 2 * cells) return fail(c, CVR_ERR_INVALID_ARG, "cvr_download_light_cache: need 2 floats per cell");
+  CK(c, cudaSetDevice(c->device));
+  CK(c, cudaMemcpyAsync(host, c->d_lcache, cells * sizeof(float2), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
   return CVR_OK;
 }
 

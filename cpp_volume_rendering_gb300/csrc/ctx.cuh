@@ -187,6 +187,10 @@ struct cvr_ctx {
   void* d_vbrick = nullptr;
   size_t vbrick_cap = 0;
   int vbrick_bs = -1;                        // layout of d_vbrick's contents (-1: stale)
+  // object-space light cache (cvr_set_light_cache): 0 = off
+  int lc_dims[3] = {0, 0, 0};
+  float2* d_lcache = nullptr;
+  size_t lcache_cap = 0;
 };
 
 // Exchanges the current-volume fields of c with slot s.

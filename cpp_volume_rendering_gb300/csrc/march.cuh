@@ -120,6 +120,15 @@ struct BatchExtJob {
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
                                     int tf_n, int max_table, int tile_threads, int variant, cudaStream_t st);
 
+// Object-space light cache (lightcache.cu).  Cells of dims[0] x dims[1] x
+// dims[2], x fastest, float2 (occlusion, shadow).  table: the directional
+// shadow-box table or null (storage: any table object, passed when null).
+cudaError_t launch_cache_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
+                                    const ShadowBoxTable& storage, const int dims[3], float2* out, cudaStream_t st);
+cudaError_t launch_cache_dos(const FrameArgs& f, const DosArgs& d, const int dims[3], float2* out, cudaStream_t st);
+cudaError_t launch_march_cached(const FrameArgs& f, const float2* cache, const int dims[3], int apply_occ,
+                                int apply_sdw, float ka, float kd, cudaStream_t st);
+
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
 // table == nullptr: per-sample cone geometry (point lights, or too many boxes).
 cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st);

@@ -277,6 +277,17 @@ cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
  * or the size changed.  Results do not depend on it. */
 cvr_status cvr_set_brick_size(cvr_ctx* ctx, int edge);
 int cvr_get_brick_size(cvr_ctx* ctx);
+/* Object-space light cache (PreIlluminationStructuredVolume,
+ * cppvolrend/utils/preillumination.h:15-47; reference default 32^3, off):
+ * when on, CVR_METHOD_EXTINCTION and CVR_METHOD_CONE_DOS evaluate occlusion
+ * and shadow once per frame at the centres of a w x h x d grid
+ * (lightcachecomputation.comp of rc1pextbsd / rc1pdosct) and shade every
+ * sample from a trilinear lookup of it (obj_ray_marching.comp, which, like
+ * the reference, composites nothing when both terms are off).  0,0,0 = off.
+ * The cache is stored as FP32 pairs (the reference: RG16F). */
+cvr_status cvr_set_light_cache(cvr_ctx* ctx, int w, int h, int d);
+/* The last frame's cache: (occlusion, shadow) per cell, x fastest; synchronous. */
+cvr_status cvr_download_light_cache(cvr_ctx* ctx, float* host_out, size_t n_floats);
 /* Autotuner: renders the given frame with every tile shape x register variant
  * (reps timed frames each, CUDA events, L2 flushed before each), then every
  * brick size at the best of those; keeps the fastest configuration on the

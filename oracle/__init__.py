@@ -51,6 +51,7 @@ def load():
             "oracle_render": (I, [P, I, I, C.POINTER(abi.Camera), C.POINTER(abi.Light), P, I, I, I, I, P, P,
                                   C.POINTER(C.c_uint64), I]),
             "oracle_set_mlp": (I, [P, P, I]),
+            "oracle_set_light_cache": (I, [P, I, I, I]),
             "oracle_sur_features": (I, [P, I, C.POINTER(abi.Light), I, D, P, I, P, P]),
             "oracle_gt_points": (I, [P, C.POINTER(abi.Light), C.POINTER(abi.GtParams), P, I, P]),
         }
@@ -146,6 +147,9 @@ class Oracle:
         occ = np.ascontiguousarray(occ, np.float32)
         sdw = np.ascontiguousarray(sdw, np.float32)
         self._ck(self.lib.oracle_set_gt_kernels(self.h, _p(occ), len(occ), _p(sdw), len(sdw)))
+
+    def set_light_cache(self, w, h, d):
+        self._ck(self.lib.oracle_set_light_cache(self.h, w, h, d))
 
     def set_mlp(self, params):
         params = np.ascontiguousarray(params, np.float32)

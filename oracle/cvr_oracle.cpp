@@ -74,6 +74,7 @@ struct Scene {
   std::vector<float> occ_vec, sdw_vec;
   bool gt_ready = false;
   std::vector<float> mlp;  // surrogate network parameters (CVR_MLP_PARAMS floats)
+  int lc[3] = {0, 0, 0};   // object-space light cache dims (0: off)
 
   double vox_norm(size_t i) const {
     if (dtype == CVR_U8) return (double)vox[i] / 255.0;
@@ -610,7 +611,7 @@ inline void mlp_forward_bf16(const std::vector<float>& P, const double* x, doubl
 // ray_marching_1p.comp:160-247 and the identical loops of the other shaders.
 template <class T, class ShadeFn>
 void march_rows(const Scene& s, const cvr_camera& camc, T step, int W, int H, int y0, int y1, double* out,
-                uint32_t* counts, uint64_t* total, int threads, ShadeFn shade) {
+                uint32_t* counts, uint64_t* total, int threads, ShadeFn shade, bool gate = true) {
   Frame<T> f;
   f.s = &s;
   f.spacing = v3<T>(T(s.sx), T(s.sy), T(s.sz));
@@ -634,7 +635,7 @@ void march_rows(const Scene& s, const cvr_camera& camc, T step, int W, int H, in
           T dens = sample_volume(s, p);
           V4<T> src = tf_lookup<T>(s.rgbt, s.tf_n, dens);
           ++n;
-          if (src.a > T(0)) {
+          if (src.a > T(0) && gate) {
             src = shade(f, src, p, dir);
             src.a = T(1) - std::exp(-src.a * h);
             src.r *= src.a; src.g *= src.a; src.b *= src.a;
@@ -653,6 +654,46 @@ void march_rows(const Scene& s, const cvr_camera& camc, T step, int W, int H, in
     }
   }
   if (total) *total = acc;
+}
+
+// ------------------------------------------------------------ light cache
+// Object-space light cache: (occlusion, shadow) at the cell centres
+// tex_pos = (cell + 0.5) * (VolumeScales * (VolumeDimensions / LightCacheDimensions))
+// (rc1pextbsd/lightcachecomputation.comp:443-468, rc1pdosct/lightcachecomputation.comp:523-547).
+template <class T, class CellFn>
+std::vector<T> build_cache(const Scene& s, CellFn cell) {
+  const int* d = s.lc;
+  std::vector<T> c(2 * (size_t)d[0] * d[1] * d[2]);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int z = 0; z < d[2]; ++z)
+    for (int y = 0; y < d[1]; ++y)
+      for (int x = 0; x < d[0]; ++x) {
+        V3<T> tx = v3<T>((T(x) + T(0.5)) * (T(s.sx) * (T(s.nx) / T(d[0]))),
+                         (T(y) + T(0.5)) * (T(s.sy) * (T(s.ny) / T(d[1]))),
+                         (T(z) + T(0.5)) * (T(s.sz) * (T(s.nz) / T(d[2]))));
+        T io, is;
+        cell(tx, io, is);
+        size_t i = (size_t)x + (size_t)d[0] * ((size_t)y + (size_t)d[1] * z);
+        c[2 * i] = io;
+        c[2 * i + 1] = is;
+      }
+  return c;
+}
+// texture(TexVolumeLightCache, tx_pos / VolumeScaledSizes).rg
+template <class T> void cache_lookup(const Scene& s, const std::vector<T>& c, V3<T> grid, V3<T> tx, T& io, T& is) {
+  const int* d = s.lc;
+  Tap<T> a = axis_tap<T>(tx.x / grid.x * T(d[0]) - T(0.5), d[0]);
+  Tap<T> b = axis_tap<T>(tx.y / grid.y * T(d[1]) - T(0.5), d[1]);
+  Tap<T> g = axis_tap<T>(tx.z / grid.z * T(d[2]) - T(0.5), d[2]);
+  for (int ch = 0; ch < 2; ++ch) {
+    auto at = [&](int x, int y, int z) { return c[2 * ((size_t)x + (size_t)d[0] * ((size_t)y + (size_t)d[1] * z)) + ch]; };
+    T c00 = at(a.i0, b.i0, g.i0) + a.t * (at(a.i1, b.i0, g.i0) - at(a.i0, b.i0, g.i0));
+    T c10 = at(a.i0, b.i1, g.i0) + a.t * (at(a.i1, b.i1, g.i0) - at(a.i0, b.i1, g.i0));
+    T c01 = at(a.i0, b.i0, g.i1) + a.t * (at(a.i1, b.i0, g.i1) - at(a.i0, b.i0, g.i1));
+    T c11 = at(a.i0, b.i1, g.i1) + a.t * (at(a.i1, b.i1, g.i1) - at(a.i0, b.i1, g.i1));
+    T c0 = c00 + b.t * (c10 - c00), c1 = c01 + b.t * (c11 - c01);
+    (ch == 0 ? io : is) = c0 + g.t * (c1 - c0);
+  }
 }
 
 template <class T> V4<T> combine(V4<T> L, bool occ_on, T ka_in, T io, bool sdw_on, T kd_in, T is) {
@@ -686,6 +727,26 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
       if constexpr (sizeof(T) == 8) e.sat = s.sat64.data();
       else e.sat = s.sat32.data();
       e.sx = s.nx + 2; e.sy = s.ny + 2; e.sz = s.nz + 2;
+      if (s.lc[0] > 0) {
+        // obj_ray_marching.comp with the cache of lightcachecomputation.comp (rc1pextbsd)
+        Frame<T> fc;
+        fc.s = &s;
+        fc.spacing = v3<T>(T(s.sx), T(s.sy), T(s.sz));
+        fc.grid = v3<T>(T(s.nx * s.sx), T(s.ny * s.sy), T(s.nz * s.sz));
+        std::vector<T> cache = build_cache<T>(s, [&](V3<T> tx, T& io, T& is) {
+          io = p->apply_occlusion ? ext_ao(fc, e, tx) : T(1);
+          is = p->apply_shadow ? ext_shadow(fc, e, tx) : T(1);
+        });
+        march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
+                      [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
+                        T io, is;
+                        cache_lookup<T>(s, cache, f.grid, tx, io, is);
+                        return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd),
+                                       is);
+                      },
+                      p->apply_occlusion || p->apply_shadow);
+        return 0;
+      }
       march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
                     [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
                       T io = p->apply_occlusion ? ext_ao(f, e, tx) : T(0);
@@ -704,6 +765,49 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
       d.light_pos = from<T>(light.position); d.light_fwd = from<T>(light.forward);
       d.light_up = from<T>(light.up); d.light_right = from<T>(light.right);
       d.spot_cos = T(light.spot_cos_max);
+      // ShadowEvaluationKernel (:533-562); Cone1RayShadow's (k, v, u)
+      // parameter order swaps u and v.
+      auto dos_shadow = [&](const Frame<T>& f, V3<T> tx) -> T {
+        V3<T> k, u, v;
+        if (p->shadow_type == 0 || p->shadow_type == 1) {
+          k = normalize(d.light_pos - (tx - f.grid * T(0.5)));
+          u = normalize(cross(k, d.light_right));
+          v = normalize(cross(k, u));
+          if (p->shadow_type == 1 && dot(k, d.light_fwd) < d.spot_cos) return T(0);
+        } else {
+          k = d.light_fwd; v = d.light_up; u = d.light_right;
+        }
+        return cone_integrate(f, d, s.sdw, tx, k, v, u);
+      };
+      if (s.lc[0] > 0) {
+        // obj_ray_marching.comp with the cache of lightcachecomputation.comp (rc1pdosct): the
+        // occlusion cone's frame comes from the camera's up vector (:280-292)
+        Frame<T> fc;
+        fc.s = &s;
+        fc.spacing = v3<T>(T(s.sx), T(s.sy), T(s.sz));
+        fc.grid = v3<T>(T(s.nx * s.sx), T(s.ny * s.sy), T(s.nz * s.sz));
+        fc.cam = make_cam<T>(cam, W, H);
+        std::vector<T> cache = build_cache<T>(s, [&](V3<T> tx, T& io, T& is) {
+          io = T(1);
+          is = T(1);
+          if (p->apply_occlusion) {
+            V3<T> k = normalize(fc.cam.eye - (tx - fc.grid * T(0.5)));
+            V3<T> v_right = normalize(cross(-k, fc.cam.u));
+            V3<T> v_up = normalize(cross(k, v_right));
+            io = cone_integrate(fc, d, s.occ, tx, k, v_up, v_right);
+          }
+          if (p->apply_shadow) is = dos_shadow(fc, tx);
+        });
+        march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
+                      [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
+                        T io, is;
+                        cache_lookup<T>(s, cache, f.grid, tx, io, is);
+                        return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd),
+                                       is);
+                      },
+                      p->apply_occlusion || p->apply_shadow);
+        return 0;
+      }
       march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
                     [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T> dir) {
                       T io = 0, is = 0;
@@ -971,6 +1075,13 @@ int oracle_set_gt_kernels(void* h, const float* occ, int n_occ, const float* sdw
   s.occ_vec.assign(occ, occ + 3 * (size_t)n_occ);
   s.sdw_vec.assign(sdw, sdw + 3 * (size_t)n_sdw);
   s.gt_ready = true;
+  return 0;
+}
+
+int oracle_set_light_cache(void* h, int w, int hh, int d) {
+  Scene& s = *(Scene*)h;
+  if (w < 0 || hh < 0 || d < 0) return CVR_ERR_INVALID_ARG;
+  s.lc[0] = w; s.lc[1] = hh; s.lc[2] = d;
   return 0;
 }
 
