@@ -43,6 +43,8 @@ WORKLOAD_DESC = {
                   "directional SAT cone shadow, step 0.5 voxel",
     "plain": "plain ray casting: 64^3 u8 8-blob volume, unit cube -> 256^2, step 0.5 voxel",
     "plain_large": "plain ray casting: 256^3 u8 8-blob volume, unit cube -> 1024^2, step 0.5 voxel",
+    "extinction_lightcache": "extinction shading with the 32^3 object-space light cache: 256^3 u16 value-noise "
+                             "shells -> 1024^2, AO radii {2,6,16} + directional SAT cone shadow per cache cell",
     "cone": "cone DOS shading: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 5-level extinction pyramid, "
             "occlusion + point-light shadow cones",
     "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
@@ -526,11 +528,13 @@ def run_ours(args):
         reset_tuning()
         # every renderer tuned on its own frame (tile x registers x brick), with
         # FP32 volume samples and with the texture-unit variant
-        for name in ("plain", "plain_large", "cone", "ground_truth"):
+        for name in ("plain", "plain_large", "cone", "ground_truth", "extinction_lightcache"):
             if name == args.workload:
                 continue
-            w2 = scene.workload(name)
+            w2 = scene.workload("extinction" if name == "extinction_lightcache" else name)
             scene.prepare(ctx, w2)
+            abi.check(lib.cvr_set_light_cache(ctx.h, *((32, 32, 32) if name == "extinction_lightcache" else (0, 0, 0))),
+                      ctx.h)
             o2 = C.POINTER(C.c_float)()
             abi.check(lib.cvr_get_frame_buffer(ctx.h, w2.width, w2.height, C.byref(o2)), ctx.h)
             entry = {"workload": WORKLOAD_DESC[name]}
@@ -552,6 +556,7 @@ def run_ours(args):
                               key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
                                                "brick": lib.cvr_get_brick_size(ctx.h)}})
             ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+            abi.check(lib.cvr_set_light_cache(ctx.h, 0, 0, 0), ctx.h)
             renderers[name] = entry
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
