@@ -258,6 +258,104 @@ def time_frames(ctx, lib, wl, params, out_ptr, steps, warmup, flush=True):
     return times
 
 
+def tuned_frames(ctx, lib, w2):
+    """One prepared frame autotuned (tile x registers x brick) and timed with
+    FP32 volume samples and with the texture-unit variant."""
+    import ctypes as C
+    from cpp_volume_rendering_gb300 import abi
+    o2 = C.POINTER(C.c_float)()
+    abi.check(lib.cvr_get_frame_buffer(ctx.h, w2.width, w2.height, C.byref(o2)), ctx.h)
+    entry = {}
+    for key, flags in (("", abi.SAMPLING_TEX_FEATURES),
+                       ("tex_", abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)):
+        ctx.set_sampling(flags)
+        tw, th, tv = C.c_int(), C.c_int(), C.c_int()
+        abi.check(lib.cvr_autotune(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
+                                   C.sizeof(w2.params), w2.width, w2.height, 1, C.byref(tw), C.byref(th),
+                                   C.byref(tv), None), ctx.h)
+        s2 = abi.FrameStats()
+        abi.check(lib.cvr_render(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
+                                 C.sizeof(w2.params), C.cast(o2, C.c_void_p), w2.width, w2.height, None,
+                                 C.byref(s2)), ctx.h)
+        tt = time_frames(ctx, lib, w2, w2.params, C.cast(o2, C.c_void_p), 3, 1)
+        m = statistics.median(tt)
+        entry.update({key + "ms": m, key + "fps": 1000.0 / m, key + "msamples_s": s2.samples / (m / 1000.0) / 1e6,
+                      key + "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9,
+                      key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
+                                       "brick": lib.cvr_get_brick_size(ctx.h)}})
+    ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+    return entry
+
+
+def gradient_section(ctx, lib, args, log=print):
+    """Gradient Blinn-Phong: the device gradient builders (HBM-bound: each
+    voxel read once from L1/L2-cached neighbourhoods, 8 bytes written) against
+    the measured copy bandwidth and the FP64 CPU restatement of the
+    reference's builders, then shaded frames of the plain and extinction
+    workloads with the finite-difference gradient and the reference's default
+    Blinn-Phong terms (ka 0.5, kd 0.5, ks 0.8, shininess 30)."""
+    import ctypes as C
+
+    import numpy as np
+
+    import oracle
+    from cpp_volume_rendering_gb300 import abi, scene
+    peak, peak_src = measured_peak_hbm()
+    out = {"build": {}, "frames": {}}
+    vols = {"512^3 u8 blobs": scene.synth_blobs(512, 512, 512, abi.CVR_U8, 32, seed=4020, noise_max=20.0),
+            "256^3 u16 value noise": scene.synth_value_noise(256, 256, 256, abi.CVR_U16, seed=2000)}
+    ms = C.c_float()
+    for vname, vol in vols.items():
+        ctx.set_volume(vol, (1.0, 1.0, 1.0))
+        nvox = vol.size
+        for mname, model in (("finite_differences", abi.GRADIENT_FINITE_DIFFERENCES),
+                             ("sobel_feldman", abi.GRADIENT_SOBEL_FELDMAN)):
+            gp = abi.GradientParams(model, 1, 0, 1)
+            for _ in range(2):
+                abi.check(lib.cvr_build_gradient(ctx.h, C.byref(gp)), ctx.h)
+            times = []
+            for _ in range(5):
+                abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+                abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+                abi.check(lib.cvr_build_gradient(ctx.h, C.byref(gp)), ctx.h)
+                abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+                times.append(ms.value)
+            m = statistics.median(times)
+            algo = nvox * (vol.itemsize + 8)
+            out["build"][f"{vname} {mname}"] = {
+                "ms": m, "gvoxels_s": nvox / (m / 1000.0) / 1e9,
+                "roofline": {"bound": "hbm", "achieved": algo / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": algo / (m / 1000.0) / 1e9 / peak, "peak_source": peak_src,
+                             "algorithmic_bytes": algo}}
+    # CPU: the FP64 restatement of GenerateGradientTexture (the reference's own
+    # loop, single-threaded like it) on a 128^3 sample of the u8 volume
+    sample = np.ascontiguousarray(vols["512^3 u8 blobs"][192:320, 192:320, 192:320])
+    orc = oracle.Oracle()
+    orc.set_volume(sample, (1.0, 1.0, 1.0))
+    t0 = time.perf_counter()
+    orc.build_gradient(abi.GRADIENT_FINITE_DIFFERENCES)
+    dt = time.perf_counter() - t0
+    out["build"]["cpu_baseline"] = {"value": sample.size / dt / 1e9, "unit": "Gvoxels/s", "cores": 1, "kind": "port",
+                                    "sample": f"finite differences on a 128^3 crop of the 512^3 u8 volume, FP64, "
+                                              f"{dt:.2f} s"}
+    ctx.build_gradient(abi.GRADIENT_NONE)
+    for name in ("plain_large", "extinction"):
+        w2 = scene.workload(name)
+        if name == "plain_large":
+            w2.light = scene.light(abi.LIGHT_POINT, position=(1.5, 2.5, 1.0))
+        scene.prepare(ctx, w2)
+        ctx.build_gradient(abi.GRADIENT_FINITE_DIFFERENCES)
+        ctx.set_blinn_phong(True)
+        try:
+            out["frames"][name] = {"workload": WORKLOAD_DESC[name] + ", gradient Blinn-Phong (finite differences)",
+                                   **tuned_frames(ctx, lib, w2)}
+        finally:
+            ctx.set_blinn_phong(False)
+            ctx.build_gradient(abi.GRADIENT_NONE)
+        log(f"gradient frame {name}: {out['frames'][name]['ms']:.3f} ms")
+    return out
+
+
 def measured_peak_bf16():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -515,6 +613,7 @@ def run_ours(args):
                        "cvr_render_host readback"}
     renderers = {}
     batch = None
+    gradient = None
     if not args.quick:
         def reset_tuning():
             ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
@@ -535,29 +634,12 @@ def run_ours(args):
             scene.prepare(ctx, w2)
             abi.check(lib.cvr_set_light_cache(ctx.h, *((32, 32, 32) if name == "extinction_lightcache" else (0, 0, 0))),
                       ctx.h)
-            o2 = C.POINTER(C.c_float)()
-            abi.check(lib.cvr_get_frame_buffer(ctx.h, w2.width, w2.height, C.byref(o2)), ctx.h)
-            entry = {"workload": WORKLOAD_DESC[name]}
-            for key, flags in (("", abi.SAMPLING_TEX_FEATURES),
-                               ("tex_", abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)):
-                ctx.set_sampling(flags)
-                tw, th, tv = C.c_int(), C.c_int(), C.c_int()
-                abi.check(lib.cvr_autotune(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
-                                           C.sizeof(w2.params), w2.width, w2.height, 1, C.byref(tw), C.byref(th),
-                                           C.byref(tv), None), ctx.h)
-                s2 = abi.FrameStats()
-                abi.check(lib.cvr_render(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),
-                                         C.sizeof(w2.params), C.cast(o2, C.c_void_p), w2.width, w2.height, None,
-                                         C.byref(s2)), ctx.h)
-                tt = time_frames(ctx, lib, w2, w2.params, C.cast(o2, C.c_void_p), 3, 1)
-                m = statistics.median(tt)
-                entry.update({key + "ms": m, key + "fps": 1000.0 / m, key + "msamples_s": s2.samples / (m / 1000.0) / 1e6,
-                              key + "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9,
-                              key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
-                                               "brick": lib.cvr_get_brick_size(ctx.h)}})
-            ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
+            renderers[name] = {"workload": WORKLOAD_DESC[name], **tuned_frames(ctx, lib, w2)}
             abi.check(lib.cvr_set_light_cache(ctx.h, 0, 0, 0), ctx.h)
-            renderers[name] = entry
+        reset_tuning()
+        if not args.no_gradient:
+            gradient = gradient_section(ctx, lib, args)
+        reset_tuning()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, target_s=args.cpu_seconds)
@@ -574,7 +656,8 @@ def run_ours(args):
         "fps": 1000.0 / ms_per_step,
         "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-        "clocks": clocks, "renderers": renderers, "surrogate": surrogate, "batch": batch}))
+        "clocks": clocks, "renderers": renderers, "surrogate": surrogate, "batch": batch,
+        "gradient": gradient}))
 
 
 def main():
@@ -589,6 +672,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the surrogate")
     ap.add_argument("--surrogate-points", type=int, default=4_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
+    ap.add_argument("--no-gradient", action="store_true", help="skip the gradient Blinn-Phong section")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--size", type=int, default=None, help="volume side override (profiling / small cases)")
     ap.add_argument("--image", type=int, default=None, help="image side override (profiling / small cases)")

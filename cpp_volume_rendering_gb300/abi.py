@@ -40,6 +40,7 @@ SAMPLING_TEX_VOLUME = 2
 MLP_NOALLOC_MAX_POINTS = 8192
 MAX_VOLUMES = 16
 MAX_CONE_SECTIONS = 512
+GRADIENT_SOBEL_FELDMAN, GRADIENT_FINITE_DIFFERENCES, GRADIENT_COMPUTE_SOBEL, GRADIENT_NONE = 0, 1, 2, 3
 
 F3 = C.c_float * 3
 
@@ -89,6 +90,15 @@ class PyramidParams(C.Structure):
 class FrameStats(C.Structure):
     _fields_ = [("samples", C.c_uint64), ("shaded_samples", C.c_uint64), ("aux_fetches", C.c_uint64),
                 ("kernel_ms", C.c_float)]
+
+
+class GradientParams(C.Structure):
+    _fields_ = [("model", C.c_int), ("sample_size", C.c_int), ("filter_nxnxn", C.c_int), ("normalized", C.c_int)]
+
+
+class BlinnPhong(C.Structure):
+    _fields_ = [("apply", C.c_int), ("ka", C.c_float), ("kd", C.c_float), ("ks", C.c_float),
+                ("shininess", C.c_float), ("specular", F3)]
 
 
 class Job(C.Structure):
@@ -168,6 +178,10 @@ SIGNATURES = {
     "cvr_download_light_cache": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_brick_size": (_I, [_P, _I]),
     "cvr_get_brick_size": (_I, [_P]),
+    "cvr_build_gradient": (_I, [_P, C.POINTER(GradientParams)]),
+    "cvr_download_gradient": (_I, [_P, _FP, C.c_size_t]),
+    "cvr_set_blinn_phong": (_I, [_P, C.POINTER(BlinnPhong)]),
+    "cvr_get_blinn_phong": (_I, [_P, C.POINTER(BlinnPhong)]),
     "cvr_set_sampling": (_I, [_P, _I]),
     "cvr_get_sampling": (_I, [_P]),
     "cvr_mlp_save": (_I, [_P, C.c_char_p]),

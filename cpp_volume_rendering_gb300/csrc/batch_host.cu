@@ -106,6 +106,8 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
     FrameArgs f;
     st = frame_args(c, &j.camera, j.params, j.out_rgba_dev, j.width, j.height, &f);
     if (st != CVR_OK) break;
+    st = grad_args(c, j.method, &j.light, &f);
+    if (st != CVR_OK) break;
     f.stats = b->d_stats + 3 * (size_t)i;
     if (j.method == CVR_METHOD_EXTINCTION) {
       BatchExtJob J{};

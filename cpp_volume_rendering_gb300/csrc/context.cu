@@ -19,8 +19,6 @@ thread_local std::string cvr::ctxutil::g_create_err;
 
 namespace {
 
-bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
-
 // The boxes ConeZAxis / ConeYAxis / ConeXAxis (ebs_ray_bbox_marching.comp:190-430)
 // walk for a fixed cone direction, evaluated once per frame in double
 // precision.  Returns false when the walk has more boxes than the table holds
@@ -151,6 +149,7 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
   f.out = reinterpret_cast<float4*>(out);
   f.counts = nullptr;
   f.stats = c->d_stats;
+  f.grad = GradView{};
   f.step = *static_cast<const float*>(params);  // every params struct starts with step_size
   if (c->tf_n * sizeof(float4) > 48 * 1024) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: TF larger than 3072 entries");
   // Steps below 1e-6 of the diagonal would not advance a single-precision
@@ -240,7 +239,7 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache};
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -278,6 +277,8 @@ static cvr_status set_volume_common(cvr_ctx* c, const void* src, bool src_device
   c->tex.vol_valid = false;
   c->tex.pyr_valid = false;
   c->vbrick_bs = -1;
+  c->grad_ready = false;  // rebuilt with the slot's gradient model on the next shaded frame
+  c->tex.grad_valid = false;
   return CVR_OK;
 }
 
@@ -481,6 +482,8 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
   cvr_status fs = frame_args(c, cam, params, out, w, h, &f);
   if (fs != CVR_OK) return fs;
   f.counts = counts;
+  fs = grad_args(c, method, light, &f);
+  if (fs != CVR_OK) return fs;
   CK(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
   cvr_light dl{};
   if (!light) { light = &dl; }

@@ -70,9 +70,12 @@ struct TexState {
   TexImage pyr[CVR_MAX_LEVELS];
   int n_pyr = 0;
   bool pyr_valid = false;
+  TexImage grad;
+  bool grad_valid = false;
   ~TexState() {
     vol.release();
     for (auto& t : pyr) t.release();
+    grad.release();
   }
 };
 
@@ -82,6 +85,8 @@ inline void swap_tex(TexState& a, TexState& b) {
   for (int l = 0; l < CVR_MAX_LEVELS; ++l) std::swap(a.pyr[l], b.pyr[l]);
   std::swap(a.n_pyr, b.n_pyr);
   std::swap(a.pyr_valid, b.pyr_valid);
+  std::swap(a.grad, b.grad);
+  std::swap(a.grad_valid, b.grad_valid);
 }
 
 // A resident volume that is not the current one (cvr_select_volume): the
@@ -106,8 +111,12 @@ struct VolSlot {
   void* d_vbrick = nullptr;
   size_t vbrick_cap = 0;
   int vbrick_bs = -1;
+  uint2* d_grad = nullptr;
+  size_t grad_cap = 0;
+  bool grad_ready = false;
+  cvr_gradient_params grad_params{CVR_GRADIENT_NONE, 1, 0, 1};
   ~VolSlot() {
-    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick};
+    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick, d_grad};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }
@@ -191,6 +200,13 @@ struct cvr_ctx {
   int lc_dims[3] = {0, 0, 0};
   float2* d_lcache = nullptr;
   size_t lcache_cap = 0;
+  // per-voxel gradient of the current volume (cvr_build_gradient) and the
+  // Blinn-Phong settings of cvr_set_blinn_phong (context-wide)
+  uint2* d_grad = nullptr;
+  size_t grad_cap = 0;
+  bool grad_ready = false;
+  cvr_gradient_params grad_params{CVR_GRADIENT_NONE, 1, 0, 1};
+  cvr_blinn_phong bp{0, 0.5f, 0.5f, 0.8f, 30.0f, {1.0f, 1.0f, 1.0f}};
 };
 
 // Exchanges the current-volume fields of c with slot s.
@@ -214,12 +230,18 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->d_vbrick, s.d_vbrick);
   std::swap(c->vbrick_cap, s.vbrick_cap);
   std::swap(c->vbrick_bs, s.vbrick_bs);
+  std::swap(c->d_grad, s.d_grad);
+  std::swap(c->grad_cap, s.grad_cap);
+  std::swap(c->grad_ready, s.grad_ready);
+  std::swap(c->grad_params, s.grad_params);
 }
 
 namespace cvr {
 namespace ctxutil {
 
 extern thread_local std::string g_create_err;
+
+inline bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
 inline cvr_status fail(cvr_ctx* c, cvr_status code, const std::string& msg) {
   if (c) c->err = msg;
@@ -294,6 +316,10 @@ cvr_status mlp_check_err(cvr_ctx* c);
 // Texture objects of the volume / pyramid levels, (re)made when stale.
 cvr_status ensure_volume_texture(cvr_ctx* c);
 cvr_status ensure_pyramid_textures(cvr_ctx* c);
+cvr_status ensure_gradient_texture(cvr_ctx* c);
+// Gradient shading of a frame of 'method' (f->grad; off unless cvr_set_blinn_phong
+// applies it and the volume has a gradient model, built here when stale).
+cvr_status grad_args(cvr_ctx* c, int method, const cvr_light* light, FrameArgs* f);
 // The volume as the marchers read it: the plain layout, or the bricked copy
 // of the context's brick size (made on first use after the volume changed).
 cvr_status render_volume_view(cvr_ctx* c, VolumeView* v);

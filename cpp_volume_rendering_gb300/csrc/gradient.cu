@@ -1,0 +1,216 @@
+// gradient.cu — per-voxel gradients for gradient Blinn-Phong shading
+// (DataManager::GenerateStructuredGradientTexture,
+// libs/volvis_utils/datamanager.cpp:332-352) built on the device, and the
+// per-frame gradient-shading arguments of the marchers.
+//
+// The reference computes the gradient on the host in double precision
+// (utils.cpp:146-351) and uploads it as RGB16F; here one thread per voxel
+// forms the same stencils from the integer voxel values (exact), scales once
+// in FP32 and stores four FP16 values (x, y, z, 0: one 8-byte load per tap).
+#include <cuda_fp16.h>
+
+#include "ctx.cuh"
+
+using namespace cvr::ctxutil;
+
+namespace {
+
+// GetNormalizedSample's integer numerator: the voxel, 0 outside the grid
+// (structuredgridvolume.cpp:121-128).
+template <class T>
+__device__ __forceinline__ int vox(const T* __restrict__ v, int nx, int ny, int nz, int x, int y, int z) {
+  if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) return 0;
+  return (int)__ldg(v + (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z));
+}
+
+struct GradBuild {
+  int model, n, filter, normalized;
+  float inv_max;  // 1/255 or 1/65535
+};
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gradient(const T* __restrict__ v, int nx, int ny, int nz, GradBuild b,
+                                                  uint2* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z * blockDim.z + threadIdx.z;
+  if (x >= nx || y >= ny || z >= nz) return;
+  float gx, gy, gz;
+  if (b.model == CVR_GRADIENT_FINITE_DIFFERENCES) {
+    // GenerateGradientTexture step 1 (utils.cpp:156-193): s2 - s1 over +-n.
+    const int n = b.n;
+    const float dx = float(vox(v, nx, ny, nz, x + n, y, z) - vox(v, nx, ny, nz, x - n, y, z));
+    const float dy = float(vox(v, nx, ny, nz, x, y + n, z) - vox(v, nx, ny, nz, x, y - n, z));
+    const float dz = float(vox(v, nx, ny, nz, x, y, z + n) - vox(v, nx, ny, nz, x, y, z - n));
+    if (b.normalized) {
+      // normalize(s2 - s1) is normalize of the integer differences (the common
+      // 1/255 scale cancels); the zero vector gives NaN there, then 0.
+      const float l2 = dx * dx + dy * dy + dz * dz;
+      if (l2 > 0.0f) {
+        const float l = sqrtf(l2);
+        gx = dx / l; gy = dy / l; gz = dz / l;
+      } else {
+        gx = gy = gz = 0.0f;
+      }
+    } else {
+      // s2s1 / 2.0f * (float)gradient_sample_size
+      const float k = b.inv_max * 0.5f * float(n);
+      gx = dx * k; gy = dy * k; gz = dz * k;
+    }
+    if (b.filter > 0 && gx != 0.0f && gy != 0.0f && gz != 0.0f) {
+      // Step 2 (utils.cpp:196-233) sums gradients[x, y, z] -- the centre, not
+      // the neighbour -- over the in-bounds window and divides by the count,
+      // so the average is the centre itself; it is then normalised when no
+      // component is zero.
+      const float l = sqrtf(gx * gx + gy * gy + gz * gz);
+      gx /= l; gy /= l; gz /= l;
+    }
+  } else {
+    // Sobel-Feldman (utils.cpp:295-321, sobelfeldman_generator.comp:37-60):
+    // weights 4 / 2^(|v1|+|v2|) on the planes at -1 minus those at +1.
+    int sx = 0, sy = 0, sz = 0;
+#pragma unroll
+    for (int v1 = -1; v1 <= 1; ++v1) {
+#pragma unroll
+      for (int v2 = -1; v2 <= 1; ++v2) {
+        const int w = 4 >> ((v1 < 0 ? -v1 : v1) + (v2 < 0 ? -v2 : v2));
+        sz += w * (vox(v, nx, ny, nz, x + v1, y + v2, z - 1) - vox(v, nx, ny, nz, x + v1, y + v2, z + 1));
+        sy += w * (vox(v, nx, ny, nz, x + v1, y - 1, z + v2) - vox(v, nx, ny, nz, x + v1, y + 1, z + v2));
+        sx += w * (vox(v, nx, ny, nz, x - 1, y + v2, z + v1) - vox(v, nx, ny, nz, x + 1, y + v2, z + v1));
+      }
+    }
+    gx = float(sx) * b.inv_max; gy = float(sy) * b.inv_max; gz = float(sz) * b.inv_max;
+  }
+  const __half2 xy = __floats2half2_rn(gx, gy);
+  const __half2 zw = __floats2half2_rn(gz, 0.0f);
+  uint2 o;
+  o.x = *reinterpret_cast<const unsigned int*>(&xy);
+  o.y = *reinterpret_cast<const unsigned int*>(&zw);
+  out[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)] = o;
+}
+
+__global__ void k_gradient_to_float(const uint2* __restrict__ g, float* __restrict__ out, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint2 q = g[i];
+  const float2 xy = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+  const float2 zw = __half22float2(*reinterpret_cast<const __half2*>(&q.y));
+  out[3 * i] = xy.x;
+  out[3 * i + 1] = xy.y;
+  out[3 * i + 2] = zw.x;
+}
+
+cvr_status check_gradient_params(cvr_ctx* c, const cvr_gradient_params& p) {
+  if (p.model < 0 || p.model > CVR_GRADIENT_NONE) return fail(c, CVR_ERR_INVALID_ARG, "gradient: unknown model");
+  if (p.model == CVR_GRADIENT_FINITE_DIFFERENCES && (p.sample_size < 1 || p.sample_size > 32768 || p.filter_nxnxn < 0))
+    return fail(c, CVR_ERR_INVALID_ARG, "gradient: sample_size must be in [1, 32768], filter_nxnxn >= 0");
+  return CVR_OK;
+}
+
+// Builds the current volume's gradient with c->grad_params.
+cvr_status build_gradient(cvr_ctx* c) {
+  const cvr_gradient_params& p = c->grad_params;
+  const size_t n = (size_t)c->nx * c->ny * c->nz;
+  CK(c, ensure(c->d_grad, c->grad_cap, n * sizeof(uint2)));
+  GradBuild b{p.model, p.sample_size, p.filter_nxnxn, p.normalized, c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f};
+  const dim3 block(32, 4, 2);
+  const dim3 grid((c->nx + 31) / 32, (c->ny + 3) / 4, (c->nz + 1) / 2);
+  if (c->dtype == CVR_U8)
+    k_gradient<uint8_t><<<grid, block, 0, c->stream>>>(static_cast<const uint8_t*>(c->d_vol), c->nx, c->ny, c->nz, b,
+                                                       c->d_grad);
+  else
+    k_gradient<uint16_t><<<grid, block, 0, c->stream>>>(static_cast<const uint16_t*>(c->d_vol), c->nx, c->ny, c->nz,
+                                                        b, c->d_grad);
+  CK(c, cudaGetLastError());
+  c->grad_ready = true;
+  c->tex.grad_valid = false;
+  return CVR_OK;
+}
+
+}  // namespace
+
+namespace cvr {
+namespace ctxutil {
+
+cvr_status grad_args(cvr_ctx* c, int method, const cvr_light* light, FrameArgs* f) {
+  f->grad = GradView{};
+  if (!c->bp.apply || c->grad_params.model == CVR_GRADIENT_NONE) return CVR_OK;
+  if (!light) return fail(c, CVR_ERR_INVALID_ARG, "gradient shading needs a light (its position)");
+  if (!finite3(light->position)) return fail(c, CVR_ERR_INVALID_ARG, "gradient shading: non-finite light position");
+  if (!c->grad_ready) {
+    cvr_status s = build_gradient(c);
+    if (s != CVR_OK) return s;
+  }
+  GradView& g = f->grad;
+  g.g = c->d_grad;
+  g.tex = 0;
+  if (c->sampling & CVR_SAMPLING_TEX_VOLUME) {
+    cvr_status s = ensure_gradient_texture(c);
+    if (s != CVR_OK) return s;
+    g.tex = c->tex.grad.tex;
+  }
+  g.nx = c->nx; g.ny = c->ny; g.nz = c->nz;
+  g.inv_grid = f->vol.inv_grid;
+  g.inv_spacing = f->vol.inv_spacing;
+  g.light_pos = make3(light->position);
+  // the ground truth's (and so the surrogate's) specular colour is vec3(1)
+  // (gt_ray_marching.comp:293-294)
+  const bool unit = method == CVR_METHOD_GROUND_TRUTH || method == CVR_METHOD_SURROGATE;
+  g.ispec = unit ? f3(1.0f, 1.0f, 1.0f) : make3(c->bp.specular);
+  g.ka = c->bp.ka; g.kd = c->bp.kd;
+  g.ks = c->bp.ks; g.shininess = c->bp.shininess;
+  return CVR_OK;
+}
+
+}  // namespace ctxutil
+}  // namespace cvr
+
+extern "C" {
+
+cvr_status cvr_build_gradient(cvr_ctx* c, const cvr_gradient_params* p) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  cvr_gradient_params q = p ? *p : cvr_gradient_params{CVR_GRADIENT_NONE, 1, 0, 1};
+  cvr_status s = check_gradient_params(c, q);
+  if (s != CVR_OK) return s;
+  CK(c, cudaSetDevice(c->device));
+  c->grad_params = q;
+  c->grad_ready = false;
+  c->tex.grad_valid = false;
+  if (q.model == CVR_GRADIENT_NONE) return CVR_OK;
+  if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_build_gradient: no volume");
+  return build_gradient(c);
+}
+
+cvr_status cvr_download_gradient(cvr_ctx* c, float* host, size_t n_floats) {
+  if (!c || !host) return CVR_ERR_INVALID_ARG;
+  if (!c->grad_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_download_gradient: no gradient built");
+  const long long n = (long long)c->nx * c->ny * c->nz;
+  if (n_floats < 3 * (size_t)n) return fail(c, CVR_ERR_INVALID_ARG, "cvr_download_gradient: buffer too small");
+  CK(c, cudaSetDevice(c->device));
+  float* tmp = nullptr;
+  CK(c, cudaMalloc((void**)&tmp, sizeof(float) * 3 * (size_t)n));
+  k_gradient_to_float<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_grad, tmp, n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, tmp, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return cuda_fail(c, e, "cvr_download_gradient");
+  return CVR_OK;
+}
+
+cvr_status cvr_set_blinn_phong(cvr_ctx* c, const cvr_blinn_phong* bp) {
+  if (!c || !bp) return CVR_ERR_INVALID_ARG;
+  const float v[] = {bp->ka, bp->kd, bp->ks, bp->shininess, bp->specular[0], bp->specular[1], bp->specular[2]};
+  for (float x : v)
+    if (!std::isfinite(x)) return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_blinn_phong: non-finite value");
+  c->bp = *bp;
+  return CVR_OK;
+}
+
+cvr_status cvr_get_blinn_phong(cvr_ctx* c, cvr_blinn_phong* out) {
+  if (!c || !out) return CVR_ERR_INVALID_ARG;
+  *out = c->bp;
+  return CVR_OK;
+}
+
+}  // extern "C"

@@ -29,6 +29,10 @@ void RenderingParameters::LightForward(float out[3]) const {
   for (int i = 0; i < 3; ++i) out[i] = -lights[current_light].z_axis[i];
 }
 
+void RenderingParameters::LightSpecular(float out[3]) const {
+  for (int i = 0; i < 3; ++i) out[i] = lights.empty() ? 1.0f : lights[current_light].specular[i];
+}
+
 DataManager::DataManager() {}
 DataManager::~DataManager() {
   if (ctx) cvr_destroy(ctx);
@@ -75,6 +79,16 @@ cvr_ctx* DataManager::GetDeviceContext(std::string* err) {
       }
     }
     uploaded = true;
+    gradient_built = false;
+  }
+  if (!gradient_built) {
+    // GenerateStructuredGradientTexture (datamanager.cpp:332-352), library defaults
+    cvr_gradient_params gp{gradient_model, 1, 0, 1};
+    if (cvr_build_gradient(ctx, &gp) != CVR_OK) {
+      if (err) *err = cvr_last_error(ctx);
+      return nullptr;
+    }
+    gradient_built = true;
   }
   return ctx;
 }
@@ -129,6 +143,18 @@ bool BaseVolumeRenderer::Redraw() {
   if (!IsBuilt()) return Fail("Redraw: renderer not built");
   size_t n = 0;
   const void* p = Params(&n);
+  // ApplyGradientPhongShading = checkbox && gradient texture, with
+  // RenderingParameters' Blinn-Phong terms (rc1prenderer.cpp:112-130)
+  cvr_blinn_phong bp{};
+  bp.apply = m_apply_gradient_shading && m_ext_data_manager && m_ext_data_manager->HasGradient();
+  vis::RenderingParameters dflt;
+  vis::RenderingParameters* rp = m_ext_rendering_parameters ? m_ext_rendering_parameters : &dflt;
+  bp.ka = rp->GetBlinnPhongKambient();
+  bp.kd = rp->GetBlinnPhongKdiffuse();
+  bp.ks = rp->GetBlinnPhongKspecular();
+  bp.shininess = rp->GetBlinnPhongNshininess();
+  rp->LightSpecular(bp.specular);
+  if (!CheckABI(cvr_set_blinn_phong(m_ctx, &bp), "Redraw")) return false;
   return CheckABI(cvr_render(m_ctx, Method(), &m_cam, &m_light, p, n, m_frame, m_width, m_height, nullptr, &m_stats),
                   "Redraw");
 }

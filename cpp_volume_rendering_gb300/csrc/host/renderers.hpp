@@ -42,6 +42,8 @@ class RenderingParameters {
   float GetBlinnPhongKspecular() const { return ks; }
   float GetBlinnPhongNshininess() const { return shininess; }
   void SetPhongParameters(float a, float d, float s, float n) { ka = a; kd = d; ks = s; shininess = n; }
+  // GetLightSourceSpecular (renderingparameters.cpp:132-135); (1,1,1) without lights.
+  void LightSpecular(float out[3]) const;
   int GetNumberOfLightSources() const { return (int)lights.size(); }
   void CreateNewLightSource(const LightSourceData& l) { lights.push_back(l); }
   LightSourceData* GetCurrentLight() { return lights.empty() ? nullptr : &lights[current_light]; }
@@ -69,13 +71,22 @@ class DataManager {
   void SetTransferFunction(const TransferFunction1D& t) { tf = t; has_tf = true; uploaded = false; }
   StructuredGridVolume* GetCurrentStructuredVolume() { return has_volume ? &volume : nullptr; }
   TransferFunction1D* GetCurrentTransferFunction() { return has_tf ? &tf : nullptr; }
-  // GetCurrentVolumeTexture(): the device context with the volume uploaded.
+  // GetCurrentVolumeTexture(): the device context with the volume uploaded
+  // (and its gradient, built with the current gradient model).
   cvr_ctx* GetDeviceContext(std::string* err);
+  // STRUCTURED_GRADIENT_TYPE (datamanager.h:64-69): CVR_GRADIENT_*; the
+  // gradient is (re)built with the next upload (UpdateStructuredGradientTexture).
+  void SetCurrentGradient(int model) { gradient_model = model; gradient_built = false; }
+  int GetCurrentGradientGenerationTypeID() const { return gradient_model; }
+  // GetCurrentGradientTexture() != nullptr
+  bool HasGradient() const { return gradient_model != CVR_GRADIENT_NONE; }
 
  private:
   StructuredGridVolume volume;
   TransferFunction1D tf;
   bool has_volume = false, has_tf = false, uploaded = false;
+  int gradient_model = CVR_GRADIENT_NONE;  // curr_gradient_comp_model (datamanager.cpp:27)
+  bool gradient_built = false;
   cvr_ctx* ctx = nullptr;
 };
 
@@ -117,6 +128,10 @@ class BaseVolumeRenderer {
   // The occlusion / shadow check boxes of the illumination renderers' UI
   // (SetImGuiComponents); a no-op for renderers without illumination.
   virtual void SetIllumination(bool occlusion, bool shadow) { (void)occlusion; (void)shadow; }
+  // The "Apply Gradient Shading" checkbox of every renderer
+  // (m_apply_gradient_shading / m_apply_gradient, default false).
+  void SetApplyGradientShading(bool on) { m_apply_gradient_shading = on; SetOutdated(); }
+  bool GetApplyGradientShading() const { return m_apply_gradient_shading; }
 
   // volrenderbase.cpp:77-84: Update only when outdated.
   bool PrepareRender(const vis::Camera& camera);
@@ -140,6 +155,7 @@ class BaseVolumeRenderer {
   bool BeginInit(int w, int h);  // common part of Init(): device context + frame
 
   bool vr_built = false, vr_outdated = true;
+  bool m_apply_gradient_shading = false;
   vis::DataManager* m_ext_data_manager = nullptr;
   vis::RenderingParameters* m_ext_rendering_parameters = nullptr;
   cvr_ctx* m_ctx = nullptr;

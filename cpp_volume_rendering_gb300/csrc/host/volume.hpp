@@ -67,6 +67,7 @@ struct LightSourceData {
   float y_axis[3] = {0, 1, 0};
   float x_axis[3] = {1, 0, 0};
   float spot_light_angle = 4.0f;
+  float specular[3] = {1, 1, 1};  // LightSourceData::specular (lightsourcelist.cpp:24)
 };
 struct LightSourceList {
   std::string name;

@@ -95,7 +95,7 @@ __device__ __forceinline__ float2 cache_lookup(const float2* __restrict__ c, con
   return lerp2(g.t, c0, c1);
 }
 
-// obj_ray_marching.comp main() + ShadeSample (non-gradient branch): the a5
+// obj_ray_marching.comp main() + ShadeSample (both branches): the a5
 // loop, but a sample is composited only when occlusion or shadow is on (the
 // reference's `src.a > 0.0 && Shade`), its light terms read from the cache.
 __global__ void __launch_bounds__(128) k_march_cached(FrameArgs f, CacheDims cd, const float2* __restrict__ cache,
@@ -128,9 +128,13 @@ __global__ void __launch_bounds__(128) k_march_cached(FrameArgs f, CacheDims cd,
           ++shaded;
           const float2 IaIs = cache_lookup(cache, cd, p, inv_grid);
           const float io = apply_occ ? IaIs.x : 0.0f, is = apply_sdw ? IaIs.y : 0.0f;
-          src.x = kk * (src.x * io * ka + src.x * is * kd);
-          src.y = kk * (src.y * io * ka + src.y * is * kd);
-          src.z = kk * (src.z * io * ka + src.z * is * kd);
+          if (f.grad.g) {
+            src = phong_ext(f, src, p, io, ka, is, kd);
+          } else {
+            src.x = kk * (src.x * io * ka + src.x * is * kd);
+            src.y = kk * (src.y * io * ka + src.y * is * kd);
+            src.z = kk * (src.z * io * ka + src.z * is * kd);
+          }
           src.w = 1.0f - expf(-src.w * h);
           src.x *= src.w; src.y *= src.w; src.z *= src.w;
           const float r = 1.0f - dst.w;

@@ -7,6 +7,21 @@ namespace cvr {
 
 #define CVR_MAX_GT_RAYS 256
 
+// Gradient Blinn-Phong shading (the ApplyPhongShading / ApplyGradientPhongShading
+// branches of the four ShadeSample functions): the per-voxel gradient of
+// cvr_build_gradient, the light position and the Blinn-Phong constants.
+struct GradView {
+  const uint2* g;             // 4 halves per voxel (gx, gy, gz, 0), x fastest; nullptr: shading off
+  cudaTextureObject_t tex;    // texture copy (hardware trilinear) or 0: the array with FP32 weights
+  int nx, ny, nz;
+  float3 inv_grid;            // 1 / VolumeGridSize (texture coordinates)
+  float3 inv_spacing;         // 1 / VolumeScales (texel coordinates)
+  float3 light_pos;           // LightSourcePosition / WorldLightingPos
+  float3 ispec;               // BlinnPhongIspecular / Ispecular
+  float ka, kd;               // BlinnPhongKa / Kd (the plain renderer's; the others bring theirs)
+  float ks, shininess;        // BlinnPhongKs / Kspecular, BlinnPhongShininess / Nshininess
+};
+
 // Launch geometry: each CTA covers a tile_w x tile_h block of pixels; each
 // warp covers an 8x4 sub-tile so the 32 rays of a warp stay spatially
 // coherent (they walk neighbouring voxels, which keeps gathers in L1).
@@ -22,6 +37,7 @@ struct FrameArgs {
   float4* out;
   uint32_t* counts;                // per-pixel step count, nullable
   unsigned long long* stats;       // [0] samples, [1] shaded samples, [2] secondary fetches
+  GradView grad;                   // gradient shading (grad.g == nullptr: off)
 };
 
 struct ExtArgs {

@@ -4,6 +4,8 @@
 // the surrogate-shaded marcher reuse the ground-truth light rays).
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "march.cuh"
 
 namespace cvr {
@@ -15,13 +17,105 @@ namespace cvr {
 constexpr int kMaxConeBoxes = 1 << 16;
 constexpr int kMaxLightSteps = 1 << 20;
 
+// ============================================= gradient Blinn-Phong terms
+// texture(TexVolumeGradient, Tpos / VolumeGridSize).xyz: GL_LINEAR,
+// clamp-to-edge on the voxel grid (the texture copy when there is one).
+__device__ __forceinline__ float3 sample_gradient(const GradView& g, float3 p) {
+  if (g.tex) {
+    const float4 r = tex3D<float4>(g.tex, p.x * g.inv_grid.x, p.y * g.inv_grid.y, p.z * g.inv_grid.z);
+    return f3(r.x, r.y, r.z);
+  }
+  const Tap a = axis_tap(fmaf(p.x, g.inv_spacing.x, -0.5f), g.nx);
+  const Tap b = axis_tap(fmaf(p.y, g.inv_spacing.y, -0.5f), g.ny);
+  const Tap c = axis_tap(fmaf(p.z, g.inv_spacing.z, -0.5f), g.nz);
+  const size_t sy = (size_t)g.nx, sz = (size_t)g.nx * g.ny;
+  auto at = [&](int x, int y, int z) {
+    const uint2 q = __ldg(g.g + (size_t)x + sy * y + sz * z);
+    const float2 xy = __half22float2(*reinterpret_cast<const __half2*>(&q.x));
+    return f3(xy.x, xy.y, __low2float(*reinterpret_cast<const __half2*>(&q.y)));
+  };
+  auto lerp = [](float t, float3 u, float3 v) {
+    return f3(fmaf(t, v.x - u.x, u.x), fmaf(t, v.y - u.y, u.y), fmaf(t, v.z - u.z, u.z));
+  };
+  const float3 c00 = lerp(a.t, at(a.i0, b.i0, c.i0), at(a.i1, b.i0, c.i0));
+  const float3 c10 = lerp(a.t, at(a.i0, b.i1, c.i0), at(a.i1, b.i1, c.i0));
+  const float3 c01 = lerp(a.t, at(a.i0, b.i0, c.i1), at(a.i1, b.i0, c.i1));
+  const float3 c11 = lerp(a.t, at(a.i0, b.i1, c.i1), at(a.i1, b.i1, c.i1));
+  return lerp(c.t, lerp(b.t, c00, c10), lerp(b.t, c01, c11));
+}
+
+// The terms every gradient branch shares (ray_marching_1p.comp:50-70 and its
+// copies in the other shaders): false when the interpolated gradient is the
+// zero vector, where the sample keeps its unshaded colour.
+struct BlinnTerms {
+  float diff;  // max(0, dot(N, L))
+  float spec;  // pow(max(0, dot(H, N)), shininess)
+};
+__device__ __forceinline__ bool blinn_terms(const FrameArgs& f, float3 tx, BlinnTerms& t) {
+  float3 n = sample_gradient(f.grad, tx);
+  if (n.x == 0.0f && n.y == 0.0f && n.z == 0.0f) return false;
+  n = normalize3(n);
+  const float3 w = tx - f.vol.grid * 0.5f;
+  const float3 l = normalize3(f.grad.light_pos - w);
+  const float3 e = normalize3(f.cam.eye - w);
+  const float3 hv = normalize3(e + l);
+  t.diff = fmaxf(0.0f, dot3(n, l));
+  t.spec = powf(fmaxf(0.0f, dot3(hv, n)), f.grad.shininess);
+  return true;
+}
+
+// ShadeBlinnPhong (ray_marching_1p.comp:48-81):
+// clr * (Ka + Kd * diff) + Ispecular * Ks * spec.
+__device__ __forceinline__ float4 phong_plain(const FrameArgs& f, float4 L, float3 tx) {
+  BlinnTerms t;
+  if (!blinn_terms(f, tx, t)) return L;
+  const float m = f.grad.ka + f.grad.kd * t.diff;
+  const float s = f.grad.ks * t.spec;
+  L.x = L.x * m + f.grad.ispec.x * s;
+  L.y = L.y * m + f.grad.ispec.y * s;
+  L.z = L.z * m + f.grad.ispec.z * s;
+  return L;
+}
+
+// Extinction / light cache (ebs_ray_bbox_marching.comp:524-546,
+// obj_ray_marching.comp:111-129):
+// (1/(ka+kd)) * (L*Io*ka + Is*(L*kd*diff)) + Is*(ks*Ispecular*spec).
+__device__ __forceinline__ float4 phong_ext(const FrameArgs& f, float4 L, float3 tx, float io, float ka, float is,
+                                            float kd) {
+  BlinnTerms t;
+  if (!blinn_terms(f, tx, t)) return L;
+  const float kk = 1.0f / (ka + kd);
+  const float s = is * (f.grad.ks * t.spec);
+  L.x = kk * (L.x * io * ka + is * (L.x * kd * t.diff)) + s * f.grad.ispec.x;
+  L.y = kk * (L.y * io * ka + is * (L.y * kd * t.diff)) + s * f.grad.ispec.y;
+  L.z = kk * (L.z * io * ka + is * (L.z * kd * t.diff)) + s * f.grad.ispec.z;
+  return L;
+}
+
+// Cone and ground truth (ray_bbox_marching.comp:630-648, gt_ray_marching.comp:
+// 277-295, whose specular colour is 1): L * ((1/(ka+kd)) * (Io*ka + Is*kd*diff))
+// + Ispecular * (Is*ks*spec).
+__device__ __forceinline__ float4 phong_cone(const FrameArgs& f, float4 L, float3 tx, float io, float ka, float is,
+                                             float kd) {
+  BlinnTerms t;
+  if (!blinn_terms(f, tx, t)) return L;
+  const float m = (1.0f / (ka + kd)) * (io * ka + is * kd * t.diff);
+  const float s = is * f.grad.ks * t.spec;
+  L.x = L.x * m + f.grad.ispec.x * s;
+  L.y = L.y * m + f.grad.ispec.y * s;
+  L.z = L.z * m + f.grad.ispec.z * s;
+  return L;
+}
+
 // ============================================================ plain (rc1pass)
 struct PlainShade {
   struct Ray {};
   __device__ __forceinline__ void begin(Ray&, float3) const {}
-  // Gradient Blinn-Phong is off by default (m_apply_gradient_shading=false,
-  // rc1prenderer.cpp:22), so ShadeSample is the identity here.
-  __device__ __forceinline__ float4 shade(float4 src, float3, const Ray&, const FrameArgs&, unsigned&) const { return src; }
+  // ShadeSample is the identity unless gradient shading is on
+  // (ApplyGradientPhongShading, ray_marching_1p.comp:143-145).
+  __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray&, const FrameArgs& f, unsigned&) const {
+    return f.grad.g ? phong_plain(f, src, tx) : src;
+  }
 };
 
 // ====================================================== extinction (rc1pextbsd)
@@ -212,11 +306,12 @@ struct ExtShade {
     return expf(-st);
   }
 
-  // ShadeSample, non-gradient branch (ebs_ray_bbox_marching.comp:500-551).
+  // ShadeSample (ebs_ray_bbox_marching.comp:500-551).
   __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray&, const FrameArgs& f, unsigned& aux) const {
     float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
     if (e->apply_occ) { ka = e->ka; io = ambient_occlusion(tx, f); aux += e->n_shells; }
     if (e->apply_sdw) { kd = e->kd; is = tlo ? shadow_table(tx, f, aux) : shadow(tx, f, aux); }
+    if (f.grad.g) return phong_ext(f, src, tx, io, ka, is, kd);
     float k = 1.0f / (ka + kd);
     src.x = k * (src.x * io * ka + src.x * is * kd);
     src.y = k * (src.y * io * ka + src.y * is * kd);
@@ -342,11 +437,12 @@ struct DosShade {
     return cone(sdw_tab, d->sdw, tx, k, v, u, f, aux);
   }
 
-  // ShadeSample, non-gradient branch (ray_bbox_marching.comp:607-656).
+  // ShadeSample (ray_bbox_marching.comp:607-656).
   __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray& r, const FrameArgs& f, unsigned& aux) const {
     float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
     if (d->apply_occ) { ka = d->ka; io = occlusion(tx, r, f, aux); }
     if (d->apply_sdw) { kd = d->kd; is = shadow(tx, f, aux); }
+    if (f.grad.g) return phong_cone(f, src, tx, io, ka, is, kd);
     float kk = 1.0f / (ka + kd);
     src.x = kk * (src.x * io * ka + src.x * is * kd);
     src.y = kk * (src.y * io * ka + src.y * is * kd);
@@ -433,11 +529,12 @@ struct GtShade {
     return ssdw / swgt;
   }
 
-  // ShadeSample, non-gradient branch (gt_ray_marching.comp:254-303).
+  // ShadeSample (gt_ray_marching.comp:254-303).
   __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray& r, const FrameArgs& f, unsigned& aux) const {
     float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
     if (g->apply_occ) { ka = g->ka; io = occlusion(tx, r, f, aux); }
     if (g->apply_sdw) { kd = g->kd; is = shadow(tx, f, aux); }
+    if (f.grad.g) return phong_cone(f, src, tx, io, ka, is, kd);
     float kk = 1.0f / (ka + kd);
     src.x = kk * (src.x * io * ka + src.x * is * kd);
     src.y = kk * (src.y * io * ka + src.y * is * kd);

@@ -242,6 +242,16 @@ struct SurCounts {
   }
 };
 
+// sur_shade's light terms through the ground truth's gradient branch
+// (gt_ray_marching.comp:277-295) when gradient shading is on.
+__device__ __forceinline__ float4 sur_phong(const SurArgs& a, const FrameArgs& f, float4 src, float3 p, float ao,
+                                            float sdw) {
+  float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
+  if (a.apply_occ) { ka = a.ka; io = fminf(fmaxf(ao, 0.0f), 1.0f); }
+  if (a.apply_sdw) { kd = a.kd; is = a.shadow_type == 1 ? 0.0f : fminf(fmaxf(sdw, 0.0f), 1.0f); }
+  return phong_cone(f, src, p, io, ka, is, kd);
+}
+
 __device__ __forceinline__ void sur_finish(const FrameArgs& f, const SurRay& r) {
   size_t o = (size_t)r.py * f.W + r.px;
   f.out[o] = r.dst;
@@ -357,7 +367,9 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
     if (pending) {
       ++cnt.shaded;
       pending = false;
-      src = sur_shade(src_rays.a(ray.job), src, y[0], y[1]);
+      const FrameArgs& fj = src_rays.f(ray.job);
+      src = fj.grad.g ? sur_phong(src_rays.a(ray.job), fj, src, p, y[0], y[1])
+                      : sur_shade(src_rays.a(ray.job), src, y[0], y[1]);
       src.w = 1.0f - expf(-src.w * h);
       src.x *= src.w; src.y *= src.w; src.z *= src.w;
       float r = 1.0f - ray.dst.w;

@@ -98,6 +98,21 @@ cvr_status ensure_pyramid_textures(cvr_ctx* c) {
   return CVR_OK;
 }
 
+// The gradient as an RGBA16F texture (the reference's RGB16F gradient
+// texture, utils.cpp:274-278, with a fourth channel for 8-byte texels).
+cvr_status ensure_gradient_texture(cvr_ctx* c) {
+  if (c->tex.grad_valid) return CVR_OK;
+  if (!c->grad_ready) return fail(c, CVR_ERR_NOT_READY, "gradient texture: no gradient");
+  cudaError_t e = make_texture(c, c->tex.grad, c->d_grad, sizeof(uint2), cudaCreateChannelDescHalf4(), c->nx, c->ny,
+                               c->nz, cudaReadModeElementType);
+  if (e != cudaSuccess) {
+    c->tex.grad.release();
+    return cuda_fail(c, e, "gradient texture");
+  }
+  c->tex.grad_valid = true;
+  return CVR_OK;
+}
+
 }  // namespace ctxutil
 }  // namespace cvr
 

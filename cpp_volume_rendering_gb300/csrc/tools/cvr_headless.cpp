@@ -8,6 +8,7 @@
 //                [--width 768 --height 768] [--frames 1]
 //                [--cameras LIST --camera-index i] [--lights LIST --light-index i]
 //                [--eye x y z] [--fovy deg] [--occlusion 0|1] [--shadow 0|1]
+//                [--gradient sobel|fd|cs|none] [--gradient-shading 0|1]
 //                [--out frame.pfm]
 // Exit code 0 on success, 1 on a usage error, 2 on a data error, 3 on a
 // rendering error; messages go to stderr.
@@ -24,6 +25,7 @@ static int usage() {
                "usage: cvr_headless --volume FILE --tf FILE --renderer ABBR [--width W --height H] [--frames N]\n"
                "       [--cameras FILE --camera-index I] [--lights FILE --light-index I] [--eye X Y Z]\n"
                "       [--fovy DEG] [--occlusion 0|1] [--shadow 0|1] [--weights FILE] [--out FILE.pfm]\n"
+               "       [--gradient sobel|fd|cs|none] [--gradient-shading 0|1]\n"
                "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt s_1psurr (needs --weights)\n");
   return 1;
 }
@@ -32,7 +34,7 @@ int main(int argc, char** argv) {
   std::string vol, tf, rend, out, cams, lights, weights;
   int w = 768, h = 768, frames = 1, cam_i = 0, light_i = 0;
   bool have_eye = false;
-  int occlusion = -1, shadow = -1;
+  int occlusion = -1, shadow = -1, gradient = CVR_GRADIENT_NONE, gradient_shading = 0;
   float eye[3] = {0, 0, 0}, fovy = 45.0f;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
@@ -53,6 +55,16 @@ int main(int argc, char** argv) {
     else if (a == "--fovy" && (v = next())) fovy = (float)std::atof(v);
     else if (a == "--occlusion" && (v = next())) occlusion = std::atoi(v);
     else if (a == "--shadow" && (v = next())) shadow = std::atoi(v);
+    else if (a == "--gradient-shading" && (v = next())) gradient_shading = std::atoi(v);
+    else if (a == "--gradient" && (v = next())) {
+      // DataManager's gradient models (datamanager.h:64-69)
+      std::string g = v;
+      if (g == "sobel") gradient = CVR_GRADIENT_SOBEL_FELDMAN;
+      else if (g == "fd") gradient = CVR_GRADIENT_FINITE_DIFFERENCES;
+      else if (g == "cs") gradient = CVR_GRADIENT_COMPUTE_SOBEL;
+      else if (g == "none") gradient = CVR_GRADIENT_NONE;
+      else return usage();
+    }
     else if (a == "--eye" && i + 3 < argc) {
       for (int k = 0; k < 3; ++k) eye[k] = (float)std::atof(argv[++i]);
       have_eye = true;
@@ -76,6 +88,7 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "cvr_headless: %s\n", err.c_str());
     return 2;
   }
+  mgr.data.SetCurrentGradient(gradient);
   mgr.params.SetScreenSize(w, h);
   vis::Camera& cam = mgr.params.camera;
   cam.fovy = fovy;
@@ -116,6 +129,7 @@ int main(int argc, char** argv) {
     BaseVolumeRenderer* r = mgr.GetCurrentVolumeRenderer();
     r->SetIllumination(occlusion != 0, shadow != 0);
   }
+  mgr.GetCurrentVolumeRenderer()->SetApplyGradientShading(gradient_shading != 0);
   auto t0 = std::chrono::steady_clock::now();
   for (int f = 0; f < frames; ++f) {
     if (!mgr.Display()) {

@@ -289,6 +289,25 @@ class Context:
     def set_sampling(self, flags: int):
         self._ck(self.lib.cvr_set_sampling(self.h, flags))
 
+    # ---- gradient Blinn-Phong shading
+    def build_gradient(self, model: int = abi.GRADIENT_FINITE_DIFFERENCES, sample_size: int = 1,
+                       filter_nxnxn: int = 0, normalized: bool = True):
+        p = abi.GradientParams(model, sample_size, filter_nxnxn, int(normalized))
+        self._ck(self.lib.cvr_build_gradient(self.h, C.byref(p)))
+
+    def gradient(self) -> np.ndarray:
+        """The current volume's gradient, (d, h, w, 3) float32."""
+        n = self.dims[0] * self.dims[1] * self.dims[2]
+        out = np.zeros(3 * n, np.float32)
+        self._ck(self.lib.cvr_download_gradient(self.h, out.ctypes.data_as(C.POINTER(C.c_float)), out.size))
+        w, h, d = self.dims
+        return out.reshape(d, h, w, 3)
+
+    def set_blinn_phong(self, apply: bool = True, ka: float = 0.5, kd: float = 0.5, ks: float = 0.8,
+                        shininess: float = 30.0, specular=(1.0, 1.0, 1.0)):
+        bp = abi.BlinnPhong(int(apply), ka, kd, ks, shininess, abi.F3(*specular))
+        self._ck(self.lib.cvr_set_blinn_phong(self.h, C.byref(bp)))
+
     # ---- surrogate network and shading points
     def mlp_init(self, seed: int):
         self._ck(self.lib.cvr_mlp_init(self.h, seed))

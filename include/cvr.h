@@ -314,6 +314,46 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
 cvr_status cvr_set_sampling(cvr_ctx* ctx, int flags);
 int cvr_get_sampling(cvr_ctx* ctx);
 
+/* ---- gradient Blinn-Phong shading -------------------------------------------
+ * Gradient models: DataManager::STRUCTURED_GRADIENT_TYPE
+ * (libs/volvis_utils/datamanager.h:64-69, default NONE_GRADIENT). */
+#define CVR_GRADIENT_SOBEL_FELDMAN 0       /* GenerateSobelFeldmanGradientTexture (libs/volvis_utils/utils.cpp:287-351) */
+#define CVR_GRADIENT_FINITE_DIFFERENCES 1  /* GenerateGradientTexture (utils.cpp:146-284) */
+#define CVR_GRADIENT_COMPUTE_SOBEL 2       /* GenerateGradientWithComputeShader (datamanager.cpp:623-700) */
+#define CVR_GRADIENT_NONE 3
+typedef struct cvr_gradient_params {
+  int model;          /* CVR_GRADIENT_* */
+  int sample_size;    /* gradient_sample_size, finite differences only (default 1) */
+  int filter_nxnxn;   /* filter_nxnxn, finite differences only (default 0) */
+  int normalized;     /* normalized_gradient, finite differences only (default 1) */
+} cvr_gradient_params;
+/* Builds the current volume's per-voxel gradient on the device (stored as
+ * FP16 x, y, z like the reference's RGB16F texture) and keeps the model: a
+ * later cvr_set_volume into this slot rebuilds it on the next shaded frame, as
+ * DataManager regenerates it with each volume (datamanager.cpp:326-327).
+ * params NULL or model CVR_GRADIENT_NONE drops it. */
+cvr_status cvr_build_gradient(cvr_ctx* ctx, const cvr_gradient_params* params);
+/* The gradient as 3 floats per voxel (x fastest); synchronous. */
+cvr_status cvr_download_gradient(cvr_ctx* ctx, float* host_xyz, size_t n_floats);
+/* RenderingParameters' Blinn-Phong terms (renderingparameters.cpp:23-26,
+ * lightsourcelist.cpp:24) and the renderers' "Apply Gradient Shading" switch
+ * (m_apply_gradient_shading, default off).  When apply is set and the volume
+ * has a gradient, every method shades with the gradient branch of its
+ * ShadeSample: plain ShadeBlinnPhong (ray_marching_1p.comp:48-81, with ka,
+ * kd here), extinction and the light cache (ebs_ray_bbox_marching.comp:524-546,
+ * obj_ray_marching.comp:111-129), cone (ray_bbox_marching.comp:630-648),
+ * ground truth and surrogate (gt_ray_marching.comp:277-295, specular colour
+ * 1).  The light position is cvr_light.position (a light is then required). */
+typedef struct cvr_blinn_phong {
+  int apply;           /* default 0 */
+  float ka, kd;        /* BlinnPhongKa / Kd (0.5, 0.5): the plain renderer's; the others use their params' */
+  float ks;            /* BlinnPhongKs / Kspecular (0.8) */
+  float shininess;     /* BlinnPhongShininess / Nshininess (30) */
+  float specular[3];   /* light source specular colour, Ispecular (1, 1, 1) */
+} cvr_blinn_phong;
+cvr_status cvr_set_blinn_phong(cvr_ctx* ctx, const cvr_blinn_phong* bp);
+cvr_status cvr_get_blinn_phong(cvr_ctx* ctx, cvr_blinn_phong* out);
+
 /* ---- batched rendering ------------------------------------------------------
  * No reference counterpart (the reference renders one view per Redraw()).
  * A batch is a fixed list of frames over the resident volumes, views and

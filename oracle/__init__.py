@@ -52,6 +52,9 @@ def load():
                                   C.POINTER(C.c_uint64), I]),
             "oracle_set_mlp": (I, [P, P, I]),
             "oracle_set_light_cache": (I, [P, I, I, I]),
+            "oracle_build_gradient": (I, [P, C.POINTER(abi.GradientParams)]),
+            "oracle_get_gradient": (I, [P, P]),
+            "oracle_set_blinn_phong": (I, [P, C.POINTER(abi.BlinnPhong)]),
             "oracle_sur_features": (I, [P, I, C.POINTER(abi.Light), I, D, P, I, P, P]),
             "oracle_gt_points": (I, [P, C.POINTER(abi.Light), C.POINTER(abi.GtParams), P, I, P]),
         }
@@ -150,6 +153,20 @@ class Oracle:
 
     def set_light_cache(self, w, h, d):
         self._ck(self.lib.oracle_set_light_cache(self.h, w, h, d))
+
+    def build_gradient(self, model=abi.GRADIENT_FINITE_DIFFERENCES, sample_size=1, filter_nxnxn=0, normalized=True):
+        p = abi.GradientParams(model, sample_size, filter_nxnxn, int(normalized))
+        self._ck(self.lib.oracle_build_gradient(self.h, C.byref(p)))
+
+    def gradient(self):
+        d, h, w = self.vol.shape
+        out = np.zeros((d, h, w, 3), np.float32)
+        self._ck(self.lib.oracle_get_gradient(self.h, _p(out)))
+        return out
+
+    def set_blinn_phong(self, apply=True, ka=0.5, kd=0.5, ks=0.8, shininess=30.0, specular=(1.0, 1.0, 1.0)):
+        bp = abi.BlinnPhong(int(apply), ka, kd, ks, shininess, abi.F3(*specular))
+        self._ck(self.lib.oracle_set_blinn_phong(self.h, C.byref(bp)))
 
     def set_mlp(self, params):
         params = np.ascontiguousarray(params, np.float32)

@@ -3,6 +3,8 @@
 Compiles the reference's own CPU table builders from its sources, in place
 (nothing is copied into this repository), together with oracle/ref_shim.cpp:
   libs/volvis_utils/transferfunction1d.cpp, transferfunction.cpp,
+  libs/volvis_utils/utils.cpp, structuredgridvolume.cpp, gridvolume.cpp
+  (the gradient builders),
   libs/math_utils/utils.cpp,
   cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp,
   libs/vis_utils/summedareatable.h (header only).
@@ -37,6 +39,9 @@ def build(verbose: bool = False) -> Path | None:
         ref / "libs/volvis_utils/transferfunction.cpp",
         ref / "libs/math_utils/utils.cpp",
         ref / "cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp",
+        ref / "libs/volvis_utils/utils.cpp",
+        ref / "libs/volvis_utils/structuredgridvolume.cpp",
+        ref / "libs/volvis_utils/gridvolume.cpp",
     ]
     if LIB.exists() and all(s.stat().st_mtime < LIB.stat().st_mtime for s in srcs):
         return LIB

@@ -75,6 +75,9 @@ struct Scene {
   bool gt_ready = false;
   std::vector<float> mlp;  // surrogate network parameters (CVR_MLP_PARAMS floats)
   int lc[3] = {0, 0, 0};   // object-space light cache dims (0: off)
+  std::vector<float> grad; // per-voxel gradient, 3 per voxel, FP16-rounded (the RGB16F texture)
+  bool grad_ready = false;
+  cvr_blinn_phong bp{0, 0.5f, 0.5f, 0.8f, 30.0f, {1.0f, 1.0f, 1.0f}};
 
   double vox_norm(size_t i) const {
     if (dtype == CVR_U8) return (double)vox[i] / 255.0;
@@ -607,6 +610,69 @@ inline void mlp_forward_bf16(const std::vector<float>& P, const double* x, doubl
   }
 }
 
+// ------------------------------------------------------------ gradient shading
+// texture(TexVolumeGradient, Tpos / VolumeGridSize).xyz
+template <class T> V3<T> sample_gradient(const Scene& s, V3<T> p) {
+  V3<T> grid = v3<T>(T(s.nx * s.sx), T(s.ny * s.sy), T(s.nz * s.sz));
+  Tap<T> tx = axis_tap<T>(p.x / grid.x * T(s.nx) - T(0.5), s.nx);
+  Tap<T> ty = axis_tap<T>(p.y / grid.y * T(s.ny) - T(0.5), s.ny);
+  Tap<T> tz = axis_tap<T>(p.z / grid.z * T(s.nz) - T(0.5), s.nz);
+  T r[3];
+  for (int ch = 0; ch < 3; ++ch) {
+    auto at = [&](int x, int y, int z) {
+      return (T)s.grad[3 * ((size_t)x + (size_t)s.nx * ((size_t)y + (size_t)s.ny * z)) + ch];
+    };
+    T c00 = at(tx.i0, ty.i0, tz.i0) + tx.t * (at(tx.i1, ty.i0, tz.i0) - at(tx.i0, ty.i0, tz.i0));
+    T c10 = at(tx.i0, ty.i1, tz.i0) + tx.t * (at(tx.i1, ty.i1, tz.i0) - at(tx.i0, ty.i1, tz.i0));
+    T c01 = at(tx.i0, ty.i0, tz.i1) + tx.t * (at(tx.i1, ty.i0, tz.i1) - at(tx.i0, ty.i0, tz.i1));
+    T c11 = at(tx.i0, ty.i1, tz.i1) + tx.t * (at(tx.i1, ty.i1, tz.i1) - at(tx.i0, ty.i1, tz.i1));
+    T c0 = c00 + ty.t * (c10 - c00), c1 = c01 + ty.t * (c11 - c01);
+    r[ch] = c0 + tz.t * (c1 - c0);
+  }
+  return v3<T>(r[0], r[1], r[2]);
+}
+
+// The shared terms of the gradient branches (ray_marching_1p.comp:50-70):
+// false for a zero gradient (the colour is left unshaded).
+template <class T>
+bool blinn_terms(const Scene& s, V3<T> grid, V3<T> eye, V3<T> tx, V3<T> light_pos, T& diff, T& spec) {
+  V3<T> n = sample_gradient<T>(s, tx);
+  if (n.x == T(0) && n.y == T(0) && n.z == T(0)) return false;
+  n = normalize(n);
+  V3<T> w = tx - grid * T(0.5);
+  V3<T> l = normalize(light_pos - w);
+  V3<T> e = normalize(eye - w);
+  V3<T> hv = normalize(e + l);
+  diff = std::max(T(0), dot(n, l));
+  spec = std::pow(std::max(T(0), dot(hv, n)), T(s.bp.shininess));
+  return true;
+}
+
+enum PhongKind { PHONG_PLAIN, PHONG_EXT, PHONG_CONE, PHONG_GT };
+
+// The gradient branch of each ShadeSample:
+//  plain  ShadeBlinnPhong (ray_marching_1p.comp:71-76): L*(Ka + Kd*diff) + Is*Ks*spec
+//  ext    ebs_ray_bbox_marching.comp:540-542, obj_ray_marching.comp:127-128:
+//         (1/(ka+kd))*(L*Io*ka + IS*(L*kd*diff)) + IS*(ks*Is*spec)
+//  cone   ray_bbox_marching.comp:646-647: L*((1/(ka+kd))*(Io*ka + IS*kd*diff)) + Is*(IS*ks*spec)
+//  gt     gt_ray_marching.comp:293-294: the cone form with specular colour 1
+template <class T>
+V4<T> phong(const Scene& s, const Frame<T>& f, V4<T> L, V3<T> tx, V3<T> light_pos, int kind, T io, T ka, T is, T kd) {
+  T diff, spec;
+  if (!blinn_terms<T>(s, f.grid, f.cam.eye, tx, light_pos, diff, spec)) return L;
+  V3<T> isp = kind == PHONG_GT ? v3<T>(1, 1, 1) : from<T>(s.bp.specular);
+  T ks = T(s.bp.ks);
+  T* c[3] = {&L.r, &L.g, &L.b};
+  T sp[3] = {isp.x, isp.y, isp.z};
+  for (int i = 0; i < 3; ++i) {
+    T& v = *c[i];
+    if (kind == PHONG_PLAIN) v = v * (T(s.bp.ka) + T(s.bp.kd) * diff) + sp[i] * ks * spec;
+    else if (kind == PHONG_EXT) v = (T(1) / (ka + kd)) * (v * io * ka + is * (v * kd * diff)) + is * (ks * sp[i] * spec);
+    else v = v * ((T(1) / (ka + kd)) * (io * ka + is * kd * diff)) + sp[i] * (is * ks * spec);
+  }
+  return L;
+}
+
 // ------------------------------------------------------------ primary loop
 // ray_marching_1p.comp:160-247 and the identical loops of the other shaders.
 template <class T, class ShadeFn>
@@ -707,14 +773,30 @@ template <class T> V4<T> combine(V4<T> L, bool occ_on, T ka_in, T io, bool sdw_o
   return L;
 }
 
+// ShadeSample's final combination: the gradient branch when gradient shading
+// is on (ApplyPhongShading), else combine().
+template <class T>
+V4<T> shade_mix(const Scene& s, const Frame<T>& f, V4<T> L, V3<T> tx, V3<T> light_pos, int kind, bool occ_on, T ka_in,
+                T io, bool sdw_on, T kd_in, T is) {
+  if (!(s.bp.apply && s.grad_ready)) return combine(L, occ_on, ka_in, io, sdw_on, kd_in, is);
+  T ka = occ_on ? ka_in : T(0), kd = sdw_on ? kd_in : T(0);
+  if (!occ_on) io = 0;
+  if (!sdw_on) is = 0;
+  return phong<T>(s, f, L, tx, light_pos, kind, io, ka, is, kd);
+}
+
 template <class T>
 int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light, const void* params, int W, int H,
              int y0, int y1, double* out, uint32_t* counts, uint64_t* total, int threads) {
   switch (method) {
     case CVR_METHOD_PLAIN: {
       const cvr_plain_params* p = (const cvr_plain_params*)params;
+      const bool grad = s.bp.apply && s.grad_ready;
+      const V3<T> lpos = from<T>(light.position);
       march_rows<T>(s, cam, T(p->step_size), W, H, y0, y1, out, counts, total, threads,
-                    [](const Frame<T>&, V4<T> src, V3<T>, V3<T>) { return src; });
+                    [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
+                      return grad ? phong<T>(s, f, src, tx, lpos, PHONG_PLAIN, T(0), T(0), T(0), T(0)) : src;
+                    });
       return 0;
     }
     case CVR_METHOD_EXTINCTION: {
@@ -741,7 +823,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                       [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
                         T io, is;
                         cache_lookup<T>(s, cache, f.grid, tx, io, is);
-                        return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd),
+                        return shade_mix<T>(s, f, src, tx, e.light_pos, PHONG_EXT, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd),
                                        is);
                       },
                       p->apply_occlusion || p->apply_shadow);
@@ -751,7 +833,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                     [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
                       T io = p->apply_occlusion ? ext_ao(f, e, tx) : T(0);
                       T is = p->apply_shadow ? ext_shadow(f, e, tx) : T(0);
-                      return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
+                      return shade_mix<T>(s, f, src, tx, e.light_pos, PHONG_EXT, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
                     });
       return 0;
     }
@@ -802,7 +884,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                       [&](const Frame<T>& f, V4<T> src, V3<T> tx, V3<T>) {
                         T io, is;
                         cache_lookup<T>(s, cache, f.grid, tx, io, is);
-                        return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd),
+                        return shade_mix<T>(s, f, src, tx, d.light_pos, PHONG_EXT, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd),
                                        is);
                       },
                       p->apply_occlusion || p->apply_shadow);
@@ -833,7 +915,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                         }
                         is = dark ? T(0) : cone_integrate(f, d, s.sdw, tx, k, v, u);
                       }
-                      return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
+                      return shade_mix<T>(s, f, src, tx, d.light_pos, PHONG_CONE, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
                     });
       return 0;
     }
@@ -850,7 +932,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                       V3<T> v_up = normalize(cross(-dir, v_right));
                       T io = p->apply_occlusion ? gt_occlusion(f, g, tx, v_up, v_right, dir) : T(0);
                       T is = p->apply_shadow ? gt_shadow(f, g, tx) : T(0);
-                      return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
+                      return shade_mix<T>(s, f, src, tx, g.light_pos, PHONG_GT, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
                     });
       return 0;
     }
@@ -873,7 +955,7 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                       mlp_forward_bf16(s.mlp, xd, y);
                       T io = T(std::min(std::max(y[0], 0.0), 1.0));
                       T is = p->shadow_type == 1 ? T(0) : T(std::min(std::max(y[1], 0.0), 1.0));
-                      return combine(src, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
+                      return shade_mix<T>(s, f, src, tx, lpos, PHONG_GT, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
                     });
       return 0;
     }
@@ -940,6 +1022,84 @@ template <class T> void build_pyramid_t(Scene& s, float s0f, std::vector<T>& out
   for (auto& v : out) v = T(-1) * std::log(T(1) - v);
 }
 
+// float -> IEEE binary16 (round to nearest, ties to even) -> float: the
+// RGB16F storage of the reference's gradient texture.
+float to_half(float v) {
+  if (!std::isfinite(v) || v == 0.0f) return v;
+  const double a = std::fabs((double)v);
+  if (a >= 65520.0) return std::copysign(INFINITY, v);
+  int e;
+  std::frexp(a, &e);                     // a = m 2^e, m in [0.5, 1)
+  const int ue = std::max(e - 11, -24);  // 11 significant bits; subnormal spacing 2^-24
+  const double r = std::nearbyint(std::ldexp(a, -ue));
+  return (float)std::copysign(std::ldexp(r, ue), (double)v);
+}
+
+// DataManager::GenerateStructuredGradientTexture (datamanager.cpp:332-352):
+// GenerateGradientTexture (utils.cpp:146-284) for finite differences,
+// GenerateSobelFeldmanGradientTexture (utils.cpp:287-351) for both Sobel
+// models (the compute-shader one, sobelfeldman_generator.comp, is the same
+// stencil), in double, stored as float then FP16.
+void build_gradient(Scene& s, const cvr_gradient_params& p) {
+  const int W = s.nx, H = s.ny, D = s.nz;
+  auto S = [&](int x, int y, int z) -> double {  // GetNormalizedSample (structuredgridvolume.cpp:121-150)
+    if (x < 0 || y < 0 || z < 0 || x >= W || y >= H || z >= D) return 0.0;
+    return s.vox_norm((size_t)x + (size_t)W * ((size_t)y + (size_t)H * z));
+  };
+  std::vector<V3<double>> g((size_t)W * H * D);
+  for (int z = 0; z < D; ++z)
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        V3<double> r{0, 0, 0};
+        if (p.model == CVR_GRADIENT_FINITE_DIFFERENCES) {
+          const int n = p.sample_size;
+          V3<double> s1{S(x - n, y, z), S(x, y - n, z), S(x, y, z - n)};
+          V3<double> s2{S(x + n, y, z), S(x, y + n, z), S(x, y, z + n)};
+          r = s2 - s1;
+          if (p.normalized) r = normalize(r);
+          else r = v3<double>(r.x / 2.0f * (float)n, r.y / 2.0f * (float)n, r.z / 2.0f * (float)n);
+          if (r.x != r.x) r = v3<double>(0, 0, 0);
+        } else {
+          for (int v1 = -1; v1 <= 1; ++v1)
+            for (int v2 = -1; v2 <= 1; ++v2) {
+              const double w = 4.0 / std::pow(2.0, std::abs(v1) + std::abs(v2));
+              r.z += S(x + v1, y + v2, z - 1) * w + S(x + v1, y + v2, z + 1) * -w;
+              r.y += S(x + v1, y - 1, z + v2) * w + S(x + v1, y + 1, z + v2) * -w;
+              r.x += S(x - 1, y + v2, z + v1) * w + S(x + 1, y + v2, z + v1) * -w;
+            }
+        }
+        g[(size_t)x + (size_t)W * ((size_t)y + (size_t)H * z)] = r;
+      }
+  if (p.model == CVR_GRADIENT_FINITE_DIFFERENCES && p.filter_nxnxn > 0) {
+    // utils.cpp:196-233: the window sums the centre's own gradient num times
+    const int fn = (p.filter_nxnxn - 1) / 2;
+    size_t index = 0;
+    for (int z = 0; z < D; ++z)
+      for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+          V3<double> avg{0, 0, 0};
+          int num = 0;
+          for (int k = z - fn; k <= z + fn; ++k)
+            for (int j = y - fn; j <= y + fn; ++j)
+              for (int i = x - fn; i <= x + fn; ++i)
+                if (!(i < 0 || j < 0 || k < 0 || i >= W || j >= H || k >= D)) {
+                  avg = avg + g[(size_t)x + (size_t)W * ((size_t)y + (size_t)H * z)];
+                  ++num;
+                }
+          avg = v3<double>(avg.x / (double)num, avg.y / (double)num, avg.z / (double)num);
+          if (avg.x != 0.0 && avg.y != 0.0 && avg.z != 0.0) avg = normalize(avg);
+          g[index++] = avg;
+        }
+  }
+  s.grad.resize(3 * g.size());
+  for (size_t i = 0; i < g.size(); ++i) {
+    s.grad[3 * i] = to_half((float)g[i].x);
+    s.grad[3 * i + 1] = to_half((float)g[i].y);
+    s.grad[3 * i + 2] = to_half((float)g[i].z);
+  }
+  s.grad_ready = true;
+}
+
 }  // namespace
 
 extern "C" {
@@ -955,6 +1115,7 @@ int oracle_set_volume(void* h, const void* vox, int w, int hh, int d, int dtype,
   size_t n = (size_t)w * hh * d * (dtype == CVR_U8 ? 1 : 2);
   s.vox.assign((const uint8_t*)vox, (const uint8_t*)vox + n);
   s.sat_ready = s.pyr_ready = false;
+  s.grad_ready = false;
   return 0;
 }
 
@@ -1082,6 +1243,30 @@ int oracle_set_light_cache(void* h, int w, int hh, int d) {
   Scene& s = *(Scene*)h;
   if (w < 0 || hh < 0 || d < 0) return CVR_ERR_INVALID_ARG;
   s.lc[0] = w; s.lc[1] = hh; s.lc[2] = d;
+  return 0;
+}
+
+int oracle_build_gradient(void* h, const cvr_gradient_params* p) {
+  Scene& s = *(Scene*)h;
+  s.grad_ready = false;
+  s.grad.clear();
+  if (!p || p->model == CVR_GRADIENT_NONE) return 0;
+  if (p->model < 0 || p->model > CVR_GRADIENT_NONE || s.vox.empty()) return CVR_ERR_INVALID_ARG;
+  if (p->model == CVR_GRADIENT_FINITE_DIFFERENCES && p->sample_size < 1) return CVR_ERR_INVALID_ARG;
+  build_gradient(s, *p);
+  return 0;
+}
+
+int oracle_get_gradient(void* h, float* out) {
+  Scene& s = *(Scene*)h;
+  if (!s.grad_ready) return CVR_ERR_NOT_READY;
+  std::memcpy(out, s.grad.data(), sizeof(float) * s.grad.size());
+  return 0;
+}
+
+int oracle_set_blinn_phong(void* h, const cvr_blinn_phong* bp) {
+  if (!bp) return CVR_ERR_INVALID_ARG;
+  ((Scene*)h)->bp = *bp;
   return 0;
 }
 

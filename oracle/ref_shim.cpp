@@ -8,6 +8,8 @@
 //   * ConeGaussianSampler::ComputeConeIntegrationSteps
 //                                                (cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp:212-386)
 //   * RodriguesRotation                          (libs/math_utils/utils.cpp:149-156)
+//   * GenerateGradientTexture / GenerateSobelFeldmanGradientTexture
+//                                                (libs/volvis_utils/utils.cpp:146-351)
 // The GL texture classes those headers mention are stubbed below; no GL code
 // runs.  Private members of ConeGaussianSampler are read through the access
 // macro below (the interval list feeds the shader table but has no getter).
@@ -19,6 +21,8 @@
 #include <vis_utils/summedareatable.h>
 #include <volvis_utils/transferfunction1d.h>
 #include <math_utils/utils.h>
+#include <volvis_utils/structuredgridvolume.h>
+#include <volvis_utils/utils.h>
 #define private public
 #include "structured/rc1pdosct/conegaussiansampler.h"
 #undef private
@@ -32,6 +36,21 @@ bool Texture1D::SetData(GLvoid*, GLint, GLenum, GLenum) { return true; }
 GLuint Texture1D::GetTextureID() { return 0; }
 unsigned int Texture1D::GetLength() { return 0; }
 void ExitOnGLError(const char*) {}
+Texture2D::Texture2D(unsigned int, unsigned int) {}
+void Texture2D::GenerateTexture(GLint, GLint, GLint, GLint) {}
+bool Texture2D::SetData(GLvoid*, GLint, GLenum, GLenum) { return true; }
+// A 3D texture keeps its size; SetData hands the host array to the capture
+// buffer below (the gradient builders upload glm::vec3 RGB float texels).
+std::vector<float> g_tex3d_data;
+Texture3D::Texture3D(unsigned int w, unsigned int h, unsigned int d) : m_width(w), m_height(h), m_depth(d), m_textureID(0) {}
+Texture3D::~Texture3D() {}
+void Texture3D::GenerateTexture(GLint, GLint, GLint, GLint, GLint, bool) {}
+bool Texture3D::SetData(GLvoid* data, GLint, GLenum format, GLenum type) {
+  if (format != GL_RGB || type != GL_FLOAT) return false;
+  const float* f = static_cast<const float*>(data);
+  g_tex3d_data.assign(f, f + 3 * (size_t)m_width * m_height * m_depth);
+  return true;
+}
 }  // namespace gl
 
 namespace {
@@ -132,6 +151,32 @@ int ref_gt_vectors(int n_occ, float occ_ap, int n_sdw, float sdw_ap, unsigned se
     v = RodriguesRotation(v, phi, gtray);
     sdw[3 * i] = v.x; sdw[3 * i + 1] = v.y; sdw[3 * i + 2] = v.z;
   }
+  return 0;
+}
+
+// The reference's gradient texture contents (float RGB per voxel, before
+// the driver's RGB16F rounding) of a u8 (bytes 1) or u16 (bytes 2) volume.
+// model: 0 Sobel-Feldman, 1 finite differences (sample size, filter,
+// normalized as given).
+int ref_gradient(const void* vox, int w, int h, int d, int bytes, int model, int sample_size, int filter,
+                 int normalized, float* out) {
+  const size_t n = (size_t)w * h * d;
+  vis::StructuredGridVolume vol("shim", w, h, d);
+  if (bytes == 1) {
+    unsigned char* a = new unsigned char[n];
+    std::memcpy(a, vox, n);
+    vol.SetArrayData(a, vis::DataStorageSize::_8_BITS);  // the volume frees it
+  } else {
+    unsigned short* a = new unsigned short[n];
+    std::memcpy(a, vox, 2 * n);
+    vol.SetArrayData(a, vis::DataStorageSize::_16_BITS);
+  }
+  gl::g_tex3d_data.clear();
+  gl::Texture3D* t = model == 0 ? vis::GenerateSobelFeldmanGradientTexture(&vol)
+                                : vis::GenerateGradientTexture(&vol, sample_size, filter, normalized != 0);
+  delete t;
+  if (gl::g_tex3d_data.size() != 3 * n) return -1;
+  std::memcpy(out, gl::g_tex3d_data.data(), sizeof(float) * 3 * n);
   return 0;
 }
 

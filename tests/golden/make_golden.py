@@ -8,6 +8,8 @@ the committed .npz.  Every array is produced by reference code:
   cone_*      ConeGaussianSampler::ComputeConeIntegrationSteps
   gt_*        RodriguesRotation + std::default_random_engine as in
               RC1PConeLightGroundTruthSteps::Update
+  grad_*      GenerateSobelFeldmanGradientTexture / GenerateGradientTexture
+              (the float RGB texels they upload) on small u8 / u16 volumes
 The inputs (control points, grid values, sampler settings) are this
 project's own test values.
 
@@ -59,6 +61,27 @@ def arr(pts, n):
     return np.ascontiguousarray(a)
 
 
+# name: (model, gradient_sample_size, filter_nxnxn, normalized_gradient)
+GRADIENT_CASES = {
+    "sobel": (0, 1, 0, 1),
+    "fd": (1, 1, 0, 1),
+    "fd_n2_raw": (1, 2, 0, 0),
+    "fd_filter3": (1, 1, 3, 1),
+}
+
+
+def gradient_volumes():
+    """A u8 volume with a smooth blob, flat runs and noise (ragged dims), and
+    a u16 one with full-range values."""
+    rng = np.random.default_rng(11)
+    z, y, x = np.meshgrid(np.arange(8), np.arange(9), np.arange(10), indexing="ij")
+    blob = 255.0 * np.exp(-((x - 4.5) ** 2 + (y - 3.0) ** 2 + (z - 4.0) ** 2) / 9.0)
+    u8 = np.clip(blob + rng.integers(-3, 4, size=blob.shape), 0, 255).astype(np.uint8)
+    u8[:, :, 7:] = 40  # flat slab: zero gradients inside it
+    u16 = rng.integers(0, 65536, size=(6, 7, 5)).astype(np.uint16)
+    return {"u8": np.ascontiguousarray(u8), "u16": np.ascontiguousarray(u16)}
+
+
 def main():
     if not oracle.ref_available():
         raise SystemExit("reference checkout not available: cannot regenerate golden vectors")
@@ -107,6 +130,14 @@ def main():
                            P(sdw.ctypes.data))
         out[f"gt_{name}_occ"] = occ
         out[f"gt_{name}_sdw"] = sdw
+    for name, vol in gradient_volumes().items():
+        d, h, w = vol.shape
+        out[f"grad_{name}_volume"] = vol
+        for cfg, (model, n, filt, norm) in GRADIENT_CASES.items():
+            g = np.zeros((d, h, w, 3), np.float32)
+            r = ref.ref_gradient(P(vol.ctypes.data), w, h, d, vol.itemsize, model, n, filt, norm, P(g.ctypes.data))
+            assert r == 0
+            out[f"grad_{name}_{cfg}"] = g
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(out)} arrays)")
 

@@ -37,6 +37,7 @@ def test_usage_errors(data):
     assert run().returncode == 1
     assert run("--volume", data["vp"]).returncode == 1
     assert run("--bogus").returncode == 1
+    assert run("--gradient", "laplace").returncode == 1
 
 
 def test_data_errors_before_any_device_call(data, tmp_path):
@@ -100,3 +101,27 @@ def test_headless_surrogate_renderer(ctx, tmp_path):
     assert np.isfinite(img).all() and img.max() > 0.0
     r = run("--volume", vp, "--tf", tp, "--renderer", "s_1psurr", "--width", "16", "--height", "16")
     assert r.returncode != 0 and "network" in (r.stdout + r.stderr)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("abbr,model", [("s_1rc", "fd"), ("s_1pebs", "sobel"), ("s_1pdosct", "cs")])
+def test_headless_gradient_shading(data, abbr, model, tmp_path):
+    """--gradient picks DataManager's gradient model and --gradient-shading the
+    renderers' "Apply Gradient Shading" switch: the frame changes, opacity does not.
+    (With the cone renderer's default of no shadows the gradient branch only
+    differs from the plain one where the gradient vanishes, so shadows are on.)"""
+    illum = ["--occlusion", "1", "--shadow", "1"] if abbr == "s_1pdosct" else []
+
+    def frame(*extra):
+        out = tmp_path / f"{abbr}_{len(extra)}.pfm"
+        r = run("--volume", data["vp"], "--tf", data["tp"], "--renderer", abbr, "--width", "40", "--height", "32",
+                "--cameras", data["cp"], "--camera-index", "0", "--lights", data["lp"], "--out", out, *illum,
+                *extra)
+        assert r.returncode == 0, r.stderr
+        raw = out.read_bytes()
+        return np.frombuffer(raw[raw.index(b"-1.0\n") + 5:], np.float32).reshape(32, 40, 3)
+    plain = frame()
+    model_only = frame("--gradient", model)
+    shaded = frame("--gradient", model, "--gradient-shading", "1")
+    assert np.array_equal(plain, model_only)  # a gradient alone changes nothing
+    assert np.isfinite(shaded).all() and not np.array_equal(shaded, plain)
