@@ -4,9 +4,9 @@
 // per-frame gradient-shading arguments of the marchers.
 //
 // The reference computes the gradient on the host in double precision
-// (utils.cpp:146-351) and uploads it as RGB16F; here one thread per voxel
-// forms the same stencils from the integer voxel values (exact), scales once
-// in FP32 and stores four FP16 values (x, y, z, 0: one 8-byte load per tap).
+// (utils.cpp:146-351) and uploads it as RGB16F; here the same stencils are
+// formed from the integer voxel values (exact), scaled once in FP32 and
+// stored as four FP16 values (x, y, z, 0: one 8-byte load per tap).
 #include <cuda_fp16.h>
 
 #include "ctx.cuh"
@@ -28,6 +28,48 @@ struct GradBuild {
   float inv_max;  // 1/255 or 1/65535
 };
 
+// GenerateGradientTexture's per-voxel result from the integer differences
+// s2 - s1 (utils.cpp:156-193), its filter step (utils.cpp:196-233), and the
+// FP16 store.
+__device__ __forceinline__ void fd_finish(const GradBuild& b, float dx, float dy, float dz, float& gx, float& gy,
+                                          float& gz) {
+  if (b.normalized) {
+    // normalize(s2 - s1) is normalize of the integer differences (the common
+    // 1/255 scale cancels); the zero vector gives NaN there, then 0.
+    // glm::normalize: v * inversesqrt(dot(v, v))
+    const float l2 = dx * dx + dy * dy + dz * dz;
+    if (l2 > 0.0f) {
+      const float il = 1.0f / sqrtf(l2);
+      gx = dx * il; gy = dy * il; gz = dz * il;
+    } else {
+      gx = gy = gz = 0.0f;
+    }
+  } else {
+    // s2s1 / 2.0f * (float)gradient_sample_size
+    const float k = b.inv_max * 0.5f * float(b.n);
+    gx = dx * k; gy = dy * k; gz = dz * k;
+  }
+  if (b.filter > 0 && gx != 0.0f && gy != 0.0f && gz != 0.0f) {
+    // The filter sums gradients[x, y, z] -- the centre, not the neighbour --
+    // over the in-bounds window and divides by the count, so the average is
+    // the centre itself; it is then normalised when no component is zero.
+    const float il = 1.0f / sqrtf(gx * gx + gy * gy + gz * gz);
+    gx *= il; gy *= il; gz *= il;
+  }
+}
+
+__device__ __forceinline__ void store_grad(uint2* __restrict__ out, size_t i, float gx, float gy, float gz) {
+  const __half2 xy = __floats2half2_rn(gx, gy);
+  const __half2 zw = __floats2half2_rn(gz, 0.0f);
+  uint2 o;
+  o.x = *reinterpret_cast<const unsigned int*>(&xy);
+  o.y = *reinterpret_cast<const unsigned int*>(&zw);
+  out[i] = o;
+}
+
+// Any model and sample size: one thread per voxel, neighbours straight from
+// global memory (finite differences with gradient_sample_size > 1 reach n
+// voxels away).
 template <class T>
 __global__ void __launch_bounds__(256) k_gradient(const T* __restrict__ v, int nx, int ny, int nz, GradBuild b,
                                                   uint2* __restrict__ out) {
@@ -37,34 +79,11 @@ __global__ void __launch_bounds__(256) k_gradient(const T* __restrict__ v, int n
   if (x >= nx || y >= ny || z >= nz) return;
   float gx, gy, gz;
   if (b.model == CVR_GRADIENT_FINITE_DIFFERENCES) {
-    // GenerateGradientTexture step 1 (utils.cpp:156-193): s2 - s1 over +-n.
     const int n = b.n;
     const float dx = float(vox(v, nx, ny, nz, x + n, y, z) - vox(v, nx, ny, nz, x - n, y, z));
     const float dy = float(vox(v, nx, ny, nz, x, y + n, z) - vox(v, nx, ny, nz, x, y - n, z));
     const float dz = float(vox(v, nx, ny, nz, x, y, z + n) - vox(v, nx, ny, nz, x, y, z - n));
-    if (b.normalized) {
-      // normalize(s2 - s1) is normalize of the integer differences (the common
-      // 1/255 scale cancels); the zero vector gives NaN there, then 0.
-      const float l2 = dx * dx + dy * dy + dz * dz;
-      if (l2 > 0.0f) {
-        const float l = sqrtf(l2);
-        gx = dx / l; gy = dy / l; gz = dz / l;
-      } else {
-        gx = gy = gz = 0.0f;
-      }
-    } else {
-      // s2s1 / 2.0f * (float)gradient_sample_size
-      const float k = b.inv_max * 0.5f * float(n);
-      gx = dx * k; gy = dy * k; gz = dz * k;
-    }
-    if (b.filter > 0 && gx != 0.0f && gy != 0.0f && gz != 0.0f) {
-      // Step 2 (utils.cpp:196-233) sums gradients[x, y, z] -- the centre, not
-      // the neighbour -- over the in-bounds window and divides by the count,
-      // so the average is the centre itself; it is then normalised when no
-      // component is zero.
-      const float l = sqrtf(gx * gx + gy * gy + gz * gz);
-      gx /= l; gy /= l; gz /= l;
-    }
+    fd_finish(b, dx, dy, dz, gx, gy, gz);
   } else {
     // Sobel-Feldman (utils.cpp:295-321, sobelfeldman_generator.comp:37-60):
     // weights 4 / 2^(|v1|+|v2|) on the planes at -1 minus those at +1.
@@ -81,12 +100,99 @@ __global__ void __launch_bounds__(256) k_gradient(const T* __restrict__ v, int n
     }
     gx = float(sx) * b.inv_max; gy = float(sy) * b.inv_max; gz = float(sz) * b.inv_max;
   }
-  const __half2 xy = __floats2half2_rn(gx, gy);
-  const __half2 zw = __floats2half2_rn(gz, 0.0f);
-  uint2 o;
-  o.x = *reinterpret_cast<const unsigned int*>(&xy);
-  o.y = *reinterpret_cast<const unsigned int*>(&zw);
-  out[(size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z)] = o;
+  store_grad(out, (size_t)x + (size_t)nx * ((size_t)y + (size_t)ny * z), gx, gy, gz);
+}
+
+// The 3x3x3 stencils (Sobel-Feldman, finite differences of sample size 1),
+// HBM-bound form: a CTA owns a 32 x 8 column of voxels and walks kGradZ
+// planes along z with the planes z-1, z, z+1 of its tile (plus a one-voxel
+// halo, 0 outside the grid) in a shared-memory ring, so each voxel is read
+// from memory about once and the 8-byte results stream out coalesced.  The
+// (x, y) part of every load address and bounds test is computed once per
+// thread; a plane costs each thread one or two loads.
+constexpr int kGradTX = 32, kGradTY = 8, kGradZ = 32;
+constexpr int kGradPW = kGradTX + 2, kGradPH = kGradTY + 2;
+constexpr int kGradHalo = kGradPW * kGradPH - kGradTX * kGradTY;  // 84 halo cells
+
+template <class T>
+__global__ void __launch_bounds__(kGradTX * kGradTY) k_gradient_tiled(const T* __restrict__ v, int nx, int ny, int nz,
+                                                                      GradBuild b, uint2* __restrict__ out) {
+  __shared__ int ring[3][kGradPH][kGradPW];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kGradTX + tx;
+  const int x0 = blockIdx.x * kGradTX, y0 = blockIdx.y * kGradTY, z0 = blockIdx.z * kGradZ;
+  const int z1 = min(z0 + kGradZ, nz);
+  const size_t plane = (size_t)nx * ny;
+  // this thread's interior cell and, for the first kGradHalo threads, one halo cell
+  const int x = x0 + tx, y = y0 + ty;
+  const bool in_xy = x < nx && y < ny;
+  const size_t off_xy = in_xy ? (size_t)x + (size_t)nx * y : 0;
+  int hx = 0, hy = 0;
+  bool h_on = false, h_xy = false;
+  size_t h_off = 0;
+  if (tid < kGradHalo) {
+    // halo ring of the (kGradPW x kGradPH) tile: top row, bottom row, then the side columns
+    if (tid < kGradPW) { hx = tid; hy = 0; }
+    else if (tid < 2 * kGradPW) { hx = tid - kGradPW; hy = kGradPH - 1; }
+    else { const int k = tid - 2 * kGradPW; hx = (k & 1) ? kGradPW - 1 : 0; hy = 1 + (k >> 1); }
+    h_on = true;
+    const int gx = x0 + hx - 1, gy = y0 + hy - 1;
+    h_xy = gx >= 0 && gy >= 0 && gx < nx && gy < ny;
+    h_off = h_xy ? (size_t)gx + (size_t)nx * gy : 0;
+  }
+  // a plane's two cells of this thread: fetched into registers one plane
+  // ahead, so the loads are in flight while the current plane is computed
+  int pv = 0, ph = 0;
+  auto fetch = [&](int z) {
+    const bool zin = z >= 0 && z < nz;
+    const size_t zo = zin ? plane * (size_t)z : 0;
+    pv = (zin && in_xy) ? (int)__ldg(v + zo + off_xy) : 0;
+    ph = (zin && h_xy) ? (int)__ldg(v + zo + h_off) : 0;
+  };
+  auto put = [&](int slot) {
+    ring[slot][ty + 1][tx + 1] = pv;
+    if (h_on) ring[slot][hy][hx] = ph;
+  };
+  int s0 = 0, sm = 1, sp = 2;  // ring slots of the planes z - 1, z, z + 1
+  fetch(z0 - 1);
+  put(s0);
+  fetch(z0);
+  put(sm);
+  fetch(z0 + 1);
+  const bool sobel = b.model != CVR_GRADIENT_FINITE_DIFFERENCES;
+  const int cx = tx + 1, cy = ty + 1;
+  uint2* o = out + off_xy + plane * (size_t)z0;
+  for (int z = z0; z < z1; ++z, o += plane) {
+    put(sp);         // plane z + 1
+    fetch(z + 2);    // lands during this plane's stencil
+    __syncthreads();
+    if (in_xy) {
+      float gx, gy, gz;
+      if (sobel) {
+        int sx = 0, sy = 0, sz = 0;
+#pragma unroll
+        for (int v1 = -1; v1 <= 1; ++v1) {
+#pragma unroll
+          for (int v2 = -1; v2 <= 1; ++v2) {
+            const int w = 4 >> ((v1 < 0 ? -v1 : v1) + (v2 < 0 ? -v2 : v2));
+            const int pz = v2 < 0 ? s0 : (v2 > 0 ? sp : sm);  // plane z + v2
+            const int qz = v1 < 0 ? s0 : (v1 > 0 ? sp : sm);  // plane z + v1
+            sz += w * (ring[s0][cy + v2][cx + v1] - ring[sp][cy + v2][cx + v1]);
+            sy += w * (ring[pz][cy - 1][cx + v1] - ring[pz][cy + 1][cx + v1]);
+            sx += w * (ring[qz][cy + v2][cx - 1] - ring[qz][cy + v2][cx + 1]);
+          }
+        }
+        gx = float(sx) * b.inv_max; gy = float(sy) * b.inv_max; gz = float(sz) * b.inv_max;
+      } else {
+        const float dx = float(ring[sm][cy][cx + 1] - ring[sm][cy][cx - 1]);
+        const float dy = float(ring[sm][cy + 1][cx] - ring[sm][cy - 1][cx]);
+        const float dz = float(ring[sp][cy][cx] - ring[s0][cy][cx]);
+        fd_finish(b, dx, dy, dz, gx, gy, gz);
+      }
+      store_grad(o, 0, gx, gy, gz);
+    }
+    __syncthreads();  // the next iteration overwrites the slot of z - 1
+    const int t = s0; s0 = sm; sm = sp; sp = t;
+  }
 }
 
 __global__ void k_gradient_to_float(const uint2* __restrict__ g, float* __restrict__ out, long long n) {
@@ -113,14 +219,26 @@ cvr_status build_gradient(cvr_ctx* c) {
   const size_t n = (size_t)c->nx * c->ny * c->nz;
   CK(c, ensure(c->d_grad, c->grad_cap, n * sizeof(uint2)));
   GradBuild b{p.model, p.sample_size, p.filter_nxnxn, p.normalized, c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f};
-  const dim3 block(32, 4, 2);
-  const dim3 grid((c->nx + 31) / 32, (c->ny + 3) / 4, (c->nz + 1) / 2);
-  if (c->dtype == CVR_U8)
-    k_gradient<uint8_t><<<grid, block, 0, c->stream>>>(static_cast<const uint8_t*>(c->d_vol), c->nx, c->ny, c->nz, b,
-                                                       c->d_grad);
-  else
-    k_gradient<uint16_t><<<grid, block, 0, c->stream>>>(static_cast<const uint16_t*>(c->d_vol), c->nx, c->ny, c->nz,
-                                                        b, c->d_grad);
+  const bool u8 = c->dtype == CVR_U8;
+  if (p.model != CVR_GRADIENT_FINITE_DIFFERENCES || p.sample_size == 1) {
+    const dim3 block(kGradTX, kGradTY, 1);
+    const dim3 grid((c->nx + kGradTX - 1) / kGradTX, (c->ny + kGradTY - 1) / kGradTY, (c->nz + kGradZ - 1) / kGradZ);
+    if (u8)
+      k_gradient_tiled<uint8_t><<<grid, block, 0, c->stream>>>(static_cast<const uint8_t*>(c->d_vol), c->nx, c->ny,
+                                                               c->nz, b, c->d_grad);
+    else
+      k_gradient_tiled<uint16_t><<<grid, block, 0, c->stream>>>(static_cast<const uint16_t*>(c->d_vol), c->nx, c->ny,
+                                                                c->nz, b, c->d_grad);
+  } else {
+    const dim3 block(32, 4, 2);
+    const dim3 grid((c->nx + 31) / 32, (c->ny + 3) / 4, (c->nz + 1) / 2);
+    if (u8)
+      k_gradient<uint8_t><<<grid, block, 0, c->stream>>>(static_cast<const uint8_t*>(c->d_vol), c->nx, c->ny, c->nz,
+                                                         b, c->d_grad);
+    else
+      k_gradient<uint16_t><<<grid, block, 0, c->stream>>>(static_cast<const uint16_t*>(c->d_vol), c->nx, c->ny,
+                                                          c->nz, b, c->d_grad);
+  }
   CK(c, cudaGetLastError());
   c->grad_ready = true;
   c->tex.grad_valid = false;

@@ -60,7 +60,9 @@ __device__ __forceinline__ bool blinn_terms(const FrameArgs& f, float3 tx, Blinn
   const float3 e = normalize3(f.cam.eye - w);
   const float3 hv = normalize3(e + l);
   t.diff = fmaxf(0.0f, dot3(n, l));
-  t.spec = powf(fmaxf(0.0f, dot3(hv, n)), f.grad.shininess);
+  // pow(x, N) = exp2(N log2 x) on the special-function unit (relative error
+  // ~1e-6 for N = 30; 0 at x = 0 as GLSL's pow gives for N > 0)
+  t.spec = __powf(fmaxf(0.0f, dot3(hv, n)), f.grad.shininess);
   return true;
 }
 
