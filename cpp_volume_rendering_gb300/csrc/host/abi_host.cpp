@@ -156,6 +156,23 @@ cvr_status cvr_read_volume_info(const char* path, int dims[3], int* dtype, float
     if (ok != 3 || w <= 0 || h <= 0 || d <= 0) return CVR_ERR_FORMAT;
     dims[0] = w; dims[1] = h; dims[2] = d;
     *dtype = CVR_U8;
+  } else if (ext == "pvm" || ext == "pvmold" || ext == "nrrd" || ext == "nhrd" || ext == "dat") {
+    // the header of a DDS-compressed .pvm sits inside the compressed stream: read it whole
+    vis::StructuredGridVolume v;
+    std::string err;
+    if (!vis::ReadStructuredVolume(p, &v, &err)) {
+      FILE* f = std::fopen(path, "rb");
+      if (!f) return CVR_ERR_IO;
+      std::fclose(f);
+      return (err.find("short") != std::string::npos || err.find("opening") != std::string::npos) ? CVR_ERR_IO
+                                                                                                     : CVR_ERR_FORMAT;
+    }
+    dims[0] = v.GetWidth(); dims[1] = v.GetHeight(); dims[2] = v.GetDepth();
+    *dtype = v.GetStorage() == vis::DataStorageSize::_16_BITS ? CVR_U16 : CVR_U8;
+    if (spacing) {
+      spacing[0] = (float)v.GetScaleX(); spacing[1] = (float)v.GetScaleY(); spacing[2] = (float)v.GetScaleZ();
+    }
+    return CVR_OK;
   } else {
     return CVR_ERR_UNSUPPORTED;
   }
@@ -171,7 +188,8 @@ cvr_status cvr_read_volume(const char* path, void* host_out, size_t out_bytes) {
     FILE* f = std::fopen(path, "rb");
     if (!f) return CVR_ERR_IO;
     std::fclose(f);
-    return err.find("short") != std::string::npos ? CVR_ERR_IO : CVR_ERR_FORMAT;
+    return (err.find("short") != std::string::npos || err.find("opening") != std::string::npos) ? CVR_ERR_IO
+                                                                                                   : CVR_ERR_FORMAT;
   }
   size_t n = v.GetNumVoxels() * v.GetBytesPerVoxel();
   if (out_bytes < n) return CVR_ERR_INVALID_ARG;

@@ -143,6 +143,9 @@ bool ReadStructuredVolume(const std::string& path, StructuredGridVolume* out, st
   std::string ext = dot == std::string::npos ? std::string() : path.substr(dot + 1);
   if (ext == "raw") return read_raw(path, out, err);
   if (ext == "syn") return read_syn(path, out, err);
+  if (ext == "pvm" || ext == "pvmold") return ReadPVM(path, out, err);  // one format, two reference loaders
+  if (ext == "nrrd" || ext == "nhrd") return ReadNRRD(path, out, err);
+  if (ext == "dat") return ReadDAT(path, out, err);
   if (err) *err = "unsupported volume format: ." + ext;
   return false;
 }

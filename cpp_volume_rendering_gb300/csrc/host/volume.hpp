@@ -1,5 +1,5 @@
 // volume.hpp — host mirror of vis::StructuredGridVolume and its readers
-// (libs/volvis_utils/structuredgridvolume.h:40-88, reader.cpp:28-371,
+// (libs/volvis_utils/structuredgridvolume.h:40-88, reader.cpp:28-628,
 // libs/file_utils/rawloader.cpp:5-42).
 #pragma once
 
@@ -49,9 +49,14 @@ class StructuredGridVolume {
 // (reader.cpp:162-225).  Returns false on a malformed name.
 bool ParseRawName(const std::string& path, int* w, int* h, int* d, int* bytes_per_value);
 
-// VolumeReader::ReadStructuredVolume dispatch on the extension (.raw, .syn).
-// Returns false (with a message) instead of exiting on a missing or short file.
+// VolumeReader::ReadStructuredVolume dispatch on the extension (.raw, .syn,
+// .pvm / .pvmold, .nrrd / .nhrd, .dat).  Returns false (with a message)
+// instead of exiting on a missing, short or malformed file.
 bool ReadStructuredVolume(const std::string& path, StructuredGridVolume* out, std::string* err);
+// The readers of readers.cpp (also reached through ReadStructuredVolume).
+bool ReadPVM(const std::string& path, StructuredGridVolume* out, std::string* err);
+bool ReadNRRD(const std::string& path, StructuredGridVolume* out, std::string* err);
+bool ReadDAT(const std::string& path, StructuredGridVolume* out, std::string* err);
 
 // Camera / light list files (camerastatelist.cpp:26-87, lightsourcelist.cpp:81-148).
 struct CameraState {

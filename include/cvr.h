@@ -506,8 +506,13 @@ cvr_status cvr_tf_ext_per_value(int max_density, int n_rgb, const double* rgb_po
 cvr_status cvr_read_tf1d(const char* path, int* max_density, int* extinction_input,
                          int* n_rgb, double* rgb_points, int max_rgb,
                          int* n_alpha, double* alpha_points, int max_alpha);
-/* .raw / .syn reader header: dims and dtype from the file (readraw name convention
- * "name.<bytes>.<W>x<H>x<D>.raw", reader.cpp:162-225; readsyn, reader.cpp:283-371). */
+/* Volume file header: dims, dtype and voxel spacing, by extension as
+ * VolumeReader::ReadStructuredVolume (reader.cpp:28-58): .raw (name convention
+ * "name.<bytes>.<W>x<H>x<D>.raw", reader.cpp:162-225), .syn (reader.cpp:283-371),
+ * .pvm / .pvmold (V^3 PVM, plain or DDS-compressed, readpvm reader.cpp:100-160),
+ * .nrrd / .nhrd (detached header, reader.cpp:373-496), .dat (reader.cpp:498-628).
+ * CVR_ERR_IO: missing or short file; CVR_ERR_FORMAT: malformed;
+ * CVR_ERR_UNSUPPORTED: other extensions. */
 cvr_status cvr_read_volume_info(const char* path, int dims[3], int* dtype, float spacing[3]);
 /* Reads the voxels into host_out (W*H*D*bytes). */
 cvr_status cvr_read_volume(const char* path, void* host_out, size_t out_bytes);

@@ -4,7 +4,8 @@ Compiles the reference's own CPU table builders from its sources, in place
 (nothing is copied into this repository), together with oracle/ref_shim.cpp:
   libs/volvis_utils/transferfunction1d.cpp, transferfunction.cpp,
   libs/volvis_utils/utils.cpp, structuredgridvolume.cpp, gridvolume.cpp
-  (the gradient builders),
+  (the gradient builders), libs/file_utils/pvm.cpp (the PVM / DDS reader; its
+  MSVC runtime calls are mapped by oracle/ref_compat.h),
   libs/math_utils/utils.cpp,
   cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp,
   libs/vis_utils/summedareatable.h (header only).
@@ -42,12 +43,13 @@ def build(verbose: bool = False) -> Path | None:
         ref / "libs/volvis_utils/utils.cpp",
         ref / "libs/volvis_utils/structuredgridvolume.cpp",
         ref / "libs/volvis_utils/gridvolume.cpp",
+        ref / "libs/file_utils/pvm.cpp",
     ]
     if LIB.exists() and all(s.stat().st_mtime < LIB.stat().st_mtime for s in srcs):
         return LIB
     OUT.mkdir(exist_ok=True)
     cmd = ["g++", "-O2", "-fPIC", "-shared", "-std=c++14", "-ffp-contract=off", "-fopenmp", "-w", "-fpermissive",
-           "-DGLEW_NO_GLU", "-DGLEW_STATIC",
+           "-DGLEW_NO_GLU", "-DGLEW_STATIC", "-include", str(HERE / "ref_compat.h"),
            # math_utils/matrix.h is not needed by these files and trips a GCC
            # template-shadowing error; its include guard is pre-defined.
            "-DMATH_UTILS_T_MATRIX_H",

@@ -10,6 +10,7 @@
 //   * RodriguesRotation                          (libs/math_utils/utils.cpp:149-156)
 //   * GenerateGradientTexture / GenerateSobelFeldmanGradientTexture
 //                                                (libs/volvis_utils/utils.cpp:146-351)
+//   * Pvm (DDSV3::readPVMvolume + PostProcessData) (libs/file_utils/pvm.cpp:23-108,191-309)
 // The GL texture classes those headers mention are stubbed below; no GL code
 // runs.  Private members of ConeGaussianSampler are read through the access
 // macro below (the interval list feeds the shader table but has no getter).
@@ -23,6 +24,7 @@
 #include <math_utils/utils.h>
 #include <volvis_utils/structuredgridvolume.h>
 #include <volvis_utils/utils.h>
+#include <file_utils/pvm.h>
 #define private public
 #include "structured/rc1pdosct/conegaussiansampler.h"
 #undef private
@@ -177,6 +179,23 @@ int ref_gradient(const void* vox, int w, int h, int d, int bytes, int model, int
   delete t;
   if (gl::g_tex3d_data.size() != 3 * n) return -1;
   std::memcpy(out, gl::g_tex3d_data.data(), sizeof(float) * 3 * n);
+  return 0;
+}
+
+// The reference's .pvm loader (readpvm's Pvm object): dims, bytes per voxel,
+// spacing and the voxels (u8, or u16 as PostProcessData assembles them).
+// The reference exits the process on a malformed file: valid files only.
+int ref_read_pvm(const char* path, int* dims, int* components, double* scale, void* out, size_t out_bytes) {
+  Pvm p(path);
+  unsigned int w, h, d;
+  p.GetDimensions(&w, &h, &d);
+  dims[0] = (int)w; dims[1] = (int)h; dims[2] = (int)d;
+  *components = p.GetComponents();
+  p.GetScale(&scale[0], &scale[1], &scale[2]);
+  const size_t n = (size_t)w * h * d * (size_t)(*components);
+  if (!out) return 0;
+  if (out_bytes < n || !p.GetData()) return -1;
+  std::memcpy(out, p.GetData(), n);
   return 0;
 }
 

@@ -125,3 +125,15 @@ def test_headless_gradient_shading(data, abbr, model, tmp_path):
     shaded = frame("--gradient", model, "--gradient-shading", "1")
     assert np.array_equal(plain, model_only)  # a gradient alone changes nothing
     assert np.isfinite(shaded).all() and not np.array_equal(shaded, plain)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fixture", ["smooth_v3e_strip143.pvm", "wide_u16_v3_dds_skip2.pvm"])
+def test_headless_reads_pvm(data, fixture, tmp_path):
+    """A DDS-compressed .pvm goes through ReadStructuredVolume to a frame."""
+    vol = Path(__file__).resolve().parent / "golden" / "pvm" / fixture
+    out = tmp_path / "pvm.pfm"
+    r = run("--volume", vol, "--tf", data["tp"], "--renderer", "s_1rc", "--width", "24", "--height", "24",
+            "--eye", "0", "0", "40", "--out", out)
+    assert r.returncode == 0, r.stderr
+    assert out.stat().st_size > 24 * 24 * 12
