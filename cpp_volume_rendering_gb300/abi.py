@@ -41,6 +41,9 @@ MLP_NOALLOC_MAX_POINTS = 8192
 MAX_VOLUMES = 16
 MAX_CONE_SECTIONS = 512
 GRADIENT_SOBEL_FELDMAN, GRADIENT_FINITE_DIFFERENCES, GRADIENT_COMPUTE_SOBEL, GRADIENT_NONE = 0, 1, 2, 3
+MULTISCALE_SINGLE, MULTISCALE_MULTISAMPLE, MULTISCALE_DOWNSCALE, MULTISCALE_UPSCALE = 0, 1, 2, 3
+(FILTER_BOX, FILTER_HAT, FILTER_CATMULL_ROM, FILTER_MITCHELL_NETRAVALI, FILTER_CARDINAL_BSPLINE3,
+ FILTER_CARDINAL_OMOMS3) = range(6)
 
 F3 = C.c_float * 3
 
@@ -178,6 +181,10 @@ SIGNATURES = {
     "cvr_download_light_cache": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_brick_size": (_I, [_P, _I]),
     "cvr_get_brick_size": (_I, [_P]),
+    "cvr_set_multiscaling": (_I, [_P, _I, _I, _I, _I]),
+    "cvr_get_multiscaling": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                  C.POINTER(C.c_int)]),
+    "cvr_rescale_frame": (_I, [_P, _I, _I, _P, _I, _I, _P, _I, _I]),
     "cvr_build_gradient": (_I, [_P, C.POINTER(GradientParams)]),
     "cvr_download_gradient": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_blinn_phong": (_I, [_P, C.POINTER(BlinnPhong)]),

@@ -82,6 +82,8 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   }
   if (c->lc_dims[0] > 0)
     return fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: the light cache is per frame, not batched (turn it off)");
+  if (c->ms_mode != CVR_MULTISCALE_SINGLE)
+    return fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: multiscaling is per frame, not batched (turn it off)");
   CK(c, cudaSetDevice(c->device));
   CK(c, cudaStreamSynchronize(c->stream));
   std::unique_ptr<cvr_batch> b(new cvr_batch());

@@ -239,7 +239,7 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad};
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -473,9 +473,39 @@ cvr_status cvr_set_gt_kernels(cvr_ctx* c, const float* occ, int n_occ, const flo
 }
 
 
+static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
+                               const void* params, size_t params_size, float* out, int w, int h, uint32_t* counts,
+                               cvr_frame_stats* stats);
+
+// A frame of the context's multiscaling mode: the marcher renders the
+// generated frame into the context's buffer, the post-pass writes out.
 static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
                               const void* params, size_t params_size, float* out, int w, int h, uint32_t* counts,
                               cvr_frame_stats* stats) {
+  if (!c || c->ms_mode == CVR_MULTISCALE_SINGLE)
+    return render_frame(c, method, cam, light, params, params_size, out, w, h, counts, stats);
+  if (counts) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: per-pixel step counts with multiscaling");
+  if (!out || w <= 0 || h <= 0) return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: bad arguments");
+  int gw, gh;
+  multiscale_size(c->ms_mode, c->ms_fw, c->ms_fh, w, h, &gw, &gh);
+  if (gw < 1 || gh < 1 || gw > 32768 || gh > 32768)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: multiscaled frame size out of range");
+  CK(c, cudaSetDevice(c->device));
+  CK(c, ensure(c->d_ms, c->ms_cap, (size_t)gw * gh * sizeof(float4)));
+  // the camera keeps the output's aspect (u_CameraAspectRatio is the screen's)
+  cvr_camera cm = cam ? *cam : cvr_camera{};
+  if (cam && !(cm.aspect > 0.0f)) cm.aspect = (float)w / (float)h;
+  cvr_status s = render_frame(c, method, cam ? &cm : nullptr, light, params, params_size,
+                              reinterpret_cast<float*>(c->d_ms), gw, gh, nullptr, stats);
+  if (s != CVR_OK) return s;
+  CK(c, launch_multiscale(c->ms_mode, c->ms_kernel, c->d_ms, gw, gh, reinterpret_cast<float4*>(out), w, h,
+                          c->stream));
+  return CVR_OK;
+}
+
+static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
+                               const void* params, size_t params_size, float* out, int w, int h, uint32_t* counts,
+                               cvr_frame_stats* stats) {
   if (!c) return CVR_ERR_INVALID_ARG;
   CK(c, cudaSetDevice(c->device));
   FrameArgs f;

@@ -207,6 +207,10 @@ struct cvr_ctx {
   bool grad_ready = false;
   cvr_gradient_params grad_params{CVR_GRADIENT_NONE, 1, 0, 1};
   cvr_blinn_phong bp{0, 0.5f, 0.5f, 0.8f, 30.0f, {1.0f, 1.0f, 1.0f}};
+  // pixel multiscaling (cvr_set_multiscaling) and its generated-frame buffer
+  int ms_mode = CVR_MULTISCALE_SINGLE, ms_kernel = CVR_FILTER_HAT, ms_fw = 2, ms_fh = 2;
+  float4* d_ms = nullptr;
+  size_t ms_cap = 0;
 };
 
 // Exchanges the current-volume fields of c with slot s.
@@ -320,6 +324,11 @@ cvr_status ensure_gradient_texture(cvr_ctx* c);
 // Gradient shading of a frame of 'method' (f->grad; off unless cvr_set_blinn_phong
 // applies it and the volume has a gradient model, built here when stale).
 cvr_status grad_args(cvr_ctx* c, int method, const cvr_light* light, FrameArgs* f);
+// Pixel multiscaling (postpass.cu): the generated frame's size for an output of
+// w x h, and the post-pass from it (modified in place by up-scaling filters).
+void multiscale_size(int mode, int fw, int fh, int w, int h, int* gw, int* gh);
+cudaError_t launch_multiscale(int mode, int kern, float4* src, int gw, int gh, float4* dst, int w, int h,
+                              cudaStream_t st);
 // The volume as the marchers read it: the plain layout, or the bricked copy
 // of the context's brick size (made on first use after the volume changed).
 cvr_status render_volume_view(cvr_ctx* c, VolumeView* v);

@@ -155,6 +155,10 @@ bool BaseVolumeRenderer::Redraw() {
   bp.shininess = rp->GetBlinnPhongNshininess();
   rp->LightSpecular(bp.specular);
   if (!CheckABI(cvr_set_blinn_phong(m_ctx, &bp), "Redraw")) return false;
+  // Redraw / MultiSampleRedraw / DownScalingRedraw / UpScalingRedraw
+  // (renderingmanager.cpp:1196-1218) by the current mode
+  if (!CheckABI(cvr_set_multiscaling(m_ctx, GetCurrentMultiScalingMode(), (int)m_kernel_filter, 2, 2), "Redraw"))
+    return false;
   return CheckABI(cvr_render(m_ctx, Method(), &m_cam, &m_light, p, n, m_frame, m_width, m_height, nullptr, &m_stats),
                   "Redraw");
 }
@@ -234,7 +238,9 @@ const void* RayCasting1Pass::Params(size_t* size) {
 }
 
 // ------------------------------------------------------------ rc1pextbsd
-RC1PExtinctionBasedShading::RC1PExtinctionBasedShading() {}
+RC1PExtinctionBasedShading::RC1PExtinctionBasedShading() {
+  vr_pixel_multiscaling_support = true;  // ebsrenderer.cpp:51
+}
 
 bool RC1PExtinctionBasedShading::Init(int w, int h) {
   if (!BeginInit(w, h)) return false;

@@ -132,6 +132,16 @@ class BaseVolumeRenderer {
   // (m_apply_gradient_shading / m_apply_gradient, default false).
   void SetApplyGradientShading(bool on) { m_apply_gradient_shading = on; SetOutdated(); }
   bool GetApplyGradientShading() const { return m_apply_gradient_shading; }
+  // MULTISCALING (volrenderbase.h:28-33, volrenderbase.cpp:101-114): modes 0..3,
+  // honoured only by renderers that declare support (the reference: the
+  // extinction renderer, ebsrenderer.cpp:51); 2 x 2 factors
+  // (MULTISAMPLE_NUMBEROFSAMPLES_W/H); the image kernel of RenderFrameToScreen
+  // (IMAGE_FILTER_KERNEL, default K2_HAT).
+  bool IsPixelMultiScalingSupported() const { return vr_pixel_multiscaling_support; }
+  int GetCurrentMultiScalingMode() const { return IsPixelMultiScalingSupported() ? vr_pixel_multiscaling_mode : 0; }
+  void SetCurrentMultiScalingMode(int f) { vr_pixel_multiscaling_mode = f; SetOutdated(); }
+  unsigned int GetImageKernelFilter() const { return m_kernel_filter; }
+  void SetImageKernelFilter(unsigned int k) { m_kernel_filter = k; SetOutdated(); }
 
   // volrenderbase.cpp:77-84: Update only when outdated.
   bool PrepareRender(const vis::Camera& camera);
@@ -156,6 +166,9 @@ class BaseVolumeRenderer {
 
   bool vr_built = false, vr_outdated = true;
   bool m_apply_gradient_shading = false;
+  bool vr_pixel_multiscaling_support = false;
+  int vr_pixel_multiscaling_mode = 0;
+  unsigned int m_kernel_filter = CVR_FILTER_HAT;
   vis::DataManager* m_ext_data_manager = nullptr;
   vis::RenderingParameters* m_ext_rendering_parameters = nullptr;
   cvr_ctx* m_ctx = nullptr;

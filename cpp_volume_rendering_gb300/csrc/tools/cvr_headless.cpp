@@ -9,6 +9,7 @@
 //                [--cameras LIST --camera-index i] [--lights LIST --light-index i]
 //                [--eye x y z] [--fovy deg] [--occlusion 0|1] [--shadow 0|1]
 //                [--gradient sobel|fd|cs|none] [--gradient-shading 0|1]
+//                [--multiscaling 0..3] [--image-filter 0..5]
 //                [--out frame.pfm]
 // Exit code 0 on success, 1 on a usage error, 2 on a data error, 3 on a
 // rendering error; messages go to stderr.
@@ -26,6 +27,7 @@ static int usage() {
                "       [--cameras FILE --camera-index I] [--lights FILE --light-index I] [--eye X Y Z]\n"
                "       [--fovy DEG] [--occlusion 0|1] [--shadow 0|1] [--weights FILE] [--out FILE.pfm]\n"
                "       [--gradient sobel|fd|cs|none] [--gradient-shading 0|1]\n"
+               "       [--multiscaling 0..3 (s_1pebs)] [--image-filter 0..5]\n"
                "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt s_1psurr (needs --weights)\n");
   return 1;
 }
@@ -35,6 +37,7 @@ int main(int argc, char** argv) {
   int w = 768, h = 768, frames = 1, cam_i = 0, light_i = 0;
   bool have_eye = false;
   int occlusion = -1, shadow = -1, gradient = CVR_GRADIENT_NONE, gradient_shading = 0;
+  int multiscaling = 0, image_filter = CVR_FILTER_HAT;
   float eye[3] = {0, 0, 0}, fovy = 45.0f;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
@@ -56,6 +59,8 @@ int main(int argc, char** argv) {
     else if (a == "--occlusion" && (v = next())) occlusion = std::atoi(v);
     else if (a == "--shadow" && (v = next())) shadow = std::atoi(v);
     else if (a == "--gradient-shading" && (v = next())) gradient_shading = std::atoi(v);
+    else if (a == "--multiscaling" && (v = next())) multiscaling = std::atoi(v);
+    else if (a == "--image-filter" && (v = next())) image_filter = std::atoi(v);
     else if (a == "--gradient" && (v = next())) {
       // DataManager's gradient models (datamanager.h:64-69)
       std::string g = v;
@@ -71,7 +76,9 @@ int main(int argc, char** argv) {
     } else
       return usage();
   }
-  if (vol.empty() || tf.empty() || rend.empty() || w <= 0 || h <= 0 || frames <= 0) return usage();
+  if (vol.empty() || tf.empty() || rend.empty() || w <= 0 || h <= 0 || frames <= 0 || multiscaling < 0 ||
+      multiscaling > 3 || image_filter < 0 || image_filter > 5)
+    return usage();
 
   RenderingManager mgr;
   // main.cpp:57-68: the renderers available to the manager.
@@ -130,6 +137,8 @@ int main(int argc, char** argv) {
     r->SetIllumination(occlusion != 0, shadow != 0);
   }
   mgr.GetCurrentVolumeRenderer()->SetApplyGradientShading(gradient_shading != 0);
+  mgr.GetCurrentVolumeRenderer()->SetCurrentMultiScalingMode(multiscaling);
+  mgr.GetCurrentVolumeRenderer()->SetImageKernelFilter((unsigned)image_filter);
   auto t0 = std::chrono::steady_clock::now();
   for (int f = 0; f < frames; ++f) {
     if (!mgr.Display()) {

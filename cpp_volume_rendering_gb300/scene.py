@@ -289,6 +289,10 @@ class Context:
     def set_sampling(self, flags: int):
         self._ck(self.lib.cvr_set_sampling(self.h, flags))
 
+    # ---- pixel multiscaling
+    def set_multiscaling(self, mode: int, kernel: int = abi.FILTER_HAT, factor_w: int = 2, factor_h: int = 2):
+        self._ck(self.lib.cvr_set_multiscaling(self.h, mode, kernel, factor_w, factor_h))
+
     # ---- gradient Blinn-Phong shading
     def build_gradient(self, model: int = abi.GRADIENT_FINITE_DIFFERENCES, sample_size: int = 1,
                        filter_nxnxn: int = 0, normalized: bool = True):

@@ -314,6 +314,38 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
 cvr_status cvr_set_sampling(cvr_ctx* ctx, int flags);
 int cvr_get_sampling(cvr_ctx* ctx);
 
+/* ---- pixel multiscaling --------------------------------------------------------
+ * BaseVolumeRenderer::MULTISCALING (cppvolrend/volrenderbase.h:28-33) with
+ * RenderFrameToScreen's post-passes (libs/vis_utils/renderoutputframe.cpp:
+ * 265-539, shader/renderoutputframe/*.comp), run on the device after the
+ * marcher: MULTISAMPLE renders factor_w x factor_h times the output size and
+ * takes a bilinear lookup per output pixel; DOWNSCALE renders at that size
+ * and filters down with the kernel; UPSCALE renders at the output size divided
+ * by the factors (integer division) and filters up.  The cardinal B-spline
+ * and OMOMS kernels add their recursive digital filter (rows then columns) on
+ * the output (down) or on the generated frame (up).  The reference's factors
+ * are 2 x 2 (MULTISAMPLE_NUMBEROFSAMPLES_W/H, cppvolrend/defines.h:16-17) and
+ * its kernel K2_HAT (renderoutputframe.cpp:34).  Applies to cvr_render /
+ * cvr_render_host of every method (the per-pixel step counts are then not
+ * available); not to batches. */
+#define CVR_MULTISCALE_SINGLE 0       /* SINGLE_RAY_PER_PIXEL (default) */
+#define CVR_MULTISCALE_MULTISAMPLE 1  /* MULTIPLE_RAYS_PER_PIXEL */
+#define CVR_MULTISCALE_DOWNSCALE 2    /* DOWN_SCALING_RENDER */
+#define CVR_MULTISCALE_UPSCALE 3      /* UP_SCALING_RENDER */
+/* IMAGE_FILTER_KERNEL (libs/vis_utils/filters/utils.hpp:8-15) */
+#define CVR_FILTER_BOX 0
+#define CVR_FILTER_HAT 1
+#define CVR_FILTER_CATMULL_ROM 2
+#define CVR_FILTER_MITCHELL_NETRAVALI 3
+#define CVR_FILTER_CARDINAL_BSPLINE3 4
+#define CVR_FILTER_CARDINAL_OMOMS3 5
+cvr_status cvr_set_multiscaling(cvr_ctx* ctx, int mode, int kernel, int factor_w, int factor_h);
+cvr_status cvr_get_multiscaling(cvr_ctx* ctx, int* mode, int* kernel, int* factor_w, int* factor_h);
+/* The post-pass alone: src (sw x sh RGBA32F, device; not modified) to dst
+ * (w x h, device) with mode MULTISAMPLE / DOWNSCALE / UPSCALE and a kernel. */
+cvr_status cvr_rescale_frame(cvr_ctx* ctx, int mode, int kernel, const float* src_dev, int sw, int sh,
+                             float* dst_dev, int w, int h);
+
 /* ---- gradient Blinn-Phong shading -------------------------------------------
  * Gradient models: DataManager::STRUCTURED_GRADIENT_TYPE
  * (libs/volvis_utils/datamanager.h:64-69, default NONE_GRADIENT). */

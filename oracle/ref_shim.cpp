@@ -11,6 +11,8 @@
 //   * GenerateGradientTexture / GenerateSobelFeldmanGradientTexture
 //                                                (libs/volvis_utils/utils.cpp:146-351)
 //   * Pvm (DDSV3::readPVMvolume + PostProcessData) (libs/file_utils/pvm.cpp:23-108,191-309)
+//   * the image reconstruction kernels and digital filters (libs/vis_utils/filters/*.hpp,
+//     header-only; the CPU twins of shader/renderoutputframe/*.comp)
 // The GL texture classes those headers mention are stubbed below; no GL code
 // runs.  Private members of ConeGaussianSampler are read through the access
 // macro below (the interval list feeds the shader table but has no getter).
@@ -25,6 +27,19 @@
 #include <volvis_utils/structuredgridvolume.h>
 #include <volvis_utils/utils.h>
 #include <file_utils/pvm.h>
+// filters/utils.hpp's Symmetric4Pieces names its base class's buffer 'b'
+// unqualified, which GCC's two-phase lookup rejects; a namespace-scope 'b'
+// makes the header compile.  Only the kernels' operator() and digital_filter
+// are called here, and neither touches the buffer.
+namespace vis {
+static float b[4];
+}
+#include <vis_utils/filters/box.hpp>
+#include <vis_utils/filters/bspline3.hpp>
+#include <vis_utils/filters/catmullrom.hpp>
+#include <vis_utils/filters/hat.hpp>
+#include <vis_utils/filters/mitchellnetravali.hpp>
+#include <vis_utils/filters/omoms3.hpp>
 #define private public
 #include "structured/rc1pdosct/conegaussiansampler.h"
 #undef private
@@ -67,7 +82,45 @@ vis::TransferFunction1D* make_tf(int max_density, int n_rgb, const double* rgb, 
 }
 }  // namespace
 
+namespace {
+template <class K>
+int kernel_weights(K& kern, const float* x, int n, float* out, int* support) {
+  *support = kern.support();
+  for (int i = 0; i < n; ++i) out[i] = kern(x[i]);
+  return 0;
+}
+template <class K>
+int kernel_digital_filter(K& kern, float* f, int n) {
+  std::vector<float> v(f, f + n);
+  kern.digital_filter(v);
+  for (int i = 0; i < n; ++i) f[i] = v[i];
+  return 0;
+}
+}  // namespace
+
 extern "C" {
+
+// IMAGE_FILTER_KERNEL k: support and weights at n points x[i].
+int ref_filter_weights(int k, const float* x, int n, float* out, int* support) {
+  switch (k) {
+    case 0: { vis::Box q; return kernel_weights(q, x, n, out, support); }
+    case 1: { vis::Hat q; return kernel_weights(q, x, n, out, support); }
+    case 2: { vis::CatmullRom q; return kernel_weights(q, x, n, out, support); }
+    case 3: { vis::MitchellNetravali q; return kernel_weights(q, x, n, out, support); }
+    case 4: { vis::CardinalBspline3 q; return kernel_weights(q, x, n, out, support); }
+    case 5: { vis::CardinalOMOMS3 q; return kernel_weights(q, x, n, out, support); }
+  }
+  return -1;
+}
+
+// The kernel's digital filter applied to one line in place.
+int ref_digital_filter(int k, float* f, int n) {
+  switch (k) {
+    case 4: { vis::CardinalBspline3 q; return kernel_digital_filter(q, f, n); }
+    case 5: { vis::CardinalOMOMS3 q; return kernel_digital_filter(q, f, n); }
+  }
+  return -1;
+}
 
 // SAT of a full (W x H x D) grid given cell values (x fastest).
 int ref_sat_build(int w, int h, int d, const double* cells, double* out) {

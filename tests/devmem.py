@@ -30,6 +30,12 @@ class DeviceMemory:
             assert self.rt.cudaMemset(p, fill, nbytes) == 0
         return p
 
+    def upload(self, arr):
+        arr = np.ascontiguousarray(arr)
+        p = self.alloc(arr.nbytes)
+        assert self.rt.cudaMemcpy(p, arr.ctypes.data, arr.nbytes, 1) == 0
+        return p
+
     def download(self, p, shape, dtype=np.float32):
         out = np.zeros(shape, dtype)
         assert self.rt.cudaMemcpy(out.ctypes.data, p, out.nbytes, 2) == 0

@@ -10,6 +10,8 @@ the committed .npz.  Every array is produced by reference code:
               RC1PConeLightGroundTruthSteps::Update
   grad_*      GenerateSobelFeldmanGradientTexture / GenerateGradientTexture
               (the float RGB texels they upload) on small u8 / u16 volumes
+  filt_*      the image reconstruction kernels (filters/*.hpp operator())
+              on a grid of x, and the B-spline / OMOMS digital filters on a line
 The inputs (control points, grid values, sampler settings) are this
 project's own test values.
 
@@ -138,6 +140,20 @@ def main():
             r = ref.ref_gradient(P(vol.ctypes.data), w, h, d, vol.itemsize, model, n, filt, norm, P(g.ctypes.data))
             assert r == 0
             out[f"grad_{name}_{cfg}"] = g
+    xs = np.linspace(-2.6, 2.6, 1041).astype(np.float32)
+    out["filt_x"] = xs
+    for k in range(6):
+        wts = np.zeros_like(xs)
+        sup = C.c_int()
+        assert ref.ref_filter_weights(k, P(xs.ctypes.data), len(xs), P(wts.ctypes.data), C.byref(sup)) == 0
+        out[f"filt_{k}_weights"] = wts
+        out[f"filt_{k}_support"] = np.array([sup.value], np.int32)
+    line = np.random.default_rng(13).uniform(0.0, 1.0, size=53).astype(np.float32)
+    out["filt_line"] = line
+    for k in (4, 5):
+        g = line.copy()
+        assert ref.ref_digital_filter(k, P(g.ctypes.data), len(g)) == 0
+        out[f"filt_{k}_digital"] = g
     np.savez_compressed(OUT, **out)
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(out)} arrays)")
 

@@ -38,6 +38,7 @@ def test_usage_errors(data):
     assert run("--volume", data["vp"]).returncode == 1
     assert run("--bogus").returncode == 1
     assert run("--gradient", "laplace").returncode == 1
+    assert run("--volume", data["vp"], "--tf", data["tp"], "--renderer", "s_1rc", "--multiscaling", "4").returncode == 1
 
 
 def test_data_errors_before_any_device_call(data, tmp_path):
@@ -137,3 +138,22 @@ def test_headless_reads_pvm(data, fixture, tmp_path):
             "--eye", "0", "0", "40", "--out", out)
     assert r.returncode == 0, r.stderr
     assert out.stat().st_size > 24 * 24 * 12
+
+
+@pytest.mark.gpu
+def test_headless_multiscaling(data, tmp_path):
+    """--multiscaling picks the extinction renderer's MULTISCALING mode (the
+    others do not declare support, as in the reference): frames change with
+    the mode and stay finite; the plain renderer ignores it."""
+    def frame(abbr, *extra):
+        out = tmp_path / f"{abbr}_{'_'.join(extra)}.pfm"
+        r = run("--volume", data["vp"], "--tf", data["tp"], "--renderer", abbr, "--width", "40", "--height", "32",
+                "--cameras", data["cp"], "--camera-index", "0", "--lights", data["lp"], "--out", out, *extra)
+        assert r.returncode == 0, r.stderr
+        raw = out.read_bytes()
+        return np.frombuffer(raw[raw.index(b"-1.0\n") + 5:], np.float32).reshape(32, 40, 3)
+    base = frame("s_1pebs")
+    for mode in ("1", "2", "3"):
+        img = frame("s_1pebs", "--multiscaling", mode, "--image-filter", "4")
+        assert np.isfinite(img).all() and not np.array_equal(img, base), mode
+    assert np.array_equal(frame("s_1rc", "--multiscaling", "2"), frame("s_1rc"))
