@@ -45,6 +45,8 @@ WORKLOAD_DESC = {
     "plain_large": "plain ray casting: 256^3 u8 8-blob volume, unit cube -> 1024^2, step 0.5 voxel",
     "extinction_lightcache": "extinction shading with the 32^3 object-space light cache: 256^3 u16 value-noise "
                              "shells -> 1024^2, AO radii {2,6,16} + directional SAT cone shadow per cache cell",
+    "iso": "adaptive-step isosurface caster: 256^3 u16 value-noise shells -> 1024^2, isovalue 0.5, steps "
+           "0.05 / 1.0 voxels within / beyond 0.1 of it, opaque colour",
     "cone": "cone DOS shading: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 5-level extinction pyramid, "
             "occlusion + point-light shadow cones",
     "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
@@ -164,7 +166,8 @@ def algorithmic_bytes(wl, st, abi):
     bvox = 1 if wl.dtype == abi.CVR_U8 else 2
     if wl.method == abi.SURROGATE:  # per shaded sample: 42 pyramid taps (8 float32) + 6 volume taps
         return st.samples * 8 * bvox + st.shaded_samples * (42 * 8 * 4 + 6 * 8 * bvox) + wl.width * wl.height * 16
-    per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 8, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox}[wl.method]
+    per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 8, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox,
+               abi.ISO: 0}[wl.method]
     return st.samples * 8 * bvox + st.aux_fetches * per_aux + wl.width * wl.height * 16
 
 
@@ -627,7 +630,7 @@ def run_ours(args):
         reset_tuning()
         # every renderer tuned on its own frame (tile x registers x brick), with
         # FP32 volume samples and with the texture-unit variant
-        for name in ("plain", "plain_large", "cone", "ground_truth", "extinction_lightcache"):
+        for name in ("plain", "plain_large", "cone", "ground_truth", "extinction_lightcache", "iso"):
             if name == args.workload:
                 continue
             w2 = scene.workload("extinction" if name == "extinction_lightcache" else name)

@@ -28,7 +28,7 @@ CVR_ERR_UNSUPPORTED = -9
 CVR_U8 = 1
 CVR_U16 = 2
 
-PLAIN, EXTINCTION, CONE_DOS, GROUND_TRUTH, SURROGATE = 0, 1, 2, 3, 4
+PLAIN, EXTINCTION, CONE_DOS, GROUND_TRUTH, SURROGATE, ISO = 0, 1, 2, 3, 4, 5
 LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL = 0, 1, 2
 
 MAX_AO_SHELLS = 32
@@ -80,6 +80,11 @@ class GtParams(C.Structure):
                 ("sdw_distance", C.c_float), ("shadow_type", C.c_int), ("ka", C.c_float), ("kd", C.c_float)]
 
 
+class IsoParams(C.Structure):
+    _fields_ = [("step_size_small", C.c_float), ("step_size_large", C.c_float), ("step_size_range", C.c_float),
+                ("isovalue", C.c_float), ("color", C.c_float * 4)]
+
+
 class ConeTable(C.Structure):
     _fields_ = [("n_sections", C.c_int), ("sections", (C.c_float * 4) * MAX_CONE_SECTIONS),
                 ("integration_samples", C.c_int * 3), ("axes", F3 * 10), ("initial_step", C.c_float),
@@ -111,7 +116,7 @@ class Job(C.Structure):
 
 
 PARAMS_OF_METHOD = {PLAIN: PlainParams, EXTINCTION: ExtParams, CONE_DOS: DosParams, GROUND_TRUTH: GtParams,
-                    SURROGATE: GtParams}
+                    SURROGATE: GtParams, ISO: IsoParams}
 
 _P = C.c_void_p
 _I = C.c_int

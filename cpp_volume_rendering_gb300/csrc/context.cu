@@ -130,11 +130,11 @@ cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
 }
 
 cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,
-                      FrameArgs* fo) {
+                      FrameArgs* fo, bool need_tf) {
   if (!c || !cam || !params || !out || w <= 0 || h <= 0 || w > 32768 || h > 32768)
     return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: bad arguments");
   if (!c->has_volume) return fail(c, CVR_ERR_NO_VOLUME, "cvr_render: no volume loaded");
-  if (c->tf_n == 0) return fail(c, CVR_ERR_NOT_READY, "cvr_render: no transfer function");
+  if (need_tf && c->tf_n == 0) return fail(c, CVR_ERR_NOT_READY, "cvr_render: no transfer function");
   if (!finite3(cam->eye) || !finite3(cam->center) || !finite3(cam->up))
     return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: non-finite camera");
   FrameArgs f;
@@ -509,7 +509,7 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
   if (!c) return CVR_ERR_INVALID_ARG;
   CK(c, cudaSetDevice(c->device));
   FrameArgs f;
-  cvr_status fs = frame_args(c, cam, params, out, w, h, &f);
+  cvr_status fs = frame_args(c, cam, params, out, w, h, &f, method != CVR_METHOD_ISO);
   if (fs != CVR_OK) return fs;
   f.counts = counts;
   fs = grad_args(c, method, light, &f);
@@ -596,6 +596,20 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
       a.light_up = make3(light->up); a.light_right = make3(light->right);
       a.ka = p->ka; a.kd = p->kd;
       e = launch_gt(f, a, c->stream);
+      break;
+    }
+    case CVR_METHOD_ISO: {
+      if (params_size != sizeof(cvr_iso_params)) return fail(c, CVR_ERR_INVALID_ARG, "iso params size");
+      const cvr_iso_params* p = static_cast<const cvr_iso_params*>(params);
+      const float min_step = 1.0e-6f * std::sqrt(dot3(f.vol.grid, f.vol.grid));
+      if (!(p->step_size_large >= min_step) || !std::isfinite(p->step_size_large) || !std::isfinite(p->isovalue) ||
+          !std::isfinite(p->step_size_range) || !finite3(p->color) || !std::isfinite(p->color[3]))
+        return fail(c, CVR_ERR_INVALID_ARG, "iso params: steps >= 1e-6 * diagonal, finite values");
+      IsoArgs a;
+      a.step_small = p->step_size_small; a.step_large = p->step_size_large;
+      a.step_range = p->step_size_range; a.iso = p->isovalue;
+      a.color = make_float4(p->color[0], p->color[1], p->color[2], p->color[3]);
+      e = launch_iso(f, a, c->stream);
       break;
     }
     case CVR_METHOD_SURROGATE: {

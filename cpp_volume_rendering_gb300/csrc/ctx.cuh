@@ -335,7 +335,7 @@ cvr_status render_volume_view(cvr_ctx* c, VolumeView* v);
 // Frame arguments of a render of the current volume (validated; f.step from
 // the params struct's leading step_size, f.counts null, f.stats the context's).
 cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,
-                      FrameArgs* f);
+                      FrameArgs* f, bool need_tf = true);
 // Extinction arguments of the current volume; *table: the directional
 // shadow-box table (context-owned staging, valid until the next call) or null.
 cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light, const FrameArgs& f, ExtArgs* e,

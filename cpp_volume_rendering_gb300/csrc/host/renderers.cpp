@@ -112,11 +112,11 @@ bool BaseVolumeRenderer::CheckABI(int code, const char* what) {
   return Fail(std::string(what) + ": " + (m_ctx ? cvr_last_error(m_ctx) : cvr_last_error(nullptr)));
 }
 
-bool BaseVolumeRenderer::BeginInit(int w, int h) {
+bool BaseVolumeRenderer::BeginInit(int w, int h, bool need_tf) {
   if (IsBuilt()) Clean();
   if (!m_ext_data_manager || !m_ext_data_manager->GetCurrentStructuredVolume())
     return Fail("Init: no volume loaded");  // rc1prenderer.cpp:54
-  if (!m_ext_data_manager->GetCurrentTransferFunction()) return Fail("Init: no transfer function");
+  if (need_tf && !m_ext_data_manager->GetCurrentTransferFunction()) return Fail("Init: no transfer function");
   std::string err;
   m_ctx = m_ext_data_manager->GetDeviceContext(&err);
   if (!m_ctx) return Fail("Init: " + err);
@@ -233,6 +233,34 @@ void RayCasting1Pass::FillParameterSpace(ParameterSpace& ps) {
   ps.AddParameterDimension({"StepSize", &m_u_step_size, 0.2f, 2.0f, 0.1f});  // rc1prenderer.cpp:225-229
 }
 const void* RayCasting1Pass::Params(size_t* size) {
+  *size = sizeof(m_p);
+  return &m_p;
+}
+
+// ------------------------------------------------------------ rc1pisoadapt
+bool RayCasting1PassIsoAdapt::Init(int w, int h) {
+  if (!BeginInit(w, h, false)) return false;  // the volume alone (rc1pisoadaptrenderer.cpp:58)
+  vr_built = true;
+  SetOutdated();
+  return true;
+}
+bool RayCasting1PassIsoAdapt::Update(const vis::Camera& camera) {
+  m_cam = camera.ToABI();
+  fill_light(m_ext_rendering_parameters, camera, &m_light, CVR_LIGHT_POINT);  // LightSourcePosition
+  m_p.step_size_small = m_u_step_size_small;
+  m_p.step_size_large = m_u_step_size_large;
+  m_p.step_size_range = m_u_step_size_range;
+  m_p.isovalue = m_u_isovalue;
+  for (int i = 0; i < 4; ++i) m_p.color[i] = m_u_color[i];
+  return true;
+}
+void RayCasting1PassIsoAdapt::FillParameterSpace(ParameterSpace& ps) {
+  ps.ClearParameterDimensions();  // rc1pisoadaptrenderer.cpp:190-196
+  ps.AddParameterDimension({"StepSizeSmall", &m_u_step_size_small, 0.01f, 0.25f, 0.05f});
+  ps.AddParameterDimension({"StepSizeLarge", &m_u_step_size_large, 0.25f, 2.0f, 0.25f});
+  ps.AddParameterDimension({"StepSizeRange", &m_u_step_size_range, 0.05f, 0.26f, 0.05f});
+}
+const void* RayCasting1PassIsoAdapt::Params(size_t* size) {
   *size = sizeof(m_p);
   return &m_p;
 }

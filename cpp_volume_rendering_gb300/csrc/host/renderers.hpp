@@ -162,7 +162,7 @@ class BaseVolumeRenderer {
   virtual const void* Params(size_t* size) = 0;
   bool Fail(const std::string& msg);
   bool CheckABI(int code, const char* what);
-  bool BeginInit(int w, int h);  // common part of Init(): device context + frame
+  bool BeginInit(int w, int h, bool need_tf = true);  // common part of Init(): device context + frame
 
   bool vr_built = false, vr_outdated = true;
   bool m_apply_gradient_shading = false;
@@ -194,6 +194,27 @@ class RayCasting1Pass : public BaseVolumeRenderer {
   int Method() const override { return CVR_METHOD_PLAIN; }
   const void* Params(size_t* size) override;
   cvr_plain_params m_p{};
+};
+
+// rc1pisoadapt: RayCasting1PassIsoAdapt (rc1pisoadaptrenderer.cpp:10-200):
+// first-hit isosurfaces with adaptive steps; needs no transfer function.
+class RayCasting1PassIsoAdapt : public BaseVolumeRenderer {
+ public:
+  const char* GetName() override { return "1-Pass - Isosurface Raycaster Adaptive"; }
+  const char* GetAbbreviationName() override { return "iso"; }
+  bool Init(int w, int h) override;
+  bool Update(const vis::Camera& camera) override;
+  void FillParameterSpace(ParameterSpace& ps) override;
+  float m_u_isovalue = 0.5f;
+  float m_u_step_size_small = 0.05f;
+  float m_u_step_size_large = 1.0f;
+  float m_u_step_size_range = 0.1f;
+  float m_u_color[4] = {0.66f, 0.6f, 0.05f, 1.0f};
+
+ protected:
+  int Method() const override { return CVR_METHOD_ISO; }
+  const void* Params(size_t* size) override;
+  cvr_iso_params m_p{};
 };
 
 // rc1pextbsd: RC1PExtinctionBasedShading (ebsrenderer.cpp:19-260).

@@ -95,6 +95,12 @@ struct GtArgs {
   float ka, kd;
 };
 
+// Isosurface ray casting with adaptive steps (ray_marching_1p_iso_adapt.comp).
+struct IsoArgs {
+  float step_small, step_large, step_range, iso;
+  float4 color;
+};
+
 // CTAs of kern that fit on one SM at once, from its shared memory (dynamic +
 // static + the per-block reservation) and registers (allocated per warp in
 // units of 8 per thread).  Persistent launches size their grids with it.
@@ -146,6 +152,7 @@ cudaError_t launch_march_cached(const FrameArgs& f, const float2* cache, const i
                                 int apply_sdw, float ka, float kd, cudaStream_t st);
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
+cudaError_t launch_iso(const FrameArgs& f, const IsoArgs& a, cudaStream_t st);
 // table == nullptr: per-sample cone geometry (point lights, or too many boxes).
 cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st);
 cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, cudaStream_t st);

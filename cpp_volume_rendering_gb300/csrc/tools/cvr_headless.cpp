@@ -28,7 +28,7 @@ static int usage() {
                "       [--fovy DEG] [--occlusion 0|1] [--shadow 0|1] [--weights FILE] [--out FILE.pfm]\n"
                "       [--gradient sobel|fd|cs|none] [--gradient-shading 0|1]\n"
                "       [--multiscaling 0..3 (s_1pebs)] [--image-filter 0..5]\n"
-               "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt s_1psurr (needs --weights)\n");
+               "renderers: s_1rc s_1pebs s_1pdosct s_1pcrtgt iso s_1psurr (needs --weights)\n");
   return 1;
 }
 
@@ -82,10 +82,12 @@ int main(int argc, char** argv) {
 
   RenderingManager mgr;
   // main.cpp:57-68: the renderers available to the manager.
+  // (in its order; the null, VCT and slice-based renderers are not built)
   mgr.AddVolumeRenderer(new RayCasting1Pass());
-  mgr.AddVolumeRenderer(new RC1PExtinctionBasedShading());
-  mgr.AddVolumeRenderer(new RC1PConeTracingDirOcclusionShading());
+  mgr.AddVolumeRenderer(new RayCasting1PassIsoAdapt());
   mgr.AddVolumeRenderer(new RC1PConeLightGroundTruthSteps());
+  mgr.AddVolumeRenderer(new RC1PConeTracingDirOcclusionShading());
+  mgr.AddVolumeRenderer(new RC1PExtinctionBasedShading());
   RC1PSurrogateShading* surr = new RC1PSurrogateShading();  // no reference counterpart
   surr->m_weights_path = weights;
   mgr.AddVolumeRenderer(surr);

@@ -174,6 +174,14 @@ def ext_params(step, diag, ao_radii=(2, 6, 16), shadow_type=1, apply_occ=True, a
     return p
 
 
+def iso_params(isovalue=0.5, small=0.05, large=1.0, step_range=0.1, color=(0.66, 0.6, 0.05, 1.0)) -> abi.IsoParams:
+    """RayCasting1PassIsoAdapt's defaults (rc1pisoadaptrenderer.cpp:10-19)."""
+    p = abi.IsoParams()
+    p.step_size_small, p.step_size_large, p.step_size_range, p.isovalue = small, large, step_range, isovalue
+    p.color[:] = list(color)
+    return p
+
+
 def dos_params(step, apply_occ=True, apply_sdw=False, shadow_type=0) -> abi.DosParams:
     p = abi.DosParams()
     p.step_size = step
@@ -422,6 +430,8 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     ground_truth / cone : 256^3 u8, 32 blobs + U[0,20] background; GT with 16
                  occlusion rays (90 deg, 32 voxels) and 1 shadow ray to a point
                  light at 1-voxel steps; cone method on a 5-level pyramid, 512^2
+    iso        : the extinction volume (256^3 u16 value-noise shells) -> 1024^2, isovalue 0.5, the
+                 iso-adaptive renderer's default steps (0.05 / 1.0 world units, range 0.1)
     surrogate  : held-out 512^3 u8 of the same blob generator (seed 4020), the
                  ground-truth camera, light and integrator parameters, network
                  inputs on a 6-level pyramid of base n/2, 1024^2
@@ -471,6 +481,14 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
             base = max(1, n // 2)
             wl.pyramid = dict(base_dims=(base, base, base), sigma0=1.0, n_levels=5)
         return wl
+    if name == "iso":
+        n = n or 256
+        image = image or 1024
+        vol = synth_value_noise(n, n, n, abi.CVR_U16, seed=2000)
+        sp = (1.0, 1.0, 1.0)
+        cam = camera(orbit_eye(3.0 * n, 35.0, 25.0), fovy=30.0)
+        lt = light(abi.LIGHT_POINT, position=tuple(2.0 * n * _norm((0.4, 1.0, 0.6))))
+        return Workload(name, abi.ISO, vol, sp, BENCH_TF, cam, lt, iso_params(), image, image)
     if name == "surrogate":
         n = n or 512
         image = image or 1024

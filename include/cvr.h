@@ -63,8 +63,9 @@ typedef enum cvr_method {
   CVR_METHOD_EXTINCTION = 1,  /* rc1pextbsd : ebs_ray_bbox_marching.comp */
   CVR_METHOD_CONE_DOS = 2,    /* rc1pdosct  : ray_bbox_marching.comp */
   CVR_METHOD_GROUND_TRUTH = 3, /* rc1pcrtgt  : gt_ray_marching.comp (single pass) */
-  CVR_METHOD_SURROGATE = 4     /* no reference counterpart: rc1pcrtgt with the light integrals
+  CVR_METHOD_SURROGATE = 4,    /* no reference counterpart: rc1pcrtgt with the light integrals
                                   replaced by the learned network (see the surrogate section) */
+  CVR_METHOD_ISO = 5           /* rc1pisoadapt: ray_marching_1p_iso_adapt.comp (first-hit isosurfaces) */
 } cvr_method;
 
 typedef struct cvr_ctx cvr_ctx;
@@ -143,6 +144,20 @@ typedef struct cvr_gt_params {
   int shadow_type;              /* SdwShadowType: 0 point, 1 spot, 2 directional */
   float ka, kd;
 } cvr_gt_params;
+
+/* RayCasting1PassIsoAdapt (rc1pisoadaptrenderer.cpp:10-19): adaptive steps
+ * along the ray, small within step_size_range of the isovalue (normalised
+ * density), large elsewhere; each crossing of the isovalue between two
+ * samples is refined linearly and composited with the constant colour
+ * (premultiplied), stopping at opacity 0.99.  Gradient shading is
+ * ShadeBlinnPhong with cvr_set_blinn_phong's ka, kd, ks, shininess. */
+typedef struct cvr_iso_params {
+  float step_size_small;  /* StepSizeSmall, world units (default 0.05) */
+  float step_size_large;  /* StepSizeLarge (default 1.0) */
+  float step_size_range;  /* StepSizeRange (default 0.1) */
+  float isovalue;         /* Isovalue, normalised density (default 0.5) */
+  float color[4];         /* Color (default 0.66, 0.6, 0.05, 1) */
+} cvr_iso_params;
 
 /* Cone section table of one ConeGaussianSampler
  * (cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp:179-205, 212-386).

@@ -722,6 +722,63 @@ void march_rows(const Scene& s, const cvr_camera& camc, T step, int W, int H, in
   if (total) *total = acc;
 }
 
+// ------------------------------------------------------------ isosurfaces
+// main() of ray_marching_1p_iso_adapt.comp:84-172: the density at the entry
+// point, adaptive steps (small within StepSizeRange of the isovalue), samples
+// at interval ends, linear refinement of each crossing, constant colour
+// (ShadeBlinnPhong when gradient shading is on), front-to-back until 0.99.
+template <class T>
+void iso_rows(const Scene& s, const cvr_camera& camc, const cvr_iso_params& p, const cvr_light& light, int W, int H,
+              int y0, int y1, double* out, uint32_t* counts, uint64_t* total, int threads) {
+  Frame<T> f;
+  f.s = &s;
+  f.spacing = v3<T>(T(s.sx), T(s.sy), T(s.sz));
+  f.grid = v3<T>(T(s.nx * s.sx), T(s.ny * s.sy), T(s.nz * s.sz));
+  f.cam = make_cam<T>(camc, W, H);
+  f.step = T(p.step_size_small);
+  const T iso = T(p.isovalue), small = T(p.step_size_small), large = T(p.step_size_large), range = T(p.step_size_range);
+  const bool grad = s.bp.apply && s.grad_ready;
+  const V3<T> lpos = from<T>(light.position);
+  uint64_t acc = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(threads) reduction(+ : acc)
+  for (int y = y0; y < y1; ++y) {
+    for (int x = 0; x < W; ++x) {
+      V3<T> dir = primary_dir(f.cam, x, y, W, H);
+      T tnear, tfar;
+      V4<T> dst{0, 0, 0, 0};
+      uint32_t n = 0;
+      if (ray_aabb(f.cam.eye, dir, f.grid, tnear, tfar)) {
+        T D = std::fabs(tfar - tnear);
+        V3<T> tex0 = f.cam.eye + dir * tnear + f.grid * T(0.5);
+        T prev = sample_volume(s, tex0);
+        for (T st = 0; st < D;) {
+          T h = std::min(std::fabs(prev - iso) < range ? small : large, D - st);
+          T d = sample_volume(s, tex0 + dir * (st + h));
+          ++n;
+          if ((prev <= iso && iso < d) || (prev >= iso && iso > d)) {
+            T t = (iso - prev) / (d - prev);
+            V3<T> pos = tex0 + dir * (st + t * h);
+            V4<T> src{T(p.color[0]), T(p.color[1]), T(p.color[2]), T(p.color[3])};
+            if (grad) src = phong<T>(s, f, src, pos, lpos, PHONG_PLAIN, T(0), T(0), T(0), T(0));
+            src.r *= src.a; src.g *= src.a; src.b *= src.a;
+            T r = T(1) - dst.a;
+            dst.r += r * src.r; dst.g += r * src.g; dst.b += r * src.b; dst.a += r * src.a;
+            if (dst.a > T(0.99)) break;
+          }
+          prev = d;
+          st = st + h;
+        }
+      }
+      size_t o = (size_t)(y - y0) * W + x;
+      out[4 * o + 0] = (double)dst.r; out[4 * o + 1] = (double)dst.g;
+      out[4 * o + 2] = (double)dst.b; out[4 * o + 3] = (double)dst.a;
+      if (counts) counts[o] = n;
+      acc += n;
+    }
+  }
+  if (total) *total = acc;
+}
+
 // ------------------------------------------------------------ light cache
 // Object-space light cache: (occlusion, shadow) at the cell centres
 // tex_pos = (cell + 0.5) * (VolumeScales * (VolumeDimensions / LightCacheDimensions))
@@ -934,6 +991,10 @@ int render_t(Scene& s, int method, const cvr_camera& cam, const cvr_light& light
                       T is = p->apply_shadow ? gt_shadow(f, g, tx) : T(0);
                       return shade_mix<T>(s, f, src, tx, g.light_pos, PHONG_GT, p->apply_occlusion != 0, T(p->ka), io, p->apply_shadow != 0, T(p->kd), is);
                     });
+      return 0;
+    }
+    case CVR_METHOD_ISO: {
+      iso_rows<T>(s, cam, *(const cvr_iso_params*)params, light, W, H, y0, y1, out, counts, total, threads);
       return 0;
     }
     case CVR_METHOD_SURROGATE: {

@@ -63,7 +63,8 @@ def test_data_errors_before_any_device_call(data, tmp_path):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("abbr,method", [("s_1rc", abi.PLAIN), ("s_1pebs", abi.EXTINCTION),
-                                         ("s_1pdosct", abi.CONE_DOS), ("s_1pcrtgt", abi.GROUND_TRUTH)])
+                                         ("s_1pdosct", abi.CONE_DOS), ("s_1pcrtgt", abi.GROUND_TRUTH),
+                                         ("iso", abi.ISO)])
 def test_headless_frames(data, abbr, method, tmp_path):
     out = tmp_path / f"{abbr}.pfm"
     # the ground-truth renderer starts with occlusion and shadows off (crtgtrenderer.cpp:40-46)
