@@ -161,12 +161,13 @@ def profile_traffic(workload):
 
 def algorithmic_bytes(wl, st, abi):
     """Algorithmic bytes of one frame: 8 voxel texels per primary sample,
-    plus per secondary fetch 64 int64 SAT texels (extinction), 8 float32
-    pyramid texels (cone) or 8 voxel texels (ground truth), plus the image."""
+    plus per secondary fetch 64 four-byte SAT texels (extinction: the
+    reference's R32F table, this build's compact table), 8 float32 pyramid
+    texels (cone) or 8 voxel texels (ground truth), plus the image."""
     bvox = 1 if wl.dtype == abi.CVR_U8 else 2
     if wl.method == abi.SURROGATE:  # per shaded sample: 42 pyramid taps (8 float32) + 6 volume taps
         return st.samples * 8 * bvox + st.shaded_samples * (42 * 8 * 4 + 6 * 8 * bvox) + wl.width * wl.height * 16
-    per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 8, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox,
+    per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 4, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox,
                abi.ISO: 0}[wl.method]
     return st.samples * 8 * bvox + st.aux_fetches * per_aux + wl.width * wl.height * 16
 
@@ -577,9 +578,9 @@ def run_ours(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "algorithmic_bytes_per_launch": alg, "kernel_ms_median": med_ms,
-                "note": "algorithmic gather bytes (8 voxel texels per primary step + 64 int64 SAT texels per box "
-                        "query + image); the SAT and volume are L2-resident, so the effective gather rate can "
-                        "exceed the HBM line"}
+                "note": "algorithmic gather bytes (8 voxel texels per primary step + 64 four-byte SAT texels per "
+                        "box query + image); the SAT and volume are L2-resident, so the effective gather rate can "
+                        "exceed the HBM line; the marcher is bound by integer issue (see the ncu summary)"}
     if traffic_src:
         roofline["traffic_source"] = f"profiles/{traffic_src}"
     # end to end through the C ABI with host buffers

@@ -186,6 +186,8 @@ SIGNATURES = {
     "cvr_download_light_cache": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_brick_size": (_I, [_P, _I]),
     "cvr_get_brick_size": (_I, [_P]),
+    "cvr_set_compact_sat": (_I, [_P, _I]),
+    "cvr_get_compact_sat": (_I, [_P]),
     "cvr_set_multiscaling": (_I, [_P, _I, _I, _I, _I]),
     "cvr_get_multiscaling": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                   C.POINTER(C.c_int)]),

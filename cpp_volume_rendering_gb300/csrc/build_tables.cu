@@ -13,20 +13,22 @@ namespace cvr {
 // Pass 1: fill + x-scan.  One warp per SAT row (y, z).  Interior cells take
 // lut[voxel(x-1, y-1, z-1)] (the extinction of that voxel value in fixed
 // point); the one-cell border is zero (ebsrenderer.cpp:651-659).
+// W: long long (exact int64 prefix sums) or unsigned (sums modulo 2^32).
+template <class W>
 __global__ void k_sat_fill_xscan(const void* vox, int dtype, int nx, int ny, int nz,
-                                 const long long* __restrict__ lut, long long* __restrict__ sat) {
+                                 const W* __restrict__ lut, W* __restrict__ sat) {
   const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= sy * sz) return;
   int y = warp % sy, z = warp / sy;
-  long long* row = sat + ((size_t)z * sy + y) * (size_t)sx;
+  W* row = sat + ((size_t)z * sy + y) * (size_t)sx;
   bool border_row = (y == 0 || z == 0 || y == sy - 1 || z == sz - 1);
   size_t vrow = border_row ? 0 : ((size_t)(z - 1) * ny + (y - 1)) * (size_t)nx;
-  long long carry = 0;
+  W carry = 0;
   for (int base = 0; base < sx; base += 32) {
     int x = base + lane;
-    long long v = 0;
+    W v = 0;
     if (!border_row && x > 0 && x < sx - 1) {
       unsigned int q = (dtype == 1) ? (unsigned int)__ldg(static_cast<const uint8_t*>(vox) + vrow + (x - 1))
                                     : (unsigned int)__ldg(static_cast<const uint16_t*>(vox) + vrow + (x - 1));
@@ -34,7 +36,7 @@ __global__ void k_sat_fill_xscan(const void* vox, int dtype, int nx, int ny, int
     }
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      long long n = __shfl_up_sync(0xffffffffu, v, o);
+      W n = __shfl_up_sync(0xffffffffu, v, o);
       if (lane >= o) v += n;
     }
     v += carry;
@@ -46,7 +48,8 @@ __global__ void k_sat_fill_xscan(const void* vox, int dtype, int nx, int ny, int
 // Pass 2 / 3: inclusive scan along y (stride sx) or z (stride sx*sy).  One
 // thread per line; consecutive threads own consecutive x, so every step is a
 // coalesced 256-byte warp access.
-__global__ void k_sat_scan_lines(long long* __restrict__ sat, int sx, int n_lines_inner, int n_lines_outer,
+template <class W>
+__global__ void k_sat_scan_lines(W* __restrict__ sat, int sx, int n_lines_inner, int n_lines_outer,
                                  size_t line_stride_inner, size_t line_stride_outer, size_t step, int len) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int total = sx * n_lines_inner * n_lines_outer;
@@ -54,12 +57,12 @@ __global__ void k_sat_scan_lines(long long* __restrict__ sat, int sx, int n_line
   int x = t % sx;
   int r = t / sx;
   int a = r % n_lines_inner, b = r / n_lines_inner;
-  long long* p = sat + (size_t)x + (size_t)a * line_stride_inner + (size_t)b * line_stride_outer;
-  long long acc = 0;
+  W* p = sat + (size_t)x + (size_t)a * line_stride_inner + (size_t)b * line_stride_outer;
+  W acc = 0;
   int i = 0;
   for (; i + 4 <= len; i += 4) {
-    long long v0 = p[(size_t)(i + 0) * step], v1 = p[(size_t)(i + 1) * step];
-    long long v2 = p[(size_t)(i + 2) * step], v3 = p[(size_t)(i + 3) * step];
+    W v0 = p[(size_t)(i + 0) * step], v1 = p[(size_t)(i + 1) * step];
+    W v2 = p[(size_t)(i + 2) * step], v3 = p[(size_t)(i + 3) * step];
     acc += v0; p[(size_t)(i + 0) * step] = acc;
     acc += v1; p[(size_t)(i + 1) * step] = acc;
     acc += v2; p[(size_t)(i + 2) * step] = acc;
@@ -71,26 +74,36 @@ __global__ void k_sat_scan_lines(long long* __restrict__ sat, int sx, int n_line
   }
 }
 
-cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
-                             long long* sat, cudaStream_t st) {
+template <class W>
+static cudaError_t sat_build(const void* vox, int dtype, int nx, int ny, int nz, const W* lut, W* sat, cudaStream_t st) {
   const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
   {
     long long rows = (long long)sy * sz;
     int threads = 256;
     long long blocks = (rows * 32 + threads - 1) / threads;
-    k_sat_fill_xscan<<<(unsigned)blocks, threads, 0, st>>>(vox, dtype, nx, ny, nz, lut, sat);
+    k_sat_fill_xscan<W><<<(unsigned)blocks, threads, 0, st>>>(vox, dtype, nx, ny, nz, lut, sat);
   }
   {
     // y-scan: lines indexed by (x, z); stride along y = sx.
     int total = sx * sz;
-    k_sat_scan_lines<<<(total + 255) / 256, 256, 0, st>>>(sat, sx, 1, sz, 0, (size_t)sx * sy, (size_t)sx, sy);
+    k_sat_scan_lines<W><<<(total + 255) / 256, 256, 0, st>>>(sat, sx, 1, sz, 0, (size_t)sx * sy, (size_t)sx, sy);
   }
   {
     // z-scan: lines indexed by (x, y); stride along z = sx*sy.
     int total = sx * sy;
-    k_sat_scan_lines<<<(total + 255) / 256, 256, 0, st>>>(sat, sx, sy, 1, (size_t)sx, 0, (size_t)sx * sy, sz);
+    k_sat_scan_lines<W><<<(total + 255) / 256, 256, 0, st>>>(sat, sx, sy, 1, (size_t)sx, 0, (size_t)sx * sy, sz);
   }
   return cudaGetLastError();
+}
+
+cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
+                             long long* sat, cudaStream_t st) {
+  return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
+}
+
+cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
+                               unsigned* sat, cudaStream_t st) {
+  return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
 }
 
 // --------------------------------------------------------------- pyramid

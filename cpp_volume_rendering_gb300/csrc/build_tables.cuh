@@ -8,6 +8,9 @@ namespace cvr {
 // Builds the (nx+2)(ny+2)(nz+2) int64 SAT of lut[voxel] with a zero border.
 cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
                              long long* sat, cudaStream_t st);
+// The same prefix sums of a 32-bit lut, wrapping modulo 2^32 (the compact table).
+cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
+                               unsigned* sat, cudaStream_t st);
 
 // Builds every level of P (dims/offsets/grid filled by the caller) into data.
 cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, int tf_n, float s0,

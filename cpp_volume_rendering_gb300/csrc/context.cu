@@ -189,7 +189,81 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
     if (build_shadow_table(p, light->forward, f.vol.spacing, f.vol.grid, c->sdw_table.get()))
       *table = c->sdw_table.get();
   }
+  // The compact table serves the frame when the largest region any of its
+  // box queries spans is known (AO boxes; shadow boxes of a per-frame table)
+  if (c->compact_sat && (p->apply_occlusion || p->apply_shadow) && (!p->apply_shadow || *table)) {
+    const float3 sc = f.vol.spacing;
+    const double sv[3] = {sc.x, sc.y, sc.z};
+    const int n[3] = {c->nx, c->ny, c->nz};
+    // cells a query on a world extent w may span: its taps reach floor(lo) .. floor(hi) + 1,
+    // one more for single-precision positions, at most the SAT's n + 1 cells
+    auto cells = [&](double w, int ax) { return std::min(std::ceil(w / sv[ax]) + 3.0, (double)n[ax] + 1.0); };
+    double vmax = 0.0;
+    if (p->apply_occlusion) {
+      float rmax = 0.0f;
+      for (int i = 0; i < p->ao_n_shells; ++i) rmax = std::max(rmax, p->ao_radii[i]);
+      double v = 1.0;
+      for (int ax = 0; ax < 3; ++ax) v *= cells(2.0 * rmax * sv[ax], ax);
+      vmax = std::max(vmax, v);
+    }
+    if (p->apply_shadow) {
+      const ShadowBoxTable& t = **table;
+      for (int k = 0; k < t.n; ++k) {
+        const double v = cells((double)t.hi[k].x - t.lo[k].x, 0) * cells((double)t.hi[k].y - t.lo[k].y, 1) *
+                         cells((double)t.hi[k].z - t.lo[k].z, 2);
+        vmax = std::max(vmax, v);
+      }
+    }
+    float inv_scale32 = 0.0f;
+    cvr_status cs = ensure_compact_sat(c, vmax, &inv_scale32);
+    if (cs != CVR_OK) return cs;
+    if (inv_scale32 > 0.0f) {
+      a.sat.sat32 = c->d_sat32;
+      a.sat.inv_scale32 = inv_scale32;
+    }
+  }
   *eo = a;
+  return CVR_OK;
+}
+
+// The compact SAT for queries spanning at most vmax cells: fixed point
+// round(sigma * 2^F32) with F32 the largest that keeps vmax * max q below
+// 2^31, so every sub-box sum, and so every wrapped 32-bit difference of the
+// table, is exact.  Used only while that resolution stays at 2^15 or more
+// steps per largest extinction (the FP32 table of the reference resolves far
+// less); *inv_scale = 2^-F32, or 0 when the frame keeps the int64 table.
+cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
+  *inv_scale = 0.0f;
+  if (c->sat_ext.empty() || !(vmax >= 1.0)) return CVR_OK;
+  double maxv = 0.0;
+  for (double v : c->sat_ext) maxv = std::max(maxv, v);
+  const double limit = 2147483647.0;
+  int F = maxv > 0.0 ? (int)std::floor(std::log2(limit / (vmax * maxv))) : 0;
+  F = std::min(F, 52);
+  std::vector<unsigned> q(c->sat_ext.size());
+  for (;; --F) {
+    const double scale = std::ldexp(1.0, F);
+    double qmax = 0.0;
+    for (size_t i = 0; i < q.size(); ++i) {
+      const double r = std::nearbyint(c->sat_ext[i] * scale);
+      qmax = std::max(qmax, r);
+      q[i] = (unsigned)r;
+    }
+    if (qmax * vmax < limit || F < -64) {
+      if (maxv > 0.0 && qmax < 32768.0) return CVR_OK;  // too coarse: the int64 table
+      break;
+    }
+  }
+  if (c->sat32_F != F || !c->d_sat32) {
+    const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+    CK(c, ensure(c->d_lut32, c->lut32_cap, sizeof(unsigned) * q.size()));
+    CK(c, cudaMemcpyAsync(c->d_lut32, q.data(), sizeof(unsigned) * q.size(), cudaMemcpyHostToDevice, c->stream));
+    CK(c, ensure(c->d_sat32, c->sat32_cap, cells * sizeof(unsigned)));
+    CK(c, launch_sat_build32(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, c->d_sat32, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));  // q is a host temporary
+    c->sat32_F = F;
+  }
+  *inv_scale = (float)std::ldexp(1.0, -F);
   return CVR_OK;
 }
 
@@ -239,7 +313,8 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms};
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms,
+                  c->d_sat32, c->d_lut32};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -273,6 +348,7 @@ static cvr_status set_volume_common(cvr_ctx* c, const void* src, bool src_device
   c->has_volume = true;
   // Derived tables belong to the previous volume.
   c->sat_ready = false;
+  c->sat32_F = kNoCompactSat;
   c->pyr_ready = false;
   c->tex.vol_valid = false;
   c->tex.pyr_valid = false;
@@ -351,6 +427,8 @@ cvr_status cvr_build_sat(cvr_ctx* c, const double* ext, int n_values) {
   CK(c, cudaStreamSynchronize(c->stream));  // q is a host temporary
   c->sat_frac_bits = F;
   c->sat_ready = true;
+  c->sat_ext.assign(ext, ext + n_values);
+  c->sat32_F = kNoCompactSat;
   return CVR_OK;
 }
 
@@ -683,6 +761,14 @@ cvr_status cvr_get_tuning(cvr_ctx* c, int* tile_w, int* tile_h, int* variant) {
   if (variant) *variant = c->variant;
   return CVR_OK;
 }
+
+cvr_status cvr_set_compact_sat(cvr_ctx* c, int enable) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  c->compact_sat = enable != 0;
+  return CVR_OK;
+}
+
+int cvr_get_compact_sat(cvr_ctx* c) { return c ? (int)c->compact_sat : 0; }
 
 cvr_status cvr_set_light_cache(cvr_ctx* c, int w, int h, int d) {
   if (!c) return CVR_ERR_INVALID_ARG;

@@ -89,6 +89,9 @@ inline void swap_tex(TexState& a, TexState& b) {
   std::swap(a.grad_valid, b.grad_valid);
 }
 
+// sat32_F of a context / slot without a valid compact SAT.
+constexpr int kNoCompactSat = -1000;
+
 // A resident volume that is not the current one (cvr_select_volume): the
 // volume, its SAT, pyramid and texture copies.  The current volume lives in
 // the cvr_ctx fields of the same names.
@@ -103,6 +106,12 @@ struct VolSlot {
   long long* d_lut = nullptr;
   int sat_frac_bits = 0;
   bool sat_ready = false;
+  std::vector<double> sat_ext;
+  unsigned* d_sat32 = nullptr;
+  size_t sat32_cap = 0;
+  unsigned* d_lut32 = nullptr;
+  size_t lut32_cap = 0;
+  int sat32_F = kNoCompactSat;
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;
   PyramidView pyr{};
@@ -116,7 +125,7 @@ struct VolSlot {
   bool grad_ready = false;
   cvr_gradient_params grad_params{CVR_GRADIENT_NONE, 1, 0, 1};
   ~VolSlot() {
-    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick, d_grad};
+    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick, d_grad, d_sat32, d_lut32};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }
@@ -161,6 +170,15 @@ struct cvr_ctx {
   long long* d_lut = nullptr;
   int sat_frac_bits = 0;
   bool sat_ready = false;
+  // compact SAT (32-bit prefix sums modulo 2^32 at F32 fractional bits) for
+  // frames whose boxes are small enough; the extinction table it is built from
+  std::vector<double> sat_ext;
+  unsigned* d_sat32 = nullptr;
+  size_t sat32_cap = 0;
+  unsigned* d_lut32 = nullptr;
+  size_t lut32_cap = 0;
+  int sat32_F = kNoCompactSat;
+  bool compact_sat = true;                   // cvr_set_compact_sat
   // pyramid
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;
@@ -226,6 +244,12 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->d_lut, s.d_lut);
   std::swap(c->sat_frac_bits, s.sat_frac_bits);
   std::swap(c->sat_ready, s.sat_ready);
+  std::swap(c->sat_ext, s.sat_ext);
+  std::swap(c->d_sat32, s.d_sat32);
+  std::swap(c->sat32_cap, s.sat32_cap);
+  std::swap(c->d_lut32, s.d_lut32);
+  std::swap(c->lut32_cap, s.lut32_cap);
+  std::swap(c->sat32_F, s.sat32_F);
   std::swap(c->d_pyr, s.d_pyr);
   std::swap(c->pyr_cap, s.pyr_cap);
   std::swap(c->pyr, s.pyr);
@@ -340,6 +364,10 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
 // shadow-box table (context-owned staging, valid until the next call) or null.
 cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light, const FrameArgs& f, ExtArgs* e,
                     const ShadowBoxTable** table);
+// The compact 32-bit SAT for a frame whose box queries span at most vmax
+// cells, (re)built when its fixed point changes; *inv_scale = 2^-F32, or 0
+// when the frame keeps the int64 table.
+cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale);
 // Surrogate arguments of the current volume (pyramid, textures, network).
 cvr_status sur_job_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light, SurArgs* a, bool* tex);
 // The CVR_METHOD_SURROGATE launch of cvr_render.

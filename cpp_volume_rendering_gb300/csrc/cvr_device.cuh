@@ -8,6 +8,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 namespace cvr {
@@ -172,6 +173,12 @@ __device__ __forceinline__ float tf_alpha(const float4* tf, int n, float density
 // tap order, so one previous plane (9 int64) is live at a time.
 struct SatView {
   const long long* sat;  // (nx+2)(ny+2)(nz+2), x fastest
+  // The compact copy for frames whose boxes are all small enough: the same
+  // prefix sums of round(sigma * 2^F32) modulo 2^32 (F32 chosen so that every
+  // sub-box sum of the frame's boxes is below 2^31, which makes their
+  // wrapped 32-bit differences exact); nullptr: frames use the int64 table.
+  const unsigned* sat32;
+  float inv_scale32;     // 2^-F32
   int sx, sy, sz;        // SAT dims = volume dims + 2
   float inv_scale;       // 2^-F
   float3 inv_spacing;
@@ -202,55 +209,70 @@ __device__ __forceinline__ float ll_to_float(long long v) {
   return __uint_as_float(__float_as_uint(f) | ((unsigned)s & 0x80000000u));
 }
 
-struct D3 { long long d[3]; };  // consecutive x-differences of one row
-__device__ __forceinline__ D3 row_diffs(const long long* row, const BoxAxis& X) {
-  long long v0 = __ldg(row + X.s[0]), v1 = __ldg(row + X.s[1]);
-  long long v2 = __ldg(row + X.s[2]), v3 = __ldg(row + X.s[3]);
-  D3 r;
+// Exact box sums: W = long long (the int64 table) or unsigned (the compact
+// table, differences wrapping modulo 2^32 and read as signed at the end).
+template <class W>
+struct D3 { W d[3]; };  // consecutive x-differences of one row
+template <class W>
+__device__ __forceinline__ D3<W> row_diffs(const W* row, const BoxAxis& X) {
+  const W v0 = __ldg(row + X.s[0]), v1 = __ldg(row + X.s[1]);
+  const W v2 = __ldg(row + X.s[2]), v3 = __ldg(row + X.s[3]);
+  D3<W> r;
   r.d[0] = v1 - v0; r.d[1] = v2 - v1; r.d[2] = v3 - v2;
   return r;
 }
-struct D9 { D3 y[3]; };  // consecutive y-differences of x-differenced rows
-__device__ __forceinline__ D9 plane_diffs(const SatView& S, int z, const BoxAxis& X, const BoxAxis& Y) {
-  const long long* plane = S.sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
-  D9 r;
-  D3 prev = row_diffs(plane + (size_t)Y.s[0] * S.sx, X);
+template <class W>
+struct D9 { D3<W> y[3]; };  // consecutive y-differences of x-differenced rows
+template <class W>
+__device__ __forceinline__ D9<W> plane_diffs(const W* sat, const SatView& S, int z, const BoxAxis& X,
+                                             const BoxAxis& Y) {
+  const W* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
+  D9<W> r;
+  D3<W> prev = row_diffs(plane + (size_t)Y.s[0] * S.sx, X);
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
-    D3 cur = row_diffs(plane + (size_t)Y.s[b + 1] * S.sx, X);
+    D3<W> cur = row_diffs(plane + (size_t)Y.s[b + 1] * S.sx, X);
 #pragma unroll
     for (int a = 0; a < 3; ++a) r.y[b].d[a] = cur.d[a] - prev.d[a];
     prev = cur;
   }
   return r;
 }
+__device__ __forceinline__ float box_to_float(long long v) { return ll_to_float(v); }
+__device__ __forceinline__ float box_to_float(unsigned v) { return __int2float_rn((int)v); }
 // sum over y-op and x-op of wy * wx * (cur - prev), the z-difference of two planes
-__device__ __forceinline__ float weigh9(const D9& cur, const D9& prev, const BoxAxis& X, const BoxAxis& Y) {
+template <class W>
+__device__ __forceinline__ float weigh9(const D9<W>& cur, const D9<W>& prev, const BoxAxis& X, const BoxAxis& Y) {
   float acc = 0.0f;
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
     float row = 0.0f;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) row = fmaf(X.w[a], ll_to_float(cur.y[b].d[a] - prev.y[b].d[a]), row);
+    for (int a = 0; a < 3; ++a) row = fmaf(X.w[a], box_to_float(cur.y[b].d[a] - prev.y[b].d[a]), row);
     acc = fmaf(Y.w[b], row, acc);
   }
   return acc;
 }
 
-// EvaluateSAT3D(p1, p2) on already offset + clamped world positions.
+// EvaluateSAT3D(p1, p2) on already offset + clamped world positions; COMPACT
+// reads the 32-bit table.
+template <bool COMPACT>
 __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2) {
+  using W = typename std::conditional<COMPACT, unsigned, long long>::type;
+  const W* sat;
+  if constexpr (COMPACT) sat = S.sat32; else sat = S.sat;
   BoxAxis X = box_axis(fmaf(p1.x, S.inv_spacing.x, -0.5f), fmaf(p2.x, S.inv_spacing.x, -0.5f), S.sx);
   BoxAxis Y = box_axis(fmaf(p1.y, S.inv_spacing.y, -0.5f), fmaf(p2.y, S.inv_spacing.y, -0.5f), S.sy);
   BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
   float acc = 0.0f;
-  D9 prev = plane_diffs(S, Z.s[0], X, Y);
+  D9<W> prev = plane_diffs(sat, S, Z.s[0], X, Y);
 #pragma unroll
   for (int g = 0; g < 3; ++g) {
-    D9 cur = plane_diffs(S, Z.s[g + 1], X, Y);
+    D9<W> cur = plane_diffs(sat, S, Z.s[g + 1], X, Y);
     acc = fmaf(Z.w[g], weigh9(cur, prev, X, Y), acc);
     prev = cur;
   }
-  return acc * S.inv_scale;
+  return acc * (COMPACT ? S.inv_scale32 : S.inv_scale);
 }
 
 // ---------------------------------------------------------------- pyramid

@@ -20,18 +20,19 @@ __global__ void __launch_bounds__(NT) k_march_plain(FrameArgs f) {
 // pixels).  MINB: minimum resident CTAs per SM requested from the register
 // allocator, from the tuner's register variant (0: no cap, 1: <= 128, 2: <= 80
 // registers per thread).
-template <int NT, int MINB>
+// C: the SAT queries read the compact 32-bit table.
+template <int NT, int MINB, bool C>
 __global__ void __launch_bounds__(NT, MINB) k_march_extinction(FrameArgs f, ExtArgs e) {
   extern __shared__ float4 sm_tf[];
   const float4* tf = stage_tf(f, sm_tf);
   __syncthreads();
-  ExtShade sh{&e};
+  ExtShadeT<C> sh{&e};
   march_pixel(f, tf, sh);
 }
 
 // Directional light: the shadow boxes come from the per-frame table, staged
 // in shared memory after the transfer function.
-template <int NT, int MINB>
+template <int NT, int MINB, bool C>
 __global__ void __launch_bounds__(NT, MINB) k_march_extinction_dir(FrameArgs f, ExtArgs e,
                                                                     const __grid_constant__ ShadowBoxTable t) {
   extern __shared__ float4 sm_tf[];
@@ -43,7 +44,7 @@ __global__ void __launch_bounds__(NT, MINB) k_march_extinction_dir(FrameArgs f, 
     hi[i] = t.hi[i];
   }
   __syncthreads();
-  ExtShade sh{&e};
+  ExtShadeT<C> sh{&e};
   sh.tlo = lo; sh.thi = hi; sh.tn = t.n; sh.tax = t.axis;
   sh.tiw = t.interval; sh.tvmin = t.vmin; sh.tvmax = t.vmax;
   march_pixel(f, tf, sh);
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps_x = J.f.tile_w >> 3;
     const int px = (int)(local % J.blocks_x) * J.f.tile_w + (warp % warps_x) * 8 + (lane & 7);
     const int py = (int)(local / J.blocks_x) * J.f.tile_h + (warp / warps_x) * 4 + (lane >> 3);
-    ExtShade sh{&J.e};
+    ExtShade sh{&J.e};  // the int64 table: a batch's jobs share no frame-sized compact table
     if (J.tn > 0) {
       sh.tlo = sm_bt + J.f.tf_n; sh.thi = sm_bt + J.f.tf_n + J.tn; sh.tn = J.tn; sh.tax = J.tax;
       sh.tiw = J.tiw; sh.tvmin = J.tvmin; sh.tvmax = J.tvmax;
@@ -188,12 +189,15 @@ cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigne
 
 template <int NT, int MINB>
 static void launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+  const bool c = e.sat.sat32 != nullptr;
   if (table) {
     size_t sm = sizeof(float4) * (f.tf_n + 2 * table->n);
-    k_march_extinction_dir<NT, MINB><<<grid_of(f), NT, sm, st>>>(f, e, *table);
+    if (c) k_march_extinction_dir<NT, MINB, true><<<grid_of(f), NT, sm, st>>>(f, e, *table);
+    else k_march_extinction_dir<NT, MINB, false><<<grid_of(f), NT, sm, st>>>(f, e, *table);
   } else {
     size_t sm = sizeof(float4) * f.tf_n;
-    k_march_extinction<NT, MINB><<<grid_of(f), NT, sm, st>>>(f, e);
+    if (c) k_march_extinction<NT, MINB, true><<<grid_of(f), NT, sm, st>>>(f, e);
+    else k_march_extinction<NT, MINB, false><<<grid_of(f), NT, sm, st>>>(f, e);
   }
 }
 

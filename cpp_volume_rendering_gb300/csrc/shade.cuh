@@ -121,7 +121,9 @@ struct PlainShade {
 };
 
 // ====================================================== extinction (rc1pextbsd)
-struct ExtShade {
+// COMPACT: the frame's SAT box queries read the 32-bit table (SatView::sat32).
+template <bool COMPACT = false>
+struct ExtShadeT {
   const ExtArgs* e;
   // Per-frame box table of a directional light (shared memory), or nullptr.
   const float4* tlo = nullptr;
@@ -136,7 +138,7 @@ struct ExtShade {
     const SatView& S = e->sat;
     p1 = clamp3(p1 + f.vol.spacing, S.min_pos, S.max_pos);
     p2 = clamp3(p2 + f.vol.spacing, S.min_pos, S.max_pos);
-    return sat_box(S, p1, p2);
+    return sat_box<COMPACT>(S, p1, p2);
   }
 
   // ExtinctionAmbientOcclusion (ebs_ray_bbox_marching.comp:112-146), with the
@@ -165,7 +167,7 @@ struct ExtShade {
     const SatView& S = e->sat;
     p1 = clamp3(p1 + sc, S.min_pos, S.max_pos);
     p2 = clamp3(p2 + sc, S.min_pos, S.max_pos);
-    return (sat_box(S, p1, p2) / volq) * e->ui_weight;
+    return (sat_box<COMPACT>(S, p1, p2) / volq) * e->ui_weight;
   }
 
   // ConeZAxis (ebs_ray_bbox_marching.comp:190-270).
@@ -290,7 +292,7 @@ struct ExtShade {
       const float4 hi = thi[k];
       float3 p1 = clamp3(tx + f3(lo.x, lo.y, lo.z) + sc, S.min_pos, S.max_pos);
       float3 p2 = clamp3(tx + f3(hi.x, hi.y, hi.z) + sc, S.min_pos, S.max_pos);
-      st = fmaf(sat_box(S, p1, p2), hi.w, st);
+      st = fmaf(sat_box<COMPACT>(S, p1, p2), hi.w, st);
       ++aux;
     }
     return expf(-st);
@@ -321,6 +323,7 @@ struct ExtShade {
     return src;
   }
 };
+using ExtShade = ExtShadeT<false>;
 
 // ==================================================== cone DOS (rc1pdosct)
 struct DosShade {

@@ -292,6 +292,18 @@ cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
  * or the size changed.  Results do not depend on it. */
 cvr_status cvr_set_brick_size(cvr_ctx* ctx, int edge);
 int cvr_get_brick_size(cvr_ctx* ctx);
+/* Compact SAT (no reference counterpart; default on): frames of
+ * CVR_METHOD_EXTINCTION whose box queries all span a bounded region (the
+ * ambient-occlusion boxes and, for directional shadows, the per-frame cone
+ * boxes) read a 32-bit copy of the SAT: prefix sums of round(sigma * 2^F32)
+ * modulo 2^32, F32 chosen per frame so that every sub-box sum stays below
+ * 2^31 and its wrapped differences are exact; half the bytes and integer
+ * work of the int64 table.  Frames where that would resolve the largest
+ * extinction in fewer than 2^15 steps (very large boxes), point-light cone
+ * shadows, batches and the light cache keep the int64 table.  0 disables it. */
+cvr_status cvr_set_compact_sat(cvr_ctx* ctx, int enable);
+int cvr_get_compact_sat(cvr_ctx* ctx);
+
 /* Object-space light cache (PreIlluminationStructuredVolume,
  * cppvolrend/utils/preillumination.h:15-47; reference default 32^3, off):
  * when on, CVR_METHOD_EXTINCTION and CVR_METHOD_CONE_DOS evaluate occlusion

@@ -47,6 +47,8 @@ def test_volume_slots_keep_their_tables(ctx):
                                                          (abi.SAMPLING_TEX_FEATURES, (32, 8), 1, 8),
                                                          (abi.SAMPLING_TEX_FEATURES, (8, 8), 2, 16)])
 def test_batch_equals_single_renders(ctx, sampling, tile, variant, brick):
+    # batches read the int64 SAT; the single renders compared with them do too
+    abi.check(ctx.lib.cvr_set_compact_sat(ctx.h, 0), ctx.h)
     ctx.set_sampling(sampling)
     abi.check(ctx.lib.cvr_set_tuning(ctx.h, tile[0], tile[1], variant), ctx.h)
     abi.check(ctx.lib.cvr_set_brick_size(ctx.h, brick), ctx.h)
@@ -91,6 +93,7 @@ def test_batch_equals_single_renders(ctx, sampling, tile, variant, brick):
             assert np.isfinite(img).all() and img[..., 3].max() > 0
         assert not mismatches, mismatches
     finally:
+        abi.check(ctx.lib.cvr_set_compact_sat(ctx.h, 1), ctx.h)
         ctx.select_volume(0)
         ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
         abi.check(ctx.lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
