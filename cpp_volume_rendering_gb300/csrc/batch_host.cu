@@ -26,11 +26,15 @@ struct cvr_batch {
   bool sur_tex = false;
   unsigned int* d_counters = nullptr;  // [0] extinction tiles, [1] surrogate rays
   unsigned long long* d_stats = nullptr;  // 3 per job, in the caller's job order
+  bool ext_compact = false;
+  std::vector<unsigned*> sat32;           // the batch's own compact SATs, one per volume slot used
   cudaGraphExec_t graph = nullptr;
   ~cvr_batch() {
     if (graph) cudaGraphExecDestroy(graph);
     void* bufs[] = {d_ext, d_tables, d_sur, d_counters, d_stats};
     for (void* p : bufs)
+      if (p) cudaFree(p);
+    for (unsigned* p : sat32)
       if (p) cudaFree(p);
   }
 };
@@ -97,6 +101,9 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   CK(c, cudaMalloc((void**)&b->d_stats, sizeof(unsigned long long) * 3 * n_jobs));
   CK(c, cudaMalloc((void**)&b->d_counters, sizeof(unsigned int) * 2));
   std::vector<BatchExtJob> ext;
+  std::vector<int> ext_slot;
+  double slot_vmax[CVR_MAX_VOLUMES] = {};
+  bool all_compact = c->compact_sat;
   std::vector<std::vector<float4>> tables;
   std::vector<SurJob> sur;
   const int keep = c->cur_slot;
@@ -114,8 +121,12 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
     if (j.method == CVR_METHOD_EXTINCTION) {
       BatchExtJob J{};
       const ShadowBoxTable* table = nullptr;
-      st = ext_args(c, static_cast<const cvr_ext_params*>(j.params), &j.light, f, &J.e, &table);
+      double vmax = 0.0;
+      st = ext_args(c, static_cast<const cvr_ext_params*>(j.params), &j.light, f, &J.e, &table, &vmax);
       if (st != CVR_OK) break;
+      if (vmax > 0.0) slot_vmax[j.volume] = std::max(slot_vmax[j.volume], vmax);
+      else all_compact = false;
+      ext_slot.push_back(j.volume);
       J.f = f;
       J.blocks_x = (unsigned)((j.width + f.tile_w - 1) / f.tile_w);
       J.first_block = b->ext_blocks;
@@ -141,6 +152,34 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
       J.first_tile = b->sur_rays / 32u;
       b->sur_rays += (unsigned)J.tiles_x * (unsigned)((j.height + 3) / 4) * 32u;
       sur.push_back(J);
+    }
+  }
+  // Compact SATs owned by the batch (a later frame may rebuild the context's
+  // own at another fixed point): one per slot, at the largest region of its jobs
+  if (st == CVR_OK && all_compact && !ext.empty()) {
+    float inv[CVR_MAX_VOLUMES] = {};
+    unsigned* tab[CVR_MAX_VOLUMES] = {};
+    for (int v = 0; v < CVR_MAX_VOLUMES && st == CVR_OK && all_compact; ++v) {
+      if (slot_vmax[v] <= 0.0) continue;
+      select_slot(c, v);
+      int F;
+      std::vector<unsigned> q;
+      if (!compact_plan(c->sat_ext, slot_vmax[v], &F, &q)) { all_compact = false; break; }
+      const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+      unsigned* d = nullptr;
+      cudaError_t e = cudaMalloc((void**)&d, cells * sizeof(unsigned));
+      if (e != cudaSuccess) { st = cuda_fail(c, e, "cvr_batch_create: compact SAT"); break; }
+      b->sat32.push_back(d);
+      st = build_compact_sat(c, q, d);
+      tab[v] = d;
+      inv[v] = (float)std::ldexp(1.0, -F);
+    }
+    if (st == CVR_OK && all_compact) {
+      for (size_t k = 0; k < ext.size(); ++k) {
+        ext[k].e.sat.sat32 = tab[ext_slot[k]];
+        ext[k].e.sat.inv_scale32 = inv[ext_slot[k]];
+      }
+      b->ext_compact = true;
     }
   }
   select_slot(c, keep);
@@ -179,7 +218,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stats, 0, sizeof(unsigned long long) * 3 * n_jobs, c->stream);
   if (e == cudaSuccess && b->n_ext)
     e = launch_batch_extinction(b->d_ext, b->n_ext, b->ext_blocks, b->d_counters, c->tf_n, b->ext_max_table,
-                                b->ext_threads, b->ext_variant, c->stream);
+                                b->ext_threads, b->ext_variant, b->ext_compact, c->stream);
   if (e == cudaSuccess && b->n_sur)
     e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->ext_variant,
                                b->d_counters + 1, c->mlp->err, c->stream);

@@ -162,7 +162,7 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
 }
 
 cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light, const FrameArgs& f, ExtArgs* eo,
-                    const ShadowBoxTable** table) {
+                    const ShadowBoxTable** table, double* vmax_out) {
   if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: extinction SAT not built");
   if (p->apply_occlusion && (p->ao_n_shells < 1 || p->ao_n_shells > CVR_MAX_AO_SHELLS))
     return fail(c, CVR_ERR_INVALID_ARG, "ao_n_shells must be in [1, 32]");
@@ -191,6 +191,7 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
   }
   // The compact table serves the frame when the largest region any of its
   // box queries spans is known (AO boxes; shadow boxes of a per-frame table)
+  if (vmax_out) *vmax_out = 0.0;
   if (c->compact_sat && (p->apply_occlusion || p->apply_shadow) && (!p->apply_shadow || *table)) {
     const float3 sc = f.vol.spacing;
     const double sv[3] = {sc.x, sc.y, sc.z};
@@ -214,53 +215,75 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
         vmax = std::max(vmax, v);
       }
     }
-    float inv_scale32 = 0.0f;
-    cvr_status cs = ensure_compact_sat(c, vmax, &inv_scale32);
-    if (cs != CVR_OK) return cs;
-    if (inv_scale32 > 0.0f) {
-      a.sat.sat32 = c->d_sat32;
-      a.sat.inv_scale32 = inv_scale32;
+    if (vmax_out) {
+      *vmax_out = vmax;  // the caller builds the table (batches own theirs)
+    } else {
+      float inv_scale32 = 0.0f;
+      cvr_status cs = ensure_compact_sat(c, vmax, &inv_scale32);
+      if (cs != CVR_OK) return cs;
+      if (inv_scale32 > 0.0f) {
+        a.sat.sat32 = c->d_sat32;
+        a.sat.inv_scale32 = inv_scale32;
+      }
     }
   }
   *eo = a;
   return CVR_OK;
 }
 
-// The compact SAT for queries spanning at most vmax cells: fixed point
+// The fixed point of a compact SAT for queries spanning at most vmax cells:
 // round(sigma * 2^F32) with F32 the largest that keeps vmax * max q below
 // 2^31, so every sub-box sum, and so every wrapped 32-bit difference of the
-// table, is exact.  Used only while that resolution stays at 2^15 or more
-// steps per largest extinction (the FP32 table of the reference resolves far
-// less); *inv_scale = 2^-F32, or 0 when the frame keeps the int64 table.
-cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
-  *inv_scale = 0.0f;
-  if (c->sat_ext.empty() || !(vmax >= 1.0)) return CVR_OK;
+// table, is exact.  False when that would resolve the largest extinction in
+// fewer than 2^15 steps (the FP32 table of the reference resolves far less).
+bool compact_plan(const std::vector<double>& ext, double vmax, int* F_out, std::vector<unsigned>* q) {
+  if (ext.empty() || !(vmax >= 1.0)) return false;
   double maxv = 0.0;
-  for (double v : c->sat_ext) maxv = std::max(maxv, v);
+  for (double v : ext) maxv = std::max(maxv, v);
   const double limit = 2147483647.0;
   int F = maxv > 0.0 ? (int)std::floor(std::log2(limit / (vmax * maxv))) : 0;
   F = std::min(F, 52);
-  std::vector<unsigned> q(c->sat_ext.size());
+  q->resize(ext.size());
   for (;; --F) {
     const double scale = std::ldexp(1.0, F);
     double qmax = 0.0;
-    for (size_t i = 0; i < q.size(); ++i) {
-      const double r = std::nearbyint(c->sat_ext[i] * scale);
+    for (size_t i = 0; i < q->size(); ++i) {
+      const double r = std::nearbyint(ext[i] * scale);
       qmax = std::max(qmax, r);
-      q[i] = (unsigned)r;
+      (*q)[i] = (unsigned)r;
     }
     if (qmax * vmax < limit || F < -64) {
-      if (maxv > 0.0 && qmax < 32768.0) return CVR_OK;  // too coarse: the int64 table
+      if (maxv > 0.0 && qmax < 32768.0) return false;
       break;
     }
   }
+  *F_out = F;
+  return true;
+}
+
+// Builds the compact table of the current volume from q into dst (synchronous).
+cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, unsigned* dst) {
+  CK(c, ensure(c->d_lut32, c->lut32_cap, sizeof(unsigned) * q.size()));
+  CK(c, cudaMemcpyAsync(c->d_lut32, q.data(), sizeof(unsigned) * q.size(), cudaMemcpyHostToDevice, c->stream));
+  CK(c, launch_sat_build32(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, dst, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));  // q is a host temporary
+  return CVR_OK;
+}
+
+// The context's compact SAT for a frame whose queries span at most vmax
+// cells, rebuilt when its fixed point changes; *inv_scale = 2^-F32, or 0 when
+// the frame keeps the int64 table.
+cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
+  *inv_scale = 0.0f;
+  int F;
+  std::vector<unsigned> q;
+  if (!compact_plan(c->sat_ext, vmax, &F, &q)) return CVR_OK;
   if (c->sat32_F != F || !c->d_sat32) {
     const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-    CK(c, ensure(c->d_lut32, c->lut32_cap, sizeof(unsigned) * q.size()));
-    CK(c, cudaMemcpyAsync(c->d_lut32, q.data(), sizeof(unsigned) * q.size(), cudaMemcpyHostToDevice, c->stream));
     CK(c, ensure(c->d_sat32, c->sat32_cap, cells * sizeof(unsigned)));
-    CK(c, launch_sat_build32(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, c->d_sat32, c->stream));
-    CK(c, cudaStreamSynchronize(c->stream));  // q is a host temporary
+    c->sat32_F = kNoCompactSat;
+    cvr_status st = build_compact_sat(c, q, c->d_sat32);
+    if (st != CVR_OK) return st;
     c->sat32_F = F;
   }
   *inv_scale = (float)std::ldexp(1.0, -F);

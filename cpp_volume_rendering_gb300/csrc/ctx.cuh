@@ -362,12 +362,18 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
                       FrameArgs* f, bool need_tf = true);
 // Extinction arguments of the current volume; *table: the directional
 // shadow-box table (context-owned staging, valid until the next call) or null.
+// With vmax_out the compact SAT is left to the caller: *vmax_out = the largest
+// region the frame's queries span (0: the frame cannot use a compact table).
 cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light, const FrameArgs& f, ExtArgs* e,
-                    const ShadowBoxTable** table);
+                    const ShadowBoxTable** table, double* vmax_out = nullptr);
 // The compact 32-bit SAT for a frame whose box queries span at most vmax
 // cells, (re)built when its fixed point changes; *inv_scale = 2^-F32, or 0
 // when the frame keeps the int64 table.
 cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale);
+// The pieces of it: the fixed point (false: keep the int64 table) and the
+// build of the current volume's compact table into dst.
+bool compact_plan(const std::vector<double>& ext, double vmax, int* F, std::vector<unsigned>* q);
+cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, unsigned* dst);
 // Surrogate arguments of the current volume (pyramid, textures, network).
 cvr_status sur_job_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light, SurArgs* a, bool* tex);
 // The CVR_METHOD_SURROGATE launch of cvr_render.

@@ -96,7 +96,7 @@ cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
 // Batched extinction frames: persistent CTAs take tiles of all jobs from one
 // counter; the job descriptor, transfer function and shadow table are staged
 // in shared memory whenever a CTA moves to another job.
-template <int NT, int MINB>
+template <int NT, int MINB, bool C>
 __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob* __restrict__ jobs, int n_jobs,
                                                                 unsigned total, unsigned* counter) {
   __shared__ BatchExtJob J;
@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps_x = J.f.tile_w >> 3;
     const int px = (int)(local % J.blocks_x) * J.f.tile_w + (warp % warps_x) * 8 + (lane & 7);
     const int py = (int)(local / J.blocks_x) * J.f.tile_h + (warp / warps_x) * 4 + (lane >> 3);
-    ExtShade sh{&J.e};  // the int64 table: a batch's jobs share no frame-sized compact table
+    ExtShadeT<C> sh{&J.e};
     if (J.tn > 0) {
       sh.tlo = sm_bt + J.f.tf_n; sh.thi = sm_bt + J.f.tf_n + J.tn; sh.tn = J.tn; sh.tax = J.tax;
       sh.tiw = J.tiw; sh.tvmin = J.tvmin; sh.tvmax = J.tvmax;
@@ -151,8 +151,8 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
 
 template <int NT, int MINB>
 static cudaError_t launch_batch_t(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
-                                  size_t smem, cudaStream_t st) {
-  auto kern = k_batch_extinction<NT, MINB>;
+                                  size_t smem, bool compact, cudaStream_t st) {
+  auto kern = compact ? k_batch_extinction<NT, MINB, true> : k_batch_extinction<NT, MINB, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -173,13 +173,14 @@ constexpr int minb_of(int variant) {
 }
 
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
-                                    int tf_n, int max_table, int tile_threads, int variant, cudaStream_t st) {
+                                    int tf_n, int max_table, int tile_threads, int variant, bool compact,
+                                    cudaStream_t st) {
   const size_t smem = sizeof(float4) * (tf_n + 2 * max_table);
 #define CVR_BATCH(NT)                                                                                          \
   switch (variant) {                                                                                          \
-    case 1: return launch_batch_t<NT, minb_of<NT>(1)>(jobs, n_jobs, total_blocks, counter, smem, st);        \
-    case 2: return launch_batch_t<NT, minb_of<NT>(2)>(jobs, n_jobs, total_blocks, counter, smem, st);        \
-    default: return launch_batch_t<NT, 1>(jobs, n_jobs, total_blocks, counter, smem, st);                    \
+    case 1: return launch_batch_t<NT, minb_of<NT>(1)>(jobs, n_jobs, total_blocks, counter, smem, compact, st); \
+    case 2: return launch_batch_t<NT, minb_of<NT>(2)>(jobs, n_jobs, total_blocks, counter, smem, compact, st); \
+    default: return launch_batch_t<NT, 1>(jobs, n_jobs, total_blocks, counter, smem, compact, st);           \
   }
   if (tile_threads == 64) { CVR_BATCH(64) }
   if (tile_threads == 256) { CVR_BATCH(256) }

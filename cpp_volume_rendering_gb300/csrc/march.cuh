@@ -138,9 +138,11 @@ struct BatchExtJob {
 
 // Persistent launch over all tiles of all jobs (jobs ordered by first_block):
 // each CTA takes tiles from *counter (zeroed before the launch).  variant as
-// in FrameArgs; max_table = the largest shadow table of the jobs.
+// in FrameArgs; max_table = the largest shadow table of the jobs; compact:
+// every job reads its compact SAT (ExtArgs::sat.sat32).
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
-                                    int tf_n, int max_table, int tile_threads, int variant, cudaStream_t st);
+                                    int tf_n, int max_table, int tile_threads, int variant, bool compact,
+                                    cudaStream_t st);
 
 // Object-space light cache (lightcache.cu).  Cells of dims[0] x dims[1] x
 // dims[2], x fastest, float2 (occlusion, shadow).  table: the directional

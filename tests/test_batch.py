@@ -110,3 +110,39 @@ def test_batch_rejects_other_methods(ctx):
     bh = C.c_void_p()
     arr = (abi.Job * 1)(j)
     assert ctx.lib.cvr_batch_create(ctx.h, arr, 1, C.byref(bh)) == abi.CVR_ERR_INVALID_ARG
+
+
+def test_batch_with_compact_sats(ctx):
+    """With the compact SAT on (the default) a batch builds one compact table
+    per volume at the largest region of its jobs; its images stay within 1/255
+    of the single renders (which choose the fixed point per frame)."""
+    vols = scene.batch_volumes(0.5)
+    scene.prepare_batch_volumes(ctx, vols)
+    small_network(ctx)
+    W = H = 40
+    mem = DeviceMemory()
+    try:
+        probe = scene.batch_jobs(vols, n_views=2, lights=scene.BATCH_LIGHTS[:2], image=W)
+        n = len(probe.jobs)
+        outs = [mem.alloc(W * H * 16, fill=0) for _ in range(n)]
+        b = scene.batch_jobs(vols, n_views=2, lights=scene.BATCH_LIGHTS[:2], image=W, out_ptrs=outs)
+        arr = (abi.Job * n)(*b.jobs)
+        bh = C.c_void_p()
+        abi.check(ctx.lib.cvr_batch_create(ctx.h, arr, n, C.byref(bh)), ctx.h)
+        try:
+            abi.check(ctx.lib.cvr_batch_run(bh), ctx.h)
+            abi.check(ctx.lib.cvr_sync(ctx.h), ctx.h)
+            got = [mem.download(p, (H, W, 4)) for p in outs]
+        finally:
+            ctx.lib.cvr_batch_destroy(bh)
+        worst = 0.0
+        for k, j in enumerate(b.jobs):
+            if j.method != abi.EXTINCTION:
+                continue
+            ctx.select_volume(j.volume)
+            img, _ = ctx.render(j.method, j.camera, j.light, b.params[k], W, H)
+            worst = max(worst, float(np.abs(img - got[k]).max()))
+        assert worst <= 1.0 / 255.0, worst
+    finally:
+        ctx.select_volume(0)
+        mem.close()
