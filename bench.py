@@ -640,6 +640,9 @@ def run_ours(args):
                       ctx.h)
             renderers[name] = {"workload": WORKLOAD_DESC[name], **tuned_frames(ctx, lib, w2)}
             abi.check(lib.cvr_set_light_cache(ctx.h, 0, 0, 0), ctx.h)
+            if rank == 0 and not args.no_cpu_baseline and name != "extinction_lightcache":
+                # the FP32 oracle on the host cores, a few seconds of rows of the same frame
+                renderers[name]["cpu_baseline"] = cpu_baseline(w2, target_s=args.cpu_seconds / 3.0)
         reset_tuning()
         if not args.no_gradient:
             gradient = gradient_section(ctx, lib, args)

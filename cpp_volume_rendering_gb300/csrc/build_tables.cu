@@ -106,6 +106,21 @@ cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int n
   return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
 }
 
+// x-pairs of a table: out[i] = (s[i], s[i + 1]) within each x row, the last
+// cell of a row paired with itself.
+__global__ void k_sat_pairs(const unsigned* __restrict__ s, uint2* __restrict__ out, int sx, long long cells) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cells) return;
+  const int x = (int)(i % sx);
+  out[i] = make_uint2(s[i], s[x + 1 < sx ? i + 1 : i]);
+}
+
+cudaError_t launch_sat_pairs(const unsigned* sat, uint2* out, int sx, int sy, int sz, cudaStream_t st) {
+  const long long cells = (long long)sx * sy * sz;
+  k_sat_pairs<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(sat, out, sx, cells);
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------------- pyramid
 // gen_extcoefvol_anysize.comp: base level voxel (i,j,k) holds the normalised
 // 7x7x7 Gaussian average (sigma S0, taps at integer multiples of S0) of the

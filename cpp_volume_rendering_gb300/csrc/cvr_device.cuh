@@ -176,8 +176,10 @@ struct SatView {
   // The compact copy for frames whose boxes are all small enough: the same
   // prefix sums of round(sigma * 2^F32) modulo 2^32 (F32 chosen so that every
   // sub-box sum of the frame's boxes is below 2^31, which makes their
-  // wrapped 32-bit differences exact); nullptr: frames use the int64 table.
-  const unsigned* sat32;
+  // wrapped 32-bit differences exact), stored as x-pairs: cell x holds
+  // (S[x], S[min(x + 1, sx - 1)]), the two taps of a GL_LINEAR lookup in one
+  // 8-byte load; nullptr: frames use the int64 table.
+  const uint2* sat32;
   float inv_scale32;     // 2^-F32
   int sx, sy, sz;        // SAT dims = volume dims + 2
   float inv_scale;       // 2^-F
@@ -213,20 +215,27 @@ __device__ __forceinline__ float ll_to_float(long long v) {
 // table, differences wrapping modulo 2^32 and read as signed at the end).
 template <class W>
 struct D3 { W d[3]; };  // consecutive x-differences of one row
-template <class W>
-__device__ __forceinline__ D3<W> row_diffs(const W* row, const BoxAxis& X) {
-  const W v0 = __ldg(row + X.s[0]), v1 = __ldg(row + X.s[1]);
-  const W v2 = __ldg(row + X.s[2]), v3 = __ldg(row + X.s[3]);
-  D3<W> r;
+__device__ __forceinline__ D3<long long> row_diffs(const long long* row, const BoxAxis& X) {
+  const long long v0 = __ldg(row + X.s[0]), v1 = __ldg(row + X.s[1]);
+  const long long v2 = __ldg(row + X.s[2]), v3 = __ldg(row + X.s[3]);
+  D3<long long> r;
   r.d[0] = v1 - v0; r.d[1] = v2 - v1; r.d[2] = v3 - v2;
+  return r;
+}
+// The x-pair table: taps a0, a1 from one load, b0, b1 from another (a1 and b1
+// are the clamped successors of a0 and b0, as compact_axis guarantees).
+__device__ __forceinline__ D3<unsigned> row_diffs(const uint2* row, const BoxAxis& X) {
+  const uint2 a = __ldg(row + X.s[0]), b = __ldg(row + X.s[2]);
+  D3<unsigned> r;
+  r.d[0] = a.y - a.x; r.d[1] = b.x - a.y; r.d[2] = b.y - b.x;
   return r;
 }
 template <class W>
 struct D9 { D3<W> y[3]; };  // consecutive y-differences of x-differenced rows
-template <class W>
-__device__ __forceinline__ D9<W> plane_diffs(const W* sat, const SatView& S, int z, const BoxAxis& X,
+template <class W, class T>
+__device__ __forceinline__ D9<W> plane_diffs(const T* sat, const SatView& S, int z, const BoxAxis& X,
                                              const BoxAxis& Y) {
-  const W* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
+  const T* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
   D9<W> r;
   D3<W> prev = row_diffs(plane + (size_t)Y.s[0] * S.sx, X);
 #pragma unroll
@@ -259,16 +268,21 @@ __device__ __forceinline__ float weigh9(const D9<W>& cur, const D9<W>& prev, con
 template <bool COMPACT>
 __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2) {
   using W = typename std::conditional<COMPACT, unsigned, long long>::type;
-  const W* sat;
+  using T = typename std::conditional<COMPACT, uint2, long long>::type;
+  const T* sat;
   if constexpr (COMPACT) sat = S.sat32; else sat = S.sat;
-  BoxAxis X = box_axis(fmaf(p1.x, S.inv_spacing.x, -0.5f), fmaf(p2.x, S.inv_spacing.x, -0.5f), S.sx);
+  // The clamped positions give texel coordinates in [0, sx - 1]; single
+  // precision can put the lowest a hair below 0, where floor would break the
+  // pair layout's successor taps: clamp it (the interpolated value is the same).
+  const float lx = fmaf(p1.x, S.inv_spacing.x, -0.5f), hx = fmaf(p2.x, S.inv_spacing.x, -0.5f);
+  BoxAxis X = COMPACT ? box_axis(fmaxf(lx, 0.0f), fmaxf(hx, 0.0f), S.sx) : box_axis(lx, hx, S.sx);
   BoxAxis Y = box_axis(fmaf(p1.y, S.inv_spacing.y, -0.5f), fmaf(p2.y, S.inv_spacing.y, -0.5f), S.sy);
   BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
   float acc = 0.0f;
-  D9<W> prev = plane_diffs(sat, S, Z.s[0], X, Y);
+  D9<W> prev = plane_diffs<W>(sat, S, Z.s[0], X, Y);
 #pragma unroll
   for (int g = 0; g < 3; ++g) {
-    D9<W> cur = plane_diffs(sat, S, Z.s[g + 1], X, Y);
+    D9<W> cur = plane_diffs<W>(sat, S, Z.s[g + 1], X, Y);
     acc = fmaf(Z.w[g], weigh9(cur, prev, X, Y), acc);
     prev = cur;
   }
