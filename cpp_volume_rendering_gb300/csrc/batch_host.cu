@@ -27,14 +27,14 @@ struct cvr_batch {
   unsigned int* d_counters = nullptr;  // [0] extinction tiles, [1] surrogate rays
   unsigned long long* d_stats = nullptr;  // 3 per job, in the caller's job order
   bool ext_compact = false;
-  std::vector<uint2*> sat32;              // the batch's own compact SATs, one per volume slot used
+  std::vector<uint4*> sat32;              // the batch's own compact SATs, one per volume slot used
   cudaGraphExec_t graph = nullptr;
   ~cvr_batch() {
     if (graph) cudaGraphExecDestroy(graph);
     void* bufs[] = {d_ext, d_tables, d_sur, d_counters, d_stats};
     for (void* p : bufs)
       if (p) cudaFree(p);
-    for (uint2* p : sat32)
+    for (uint4* p : sat32)
       if (p) cudaFree(p);
   }
 };
@@ -158,7 +158,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   // own at another fixed point): one per slot, at the largest region of its jobs
   if (st == CVR_OK && all_compact && !ext.empty()) {
     float inv[CVR_MAX_VOLUMES] = {};
-    uint2* tab[CVR_MAX_VOLUMES] = {};
+    uint4* tab[CVR_MAX_VOLUMES] = {};
     for (int v = 0; v < CVR_MAX_VOLUMES && st == CVR_OK && all_compact; ++v) {
       if (slot_vmax[v] <= 0.0) continue;
       select_slot(c, v);
@@ -166,8 +166,8 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
       std::vector<unsigned> q;
       if (!compact_plan(c->sat_ext, slot_vmax[v], &F, &q)) { all_compact = false; break; }
       const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-      uint2* d = nullptr;
-      cudaError_t e = cudaMalloc((void**)&d, cells * sizeof(uint2));
+      uint4* d = nullptr;
+      cudaError_t e = cudaMalloc((void**)&d, cells * sizeof(uint4));
       if (e != cudaSuccess) { st = cuda_fail(c, e, "cvr_batch_create: compact SAT"); break; }
       b->sat32.push_back(d);
       st = build_compact_sat(c, q, d);

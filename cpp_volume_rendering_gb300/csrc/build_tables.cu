@@ -106,18 +106,20 @@ cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int n
   return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
 }
 
-// x-pairs of a table: out[i] = (s[i], s[i + 1]) within each x row, the last
-// cell of a row paired with itself.
-__global__ void k_sat_pairs(const unsigned* __restrict__ s, uint2* __restrict__ out, int sx, long long cells) {
+// x-y quads of a table: out[(x, y, z)] = s at (x, y), (x', y), (x, y'),
+// (x', y') of plane z, with x' = min(x + 1, sx - 1), y' = min(y + 1, sy - 1).
+__global__ void k_sat_quads(const unsigned* __restrict__ s, uint4* __restrict__ out, int sx, int sy,
+                            long long cells) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cells) return;
-  const int x = (int)(i % sx);
-  out[i] = make_uint2(s[i], s[x + 1 < sx ? i + 1 : i]);
+  const int x = (int)(i % sx), y = (int)((i / sx) % sy);
+  const long long dx = x + 1 < sx ? 1 : 0, dy = y + 1 < sy ? sx : 0;
+  out[i] = make_uint4(s[i], s[i + dx], s[i + dy], s[i + dy + dx]);
 }
 
-cudaError_t launch_sat_pairs(const unsigned* sat, uint2* out, int sx, int sy, int sz, cudaStream_t st) {
+cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st) {
   const long long cells = (long long)sx * sy * sz;
-  k_sat_pairs<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(sat, out, sx, cells);
+  k_sat_quads<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(sat, out, sx, sy, cells);
   return cudaGetLastError();
 }
 

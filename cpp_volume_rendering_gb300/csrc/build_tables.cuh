@@ -11,8 +11,9 @@ cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz,
 // The same prefix sums of a 32-bit lut, wrapping modulo 2^32 (the compact table).
 cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
                                unsigned* sat, cudaStream_t st);
-// The x-pair layout of a (sx, sy, sz) table: (S[x], S[min(x + 1, sx - 1)]) per cell.
-cudaError_t launch_sat_pairs(const unsigned* sat, uint2* out, int sx, int sy, int sz, cudaStream_t st);
+// The x-y quad layout of a (sx, sy, sz) table: S at (x, y), (x', y), (x, y'),
+// (x', y') per cell, x' and y' the successors clamped to the table.
+cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st);
 
 // Builds every level of P (dims/offsets/grid filled by the caller) into data.
 cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, int tf_n, float s0,

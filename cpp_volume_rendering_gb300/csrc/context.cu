@@ -261,16 +261,16 @@ bool compact_plan(const std::vector<double>& ext, double vmax, int* F_out, std::
   return true;
 }
 
-// Builds the compact table of the current volume from q into dst, in x-pair
-// layout (synchronous; the plain 32-bit table is a temporary).
-cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint2* dst) {
+// Builds the compact table of the current volume from q into dst, in x-y
+// quad layout (synchronous; the plain 32-bit table is a temporary).
+cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint4* dst) {
   const int sx = c->nx + 2, sy = c->ny + 2, sz = c->nz + 2;
   CK(c, ensure(c->d_lut32, c->lut32_cap, sizeof(unsigned) * q.size()));
   CK(c, cudaMemcpyAsync(c->d_lut32, q.data(), sizeof(unsigned) * q.size(), cudaMemcpyHostToDevice, c->stream));
   unsigned* plain = nullptr;
   CK(c, cudaMalloc((void**)&plain, sizeof(unsigned) * (size_t)sx * sy * sz));
   cudaError_t e = launch_sat_build32(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, plain, c->stream);
-  if (e == cudaSuccess) e = launch_sat_pairs(plain, dst, sx, sy, sz, c->stream);
+  if (e == cudaSuccess) e = launch_sat_quads(plain, dst, sx, sy, sz, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // q is a host temporary
   cudaFree(plain);
   if (e != cudaSuccess) return cuda_fail(c, e, "compact SAT build");
@@ -287,7 +287,7 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
   if (!compact_plan(c->sat_ext, vmax, &F, &q)) return CVR_OK;
   if (c->sat32_F != F || !c->d_sat32) {
     const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-    CK(c, ensure(c->d_sat32, c->sat32_cap, cells * sizeof(uint2)));
+    CK(c, ensure(c->d_sat32, c->sat32_cap, cells * sizeof(uint4)));
     c->sat32_F = kNoCompactSat;
     cvr_status st = build_compact_sat(c, q, c->d_sat32);
     if (st != CVR_OK) return st;

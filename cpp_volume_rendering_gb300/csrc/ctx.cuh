@@ -107,7 +107,7 @@ struct VolSlot {
   int sat_frac_bits = 0;
   bool sat_ready = false;
   std::vector<double> sat_ext;
-  uint2* d_sat32 = nullptr;
+  uint4* d_sat32 = nullptr;
   size_t sat32_cap = 0;
   unsigned* d_lut32 = nullptr;
   size_t lut32_cap = 0;
@@ -173,7 +173,7 @@ struct cvr_ctx {
   // compact SAT (32-bit prefix sums modulo 2^32 at F32 fractional bits) for
   // frames whose boxes are small enough; the extinction table it is built from
   std::vector<double> sat_ext;
-  uint2* d_sat32 = nullptr;                  // x-pair layout
+  uint4* d_sat32 = nullptr;                  // x-y quad layout
   size_t sat32_cap = 0;
   unsigned* d_lut32 = nullptr;
   size_t lut32_cap = 0;
@@ -373,7 +373,7 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale);
 // The pieces of it: the fixed point (false: keep the int64 table) and the
 // build of the current volume's compact table into dst.
 bool compact_plan(const std::vector<double>& ext, double vmax, int* F, std::vector<unsigned>* q);
-cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint2* dst);
+cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint4* dst);
 // Surrogate arguments of the current volume (pyramid, textures, network).
 cvr_status sur_job_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light, SurArgs* a, bool* tex);
 // The CVR_METHOD_SURROGATE launch of cvr_render.

@@ -176,10 +176,11 @@ struct SatView {
   // The compact copy for frames whose boxes are all small enough: the same
   // prefix sums of round(sigma * 2^F32) modulo 2^32 (F32 chosen so that every
   // sub-box sum of the frame's boxes is below 2^31, which makes their
-  // wrapped 32-bit differences exact), stored as x-pairs: cell x holds
-  // (S[x], S[min(x + 1, sx - 1)]), the two taps of a GL_LINEAR lookup in one
-  // 8-byte load; nullptr: frames use the int64 table.
-  const uint2* sat32;
+  // wrapped 32-bit differences exact), stored as x-y quads: cell (x, y)
+  // holds S at (x, y), (x', y), (x, y'), (x', y') with x' = min(x + 1, sx - 1),
+  // y' = min(y + 1, sy - 1) -- the four taps of a GL_LINEAR lookup in a plane
+  // in one 16-byte load; nullptr: frames use the int64 table.
+  const uint4* sat32;
   float inv_scale32;     // 2^-F32
   int sx, sy, sz;        // SAT dims = volume dims + 2
   float inv_scale;       // 2^-F
@@ -222,25 +223,40 @@ __device__ __forceinline__ D3<long long> row_diffs(const long long* row, const B
   r.d[0] = v1 - v0; r.d[1] = v2 - v1; r.d[2] = v3 - v2;
   return r;
 }
-// The x-pair table: taps a0, a1 from one load, b0, b1 from another (a1 and b1
-// are the clamped successors of a0 and b0, as compact_axis guarantees).
-__device__ __forceinline__ D3<unsigned> row_diffs(const uint2* row, const BoxAxis& X) {
-  const uint2 a = __ldg(row + X.s[0]), b = __ldg(row + X.s[2]);
+__device__ __forceinline__ D3<unsigned> x_diffs(unsigned v0, unsigned v1, unsigned v2, unsigned v3) {
   D3<unsigned> r;
-  r.d[0] = a.y - a.x; r.d[1] = b.x - a.y; r.d[2] = b.y - b.x;
+  r.d[0] = v1 - v0; r.d[1] = v2 - v1; r.d[2] = v3 - v2;
   return r;
 }
 template <class W>
 struct D9 { D3<W> y[3]; };  // consecutive y-differences of x-differenced rows
-template <class W, class T>
-__device__ __forceinline__ D9<W> plane_diffs(const T* sat, const SatView& S, int z, const BoxAxis& X,
-                                             const BoxAxis& Y) {
-  const T* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
-  D9<W> r;
-  D3<W> prev = row_diffs(plane + (size_t)Y.s[0] * S.sx, X);
+// The quad table: the 16 taps of a plane from four 16-byte loads (the second
+// tap of each axis pair is the clamped successor of the first, as sat_box's
+// coordinate clamp guarantees).
+__device__ __forceinline__ D9<unsigned> plane_diffs_quad(const uint4* sat, const SatView& S, int z,
+                                                         const BoxAxis& X, const BoxAxis& Y) {
+  const uint4* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
+  const uint4* r0 = plane + (size_t)Y.s[0] * S.sx;
+  const uint4* r2 = plane + (size_t)Y.s[2] * S.sx;
+  const uint4 q00 = __ldg(r0 + X.s[0]), q01 = __ldg(r0 + X.s[2]);
+  const uint4 q10 = __ldg(r2 + X.s[0]), q11 = __ldg(r2 + X.s[2]);
+  const D3<unsigned> rows[4] = {x_diffs(q00.x, q00.y, q01.x, q01.y), x_diffs(q00.z, q00.w, q01.z, q01.w),
+                                x_diffs(q10.x, q10.y, q11.x, q11.y), x_diffs(q10.z, q10.w, q11.z, q11.w)};
+  D9<unsigned> r;
+#pragma unroll
+  for (int b = 0; b < 3; ++b)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) r.y[b].d[a] = rows[b + 1].d[a] - rows[b].d[a];
+  return r;
+}
+__device__ __forceinline__ D9<long long> plane_diffs(const long long* sat, const SatView& S, int z,
+                                                     const BoxAxis& X, const BoxAxis& Y) {
+  const long long* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
+  D9<long long> r;
+  D3<long long> prev = row_diffs(plane + (size_t)Y.s[0] * S.sx, X);
 #pragma unroll
   for (int b = 0; b < 3; ++b) {
-    D3<W> cur = row_diffs(plane + (size_t)Y.s[b + 1] * S.sx, X);
+    D3<long long> cur = row_diffs(plane + (size_t)Y.s[b + 1] * S.sx, X);
 #pragma unroll
     for (int a = 0; a < 3; ++a) r.y[b].d[a] = cur.d[a] - prev.d[a];
     prev = cur;
@@ -268,21 +284,26 @@ __device__ __forceinline__ float weigh9(const D9<W>& cur, const D9<W>& prev, con
 template <bool COMPACT>
 __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2) {
   using W = typename std::conditional<COMPACT, unsigned, long long>::type;
-  using T = typename std::conditional<COMPACT, uint2, long long>::type;
+  using T = typename std::conditional<COMPACT, uint4, long long>::type;
   const T* sat;
   if constexpr (COMPACT) sat = S.sat32; else sat = S.sat;
-  // The clamped positions give texel coordinates in [0, sx - 1]; single
+  // The clamped positions give texel coordinates in [0, s - 1]; single
   // precision can put the lowest a hair below 0, where floor would break the
-  // pair layout's successor taps: clamp it (the interpolated value is the same).
+  // quad layout's successor taps: clamp it (the interpolated value is the same).
   const float lx = fmaf(p1.x, S.inv_spacing.x, -0.5f), hx = fmaf(p2.x, S.inv_spacing.x, -0.5f);
+  const float ly = fmaf(p1.y, S.inv_spacing.y, -0.5f), hy = fmaf(p2.y, S.inv_spacing.y, -0.5f);
   BoxAxis X = COMPACT ? box_axis(fmaxf(lx, 0.0f), fmaxf(hx, 0.0f), S.sx) : box_axis(lx, hx, S.sx);
-  BoxAxis Y = box_axis(fmaf(p1.y, S.inv_spacing.y, -0.5f), fmaf(p2.y, S.inv_spacing.y, -0.5f), S.sy);
+  BoxAxis Y = COMPACT ? box_axis(fmaxf(ly, 0.0f), fmaxf(hy, 0.0f), S.sy) : box_axis(ly, hy, S.sy);
   BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
+  auto plane = [&](int z) {
+    if constexpr (COMPACT) return plane_diffs_quad(sat, S, z, X, Y);
+    else return plane_diffs(sat, S, z, X, Y);
+  };
   float acc = 0.0f;
-  D9<W> prev = plane_diffs<W>(sat, S, Z.s[0], X, Y);
+  D9<W> prev = plane(Z.s[0]);
 #pragma unroll
   for (int g = 0; g < 3; ++g) {
-    D9<W> cur = plane_diffs<W>(sat, S, Z.s[g + 1], X, Y);
+    D9<W> cur = plane(Z.s[g + 1]);
     acc = fmaf(Z.w[g], weigh9(cur, prev, X, Y), acc);
     prev = cur;
   }
