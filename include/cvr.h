@@ -297,10 +297,11 @@ int cvr_get_brick_size(cvr_ctx* ctx);
  * ambient-occlusion boxes and, for directional shadows, the per-frame cone
  * boxes) read a 32-bit copy of the SAT: prefix sums of round(sigma * 2^F32)
  * modulo 2^32, F32 chosen per frame so that every sub-box sum stays below
- * 2^31 and its wrapped differences are exact; half the bytes and integer
- * work of the int64 table.  Frames where that would resolve the largest
+ * 2^31 and its wrapped differences are exact, stored as x-y quads (the four
+ * taps of a plane in one load).  Frames where that would resolve the largest
  * extinction in fewer than 2^15 steps (very large boxes), point-light cone
- * shadows, batches and the light cache keep the int64 table.  0 disables it. */
+ * shadows and the light cache keep the int64 table; batches build their own.
+ * 0 disables it. */
 cvr_status cvr_set_compact_sat(cvr_ctx* ctx, int enable);
 int cvr_get_compact_sat(cvr_ctx* ctx);
 
