@@ -192,7 +192,23 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
   // The compact table serves the frame when the largest region any of its
   // box queries spans is known (AO boxes; shadow boxes of a per-frame table)
   if (vmax_out) *vmax_out = 0.0;
-  if (c->compact_sat && (p->apply_occlusion || p->apply_shadow) && (!p->apply_shadow || *table)) {
+  // Without a per-frame table (point lights, or more boxes than it holds) the
+  // cone direction varies per sample; its dominant component is at least
+  // 1/sqrt(3), so the cone axis leans at most atan(sqrt(2)) off the walk axis
+  // and a box's lateral extent at depth zm is at most
+  // zm (tan(lean + angle) - tan(lean - angle)) plus one voxel of rounding, with
+  // zm below max_dist + interval.  Unbounded when lean + angle reaches 90 deg.
+  double cone_extent = -1.0;  // world units, < 0: unknown
+  if (p->apply_shadow && !*table) {
+    const double lean = std::atan(std::sqrt(2.0)), ang = std::fabs((double)p->sdw_cone_angle_rad);
+    const double msc = std::max((double)f.vol.spacing.x, std::max((double)f.vol.spacing.y, (double)f.vol.spacing.z));
+    const double iw = (double)p->sdw_sample_interval * msc;
+    if (lean + ang < 1.5 && std::isfinite((double)p->sdw_max_distance) && p->sdw_max_distance >= 0.0f) {
+      const double zm = (double)p->sdw_max_distance + iw;
+      cone_extent = std::max(zm * (std::tan(lean + ang) - std::tan(lean - ang)) + msc, iw);
+    }
+  }
+  if (c->compact_sat && (p->apply_occlusion || p->apply_shadow) && (!p->apply_shadow || *table || cone_extent >= 0.0)) {
     const float3 sc = f.vol.spacing;
     const double sv[3] = {sc.x, sc.y, sc.z};
     const int n[3] = {c->nx, c->ny, c->nz};
@@ -207,7 +223,15 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
       for (int ax = 0; ax < 3; ++ax) v *= cells(2.0 * rmax * sv[ax], ax);
       vmax = std::max(vmax, v);
     }
-    if (p->apply_shadow) {
+    if (p->apply_shadow && !*table) {
+      // lateral extent on two axes, one interval along the walk's (any) axis
+      const double iw = (double)p->sdw_sample_interval;
+      for (int walk = 0; walk < 3; ++walk) {
+        double v = 1.0;
+        for (int ax = 0; ax < 3; ++ax) v *= ax == walk ? cells(iw * sv[ax], ax) : cells(cone_extent, ax);
+        vmax = std::max(vmax, v);
+      }
+    } else if (p->apply_shadow) {
       const ShadowBoxTable& t = **table;
       for (int k = 0; k < t.n; ++k) {
         const double v = cells((double)t.hi[k].x - t.lo[k].x, 0) * cells((double)t.hi[k].y - t.lo[k].y, 1) *

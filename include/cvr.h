@@ -299,9 +299,9 @@ int cvr_get_brick_size(cvr_ctx* ctx);
  * modulo 2^32, F32 chosen per frame so that every sub-box sum stays below
  * 2^31 and its wrapped differences are exact, stored as x-y quads (the four
  * taps of a plane in one load).  Frames where that would resolve the largest
- * extinction in fewer than 2^15 steps (very large boxes), point-light cone
- * shadows and the light cache keep the int64 table; batches build their own.
- * 0 disables it. */
+ * extinction in fewer than 2^15 steps (very large boxes), point-light cones
+ * too wide to bound (lean + angle >= 90 degrees) and the light cache keep the
+ * int64 table; batches build their own.  0 disables it. */
 cvr_status cvr_set_compact_sat(cvr_ctx* ctx, int enable);
 int cvr_get_compact_sat(cvr_ctx* ctx);
 

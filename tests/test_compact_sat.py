@@ -13,10 +13,16 @@ from tests.test_gpu_parity import compare
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("radii,shadow_type", [((2, 6, 16), 1), ((1, 3), 1), ((3, 9, 40), 1), ((2, 6), 0)])
-def test_compact_and_int64_frames_match_oracle(ctx, radii, shadow_type):
+# (AO radii, shadow type, cone angle): directional lights use the per-frame box
+# table; point lights the per-sample cone bound (a 0.7 rad cone is unbounded:
+# int64); AO radius 40 exceeds the compact table's resolution floor (int64)
+@pytest.mark.parametrize("radii,shadow_type,angle", [((2, 6, 16), 1, None), ((1, 3), 1, None), ((3, 9, 40), 1, None),
+                                                     ((2, 6), 0, None), ((2, 6), 0, 0.7)])
+def test_compact_and_int64_frames_match_oracle(ctx, radii, shadow_type, angle):
     wl = scene.workload("extinction", n=48, image=80)
     wl.params = scene.ext_params(scene.default_step(wl.spacing), wl.diagonal, ao_radii=radii, shadow_type=shadow_type)
+    if angle is not None:
+        wl.params.sdw_cone_angle_rad = angle
     if shadow_type == 0:
         f, u, r = scene.light_frame((0.3, 0.8, 0.5))
         wl.light = scene.light(abi.LIGHT_POINT, position=tuple(100.0 * np.array(f)), forward=f, up=u, right=r)
