@@ -271,7 +271,7 @@ def tuned_frames(ctx, lib, w2):
     abi.check(lib.cvr_get_frame_buffer(ctx.h, w2.width, w2.height, C.byref(o2)), ctx.h)
     entry = {}
     for key, flags in (("", abi.SAMPLING_TEX_FEATURES),
-                       ("tex_", abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)):
+                       ("tex_", abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME | abi.SAMPLING_TEX_PYRAMID)):
         ctx.set_sampling(flags)
         tw, th, tv = C.c_int(), C.c_int(), C.c_int()
         abi.check(lib.cvr_autotune(ctx.h, w2.method, C.byref(w2.cam), C.byref(w2.light), C.byref(w2.params),

@@ -37,6 +37,7 @@ MLP_INPUTS = 48
 SURROGATE_LEVELS = 6
 SAMPLING_TEX_FEATURES = 1
 SAMPLING_TEX_VOLUME = 2
+SAMPLING_TEX_PYRAMID = 4
 MLP_NOALLOC_MAX_POINTS = 8192
 MAX_VOLUMES = 16
 MAX_CONE_SECTIONS = 512

@@ -706,7 +706,14 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
           e = launch_march_cached(f, c->d_lcache, c->lc_dims, p->apply_occlusion, p->apply_shadow, p->ka, p->kd,
                                   c->stream);
       } else {
-        e = launch_dos(f, a, c->stream);
+        bool tex = false;
+        if (c->sampling & CVR_SAMPLING_TEX_PYRAMID) {
+          cvr_status ts = ensure_pyramid_textures(c);
+          if (ts != CVR_OK) return ts;
+          for (int l = 0; l < c->tex.n_pyr; ++l) a.ptex[l] = c->tex.pyr[l].tex;
+          tex = true;
+        }
+        e = launch_dos(f, a, tex, c->stream);
       }
       break;
     }

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(NT, MINB) k_march_extinction_dir(FrameArgs f, 
   march_pixel(f, tf, sh);
 }
 
-template <int NT>
+template <int NT, bool TEX>
 __global__ void __launch_bounds__(NT) k_march_dos(DosArgs d, FrameArgs f) {
   extern __shared__ float4 sm[];
   float4* tf = sm;
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(NT) k_march_dos(DosArgs d, FrameArgs f) {
   for (int i = threadIdx.x; i < d.occ.n_sections; i += blockDim.x) occ[i] = d.occ_sections[i];
   for (int i = threadIdx.x; i < d.sdw.n_sections; i += blockDim.x) sdw[i] = d.sdw_sections[i];
   __syncthreads();
-  DosShade sh{&d, occ, sdw};
+  DosShadeT<TEX> sh{&d, occ, sdw};
   march_pixel(f, tf, sh);
 }
 
@@ -220,22 +220,23 @@ cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const Shadow
   return cudaGetLastError();
 }
 
-template <int NT>
+template <int NT, bool TEX>
 static cudaError_t launch_dos_t(const FrameArgs& f, const DosArgs& d, size_t sm, cudaStream_t st) {
   if (sm > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(k_march_dos<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_march_dos<NT, TEX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_march_dos<NT><<<grid_of(f), NT, sm, st>>>(d, f);
+  k_march_dos<NT, TEX><<<grid_of(f), NT, sm, st>>>(d, f);
   return cudaGetLastError();
 }
 
-cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, cudaStream_t st) {
+cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, bool tex_pyramid, cudaStream_t st) {
   size_t sm = sizeof(float4) * (f.tf_n + d.occ.n_sections + d.sdw.n_sections);
   switch (threads_of(f)) {
-    case 64: return launch_dos_t<64>(f, d, sm, st);
-    case 256: return launch_dos_t<256>(f, d, sm, st);
-    default: return launch_dos_t<128>(f, d, sm, st);
+    case 64: return tex_pyramid ? launch_dos_t<64, true>(f, d, sm, st) : launch_dos_t<64, false>(f, d, sm, st);
+    case 256: return tex_pyramid ? launch_dos_t<256, true>(f, d, sm, st) : launch_dos_t<256, false>(f, d, sm, st);
+    default: return tex_pyramid ? launch_dos_t<128, true>(f, d, sm, st) : launch_dos_t<128, false>(f, d, sm, st);
   }
 }
 

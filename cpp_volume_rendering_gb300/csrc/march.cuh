@@ -75,6 +75,9 @@ struct ConeTableDev {
 
 struct DosArgs {
   PyramidView pyr;
+  // FP16 texture copies of the levels (the reference's R16F pyramid, sampled
+  // by the texture unit) when CVR_SAMPLING_TEX_PYRAMID is set, else unused
+  cudaTextureObject_t ptex[CVR_MAX_LEVELS];
   const float4* occ_sections;  // device, n_sections entries
   const float4* sdw_sections;
   ConeTableDev occ, sdw;
@@ -157,7 +160,8 @@ cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
 cudaError_t launch_iso(const FrameArgs& f, const IsoArgs& a, cudaStream_t st);
 // table == nullptr: per-sample cone geometry (point lights, or too many boxes).
 cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st);
-cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, cudaStream_t st);
+// tex_pyramid: the pyramid taps read d.ptex (FP16 level textures).
+cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, bool tex_pyramid, cudaStream_t st);
 cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st);
 
 }  // namespace cvr

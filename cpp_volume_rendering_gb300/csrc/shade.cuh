@@ -326,7 +326,9 @@ struct ExtShadeT {
 using ExtShade = ExtShadeT<false>;
 
 // ==================================================== cone DOS (rc1pdosct)
-struct DosShade {
+// TEX: the pyramid taps through the texture unit (DosArgs::ptex).
+template <bool TEX = false>
+struct DosShadeT {
   const DosArgs* d;
   const float4* occ_tab;  // shared-memory copies of the section tables
   const float4* sdw_tab;
@@ -340,7 +342,7 @@ struct DosShade {
 
   // GetGaussianExtinction with CONSIDER_BORDERS (ray_bbox_marching.comp:92-112).
   __device__ __forceinline__ float gauss_ext(float3 p, float level, const FrameArgs& f) const {
-    float rg = pyr_sample(d->pyr, level, p);
+    float rg = TEX ? pyr_sample_tex(level, p) : pyr_sample(d->pyr, level, p);
     float3 S = f.vol.grid;
     if (p.x < 0.0f || p.x > S.x || p.y < 0.0f || p.y > S.y || p.z < 0.0f || p.z > S.z) {
       float sg = exp2f(level);
@@ -349,6 +351,22 @@ struct DosShade {
       rg = rg * expf(-(dist) / (2.0f * sg * sg));
     }
     return rg;
+  }
+
+  // pyr_sample's GL_LINEAR_MIPMAP_LINEAR lookup on the level textures: hardware
+  // trilinear within a level (normalised coordinates, all levels span the
+  // grid), linear between the two levels of a fractional lod.
+  __device__ __forceinline__ float pyr_sample_tex(float lod, float3 p) const {
+    const PyramidView& P = d->pyr;
+    lod = fminf(fmaxf(lod, 0.0f), float(P.n_levels - 1));
+    const float fl = floorf(lod);
+    const int l0 = int(fl);
+    const float t = lod - fl;
+    const float u = p.x * P.inv_grid.x, v = p.y * P.inv_grid.y, w = p.z * P.inv_grid.z;
+    const float a = tex3D<float>(d->ptex[l0], u, v, w);
+    if (t == 0.0f) return a;
+    const float b = tex3D<float>(d->ptex[min(l0 + 1, P.n_levels - 1)], u, v, w);
+    return fmaf(t, b - a, a);
   }
 
   // Cone1/3/7Ray{Occlusion,Shadow} (ray_bbox_marching.comp:124-322, 345-531):
@@ -455,6 +473,8 @@ struct DosShade {
     return src;
   }
 };
+using DosShade = DosShadeT<false>;
+
 
 // ================================================= ground truth (rc1pcrtgt)
 struct GtShade {

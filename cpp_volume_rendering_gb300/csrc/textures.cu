@@ -120,7 +120,7 @@ extern "C" {
 
 cvr_status cvr_set_sampling(cvr_ctx* c, int flags) {
   if (!c) return CVR_ERR_INVALID_ARG;
-  if (flags & ~(CVR_SAMPLING_TEX_FEATURES | CVR_SAMPLING_TEX_VOLUME))
+  if (flags & ~(CVR_SAMPLING_TEX_FEATURES | CVR_SAMPLING_TEX_VOLUME | CVR_SAMPLING_TEX_PYRAMID))
     return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_sampling: unknown flags");
   c->sampling = flags;
   return CVR_OK;

@@ -339,6 +339,10 @@ cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, cons
  * trained with. */
 #define CVR_SAMPLING_TEX_FEATURES 1
 #define CVR_SAMPLING_TEX_VOLUME 2
+/* CVR_SAMPLING_TEX_PYRAMID: the cone method's pyramid taps through the
+ * texture unit from FP16 level textures (the reference's R16F pyramid and
+ * GL_LINEAR_MIPMAP_LINEAR filtering, with 8-bit interpolation weights). */
+#define CVR_SAMPLING_TEX_PYRAMID 4
 cvr_status cvr_set_sampling(cvr_ctx* ctx, int flags);
 int cvr_get_sampling(cvr_ctx* ctx);
 
