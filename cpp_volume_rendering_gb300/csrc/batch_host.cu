@@ -168,9 +168,11 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
       const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
       uint4* d = nullptr;
       cudaError_t e = cudaMalloc((void**)&d, cells * sizeof(uint4));
+      if (e == cudaErrorMemoryAllocation) { cudaGetLastError(); all_compact = false; break; }  // int64 tables
       if (e != cudaSuccess) { st = cuda_fail(c, e, "cvr_batch_create: compact SAT"); break; }
       b->sat32.push_back(d);
       st = build_compact_sat(c, q, d);
+      if (st == CVR_ERR_OUT_OF_MEMORY) { st = CVR_OK; all_compact = false; break; }
       tab[v] = d;
       inv[v] = (float)std::ldexp(1.0, -F);
     }

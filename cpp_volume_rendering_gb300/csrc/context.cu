@@ -311,9 +311,17 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
   if (!compact_plan(c->sat_ext, vmax, &F, &q)) return CVR_OK;
   if (c->sat32_F != F || !c->d_sat32) {
     const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-    CK(c, ensure(c->d_sat32, c->sat32_cap, cells * sizeof(uint4)));
     c->sat32_F = kNoCompactSat;
+    // the quad table is twice the int64 one: without room for it the frame
+    // keeps the int64 table
+    cudaError_t e = ensure(c->d_sat32, c->sat32_cap, cells * sizeof(uint4));
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      return CVR_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "compact SAT");
     cvr_status st = build_compact_sat(c, q, c->d_sat32);
+    if (st == CVR_ERR_OUT_OF_MEMORY) return CVR_OK;
     if (st != CVR_OK) return st;
     c->sat32_F = F;
   }
