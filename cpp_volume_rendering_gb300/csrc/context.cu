@@ -674,7 +674,8 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
       if (!(p->step_size > 0.0f)) return fail(c, CVR_ERR_INVALID_ARG, "step_size must be > 0");
       ExtArgs a{};
       const ShadowBoxTable* table = nullptr;
-      cvr_status es = ext_args(c, p, light, f, &a, &table);
+      double no_compact = 0.0;  // the light cache reads the int64 table: no compact one to build
+      cvr_status es = ext_args(c, p, light, f, &a, &table, c->lc_dims[0] > 0 ? &no_compact : nullptr);
       if (es != CVR_OK) return es;
       if (c->lc_dims[0] > 0) {  // object-space light cache, then the object-space marcher
         if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
