@@ -263,7 +263,7 @@ def time_frames(ctx, lib, wl, params, out_ptr, steps, warmup, flush=True):
 
 
 def tuned_frames(ctx, lib, w2):
-    """One prepared frame autotuned (tile x registers x brick) and timed with
+    """One prepared frame autotuned (tile x registers x volume layout) and timed with
     FP32 volume samples and with the texture-unit variant."""
     import ctypes as C
     from cpp_volume_rendering_gb300 import abi
@@ -286,7 +286,8 @@ def tuned_frames(ctx, lib, w2):
         entry.update({key + "ms": m, key + "fps": 1000.0 / m, key + "msamples_s": s2.samples / (m / 1000.0) / 1e6,
                       key + "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9,
                       key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
-                                       "brick": lib.cvr_get_brick_size(ctx.h)}})
+                                       "brick": lib.cvr_get_brick_size(ctx.h),
+                  "quads": lib.cvr_get_volume_layout(ctx.h)}})
     ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
     return entry
 
@@ -467,7 +468,8 @@ def surrogate_section(ctx, lib, args, log=print):
                                        C.sizeof(wl.params), size, size, 1, C.byref(tw), C.byref(th), C.byref(tv),
                                        None), ctx.h)
             cfg = {"sampling": flags, "tile": [tw.value, th.value], "variant": tv.value,
-                   "brick": lib.cvr_get_brick_size(ctx.h)}
+                   "brick": lib.cvr_get_brick_size(ctx.h),
+                  "quads": lib.cvr_get_volume_layout(ctx.h)}
             wl.method = method
             t = time_frames(ctx, lib, wl, wl.params, optr, 2 if method == abi.GROUND_TRUTH else 3, 1)
             if best is None or statistics.median(t) < statistics.median(best[1]):
@@ -476,6 +478,7 @@ def surrogate_section(ctx, lib, args, log=print):
         ctx.set_sampling(cfg["sampling"])
         abi.check(lib.cvr_set_tuning(ctx.h, cfg["tile"][0], cfg["tile"][1], cfg["variant"]), ctx.h)
         abi.check(lib.cvr_set_brick_size(ctx.h, cfg["brick"]), ctx.h)
+        abi.check(lib.cvr_set_volume_layout(ctx.h, cfg["quads"]), ctx.h)
         return best
     sampling_modes = (abi.SAMPLING_TEX_FEATURES, abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)
     gt_tuning, tg = tuned(abi.GROUND_TRUTH, 256, sampling_modes)
@@ -584,7 +587,8 @@ def batch_section(ctx, lib, args, log=print):
             "msamples_s": tot / (med / 1000.0) / 1e6, "samples": {"extinction": samples[abi.EXTINCTION],
                                                                   "surrogate": samples[abi.SURROGATE]},
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
-            "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h)},
+            "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
+                  "quads": lib.cvr_get_volume_layout(ctx.h)},
             "prepare_s": t_prep,
             "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
 
@@ -615,6 +619,7 @@ def run_ours(args):
                                C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
                                C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
+                  "quads": lib.cvr_get_volume_layout(ctx.h),
               "autotune_ms": tms.value}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
@@ -684,6 +689,7 @@ def run_ours(args):
             ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
             abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
             abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
+            abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)
         reset_tuning()

@@ -38,6 +38,9 @@ SURROGATE_LEVELS = 6
 SAMPLING_TEX_FEATURES = 1
 SAMPLING_TEX_VOLUME = 2
 SAMPLING_TEX_PYRAMID = 4
+# cvr_set_volume_layout
+LAYOUT_PLAIN = 0
+LAYOUT_QUADS = 1
 MLP_NOALLOC_MAX_POINTS = 8192
 MAX_VOLUMES = 16
 MAX_CONE_SECTIONS = 512
@@ -187,6 +190,8 @@ SIGNATURES = {
     "cvr_download_light_cache": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_brick_size": (_I, [_P, _I]),
     "cvr_get_brick_size": (_I, [_P]),
+    "cvr_set_volume_layout": (_I, [_P, _I]),
+    "cvr_get_volume_layout": (_I, [_P]),
     "cvr_set_compact_sat": (_I, [_P, _I]),
     "cvr_get_compact_sat": (_I, [_P]),
     "cvr_set_multiscaling": (_I, [_P, _I, _I, _I, _I]),

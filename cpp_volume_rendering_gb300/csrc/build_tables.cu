@@ -106,6 +106,31 @@ cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int n
   return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
 }
 
+// x-y quads of the volume: cell (x, y, z) = the voxels at (x, y), (x', y),
+// (x, y'), (x', y') of plane z, with the successors clamped to the volume.
+template <class T, class Q>
+__global__ void k_quad_volume(const T* __restrict__ v, Q* __restrict__ out, int nx, int ny, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = (int)(i % nx), y = (int)((i / nx) % ny);
+  const long long dx = x + 1 < nx ? 1 : 0, dy = y + 1 < ny ? nx : 0;
+  Q q;
+  q.x = v[i]; q.y = v[i + dx]; q.z = v[i + dy]; q.w = v[i + dy + dx];
+  out[i] = q;
+}
+
+cudaError_t launch_quad_volume(const void* src, void* dst, int dtype, int nx, int ny, int nz, cudaStream_t st) {
+  const long long n = (long long)nx * ny * nz;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (dtype == 1)
+    k_quad_volume<uint8_t, uchar4><<<blocks, 256, 0, st>>>(static_cast<const uint8_t*>(src), static_cast<uchar4*>(dst),
+                                                           nx, ny, n);
+  else
+    k_quad_volume<uint16_t, ushort4><<<blocks, 256, 0, st>>>(static_cast<const uint16_t*>(src),
+                                                             static_cast<ushort4*>(dst), nx, ny, n);
+  return cudaGetLastError();
+}
+
 // x-y quads of a table: out[(x, y, z)] = s at (x, y), (x', y), (x, y'),
 // (x', y') of plane z, with x' = min(x + 1, sx - 1), y' = min(y + 1, sy - 1).
 __global__ void k_sat_quads(const unsigned* __restrict__ s, uint4* __restrict__ out, int sx, int sy,

@@ -105,7 +105,16 @@ namespace ctxutil {
 
 cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
   VolumeView v = volume_view(c);
-  if (c->brick_bs > 0) {
+  if (c->quads) {
+    if (c->vbrick_bs != kQuadCopy) {
+      const size_t n = (size_t)c->nx * c->ny * c->nz;
+      CK(c, ensure(c->d_vbrick, c->vbrick_cap, n * 4 * (c->dtype == CVR_U8 ? 1 : 2)));
+      CK(c, launch_quad_volume(c->d_vol, c->d_vbrick, c->dtype, c->nx, c->ny, c->nz, c->stream));
+      c->vbrick_bs = kQuadCopy;
+    }
+    v.voxels = c->d_vbrick;
+    v.quad = 1;
+  } else if (c->brick_bs > 0) {
     if (c->vbrick_bs != c->brick_bs) {
       const long long n = brick_elements(c->nx, c->ny, c->nz, c->brick_bs);
       CK(c, ensure(c->d_vbrick, c->vbrick_cap, (size_t)n * (c->dtype == CVR_U8 ? 1 : 2)));
@@ -870,6 +879,16 @@ cvr_status cvr_set_brick_size(cvr_ctx* c, int edge) {
 
 int cvr_get_brick_size(cvr_ctx* c) { return (c && c->brick_bs > 0) ? (1 << c->brick_bs) : 0; }
 
+cvr_status cvr_set_volume_layout(cvr_ctx* c, int layout) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (layout != CVR_LAYOUT_PLAIN && layout != CVR_LAYOUT_QUADS)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_volume_layout: CVR_LAYOUT_PLAIN or CVR_LAYOUT_QUADS");
+  c->quads = layout == CVR_LAYOUT_QUADS;
+  return CVR_OK;
+}
+
+int cvr_get_volume_layout(cvr_ctx* c) { return (c && c->quads) ? CVR_LAYOUT_QUADS : CVR_LAYOUT_PLAIN; }
+
 // Mean device time of reps frames of the current tuning (one untimed frame
 // first, L2 flushed before each timed one).
 static cvr_status time_config(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light,
@@ -893,16 +912,19 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
                         size_t params_size, int w, int h, int reps, int* btw, int* bth, int* bv, float* bms) {
   if (!c || reps <= 0 || reps > 100) return fail(c, CVR_ERR_INVALID_ARG, "cvr_autotune: bad arguments");
   // ray tiles from 8x8 to 32x8 (2, 4 and 8 warps) x register variants, then
-  // the volume's brick size at the best of those (plain layout, 8^3, 16^3, 32^3)
+  // the volume's layout at the best of those (plain, bricks of 8^3, 16^3,
+  // 32^3, x-y quads; -1 stands for the quads)
   static const int tiles[6][2] = {{8, 8}, {16, 8}, {32, 4}, {8, 16}, {32, 8}, {16, 16}};
-  static const int bricks[4] = {0, 3, 4, 5};
+  static const int bricks[5] = {0, 3, 4, 5, -1};
   float* frame = nullptr;
   cvr_status s = cvr_get_frame_buffer(c, w, h, &frame);
   if (s != CVR_OK) return s;
   const int keep_w = c->tile_w, keep_h = c->tile_h, keep_v = c->variant, keep_b = c->brick_bs;
+  const bool keep_q = c->quads;
   float best = 1e30f;
   int bw = keep_w, bh = keep_h, bvar = keep_v, bb = 0;
   c->brick_bs = 0;
+  c->quads = false;
   for (int t = 0; t < 6 && s == CVR_OK; ++t) {
     for (int v = 0; v < 3 && s == CVR_OK; ++v) {
       c->tile_w = tiles[t][0]; c->tile_h = tiles[t][1]; c->variant = v;
@@ -915,8 +937,9 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
     }
   }
   c->tile_w = bw; c->tile_h = bh; c->variant = bvar;
-  for (int k = 1; k < 4 && s == CVR_OK; ++k) {
-    c->brick_bs = bricks[k];
+  for (int k = 1; k < 5 && s == CVR_OK; ++k) {
+    c->brick_bs = bricks[k] > 0 ? bricks[k] : 0;
+    c->quads = bricks[k] < 0;
     float ms = 0.0f;
     s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
     if (s == CVR_OK && ms < best) {
@@ -925,10 +948,11 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
     }
   }
   if (s != CVR_OK) {
-    c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b;
+    c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b; c->quads = keep_q;
     return s;
   }
-  c->brick_bs = bb;
+  c->brick_bs = bb > 0 ? bb : 0;
+  c->quads = bb < 0;
   if (btw) *btw = bw;
   if (bth) *bth = bh;
   if (bv) *bv = bvar;

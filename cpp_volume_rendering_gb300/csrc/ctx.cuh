@@ -91,6 +91,8 @@ inline void swap_tex(TexState& a, TexState& b) {
 
 // sat32_F of a context / slot without a valid compact SAT.
 constexpr int kNoCompactSat = -1000;
+// vbrick_bs of a copy in the x-y quad layout.
+constexpr int kQuadCopy = 100;
 
 // A resident volume that is not the current one (cvr_select_volume): the
 // volume, its SAT, pyramid and texture copies.  The current volume lives in
@@ -209,11 +211,13 @@ struct cvr_ctx {
   int sampling = CVR_SAMPLING_TEX_FEATURES;  // cvr_set_sampling flags
   VolSlot slots[CVR_MAX_VOLUMES];            // the other resident volumes
   int cur_slot = 0;
-  // bricked copy of the current volume for the marchers (cvr_set_brick_size)
+  // bricked or quad copy of the current volume for the marchers
+  // (cvr_set_brick_size, cvr_set_volume_layout)
   int brick_bs = 0;                          // tuning: 0 plain layout, else log2 of the brick edge
+  bool quads = false;                        // tuning: the x-y quad layout (takes precedence)
   void* d_vbrick = nullptr;
   size_t vbrick_cap = 0;
-  int vbrick_bs = -1;                        // layout of d_vbrick's contents (-1: stale)
+  int vbrick_bs = -1;                        // layout of d_vbrick's contents (-1: stale, kQuadCopy: quads)
   // object-space light cache (cvr_set_light_cache): 0 = off
   int lc_dims[3] = {0, 0, 0};
   float2* d_lcache = nullptr;
@@ -312,6 +316,7 @@ inline VolumeView volume_view(const cvr_ctx* c) {
   v.tex = 0;
   v.inv_grid = f3(1.0f / v.grid.x, 1.0f / v.grid.y, 1.0f / v.grid.z);
   v.bs = 0;
+  v.quad = 0;
   v.stride[0] = 1;
   v.stride[1] = c->nx;
   v.stride[2] = (long long)c->nx * c->ny;

@@ -56,6 +56,10 @@ struct VolumeView {
   // sample_volume reads it instead of the array (CVR_SAMPLING_TEX_VOLUME).
   cudaTextureObject_t tex;
   float3 inv_grid;
+  // 1: voxels hold the x-y quad layout (cell (x, y, z) = the voxels at (x, y),
+  // (x', y), (x, y'), (x', y') of plane z, x' = min(x + 1, nx - 1), y' likewise;
+  // uchar4 / ushort4): a trilinear sample is two loads (planes z0 and z1).
+  int quad;
 };
 
 // Per-frame camera frame (glm::lookAt rows s, u, f) and projection terms.
@@ -128,6 +132,31 @@ __device__ __forceinline__ Tap axis_tap(float u, int n) {
 // texel coordinate = tex_pos / spacing - 0.5.
 __device__ __forceinline__ float sample_volume(const VolumeView& v, float3 tex_pos) {
   if (v.tex) return tex3D<float>(v.tex, tex_pos.x * v.inv_grid.x, tex_pos.y * v.inv_grid.y, tex_pos.z * v.inv_grid.z);
+  if (v.quad) {
+    // Texel coordinates below 0 (the half texel at the low faces) are raised
+    // to 0 so the successor taps are the quad's; both read voxel 0 there.
+    const Tap tx = axis_tap(fmaxf(fmaf(tex_pos.x, v.inv_spacing.x, -0.5f), 0.0f), v.nx);
+    const Tap ty = axis_tap(fmaxf(fmaf(tex_pos.y, v.inv_spacing.y, -0.5f), 0.0f), v.ny);
+    const Tap tz = axis_tap(fmaf(tex_pos.z, v.inv_spacing.z, -0.5f), v.nz);
+    const size_t cell = (size_t)tx.i0 + (size_t)v.nx * (size_t)ty.i0;
+    const size_t plane = (size_t)v.nx * (size_t)v.ny;
+    float c000, c100, c010, c110, c001, c101, c011, c111;
+    if (v.dtype == 1) {
+      const uchar4* q = static_cast<const uchar4*>(v.voxels) + cell;
+      const uchar4 a = __ldg(q + plane * (size_t)tz.i0), b = __ldg(q + plane * (size_t)tz.i1);
+      c000 = a.x; c100 = a.y; c010 = a.z; c110 = a.w;
+      c001 = b.x; c101 = b.y; c011 = b.z; c111 = b.w;
+    } else {
+      const ushort4* q = static_cast<const ushort4*>(v.voxels) + cell;
+      const ushort4 a = __ldg(q + plane * (size_t)tz.i0), b = __ldg(q + plane * (size_t)tz.i1);
+      c000 = a.x; c100 = a.y; c010 = a.z; c110 = a.w;
+      c001 = b.x; c101 = b.y; c011 = b.z; c111 = b.w;
+    }
+    const float c00 = fmaf(tx.t, c100 - c000, c000), c10 = fmaf(tx.t, c110 - c010, c010);
+    const float c01 = fmaf(tx.t, c101 - c001, c001), c11 = fmaf(tx.t, c111 - c011, c011);
+    const float c0 = fmaf(ty.t, c10 - c00, c00), c1 = fmaf(ty.t, c11 - c01, c01);
+    return fmaf(tz.t, c1 - c0, c0) * v.norm;
+  }
   Tap tx = axis_tap(fmaf(tex_pos.x, v.inv_spacing.x, -0.5f), v.nx);
   Tap ty = axis_tap(fmaf(tex_pos.y, v.inv_spacing.y, -0.5f), v.ny);
   Tap tz = axis_tap(fmaf(tex_pos.z, v.inv_spacing.z, -0.5f), v.nz);

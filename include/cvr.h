@@ -292,6 +292,15 @@ cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
  * or the size changed.  Results do not depend on it. */
 cvr_status cvr_set_brick_size(cvr_ctx* ctx, int edge);
 int cvr_get_brick_size(cvr_ctx* ctx);
+/* Volume layout of the marchers' FP32 samples (no reference counterpart):
+ * CVR_LAYOUT_QUADS keeps a copy where each voxel cell holds the 2 x 2 voxels
+ * of its x-y neighbourhood (4 x the volume's bytes), so a trilinear sample is
+ * two loads instead of eight; results are bit-identical to the plain layout.
+ * It takes precedence over bricks; the autotuner tries it with them. */
+#define CVR_LAYOUT_PLAIN 0
+#define CVR_LAYOUT_QUADS 1
+cvr_status cvr_set_volume_layout(cvr_ctx* ctx, int layout);
+int cvr_get_volume_layout(cvr_ctx* ctx);
 /* Compact SAT (no reference counterpart; default on): frames of
  * CVR_METHOD_EXTINCTION whose box queries all span a bounded region (the
  * ambient-occlusion boxes and, for directional shadows, the per-frame cone
@@ -318,9 +327,9 @@ cvr_status cvr_set_light_cache(cvr_ctx* ctx, int w, int h, int d);
 cvr_status cvr_download_light_cache(cvr_ctx* ctx, float* host_out, size_t n_floats);
 /* Autotuner: renders the given frame with every tile shape x register variant
  * (reps timed frames each, CUDA events, L2 flushed before each), then every
- * brick size at the best of those; keeps the fastest configuration on the
- * context and reports it (cvr_get_brick_size reports the brick).  best_ms may
- * be NULL. */
+ * brick size and the quad layout at the best of those; keeps the fastest
+ * configuration on the context and reports it (cvr_get_brick_size and
+ * cvr_get_volume_layout report the layout).  best_ms may be NULL. */
 cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
                         const void* params, size_t params_size, int w, int h, int reps,
                         int* best_tile_w, int* best_tile_h, int* best_variant, float* best_ms);

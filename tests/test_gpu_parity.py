@@ -91,6 +91,32 @@ def test_extinction_anisotropic_spacing_and_aspect(ctx):
     compare(img, ref, "extinction anisotropic")
 
 
+@pytest.mark.parametrize("dtype", [abi.CVR_U8, abi.CVR_U16])
+def test_quad_layout_is_bit_identical_on_ragged_volumes(ctx, dtype):
+    """The x-y quad copy (successors clamped at the high faces, texel
+    coordinates raised to 0 at the low faces) renders the plain layout's bits
+    on odd, non-cubic volumes with anisotropic spacing, rays entering through
+    every face."""
+    vol = scene.synth_value_noise(37, 23, 29, dtype, seed=12)
+    for name in ("plain", "ground_truth", "iso"):
+        wl = scene.workload(name, n=8, image=8)
+        wl.volume = vol
+        wl.spacing = (1.0, 1.5, 0.75)
+        wl.width, wl.height = 64, 48
+        scene.prepare(ctx, wl)
+        for eye in ((120.0, 60.0, 35.0), (120.0, -150.0, -40.0)):
+            wl.cam = scene.camera(scene.orbit_eye(*eye), fovy=40.0)
+            abi.check(ctx.lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+            a, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+            abi.check(ctx.lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_QUADS), ctx.h)
+            try:
+                b, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+            finally:
+                abi.check(ctx.lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+            assert np.array_equal(a, b), (name, eye)
+            assert np.abs(a).max() > 0
+
+
 def test_sat_bit_exact_and_relative_error(ctx):
     vol = scene.synth_value_noise(48, 40, 36, abi.CVR_U16, seed=4)
     ext = scene.BENCH_TF.ext_per_value(abi.CVR_U16)
@@ -245,7 +271,7 @@ TILES = [(8, 8), (16, 8), (32, 4), (8, 16), (32, 8), (16, 16)]
 
 
 @pytest.mark.parametrize("name,n,image", [("extinction", 48, 72), ("plain", 40, 56), ("cone", 40, 48),
-                                          ("ground_truth", 24, 40)])
+                                          ("ground_truth", 24, 40), ("iso", 40, 48)])
 def test_tuning_does_not_change_results(ctx, name, n, image):
     """Every tile shape / register variant / brick size renders the same bits."""
     import ctypes as C
@@ -265,11 +291,20 @@ def test_tuning_does_not_change_results(ctx, name, n, image):
         img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
         images.append(img)
     abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
+    abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_QUADS), ctx.h)
+    assert lib.cvr_get_volume_layout(ctx.h) == abi.LAYOUT_QUADS
+    for tw, th in ((16, 8), (32, 8)):
+        abi.check(lib.cvr_set_tuning(ctx.h, tw, th, 0), ctx.h)
+        img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+        images.append(img)
+    abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+    abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
     for im in images[1:]:
         assert np.array_equal(im, images[0])
     assert lib.cvr_set_tuning(ctx.h, 24, 8, 0) == abi.CVR_ERR_INVALID_ARG  # 6 warps
     assert lib.cvr_set_tuning(ctx.h, 12, 8, 0) == abi.CVR_ERR_INVALID_ARG  # not whole warps
     assert lib.cvr_set_brick_size(ctx.h, 12) == abi.CVR_ERR_INVALID_ARG
+    assert lib.cvr_set_volume_layout(ctx.h, 2) == abi.CVR_ERR_INVALID_ARG
 
 
 def test_autotune_picks_a_valid_configuration(ctx):
@@ -284,9 +319,11 @@ def test_autotune_picks_a_valid_configuration(ctx):
                                C.byref(ms)), ctx.h)
     assert (tw.value, th.value) in TILES and v.value in (0, 1, 2) and ms.value > 0
     assert lib.cvr_get_brick_size(ctx.h) in (0, 8, 16, 32)
+    assert lib.cvr_get_volume_layout(ctx.h) in (abi.LAYOUT_PLAIN, abi.LAYOUT_QUADS)
     img, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
     abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
     abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
+    abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
     ref, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
     assert np.array_equal(img, ref)
 
