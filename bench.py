@@ -56,6 +56,7 @@ WORKLOAD_DESC = {
 }
 
 MLP_FLOP_PER_SAMPLE = 2 * (48 * 64 + 64 * 64 + 64 * 2)  # 14,592
+GRADIENT_BUILDERS = {1: "k_gradient_tiled", 2: "k_gradient", 3: "k_gradient_tma"}
 
 
 def dist_env():
@@ -316,22 +317,28 @@ def gradient_section(ctx, lib, args, log=print):
         for mname, model in (("finite_differences", abi.GRADIENT_FINITE_DIFFERENCES),
                              ("sobel_feldman", abi.GRADIENT_SOBEL_FELDMAN)):
             gp = abi.GradientParams(model, 1, 0, 1)
-            for _ in range(2):
-                abi.check(lib.cvr_build_gradient(ctx.h, C.byref(gp)), ctx.h)
-            times = []
-            for _ in range(5):
-                abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
-                abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
-                abi.check(lib.cvr_build_gradient(ctx.h, C.byref(gp)), ctx.h)
-                abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
-                times.append(ms.value)
-            m = statistics.median(times)
-            algo = nvox * (vol.itemsize + 8)
-            out["build"][f"{vname} {mname}"] = {
-                "ms": m, "gvoxels_s": nvox / (m / 1000.0) / 1e9,
-                "roofline": {"bound": "hbm", "achieved": algo / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
-                             "frac": algo / (m / 1000.0) / 1e9 / peak, "peak_source": peak_src,
-                             "algorithmic_bytes": algo}}
+            # the default builder (tensor-memory-accelerator plane streaming
+            # where the row pitch allows) and the shared-memory ring builder
+            for suffix, kern in (("", abi.GRADIENT_KERNEL_AUTO), (" tiled", abi.GRADIENT_KERNEL_TILED)):
+                abi.check(lib.cvr_set_gradient_kernel(ctx.h, kern), ctx.h)
+                for _ in range(2):
+                    abi.check(lib.cvr_build_gradient(ctx.h, C.byref(gp)), ctx.h)
+                times = []
+                for _ in range(5):
+                    abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+                    abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+                    abi.check(lib.cvr_build_gradient(ctx.h, C.byref(gp)), ctx.h)
+                    abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+                    times.append(ms.value)
+                m = statistics.median(times)
+                algo = nvox * (vol.itemsize + 8)
+                out["build"][f"{vname} {mname}{suffix}"] = {
+                    "ms": m, "gvoxels_s": nvox / (m / 1000.0) / 1e9,
+                    "builder": GRADIENT_BUILDERS.get(lib.cvr_get_gradient_kernel(ctx.h), "?"),
+                    "roofline": {"bound": "hbm", "achieved": algo / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                                 "frac": algo / (m / 1000.0) / 1e9 / peak, "peak_source": peak_src,
+                                 "algorithmic_bytes": algo}}
+            abi.check(lib.cvr_set_gradient_kernel(ctx.h, abi.GRADIENT_KERNEL_AUTO), ctx.h)
     # CPU: the FP64 restatement of GenerateGradientTexture (the reference's own
     # loop, single-threaded like it) on a 128^3 sample of the u8 volume
     sample = np.ascontiguousarray(vols["512^3 u8 blobs"][192:320, 192:320, 192:320])

@@ -38,6 +38,11 @@ SURROGATE_LEVELS = 6
 SAMPLING_TEX_FEATURES = 1
 SAMPLING_TEX_VOLUME = 2
 SAMPLING_TEX_PYRAMID = 4
+# cvr_set_gradient_kernel / cvr_get_gradient_kernel
+GRADIENT_KERNEL_AUTO = 0
+GRADIENT_KERNEL_TILED = 1
+GRADIENT_KERNEL_GENERIC = 2
+GRADIENT_KERNEL_TMA = 3
 # cvr_set_volume_layout
 LAYOUT_PLAIN = 0
 LAYOUT_QUADS = 1
@@ -190,6 +195,8 @@ SIGNATURES = {
     "cvr_download_light_cache": (_I, [_P, _FP, C.c_size_t]),
     "cvr_set_brick_size": (_I, [_P, _I]),
     "cvr_get_brick_size": (_I, [_P]),
+    "cvr_set_gradient_kernel": (_I, [_P, _I]),
+    "cvr_get_gradient_kernel": (_I, [_P]),
     "cvr_set_volume_layout": (_I, [_P, _I]),
     "cvr_get_volume_layout": (_I, [_P]),
     "cvr_set_compact_sat": (_I, [_P, _I]),

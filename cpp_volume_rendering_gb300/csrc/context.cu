@@ -338,6 +338,15 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
   return CVR_OK;
 }
 
+cvr_status check_kernel_flag(cvr_ctx* c, const char* what) {
+  int e = 0;
+  CK(c, cudaMemcpyAsync(&e, c->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  CK(c, cudaStreamSynchronize(c->stream));
+  if (e == 0) return CVR_OK;
+  CK(c, cudaMemsetAsync(c->d_kerr, 0, sizeof(int), c->stream));
+  return fail(c, CVR_ERR_TIMEOUT, what);
+}
+
 }  // namespace ctxutil
 }  // namespace cvr
 
@@ -375,6 +384,8 @@ cvr_status cvr_create(cvr_ctx** out, int device) {
     if ((e = cudaEventCreate(&c->ev[i])) != cudaSuccess) return bail(e, "cudaEventCreate");
   if ((e = cudaMalloc((void**)&c->d_stats, 4 * sizeof(unsigned long long))) != cudaSuccess)
     return bail(e, "cudaMalloc(stats)");
+  if ((e = cudaMalloc((void**)&c->d_kerr, sizeof(int))) != cudaSuccess) return bail(e, "cudaMalloc(kernel flag)");
+  if ((e = cudaMemset(c->d_kerr, 0, sizeof(int))) != cudaSuccess) return bail(e, "cudaMemset(kernel flag)");
   *out = c;
   return CVR_OK;
 }
@@ -385,7 +396,7 @@ void cvr_destroy(cvr_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
                   c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms,
-                  c->d_sat32, c->d_lut32};
+                  c->d_sat32, c->d_lut32, c->d_kerr};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)

@@ -228,6 +228,9 @@ struct cvr_ctx {
   size_t grad_cap = 0;
   bool grad_ready = false;
   cvr_gradient_params grad_params{CVR_GRADIENT_NONE, 1, 0, 1};
+  int grad_kernel = CVR_GRADIENT_KERNEL_AUTO;  // cvr_set_gradient_kernel
+  int grad_last = -1;                          // the builder the last build ran
+  int* d_kerr = nullptr;                       // set by a table builder whose bounded wait gave up
   cvr_blinn_phong bp{0, 0.5f, 0.5f, 0.8f, 30.0f, {1.0f, 1.0f, 1.0f}};
   // pixel multiscaling (cvr_set_multiscaling) and its generated-frame buffer
   int ms_mode = CVR_MULTISCALE_SINGLE, ms_kernel = CVR_FILTER_HAT, ms_fw = 2, ms_fh = 2;
@@ -279,6 +282,9 @@ inline cvr_status fail(cvr_ctx* c, cvr_status code, const std::string& msg) {
   if (c) c->err = msg;
   return code;
 }
+
+// Reads (synchronously) and clears the context's kernel error flag.
+cvr_status check_kernel_flag(cvr_ctx* c, const char* what);
 
 inline cvr_status cuda_fail(cvr_ctx* c, cudaError_t e, const char* what) {
   cudaGetLastError();  // clear a sticky launch error where possible

@@ -7,11 +7,17 @@
 // (utils.cpp:146-351) and uploads it as RGB16F; here the same stencils are
 // formed from the integer voxel values (exact), scaled once in FP32 and
 // stored as four FP16 values (x, y, z, 0: one 8-byte load per tap).
+#include <cuda.h>  // CUtensorMap (encoded through the runtime's driver entry point)
+#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
 #include "ctx.cuh"
+#include "tc.cuh"  // mbarrier helpers
 
 using namespace cvr::ctxutil;
+using cvr::tc::mbar_init;
+using cvr::tc::mbar_wait;
+using cvr::tc::smem_u32;
 
 namespace {
 
@@ -195,6 +201,183 @@ __global__ void __launch_bounds__(kGradTX * kGradTY) k_gradient_tiled(const T* _
   }
 }
 
+// The 3x3x3 stencils with the planes brought in by the tensor memory
+// accelerator: a CTA owns a 32 x 16 column of voxels over kTmaZ planes; one
+// thread keeps kTmaBuf plane tiles (the column plus a one-voxel halo, read
+// from an x origin rounded down to 16 bytes; the copy engine writes 0 outside
+// the grid, which is GetNormalizedSample's 0) in flight, each completing on
+// its own mbarrier.  Every thread computes two voxels (rows y, y + 1) and
+// keeps, per voxel, three separable in-plane partial sums of the last three
+// planes in registers, so a plane costs it 12 shared-memory reads for both
+// voxels.  Sobel-Feldman's weights 4 / 2^(|v1|+|v2|) are (2 >> |v1|)(2 >> |v2|):
+//   sx = sum_z w_z D[z],  D = sum_y w_y (P(x-1) - P(x+1))
+//   sy = sum_z w_z E[z],  E = Sx(y-1) - Sx(y+1),   Sx = P(x-1) + 2 P(x) + P(x+1)
+//   sz = Q[z-1] - Q[z+1], Q = sum_y w_y Sx
+// -- the same integers as the direct 27-tap sums.  Needs the row pitch
+// (nx x voxel bytes) to be a multiple of 16 bytes.
+constexpr int kTmaTX = 32, kTmaTY = 16, kTmaZ = 32, kTmaBuf = 4;
+constexpr int kTmaRows = kTmaTY + 2;
+constexpr int kTmaPitch = 96;                        // bytes of a tile row: 64 u8 or 48 u16 voxels
+constexpr int kTmaBufStride = 1792;                  // 128-byte aligned slots
+static_assert(kTmaPitch * kTmaRows <= kTmaBufStride && kTmaBufStride % 128 == 0, "plane slot");
+constexpr int kGradErrTma = 1;                       // d_kerr: a plane copy did not complete
+constexpr uint32_t kTmaPolls = 1u << 22;             // bound of every plane wait
+
+template <class T>
+struct TmaGeom {
+  static constexpr int OX = 16 / (int)sizeof(T);                 // x origin offset (16 bytes)
+  static constexpr int BW = (sizeof(T) == 1) ? 64 : 48;          // box width in voxels (>= OX + 32 + 1)
+  static constexpr unsigned kBytes = (unsigned)(BW * kTmaRows * sizeof(T));
+  static_assert(BW * sizeof(T) <= kTmaPitch && (BW * sizeof(T)) % 16 == 0 && BW >= OX + kTmaTX + 1, "tile box");
+};
+
+template <class T, bool SOBEL>
+__global__ void __launch_bounds__(256) k_gradient_tma(const __grid_constant__ CUtensorMap vol, int nx, int ny, int nz,
+                                                      GradBuild b, uint2* __restrict__ out, int* __restrict__ err) {
+  using G = TmaGeom<T>;
+  __shared__ __align__(128) uint8_t tiles[kTmaBuf][kTmaBufStride];
+  __shared__ __align__(8) uint64_t bars[kTmaBuf];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTmaTX + tx;
+  const int x0 = blockIdx.x * kTmaTX, y0 = blockIdx.y * kTmaTY, z0 = blockIdx.z * kTmaZ;
+  const int z1 = min(z0 + kTmaZ, nz);
+  const int n_planes = z1 - z0 + 2;  // planes z0 - 1 .. z1
+  if (tid == 0) {
+#pragma unroll
+    for (int i = 0; i < kTmaBuf; ++i) mbar_init(&bars[i], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int i) {  // plane z0 - 1 + i into slot i % kTmaBuf
+    const uint32_t bar = smem_u32(&bars[i % kTmaBuf]);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(G::kBytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(tiles[i % kTmaBuf])),
+        "l"(reinterpret_cast<uint64_t>(&vol)), "r"(x0 - G::OX), "r"(y0 - 1), "r"(z0 - 1 + i), "r"(bar)
+        : "memory");
+  };
+  if (tid == 0)
+    for (int i = 0; i < kTmaBuf && i < n_planes; ++i) issue(i);
+
+  const int x = x0 + tx, ya = y0 + 2 * ty;
+  const bool on_a = x < nx && ya < ny, on_b = x < nx && ya + 1 < ny;
+  const int c = tx + G::OX;  // tile column of x
+  // per voxel (a, b) and plane: the three partial sums (Sobel: D, E, Q;
+  // finite differences: P(x+1) - P(x-1), P(y+1) - P(y-1), P) of the planes
+  // z - 1 (p0), z (p1), z + 1 (p2)
+  int p0[2][3] = {}, p1[2][3] = {}, p2[2][3] = {};
+  const size_t plane = (size_t)nx * ny;
+  uint2* o = out + (size_t)x + (size_t)nx * ya + plane * (size_t)z0;
+  for (int i = 0; i < n_planes; ++i) {
+    const bool ok = mbar_wait(&bars[i % kTmaBuf], (uint32_t)((i / kTmaBuf) & 1), kTmaPolls);
+    const T* t = reinterpret_cast<const T*>(tiles[i % kTmaBuf]) + (size_t)(2 * ty) * G::BW + c;
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { p0[j][k] = p1[j][k]; p1[j][k] = p2[j][k]; }
+    if (SOBEL) {
+      int sx[4], df[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {  // tile rows of y - 1 .. y + 2
+        const int l = t[r * G::BW - 1], m = t[r * G::BW], h = t[r * G::BW + 1];
+        sx[r] = l + 2 * m + h;
+        df[r] = l - h;
+      }
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        p2[j][0] = df[j] + 2 * df[j + 1] + df[j + 2];
+        p2[j][1] = sx[j] - sx[j + 2];
+        p2[j][2] = sx[j] + 2 * sx[j + 1] + sx[j + 2];
+      }
+    } else {
+      int ctr[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) ctr[r] = t[r * G::BW];
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        p2[j][0] = (int)t[(j + 1) * G::BW + 1] - (int)t[(j + 1) * G::BW - 1];
+        p2[j][1] = ctr[j + 2] - ctr[j];
+        p2[j][2] = ctr[j + 1];
+      }
+    }
+    // one barrier per plane: every thread has read slot i and seen its copy
+    // complete (or the CTA gives up together)
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        atomicExch(err, kGradErrTma);
+        // wait (bounded) for the copies still in flight before leaving
+        for (int k = i; k < n_planes && k < i + kTmaBuf; ++k)
+          mbar_wait(&bars[k % kTmaBuf], (uint32_t)((k / kTmaBuf) & 1), kTmaPolls);
+      }
+      return;
+    }
+    if (tid == 0 && i + kTmaBuf < n_planes) issue(i + kTmaBuf);
+    if (i >= 2) {  // p0, p1, p2 hold the planes z - 1, z, z + 1 of z = z0 + i - 2
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        if (!(j ? on_b : on_a)) continue;
+        float gx, gy, gz;
+        if (SOBEL) {
+          gx = float(p0[j][0] + 2 * p1[j][0] + p2[j][0]) * b.inv_max;
+          gy = float(p0[j][1] + 2 * p1[j][1] + p2[j][1]) * b.inv_max;
+          gz = float(p0[j][2] - p2[j][2]) * b.inv_max;
+        } else {
+          fd_finish(b, float(p1[j][0]), float(p1[j][1]), float(p2[j][2] - p0[j][2]), gx, gy, gz);
+        }
+        store_grad(o, j ? (size_t)nx : 0, gx, gy, gz);
+      }
+      o += plane;
+    }
+  }
+}
+
+using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
+
+EncodeTiled encode_tiled() {
+  static EncodeTiled fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiled>(p);
+  }();
+  return fn;
+}
+
+// The volume's tensor map for k_gradient_tma: false when the layout does not
+// allow one (row pitch not a multiple of 16 bytes, or no encoder).
+template <class T>
+bool volume_tensor_map(const void* vol, int nx, int ny, int nz, CUtensorMap* m) {
+  using G = TmaGeom<T>;
+  const cuuint64_t pitch = (cuuint64_t)nx * sizeof(T);
+  if (pitch % 16 != 0 || (reinterpret_cast<uintptr_t>(vol) & 15) != 0) return false;
+  EncodeTiled enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {pitch, pitch * (cuuint64_t)ny};
+  const cuuint32_t box[3] = {(cuuint32_t)G::BW, (cuuint32_t)kTmaRows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  return enc(m, sizeof(T) == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 3,
+             const_cast<void*>(vol), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <class T>
+bool launch_gradient_tma(const void* vol, int nx, int ny, int nz, const GradBuild& b, uint2* out, int* err,
+                         cudaStream_t st) {
+  CUtensorMap m;
+  if (!volume_tensor_map<T>(vol, nx, ny, nz, &m)) return false;
+  const dim3 block(kTmaTX, kTmaTY / 2, 1);
+  const dim3 grid((nx + kTmaTX - 1) / kTmaTX, (ny + kTmaTY - 1) / kTmaTY, (nz + kTmaZ - 1) / kTmaZ);
+  if (b.model == CVR_GRADIENT_FINITE_DIFFERENCES)
+    k_gradient_tma<T, false><<<grid, block, 0, st>>>(m, nx, ny, nz, b, out, err);
+  else
+    k_gradient_tma<T, true><<<grid, block, 0, st>>>(m, nx, ny, nz, b, out, err);
+  return true;
+}
+
 __global__ void k_gradient_to_float(const uint2* __restrict__ g, float* __restrict__ out, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -220,7 +403,17 @@ cvr_status build_gradient(cvr_ctx* c) {
   CK(c, ensure(c->d_grad, c->grad_cap, n * sizeof(uint2)));
   GradBuild b{p.model, p.sample_size, p.filter_nxnxn, p.normalized, c->dtype == CVR_U8 ? 1.0f / 255.0f : 1.0f / 65535.0f};
   const bool u8 = c->dtype == CVR_U8;
-  if (p.model != CVR_GRADIENT_FINITE_DIFFERENCES || p.sample_size == 1) {
+  const bool stencil = p.model != CVR_GRADIENT_FINITE_DIFFERENCES || p.sample_size == 1;
+  const int kern = stencil ? c->grad_kernel : CVR_GRADIENT_KERNEL_GENERIC;
+  bool done = false;
+  if (kern == CVR_GRADIENT_KERNEL_AUTO) {
+    done = u8 ? launch_gradient_tma<uint8_t>(c->d_vol, c->nx, c->ny, c->nz, b, c->d_grad, c->d_kerr, c->stream)
+              : launch_gradient_tma<uint16_t>(c->d_vol, c->nx, c->ny, c->nz, b, c->d_grad, c->d_kerr, c->stream);
+  }
+  c->grad_last = done ? CVR_GRADIENT_KERNEL_TMA : kern == CVR_GRADIENT_KERNEL_GENERIC ? kern : CVR_GRADIENT_KERNEL_TILED;
+  if (done) {
+    // nothing else to launch
+  } else if (kern != CVR_GRADIENT_KERNEL_GENERIC) {
     const dim3 block(kGradTX, kGradTY, 1);
     const dim3 grid((c->nx + kGradTX - 1) / kGradTX, (c->ny + kGradTY - 1) / kGradTY, (c->nz + kGradZ - 1) / kGradZ);
     if (u8)
@@ -240,6 +433,16 @@ cvr_status build_gradient(cvr_ctx* c) {
                                                           c->nz, b, c->d_grad);
   }
   CK(c, cudaGetLastError());
+  if (done) {
+    // a copy that never completed leaves the flag set: checked here unless
+    // the stream is being captured (then by cvr_download_gradient)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CK(c, cudaStreamIsCapturing(c->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+      cvr_status s = check_kernel_flag(c, "gradient build: a plane copy did not complete");
+      if (s != CVR_OK) return s;
+    }
+  }
   c->grad_ready = true;
   c->tex.grad_valid = false;
   return CVR_OK;
@@ -299,12 +502,24 @@ cvr_status cvr_build_gradient(cvr_ctx* c, const cvr_gradient_params* p) {
   return build_gradient(c);
 }
 
+cvr_status cvr_set_gradient_kernel(cvr_ctx* c, int kernel) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (kernel < CVR_GRADIENT_KERNEL_AUTO || kernel > CVR_GRADIENT_KERNEL_GENERIC)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_gradient_kernel: AUTO, TILED or GENERIC");
+  c->grad_kernel = kernel;
+  return CVR_OK;
+}
+
+int cvr_get_gradient_kernel(cvr_ctx* c) { return c ? c->grad_last : -1; }
+
 cvr_status cvr_download_gradient(cvr_ctx* c, float* host, size_t n_floats) {
   if (!c || !host) return CVR_ERR_INVALID_ARG;
   if (!c->grad_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_download_gradient: no gradient built");
   const long long n = (long long)c->nx * c->ny * c->nz;
   if (n_floats < 3 * (size_t)n) return fail(c, CVR_ERR_INVALID_ARG, "cvr_download_gradient: buffer too small");
   CK(c, cudaSetDevice(c->device));
+  cvr_status ks = check_kernel_flag(c, "gradient build: a plane copy did not complete");
+  if (ks != CVR_OK) return ks;
   float* tmp = nullptr;
   CK(c, cudaMalloc((void**)&tmp, sizeof(float) * 3 * (size_t)n));
   k_gradient_to_float<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(c->d_grad, tmp, n);

@@ -408,6 +408,21 @@ typedef struct cvr_gradient_params {
 cvr_status cvr_build_gradient(cvr_ctx* ctx, const cvr_gradient_params* params);
 /* The gradient as 3 floats per voxel (x fastest); synchronous. */
 cvr_status cvr_download_gradient(cvr_ctx* ctx, float* host_xyz, size_t n_floats);
+/* Device builder of the 3x3x3 stencils (Sobel-Feldman, compute Sobel and
+ * finite differences of sample size 1; no reference counterpart, all give the
+ * same values): AUTO streams the volume's planes through the tensor memory
+ * accelerator when the row pitch (width x voxel bytes) is a multiple of 16
+ * bytes and falls back to TILED (plain loads into a shared-memory ring)
+ * otherwise; GENERIC is one thread per voxel straight from global memory
+ * (always used for finite differences of sample size > 1).
+ * cvr_get_gradient_kernel reports the builder the last build ran
+ * (CVR_GRADIENT_KERNEL_TMA, _TILED or _GENERIC; -1 before any build). */
+#define CVR_GRADIENT_KERNEL_AUTO 0
+#define CVR_GRADIENT_KERNEL_TILED 1
+#define CVR_GRADIENT_KERNEL_GENERIC 2
+#define CVR_GRADIENT_KERNEL_TMA 3
+cvr_status cvr_set_gradient_kernel(cvr_ctx* ctx, int kernel);
+int cvr_get_gradient_kernel(cvr_ctx* ctx);
 /* RenderingParameters' Blinn-Phong terms (renderingparameters.cpp:23-26,
  * lightsourcelist.cpp:24) and the renderers' "Apply Gradient Shading" switch
  * (m_apply_gradient_shading, default off).  When apply is set and the volume

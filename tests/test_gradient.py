@@ -121,6 +121,40 @@ def test_gpu_gradient_larger_volumes(ctx):
             _gpu_vs_oracle_gradient(ctx, vol, model, n, filt, norm)
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,dtype,tma", [((48, 37, 29), abi.CVR_U8, True), ((40, 23, 35), abi.CVR_U16, True),
+                                             ((64, 64, 70), abi.CVR_U8, True), ((16, 9, 5), abi.CVR_U8, True),
+                                             ((37, 20, 18), abi.CVR_U8, False), ((36, 17, 9), abi.CVR_U16, False)])
+def test_gradient_builders_agree_bit_for_bit(ctx, dims, dtype, tma):
+    """The tensor-memory-accelerator builder (rows a multiple of 16 bytes;
+    ragged tiles in x, y and z, out-of-grid halo filled by the copy engine),
+    the shared-memory ring builder and the per-voxel builder give the same
+    FP16 gradients for every 3x3x3 stencil."""
+    w, h, d = dims
+    rng = np.random.default_rng(w * 10000 + h * 100 + d)
+    top = 256 if dtype == abi.CVR_U8 else 65536
+    vol = rng.integers(0, top, size=(d, h, w)).astype(np.uint8 if dtype == abi.CVR_U8 else np.uint16)
+    vol[: d // 2, : h // 2, : w // 2] = top // 3  # a flat block: zero gradients
+    ctx.set_volume(vol, (1.0, 1.0, 1.0))
+    want_first = abi.GRADIENT_KERNEL_TMA if tma else abi.GRADIENT_KERNEL_TILED
+    try:
+        for model, n, filt, norm in [(0, 1, 0, True), (1, 1, 0, True), (1, 1, 0, False), (1, 1, 3, True),
+                                     (2, 1, 0, True)]:
+            outs, kinds = [], []
+            for kern in (abi.GRADIENT_KERNEL_AUTO, abi.GRADIENT_KERNEL_TILED, abi.GRADIENT_KERNEL_GENERIC):
+                ctx._ck(ctx.lib.cvr_set_gradient_kernel(ctx.h, kern))
+                ctx.build_gradient(model, n, filt, norm)
+                outs.append(ctx.gradient())
+                kinds.append(ctx.lib.cvr_get_gradient_kernel(ctx.h))
+            assert kinds == [want_first, abi.GRADIENT_KERNEL_TILED, abi.GRADIENT_KERNEL_GENERIC], kinds
+            assert np.array_equal(outs[0], outs[1]), (model, n, filt, norm)
+            assert np.array_equal(outs[0], outs[2]), (model, n, filt, norm)
+            assert np.abs(outs[0]).max() > 0
+    finally:
+        ctx._ck(ctx.lib.cvr_set_gradient_kernel(ctx.h, abi.GRADIENT_KERNEL_AUTO))
+    assert ctx.lib.cvr_set_gradient_kernel(ctx.h, abi.GRADIENT_KERNEL_TMA) == abi.CVR_ERR_INVALID_ARG
+
+
 def _shaded_pair(ctx, wl, model, bp, cache=None, sampling=0):
     scene.prepare(ctx, wl)
     ctx.build_gradient(model)
