@@ -368,6 +368,94 @@ def gradient_section(ctx, lib, args, log=print):
     return out
 
 
+def postpass_section(ctx, lib, args, log=print):
+    """Pixel multiscaling (BaseVolumeRenderer's MULTISCALING modes and
+    RenderFrameToScreen's image kernels) as device post-passes.  Each pass
+    alone on a 1024^2 output: multisample and down-scale from a rendered
+    2048^2 frame, up-scale from a rendered 512^2 frame (the cardinal B-spline
+    and o-MOMS up-scales include their digital prefilter of the source); HBM
+    roofline on 16 bytes read per source pixel + 16 written per output pixel.
+    Against the FP64 restatement of the passes on a 64^2 output.  Then whole
+    multiscaled plain frames (256^3 u8 -> 1024^2) against the single-scale frame."""
+    import ctypes as C
+
+    import numpy as np
+
+    from cpp_volume_rendering_gb300 import abi, scene
+    from oracle import postpass as pp
+    peak, peak_src = measured_peak_hbm()
+    W = 1024
+    fb_w = 32768
+    buf = C.POINTER(C.c_float)()
+    abi.check(lib.cvr_get_frame_buffer(ctx.h, fb_w, (2048 * 2048 + W * W + fb_w - 1) // fb_w, C.byref(buf)), ctx.h)
+    base = C.cast(buf, C.c_void_p).value
+    src, dst = C.c_void_p(base), C.c_void_p(base + 2048 * 2048 * 16)
+    wl = scene.workload("plain_large")
+    scene.prepare(ctx, wl)
+    ms = C.c_float()
+
+    def render_into(ptr, w, h):
+        abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(wl.params),
+                                 C.sizeof(wl.params), ptr, w, h, None, None), ctx.h)
+
+    def timed(fn, reps=10):
+        for _ in range(2):
+            fn()
+        ts = []
+        for _ in range(reps):
+            abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+            abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+            fn()
+            abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+            ts.append(ms.value)
+        return statistics.median(ts)
+
+    names = ["box", "hat", "catmull_rom", "mitchell_netravali", "cardinal_bspline3", "cardinal_omoms3"]
+    cases = [("multisample", abi.MULTISCALE_MULTISAMPLE, abi.FILTER_HAT, 2048)]
+    cases += [("downscale", abi.MULTISCALE_DOWNSCALE, k, 2048) for k in range(6)]
+    cases += [("upscale", abi.MULTISCALE_UPSCALE, k, 512) for k in range(6)]
+    out = {"passes": {}, "frames": {}}
+    rng = np.random.default_rng(5)
+    rendered = None
+    for mode_name, mode, k, sw in cases:
+        if rendered != sw:
+            render_into(src, sw, sw)
+            rendered = sw
+        m = timed(lambda: abi.check(lib.cvr_rescale_frame(ctx.h, mode, k, src, sw, sw, dst, W, W), ctx.h))
+        algo = (sw * sw + W * W) * 16
+        # the FP64 restatement on a 64^2 output (its sources scaled alike)
+        ssw = 128 if sw > W else 32
+        small = rng.uniform(0.0, 1.0, size=(ssw, ssw, 4))
+        t0 = time.perf_counter()
+        pp.rescale(small, mode, k, 64, 64)
+        cpu_s = time.perf_counter() - t0
+        out["passes"][f"{mode_name} {names[k]} {sw}^2 -> {W}^2"] = {
+            "ms": m, "mpixels_s": W * W / (m / 1000.0) / 1e6,
+            "roofline": {"bound": "hbm", "achieved": algo / (m / 1000.0) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": algo / (m / 1000.0) / 1e9 / peak, "peak_source": peak_src,
+                         "algorithmic_bytes": algo},
+            "cpu_baseline": {"value": 64 * 64 / cpu_s / 1e6, "unit": "Mpixels/s", "cores": 1, "kind": "port",
+                             "sample": f"a 64^2 output from a {ssw}^2 source, FP64 restatement"}}
+    # whole multiscaled frames through cvr_render
+    out_ptr = dst
+    single = statistics.median(time_frames(ctx, lib, wl, wl.params, out_ptr, 5, 2))
+    out["frames"]["single 1024^2"] = {"ms": single}
+    for label, mode, k in (("multisample hat (2048^2 generated)", abi.MULTISCALE_MULTISAMPLE, abi.FILTER_HAT),
+                           ("downscale cardinal_omoms3 (2048^2 generated)", abi.MULTISCALE_DOWNSCALE,
+                            abi.FILTER_CARDINAL_OMOMS3),
+                           ("upscale catmull_rom (512^2 generated)", abi.MULTISCALE_UPSCALE, abi.FILTER_CATMULL_ROM),
+                           ("upscale cardinal_bspline3 (512^2 generated)", abi.MULTISCALE_UPSCALE,
+                            abi.FILTER_CARDINAL_BSPLINE3)):
+        ctx.set_multiscaling(mode, k)
+        try:
+            t = statistics.median(time_frames(ctx, lib, wl, wl.params, out_ptr, 5, 2))
+        finally:
+            ctx.set_multiscaling(abi.MULTISCALE_SINGLE)
+        out["frames"][label] = {"ms": t, "vs_single": t / single}
+    out["workload"] = WORKLOAD_DESC["plain_large"]
+    return out
+
+
 def tables_section(ctx, lib, wl, log=print):
     """The table builders of the headline workload: the GPU extinction SAT
     (int64, HBM streaming: N^3 voxels read + (N+2)^3 8-byte cells written in the
@@ -691,6 +779,7 @@ def run_ours(args):
     renderers = {}
     batch = None
     gradient = None
+    postpass = None
     tables = None
     if not args.quick:
         def reset_tuning():
@@ -722,6 +811,9 @@ def run_ours(args):
         if not args.no_gradient:
             gradient = gradient_section(ctx, lib, args)
         reset_tuning()
+        if not args.no_postpass:
+            postpass = postpass_section(ctx, lib, args)
+        reset_tuning()
         tables = tables_section(ctx, lib, wl)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -740,7 +832,7 @@ def run_ours(args):
         "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
         "clocks": clocks, "renderers": renderers, "surrogate": surrogate, "batch": batch,
-        "gradient": gradient, "tables": tables}))
+        "gradient": gradient, "postpass": postpass, "tables": tables}))
 
 
 def main():
@@ -756,6 +848,7 @@ def main():
     ap.add_argument("--surrogate-points", type=int, default=4_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient Blinn-Phong section")
+    ap.add_argument("--no-postpass", action="store_true", help="skip the pixel-multiscaling section")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--size", type=int, default=None, help="volume side override (profiling / small cases)")
     ap.add_argument("--image", type=int, default=None, help="image side override (profiling / small cases)")

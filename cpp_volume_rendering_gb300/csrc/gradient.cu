@@ -45,7 +45,7 @@ __device__ __forceinline__ void fd_finish(const GradBuild& b, float dx, float dy
     // glm::normalize: v * inversesqrt(dot(v, v))
     const float l2 = dx * dx + dy * dy + dz * dz;
     if (l2 > 0.0f) {
-      const float il = 1.0f / sqrtf(l2);
+      const float il = __frsqrt_rn(l2);  // correctly rounded 1/sqrt
       gx = dx * il; gy = dy * il; gz = dz * il;
     } else {
       gx = gy = gz = 0.0f;
@@ -59,7 +59,7 @@ __device__ __forceinline__ void fd_finish(const GradBuild& b, float dx, float dy
     // The filter sums gradients[x, y, z] -- the centre, not the neighbour --
     // over the in-bounds window and divides by the count, so the average is
     // the centre itself; it is then normalised when no component is zero.
-    const float il = 1.0f / sqrtf(gx * gx + gy * gy + gz * gz);
+    const float il = __frsqrt_rn(gx * gx + gy * gy + gz * gz);
     gx *= il; gy *= il; gz *= il;
   }
 }
@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(kGradTX * kGradTY) k_gradient_tiled(const T* _
 }
 
 // The 3x3x3 stencils with the planes brought in by the tensor memory
-// accelerator: a CTA owns a 32 x 16 column of voxels over kTmaZ planes; one
+// accelerator: a CTA owns a 32 x 16 column of voxels over zc planes; one
 // thread keeps kTmaBuf plane tiles (the column plus a one-voxel halo, read
 // from an x origin rounded down to 16 bytes; the copy engine writes 0 outside
 // the grid, which is GetNormalizedSample's 0) in flight, each completing on
@@ -214,8 +214,9 @@ __global__ void __launch_bounds__(kGradTX * kGradTY) k_gradient_tiled(const T* _
 //   sy = sum_z w_z E[z],  E = Sx(y-1) - Sx(y+1),   Sx = P(x-1) + 2 P(x) + P(x+1)
 //   sz = Q[z-1] - Q[z+1], Q = sum_y w_y Sx
 // -- the same integers as the direct 27-tap sums.  Needs the row pitch
-// (nx x voxel bytes) to be a multiple of 16 bytes.
-constexpr int kTmaTX = 32, kTmaTY = 16, kTmaZ = 32, kTmaBuf = 4;
+// (nx x voxel bytes) to be a multiple of 16 bytes.  A CTA walks zc planes
+// (32, or 16 / 8 when that is needed for two waves of CTAs on a small volume).
+constexpr int kTmaTX = 32, kTmaTY = 16, kTmaBuf = 4;
 constexpr int kTmaRows = kTmaTY + 2;
 constexpr int kTmaPitch = 96;                        // bytes of a tile row: 64 u8 or 48 u16 voxels
 constexpr int kTmaBufStride = 1792;                  // 128-byte aligned slots
@@ -233,13 +234,14 @@ struct TmaGeom {
 
 template <class T, bool SOBEL>
 __global__ void __launch_bounds__(256) k_gradient_tma(const __grid_constant__ CUtensorMap vol, int nx, int ny, int nz,
-                                                      GradBuild b, uint2* __restrict__ out, int* __restrict__ err) {
+                                                      int zc, GradBuild b, uint2* __restrict__ out,
+                                                      int* __restrict__ err) {
   using G = TmaGeom<T>;
   __shared__ __align__(128) uint8_t tiles[kTmaBuf][kTmaBufStride];
   __shared__ __align__(8) uint64_t bars[kTmaBuf];
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kTmaTX + tx;
-  const int x0 = blockIdx.x * kTmaTX, y0 = blockIdx.y * kTmaTY, z0 = blockIdx.z * kTmaZ;
-  const int z1 = min(z0 + kTmaZ, nz);
+  const int x0 = blockIdx.x * kTmaTX, y0 = blockIdx.y * kTmaTY, z0 = blockIdx.z * zc;
+  const int z1 = min(z0 + zc, nz);
   const int n_planes = z1 - z0 + 2;  // planes z0 - 1 .. z1
   if (tid == 0) {
 #pragma unroll
@@ -369,12 +371,18 @@ bool launch_gradient_tma(const void* vol, int nx, int ny, int nz, const GradBuil
                          cudaStream_t st) {
   CUtensorMap m;
   if (!volume_tensor_map<T>(vol, nx, ny, nz, &m)) return false;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 152;
+  const long long xy = (long long)((nx + kTmaTX - 1) / kTmaTX) * ((ny + kTmaTY - 1) / kTmaTY);
+  int zc = 32;
+  while (zc > 8 && xy * ((nz + zc - 1) / zc) < 16LL * sms) zc /= 2;
   const dim3 block(kTmaTX, kTmaTY / 2, 1);
-  const dim3 grid((nx + kTmaTX - 1) / kTmaTX, (ny + kTmaTY - 1) / kTmaTY, (nz + kTmaZ - 1) / kTmaZ);
+  const dim3 grid((nx + kTmaTX - 1) / kTmaTX, (ny + kTmaTY - 1) / kTmaTY, (nz + zc - 1) / zc);
   if (b.model == CVR_GRADIENT_FINITE_DIFFERENCES)
-    k_gradient_tma<T, false><<<grid, block, 0, st>>>(m, nx, ny, nz, b, out, err);
+    k_gradient_tma<T, false><<<grid, block, 0, st>>>(m, nx, ny, nz, zc, b, out, err);
   else
-    k_gradient_tma<T, true><<<grid, block, 0, st>>>(m, nx, ny, nz, b, out, err);
+    k_gradient_tma<T, true><<<grid, block, 0, st>>>(m, nx, ny, nz, zc, b, out, err);
   return true;
 }
 
