@@ -395,7 +395,7 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms,
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
                   c->d_sat32, c->d_lut32, c->d_kerr};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -652,6 +652,8 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
     return fail(c, CVR_ERR_INVALID_ARG, "cvr_render: multiscaled frame size out of range");
   CK(c, cudaSetDevice(c->device));
   CK(c, ensure(c->d_ms, c->ms_cap, (size_t)gw * gh * sizeof(float4)));
+  if (const size_t sb = multiscale_scratch(c->ms_mode, c->ms_kernel, gw, gh, w, h))
+    CK(c, ensure(c->d_msf, c->msf_cap, sb));
   // the camera keeps the output's aspect (u_CameraAspectRatio is the screen's)
   cvr_camera cm = cam ? *cam : cvr_camera{};
   if (cam && !(cm.aspect > 0.0f)) cm.aspect = (float)w / (float)h;
@@ -659,7 +661,7 @@ static cvr_status render_impl(cvr_ctx* c, int method, const cvr_camera* cam, con
                               reinterpret_cast<float*>(c->d_ms), gw, gh, nullptr, stats);
   if (s != CVR_OK) return s;
   CK(c, launch_multiscale(c->ms_mode, c->ms_kernel, c->d_ms, gw, gh, reinterpret_cast<float4*>(out), w, h,
-                          c->stream));
+                          c->d_msf, c->stream));
   return CVR_OK;
 }
 

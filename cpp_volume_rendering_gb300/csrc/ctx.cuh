@@ -236,6 +236,8 @@ struct cvr_ctx {
   int ms_mode = CVR_MULTISCALE_SINGLE, ms_kernel = CVR_FILTER_HAT, ms_fw = 2, ms_fh = 2;
   float4* d_ms = nullptr;
   size_t ms_cap = 0;
+  float4* d_msf = nullptr;  // digital-filter scratch
+  size_t msf_cap = 0;
 };
 
 // Exchanges the current-volume fields of c with slot s.
@@ -363,7 +365,9 @@ cvr_status grad_args(cvr_ctx* c, int method, const cvr_light* light, FrameArgs* 
 // w x h, and the post-pass from it (modified in place by up-scaling filters).
 void multiscale_size(int mode, int fw, int fh, int w, int h, int* gw, int* gh);
 cudaError_t launch_multiscale(int mode, int kern, float4* src, int gw, int gh, float4* dst, int w, int h,
-                              cudaStream_t st);
+                              float4* scratch, cudaStream_t st);
+// Bytes of the digital-filter scratch launch_multiscale needs (0: none).
+size_t multiscale_scratch(int mode, int kern, int gw, int gh, int w, int h);
 // The volume as the marchers read it: the plain layout, or the bricked copy
 // of the context's brick size (made on first use after the volume changed).
 cvr_status render_volume_view(cvr_ctx* c, VolumeView* v);

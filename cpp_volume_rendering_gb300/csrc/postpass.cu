@@ -121,34 +121,86 @@ struct LuTable {
   float L[9];
 };
 
-__global__ void k_digital_filter(float4* __restrict__ img, int w, int h, int dir, LuTable t) {
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
+// The digital filter (cbs_digital_filter.comp / comoms_digital_filter.comp:
+// the LU solve of the interpolation condition along every row, then every
+// column) as chunked first-order recursions.  Forward y[i] = f[i] - L y[i-1]
+// and reverse o[i] = L (y[i] - o[i+1]) both have |L| < 0.35 from the m-th
+// entry on, so a chunk of a line can start kDfWarm entries before its first
+// one from a zero state: the start's error is scaled by L^kDfWarm (< 2e-15)
+// before the chunk begins.  The chunk holding the line's first m entries (the
+// varying L) starts exactly at the line's end, as does the last chunk of the
+// reverse.  One thread per chunk of kDfChunk entries: many threads per line
+// instead of one long dependent walk.  Forward reads f and writes y to a
+// second buffer, reverse reads y and writes the result over f (a chunk's
+// warm-up reads its neighbour's entries, so neither pass runs in place).
+constexpr int kDfChunk = 64, kDfWarm = 32;
+
+struct DfLine {
+  size_t base, step;
+  int n, s, e;  // line length, chunk [s, e)
+};
+__device__ __forceinline__ bool df_line(int w, int h, int dir, DfLine& d) {
   const int lines = dir == 0 ? h : w, n = dir == 0 ? w : h;
-  if (line >= lines || n < t.m) return;
-  const size_t step = dir == 0 ? 1 : (size_t)w;
-  float4* __restrict__ p = img + (dir == 0 ? (size_t)line * w : (size_t)line);
+  const int chunks = (n + kDfChunk - 1) / kDfChunk;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)lines * chunks) return false;
+  int line, chunk;
+  if (dir == 0) { chunk = (int)(idx % chunks); line = (int)(idx / chunks); }  // rows: a thread per chunk of a row
+  else { line = (int)(idx % lines); chunk = (int)(idx / lines); }             // columns: lanes on adjacent columns
+  d.base = dir == 0 ? (size_t)line * w : (size_t)line;
+  d.step = dir == 0 ? 1 : (size_t)w;
+  d.n = n;
+  d.s = chunk * kDfChunk;
+  d.e = min(d.s + kDfChunk, n);
+  return true;
+}
+
+__global__ void k_df_forward(const float4* __restrict__ f, float4* __restrict__ y, int w, int h, int dir, LuTable t) {
+  DfLine d;
+  if (!df_line(w, h, dir, d)) return;
   const int m = t.m;
-  const float L_inf = t.L[m - 1], v_inv = L_inf / (1.0f + L_inf);
-  // forward: f[i] -= L[i-1] f[i-1]  (L_inf from i = m on); the running value
-  // stays in registers so the loads of the line do not wait on the recursion
-  float4 prev = p[0];
+  const float L_inf = t.L[m - 1];
+  const float4* __restrict__ fp = f + d.base;
+  float4* __restrict__ yp = y + d.base;
+  int i = d.s - kDfWarm;
+  float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (i <= 0) {  // exact start: y[0] = f[0]
+    prev = fp[0];
+    if (d.s == 0) yp[0] = prev;
+    i = 1;
+  }
 #pragma unroll 4
-  for (int i = 1; i < n; ++i) {
+  for (; i < d.e; ++i) {
     const float l = i < m ? t.L[i - 1] : L_inf;
-    float4 v = p[(size_t)i * step];
+    float4 v = fp[(size_t)i * d.step];
     v.x -= l * prev.x; v.y -= l * prev.y; v.z -= l * prev.z; v.w -= l * prev.w;
-    if (i < n - 1) p[(size_t)i * step] = v;
+    if (i >= d.s) yp[(size_t)i * d.step] = v;
     prev = v;
   }
-  // f[n-1] *= p_inv v_inv (p_inv = 1); reverse: f[i] = L (f[i] - f[i+1])
-  float4 next = make_float4(prev.x * v_inv, prev.y * v_inv, prev.z * v_inv, prev.w * v_inv);
-  p[(size_t)(n - 1) * step] = next;
+}
+
+__global__ void k_df_reverse(const float4* __restrict__ y, float4* __restrict__ o, int w, int h, int dir, LuTable t) {
+  DfLine d;
+  if (!df_line(w, h, dir, d)) return;
+  const int m = t.m;
+  const float L_inf = t.L[m - 1], v_inv = L_inf / (1.0f + L_inf);
+  const float4* __restrict__ yp = y + d.base;
+  float4* __restrict__ op = o + d.base;
+  const int n = d.n;
+  int i = d.e - 1 + kDfWarm;
+  float4 next = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (i >= n - 1) {  // exact start: o[n-1] = y[n-1] * v_inv (p_inv = 1)
+    const float4 v = yp[(size_t)(n - 1) * d.step];
+    next = make_float4(v.x * v_inv, v.y * v_inv, v.z * v_inv, v.w * v_inv);
+    if (d.e == n) op[(size_t)(n - 1) * d.step] = next;
+    i = n - 2;
+  }
 #pragma unroll 4
-  for (int i = n - 2; i >= 0; --i) {
+  for (; i >= d.s; --i) {
     const float l = i >= m - 1 ? L_inf : t.L[i];
-    float4 v = p[(size_t)i * step];
+    float4 v = yp[(size_t)i * d.step];
     v.x = l * (v.x - next.x); v.y = l * (v.y - next.y); v.z = l * (v.z - next.z); v.w = l * (v.w - next.w);
-    p[(size_t)i * step] = v;
+    if (i < d.e) op[(size_t)i * d.step] = v;
     next = v;
   }
 }
@@ -168,10 +220,18 @@ LuTable lu_table(int kern) {
   return t;
 }
 
-cudaError_t digital_filter(float4* img, int w, int h, int kern, cudaStream_t st) {
+// Rows then columns (lines shorter than m are left as they are, as the
+// shaders skip them); scratch holds w x h float4.
+cudaError_t digital_filter(float4* img, float4* scratch, int w, int h, int kern, cudaStream_t st) {
   const LuTable t = lu_table(kern);
-  k_digital_filter<<<(h + 127) / 128, 128, 0, st>>>(img, w, h, 0, t);
-  k_digital_filter<<<(w + 127) / 128, 128, 0, st>>>(img, w, h, 1, t);
+  for (int dir = 0; dir < 2; ++dir) {
+    const int lines = dir == 0 ? h : w, n = dir == 0 ? w : h;
+    if (n < t.m) continue;
+    const long long threads = (long long)lines * ((n + kDfChunk - 1) / kDfChunk);
+    const unsigned blocks = (unsigned)((threads + 127) / 128);
+    k_df_forward<<<blocks, 128, 0, st>>>(img, scratch, w, h, dir, t);
+    k_df_reverse<<<blocks, 128, 0, st>>>(scratch, img, w, h, dir, t);
+  }
   return cudaGetLastError();
 }
 
@@ -190,10 +250,15 @@ void multiscale_size(int mode, int fw, int fh, int w, int h, int* gw, int* gh) {
   else { *gw = w * fw; *gh = h * fh; }
 }
 
+size_t multiscale_scratch(int mode, int kern, int gw, int gh, int w, int h) {
+  if (!has_digital_filter(kern) || mode == CVR_MULTISCALE_MULTISAMPLE) return 0;
+  return (mode == CVR_MULTISCALE_UPSCALE ? (size_t)gw * gh : (size_t)w * h) * sizeof(float4);
+}
+
 // src (gw x gh) -> dst (w x h); src is modified in place by the up-scaling
-// digital filter.
+// digital filter; scratch has multiscale_scratch bytes.
 cudaError_t launch_multiscale(int mode, int kern, float4* src, int gw, int gh, float4* dst, int w, int h,
-                              cudaStream_t st) {
+                              float4* scratch, cudaStream_t st) {
   const dim3 block(16, 8);
   const dim3 grid((w + 15) / 16, (h + 7) / 8);
   cudaError_t e = cudaSuccess;
@@ -204,9 +269,9 @@ cudaError_t launch_multiscale(int mode, int kern, float4* src, int gw, int gh, f
   if (mode == CVR_MULTISCALE_DOWNSCALE) {
     k_downscale<<<grid, block, 0, st>>>(src, gw, gh, dst, w, h, kern);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    return has_digital_filter(kern) ? digital_filter(dst, w, h, kern, st) : cudaSuccess;
+    return has_digital_filter(kern) ? digital_filter(dst, scratch, w, h, kern, st) : cudaSuccess;
   }
-  if (has_digital_filter(kern) && (e = digital_filter(src, gw, gh, kern, st)) != cudaSuccess) return e;
+  if (has_digital_filter(kern) && (e = digital_filter(src, scratch, gw, gh, kern, st)) != cudaSuccess) return e;
   k_upscale<<<grid, block, 0, st>>>(src, gw, gh, dst, w, h, kern);
   return cudaGetLastError();
 }
@@ -246,8 +311,11 @@ cvr_status cvr_rescale_frame(cvr_ctx* c, int mode, int kernel, const float* src_
   CK(c, cudaSetDevice(c->device));
   const size_t bytes = (size_t)sw * sh * sizeof(float4);
   CK(c, ensure(c->d_ms, c->ms_cap, bytes));
+  if (const size_t sb = multiscale_scratch(mode, kernel, sw, sh, w, h))
+    CK(c, ensure(c->d_msf, c->msf_cap, sb));
   CK(c, cudaMemcpyAsync(c->d_ms, src_dev, bytes, cudaMemcpyDeviceToDevice, c->stream));
-  CK(c, launch_multiscale(mode, kernel, c->d_ms, sw, sh, reinterpret_cast<float4*>(dst_dev), w, h, c->stream));
+  CK(c, launch_multiscale(mode, kernel, c->d_ms, sw, sh, reinterpret_cast<float4*>(dst_dev), w, h, c->d_msf,
+                          c->stream));
   return CVR_OK;
 }
 
