@@ -166,6 +166,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
       std::vector<unsigned> q;
       if (!compact_plan(c->sat_ext, slot_vmax[v], &F, &q)) { all_compact = false; break; }
       const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+      if (cells >= kCompactMaxCells) { all_compact = false; break; }
       uint4* d = nullptr;
       cudaError_t e = cudaMalloc((void**)&d, cells * sizeof(uint4));
       if (e == cudaErrorMemoryAllocation) { cudaGetLastError(); all_compact = false; break; }  // int64 tables

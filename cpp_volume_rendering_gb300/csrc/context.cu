@@ -105,7 +105,8 @@ namespace ctxutil {
 
 cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
   VolumeView v = volume_view(c);
-  if (c->quads) {
+  // the quad copy is indexed with 32-bit cell numbers
+  if (c->quads && (size_t)c->nx * c->ny * c->nz < kCompactMaxCells) {
     if (c->vbrick_bs != kQuadCopy) {
       const size_t n = (size_t)c->nx * c->ny * c->nz;
       CK(c, ensure(c->d_vbrick, c->vbrick_cap, n * 4 * (c->dtype == CVR_U8 ? 1 : 2)));
@@ -180,6 +181,7 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
   ExtArgs a{};
   a.sat.sat = c->d_sat;
   a.sat.sx = c->nx + 2; a.sat.sy = c->ny + 2; a.sat.sz = c->nz + 2;
+  a.sat.sxy = (unsigned)a.sat.sx * (unsigned)a.sat.sy;
   a.sat.inv_scale = (float)std::ldexp(1.0, -c->sat_frac_bits);
   a.sat.inv_spacing = f.vol.inv_spacing;
   a.sat.min_pos = f.vol.spacing * 0.5f;
@@ -320,6 +322,7 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
   if (!compact_plan(c->sat_ext, vmax, &F, &q)) return CVR_OK;
   if (c->sat32_F != F || !c->d_sat32) {
     const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+    if (cells >= kCompactMaxCells) return CVR_OK;  // 32-bit cell indices: the int64 table
     c->sat32_F = kNoCompactSat;
     // the quad table is twice the int64 one: without room for it the frame
     // keeps the int64 table
@@ -552,6 +555,8 @@ cvr_status cvr_build_ext_pyramid(cvr_ctx* c, const cvr_pyramid_params* p) {
     P.offset[l] = off;
     off += (long long)P.dims[l][0] * P.dims[l][1] * P.dims[l][2];
   }
+  if (off >= (1LL << 31))
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_ext_pyramid: pyramids hold fewer than 2^31 values");
   P.n_levels = levels;
   VolumeView v = volume_view(c);
   P.grid = v.grid;

@@ -93,6 +93,9 @@ inline void swap_tex(TexState& a, TexState& b) {
 constexpr int kNoCompactSat = -1000;
 // vbrick_bs of a copy in the x-y quad layout.
 constexpr int kQuadCopy = 100;
+// Cells of a compact SAT or a quad volume copy: indexed with 32-bit cell
+// numbers, so larger grids keep the int64 table / the plain layout.
+constexpr size_t kCompactMaxCells = (size_t)1 << 31;
 
 // A resident volume that is not the current one (cvr_select_volume): the
 // volume, its SAT, pyramid and texture copies.  The current volume lives in

@@ -138,17 +138,19 @@ __device__ __forceinline__ float sample_volume(const VolumeView& v, float3 tex_p
     const Tap tx = axis_tap(fmaxf(fmaf(tex_pos.x, v.inv_spacing.x, -0.5f), 0.0f), v.nx);
     const Tap ty = axis_tap(fmaxf(fmaf(tex_pos.y, v.inv_spacing.y, -0.5f), 0.0f), v.ny);
     const Tap tz = axis_tap(fmaf(tex_pos.z, v.inv_spacing.z, -0.5f), v.nz);
-    const size_t cell = (size_t)tx.i0 + (size_t)v.nx * (size_t)ty.i0;
-    const size_t plane = (size_t)v.nx * (size_t)v.ny;
+    // 32-bit cell numbers (the quad copy is only made below 2^31 cells)
+    const unsigned cell = (unsigned)tx.i0 + (unsigned)v.nx * (unsigned)ty.i0;
+    const unsigned plane = (unsigned)v.nx * (unsigned)v.ny;
+    const unsigned k0 = cell + plane * (unsigned)tz.i0, k1 = cell + plane * (unsigned)tz.i1;
     float c000, c100, c010, c110, c001, c101, c011, c111;
     if (v.dtype == 1) {
-      const uchar4* q = static_cast<const uchar4*>(v.voxels) + cell;
-      const uchar4 a = __ldg(q + plane * (size_t)tz.i0), b = __ldg(q + plane * (size_t)tz.i1);
+      const uchar4* q = static_cast<const uchar4*>(v.voxels);
+      const uchar4 a = __ldg(q + k0), b = __ldg(q + k1);
       c000 = a.x; c100 = a.y; c010 = a.z; c110 = a.w;
       c001 = b.x; c101 = b.y; c011 = b.z; c111 = b.w;
     } else {
-      const ushort4* q = static_cast<const ushort4*>(v.voxels) + cell;
-      const ushort4 a = __ldg(q + plane * (size_t)tz.i0), b = __ldg(q + plane * (size_t)tz.i1);
+      const ushort4* q = static_cast<const ushort4*>(v.voxels);
+      const ushort4 a = __ldg(q + k0), b = __ldg(q + k1);
       c000 = a.x; c100 = a.y; c010 = a.z; c110 = a.w;
       c001 = b.x; c101 = b.y; c011 = b.z; c111 = b.w;
     }
@@ -212,6 +214,7 @@ struct SatView {
   const uint4* sat32;
   float inv_scale32;     // 2^-F32
   int sx, sy, sz;        // SAT dims = volume dims + 2
+  unsigned sxy;          // sx * sy (cells of the compact table: < 2^31)
   float inv_scale;       // 2^-F
   float3 inv_spacing;
   float3 min_pos;        // MinSATPosition = spacing*0.5
@@ -264,11 +267,11 @@ struct D9 { D3<W> y[3]; };  // consecutive y-differences of x-differenced rows
 // coordinate clamp guarantees).
 __device__ __forceinline__ D9<unsigned> plane_diffs_quad(const uint4* sat, const SatView& S, int z,
                                                          const BoxAxis& X, const BoxAxis& Y) {
-  const uint4* plane = sat + (size_t)z * (size_t)S.sx * (size_t)S.sy;
-  const uint4* r0 = plane + (size_t)Y.s[0] * S.sx;
-  const uint4* r2 = plane + (size_t)Y.s[2] * S.sx;
-  const uint4 q00 = __ldg(r0 + X.s[0]), q01 = __ldg(r0 + X.s[2]);
-  const uint4 q10 = __ldg(r2 + X.s[0]), q11 = __ldg(r2 + X.s[2]);
+  // 32-bit cell numbers (the compact table has fewer than 2^31 cells)
+  const unsigned zo = (unsigned)z * S.sxy;
+  const unsigned r0 = zo + (unsigned)Y.s[0] * (unsigned)S.sx, r2 = zo + (unsigned)Y.s[2] * (unsigned)S.sx;
+  const uint4 q00 = __ldg(sat + (r0 + (unsigned)X.s[0])), q01 = __ldg(sat + (r0 + (unsigned)X.s[2]));
+  const uint4 q10 = __ldg(sat + (r2 + (unsigned)X.s[0])), q11 = __ldg(sat + (r2 + (unsigned)X.s[2]));
   const D3<unsigned> rows[4] = {x_diffs(q00.x, q00.y, q01.x, q01.y), x_diffs(q00.z, q00.w, q01.z, q01.w),
                                 x_diffs(q10.x, q10.y, q11.x, q11.y), x_diffs(q10.z, q10.w, q11.z, q11.w)};
   D9<unsigned> r;
@@ -351,20 +354,22 @@ struct PyramidView {
   float3 inv_grid;
 };
 
-__device__ __forceinline__ float pyr_fetch(const PyramidView& P, int l, int x, int y, int z) {
-  const int* d = P.dims[l];
-  return __ldg(P.data + P.offset[l] + (long long)x + (long long)d[0] * ((long long)y + (long long)d[1] * z));
-}
-// textureLod(pyr, tex_pos / S, level) at an integer level: trilinear in that level.
+// textureLod(pyr, tex_pos / S, level) at an integer level: trilinear in that
+// level.  32-bit element numbers: pyramids hold fewer than 2^31 values.
 __device__ __forceinline__ float pyr_sample_level(const PyramidView& P, int l, float3 tex_pos) {
   const int* d = P.dims[l];
   Tap tx = axis_tap(fmaf(tex_pos.x * P.inv_grid.x, float(d[0]), -0.5f), d[0]);
   Tap ty = axis_tap(fmaf(tex_pos.y * P.inv_grid.y, float(d[1]), -0.5f), d[1]);
   Tap tz = axis_tap(fmaf(tex_pos.z * P.inv_grid.z, float(d[2]), -0.5f), d[2]);
-  float c000 = pyr_fetch(P, l, tx.i0, ty.i0, tz.i0), c100 = pyr_fetch(P, l, tx.i1, ty.i0, tz.i0);
-  float c010 = pyr_fetch(P, l, tx.i0, ty.i1, tz.i0), c110 = pyr_fetch(P, l, tx.i1, ty.i1, tz.i0);
-  float c001 = pyr_fetch(P, l, tx.i0, ty.i0, tz.i1), c101 = pyr_fetch(P, l, tx.i1, ty.i0, tz.i1);
-  float c011 = pyr_fetch(P, l, tx.i0, ty.i1, tz.i1), c111 = pyr_fetch(P, l, tx.i1, ty.i1, tz.i1);
+  const unsigned d0 = (unsigned)d[0], d01 = (unsigned)d[0] * (unsigned)d[1];
+  const unsigned b = (unsigned)P.offset[l] + (unsigned)tx.i0 + d0 * (unsigned)ty.i0 + d01 * (unsigned)tz.i0;
+  const unsigned dx = (unsigned)(tx.i1 - tx.i0), dy = (unsigned)(ty.i1 - ty.i0) * d0,
+                 dz = (unsigned)(tz.i1 - tz.i0) * d01;
+  const float* q = P.data;
+  float c000 = __ldg(q + b), c100 = __ldg(q + (b + dx));
+  float c010 = __ldg(q + (b + dy)), c110 = __ldg(q + (b + dy + dx));
+  float c001 = __ldg(q + (b + dz)), c101 = __ldg(q + (b + dz + dx));
+  float c011 = __ldg(q + (b + dz + dy)), c111 = __ldg(q + (b + dz + dy + dx));
   float c00 = fmaf(tx.t, c100 - c000, c000), c10 = fmaf(tx.t, c110 - c010, c010);
   float c01 = fmaf(tx.t, c101 - c001, c001), c11 = fmaf(tx.t, c111 - c011, c011);
   float c0 = fmaf(ty.t, c10 - c00, c00), c1 = fmaf(ty.t, c11 - c01, c01);

@@ -237,7 +237,8 @@ cvr_status cvr_get_sat_info(cvr_ctx* ctx, int dims[3], int* frac_bits);
 /* Copies the SAT to host memory (dims[0]*dims[1]*dims[2] int64). Synchronous. */
 cvr_status cvr_download_sat(cvr_ctx* ctx, int64_t* host_out);
 
-/* Gaussian extinction mip pyramid (gen_extcoefvol_anysize*.comp + backtotau.comp). */
+/* Gaussian extinction mip pyramid (gen_extcoefvol_anysize*.comp + backtotau.comp);
+ * all levels together hold fewer than 2^31 values (CVR_ERR_INVALID_ARG otherwise). */
 cvr_status cvr_build_ext_pyramid(cvr_ctx* ctx, const cvr_pyramid_params* params);
 /* Level count and per-level dims (level_dims is [max_levels][3]). */
 cvr_status cvr_get_pyramid_info(cvr_ctx* ctx, int* n_levels, int (*level_dims)[3], int max_levels);
