@@ -4,12 +4,12 @@
 // camera-state list and a light-source list), selects a renderer by its
 // abbreviation, renders frames and writes the last one as a .pfm image.
 //
-//   cvr_headless --volume V.raw|V.syn --tf T.tf1d --renderer s_1pebs
+//   cvr_headless --volume V.raw|.syn|.pvm|.nrrd|.nhrd|.dat --tf T.tf1d --renderer s_1pebs
 //                [--width 768 --height 768] [--frames 1]
 //                [--cameras LIST --camera-index i] [--lights LIST --light-index i]
 //                [--eye x y z] [--fovy deg] [--occlusion 0|1] [--shadow 0|1]
 //                [--gradient sobel|fd|cs|none] [--gradient-shading 0|1]
-//                [--multiscaling 0..3] [--image-filter 0..5]
+//                [--multiscaling 0..3 (s_1pebs)] [--image-filter 0..5]
 //                [--out frame.pfm]
 // Exit code 0 on success, 1 on a usage error, 2 on a data error, 3 on a
 // rendering error; messages go to stderr.
