@@ -131,6 +131,25 @@ cudaError_t launch_quad_volume(const void* src, void* dst, int dtype, int nx, in
   return cudaGetLastError();
 }
 
+// x-y quads of every pyramid level (successors clamped within the level).
+__global__ void k_quad_pyramid(const float* __restrict__ src, float4* __restrict__ dst, int dx, int dy,
+                               long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int x = (int)(i % dx), y = (int)((i / dx) % dy);
+  const long long ox = x + 1 < dx ? 1 : 0, oy = y + 1 < dy ? dx : 0;
+  dst[i] = make_float4(src[i], src[i + ox], src[i + oy], src[i + oy + ox]);
+}
+
+cudaError_t launch_pyramid_quads(const PyramidView& P, const float* data, float4* dst, cudaStream_t st) {
+  for (int l = 0; l < P.n_levels; ++l) {
+    const long long n = (long long)P.dims[l][0] * P.dims[l][1] * P.dims[l][2];
+    k_quad_pyramid<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(data + P.offset[l], dst + P.offset[l], P.dims[l][0],
+                                                                P.dims[l][1], n);
+  }
+  return cudaGetLastError();
+}
+
 // x-y quads of a table: out[(x, y, z)] = s at (x, y), (x', y), (x, y'),
 // (x', y') of plane z, with x' = min(x + 1, sx - 1), y' = min(y + 1, sy - 1).
 __global__ void k_sat_quads(const unsigned* __restrict__ s, uint4* __restrict__ out, int sx, int sy,

@@ -21,6 +21,8 @@ cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, i
 
 // Grid-stride fill of a device buffer (used to flush L2 between timed frames).
 cudaError_t launch_fill(void* p, size_t bytes, unsigned int v, cudaStream_t st);
+// The x-y quad copy of every pyramid level (float4 per value, same offsets).
+cudaError_t launch_pyramid_quads(const PyramidView& P, const float* data, float4* dst, cudaStream_t st);
 // The x-y quad copy of a plain volume (uchar4 / ushort4 per voxel).
 cudaError_t launch_quad_volume(const void* src, void* dst, int dtype, int nx, int ny, int nz, cudaStream_t st);
 // Bricked copy of a plain volume (bricks of 2^bs voxels per edge); the copy

@@ -341,6 +341,33 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
   return CVR_OK;
 }
 
+cvr_status pyramid_view(cvr_ctx* c, PyramidView* out) {
+  PyramidView P = c->pyr;
+  P.data = c->d_pyr;
+  P.quads = nullptr;
+  if (!c->quads) {  // the plain layout
+    *out = P;
+    return CVR_OK;
+  }
+  if (!c->pyrq_ready) {
+    const int L = c->pyr.n_levels - 1;
+    const size_t n = (size_t)c->pyr.offset[L] + (size_t)c->pyr.dims[L][0] * c->pyr.dims[L][1] * c->pyr.dims[L][2];
+    // without room for the copy the taps read the plain levels
+    cudaError_t e = ensure(c->d_pyrq, c->pyrq_cap, n * sizeof(float4));
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      *out = P;
+      return CVR_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "pyramid quads");
+    CK(c, launch_pyramid_quads(P, c->d_pyr, c->d_pyrq, c->stream));
+    c->pyrq_ready = true;
+  }
+  P.quads = c->d_pyrq;
+  *out = P;
+  return CVR_OK;
+}
+
 cvr_status check_kernel_flag(cvr_ctx* c, const char* what) {
   int e = 0;
   CK(c, cudaMemcpyAsync(&e, c->d_kerr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -399,7 +426,7 @@ void cvr_destroy(cvr_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
                   c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
-                  c->d_sat32, c->d_lut32, c->d_kerr};
+                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -566,6 +593,7 @@ cvr_status cvr_build_ext_pyramid(cvr_ctx* c, const cvr_pyramid_params* p) {
   CK(c, launch_pyramid_build(v, c->d_rgba, c->tf_n, p->sigma0, P, c->d_pyr, c->stream));
   c->pyr = P;
   c->pyr_ready = true;
+  c->pyrq_ready = false;
   c->tex.pyr_valid = false;
   return CVR_OK;
 }
@@ -725,8 +753,8 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
       if (!c->cone_ready) return fail(c, CVR_ERR_NOT_READY, "cvr_render: cone tables not set");
       f.step = p->step_size;
       DosArgs a{};
-      a.pyr = c->pyr;
-      a.pyr.data = c->d_pyr;
+      cvr_status ps = pyramid_view(c, &a.pyr);
+      if (ps != CVR_OK) return ps;
       a.occ_sections = c->d_occ_sec; a.sdw_sections = c->d_sdw_sec;
       a.occ = c->occ; a.sdw = c->sdw;
       a.apply_occ = p->apply_occlusion; a.apply_sdw = p->apply_shadow; a.shadow_type = p->shadow_type;

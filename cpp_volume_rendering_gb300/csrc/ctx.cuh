@@ -121,6 +121,9 @@ struct VolSlot {
   size_t pyr_cap = 0;
   PyramidView pyr{};
   bool pyr_ready = false;
+  float4* d_pyrq = nullptr;
+  size_t pyrq_cap = 0;
+  bool pyrq_ready = false;
   TexState tex;
   void* d_vbrick = nullptr;
   size_t vbrick_cap = 0;
@@ -130,7 +133,7 @@ struct VolSlot {
   bool grad_ready = false;
   cvr_gradient_params grad_params{CVR_GRADIENT_NONE, 1, 0, 1};
   ~VolSlot() {
-    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick, d_grad, d_sat32, d_lut32};
+    void* bufs[] = {d_vol, d_sat, d_lut, d_pyr, d_vbrick, d_grad, d_sat32, d_lut32, d_pyrq};
     for (void* p : bufs)
       if (p) cudaFree(p);
   }
@@ -184,11 +187,14 @@ struct cvr_ctx {
   size_t lut32_cap = 0;
   int sat32_F = kNoCompactSat;
   bool compact_sat = true;                   // cvr_set_compact_sat
-  // pyramid
+  // pyramid, and its x-y quad copy for FP32 taps (built with the first frame that needs it)
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;
   PyramidView pyr{};
   bool pyr_ready = false;
+  float4* d_pyrq = nullptr;
+  size_t pyrq_cap = 0;
+  bool pyrq_ready = false;
   // cone tables
   float4* d_occ_sec = nullptr;
   float4* d_sdw_sec = nullptr;
@@ -266,6 +272,9 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->pyr_cap, s.pyr_cap);
   std::swap(c->pyr, s.pyr);
   std::swap(c->pyr_ready, s.pyr_ready);
+  std::swap(c->d_pyrq, s.d_pyrq);
+  std::swap(c->pyrq_cap, s.pyrq_cap);
+  std::swap(c->pyrq_ready, s.pyrq_ready);
   swap_tex(c->tex, s.tex);
   std::swap(c->d_vbrick, s.d_vbrick);
   std::swap(c->vbrick_cap, s.vbrick_cap);
@@ -290,6 +299,10 @@ inline cvr_status fail(cvr_ctx* c, cvr_status code, const std::string& msg) {
 
 // Reads (synchronously) and clears the context's kernel error flag.
 cvr_status check_kernel_flag(cvr_ctx* c, const char* what);
+// The current pyramid's view for kernels; under the quad layout with its x-y
+// quad copy when one can be made (FP32 taps: two loads instead of eight, same
+// values).
+cvr_status pyramid_view(cvr_ctx* c, PyramidView* out);
 
 inline cvr_status cuda_fail(cvr_ctx* c, cudaError_t e, const char* what) {
   cudaGetLastError();  // clear a sticky launch error where possible

@@ -347,6 +347,9 @@ __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2)
 #define CVR_MAX_LEVELS 16
 struct PyramidView {
   const float* data;
+  // x-y quads of every level (cell (x, y, z) = the values at (x, y), (x', y),
+  // (x, y'), (x', y') of its level, successors clamped), same offsets; or nullptr
+  const float4* quads;
   int n_levels;
   int dims[CVR_MAX_LEVELS][3];
   long long offset[CVR_MAX_LEVELS];
@@ -358,10 +361,23 @@ struct PyramidView {
 // level.  32-bit element numbers: pyramids hold fewer than 2^31 values.
 __device__ __forceinline__ float pyr_sample_level(const PyramidView& P, int l, float3 tex_pos) {
   const int* d = P.dims[l];
-  Tap tx = axis_tap(fmaf(tex_pos.x * P.inv_grid.x, float(d[0]), -0.5f), d[0]);
-  Tap ty = axis_tap(fmaf(tex_pos.y * P.inv_grid.y, float(d[1]), -0.5f), d[1]);
-  Tap tz = axis_tap(fmaf(tex_pos.z * P.inv_grid.z, float(d[2]), -0.5f), d[2]);
+  const Tap tz = axis_tap(fmaf(tex_pos.z * P.inv_grid.z, float(d[2]), -0.5f), d[2]);
   const unsigned d0 = (unsigned)d[0], d01 = (unsigned)d[0] * (unsigned)d[1];
+  if (P.quads) {
+    // Texel coordinates below 0 raised to 0 so the successor taps are the
+    // quad's (both taps read the edge value there, as without the raise).
+    const Tap qx = axis_tap(fmaxf(fmaf(tex_pos.x * P.inv_grid.x, float(d[0]), -0.5f), 0.0f), d[0]);
+    const Tap qy = axis_tap(fmaxf(fmaf(tex_pos.y * P.inv_grid.y, float(d[1]), -0.5f), 0.0f), d[1]);
+    const unsigned cell = (unsigned)P.offset[l] + (unsigned)qx.i0 + d0 * (unsigned)qy.i0;
+    const float4 a = __ldg(P.quads + (cell + d01 * (unsigned)tz.i0));
+    const float4 e = __ldg(P.quads + (cell + d01 * (unsigned)tz.i1));
+    const float c00 = fmaf(qx.t, a.y - a.x, a.x), c10 = fmaf(qx.t, a.w - a.z, a.z);
+    const float c01 = fmaf(qx.t, e.y - e.x, e.x), c11 = fmaf(qx.t, e.w - e.z, e.z);
+    const float c0 = fmaf(qy.t, c10 - c00, c00), c1 = fmaf(qy.t, c11 - c01, c01);
+    return fmaf(tz.t, c1 - c0, c0);
+  }
+  const Tap tx = axis_tap(fmaf(tex_pos.x * P.inv_grid.x, float(d[0]), -0.5f), d[0]);
+  const Tap ty = axis_tap(fmaf(tex_pos.y * P.inv_grid.y, float(d[1]), -0.5f), d[1]);
   const unsigned b = (unsigned)P.offset[l] + (unsigned)tx.i0 + d0 * (unsigned)ty.i0 + d01 * (unsigned)tz.i0;
   const unsigned dx = (unsigned)(tx.i1 - tx.i0), dy = (unsigned)(ty.i1 - ty.i0) * d0,
                  dz = (unsigned)(tz.i1 - tz.i0) * d01;

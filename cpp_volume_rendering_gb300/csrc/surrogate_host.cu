@@ -70,8 +70,11 @@ SurArgs sur_args(cvr_ctx* c, const cvr_light* light, const cvr_gt_params* p, int
   const float ka = p->ka, kd = p->kd;
   SurArgs a{};
   a.sdw_dist = p->sdw_distance;
-  a.pyr = c->pyr;
-  a.pyr.data = c->d_pyr;
+  if (pyramid_view(c, &a.pyr) != CVR_OK) {  // a failed copy leaves the plain levels
+    a.pyr = c->pyr;
+    a.pyr.data = c->d_pyr;
+    a.pyr.quads = nullptr;
+  }
   a.packed = c->mlp ? c->mlp->packed : nullptr;
   a.apply_occ = apply_occ;
   a.apply_sdw = apply_sdw;
@@ -108,8 +111,11 @@ GtArgs gt_args(cvr_ctx* c, const cvr_gt_params* p, const cvr_light* light) {
 
 DosArgs dos_args(cvr_ctx* c, const cvr_dos_params* p, const cvr_light* light) {
   DosArgs a{};
-  a.pyr = c->pyr;
-  a.pyr.data = c->d_pyr;
+  if (pyramid_view(c, &a.pyr) != CVR_OK) {  // a failed copy leaves the plain levels
+    a.pyr = c->pyr;
+    a.pyr.data = c->d_pyr;
+    a.pyr.quads = nullptr;
+  }
   a.occ_sections = c->d_occ_sec; a.sdw_sections = c->d_sdw_sec;
   a.occ = c->occ; a.sdw = c->sdw;
   a.apply_occ = 1; a.apply_sdw = 1; a.shadow_type = p->shadow_type;

@@ -294,9 +294,10 @@ cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
 cvr_status cvr_set_brick_size(cvr_ctx* ctx, int edge);
 int cvr_get_brick_size(cvr_ctx* ctx);
 /* Volume layout of the marchers' FP32 samples (no reference counterpart):
- * CVR_LAYOUT_QUADS keeps a copy where each voxel cell holds the 2 x 2 voxels
- * of its x-y neighbourhood (4 x the volume's bytes), so a trilinear sample is
- * two loads instead of eight; results are bit-identical to the plain layout.
+ * CVR_LAYOUT_QUADS keeps copies of the volume and of the extinction pyramid
+ * where each cell holds the 2 x 2 values of its x-y neighbourhood (4 x the
+ * volume's bytes, 16 bytes per pyramid value), so a trilinear sample is two
+ * loads instead of eight; results are bit-identical to the plain layout.
  * It takes precedence over bricks; the autotuner tries it with them. */
 #define CVR_LAYOUT_PLAIN 0
 #define CVR_LAYOUT_QUADS 1

@@ -93,16 +93,18 @@ def test_extinction_anisotropic_spacing_and_aspect(ctx):
 
 @pytest.mark.parametrize("dtype", [abi.CVR_U8, abi.CVR_U16])
 def test_quad_layout_is_bit_identical_on_ragged_volumes(ctx, dtype):
-    """The x-y quad copy (successors clamped at the high faces, texel
-    coordinates raised to 0 at the low faces) renders the plain layout's bits
-    on odd, non-cubic volumes with anisotropic spacing, rays entering through
-    every face."""
+    """The x-y quad copies of the volume and of the pyramid (successors
+    clamped at the high faces, texel coordinates raised to 0 at the low faces)
+    render the plain layout's bits on odd, non-cubic volumes with anisotropic
+    spacing, rays entering through every face."""
     vol = scene.synth_value_noise(37, 23, 29, dtype, seed=12)
-    for name in ("plain", "ground_truth", "iso"):
+    for name in ("plain", "ground_truth", "iso", "cone"):
         wl = scene.workload(name, n=8, image=8)
         wl.volume = vol
         wl.spacing = (1.0, 1.5, 0.75)
         wl.width, wl.height = 64, 48
+        if name == "cone":  # a ragged pyramid: its quad copy is read as well
+            wl.pyramid = dict(base_dims=(19, 12, 15), sigma0=1.0, n_levels=4)
         scene.prepare(ctx, wl)
         for eye in ((120.0, 60.0, 35.0), (120.0, -150.0, -40.0)):
             wl.cam = scene.camera(scene.orbit_eye(*eye), fovy=40.0)
