@@ -172,30 +172,48 @@ cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, in
 // 7x7x7 Gaussian average (sigma S0, taps at integer multiples of S0) of the
 // TF opacity of the trilinearly sampled volume; samples outside the grid
 // count as 0 opacity but keep their weight.
+// The 7^3 Gaussian weights s^3 exp(-|f|^2 / (2 s^2)) of the tap offsets f =
+// (ptx, pty, ptz) * s, in the loops' order, and their sum in the same order:
+// the same values for every output voxel, computed once per CTA.
+__device__ __forceinline__ float stage_gauss(float s, float* w) {
+  for (int k = threadIdx.x; k < 343; k += blockDim.x) {
+    const int ptx = k / 49 - 3, pty = (k / 7) % 7 - 3, ptz = k % 7 - 3;
+    const float fx = float(ptx) * s, fy = float(pty) * s, fz = float(ptz) * s;
+    w[k] = (s * s * s) * expf(-(fx * fx + fy * fy + fz * fz) / (2.0f * s * s));
+  }
+  __syncthreads();
+  float sum_w = 0.0f;
+  for (int k = 0; k < 343; ++k) sum_w += w[k];
+  return sum_w;
+}
+
+// Inside the grid: t = p / S in [0, 1] on every axis, which for a correctly
+// rounded division is p in [0, S].
+__device__ __forceinline__ bool in_grid(float3 p, float3 g) {
+  return !(p.x < 0.0f || p.y < 0.0f || p.z < 0.0f || p.x > g.x || p.y > g.y || p.z > g.z);
+}
+
 __global__ void k_pyr_base(VolumeView vol, const float4* __restrict__ tf_rgba, int tf_n, int bx, int by, int bz,
                            float s0, float* __restrict__ out) {
+  __shared__ float sm_w[343];
   extern __shared__ float4 sm_tf[];
   for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tf[i] = tf_rgba[i];
-  __syncthreads();
+  const float sum_w = stage_gauss(s0, sm_w);
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = (long long)bx * by * bz;
   if (idx >= total) return;
   int x = int(idx % bx), y = int((idx / bx) % by), z = int(idx / ((long long)bx * by));
   float3 vs = f3(vol.grid.x / float(bx), vol.grid.y / float(by), vol.grid.z / float(bz));
   float3 gp = f3((float(x) + 0.5f) * vs.x, (float(y) + 0.5f) * vs.y, (float(z) + 0.5f) * vs.z);
-  float sum_wc = 0.0f, sum_w = 0.0f;
+  float sum_wc = 0.0f;
+  int k = 0;
   for (int ptx = -3; ptx < 4; ++ptx) {
     for (int pty = -3; pty < 4; ++pty) {
-      for (int ptz = -3; ptz < 4; ++ptz) {
-        float fx = float(ptx) * s0, fy = float(pty) * s0, fz = float(ptz) * s0;
-        float wk = (s0 * s0 * s0) * expf(-(fx * fx + fy * fy + fz * fz) / (2.0f * s0 * s0));
-        float3 p = gp + f3(fx, fy, fz);
-        float3 t = p / vol.grid;
+      for (int ptz = -3; ptz < 4; ++ptz, ++k) {
+        const float3 p = gp + f3(float(ptx) * s0, float(pty) * s0, float(ptz) * s0);
         float ck = 0.0f;
-        if (!(t.x < 0.0f || t.y < 0.0f || t.z < 0.0f || t.x > 1.0f || t.y > 1.0f || t.z > 1.0f))
-          ck = tf_alpha(sm_tf, tf_n, sample_volume(vol, p));
-        sum_wc += wk * ck;
-        sum_w += wk;
+        if (in_grid(p, vol.grid)) ck = tf_alpha(sm_tf, tf_n, sample_volume(vol, p));
+        sum_wc += sm_w[k] * ck;
       }
     }
   }
@@ -205,6 +223,8 @@ __global__ void k_pyr_base(VolumeView vol, const float4* __restrict__ tf_rgba, i
 // gen_extcoefvol_anysize_mmlevel.comp: level l from level l-1 with sigma
 // Si = S0 * 2^l, sampling level l-1 trilinearly (textureLod at an integer lod).
 __global__ void k_pyr_level(PyramidView P, int l, float si, float* __restrict__ out) {
+  __shared__ float sm_w[343];
+  const float sum_w = stage_gauss(si, sm_w);
   const int* d = P.dims[l];
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = (long long)d[0] * d[1] * d[2];
@@ -212,19 +232,15 @@ __global__ void k_pyr_level(PyramidView P, int l, float si, float* __restrict__ 
   int x = int(idx % d[0]), y = int((idx / d[0]) % d[1]), z = int(idx / ((long long)d[0] * d[1]));
   float3 lvs = P.grid / f3(float(d[0]), float(d[1]), float(d[2]));
   float3 gp = f3((float(x) + 0.5f) * lvs.x, (float(y) + 0.5f) * lvs.y, (float(z) + 0.5f) * lvs.z);
-  float sum_wc = 0.0f, sum_w = 0.0f;
+  float sum_wc = 0.0f;
+  int k = 0;
   for (int ptx = -3; ptx < 4; ++ptx) {
     for (int pty = -3; pty < 4; ++pty) {
-      for (int ptz = -3; ptz < 4; ++ptz) {
-        float fx = float(ptx) * si, fy = float(pty) * si, fz = float(ptz) * si;
-        float wk = (si * si * si) * expf(-(fx * fx + fy * fy + fz * fz) / (2.0f * si * si));
-        float3 p = gp + f3(fx, fy, fz);
-        float3 t = p / P.grid;
+      for (int ptz = -3; ptz < 4; ++ptz, ++k) {
+        const float3 p = gp + f3(float(ptx) * si, float(pty) * si, float(ptz) * si);
         float ck = 0.0f;
-        if (!(t.x < 0.0f || t.y < 0.0f || t.z < 0.0f || t.x > 1.0f || t.y > 1.0f || t.z > 1.0f))
-          ck = pyr_sample_level(P, l - 1, p);
-        sum_wc += wk * ck;
-        sum_w += wk;
+        if (in_grid(p, P.grid)) ck = pyr_sample_level(P, l - 1, p);
+        sum_wc += sm_w[k] * ck;
       }
     }
   }

@@ -103,7 +103,7 @@ bool build_shadow_table(const cvr_ext_params* p, const float fwd[3], float3 spac
 namespace cvr {
 namespace ctxutil {
 
-cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
+cvr_status render_volume_view(cvr_ctx* c, VolumeView* out, bool allow_tex) {
   VolumeView v = volume_view(c);
   // the quad copy is indexed with 32-bit cell numbers
   if (c->quads && (size_t)c->nx * c->ny * c->nz < kCompactMaxCells) {
@@ -130,7 +130,7 @@ cvr_status render_volume_view(cvr_ctx* c, VolumeView* out) {
     v.stride[1] = bx * v.stride[0];
     v.stride[2] = by * v.stride[1];
   }
-  if (c->sampling & CVR_SAMPLING_TEX_VOLUME) {
+  if (allow_tex && (c->sampling & CVR_SAMPLING_TEX_VOLUME)) {
     cvr_status st = ensure_volume_texture(c);
     if (st != CVR_OK) return st;
     v.tex = c->tex.vol.tex;
@@ -585,10 +585,14 @@ cvr_status cvr_build_ext_pyramid(cvr_ctx* c, const cvr_pyramid_params* p) {
   if (off >= (1LL << 31))
     return fail(c, CVR_ERR_INVALID_ARG, "cvr_build_ext_pyramid: pyramids hold fewer than 2^31 values");
   P.n_levels = levels;
-  VolumeView v = volume_view(c);
+  CK(c, cudaSetDevice(c->device));
+  // the base level's volume taps read the marchers' FP32 layout (bricks or
+  // quads; never the texture unit)
+  VolumeView v;
+  cvr_status vs = render_volume_view(c, &v, false);
+  if (vs != CVR_OK) return vs;
   P.grid = v.grid;
   P.inv_grid = f3(1.0f / v.grid.x, 1.0f / v.grid.y, 1.0f / v.grid.z);
-  CK(c, cudaSetDevice(c->device));
   CK(c, ensure(c->d_pyr, c->pyr_cap, (size_t)off * sizeof(float)));
   CK(c, launch_pyramid_build(v, c->d_rgba, c->tf_n, p->sigma0, P, c->d_pyr, c->stream));
   c->pyr = P;

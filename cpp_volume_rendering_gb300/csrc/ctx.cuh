@@ -386,7 +386,7 @@ cudaError_t launch_multiscale(int mode, int kern, float4* src, int gw, int gh, f
 size_t multiscale_scratch(int mode, int kern, int gw, int gh, int w, int h);
 // The volume as the marchers read it: the plain layout, or the bricked copy
 // of the context's brick size (made on first use after the volume changed).
-cvr_status render_volume_view(cvr_ctx* c, VolumeView* v);
+cvr_status render_volume_view(cvr_ctx* c, VolumeView* v, bool allow_tex = true);
 // Frame arguments of a render of the current volume (validated; f.step from
 // the params struct's leading step_size, f.counts null, f.stats the context's).
 cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, float* out, int w, int h,
