@@ -509,15 +509,23 @@ def tables_section(ctx, lib, wl, log=print):
     wc = scene.workload("cone")
     ctx.set_volume(wc.volume, wc.spacing)
     ctx.set_transfer_function(wc.tf)
-    times = []
-    for r in range(4):
-        abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
-        ctx.build_pyramid(**wc.pyramid)
-        abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
-        if r:
-            times.append(ms.value)
+    pyr_ms = {}
+    for label, layout in (("plain", abi.LAYOUT_PLAIN), ("quads", abi.LAYOUT_QUADS)):
+        # the base level's volume taps read the marchers' layout (same values)
+        abi.check(lib.cvr_set_volume_layout(ctx.h, layout), ctx.h)
+        times = []
+        for r in range(4):
+            abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+            abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+            ctx.build_pyramid(**wc.pyramid)
+            abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+            if r:
+                times.append(ms.value)
+        pyr_ms[label] = statistics.median(times)
+    abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
     out["pyramid"] = {"volume": list(wc.dims), "base": list(wc.pyramid["base_dims"]),
-                      "levels": wc.pyramid["n_levels"], "gpu_ms": statistics.median(times),
+                      "levels": wc.pyramid["n_levels"], "gpu_ms": min(pyr_ms.values()),
+                      "gpu_ms_by_layout": pyr_ms,
                       "note": "343 trilinear taps per output voxel per level (gen_extcoefvol_anysize / _mmlevel), "
                               "then the opacity -> extinction pass"}
     log(f"tables: SAT {m:.3f} ms GPU vs {cpu_s * 1000:.0f} ms CPU, pyramid {out['pyramid']['gpu_ms']:.3f} ms")
