@@ -50,8 +50,9 @@ __global__ void __launch_bounds__(NT, MINB) k_march_extinction_dir(FrameArgs f, 
   march_pixel(f, tf, sh);
 }
 
-template <int NT, bool TEX>
-__global__ void __launch_bounds__(NT) k_march_dos(DosArgs d, FrameArgs f) {
+// MINB: the tuner's register variant, as for the extinction marcher.
+template <int NT, int MINB, bool TEX>
+__global__ void __launch_bounds__(NT, MINB) k_march_dos(DosArgs d, FrameArgs f) {
   extern __shared__ float4 sm[];
   float4* tf = sm;
   float4* occ = sm + f.tf_n;
@@ -220,23 +221,33 @@ cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const Shadow
   return cudaGetLastError();
 }
 
-template <int NT, bool TEX>
-static cudaError_t launch_dos_t(const FrameArgs& f, const DosArgs& d, size_t sm, cudaStream_t st) {
+static cudaError_t launch_dos_k(void (*kern)(DosArgs, FrameArgs), int nt, const FrameArgs& f, const DosArgs& d,
+                                size_t sm, cudaStream_t st) {
   if (sm > 48 * 1024) {
-    cudaError_t e =
-        cudaFuncSetAttribute(k_march_dos<NT, TEX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_march_dos<NT, TEX><<<grid_of(f), NT, sm, st>>>(d, f);
+  kern<<<grid_of(f), nt, sm, st>>>(d, f);
   return cudaGetLastError();
+}
+
+template <int NT>
+static cudaError_t launch_dos_nt(const FrameArgs& f, const DosArgs& d, bool tex, size_t sm, cudaStream_t st) {
+  void (*kern)(DosArgs, FrameArgs);
+  switch (f.variant) {
+    case 1: kern = tex ? k_march_dos<NT, minb_of<NT>(1), true> : k_march_dos<NT, minb_of<NT>(1), false>; break;
+    case 2: kern = tex ? k_march_dos<NT, minb_of<NT>(2), true> : k_march_dos<NT, minb_of<NT>(2), false>; break;
+    default: kern = tex ? k_march_dos<NT, 1, true> : k_march_dos<NT, 1, false>; break;
+  }
+  return launch_dos_k(kern, NT, f, d, sm, st);
 }
 
 cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, bool tex_pyramid, cudaStream_t st) {
   size_t sm = sizeof(float4) * (f.tf_n + d.occ.n_sections + d.sdw.n_sections);
   switch (threads_of(f)) {
-    case 64: return tex_pyramid ? launch_dos_t<64, true>(f, d, sm, st) : launch_dos_t<64, false>(f, d, sm, st);
-    case 256: return tex_pyramid ? launch_dos_t<256, true>(f, d, sm, st) : launch_dos_t<256, false>(f, d, sm, st);
-    default: return tex_pyramid ? launch_dos_t<128, true>(f, d, sm, st) : launch_dos_t<128, false>(f, d, sm, st);
+    case 64: return launch_dos_nt<64>(f, d, tex_pyramid, sm, st);
+    case 256: return launch_dos_nt<256>(f, d, tex_pyramid, sm, st);
+    default: return launch_dos_nt<128>(f, d, tex_pyramid, sm, st);
   }
 }
 
