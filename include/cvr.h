@@ -360,7 +360,7 @@ int cvr_get_sampling(cvr_ctx* ctx);
 /* ---- pixel multiscaling --------------------------------------------------------
  * BaseVolumeRenderer::MULTISCALING (cppvolrend/volrenderbase.h:28-33) with
  * RenderFrameToScreen's post-passes (libs/vis_utils/renderoutputframe.cpp:
- * 265-539, shader/renderoutputframe/*.comp), run on the device after the
+ * 265-539, and the shader/renderoutputframe compute shaders), run on the device after the
  * marcher: MULTISAMPLE renders factor_w x factor_h times the output size and
  * takes a bilinear lookup per output pixel; DOWNSCALE renders at that size
  * and filters down with the kernel; UPSCALE renders at the output size divided
