@@ -232,6 +232,24 @@ __device__ __forceinline__ BoxAxis box_axis(float lo, float hi, int n) {
   b.w[0] = 1.0f - l.t; b.w[1] = 1.0f; b.w[2] = h.t;
   return b;
 }
+// The same for texel coordinates already raised to >= 0 (the taps' lower
+// clamp cannot bind).
+__device__ __forceinline__ Tap axis_tap_nonneg(float u, int n) {
+  const float fl = floorf(u);
+  const int i = int(fl);
+  Tap r;
+  r.t = u - fl;
+  r.i0 = min(i, n - 1);
+  r.i1 = min(i + 1, n - 1);
+  return r;
+}
+__device__ __forceinline__ BoxAxis box_axis_nonneg(float lo, float hi, int n) {
+  Tap l = axis_tap_nonneg(lo, n), h = axis_tap_nonneg(hi, n);
+  BoxAxis b;
+  b.s[0] = l.i0; b.s[1] = l.i1; b.s[2] = h.i0; b.s[3] = h.i1;
+  b.w[0] = 1.0f - l.t; b.w[1] = 1.0f; b.w[2] = h.t;
+  return b;
+}
 
 // int64 -> float without the FP64 pipe (where the hardware converts 64-bit
 // integers, at the FP64 rate, which is low on this part): |v| as two 32-bit
@@ -324,8 +342,8 @@ __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2)
   // quad layout's successor taps: clamp it (the interpolated value is the same).
   const float lx = fmaf(p1.x, S.inv_spacing.x, -0.5f), hx = fmaf(p2.x, S.inv_spacing.x, -0.5f);
   const float ly = fmaf(p1.y, S.inv_spacing.y, -0.5f), hy = fmaf(p2.y, S.inv_spacing.y, -0.5f);
-  BoxAxis X = COMPACT ? box_axis(fmaxf(lx, 0.0f), fmaxf(hx, 0.0f), S.sx) : box_axis(lx, hx, S.sx);
-  BoxAxis Y = COMPACT ? box_axis(fmaxf(ly, 0.0f), fmaxf(hy, 0.0f), S.sy) : box_axis(ly, hy, S.sy);
+  BoxAxis X = COMPACT ? box_axis_nonneg(fmaxf(lx, 0.0f), fmaxf(hx, 0.0f), S.sx) : box_axis(lx, hx, S.sx);
+  BoxAxis Y = COMPACT ? box_axis_nonneg(fmaxf(ly, 0.0f), fmaxf(hy, 0.0f), S.sy) : box_axis(ly, hy, S.sy);
   BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
   auto plane = [&](int z) {
     if constexpr (COMPACT) return plane_diffs_quad(sat, S, z, X, Y);
