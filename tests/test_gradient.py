@@ -88,6 +88,36 @@ def test_oracle_gradient_shading_identities():
     assert np.array_equal(off, base)
 
 
+def test_separable_sobel_sums_equal_the_27_tap_sums():
+    """The TMA builder's separable form of Sobel-Feldman (in-plane partial sums
+    D, E, Q of three planes, weights (2 >> |v1|)(2 >> |v2|)) gives the same
+    integers as the direct 27-tap sums with weights 4 >> (|v1| + |v2|)."""
+    rng = np.random.default_rng(8)
+    v = np.zeros((9, 10, 11), np.int64)
+    v[1:-1, 1:-1, 1:-1] = rng.integers(0, 65536, size=(7, 8, 9))  # 0 outside the grid
+    z, y, x = np.meshgrid(np.arange(1, 8), np.arange(1, 9), np.arange(1, 10), indexing="ij")
+    sx = np.zeros_like(z); sy = np.zeros_like(z); sz = np.zeros_like(z)
+    for v1 in (-1, 0, 1):
+        for v2 in (-1, 0, 1):
+            w = 4 >> (abs(v1) + abs(v2))
+            sz += w * (v[z - 1, y + v2, x + v1] - v[z + 1, y + v2, x + v1])
+            sy += w * (v[z + v2, y - 1, x + v1] - v[z + v2, y + 1, x + v1])
+            sx += w * (v[z + v1, y + v2, x - 1] - v[z + v1, y + v2, x + 1])
+
+    def partial(zz):  # the in-plane sums of plane zz at every (y, x)
+        row_s = lambda yy: v[zz, yy, x - 1] + 2 * v[zz, yy, x] + v[zz, yy, x + 1]
+        row_d = lambda yy: v[zz, yy, x - 1] - v[zz, yy, x + 1]
+        D = row_d(y - 1) + 2 * row_d(y) + row_d(y + 1)
+        E = row_s(y - 1) - row_s(y + 1)
+        Q = row_s(y - 1) + 2 * row_s(y) + row_s(y + 1)
+        return D, E, Q
+
+    (D0, E0, Q0), (D1, E1, Q1), (D2, E2, Q2) = partial(z - 1), partial(z), partial(z + 1)
+    assert np.array_equal(D0 + 2 * D1 + D2, sx)
+    assert np.array_equal(E0 + 2 * E1 + E2, sy)
+    assert np.array_equal(Q0 - Q2, sz)
+
+
 # ------------------------------------------------------------------ GPU
 def _gpu_vs_oracle_gradient(ctx, vol, model, n=1, filt=0, norm=True):
     ctx.set_volume(vol, (1.0, 1.0, 1.0))
