@@ -3,7 +3,7 @@
 //
 // A CPU restatement of the reference's rendering shaders and table builders,
 // templated on the arithmetic type: T = double is the FP64 oracle every GPU
-// image is judged against; T = float reproduces the shaders' single-precision
+// image is compared with; T = float reproduces the shaders' single-precision
 // arithmetic (and is the timed CPU baseline).  Texture fetches emulate OpenGL
 // texture() on normalised coordinates: texel centres at (i+0.5)/n,
 // clamp-to-edge, exact (tri)linear weights.  Not emulated: FP16 texture

@@ -111,10 +111,17 @@ def test_tf1d_reader_roundtrip(lib, tmp_path):
         scene.TransferFunction.read_tf1d(str(tmp_path / "missing.tf1d"))
 
 
-@pytest.mark.skipif(not __import__("pathlib").Path("/root/reference/data/tf1dcp/bonsai_01.tf1d").exists(),
+def _reference_fixture(rel):
+    from oracle.build_ref import reference_root
+    root = reference_root()
+    p = root / rel if root is not None else None
+    return p if p is not None and p.exists() else None
+
+
+@pytest.mark.skipif(_reference_fixture("data/tf1dcp/bonsai_01.tf1d") is None,
                     reason="reference data fixtures not present")
 def test_tf1d_reader_reads_reference_fixture(lib):
-    tf = scene.TransferFunction.read_tf1d("/root/reference/data/tf1dcp/bonsai_01.tf1d")
+    tf = scene.TransferFunction.read_tf1d(str(_reference_fixture("data/tf1dcp/bonsai_01.tf1d")))
     assert len(tf.rgb) == 5 and len(tf.alpha) == 4 and tf.max_density == 255
     rgbt, rgba = tf.tables()
     assert rgbt.shape == (256, 4)
