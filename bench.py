@@ -171,7 +171,7 @@ def profile_traffic(workload):
 def algorithmic_bytes(wl, st, abi):
     """Algorithmic bytes of one frame: 8 voxel texels per primary sample,
     plus per secondary fetch 64 four-byte SAT texels (extinction: the
-    reference's R32F table, this build's compact table), 8 float32 pyramid
+    reference's R32F table, this library's compact table), 8 float32 pyramid
     texels (cone) or 8 voxel texels (ground truth), plus the image."""
     bvox = 1 if wl.dtype == abi.CVR_U8 else 2
     if wl.method == abi.SURROGATE:  # per shaded sample: 42 pyramid taps (8 float32) + 6 volume taps

@@ -210,7 +210,7 @@ int ref_gt_vectors(int n_occ, float occ_ap, int n_sdw, float sdw_ap, unsigned se
 }
 
 // The reference's gradient texture contents (float RGB per voxel, before
-// the driver's RGB16F rounding) of a u8 (bytes 1) or u16 (bytes 2) volume.
+// the OpenGL driver's RGB16F rounding) of a u8 (bytes 1) or u16 (bytes 2) volume.
 // model: 0 Sobel-Feldman, 1 finite differences (sample size, filter,
 // normalized as given).
 int ref_gradient(const void* vox, int w, int h, int d, int bytes, int model, int sample_size, int filter,
