@@ -296,7 +296,7 @@ def tuned_frames(ctx, lib, w2):
                       key + "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9,
                       key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
                                        "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h)}})
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)}})
     ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
     return entry
 
@@ -580,7 +580,7 @@ def surrogate_section(ctx, lib, args, log=print):
                                        None), ctx.h)
             cfg = {"sampling": flags, "tile": [tw.value, th.value], "variant": tv.value,
                    "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h)}
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)}
             wl.method = method
             t = time_frames(ctx, lib, wl, wl.params, optr, 2 if method == abi.GROUND_TRUTH else 3, 1)
             if best is None or statistics.median(t) < statistics.median(best[1]):
@@ -590,6 +590,7 @@ def surrogate_section(ctx, lib, args, log=print):
         abi.check(lib.cvr_set_tuning(ctx.h, cfg["tile"][0], cfg["tile"][1], cfg["variant"]), ctx.h)
         abi.check(lib.cvr_set_brick_size(ctx.h, cfg["brick"]), ctx.h)
         abi.check(lib.cvr_set_volume_layout(ctx.h, cfg["quads"]), ctx.h)
+        abi.check(lib.cvr_set_warp_shape(ctx.h, cfg["warp_w"]), ctx.h)
         return best
     sampling_modes = (abi.SAMPLING_TEX_FEATURES, abi.SAMPLING_TEX_FEATURES | abi.SAMPLING_TEX_VOLUME)
     gt_tuning, tg = tuned(abi.GROUND_TRUTH, 256, sampling_modes)
@@ -699,7 +700,7 @@ def batch_section(ctx, lib, args, log=print):
                                                                   "surrogate": samples[abi.SURROGATE]},
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
             "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h)},
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)},
             "prepare_s": t_prep,
             "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
 
@@ -730,7 +731,7 @@ def run_ours(args):
                                C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
                                C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h),
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
               "autotune_ms": tms.value}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
@@ -803,6 +804,7 @@ def run_ours(args):
             abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
             abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
             abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+            abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)
         reset_tuning()

@@ -155,6 +155,7 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
   f.tf_n = c->tf_n;
   f.W = w; f.H = h;
   f.tile_w = c->tile_w; f.tile_h = c->tile_h;
+  f.warp_w = warp_fits(c->tile_w, c->tile_h, c->warp_w) ? c->warp_w : 8;
   f.variant = c->variant;
   f.out = reinterpret_cast<float4*>(out);
   f.counts = nullptr;
@@ -883,6 +884,16 @@ cvr_status cvr_set_tuning(cvr_ctx* c, int tile_w, int tile_h, int variant) {
   return CVR_OK;
 }
 
+cvr_status cvr_set_warp_shape(cvr_ctx* c, int warp_w) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (warp_w != 4 && warp_w != 8 && warp_w != 16)
+    return fail(c, CVR_ERR_INVALID_ARG, "cvr_set_warp_shape: 4, 8 or 16 pixels per warp row");
+  c->warp_w = warp_w;
+  return CVR_OK;
+}
+
+int cvr_get_warp_shape(cvr_ctx* c) { return c ? c->warp_w : 8; }
+
 cvr_status cvr_get_tuning(cvr_ctx* c, int* tile_w, int* tile_h, int* variant) {
   if (!c) return CVR_ERR_INVALID_ARG;
   if (tile_w) *tile_w = c->tile_w;
@@ -962,8 +973,8 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
                         size_t params_size, int w, int h, int reps, int* btw, int* bth, int* bv, float* bms) {
   if (!c || reps <= 0 || reps > 100) return fail(c, CVR_ERR_INVALID_ARG, "cvr_autotune: bad arguments");
   // ray tiles from 8x8 to 32x8 (2, 4 and 8 warps) x register variants, then
-  // the volume's layout at the best of those (plain, bricks of 8^3, 16^3,
-  // 32^3, x-y quads; -1 stands for the quads)
+  // the warp shape and the volume's layout at the best of those (plain,
+  // bricks of 8^3, 16^3, 32^3, x-y quads; -1 stands for the quads)
   static const int tiles[6][2] = {{8, 8}, {16, 8}, {32, 4}, {8, 16}, {32, 8}, {16, 16}};
   static const int bricks[5] = {0, 3, 4, 5, -1};
   float* frame = nullptr;
@@ -971,10 +982,12 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   if (s != CVR_OK) return s;
   const int keep_w = c->tile_w, keep_h = c->tile_h, keep_v = c->variant, keep_b = c->brick_bs;
   const bool keep_q = c->quads;
+  const int keep_ww = c->warp_w;
   float best = 1e30f;
   int bw = keep_w, bh = keep_h, bvar = keep_v, bb = 0;
   c->brick_bs = 0;
   c->quads = false;
+  c->warp_w = 8;
   for (int t = 0; t < 6 && s == CVR_OK; ++t) {
     for (int v = 0; v < 3 && s == CVR_OK; ++v) {
       c->tile_w = tiles[t][0]; c->tile_h = tiles[t][1]; c->variant = v;
@@ -987,6 +1000,19 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
     }
   }
   c->tile_w = bw; c->tile_h = bh; c->variant = bvar;
+  // warp shapes of 4x8 and 16x2 pixels at that tile
+  int bww = 8;
+  for (int ww : {4, 16}) {
+    if (s != CVR_OK || !warp_fits(bw, bh, ww)) continue;
+    c->warp_w = ww;
+    float ms = 0.0f;
+    s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
+    if (s == CVR_OK && ms < best) {
+      best = ms;
+      bww = ww;
+    }
+  }
+  c->warp_w = bww;
   for (int k = 1; k < 5 && s == CVR_OK; ++k) {
     c->brick_bs = bricks[k] > 0 ? bricks[k] : 0;
     c->quads = bricks[k] < 0;
@@ -999,6 +1025,7 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   }
   if (s != CVR_OK) {
     c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b; c->quads = keep_q;
+    c->warp_w = keep_ww;
     return s;
   }
   c->brick_bs = bb > 0 ? bb : 0;

@@ -213,6 +213,7 @@ struct cvr_ctx {
   size_t flush_bytes = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int tile_w = 16, tile_h = 8, variant = 0;
+  int warp_w = 8;                            // cvr_set_warp_shape (used where the tile holds whole warps)
   std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
   std::unique_ptr<MlpState> mlp;             // surrogate network (created by cvr_mlp_init)
   std::unique_ptr<SurState> sur;             // surrogate shading points
@@ -289,6 +290,11 @@ namespace cvr {
 namespace ctxutil {
 
 extern thread_local std::string g_create_err;
+
+// A tile holds whole warps of warp_w x (32 / warp_w) pixels.
+inline bool warp_fits(int tile_w, int tile_h, int warp_w) {
+  return (warp_w == 4 || warp_w == 8 || warp_w == 16) && tile_w % warp_w == 0 && tile_h % (32 / warp_w) == 0;
+}
 
 inline bool finite3(const float* p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 

@@ -137,9 +137,10 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
       __syncthreads();
     }
     const unsigned local = b - J.first_block;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps_x = J.f.tile_w >> 3;
-    const int px = (int)(local % J.blocks_x) * J.f.tile_w + (warp % warps_x) * 8 + (lane & 7);
-    const int py = (int)(local / J.blocks_x) * J.f.tile_h + (warp / warps_x) * 4 + (lane >> 3);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wl = warp_shift(J.f.warp_w);
+    const int warps_x = J.f.tile_w >> wl;
+    const int px = (int)(local % J.blocks_x) * J.f.tile_w + (warp % warps_x) * (1 << wl) + (lane & ((1 << wl) - 1));
+    const int py = (int)(local / J.blocks_x) * J.f.tile_h + (warp / warps_x) * (32 >> wl) + (lane >> wl);
     ExtShadeT<C> sh{&J.e};
     if (J.tn > 0) {
       sh.tlo = sm_bt + J.f.tf_n; sh.thi = sm_bt + J.f.tf_n + J.tn; sh.tn = J.tn; sh.tax = J.tax;

@@ -33,6 +33,7 @@ struct FrameArgs {
   float step;            // StepSize
   int W, H;
   int tile_w, tile_h;    // pixels per CTA: (tile_w/8) x (tile_h/4) warps of 8x4 pixels (2, 4 or 8 warps)
+  int warp_w;            // pixels per warp row: 4, 8 or 16 (warps of warp_w x 32/warp_w; other values: 8)
   int variant;           // register / occupancy variant of the kernel (0, 1, 2)
   float4* out;
   uint32_t* counts;                // per-pixel step count, nullable

@@ -569,11 +569,14 @@ struct GtShade {
 };
 
 // ============================================================ primary loop
+// The warp's log2 width in pixels (warps of 4x8, 8x4 or 16x2 pixels).
+__device__ __forceinline__ int warp_shift(int warp_w) { return warp_w == 4 ? 2 : (warp_w == 16 ? 4 : 3); }
+
 __device__ __forceinline__ void pixel_of(const FrameArgs& f, int& px, int& py) {
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int warps_x = f.tile_w >> 3;
-  px = blockIdx.x * f.tile_w + (warp % warps_x) * 8 + (lane & 7);
-  py = blockIdx.y * f.tile_h + (warp / warps_x) * 4 + (lane >> 3);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, wl = warp_shift(f.warp_w);
+  const int warps_x = f.tile_w >> wl;
+  px = blockIdx.x * f.tile_w + (warp % warps_x) * (1 << wl) + (lane & ((1 << wl) - 1));
+  py = blockIdx.y * f.tile_h + (warp / warps_x) * (32 >> wl) + (lane >> wl);
 }
 
 __device__ __forceinline__ void add_stats(const FrameArgs& f, unsigned int n, unsigned int shaded, unsigned int aux) {

@@ -299,6 +299,12 @@ int cvr_get_brick_size(cvr_ctx* ctx);
  * volume's bytes, 16 bytes per pyramid value), so a trilinear sample is two
  * loads instead of eight; results are bit-identical to the plain layout.
  * It takes precedence over bricks; the autotuner tries it with them. */
+/* Warp shape of the marchers' pixel tiles (no reference counterpart): 4, 8
+ * (default) or 16 pixels per warp row (warps of 4x8, 8x4 or 16x2 pixels),
+ * used where the tile holds whole warps of that shape (8x4 otherwise); same
+ * images.  The autotuner tries 4 and 16 at its best tile. */
+cvr_status cvr_set_warp_shape(cvr_ctx* ctx, int warp_w);
+int cvr_get_warp_shape(cvr_ctx* ctx);
 #define CVR_LAYOUT_PLAIN 0
 #define CVR_LAYOUT_QUADS 1
 cvr_status cvr_set_volume_layout(cvr_ctx* ctx, int layout);
@@ -328,10 +334,11 @@ cvr_status cvr_set_light_cache(cvr_ctx* ctx, int w, int h, int d);
 /* The last frame's cache: (occlusion, shadow) per cell, x fastest; synchronous. */
 cvr_status cvr_download_light_cache(cvr_ctx* ctx, float* host_out, size_t n_floats);
 /* Autotuner: renders the given frame with every tile shape x register variant
- * (reps timed frames each, CUDA events, L2 flushed before each), then every
- * brick size and the quad layout at the best of those; keeps the fastest
- * configuration on the context and reports it (cvr_get_brick_size and
- * cvr_get_volume_layout report the layout).  best_ms may be NULL. */
+ * (reps timed frames each, CUDA events, L2 flushed before each), then the
+ * 4x8 and 16x2 warp shapes, every brick size and the quad layout at the best
+ * of those; keeps the fastest configuration on the context and reports it
+ * (cvr_get_warp_shape, cvr_get_brick_size and cvr_get_volume_layout report
+ * the rest).  best_ms may be NULL. */
 cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
                         const void* params, size_t params_size, int w, int h, int reps,
                         int* best_tile_w, int* best_tile_h, int* best_variant, float* best_ms);

@@ -46,15 +46,18 @@ def test_volume_slots_keep_their_tables(ctx):
                                                          (0, (16, 8), 0, 0),
                                                          (abi.SAMPLING_TEX_FEATURES, (32, 8), 1, 8),
                                                          (abi.SAMPLING_TEX_FEATURES, (8, 8), 2, 16),
-                                                         (abi.SAMPLING_TEX_FEATURES, (16, 8), 0, -1)])
+                                                         (abi.SAMPLING_TEX_FEATURES, (16, 8), 0, -1),
+                                                         (abi.SAMPLING_TEX_FEATURES, (32, 8), 1, -16)])
 def test_batch_equals_single_renders(ctx, sampling, tile, variant, brick):
-    """brick -1: the x-y quad volume layout."""
+    """brick -1: the x-y quad volume layout; -16: that layout with warps of
+    16x2 pixels."""
     # batches read the int64 SAT; the single renders compared with them do too
     abi.check(ctx.lib.cvr_set_compact_sat(ctx.h, 0), ctx.h)
     ctx.set_sampling(sampling)
     abi.check(ctx.lib.cvr_set_tuning(ctx.h, tile[0], tile[1], variant), ctx.h)
     abi.check(ctx.lib.cvr_set_brick_size(ctx.h, max(brick, 0)), ctx.h)
     abi.check(ctx.lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_QUADS if brick < 0 else abi.LAYOUT_PLAIN), ctx.h)
+    abi.check(ctx.lib.cvr_set_warp_shape(ctx.h, 16 if brick == -16 else 8), ctx.h)
     vols = scene.batch_volumes(0.5)  # 64^3 u8, 96x128x80 u16, 128^3 u8, 192^3 u16
     scene.prepare_batch_volumes(ctx, vols)
     small_network(ctx)
@@ -102,6 +105,7 @@ def test_batch_equals_single_renders(ctx, sampling, tile, variant, brick):
         abi.check(ctx.lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
         abi.check(ctx.lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
         abi.check(ctx.lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+        abi.check(ctx.lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
         mem.close()
 
 

@@ -300,6 +300,12 @@ def test_tuning_does_not_change_results(ctx, name, n, image):
         img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
         images.append(img)
     abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+    for tw, th, ww in ((16, 8, 4), (16, 8, 16), (32, 4, 16), (8, 16, 4)):
+        abi.check(lib.cvr_set_tuning(ctx.h, tw, th, 0), ctx.h)
+        abi.check(lib.cvr_set_warp_shape(ctx.h, ww), ctx.h)
+        img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+        images.append(img)
+    abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
     abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
     for im in images[1:]:
         assert np.array_equal(im, images[0])
@@ -307,6 +313,7 @@ def test_tuning_does_not_change_results(ctx, name, n, image):
     assert lib.cvr_set_tuning(ctx.h, 12, 8, 0) == abi.CVR_ERR_INVALID_ARG  # not whole warps
     assert lib.cvr_set_brick_size(ctx.h, 12) == abi.CVR_ERR_INVALID_ARG
     assert lib.cvr_set_volume_layout(ctx.h, 2) == abi.CVR_ERR_INVALID_ARG
+    assert lib.cvr_set_warp_shape(ctx.h, 32) == abi.CVR_ERR_INVALID_ARG
 
 
 def test_autotune_picks_a_valid_configuration(ctx):
@@ -322,10 +329,12 @@ def test_autotune_picks_a_valid_configuration(ctx):
     assert (tw.value, th.value) in TILES and v.value in (0, 1, 2) and ms.value > 0
     assert lib.cvr_get_brick_size(ctx.h) in (0, 8, 16, 32)
     assert lib.cvr_get_volume_layout(ctx.h) in (abi.LAYOUT_PLAIN, abi.LAYOUT_QUADS)
+    assert lib.cvr_get_warp_shape(ctx.h) in (4, 8, 16)
     img, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
     abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
     abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
     abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
+    abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
     ref, _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
     assert np.array_equal(img, ref)
 
