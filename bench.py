@@ -60,8 +60,8 @@ GRADIENT_BUILDERS = {1: "k_gradient_tiled", 2: "k_gradient", 3: "k_gradient_tma"
 ROOFLINE_NOTES = {
     "extinction": "algorithmic gather bytes (8 voxel texels per primary step + 64 four-byte SAT texels per box "
                   "query + image); the SAT and volume are L2-resident, so the effective gather rate can exceed the "
-                  "HBM line; ncu shows the marcher bound by L1 throughput (83 %) with the integer pipe close behind "
-                  "(61 %), DRAM traffic about 1/2700 of the gathered bytes",
+                  "HBM line; ncu shows the marcher bound by L1 throughput (88 % with 8x4-pixel warps, 73 % with 4x8) "
+                  "with the integer pipe next (54-57 %), DRAM traffic about 1/2700 of the gathered bytes",
     "plain_large": "algorithmic gather bytes (8 voxel texels per primary step + image); ncu shows the marcher "
                    "instruction-issue bound (81 % issue active) with the gathers hitting L1 (91 %)",
 }
