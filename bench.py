@@ -12,13 +12,21 @@ and a directional SAT cone shadow, step 0.5 voxel.  A step is one frame.
            volume is copied from pinned host memory (cvr_set_volume), the SAT
            is rebuilt (cvr_build_sat) and the frame is rendered and read back
            (cvr_render_host) — the Init() + Redraw() + readback sequence.
-  roofline: algorithmic gather bytes of the marcher per launch / kernel time
-           against the measured HBM copy bandwidth.
+  roofline: the marcher is bound by the L1 load path (its volume and SAT
+           quads are cache-resident): the bytes its 16-byte gathers request
+           per launch / kernel time, against the L1 hit bandwidth of the same
+           load instruction measured in this run (cvr_measure_l1_bandwidth);
+           its DRAM traffic (ncu) against the measured HBM copy bandwidth is
+           reported beside it.
   cpu_baseline: the FP32 CPU oracle (a restatement of the reference shaders)
            on all host cores over a band of rows of the same frame.
 
+Output: one JSON line per section (renderers, surrogate, batch, gradient,
+post-passes, tables) as each finishes, then the headline line LAST.
+
 --impl reference times that CPU restatement alone (the reference's own GLSL
-path needs OpenGL, which neither machine has).
+path needs OpenGL, which neither machine has); it builds its workload with
+the oracle's own generators and tables and never loads libcvr.so.
 With torchrun (N > 1) every rank renders its own frame on its own GPU
 (replicas; the path needs no exchange), timing is the max over ranks.
 """
@@ -212,7 +220,8 @@ def run_reference(args):
     from cpp_volume_rendering_gb300 import scene
     import oracle
     oracle.build()
-    wl = scene.workload(args.workload, n=args.size, image=args.image)
+    # the same workload, volume and tables built by the oracle alone
+    wl = scene.workload(args.workload, n=args.size, image=args.image, gen=oracle.GEN)
     threads = os.cpu_count() or 1
     orc = oracle.Oracle()
     oracle.prepare(orc, wl)
@@ -239,6 +248,9 @@ def run_reference(args):
         tot_n += n
     value = tot_n / tot_t / 1e6
     sample = f"rows {y0}..{y0 + rows} of the {wl.width}x{H} frame per step, FP32 oracle on {threads} threads"
+    libs = mapped_repo_libraries()
+    if any("libcvr" in l for l in libs):
+        raise RuntimeError(f"the reference arm loaded the product library: {libs}")
     print(json.dumps({
         "impl": "reference", "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
@@ -246,8 +258,28 @@ def run_reference(args):
         "config": {"workload": WORKLOAD_DESC[args.workload], "image": [wl.width, wl.height], "volume": list(wl.dims)},
         "cpu_baseline": {"value": value, "unit": "Msamples/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "the reference renders with GLSL compute shaders (OpenGL); no graphics stack exists on this box, "
-                "so its CPU-side restatement (the oracle) is what is timed"}))
+        "native_libraries": libs,
+        "note": "the reference renders with GLSL compute shaders (OpenGL), unavailable on this box; its CPU "
+                "restatement (the oracle, with its own tables and volume generator) is what is timed"}), flush=True)
+
+
+def mapped_repo_libraries():
+    """Shared libraries of this repository mapped into the process."""
+    out = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(str(ROOT)) and ".so" in path:
+                    out.add(os.path.relpath(path, ROOT))
+    except OSError:
+        pass
+    return sorted(out)
+
+
+def emit(section, obj):
+    """One JSON line per benchmark section (the headline line comes last)."""
+    print(json.dumps({"section": section, **obj}), flush=True)
 
 
 def time_frames(ctx, lib, wl, params, out_ptr, steps, warmup, flush=True):
@@ -731,12 +763,14 @@ def run_ours(args):
                                C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
                                C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
-              "autotune_ms": tms.value}
+              "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),
                              out_ptr, wl.width, wl.height, None, C.byref(st)), ctx.h)
+    # the roofline's denominator: L1 hit bandwidth of the marchers' 16-byte loads
+    l1 = C.c_float()
+    abi.check(lib.cvr_measure_l1_bandwidth(ctx.h, C.byref(l1)), ctx.h)
     barrier_max([0.0], ws)
     with ClockSampler(local) as clk:
         times = time_frames(ctx, lib, wl, params, out_ptr, args.steps, args.warmup)
@@ -750,17 +784,17 @@ def run_ours(args):
     alg = algorithmic_bytes(wl, st, abi)
     med_ms = statistics.median(times)
     achieved = alg / (med_ms / 1000.0) / 1e9
-    peak, peak_src = measured_peak_hbm()
+    peak_hbm, peak_src = measured_peak_hbm()
     traffic, traffic_src = profile_traffic(args.workload)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
-                "algorithmic_bytes_per_launch": alg, "kernel_ms_median": med_ms,
-                "note": ROOFLINE_NOTES.get(args.workload, "algorithmic gather bytes (8 voxel texels per primary "
-                                           "step + the method's light-path texels + image); the volume and tables "
-                                           "are cache-resident, so the effective gather rate can exceed the HBM "
-                                           "line")}
-    if traffic_src:
-        roofline["traffic_source"] = f"profiles/{traffic_src}"
+    roofline = {"bound": "l1", "achieved": round(achieved, 1), "peak": round(l1.value, 1), "unit": "GB/s",
+                "frac": round(achieved / l1.value, 4), "traffic": traffic,
+                "peak_source": "measured in this run: cvr_measure_l1_bandwidth (coalesced 16-byte L1 hits)",
+                "bytes_per_launch": alg, "kernel_ms": round(med_ms, 4)}
+    if traffic:
+        roofline["hbm"] = {"achieved": round(traffic / (med_ms / 1000.0) / 1e9, 2), "peak": peak_hbm,
+                           "frac": round(traffic / (med_ms / 1000.0) / 1e9 / peak_hbm, 5),
+                           "peak_source": f"{peak_src} MEASURED_PEAKS.json hbm_gbs",
+                           "traffic_source": f"profiles/{traffic_src}"}
     # end to end through the C ABI with host buffers
     vol = wl.volume
     nbytes = vol.nbytes
@@ -772,7 +806,6 @@ def run_ours(args):
     ext = wl.tf.ext_per_value(wl.dtype)
     d, h, w = vol.shape
     e2e_times = []
-    est = abi.FrameStats()
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
         abi.check(lib.cvr_set_volume(ctx.h, pinned, w, h, d, wl.dtype, *wl.spacing), ctx.h)
@@ -788,16 +821,15 @@ def run_ours(args):
     lib.cvr_host_free_pinned(pinned)
     lib.cvr_host_free_pinned(img_pinned)
     e2e_total, = barrier_max([sum(e2e_times)], ws)
-    e2e = {"value": samples_all / e2e_total / 1e6, "unit": "Msamples/s", "h2d_bytes_per_step": int(nbytes + (ext.nbytes if wl.method == abi.EXTINCTION else 0)),
+    e2e = {"value": samples_all / e2e_total / 1e6, "unit": "Msamples/s",
+           "h2d_bytes_per_step": int(nbytes + (ext.nbytes if wl.method == abi.EXTINCTION else 0)),
            "d2h_bytes_per_step": int(wl.width * wl.height * 16),
-           "ms_per_step": 1000.0 * e2e_total / args.steps,
-           "includes": "cvr_set_volume from pinned host memory + the method's table build (SAT or pyramid) + "
+           "ms_per_step": round(1000.0 * e2e_total / args.steps, 3),
+           "includes": "cvr_set_volume from pinned host memory + the table build (SAT or pyramid) + "
                        "cvr_render_host readback"}
-    renderers = {}
-    batch = None
-    gradient = None
-    postpass = None
-    tables = None
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, target_s=args.cpu_seconds)
     if not args.quick:
         def reset_tuning():
             ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
@@ -805,11 +837,16 @@ def run_ours(args):
             abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
             abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
             abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
+        emit_here = rank == 0
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)
+        if surrogate is not None and emit_here:
+            emit("surrogate", surrogate)
         reset_tuning()
         if not args.no_batch:
             batch = batch_section(ctx, lib, args)
+            if emit_here:
+                emit("batch", batch)
         reset_tuning()
         # every renderer tuned on its own frame (tile x registers x brick), with
         # FP32 volume samples and with the texture-unit variant
@@ -820,37 +857,44 @@ def run_ours(args):
             scene.prepare(ctx, w2)
             abi.check(lib.cvr_set_light_cache(ctx.h, *((32, 32, 32) if name == "extinction_lightcache" else (0, 0, 0))),
                       ctx.h)
-            renderers[name] = {"workload": WORKLOAD_DESC[name], **tuned_frames(ctx, lib, w2)}
+            r = {"workload": WORKLOAD_DESC[name], **tuned_frames(ctx, lib, w2)}
             abi.check(lib.cvr_set_light_cache(ctx.h, 0, 0, 0), ctx.h)
             if rank == 0 and not args.no_cpu_baseline and name != "extinction_lightcache":
                 # the FP32 oracle on the host cores, a few seconds of rows of the same frame
-                renderers[name]["cpu_baseline"] = cpu_baseline(w2, target_s=args.cpu_seconds / 3.0)
+                r["cpu_baseline"] = cpu_baseline(w2, target_s=args.cpu_seconds / 3.0)
+            if emit_here:
+                emit(f"renderer {name}", r)
         reset_tuning()
         if not args.no_gradient:
-            gradient = gradient_section(ctx, lib, args)
+            g = gradient_section(ctx, lib, args)
+            if emit_here:
+                emit("gradient", g)
         reset_tuning()
         if not args.no_postpass:
-            postpass = postpass_section(ctx, lib, args)
+            pp = postpass_section(ctx, lib, args)
+            if emit_here:
+                emit("postpass", pp)
         reset_tuning()
-        tables = tables_section(ctx, lib, wl)
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(wl, target_s=args.cpu_seconds)
+        t = tables_section(ctx, lib, wl)
+        if emit_here:
+            emit("tables", t)
     ctx.close()
     if rank != 0:
         return
+    # the headline: the LAST stdout line, compact
+    if cpu is not None:
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps({
-        "metric": "Msamples/s", "value": value, "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "metric": "Msamples/s", "value": round(value, 2), "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded value noise / Gaussian blobs)",
         "config": {"workload": WORKLOAD_DESC[args.workload], "image": [wl.width, wl.height],
-                   "volume": list(wl.dims), "l2": "flushed between timed steps (cvr_flush_l2, outside the events)",
+                   "volume": list(wl.dims), "l2": "flushed between timed steps (outside the events)",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU", "tuning": tuning},
-        "fps": 1000.0 / ms_per_step,
-        "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "aux_fetches": st.aux_fetches},
+        "fps": round(1000.0 / ms_per_step, 2),
+        "frame": {"samples": st.samples, "shaded_samples": st.shaded_samples, "box_queries": st.aux_fetches},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": args.steps,
-        "clocks": clocks, "renderers": renderers, "surrogate": surrogate, "batch": batch,
-        "gradient": gradient, "postpass": postpass, "tables": tables}))
+        "clocks": clocks}), flush=True)
 
 
 def main():

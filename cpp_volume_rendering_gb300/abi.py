@@ -164,6 +164,7 @@ SIGNATURES = {
     "cvr_timer_start": (_I, [_P]),
     "cvr_timer_stop": (_I, [_P, _FP]),
     "cvr_flush_l2": (_I, [_P]),
+    "cvr_measure_l1_bandwidth": (_I, [_P, _FP]),
     "cvr_tf_build_linear": (_I, [_I, _I, _D, _I, _D, _I, _FP, _FP]),
     "cvr_tf_ext_per_value": (_I, [_I, _I, _D, _I, _D, _I, _I, _D]),
     "cvr_read_tf1d": (_I, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), _D, _I,
@@ -185,6 +186,7 @@ SIGNATURES = {
     "cvr_mlp_training_size": (_I, [_P]),
     "cvr_mlp_train": (_I, [_P, _I, _I, _F, C.c_uint64, _FP]),
     "cvr_mlp_gradients_noalloc": (_I, [_P, _P, _P, _I, _P, _P]),
+    "cvr_mlp_check": (_I, [_P]),
     "cvr_select_volume": (_I, [_P, _I]),
     "cvr_current_volume": (_I, [_P]),
     "cvr_batch_create": (_I, [_P, C.POINTER(Job), _I, C.POINTER(_P)]),

@@ -426,7 +426,7 @@ void cvr_destroy(cvr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
-                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
+                  c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_probe, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
                   c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq};
   for (void* p : bufs)
     if (p) cudaFree(p);

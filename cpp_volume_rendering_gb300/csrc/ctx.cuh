@@ -211,6 +211,8 @@ struct cvr_ctx {
   size_t out_cap = 0;
   void* d_flush = nullptr;
   size_t flush_bytes = 0;
+  void* d_probe = nullptr;  // cvr_measure_l1_bandwidth's buffer
+  size_t probe_cap = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int tile_w = 16, tile_h = 8, variant = 0;
   int warp_w = 8;                            // cvr_set_warp_shape (used where the tile holds whole warps)

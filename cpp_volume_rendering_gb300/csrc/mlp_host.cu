@@ -155,6 +155,13 @@ cvr_status cvr_mlp_forward(cvr_ctx* c, const float* x, int n, float* y) {
   return check_err(c);
 }
 
+cvr_status cvr_mlp_check(cvr_ctx* c) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  if (!c->mlp) return CVR_OK;
+  CK(c, cudaSetDevice(c->device));
+  return check_err(c);
+}
+
 cvr_status cvr_mlp_gradients(cvr_ctx* c, const float* x, const float* t, int n, float* grad, float* loss) {
   cvr_status st = need_mlp(c);
   if (st != CVR_OK) return st;

@@ -3,8 +3,12 @@
 * TransferFunction: control points -> the RGBt / RGBA tables and the per-voxel
   extinction (host code of the library, restating TransferFunction1D).
 * Context: a cvr_ctx (device state of one renderer: volume, tables, frames).
-* configuration(): the five seeded synthetic workloads (volume, transfer
-  function, camera, light, method parameters).
+* workload(): the seeded synthetic workloads (volume, transfer function,
+  camera, light, method parameters, and the specifications of the cone and
+  kernel-vector tables).  The volume generator and the table builders come
+  from a `gen` object: by default this library's (LIB_GEN); any object with
+  the same five methods can stand in, so a caller that must not load the
+  library (a CPU reference) builds the same workload from its own code.
 
 World units follow the reference: a volume of dims N and spacing s spans
 [-N*s/2, N*s/2].  The plain-casting workload uses the unit cube (s = 1/64);
@@ -102,6 +106,16 @@ def gt_vectors(n_occ, occ_aperture, n_sdw, sdw_aperture, seed=1):
                                            abi.fptr(sdw)))
     return occ[:n_occ].copy(), sdw[:n_sdw].copy()
 
+
+class LibGen:
+    """The library's volume generators and table builders (the default `gen`)."""
+    synth_blobs = staticmethod(lambda *a, **k: synth_blobs(*a, **k))
+    synth_value_noise = staticmethod(lambda *a, **k: synth_value_noise(*a, **k))
+    cone_table = staticmethod(lambda *a, **k: cone_table(*a, **k))
+    gt_vectors = staticmethod(lambda *a, **k: gt_vectors(*a, **k))
+
+
+LIB_GEN = LibGen()
 
 # ---------------------------------------------------------------- camera / light
 
@@ -402,6 +416,10 @@ class Workload:
     pyramid: dict = field(default_factory=dict)
     cones: tuple = ()
     gt: tuple = ()
+    # the arguments the cone tables (occlusion, shadow) and the kernel vectors
+    # were built from: cone_table(*spec) / gt_vectors(*spec)
+    cone_spec: tuple = ()
+    gt_spec: tuple = ()
 
     @property
     def dims(self):
@@ -419,7 +437,7 @@ class Workload:
         return abi.CVR_U8 if self.volume.dtype == np.uint8 else abi.CVR_U16
 
 
-def workload(name: str, n: int | None = None, image: int | None = None) -> Workload:
+def workload(name: str, n: int | None = None, image: int | None = None, gen=None) -> Workload:
     """The seeded synthetic workloads.  n / image shrink the volume side and
     image side for fast parity tests (same generator, same parameters).
 
@@ -435,11 +453,13 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     surrogate  : held-out 512^3 u8 of the same blob generator (seed 4020), the
                  ground-truth camera, light and integrator parameters, network
                  inputs on a 6-level pyramid of base n/2, 1024^2
+    gen        : volume generators and table builders (default: this library's)
     """
+    gen = gen or LIB_GEN
     if name in ("plain", "plain_large"):
         n = n or (64 if name == "plain" else 256)
         image = image or (256 if name == "plain" else 1024)
-        vol = synth_blobs(n, n, n, abi.CVR_U8, 8, seed=1000)
+        vol = gen.synth_blobs(n, n, n, abi.CVR_U8, 8, seed=1000)
         sp = (1.0 / n,) * 3
         cam = camera(orbit_eye(3.0, 35.0, 25.0), fovy=30.0)
         p = abi.PlainParams()
@@ -448,7 +468,7 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     if name == "extinction":
         n = n or 256
         image = image or 1024
-        vol = synth_value_noise(n, n, n, abi.CVR_U16, seed=2000)
+        vol = gen.synth_value_noise(n, n, n, abi.CVR_U16, seed=2000)
         sp = (1.0, 1.0, 1.0)
         cam = camera(orbit_eye(3.0 * n, 35.0, 25.0), fovy=30.0)
         fwd, up, right = light_frame((0.35, 0.8, 0.45))
@@ -459,7 +479,7 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     if name in ("ground_truth", "cone"):
         n = n or 256
         image = image or 512
-        vol = synth_blobs(n, n, n, abi.CVR_U8, 32, seed=3000, noise_max=20.0)
+        vol = gen.synth_blobs(n, n, n, abi.CVR_U8, 32, seed=3000, noise_max=20.0)
         sp = (1.0, 1.0, 1.0)
         cam = camera(orbit_eye(3.0 * n, -30.0, 20.0), fovy=30.0)
         lpos = tuple(2.0 * n * _norm((-0.5, 1.0, 0.4)))
@@ -470,21 +490,22 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
         if name == "ground_truth":
             wl.params = gt_params(default_step(sp), diag, occ_distance=32.0, light_step=1.0, gap=1.0,
                                   shadow_type=0)
-            wl.gt = gt_vectors(16, 90.0, 1, 0.0, seed=1)
+            wl.gt_spec = (16, 90.0, 1, 0.0, 1)
+            wl.gt = gen.gt_vectors(*wl.gt_spec)
         else:
             wl.method = abi.CONE_DOS
             wl.params = dos_params(default_step(sp), apply_occ=True, apply_sdw=True, shadow_type=0)
             # RC1PConeTracingDirOcclusionShading defaults (dosrcrenderer.cpp:47-59,112-113):
             # occlusion 20 deg, packing 3, weight 0.35, 0.5*diag; shadow 0.5 deg, packing 1, weight 1, 0.75*diag.
-            wl.cones = (cone_table(20.0, 1, 0.5 * diag, 3.0, 0.35, 1.0),
-                        cone_table(0.5, 0, 0.75 * diag, 3.0, 1.0, 1.0))
+            wl.cone_spec = ((20.0, 1, 0.5 * diag, 3.0, 0.35, 1.0), (0.5, 0, 0.75 * diag, 3.0, 1.0, 1.0))
+            wl.cones = tuple(gen.cone_table(*c) for c in wl.cone_spec)
             base = max(1, n // 2)
             wl.pyramid = dict(base_dims=(base, base, base), sigma0=1.0, n_levels=5)
         return wl
     if name == "iso":
         n = n or 256
         image = image or 1024
-        vol = synth_value_noise(n, n, n, abi.CVR_U16, seed=2000)
+        vol = gen.synth_value_noise(n, n, n, abi.CVR_U16, seed=2000)
         sp = (1.0, 1.0, 1.0)
         cam = camera(orbit_eye(3.0 * n, 35.0, 25.0), fovy=30.0)
         lt = light(abi.LIGHT_POINT, position=tuple(2.0 * n * _norm((0.4, 1.0, 0.6))))
@@ -492,8 +513,8 @@ def workload(name: str, n: int | None = None, image: int | None = None) -> Workl
     if name == "surrogate":
         n = n or 512
         image = image or 1024
-        vol = synth_blobs(n, n, n, abi.CVR_U8, 32, seed=SURROGATE_SEED + SURROGATE_VOLUMES, noise_max=20.0)
-        wl = surrogate_workload(vol, image)
+        vol = gen.synth_blobs(n, n, n, abi.CVR_U8, 32, seed=SURROGATE_SEED + SURROGATE_VOLUMES, noise_max=20.0)
+        wl = surrogate_workload(vol, image, gen=gen)
         return wl
     raise KeyError(name)
 
@@ -528,10 +549,11 @@ SURROGATE_VOLUMES = 20
 SURROGATE_SIZES = (160, 192, 224, 256, 288, 320, 352, 384, 416, 448)
 
 
-def surrogate_workload(vol: np.ndarray, image: int, spacing=(1.0, 1.0, 1.0)) -> Workload:
+def surrogate_workload(vol: np.ndarray, image: int, spacing=(1.0, 1.0, 1.0), gen=None) -> Workload:
     """Surrogate shading of a blob volume with the ground-truth workload's camera,
     point light and integrator parameters; the pyramid (base n/2, 6 levels),
     GT kernel vectors and cone tables (for the comparison) it needs."""
+    gen = gen or LIB_GEN
     d, h, w = vol.shape
     n = max(w, h, d)
     cam = camera(orbit_eye(3.0 * n, -30.0, 20.0), fovy=30.0)
@@ -541,10 +563,12 @@ def surrogate_workload(vol: np.ndarray, image: int, spacing=(1.0, 1.0, 1.0)) -> 
     wl = Workload("surrogate", abi.SURROGATE, vol, tuple(spacing), BENCH_TF, cam, lt, None, image, image)
     diag = wl.diagonal
     wl.params = gt_params(default_step(spacing), diag, occ_distance=32.0, light_step=1.0, gap=1.0, shadow_type=0)
-    wl.gt = gt_vectors(16, 90.0, 1, 0.0, seed=1)
+    wl.gt_spec = (16, 90.0, 1, 0.0, 1)
+    wl.gt = gen.gt_vectors(*wl.gt_spec)
     wl.pyramid = dict(base_dims=(max(1, w // 2), max(1, h // 2), max(1, d // 2)), sigma0=1.0,
                       n_levels=abi.SURROGATE_LEVELS)
-    wl.cones = (cone_table(20.0, 1, 0.5 * diag, 3.0, 0.35, 1.0), cone_table(0.5, 0, 0.75 * diag, 3.0, 1.0, 1.0))
+    wl.cone_spec = ((20.0, 1, 0.5 * diag, 3.0, 0.35, 1.0), (0.5, 0, 0.75 * diag, 3.0, 1.0, 1.0))
+    wl.cones = tuple(gen.cone_table(*c) for c in wl.cone_spec)
     return wl
 
 

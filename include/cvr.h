@@ -487,6 +487,11 @@ cvr_status cvr_timer_start(cvr_ctx* ctx);
 cvr_status cvr_timer_stop(cvr_ctx* ctx, float* ms);
 /* Writes a device buffer larger than L2 (flushes the L2 cache) on the stream. */
 cvr_status cvr_flush_l2(cvr_ctx* ctx);
+/* Measured L1 hit bandwidth (GB/s, whole GPU) of coalesced 16-byte
+ * non-coherent loads, the load instruction of the marchers' quad gathers: the
+ * denominator of their roofline (their tables are cache-resident).  No
+ * reference counterpart (the reference reports no roofline).  Synchronises. */
+cvr_status cvr_measure_l1_bandwidth(cvr_ctx* ctx, float* gbs);
 
 /* ---- learned occlusion / shadow surrogate ---------------------------------
  * No reference counterpart: a small MLP that stands in for the ray-traced
@@ -519,11 +524,20 @@ cvr_status cvr_mlp_gradients(cvr_ctx* ctx, const float* x, const float* t, int n
  * context on that device, so calls that overlap in time (other threads or
  * streams) race on it.  The first call on a device sets the scratch up (its
  * address, an index list written by a kernel) and synchronises the context
- * stream, so make that first call before any stream capture begins.  n above
- * CVR_MLP_NOALLOC_MAX_POINTS is an invalid argument. */
+ * stream, so make that first call before any stream capture begins; the
+ * set-up is per process and is not redone after cudaDeviceReset.  n above
+ * CVR_MLP_NOALLOC_MAX_POINTS is an invalid argument.  The call returns before
+ * its kernels run, so a tensor-core wait that gives up inside them (the
+ * kernels' bounded mbarrier waits) cannot show in its return value: it is
+ * reported by the next cvr_mlp_check (or the next synchronous network call)
+ * on the context, which reads and clears the flag. */
 #define CVR_MLP_NOALLOC_MAX_POINTS 8192
 cvr_status cvr_mlp_gradients_noalloc(cvr_ctx* ctx, const float* x_dev, const float* t_dev, int n, float* grad_dev,
                                      float* loss_dev);
+/* Synchronises the context stream and reports (then clears) a tensor-core
+ * wait that gave up in an asynchronous network call: CVR_ERR_TIMEOUT, else
+ * CVR_OK.  Allocates nothing. */
+cvr_status cvr_mlp_check(cvr_ctx* ctx);
 /* Training set from host memory (features n*48, targets n*2); n = 0 clears it. */
 cvr_status cvr_mlp_set_training_data(cvr_ctx* ctx, const float* x, const float* t, int n);
 cvr_status cvr_mlp_get_training_data(cvr_ctx* ctx, float* x, float* t, int n);

@@ -3,9 +3,14 @@ and of the reference's own table builders (oracle/_ref/libcvr_ref.so).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
 legs may use this package; the product (libcvr.so and its package) never
-imports it.  Parity status: the table builders are pinned against the
-reference's own C++ (see build_ref.py) and committed golden vectors; the
-marching loops are restatements of GLSL that cannot run on these machines.
+imports it.  The oracle never loads libcvr.so: it builds its transfer-function,
+cone and kernel-vector tables and the synthetic volumes with its own code
+(oracle_tables.cpp, exposed as GEN), and takes only the parameter structs'
+ctypes layouts from the product's header mirror (abi, which loads nothing
+until abi.load() is called).  Parity status: the table builders are pinned
+against the reference's own C++ (see build_ref.py) and committed golden
+vectors; the marching loops are restatements of GLSL that cannot run on these
+machines.
 """
 from __future__ import annotations
 
@@ -57,6 +62,12 @@ def load():
             "oracle_set_blinn_phong": (I, [P, C.POINTER(abi.BlinnPhong)]),
             "oracle_sur_features": (I, [P, I, C.POINTER(abi.Light), I, D, P, I, P, P]),
             "oracle_gt_points": (I, [P, C.POINTER(abi.Light), C.POINTER(abi.GtParams), P, I, P]),
+            "oracle_tf_tables": (I, [I, I, P, I, P, I, P, P]),
+            "oracle_tf_ext_per_value": (I, [I, I, P, I, P, I, I, P]),
+            "oracle_cone_table": (I, [C.c_float, I, C.c_float, C.c_float, C.c_float, D, C.POINTER(abi.ConeTable)]),
+            "oracle_gt_vectors": (I, [I, C.c_float, I, C.c_float, C.c_uint, P, P]),
+            "oracle_synth_blobs": (I, [P, I, I, I, I, I, C.c_uint64, C.c_float]),
+            "oracle_synth_value_noise": (I, [P, I, I, I, I, I, C.c_float, C.c_float, I, C.c_uint64]),
         }
         for k, (r, a) in sig.items():
             f = getattr(lib, k)
@@ -215,19 +226,86 @@ def sat_i64(vol, q):
     return out
 
 
+def _ck(code, what):
+    if code != 0:
+        raise RuntimeError(f"oracle {what}: error {code}")
+
+
+class Gen:
+    """The oracle's volume generators and table builders (oracle_tables.cpp):
+    the same interface as the library's scene.LIB_GEN, so scene.workload(...,
+    gen=GEN) builds a workload without loading libcvr.so."""
+
+    @staticmethod
+    def _vol(w, h, d, dtype):
+        return np.empty((d, h, w), np.uint8 if dtype == abi.CVR_U8 else np.uint16)
+
+    def synth_blobs(self, w, h, d, dtype, n_blobs, seed, noise_max=0.0):
+        out = self._vol(w, h, d, dtype)
+        _ck(load().oracle_synth_blobs(_p(out), w, h, d, dtype, n_blobs, seed, noise_max), "synth_blobs")
+        return out
+
+    def synth_value_noise(self, w, h, d, dtype, seed, octaves=4, lacunarity=2.0, gain=0.5, shells=4):
+        out = self._vol(w, h, d, dtype)
+        _ck(load().oracle_synth_value_noise(_p(out), w, h, d, dtype, octaves, lacunarity, gain, shells, seed),
+            "synth_value_noise")
+        return out
+
+    def cone_table(self, half_angle, packing, covered, initial_step, ui_weight, min_sigma):
+        t = abi.ConeTable()
+        _ck(load().oracle_cone_table(half_angle, packing, covered, initial_step, ui_weight, min_sigma, C.byref(t)),
+            "cone_table")
+        return t
+
+    def gt_vectors(self, n_occ, occ_aperture, n_sdw, sdw_aperture, seed=1):
+        occ = np.zeros((max(n_occ, 1), 3), np.float32)
+        sdw = np.zeros((max(n_sdw, 1), 3), np.float32)
+        _ck(load().oracle_gt_vectors(n_occ, occ_aperture, n_sdw, sdw_aperture, seed, _p(occ), _p(sdw)), "gt_vectors")
+        return occ[:n_occ].copy(), sdw[:n_sdw].copy()
+
+    @staticmethod
+    def _points(tf):
+        rgb = np.ascontiguousarray(np.array(tf.rgb, dtype=np.float64).reshape(-1, 4))
+        al = np.ascontiguousarray(np.array(tf.alpha, dtype=np.float64).reshape(-1, 2))
+        return rgb, al
+
+    def tf_tables(self, tf):
+        """(rgbt, rgba) tables of a scene.TransferFunction, (max_density+1) x 4 float32."""
+        rgb, al = self._points(tf)
+        n = tf.max_density + 1
+        rgbt = np.zeros((n, 4), np.float32)
+        rgba = np.zeros((n, 4), np.float32)
+        _ck(load().oracle_tf_tables(tf.max_density, len(rgb), _p(rgb), len(al), _p(al), int(tf.extinction_input),
+                                    _p(rgbt), _p(rgba)), "tf_tables")
+        return rgbt, rgba
+
+    def tf_ext_per_value(self, tf, dtype):
+        rgb, al = self._points(tf)
+        out = np.zeros(256 if dtype == abi.CVR_U8 else 65536, np.float64)
+        _ck(load().oracle_tf_ext_per_value(tf.max_density, len(rgb), _p(rgb), len(al), _p(al),
+                                           int(tf.extinction_input), dtype, _p(out)), "tf_ext_per_value")
+        return out
+
+
+GEN = Gen()
+
+
 def prepare(orc: Oracle, wl):
-    """Oracle-side Init() for a scene.Workload."""
-    rgbt, rgba = wl.tf.tables()
+    """Oracle-side Init() for a scene.Workload: every table from the oracle's
+    own builders (the workload's transfer-function points and table specs)."""
+    rgbt, rgba = GEN.tf_tables(wl.tf)
     orc.set_volume(wl.volume, wl.spacing)
     orc.set_tf(rgbt, rgba)
+    cones = tuple(GEN.cone_table(*c) for c in wl.cone_spec) if wl.cone_spec else ()
+    gt = GEN.gt_vectors(*wl.gt_spec) if wl.gt_spec else ()
     if wl.method == abi.EXTINCTION:
-        orc.build_sat(wl.tf.ext_per_value(wl.dtype))
+        orc.build_sat(GEN.tf_ext_per_value(wl.tf, wl.dtype))
     if wl.method == abi.CONE_DOS:
         orc.build_pyramid(wl.pyramid["base_dims"], wl.pyramid["sigma0"], wl.pyramid["n_levels"])
-        orc.set_cone_tables(*wl.cones)
+        orc.set_cone_tables(*cones)
     if wl.method == abi.GROUND_TRUTH:
-        orc.set_gt_kernels(*wl.gt)
+        orc.set_gt_kernels(*gt)
     if wl.method == abi.SURROGATE:
         orc.build_pyramid(wl.pyramid["base_dims"], wl.pyramid["sigma0"], wl.pyramid["n_levels"])
-        orc.set_gt_kernels(*wl.gt)
-        orc.set_cone_tables(*wl.cones)
+        orc.set_gt_kernels(*gt)
+        orc.set_cone_tables(*cones)

@@ -115,3 +115,68 @@ def test_synthetic_volumes_deterministic(lib):
     assert np.array_equal(n1, n2)
     levels = np.unique(n1)
     assert len(levels) <= 5  # 4 nested shells -> at most 5 distinct values
+
+
+# ---- the oracle's own table builders and generators (it never loads libcvr.so)
+
+
+@pytest.mark.parametrize("name", list(TFS))
+def test_oracle_tf_tables_match_reference_bit_exact(oracle_mod, name):
+    md, ext, rgb, al = TFS[name]
+    tf = scene.TransferFunction(rgb, al, md, bool(ext))
+    rgbt, rgba = oracle_mod.GEN.tf_tables(tf)
+    assert np.array_equal(rgbt, GOLD[f"tf_{name}_rgbt"])
+    assert np.array_equal(rgba, GOLD[f"tf_{name}_rgba"])
+    assert np.array_equal(oracle_mod.GEN.tf_ext_per_value(tf, abi.CVR_U8), GOLD[f"tf_{name}_ext_u8"])
+    if f"tf_{name}_ext_u16" in GOLD:
+        assert np.array_equal(oracle_mod.GEN.tf_ext_per_value(tf, abi.CVR_U16), GOLD[f"tf_{name}_ext_u16"])
+
+
+def test_oracle_cone_tables_match_reference(oracle_mod):
+    cases = {"occ_default": (20.0, 1, 0.5 * 443.40500673763256, 3.0, 1.0),
+             "sdw_default": (0.5, 0, 0.75 * 443.40500673763256, 3.0, 1.0),
+             "occ_wide7": (45.0, 2, 150.0, 3.0, 1.0),
+             "occ_small": (30.0, 2, 40.0, 2.0, 0.5)}
+    for name, (ang, pk, cov, ist, sg) in cases.items():
+        t = oracle_mod.GEN.cone_table(ang, pk, cov, ist, 1.0, sg)
+        ref = GOLD[f"cone_{name}_sections"]
+        n = t.n_sections
+        assert n == len(ref), name
+        got = np.array([[t.sections[i][k] for k in range(4)] for i in range(n)], np.float32)
+        assert np.array_equal(got, ref.astype(np.float32)), name
+        assert list(t.integration_samples) == list(GOLD[f"cone_{name}_counts"]), name
+        axes = np.array([[t.axes[i][k] for k in range(3)] for i in range(10)], np.float32)
+        assert np.array_equal(axes, GOLD[f"cone_{name}_axes"]), name
+        assert np.float32(t.ray7_adj_weight) == np.float32(GOLD[f"cone_{name}_w7"][0])
+
+
+def test_oracle_gt_kernel_vectors_match_reference(oracle_mod):
+    for name, (n_occ, a_occ, n_sdw, a_sdw, seed) in {"default": (16, 90.0, 1, 0.0, 1),
+                                                     "mixed": (24, 60.0, 8, 1.0, 5)}.items():
+        occ, sdw = oracle_mod.GEN.gt_vectors(n_occ, a_occ, n_sdw, a_sdw, seed)
+        assert np.array_equal(occ, GOLD[f"gt_{name}_occ"]), name
+        assert np.array_equal(sdw, GOLD[f"gt_{name}_sdw"]), name
+
+
+def test_oracle_generators_equal_library_generators(lib, oracle_mod):
+    """The workloads' seeded volumes: the oracle's restated generators give the
+    library's bytes, so a CPU reference can build every workload on its own."""
+    g = oracle_mod.GEN
+    for args in [(17, 13, 11, abi.CVR_U8, 8, 5, 0.0), (21, 9, 14, abi.CVR_U16, 32, 3000, 20.0),
+                 (16, 16, 16, abi.CVR_U8, 32, 4020, 20.0)]:
+        assert np.array_equal(g.synth_blobs(*args), scene.synth_blobs(*args)), args
+    for args in [(16, 16, 16, abi.CVR_U16, 1), (23, 17, 29, abi.CVR_U16, 2000), (40, 24, 32, abi.CVR_U8, 9)]:
+        assert np.array_equal(g.synth_value_noise(*args), scene.synth_value_noise(*args)), args
+
+
+def test_oracle_workload_builds_without_the_library(oracle_mod):
+    """scene.workload(..., gen=oracle.GEN) yields the same volume and tables as
+    the library's builders."""
+    for name in ("extinction", "cone", "ground_truth", "plain"):
+        a = scene.workload(name, n=20, image=16, gen=oracle_mod.GEN)
+        b = scene.workload(name, n=20, image=16)
+        assert np.array_equal(a.volume, b.volume), name
+        for ca, cb in zip(a.cones, b.cones):
+            assert bytes(ca) == bytes(cb), name
+        for ga, gb in zip(a.gt, b.gt):
+            assert np.array_equal(ga, gb), name
