@@ -27,6 +27,7 @@ struct cvr_batch {
   unsigned int* d_counters = nullptr;  // [0] extinction tiles, [1] surrogate rays
   unsigned long long* d_stats = nullptr;  // 3 per job, in the caller's job order
   bool ext_compact = false;
+  bool ext_aligned = false;  // every job: an aligned shadow table and aligned AO boxes (or AO off)
   std::vector<uint4*> sat32;              // the batch's own compact SATs, one per volume slot used
   cudaGraphExec_t graph = nullptr;
   ~cvr_batch() {
@@ -136,6 +137,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
         J.tn = table->n; J.tax = table->axis; J.tiw = table->interval; J.tvmin = table->vmin; J.tvmax = table->vmax;
         t.assign(table->lo, table->lo + table->n);
         t.insert(t.end(), table->hi, table->hi + table->n);
+        if (table->aligned) t.insert(t.end(), table->tx, table->tx + table->n);
         b->ext_max_table = std::max(b->ext_max_table, table->n);
       }
       tables.push_back(std::move(t));
@@ -204,9 +206,13 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
         CK(c, cudaMemcpy(b->d_tables + off, tables[k].data(), sizeof(float4) * tables[k].size(), cudaMemcpyHostToDevice));
         ext[k].tlo = b->d_tables + off;
         ext[k].thi = b->d_tables + off + ext[k].tn;
+        ext[k].ttx = tables[k].size() == 3 * (size_t)ext[k].tn ? b->d_tables + off + 2 * ext[k].tn : nullptr;
         off += tables[k].size();
       }
     }
+    b->ext_aligned = true;
+    for (const BatchExtJob& J : ext)
+      if (!J.ttx || !(J.e.ao_aligned || !J.e.apply_occ)) b->ext_aligned = false;
     CK(c, cudaMalloc((void**)&b->d_ext, sizeof(BatchExtJob) * ext.size()));
     CK(c, cudaMemcpy(b->d_ext, ext.data(), sizeof(BatchExtJob) * ext.size(), cudaMemcpyHostToDevice));
   }
@@ -221,7 +227,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stats, 0, sizeof(unsigned long long) * 3 * n_jobs, c->stream);
   if (e == cudaSuccess && b->n_ext)
     e = launch_batch_extinction(b->d_ext, b->n_ext, b->ext_blocks, b->d_counters, c->tf_n, b->ext_max_table,
-                                b->ext_threads, b->ext_variant, b->ext_compact, c->stream);
+                                b->ext_threads, b->ext_variant, b->ext_compact, b->ext_aligned, c->stream);
   if (e == cudaSuccess && b->n_sur)
     e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->ext_variant,
                                b->d_counters + 1, c->mlp->err, c->stream);

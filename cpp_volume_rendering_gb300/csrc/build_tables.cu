@@ -7,6 +7,8 @@
 //    extcoefvolumegenerator.cpp:230-408, gen_extcoefvol_anysize*.comp, backtotau.comp).
 #include "build_tables.cuh"
 
+#include <algorithm>
+
 namespace cvr {
 
 // ------------------------------------------------------------------ SAT
@@ -74,8 +76,157 @@ __global__ void k_sat_scan_lines(W* __restrict__ sat, int sx, int n_lines_inner,
   }
 }
 
+// ---- blocked builder: x-y prefix of every plane in shared memory, then a
+// z-scan (in place for the int64 table; fused with the quad layout for the
+// compact one).  Two passes over the table instead of three.
+
+// Pass 1: one CTA per z plane.  Chunks of R rows: a warp scans a row along x
+// (shuffles, carried across 32-cell segments) into shared memory, a thread
+// per column adds the chunk's rows to the running column sum (the y prefix of
+// the rows above), then the chunk is written out row by row (coalesced).
+// Interior cells take lut[voxel(x-1, y-1, z-1)]; the one-cell border is zero.
+constexpr int kSatPlaneThreads = 512;
 template <class W>
-static cudaError_t sat_build(const void* vox, int dtype, int nx, int ny, int nz, const W* lut, W* sat, cudaStream_t st) {
+__global__ void __launch_bounds__(kSatPlaneThreads) k_sat_planes(const void* vox, int dtype, int nx, int ny, int nz,
+                                                                  const W* __restrict__ lut, W* __restrict__ out,
+                                                                  int R) {
+  extern __shared__ __align__(16) unsigned char sm_sat[];
+  const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
+  W* chunk = reinterpret_cast<W*>(sm_sat);  // R x sx
+  W* carry = chunk + (size_t)R * sx;        // sx running column sums
+  const int z = blockIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  const bool border_plane = z == 0 || z == sz - 1;
+  W* plane = out + (size_t)z * sx * sy;
+  for (int x = threadIdx.x; x < sx; x += blockDim.x) carry[x] = 0;
+  for (int y0 = 0; y0 < sy; y0 += R) {
+    const int rows = min(R, sy - y0);
+    __syncthreads();  // the previous chunk is written out; carry initialised
+    for (int r = warp; r < rows; r += warps) {
+      const int y = y0 + r;
+      const bool border_row = border_plane || y == 0 || y == sy - 1;
+      const size_t vrow = border_row ? 0 : ((size_t)(z - 1) * ny + (y - 1)) * (size_t)nx;
+      W run = 0;
+      for (int base = 0; base < sx; base += 32) {
+        const int x = base + lane;
+        W v = 0;
+        if (!border_row && x > 0 && x < sx - 1) {
+          const unsigned q = dtype == 1 ? (unsigned)__ldg(static_cast<const uint8_t*>(vox) + vrow + (x - 1))
+                                        : (unsigned)__ldg(static_cast<const uint16_t*>(vox) + vrow + (x - 1));
+          v = __ldg(lut + q);
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const W n = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += n;
+        }
+        v += run;
+        if (x < sx) chunk[(size_t)r * sx + x] = v;
+        run = __shfl_sync(0xffffffffu, v, 31);
+      }
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < sx; x += blockDim.x) {
+      W c = carry[x];
+      for (int r = 0; r < rows; ++r) {
+        c += chunk[(size_t)r * sx + x];
+        chunk[(size_t)r * sx + x] = c;
+      }
+      carry[x] = c;
+    }
+    __syncthreads();
+    for (int r = 0; r < rows; ++r)
+      for (int x = threadIdx.x; x < sx; x += blockDim.x) plane[(size_t)(y0 + r) * sx + x] = chunk[(size_t)r * sx + x];
+  }
+}
+
+// Pass 2 (int64 table): in-place running sum along z of every (x, y) column,
+// a thread per column (coalesced along x), 16 planes loaded before they are
+// summed so that enough loads are in flight to stream at HBM rate.
+template <class W>
+__global__ void __launch_bounds__(256) k_sat_zscan(W* __restrict__ sat, long long columns, int sz) {
+  const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= columns) return;
+  W* p = sat + c;
+  W run = 0;
+  constexpr int B = 16;
+  for (int z0 = 0; z0 < sz; z0 += B) {
+    W v[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) v[k] = z0 + k < sz ? p[(size_t)(z0 + k) * columns] : W(0);
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      run += v[k];
+      if (z0 + k < sz) p[(size_t)(z0 + k) * columns] = run;
+    }
+  }
+}
+
+// Pass 2 (compact table): the z-scan of 32 x 8 columns and of their low halo
+// (x0 - 1, y0 - 1) per CTA, writing the predecessor quads of each plane
+// (S at (x-1, y-1), (x, y-1), (x-1, y), (x, y), coordinates clamped to the
+// table) from a shared-memory tile of the plane's running sums.
+constexpr int kQuadTileX = 32, kQuadTileY = 8, kQuadHaloCols = (kQuadTileX + 1) * (kQuadTileY + 1);
+constexpr int kQuadThreads = ((kQuadHaloCols + 31) / 32) * 32;
+__global__ void __launch_bounds__(kQuadThreads) k_sat_zscan_quads(const unsigned* __restrict__ P, uint4* __restrict__ out,
+                                                                  int sx, int sy, int sz) {
+  __shared__ unsigned tile[kQuadTileY + 1][kQuadTileX + 1];
+  const int x0 = blockIdx.x * kQuadTileX, y0 = blockIdx.y * kQuadTileY;
+  const int t = threadIdx.x;
+  const bool owner = t < kQuadHaloCols;
+  const int hx = t % (kQuadTileX + 1), hy = t / (kQuadTileX + 1);
+  const int gx = min(max(x0 - 1 + hx, 0), sx - 1), gy = min(max(y0 - 1 + hy, 0), sy - 1);
+  const size_t sxy = (size_t)sx * sy;
+  const unsigned* col = P + (size_t)gy * sx + gx;
+  const int lx = t % kQuadTileX, ly = t / kQuadTileX;
+  const int ox = x0 + lx, oy = y0 + ly;
+  const bool writer = t < kQuadTileX * kQuadTileY && ox < sx && oy < sy;
+  uint4* dst = out + (size_t)oy * sx + ox;
+  unsigned run = 0;
+  constexpr int B = 16;
+  for (int z0 = 0; z0 < sz; z0 += B) {
+    unsigned v[B];
+#pragma unroll
+    for (int k = 0; k < B; ++k) v[k] = (owner && z0 + k < sz) ? __ldg(col + (size_t)(z0 + k) * sxy) : 0u;
+#pragma unroll
+    for (int k = 0; k < B; ++k) {
+      if (z0 + k >= sz) break;
+      run += v[k];
+      __syncthreads();  // the previous plane's quads are read
+      if (owner) tile[hy][hx] = run;
+      __syncthreads();
+      if (writer)
+        dst[(size_t)(z0 + k) * sxy] =
+            make_uint4(tile[ly][lx], tile[ly][lx + 1], tile[ly + 1][lx], tile[ly + 1][lx + 1]);
+    }
+  }
+}
+
+// Rows per chunk of k_sat_planes for a row of sx cells of type W (0: the
+// plane does not fit shared memory; the line-scan builder below is used).
+template <class W>
+static int sat_plane_rows(int sx) {
+  const size_t budget = 200 * 1024;
+  const long long r = (long long)(budget / sizeof(W) - (size_t)sx) / sx;
+  return r >= 4 ? (int)std::min<long long>(r, 32) : 0;
+}
+
+template <class W>
+static cudaError_t sat_planes(const void* vox, int dtype, int nx, int ny, int nz, const W* lut, W* out, int R,
+                              cudaStream_t st) {
+  const int sx = nx + 2, sz = nz + 2;
+  const size_t smem = sizeof(W) * ((size_t)R * sx + sx);
+  cudaError_t e = cudaFuncSetAttribute(k_sat_planes<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  k_sat_planes<W><<<sz, kSatPlaneThreads, smem, st>>>(vox, dtype, nx, ny, nz, lut, out, R);
+  return cudaGetLastError();
+}
+
+// The previous builder (three passes: fill + x-scan, y-scan, z-scan), kept
+// for planes too wide for shared memory.
+template <class W>
+static cudaError_t sat_build_lines(const void* vox, int dtype, int nx, int ny, int nz, const W* lut, W* sat,
+                                   cudaStream_t st) {
   const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
   {
     long long rows = (long long)sy * sz;
@@ -98,12 +249,31 @@ static cudaError_t sat_build(const void* vox, int dtype, int nx, int ny, int nz,
 
 cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
                              long long* sat, cudaStream_t st) {
-  return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
+  const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
+  const int R = sat_plane_rows<long long>(sx);
+  if (R == 0) return sat_build_lines(vox, dtype, nx, ny, nz, lut, sat, st);
+  cudaError_t e = sat_planes(vox, dtype, nx, ny, nz, lut, sat, R, st);
+  if (e != cudaSuccess) return e;
+  const long long columns = (long long)sx * sy;
+  k_sat_zscan<long long><<<(unsigned)((columns + 255) / 256), 256, 0, st>>>(sat, columns, sz);
+  return cudaGetLastError();
 }
 
-cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
-                               unsigned* sat, cudaStream_t st) {
-  return sat_build(vox, dtype, nx, ny, nz, lut, sat, st);
+cudaError_t launch_sat_build_quads(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
+                                   unsigned* scratch, uint4* out, cudaStream_t st) {
+  const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
+  const int R = sat_plane_rows<unsigned>(sx);
+  cudaError_t e = R == 0 ? sat_build_lines(vox, dtype, nx, ny, nz, lut, scratch, st) : cudaSuccess;
+  if (e != cudaSuccess) return e;
+  if (R > 0) {
+    // x-y plane prefixes only: the quad pass below adds them up along z
+    e = sat_planes(vox, dtype, nx, ny, nz, lut, scratch, R, st);
+    if (e != cudaSuccess) return e;
+    dim3 grid((sx + kQuadTileX - 1) / kQuadTileX, (sy + kQuadTileY - 1) / kQuadTileY);
+    k_sat_zscan_quads<<<grid, kQuadThreads, 0, st>>>(scratch, out, sx, sy, sz);
+    return cudaGetLastError();
+  }
+  return launch_sat_quads(scratch, out, sx, sy, sz, st);  // the line builder made the whole table
 }
 
 // x-y quads of the volume: cell (x, y, z) = the voxels at (x, y), (x', y),
@@ -150,15 +320,15 @@ cudaError_t launch_pyramid_quads(const PyramidView& P, const float* data, float4
   return cudaGetLastError();
 }
 
-// x-y quads of a table: out[(x, y, z)] = s at (x, y), (x', y), (x, y'),
-// (x', y') of plane z, with x' = min(x + 1, sx - 1), y' = min(y + 1, sy - 1).
+// x-y predecessor quads of a table: out[(x, y, z)] = s at (x-1, y-1),
+// (x, y-1), (x-1, y), (x, y) of plane z, the predecessors clamped to 0.
 __global__ void k_sat_quads(const unsigned* __restrict__ s, uint4* __restrict__ out, int sx, int sy,
                             long long cells) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cells) return;
   const int x = (int)(i % sx), y = (int)((i / sx) % sy);
-  const long long dx = x + 1 < sx ? 1 : 0, dy = y + 1 < sy ? sx : 0;
-  out[i] = make_uint4(s[i], s[i + dx], s[i + dy], s[i + dy + dx]);
+  const long long dx = x > 0 ? 1 : 0, dy = y > 0 ? sx : 0;
+  out[i] = make_uint4(s[i - dy - dx], s[i - dy], s[i - dx], s[i]);
 }
 
 cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st) {

@@ -8,11 +8,12 @@ namespace cvr {
 // Builds the (nx+2)(ny+2)(nz+2) int64 SAT of lut[voxel] with a zero border.
 cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz, const long long* lut,
                              long long* sat, cudaStream_t st);
-// The same prefix sums of a 32-bit lut, wrapping modulo 2^32 (the compact table).
-cudaError_t launch_sat_build32(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
-                               unsigned* sat, cudaStream_t st);
-// The x-y quad layout of a (sx, sy, sz) table: S at (x, y), (x', y), (x, y'),
-// (x', y') per cell, x' and y' the successors clamped to the table.
+// The compact table: the same prefix sums of a 32-bit lut, wrapping modulo
+// 2^32, in the x-y predecessor-quad layout (SatView::sat32) in out;
+// scratch holds (nx+2)(ny+2)(nz+2) 32-bit values (the plane prefixes).
+cudaError_t launch_sat_build_quads(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
+                                   unsigned* scratch, uint4* out, cudaStream_t st);
+// The x-y predecessor-quad layout of a finished plain (sx, sy, sz) table.
 cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st);
 
 // Builds every level of P (dims/offsets/grid filled by the caller) into data.

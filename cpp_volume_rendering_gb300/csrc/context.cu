@@ -68,6 +68,7 @@ bool build_shadow_table(const cvr_ext_params* p, const float fwd[3], float3 spac
   const double iw = (double)p->sdw_sample_interval * signal * sc[ax];
   double mp = (double)p->sdw_initial_step * signal * sc[ax];
   int k = 0;
+  bool aligned = true;
   while ((mp / c[ax]) < (double)p->sdw_max_distance) {
     if (k == CVR_MAX_SDW_BOXES) return false;
     double mean = std::fabs(mp + iw * 0.5);
@@ -87,9 +88,22 @@ bool build_shadow_table(const cvr_ext_params* p, const float fwd[3], float3 spac
                   (std::fabs(hi[2] - lo[2]) / sc[2]);
     t->lo[k] = make_float4((float)lo[0], (float)lo[1], (float)lo[2], (float)mp);
     t->hi[k] = make_float4((float)hi[0], (float)hi[1], (float)hi[2], (float)((double)p->sdw_ui_weight / volq));
+    // integer texel widths (ceil-rounded cross-sections; the walk axis: the
+    // interval) for the compact table's equal-fraction query
+    int wpk = 0;
+    for (int a = 0; a < 3; ++a) {
+      const double wd = (hi[a] - lo[a]) / sc[a];
+      const double wr = std::nearbyint(wd);
+      if (!(std::fabs(wd - wr) <= 1e-6 * std::max(1.0, wr)) || wr < 0.0 || wr > 1023.0) aligned = false;
+      else wpk |= (int)wr << (10 * a);
+    }
+    float pk;
+    std::memcpy(&pk, &wpk, sizeof pk);
+    t->tx[k] = make_float4((float)(lo[0] / sc[0]), (float)(lo[1] / sc[1]), (float)(lo[2] / sc[2]), pk);
     mp = mp + iw;
     ++k;
   }
+  t->aligned = aligned ? 1 : 0;
   t->n = k;
   t->axis = ax;
   t->interval = (float)iw;
@@ -195,6 +209,11 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
   a.shadow_type = p->shadow_type;
   a.light_pos = make3(light->position); a.light_fwd = make3(light->forward);
   a.ka = p->ka; a.kd = p->kd;
+  a.ao_aligned = 1;
+  for (int i = 0; i < a.n_shells; ++i) {
+    const float w2 = 2.0f * p->ao_radii[i];
+    if (!(w2 >= 0.0f && w2 <= 1023.0f && w2 == std::nearbyint(w2))) a.ao_aligned = 0;
+  }
   *table = nullptr;
   if (p->apply_shadow && p->shadow_type == 1) {
     if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
@@ -298,17 +317,17 @@ bool compact_plan(const std::vector<double>& ext, double vmax, int* F_out, std::
 }
 
 // Builds the compact table of the current volume from q into dst, in x-y
-// quad layout (synchronous; the plain 32-bit table is a temporary).
+// quad layout, asynchronously on the context stream: the plane prefixes go
+// to the context's persistent scratch (grown only when a larger volume needs
+// it), and q is copied from pageable memory, which the copy call has staged
+// by the time it returns.
 cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint4* dst) {
-  const int sx = c->nx + 2, sy = c->ny + 2, sz = c->nz + 2;
+  const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
   CK(c, ensure(c->d_lut32, c->lut32_cap, sizeof(unsigned) * q.size()));
   CK(c, cudaMemcpyAsync(c->d_lut32, q.data(), sizeof(unsigned) * q.size(), cudaMemcpyHostToDevice, c->stream));
-  unsigned* plain = nullptr;
-  CK(c, cudaMalloc((void**)&plain, sizeof(unsigned) * (size_t)sx * sy * sz));
-  cudaError_t e = launch_sat_build32(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, plain, c->stream);
-  if (e == cudaSuccess) e = launch_sat_quads(plain, dst, sx, sy, sz, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);  // q is a host temporary
-  cudaFree(plain);
+  CK(c, ensure(c->d_satp, c->satp_cap, sizeof(unsigned) * cells));
+  cudaError_t e = launch_sat_build_quads(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, c->d_satp, dst,
+                                         c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "compact SAT build");
   return CVR_OK;
 }
@@ -427,7 +446,7 @@ void cvr_destroy(cvr_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
                   c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_probe, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
-                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq};
+                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq, c->d_satp};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -530,14 +549,13 @@ cvr_status cvr_build_sat(cvr_ctx* c, const double* ext, int n_values) {
   double scale = std::ldexp(1.0, F);
   for (int i = 0; i < n_values; ++i) q[i] = std::llround(ext[i] * scale);
   CK(c, cudaSetDevice(c->device));
-  size_t lut_cap = 0;
-  if (c->d_lut) { cudaFree(c->d_lut); c->d_lut = nullptr; }
-  CK(c, ensure(c->d_lut, lut_cap, sizeof(long long) * n_values));
+  // the table of every possible voxel value (65536 entries covers u8 and u16)
+  if (!c->d_lut) CK(c, cudaMalloc((void**)&c->d_lut, sizeof(long long) * 65536));
+  // pageable source: staged by the time the call returns, so q may go
   CK(c, cudaMemcpyAsync(c->d_lut, q.data(), sizeof(long long) * n_values, cudaMemcpyHostToDevice, c->stream));
   size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
   CK(c, ensure(c->d_sat, c->sat_cap, cells * sizeof(long long)));
   CK(c, launch_sat_build(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut, c->d_sat, c->stream));
-  CK(c, cudaStreamSynchronize(c->stream));  // q is a host temporary
   c->sat_frac_bits = F;
   c->sat_ready = true;
   c->sat_ext.assign(ext, ext + n_values);

@@ -187,6 +187,8 @@ struct cvr_ctx {
   size_t lut32_cap = 0;
   int sat32_F = kNoCompactSat;
   bool compact_sat = true;                   // cvr_set_compact_sat
+  unsigned* d_satp = nullptr;                // compact builds' plane-prefix scratch (any volume slot)
+  size_t satp_cap = 0;
   // pyramid, and its x-y quad copy for FP32 taps (built with the first frame that needs it)
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;

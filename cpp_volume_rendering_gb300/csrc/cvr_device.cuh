@@ -207,10 +207,14 @@ struct SatView {
   // The compact copy for frames whose boxes are all small enough: the same
   // prefix sums of round(sigma * 2^F32) modulo 2^32 (F32 chosen so that every
   // sub-box sum of the frame's boxes is below 2^31, which makes their
-  // wrapped 32-bit differences exact), stored as x-y quads: cell (x, y)
-  // holds S at (x, y), (x', y), (x, y'), (x', y') with x' = min(x + 1, sx - 1),
-  // y' = min(y + 1, sy - 1) -- the four taps of a GL_LINEAR lookup in a plane
-  // in one 16-byte load; nullptr: frames use the int64 table.
+  // wrapped 32-bit differences exact), stored as x-y "predecessor" quads:
+  // cell (x, y) holds S at (x-1, y-1), (x, y-1), (x-1, y), (x, y), each
+  // coordinate clamped to the table.  A GL_LINEAR lookup whose taps start at
+  // texel a reads the pair (S[clamp(a)], S[clamp(a+1)]) from cell
+  // clamp(a + 1): exact for every a, because S is 0 at x = 0 and y = 0 (the
+  // zero border) and repeats at the last cell, so clamping the cell equals
+  // clamping each tap.  The four taps of a plane are one 16-byte load;
+  // nullptr: frames use the int64 table.
   const uint4* sat32;
   float inv_scale32;     // 2^-F32
   int sx, sy, sz;        // SAT dims = volume dims + 2
@@ -232,22 +236,15 @@ __device__ __forceinline__ BoxAxis box_axis(float lo, float hi, int n) {
   b.w[0] = 1.0f - l.t; b.w[1] = 1.0f; b.w[2] = h.t;
   return b;
 }
-// The same for texel coordinates already raised to >= 0 (the taps' lower
-// clamp cannot bind).
-__device__ __forceinline__ Tap axis_tap_nonneg(float u, int n) {
-  const float fl = floorf(u);
-  const int i = int(fl);
-  Tap r;
-  r.t = u - fl;
-  r.i0 = min(i, n - 1);
-  r.i1 = min(i + 1, n - 1);
-  return r;
-}
-__device__ __forceinline__ BoxAxis box_axis_nonneg(float lo, float hi, int n) {
-  Tap l = axis_tap_nonneg(lo, n), h = axis_tap_nonneg(hi, n);
+// The same axis for the compact quad table: s[0] and s[2] are the quad cells
+// clamp(floor(u) + 1) holding the low and the high tap pair.
+__device__ __forceinline__ BoxAxis box_axis_quad(float lo, float hi, int n) {
+  const float fl = floorf(lo), fh = floorf(hi);
   BoxAxis b;
-  b.s[0] = l.i0; b.s[1] = l.i1; b.s[2] = h.i0; b.s[3] = h.i1;
-  b.w[0] = 1.0f - l.t; b.w[1] = 1.0f; b.w[2] = h.t;
+  b.s[0] = min(max(int(fl) + 1, 0), n - 1);
+  b.s[2] = min(max(int(fh) + 1, 0), n - 1);
+  b.s[1] = b.s[0]; b.s[3] = b.s[2];
+  b.w[0] = 1.0f - (lo - fl); b.w[1] = 1.0f; b.w[2] = hi - fh;
   return b;
 }
 
@@ -280,9 +277,9 @@ __device__ __forceinline__ D3<unsigned> x_diffs(unsigned v0, unsigned v1, unsign
 }
 template <class W>
 struct D9 { D3<W> y[3]; };  // consecutive y-differences of x-differenced rows
-// The quad table: the 16 taps of a plane from four 16-byte loads (the second
-// tap of each axis pair is the clamped successor of the first, as sat_box's
-// coordinate clamp guarantees).
+// The quad table: the 16 taps of a plane from four 16-byte loads; X.s[0] and
+// X.s[2] (Y likewise) are the quad cells of the low and high tap pairs
+// (box_axis_quad).
 __device__ __forceinline__ D9<unsigned> plane_diffs_quad(const uint4* sat, const SatView& S, int z,
                                                          const BoxAxis& X, const BoxAxis& Y) {
   // 32-bit cell numbers (the compact table has fewer than 2^31 cells)
@@ -337,13 +334,10 @@ __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2)
   using T = typename std::conditional<COMPACT, uint4, long long>::type;
   const T* sat;
   if constexpr (COMPACT) sat = S.sat32; else sat = S.sat;
-  // The clamped positions give texel coordinates in [0, s - 1]; single
-  // precision can put the lowest a hair below 0, where floor would break the
-  // quad layout's successor taps: clamp it (the interpolated value is the same).
   const float lx = fmaf(p1.x, S.inv_spacing.x, -0.5f), hx = fmaf(p2.x, S.inv_spacing.x, -0.5f);
   const float ly = fmaf(p1.y, S.inv_spacing.y, -0.5f), hy = fmaf(p2.y, S.inv_spacing.y, -0.5f);
-  BoxAxis X = COMPACT ? box_axis_nonneg(fmaxf(lx, 0.0f), fmaxf(hx, 0.0f), S.sx) : box_axis(lx, hx, S.sx);
-  BoxAxis Y = COMPACT ? box_axis_nonneg(fmaxf(ly, 0.0f), fmaxf(hy, 0.0f), S.sy) : box_axis(ly, hy, S.sy);
+  BoxAxis X = COMPACT ? box_axis_quad(lx, hx, S.sx) : box_axis(lx, hx, S.sx);
+  BoxAxis Y = COMPACT ? box_axis_quad(ly, hy, S.sy) : box_axis(ly, hy, S.sy);
   BoxAxis Z = box_axis(fmaf(p1.z, S.inv_spacing.z, -0.5f), fmaf(p2.z, S.inv_spacing.z, -0.5f), S.sz);
   auto plane = [&](int z) {
     if constexpr (COMPACT) return plane_diffs_quad(sat, S, z, X, Y);
@@ -358,6 +352,47 @@ __device__ __forceinline__ float sat_box(const SatView& S, float3 p1, float3 p2)
     prev = cur;
   }
   return acc * (COMPACT ? S.inv_scale32 : S.inv_scale);
+}
+
+// A box whose two corners sit at the same fractional texel offset on every
+// axis (integer widths w): low corner texel coordinate u, high corner u + w.
+// With equal fractions t the reference's 1-D functional
+//   (1-t) S[b0] + t S[b1] - (1-t) S[a0] - t S[a1],  b = a + w,
+// is (1-t) (S[a+w] - S[a]) + t (S[a+1+w] - S[a+1]), so the eight trilinear
+// corner fetches reduce to eight exact integer sums of boxes of width w
+// (offset by 0 or 1 cell per axis), weighted by the trilinear weights of t.
+// The 64 texels are the same; the integer work is 56 wrapped differences and
+// 8 conversions (the general query above: 165 and 27).  Coordinates need no
+// clamp: the quad cells are clamped (exact, see SatView::sat32), which equals
+// the reference's clamp of the corner positions.  Compact (quad) table only.
+__device__ __forceinline__ float sat_box_aligned(const SatView& S, float3 u, int wx, int wy, int wz) {
+  const float fx = floorf(u.x), fy = floorf(u.y), fz = floorf(u.z);
+  const float tx = u.x - fx, ty = u.y - fy, tz = u.z - fz;
+  const int ax = int(fx), ay = int(fy), az = int(fz);
+  const unsigned x0 = (unsigned)min(max(ax + 1, 0), S.sx - 1), x1 = (unsigned)min(max(ax + 1 + wx, 0), S.sx - 1);
+  const unsigned y0 = (unsigned)min(max(ay + 1, 0), S.sy - 1), y1 = (unsigned)min(max(ay + 1 + wy, 0), S.sy - 1);
+  const unsigned sx = (unsigned)S.sx;
+  // 32-bit cell numbers (the compact table has fewer than 2^31 cells)
+  const unsigned c00 = y0 * sx + x0, c01 = y0 * sx + x1, c10 = y1 * sx + x0, c11 = y1 * sx + x1;
+  const uint4* __restrict__ q = S.sat32;
+  // rectangle sums of the four (x, y) sub-boxes in plane z: component c of a
+  // quad is sub-box (c & 1, c >> 1)
+  auto rect = [&](int z) {
+    const unsigned zo = (unsigned)min(max(z, 0), S.sz - 1) * S.sxy;
+    const uint4 a = __ldg(q + (zo + c00)), b = __ldg(q + (zo + c01));
+    const uint4 c = __ldg(q + (zo + c10)), d = __ldg(q + (zo + c11));
+    return make_uint4(d.x - c.x - b.x + a.x, d.y - c.y - b.y + a.y, d.z - c.z - b.z + a.z, d.w - c.w - b.w + a.w);
+  };
+  const uint4 r0 = rect(az), r1 = rect(az + 1), r2 = rect(az + wz), r3 = rect(az + wz + 1);
+  // sub-box sums (below 2^31 by the compact table's fixed point): z-offset 0 and 1
+  const float b00 = (float)(int)(r2.x - r0.x), b10 = (float)(int)(r2.y - r0.y);
+  const float b01 = (float)(int)(r2.z - r0.z), b11 = (float)(int)(r2.w - r0.w);
+  const float e00 = (float)(int)(r3.x - r1.x), e10 = (float)(int)(r3.y - r1.y);
+  const float e01 = (float)(int)(r3.z - r1.z), e11 = (float)(int)(r3.w - r1.w);
+  const float z00 = fmaf(tz, e00 - b00, b00), z10 = fmaf(tz, e10 - b10, b10);
+  const float z01 = fmaf(tz, e01 - b01, b01), z11 = fmaf(tz, e11 - b11, b11);
+  const float y0v = fmaf(ty, z01 - z00, z00), y1v = fmaf(ty, z11 - z10, z10);
+  return fmaf(tx, y1v - y0v, y0v) * S.inv_scale32;
 }
 
 // ---------------------------------------------------------------- pyramid

@@ -31,21 +31,26 @@ __global__ void __launch_bounds__(NT, MINB) k_march_extinction(FrameArgs f, ExtA
 }
 
 // Directional light: the shadow boxes come from the per-frame table, staged
-// in shared memory after the transfer function.
-template <int NT, int MINB, bool C>
+// in shared memory after the transfer function.  A: every box (AO and
+// shadow) has integer texel widths, so every query is the compact table's
+// equal-fraction one (the host selects it; it needs C).
+template <int NT, int MINB, bool C, bool A>
 __global__ void __launch_bounds__(NT, MINB) k_march_extinction_dir(FrameArgs f, ExtArgs e,
                                                                     const __grid_constant__ ShadowBoxTable t) {
   extern __shared__ float4 sm_tf[];
   const float4* tf = stage_tf(f, sm_tf);
   float4* lo = sm_tf + f.tf_n;
   float4* hi = lo + t.n;
+  float4* tx = hi + t.n;
   for (int i = threadIdx.x; i < t.n; i += blockDim.x) {
     lo[i] = t.lo[i];
     hi[i] = t.hi[i];
+    if (A) tx[i] = t.tx[i];
   }
   __syncthreads();
-  ExtShadeT<C> sh{&e};
+  ExtShadeT<C, A> sh{&e};
   sh.tlo = lo; sh.thi = hi; sh.tn = t.n; sh.tax = t.axis;
+  if (A) sh.ttx = tx;
   sh.tiw = t.interval; sh.tvmin = t.vmin; sh.tvmax = t.vmax;
   march_pixel(f, tf, sh);
 }
@@ -97,7 +102,9 @@ cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
 // Batched extinction frames: persistent CTAs take tiles of all jobs from one
 // counter; the job descriptor, transfer function and shadow table are staged
 // in shared memory whenever a CTA moves to another job.
-template <int NT, int MINB, bool C>
+// A: every job has a shadow table and integer box widths (the equal-fraction
+// query; needs C).
+template <int NT, int MINB, bool C, bool A>
 __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob* __restrict__ jobs, int n_jobs,
                                                                 unsigned total, unsigned* counter) {
   __shared__ BatchExtJob J;
@@ -132,6 +139,7 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
       for (int i = threadIdx.x; i < J.tn; i += blockDim.x) {
         sm_bt[J.f.tf_n + i] = J.tlo[i];
         sm_bt[J.f.tf_n + J.tn + i] = J.thi[i];
+        if (A) sm_bt[J.f.tf_n + 2 * J.tn + i] = J.ttx[i];
       }
       cur = j;
       __syncthreads();
@@ -141,9 +149,10 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
     const int warps_x = J.f.tile_w >> wl;
     const int px = (int)(local % J.blocks_x) * J.f.tile_w + (warp % warps_x) * (1 << wl) + (lane & ((1 << wl) - 1));
     const int py = (int)(local / J.blocks_x) * J.f.tile_h + (warp / warps_x) * (32 >> wl) + (lane >> wl);
-    ExtShadeT<C> sh{&J.e};
+    ExtShadeT<C, A> sh{&J.e};
     if (J.tn > 0) {
       sh.tlo = sm_bt + J.f.tf_n; sh.thi = sm_bt + J.f.tf_n + J.tn; sh.tn = J.tn; sh.tax = J.tax;
+      if (A) sh.ttx = sm_bt + J.f.tf_n + 2 * J.tn;
       sh.tiw = J.tiw; sh.tvmin = J.tvmin; sh.tvmax = J.tvmax;
     }
     march_ray(J.f, sm_bt, sh, px, py);
@@ -153,8 +162,9 @@ __global__ void __launch_bounds__(NT, MINB) k_batch_extinction(const BatchExtJob
 
 template <int NT, int MINB>
 static cudaError_t launch_batch_t(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
-                                  size_t smem, bool compact, cudaStream_t st) {
-  auto kern = compact ? k_batch_extinction<NT, MINB, true> : k_batch_extinction<NT, MINB, false>;
+                                  size_t smem, bool compact, bool aligned, cudaStream_t st) {
+  auto kern = compact ? (aligned ? k_batch_extinction<NT, MINB, true, true> : k_batch_extinction<NT, MINB, true, false>)
+                      : k_batch_extinction<NT, MINB, false, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
@@ -176,13 +186,16 @@ constexpr int minb_of(int variant) {
 
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
                                     int tf_n, int max_table, int tile_threads, int variant, bool compact,
-                                    cudaStream_t st) {
-  const size_t smem = sizeof(float4) * (tf_n + 2 * max_table);
-#define CVR_BATCH(NT)                                                                                          \
-  switch (variant) {                                                                                          \
-    case 1: return launch_batch_t<NT, minb_of<NT>(1)>(jobs, n_jobs, total_blocks, counter, smem, compact, st); \
-    case 2: return launch_batch_t<NT, minb_of<NT>(2)>(jobs, n_jobs, total_blocks, counter, smem, compact, st); \
-    default: return launch_batch_t<NT, 1>(jobs, n_jobs, total_blocks, counter, smem, compact, st);           \
+                                    bool aligned, cudaStream_t st) {
+  const size_t smem = sizeof(float4) * (tf_n + 3 * max_table);
+  aligned = aligned && compact;
+#define CVR_BATCH(NT)                                                                                         \
+  switch (variant) {                                                                                         \
+    case 1:                                                                                                  \
+      return launch_batch_t<NT, minb_of<NT>(1)>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st); \
+    case 2:                                                                                                  \
+      return launch_batch_t<NT, minb_of<NT>(2)>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st); \
+    default: return launch_batch_t<NT, 1>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st);      \
   }
   if (tile_threads == 64) { CVR_BATCH(64) }
   if (tile_threads == 256) { CVR_BATCH(256) }
@@ -194,9 +207,11 @@ template <int NT, int MINB>
 static void launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
   const bool c = e.sat.sat32 != nullptr;
   if (table) {
-    size_t sm = sizeof(float4) * (f.tf_n + 2 * table->n);
-    if (c) k_march_extinction_dir<NT, MINB, true><<<grid_of(f), NT, sm, st>>>(f, e, *table);
-    else k_march_extinction_dir<NT, MINB, false><<<grid_of(f), NT, sm, st>>>(f, e, *table);
+    size_t sm = sizeof(float4) * (f.tf_n + 3 * table->n);
+    const bool a = c && table->aligned && (e.ao_aligned || !e.apply_occ);
+    if (a) k_march_extinction_dir<NT, MINB, true, true><<<grid_of(f), NT, sm, st>>>(f, e, *table);
+    else if (c) k_march_extinction_dir<NT, MINB, true, false><<<grid_of(f), NT, sm, st>>>(f, e, *table);
+    else k_march_extinction_dir<NT, MINB, false, false><<<grid_of(f), NT, sm, st>>>(f, e, *table);
   } else {
     size_t sm = sizeof(float4) * f.tf_n;
     if (c) k_march_extinction<NT, MINB, true><<<grid_of(f), NT, sm, st>>>(f, e);

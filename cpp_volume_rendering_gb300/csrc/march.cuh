@@ -50,6 +50,9 @@ struct ExtArgs {
   int shadow_type;
   float3 light_pos, light_fwd;
   float ka, kd;
+  // every AO box has integer texel widths (2 r): the compact table's
+  // equal-fraction query applies (sat_box_aligned)
+  int ao_aligned;
 };
 
 // Boxes of the SAT shadow cone of a directional light.  The cone direction is
@@ -65,6 +68,13 @@ struct ShadowBoxTable {
   float vmin, vmax;
   float4 lo[CVR_MAX_SDW_BOXES];  // xyz: low corner offset, w: position along the axis
   float4 hi[CVR_MAX_SDW_BOXES];  // xyz: high corner offset, w: UI weight / box volume in voxels
+  // Every box has integer texel widths below 1024 on all three axes (the
+  // cross-sections are rounded up to whole voxels; the walk axis has the
+  // sample interval): tx holds, per box, the low corner offset in texel units
+  // (xyz) and the widths packed as wx | wy << 10 | wz << 20 (w, as int bits),
+  // for the compact table's equal-fraction query.  0: tx is unused.
+  int aligned;
+  float4 tx[CVR_MAX_SDW_BOXES];
 };
 
 struct ConeTableDev {
@@ -134,6 +144,7 @@ struct BatchExtJob {
   ExtArgs e;
   const float4* tlo;  // directional shadow-box table in global memory, or null
   const float4* thi;
+  const float4* ttx;  // the table's texel offsets and widths (ShadowBoxTable::tx), or null
   int tn, tax;
   float tiw, tvmin, tvmax;
   unsigned first_block;  // first batch-wide tile index of the job
@@ -143,10 +154,11 @@ struct BatchExtJob {
 // Persistent launch over all tiles of all jobs (jobs ordered by first_block):
 // each CTA takes tiles from *counter (zeroed before the launch).  variant as
 // in FrameArgs; max_table = the largest shadow table of the jobs; compact:
-// every job reads its compact SAT (ExtArgs::sat.sat32).
+// every job reads its compact SAT (ExtArgs::sat.sat32); aligned: every job
+// has an aligned shadow table (ttx) and aligned AO boxes (or AO off).
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
                                     int tf_n, int max_table, int tile_threads, int variant, bool compact,
-                                    cudaStream_t st);
+                                    bool aligned, cudaStream_t st);
 
 // Object-space light cache (lightcache.cu).  Cells of dims[0] x dims[1] x
 // dims[2], x fastest, float2 (occlusion, shadow).  table: the directional

@@ -122,12 +122,18 @@ struct PlainShade {
 
 // ====================================================== extinction (rc1pextbsd)
 // COMPACT: the frame's SAT box queries read the 32-bit table (SatView::sat32).
-template <bool COMPACT = false>
+// ALIGNED (with COMPACT): every AO box and every box of the directional
+// shadow table has integer texel widths, so every query is the equal-fraction
+// one (sat_box_aligned); the kernel then always has a table (ttx set).
+template <bool COMPACT = false, bool ALIGNED = false>
 struct ExtShadeT {
+  static_assert(COMPACT || !ALIGNED, "the equal-fraction query reads the compact table");
   const ExtArgs* e;
   // Per-frame box table of a directional light (shared memory), or nullptr.
   const float4* tlo = nullptr;
   const float4* thi = nullptr;
+  // the table's texel offsets and packed integer widths (compact table only), or nullptr
+  const float4* ttx = nullptr;
   int tn = 0, tax = 0;
   float tiw = 0.0f, tvmin = 0.0f, tvmax = 0.0f;
   struct Ray {};
@@ -144,6 +150,29 @@ struct ExtShadeT {
   // ExtinctionAmbientOcclusion (ebs_ray_bbox_marching.comp:112-146), with the
   // shell radii taken from a list (reference: AmbOccRadius * (i + 1)).
   __device__ float ambient_occlusion(float3 tx, const FrameArgs& f) const {
+    if constexpr (ALIGNED) {
+      {
+        // the box [tx - r, tx + r] (voxels) starts at texel coordinate
+        // (tx + spacing) / spacing - 0.5 - r = g - r and is 2 r texels wide
+        const SatView& S = e->sat;
+        const float3 g = f3(fmaf(tx.x, S.inv_spacing.x, 0.5f), fmaf(tx.y, S.inv_spacing.y, 0.5f),
+                            fmaf(tx.z, S.inv_spacing.z, 0.5f));
+        float r0 = e->radii[0];
+        int w0 = __float2int_rn(2.0f * r0);
+        float sat0 = sat_box_aligned(S, f3(g.x - r0, g.y - r0, g.z - r0), w0, w0, w0);
+        float t = sat0 * (1.0f / (r0 * r0));
+        float sat_i = sat0;
+        for (int i = 1; i < e->n_shells; ++i) {
+          const float ri = e->radii[i];
+          const int wi = __float2int_rn(2.0f * ri);
+          const float sat_n = sat_box_aligned(S, f3(g.x - ri, g.y - ri, g.z - ri), wi, wi, wi);
+          t = t + (sat_n - sat_i) * (1.0f / (ri * ri));
+          sat_i = sat_n;
+        }
+        const float rk = e->radii[e->n_shells - 1];
+        return expf(-((1.0f / (rk * rk)) * t));
+      }
+    }
     float3 sc = f.vol.spacing;
     float r0 = e->radii[0];
     float sat0 = ao_box(tx - sc * r0, tx + sc * r0, f);
@@ -285,6 +314,22 @@ struct ExtShadeT {
     const float3 sc = f.vol.spacing;
     const float pm = tax == 0 ? tx.x : (tax == 1 ? tx.y : tx.z);
     float st = 0.0f;
+    if constexpr (ALIGNED) {
+      {  // every box has integer widths: the equal-fraction query
+        const float3 g = f3(fmaf(tx.x, S.inv_spacing.x, 0.5f), fmaf(tx.y, S.inv_spacing.y, 0.5f),
+                            fmaf(tx.z, S.inv_spacing.z, 0.5f));
+        for (int k = 0; k < tn; ++k) {
+          const float nxt = pm + (tlo[k].w + tiw);
+          if (!(nxt > tvmin && nxt < tvmax)) break;
+          const float4 o = ttx[k];
+          const int w = __float_as_int(o.w);
+          const float b = sat_box_aligned(S, f3(g.x + o.x, g.y + o.y, g.z + o.z), w & 1023, (w >> 10) & 1023, w >> 20);
+          st = fmaf(b, thi[k].w, st);
+          ++aux;
+        }
+        return expf(-st);
+      }
+    }
     for (int k = 0; k < tn; ++k) {
       const float4 lo = tlo[k];
       const float nxt = pm + (lo.w + tiw);
@@ -314,7 +359,11 @@ struct ExtShadeT {
   __device__ __forceinline__ float4 shade(float4 src, float3 tx, const Ray&, const FrameArgs& f, unsigned& aux) const {
     float ka = 0.0f, kd = 0.0f, io = 0.0f, is = 0.0f;
     if (e->apply_occ) { ka = e->ka; io = ambient_occlusion(tx, f); aux += e->n_shells; }
-    if (e->apply_sdw) { kd = e->kd; is = tlo ? shadow_table(tx, f, aux) : shadow(tx, f, aux); }
+    if (e->apply_sdw) {
+      kd = e->kd;
+      if constexpr (ALIGNED) is = shadow_table(tx, f, aux);
+      else is = tlo ? shadow_table(tx, f, aux) : shadow(tx, f, aux);
+    }
     if (f.grad.g) return phong_ext(f, src, tx, io, ka, is, kd);
     float k = 1.0f / (ka + kd);
     src.x = k * (src.x * io * ka + src.x * is * kd);

@@ -13,14 +13,20 @@ from tests.test_gpu_parity import compare
 pytestmark = pytest.mark.gpu
 
 
-# (AO radii, shadow type, cone angle): directional lights use the per-frame box
-# table; point lights the per-sample cone bound (a 0.7 rad cone is unbounded:
-# int64); AO radius 40 exceeds the compact table's resolution floor (int64)
-@pytest.mark.parametrize("radii,shadow_type,angle", [((2, 6, 16), 1, None), ((1, 3), 1, None), ((3, 9, 40), 1, None),
-                                                     ((2, 6), 0, None), ((2, 6), 0, 0.7)])
-def test_compact_and_int64_frames_match_oracle(ctx, radii, shadow_type, angle):
+# (AO radii, shadow type, cone angle, sample interval): directional lights use
+# the per-frame box table; point lights the per-sample cone bound (a 0.7 rad
+# cone is unbounded: int64); AO radius 40 exceeds the compact table's
+# resolution floor (int64).  Integer box widths everywhere (radii 2, 6, 16;
+# 1, 3; interval 2) take the equal-fraction query; radii 2.3, 5.1 (widths
+# 4.6, 10.2) or a 1.5-voxel interval take the general compact query.
+@pytest.mark.parametrize("radii,shadow_type,angle,interval",
+                         [((2, 6, 16), 1, None, 2.0), ((1, 3), 1, None, 2.0), ((3, 9, 40), 1, None, 2.0),
+                          ((2, 6), 0, None, 2.0), ((2, 6), 0, 0.7, 2.0), ((2.3, 5.1), 1, None, 2.0),
+                          ((2, 6, 16), 1, None, 1.5), ((2.5, 7.5), 1, 0.05, 3.0)])
+def test_compact_and_int64_frames_match_oracle(ctx, radii, shadow_type, angle, interval):
     wl = scene.workload("extinction", n=48, image=80)
-    wl.params = scene.ext_params(scene.default_step(wl.spacing), wl.diagonal, ao_radii=radii, shadow_type=shadow_type)
+    wl.params = scene.ext_params(scene.default_step(wl.spacing), wl.diagonal, ao_radii=radii, shadow_type=shadow_type,
+                                 interval=interval)
     if angle is not None:
         wl.params.sdw_cone_angle_rad = angle
     if shadow_type == 0:
