@@ -328,7 +328,8 @@ def tuned_frames(ctx, lib, w2):
                       key + "roofline_achieved_gbs": algorithmic_bytes(w2, s2, abi) / (m / 1000.0) / 1e9,
                       key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
                                        "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)}})
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
+              "refill": lib.cvr_get_ray_refill(ctx.h)}})
     ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
     return entry
 
@@ -612,7 +613,8 @@ def surrogate_section(ctx, lib, args, log=print):
                                        None), ctx.h)
             cfg = {"sampling": flags, "tile": [tw.value, th.value], "variant": tv.value,
                    "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)}
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
+              "refill": lib.cvr_get_ray_refill(ctx.h)}
             wl.method = method
             t = time_frames(ctx, lib, wl, wl.params, optr, 2 if method == abi.GROUND_TRUTH else 3, 1)
             if best is None or statistics.median(t) < statistics.median(best[1]):
@@ -732,7 +734,8 @@ def batch_section(ctx, lib, args, log=print):
                                                                   "surrogate": samples[abi.SURROGATE]},
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
             "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)},
+                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
+              "refill": lib.cvr_get_ray_refill(ctx.h)},
             "prepare_s": t_prep,
             "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
 
@@ -763,7 +766,8 @@ def run_ours(args):
                                C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
                                C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
-              "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h)}
+              "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
+              "refill": lib.cvr_get_ray_refill(ctx.h)}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),
@@ -837,6 +841,7 @@ def run_ours(args):
             abi.check(lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
             abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
             abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
+            abi.check(lib.cvr_set_ray_refill(ctx.h, 0), ctx.h)
         emit_here = rank == 0
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)

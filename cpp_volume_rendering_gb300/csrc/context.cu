@@ -174,6 +174,7 @@ cvr_status frame_args(cvr_ctx* c, const cvr_camera* cam, const void* params, flo
   f.out = reinterpret_cast<float4*>(out);
   f.counts = nullptr;
   f.stats = c->d_stats;
+  f.work = c->refill ? reinterpret_cast<unsigned*>(c->d_stats + 3) : nullptr;  // zeroed with the stats
   f.grad = GradView{};
   f.step = *static_cast<const float*>(params);  // every params struct starts with step_size
   if (c->tf_n * sizeof(float4) > 48 * 1024) return fail(c, CVR_ERR_UNSUPPORTED, "cvr_render: TF larger than 3072 entries");
@@ -732,7 +733,8 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
   f.counts = counts;
   fs = grad_args(c, method, light, &f);
   if (fs != CVR_OK) return fs;
-  CK(c, cudaMemsetAsync(c->d_stats, 0, 3 * sizeof(unsigned long long), c->stream));
+  // the three counters and the ray counter of the persistent marchers
+  CK(c, cudaMemsetAsync(c->d_stats, 0, 4 * sizeof(unsigned long long), c->stream));
   cvr_light dl{};
   if (!light) { light = &dl; }
   cudaError_t e = cudaSuccess;
@@ -764,7 +766,8 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
           e = launch_march_cached(f, c->d_lcache, c->lc_dims, p->apply_occlusion, p->apply_shadow, p->ka, p->kd,
                                   c->stream);
       } else {
-        e = launch_extinction(f, a, table, c->stream);
+        if (!c->sdw_table) c->sdw_table.reset(new ShadowBoxTable());
+        e = launch_extinction(f, a, table, *c->sdw_table, c->stream);
       }
       break;
     }
@@ -890,6 +893,14 @@ static bool tile_ok(int tile_w, int tile_h) {
   const int warps = (tile_w / 8) * (tile_h / 4);
   return warps == 2 || warps == 4 || warps == 8;
 }
+
+cvr_status cvr_set_ray_refill(cvr_ctx* c, int on) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  c->refill = on != 0;
+  return CVR_OK;
+}
+
+int cvr_get_ray_refill(const cvr_ctx* c) { return c && c->refill ? 1 : 0; }
 
 cvr_status cvr_set_tuning(cvr_ctx* c, int tile_w, int tile_h, int variant) {
   if (!c) return CVR_ERR_INVALID_ARG;
@@ -1048,6 +1059,33 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   }
   c->brick_bs = bb > 0 ? bb : 0;
   c->quads = bb < 0;
+  // the persistent ray-refill marcher at each register variant (the tile
+  // shape does not apply to it)
+  const bool keep_r = c->refill;
+  bool br = false;
+  c->refill = false;
+  if (method == CVR_METHOD_PLAIN || method == CVR_METHOD_EXTINCTION || method == CVR_METHOD_CONE_DOS ||
+      method == CVR_METHOD_GROUND_TRUTH) {
+    for (int v = 0; v < 3 && s == CVR_OK; ++v) {
+      c->refill = true;
+      c->variant = v;
+      float ms = 0.0f;
+      s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
+      if (s == CVR_OK && ms < best) {
+        best = ms;
+        br = true;
+        bvar = v;
+      }
+    }
+  }
+  c->variant = bvar;
+  c->refill = br;
+  if (s != CVR_OK) {
+    c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b; c->quads = keep_q;
+    c->warp_w = keep_ww;
+    c->refill = keep_r;
+    return s;
+  }
   if (btw) *btw = bw;
   if (bth) *bth = bh;
   if (bv) *bv = bvar;

@@ -218,6 +218,7 @@ struct cvr_ctx {
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   int tile_w = 16, tile_h = 8, variant = 0;
   int warp_w = 8;                            // cvr_set_warp_shape (used where the tile holds whole warps)
+  bool refill = false;                       // cvr_set_ray_refill: persistent ray-refill marchers
   std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
   std::unique_ptr<MlpState> mlp;             // surrogate network (created by cvr_mlp_init)
   std::unique_ptr<SurState> sur;             // surrogate shading points

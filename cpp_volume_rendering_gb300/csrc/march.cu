@@ -84,13 +84,104 @@ __global__ void __launch_bounds__(NT) k_march_gt(GtArgs g, FrameArgs f) {
   march_pixel(f, tf, sh);
 }
 
+// ---- persistent ray-refill variants (FrameArgs::work set): 128 threads,
+// as many CTAs as fit on the GPU, rays from the frame's counter (march_refill)
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_march_plain_refill(FrameArgs f, RayOrder o) {
+  extern __shared__ float4 sm_tf[];
+  const float4* tf = stage_tf(f, sm_tf);
+  __syncthreads();
+  march_refill(f, tf, PlainShade{}, f.work, o);
+}
+
+template <int MINB, bool C, bool A>
+__global__ void __launch_bounds__(128, MINB) k_march_extinction_refill(FrameArgs f, ExtArgs e, RayOrder o,
+                                                                      const __grid_constant__ ShadowBoxTable t,
+                                                                      int has_table) {
+  extern __shared__ float4 sm_tf[];
+  const float4* tf = stage_tf(f, sm_tf);
+  const int tn = has_table ? t.n : 0;
+  float4* lo = sm_tf + f.tf_n;
+  float4* hi = lo + tn;
+  float4* tx = hi + tn;
+  for (int i = threadIdx.x; i < tn; i += blockDim.x) {
+    lo[i] = t.lo[i];
+    hi[i] = t.hi[i];
+    if (A) tx[i] = t.tx[i];
+  }
+  __syncthreads();
+  ExtShadeT<C, A> sh{&e};
+  if (tn > 0) {
+    sh.tlo = lo; sh.thi = hi; sh.tn = tn; sh.tax = t.axis;
+    sh.tiw = t.interval; sh.tvmin = t.vmin; sh.tvmax = t.vmax;
+    if (A) sh.ttx = tx;
+  }
+  march_refill(f, tf, sh, f.work, o);
+}
+
+template <int MINB, bool TEX>
+__global__ void __launch_bounds__(128, MINB) k_march_dos_refill(DosArgs d, FrameArgs f, RayOrder o) {
+  extern __shared__ float4 sm[];
+  float4* tf = sm;
+  float4* occ = sm + f.tf_n;
+  float4* sdw = occ + d.occ.n_sections;
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
+  for (int i = threadIdx.x; i < d.occ.n_sections; i += blockDim.x) occ[i] = d.occ_sections[i];
+  for (int i = threadIdx.x; i < d.sdw.n_sections; i += blockDim.x) sdw[i] = d.sdw_sections[i];
+  __syncthreads();
+  DosShadeT<TEX> sh{&d, occ, sdw};
+  march_refill(f, tf, sh, f.work, o);
+}
+
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_march_gt_refill(GtArgs g, FrameArgs f, RayOrder o) {
+  extern __shared__ float4 sm[];
+  float4* tf = sm;
+  float3* ov = reinterpret_cast<float3*>(sm + f.tf_n);
+  float3* sv = ov + g.n_occ;
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
+  for (int i = threadIdx.x; i < g.n_occ; i += blockDim.x) ov[i] = g.occ_vec[i];
+  for (int i = threadIdx.x; i < g.n_sdw; i += blockDim.x) sv[i] = g.sdw_vec[i];
+  __syncthreads();
+  GtShade sh{&g, tf, f.tf_n, ov, sv};
+  march_refill(f, tf, sh, f.work, o);
+}
+
+// Persistent launch: every SM filled with as many CTAs of kern as fit.
+template <class K, class... Args>
+static cudaError_t launch_persistent(K kern, size_t smem, cudaStream_t st, Args... args) {
+  cudaError_t e;
+  if (smem > 48 * 1024 &&
+      (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+    return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = resident_ctas(kern, 128, smem, &per_sm)) != cudaSuccess) return e;
+  kern<<<(unsigned)(sms * per_sm), 128, smem, st>>>(args...);
+  return cudaGetLastError();
+}
+
 static dim3 grid_of(const FrameArgs& f) {
   return dim3((f.W + f.tile_w - 1) / f.tile_w, (f.H + f.tile_h - 1) / f.tile_h, 1);
 }
 static int threads_of(const FrameArgs& f) { return (f.tile_w / 8) * (f.tile_h / 4) * 32; }
 
+template <int V>
+constexpr int minb128() {
+  return V == 1 ? 65536 / (128 * 128) : (V == 2 ? 65536 / (128 * 80) : 1);
+}
+
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
   size_t sm = sizeof(float4) * f.tf_n;
+  if (f.work) {
+    const RayOrder o = ray_order(f);
+    switch (f.variant) {
+      case 1: return launch_persistent(k_march_plain_refill<minb128<1>()>, sm, st, f, o);
+      case 2: return launch_persistent(k_march_plain_refill<minb128<2>()>, sm, st, f, o);
+      default: return launch_persistent(k_march_plain_refill<1>, sm, st, f, o);
+    }
+  }
   switch (threads_of(f)) {
     case 64: k_march_plain<64><<<grid_of(f), 64, sm, st>>>(f); break;
     case 256: k_march_plain<256><<<grid_of(f), 256, sm, st>>>(f); break;
@@ -228,7 +319,29 @@ static void launch_extinction_nt(const FrameArgs& f, const ExtArgs& e, const Sha
   }
 }
 
-cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+template <int MINB>
+static cudaError_t launch_extinction_refill(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
+                                           const ShadowBoxTable& storage, cudaStream_t st) {
+  const RayOrder o = ray_order(f);
+  const bool c = e.sat.sat32 != nullptr;
+  const bool a = c && table && table->aligned && (e.ao_aligned || !e.apply_occ);
+  const ShadowBoxTable& t = table ? *table : storage;
+  const int has = table ? 1 : 0;
+  const size_t sm = sizeof(float4) * (f.tf_n + (table ? 3 * table->n : 0));
+  if (a) return launch_persistent(k_march_extinction_refill<MINB, true, true>, sm, st, f, e, o, t, has);
+  if (c) return launch_persistent(k_march_extinction_refill<MINB, true, false>, sm, st, f, e, o, t, has);
+  return launch_persistent(k_march_extinction_refill<MINB, false, false>, sm, st, f, e, o, t, has);
+}
+
+cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
+                              const ShadowBoxTable& storage, cudaStream_t st) {
+  if (f.work) {
+    switch (f.variant) {
+      case 1: return launch_extinction_refill<minb128<1>()>(f, e, table, storage, st);
+      case 2: return launch_extinction_refill<minb128<2>()>(f, e, table, storage, st);
+      default: return launch_extinction_refill<1>(f, e, table, storage, st);
+    }
+  }
   switch (threads_of(f)) {
     case 64: launch_extinction_nt<64>(f, e, table, st); break;
     case 256: launch_extinction_nt<256>(f, e, table, st); break;
@@ -260,6 +373,20 @@ static cudaError_t launch_dos_nt(const FrameArgs& f, const DosArgs& d, bool tex,
 
 cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, bool tex_pyramid, cudaStream_t st) {
   size_t sm = sizeof(float4) * (f.tf_n + d.occ.n_sections + d.sdw.n_sections);
+  if (f.work) {
+    const RayOrder o = ray_order(f);
+    switch (f.variant) {
+      case 1:
+        return tex_pyramid ? launch_persistent(k_march_dos_refill<minb128<1>(), true>, sm, st, d, f, o)
+                           : launch_persistent(k_march_dos_refill<minb128<1>(), false>, sm, st, d, f, o);
+      case 2:
+        return tex_pyramid ? launch_persistent(k_march_dos_refill<minb128<2>(), true>, sm, st, d, f, o)
+                           : launch_persistent(k_march_dos_refill<minb128<2>(), false>, sm, st, d, f, o);
+      default:
+        return tex_pyramid ? launch_persistent(k_march_dos_refill<1, true>, sm, st, d, f, o)
+                           : launch_persistent(k_march_dos_refill<1, false>, sm, st, d, f, o);
+    }
+  }
   switch (threads_of(f)) {
     case 64: return launch_dos_nt<64>(f, d, tex_pyramid, sm, st);
     case 256: return launch_dos_nt<256>(f, d, tex_pyramid, sm, st);
@@ -279,6 +406,14 @@ static cudaError_t launch_gt_t(const FrameArgs& f, const GtArgs& g, size_t sm, c
 
 cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st) {
   size_t sm = sizeof(float4) * f.tf_n + sizeof(float3) * (g.n_occ + g.n_sdw);
+  if (f.work) {
+    const RayOrder o = ray_order(f);
+    switch (f.variant) {
+      case 1: return launch_persistent(k_march_gt_refill<minb128<1>()>, sm, st, g, f, o);
+      case 2: return launch_persistent(k_march_gt_refill<minb128<2>()>, sm, st, g, f, o);
+      default: return launch_persistent(k_march_gt_refill<1>, sm, st, g, f, o);
+    }
+  }
   switch (threads_of(f)) {
     case 64: return launch_gt_t<64>(f, g, sm, st);
     case 256: return launch_gt_t<256>(f, g, sm, st);

@@ -39,6 +39,9 @@ struct FrameArgs {
   uint32_t* counts;                // per-pixel step count, nullable
   unsigned long long* stats;       // [0] samples, [1] shaded samples, [2] secondary fetches
   GradView grad;                   // gradient shading (grad.g == nullptr: off)
+  // Ray counter of the persistent ray-refill marchers (zeroed before the
+  // launch), or nullptr: one CTA per tile_w x tile_h block of pixels.
+  unsigned* work;
 };
 
 struct ExtArgs {
@@ -171,8 +174,10 @@ cudaError_t launch_march_cached(const FrameArgs& f, const float2* cache, const i
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
 cudaError_t launch_iso(const FrameArgs& f, const IsoArgs& a, cudaStream_t st);
-// table == nullptr: per-sample cone geometry (point lights, or too many boxes).
-cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st);
+// table == nullptr: per-sample cone geometry (point lights, or too many boxes);
+// storage: any table object (the persistent variant's argument when table is null).
+cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
+                              const ShadowBoxTable& storage, cudaStream_t st);
 // tex_pyramid: the pyramid taps read d.ptex (FP16 level textures).
 cudaError_t launch_dos(const FrameArgs& f, const DosArgs& d, bool tex_pyramid, cudaStream_t st);
 cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st);

@@ -4,6 +4,8 @@
 // the surrogate-shaded marcher reuse the ground-truth light rays).
 #pragma once
 
+#include <algorithm>
+
 #include <cuda_fp16.h>
 
 #include "march.cuh"
@@ -693,6 +695,154 @@ __device__ __forceinline__ void march_pixel(const FrameArgs& f, const float4* tf
   int px, py;
   pixel_of(f, px, py);
   march_ray(f, tf, sh, px, py);
+}
+
+// ============================================ persistent marcher, ray refill
+// Next ray index for every active lane of a warp with one atomic.
+__device__ __forceinline__ unsigned take_ray(unsigned int* work) {
+  const unsigned m = __activemask();
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(work, (unsigned)__popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + (unsigned)__popc(m & ((1u << lane) - 1u));
+}
+
+// Square spiral of 8x4-pixel tiles around the tile (cx, cy): sequence number
+// k -> ring r = ceil((sqrt(k+1) - 1) / 2), then the position on that ring.
+// Tiles near the projected volume centre (the longest rays) come first and
+// consecutive tiles are neighbours, so the CTAs' working sets overlap.
+__device__ __forceinline__ void spiral_tile(unsigned k, int& dx, int& dy) {
+  if (k == 0) { dx = dy = 0; return; }
+  int r = (int)((sqrtf((float)k + 1.0f) - 1.0f) * 0.5f);
+  while ((unsigned)(2 * r + 1) * (unsigned)(2 * r + 1) <= k) ++r;  // fix float rounding
+  while (r > 0 && (unsigned)(2 * r - 1) * (unsigned)(2 * r - 1) > k) --r;
+  const int m = (int)(k - (unsigned)(2 * r - 1) * (unsigned)(2 * r - 1));
+  const int side = m / (2 * r), off = m % (2 * r);
+  switch (side) {
+    case 0: dx = r; dy = -r + 1 + off; break;
+    case 1: dx = r - 1 - off; dy = r; break;
+    case 2: dx = -r; dy = r - 1 - off; break;
+    default: dx = -r + 1 + off; dy = -r; break;
+  }
+}
+
+
+// Ray order of the persistent marchers: 8x4-pixel tiles in the square spiral
+// around the tile of the projected volume centre (long rays first,
+// neighbouring tiles together); total = 32 x the tiles of the spiral's
+// bounding square (positions outside the image are skipped).
+struct RayOrder {
+  int cx, cy, tiles_x, tiles_y;
+  unsigned total;
+};
+
+// The a5 loop with persistent ray refill and warp-ballot control flow: each
+// lane advances its own ray to its next shaded sample, then the lanes with a
+// pending sample run ShadeSample together (the expensive light integrals run
+// with the warp's lanes aligned); a lane whose ray ends (front-to-back
+// termination or the far side of the box) writes its pixel and takes the
+// next ray of the frame from *work, so no lane idles until the longest ray of
+// its tile ends.  The warp leaves when a ballot finds no lane with a ray.
+// Same arithmetic per ray as march_ray.
+template <class Shade>
+__device__ __forceinline__ void march_refill(const FrameArgs& f, const float4* tf, const Shade& sh, unsigned* work,
+                                             const RayOrder& o) {
+  unsigned n_all = 0, shaded = 0, aux = 0;
+  bool have = false, done = false;
+  int px = 0, py = 0;
+  float3 dir = f3(0.0f, 0.0f, 1.0f), tex0 = f3(0.0f, 0.0f, 0.0f);
+  float D = 0.0f, s = 0.0f;
+  float4 dst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  unsigned n = 0, max_iter = 0;
+  typename Shade::Ray ray;
+  auto finish = [&]() {
+    const size_t off = (size_t)py * f.W + px;
+    f.out[off] = dst;
+    if (f.counts) f.counts[off] = n;
+    n_all += n;
+    have = false;
+  };
+  for (;;) {
+    // lanes without a ray take new ones; rays that miss the box are written at once
+    while (!have && !done) {
+      const unsigned idx = take_ray(work);
+      if (idx >= o.total) { done = true; break; }
+      int dx, dy;
+      spiral_tile(idx >> 5, dx, dy);
+      const int tx = o.cx + dx, ty = o.cy + dy;
+      if (tx < 0 || ty < 0 || tx >= o.tiles_x || ty >= o.tiles_y) continue;
+      px = tx * 8 + (int)(idx & 7u);
+      py = ty * 4 + (int)((idx >> 3) & 3u);
+      if (px >= f.W || py >= f.H) continue;
+      dir = primary_dir(f.cam, px, py, f.W, f.H);
+      dst = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      n = 0;
+      float tnear, tfar;
+      if (!ray_aabb(f.cam.eye, dir, f.vol.grid, tnear, tfar)) {
+        finish();
+        continue;
+      }
+      sh.begin(ray, dir);
+      D = fabsf(tfar - tnear);
+      tex0 = f.cam.eye + dir * tnear + f.vol.grid * 0.5f;
+      s = 0.0f;
+      max_iter = (unsigned)fminf(D / f.step, 1.0e9f) + 4u;
+      have = true;
+    }
+    if (__ballot_sync(0xffffffffu, have) == 0u) break;
+    bool pending = false;
+    float4 src = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float3 p = f3(0.0f, 0.0f, 0.0f);
+    float h = 0.0f;
+    if (have) {
+      while (s < D && n < max_iter) {
+        h = fminf(f.step, D - s);
+        p = tex0 + dir * (s + h * 0.5f);
+        src = tf_lookup(tf, f.tf_n, sample_volume(f.vol, p));
+        ++n;
+        if (src.w > 0.0f) { pending = true; break; }
+        s = s + h;
+      }
+      if (!pending) finish();
+    }
+    if (pending) {
+      ++shaded;
+      src = sh.shade(src, p, ray, f, aux);
+      src.w = 1.0f - expf(-src.w * h);
+      src.x *= src.w; src.y *= src.w; src.z *= src.w;
+      const float r = 1.0f - dst.w;
+      dst.x += r * src.x; dst.y += r * src.y; dst.z += r * src.z; dst.w += r * src.w;
+      s = s + h;
+      if (dst.w > 0.99f) finish();
+    }
+  }
+  add_stats(f, n_all, shaded, aux);
+}
+
+// The spiral order of a frame: centred on the pixel where the volume centre
+// projects (the frame centre when it projects behind or far off the camera).
+inline RayOrder ray_order(const FrameArgs& f) {
+  const float3 d = f3(0.0f, 0.0f, 0.0f) - f.cam.eye;
+  const float zf = dot3(d, f.cam.f);
+  int px = f.W / 2, py = f.H / 2;
+  if (zf > 1e-6f) {
+    const float xn = dot3(d, f.cam.s) / (zf * f.cam.tan_half_fovy * f.cam.aspect);
+    const float yn = dot3(d, f.cam.u) / (zf * f.cam.tan_half_fovy);
+    if (xn == xn && yn == yn && fabsf(xn) < 4.0f && fabsf(yn) < 4.0f) {
+      px = (int)((xn * 0.5f + 0.5f) * (float)f.W);
+      py = (int)((yn * 0.5f + 0.5f) * (float)f.H);
+    }
+  }
+  RayOrder o;
+  o.tiles_x = (f.W + 7) / 8;
+  o.tiles_y = (f.H + 3) / 4;
+  o.cx = px / 8 < 0 ? 0 : (px / 8 >= o.tiles_x ? o.tiles_x - 1 : px / 8);
+  o.cy = py / 4 < 0 ? 0 : (py / 4 >= o.tiles_y ? o.tiles_y - 1 : py / 4);
+  const int R = std::max(std::max(o.cx, o.tiles_x - 1 - o.cx), std::max(o.cy, o.tiles_y - 1 - o.cy));
+  o.total = (unsigned)(2 * R + 1) * (unsigned)(2 * R + 1) * 32u;  // frames <= 32768^2: below 2^32
+  return o;
 }
 
 // Loads the RGBt table into shared memory (n <= tf_smem_cap) and returns it.

@@ -141,17 +141,6 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
 }
 
 // ---------------------------------------------------------------- fused marcher
-// Next ray index for every active lane of a warp with one atomic.
-__device__ __forceinline__ unsigned take_ray(unsigned int* work) {
-  const unsigned m = __activemask();
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(m) - 1;
-  unsigned base = 0;
-  if (lane == leader) base = atomicAdd(work, (unsigned)__popc(m));
-  base = __shfl_sync(m, base, leader);
-  return base + (unsigned)__popc(m & ((1u << lane) - 1u));
-}
-
 struct SurRay {
   float3 dir, tex0;
   float D, s;
@@ -160,28 +149,6 @@ struct SurRay {
   int px, py;
   int job;
 };
-
-// Where a marcher thread's rays come from.  SingleSource: one frame, rays in
-// the longest-first block order.  BatchSource: the jobs of a batch, each a
-// run of 8x4-pixel tiles of one counter (jobs ordered by first tile).
-// Square spiral of 8x4-pixel tiles around the tile (cx, cy): sequence number
-// k -> ring r = ceil((sqrt(k+1) - 1) / 2), then the position on that ring.
-// Tiles near the projected volume centre (the longest rays) come first and
-// consecutive tiles are neighbours, so the CTAs' working sets overlap.
-__device__ __forceinline__ void spiral_tile(unsigned k, int& dx, int& dy) {
-  if (k == 0) { dx = dy = 0; return; }
-  int r = (int)((sqrtf((float)k + 1.0f) - 1.0f) * 0.5f);
-  while ((unsigned)(2 * r + 1) * (unsigned)(2 * r + 1) <= k) ++r;  // fix float rounding
-  while (r > 0 && (unsigned)(2 * r - 1) * (unsigned)(2 * r - 1) > k) --r;
-  const int m = (int)(k - (unsigned)(2 * r - 1) * (unsigned)(2 * r - 1));
-  const int side = m / (2 * r), off = m % (2 * r);
-  switch (side) {
-    case 0: dx = r; dy = -r + 1 + off; break;
-    case 1: dx = r - 1 - off; dy = r; break;
-    case 2: dx = -r; dy = r - 1 - off; break;
-    default: dx = -r + 1 + off; dy = -r; break;
-  }
-}
 
 // Where a marcher thread's rays come from.  SingleSource: one frame, tiles
 // in the square spiral around (cx, cy) (positions outside the image are

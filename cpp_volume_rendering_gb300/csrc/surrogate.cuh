@@ -12,13 +12,20 @@
 //   light  L = normalize(light_pos - world(tx)) for point and spot lights,
 //          L = light forward vector for directional lights
 //   taps   for level l = 0..5, d_l = unit * 2^(l+1) (unit = mean voxel
-//          spacing), offsets {0, L, 3L, n, 3n, r, u} * d_l:
-//          x[7l + k] = 1 - exp(-sigma_l(tx + offset_k) * d_l), where sigma_l
-//          is level l of the Gaussian extinction pyramid (trilinear within
-//          the level) and 0 outside the volume box; except x[35] (level 5,
-//          centre): the far light path, 1 - exp(-sum_j sigma_5(tx + L s_j) d_5)
-//          over s_j = (4 + j) d_5, j = 0..7, while s_j <= the shadow-ray
-//          length and tx + L s_j is inside the box
+//          spacing): x[7l + k] = 1 - exp(-sigma_l(tx + offset_k) * d_l), where
+//          sigma_l is level l of the Gaussian extinction pyramid (trilinear
+//          within the level) and 0 outside the volume box, with offsets
+//            k = 0: 0 (the centre)
+//            k = 1, 2: L * (2.5 d_l - 4 unit), L * (3.5 d_l - 4 unit): the
+//                   centres of two consecutive segments of length d_l, so the
+//                   twelve light taps partition the light ray over
+//                   [0, 252 unit] into segments of doubling length
+//            k = 3, 4: n * d_l, n * 3 d_l;  k = 5: r * d_l;  k = 6: u * d_l
+//          except x[35] (level 5, centre): the rest of the light path,
+//          1 - exp(-sum_j sigma_5(tx + L s_j) d_5) over the segments of length
+//          d_5 centred at s_j = (4.5 + j) d_5 - 4 unit, j = 0..7 (252 ... 764
+//          unit), while s_j <= the shadow-ray length and tx + L s_j is inside
+//          the box
 //   x[42..44] = (L.r, L.u, L.n)
 //   x[45..47] = (g.r, g.u, g.n), g = central differences of pyramid level 0
 //               at +-1 voxel, times the voxel length (the level-0 taps are
@@ -84,7 +91,7 @@ __device__ __forceinline__ float sur_far(const SurArgs& a, float3 tx, float3 L, 
   float tau = 0.0f;
 #pragma unroll 1
   for (int j = 0; j < 8; ++j) {
-    float s = (4.0f + (float)j) * d5;
+    float s = fmaf(4.5f + (float)j, d5, -4.0f * a.unit);
     float3 q = tx + L * s;
     if (s > a.sdw_dist || q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) break;
     tau += sur_sigma<TEX>(a, kSurLevels - 1, q) * d5;
@@ -103,8 +110,8 @@ __device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView&
 #pragma unroll
   for (int l = 0; l < kSurLevels; ++l) {
     out(7 * l + 0, l == kSurLevels - 1 ? sur_far<TEX>(a, tx, F.L, d, S) : sur_tap<TEX>(a, l, tx, d, S));
-    out(7 * l + 1, sur_tap<TEX>(a, l, tx + F.L * d, d, S));
-    out(7 * l + 2, sur_tap<TEX>(a, l, tx + F.L * (3.0f * d), d, S));
+    out(7 * l + 1, sur_tap<TEX>(a, l, tx + F.L * fmaf(2.5f, d, -4.0f * a.unit), d, S));
+    out(7 * l + 2, sur_tap<TEX>(a, l, tx + F.L * fmaf(3.5f, d, -4.0f * a.unit), d, S));
     out(7 * l + 3, sur_tap<TEX>(a, l, tx + F.n * d, d, S));
     out(7 * l + 4, sur_tap<TEX>(a, l, tx + F.n * (3.0f * d), d, S));
     out(7 * l + 5, sur_tap<TEX>(a, l, tx + F.r * d, d, S));

@@ -305,6 +305,15 @@ int cvr_get_brick_size(cvr_ctx* ctx);
  * images.  The autotuner tries 4 and 16 at its best tile. */
 cvr_status cvr_set_warp_shape(cvr_ctx* ctx, int warp_w);
 int cvr_get_warp_shape(cvr_ctx* ctx);
+/* Persistent ray refill (no reference counterpart; default off): the plain,
+ * extinction, cone and ground-truth marchers run as persistent CTAs of 128
+ * threads whose lanes each advance their own ray to its next shaded sample,
+ * shade together, and take the next ray of the frame (8x4-pixel tiles in a
+ * spiral around the projected volume centre) when theirs ends; a warp leaves
+ * when a ballot finds no lane with a ray.  Same images; the tile shape does
+ * not apply.  The autotuner tries it at every register variant. */
+cvr_status cvr_set_ray_refill(cvr_ctx* ctx, int enable);
+int cvr_get_ray_refill(const cvr_ctx* ctx);
 #define CVR_LAYOUT_PLAIN 0
 #define CVR_LAYOUT_QUADS 1
 cvr_status cvr_set_volume_layout(cvr_ctx* ctx, int layout);
@@ -336,9 +345,11 @@ cvr_status cvr_download_light_cache(cvr_ctx* ctx, float* host_out, size_t n_floa
 /* Autotuner: renders the given frame with every tile shape x register variant
  * (reps timed frames each, CUDA events, L2 flushed before each), then the
  * 4x8 and 16x2 warp shapes, every brick size and the quad layout at the best
- * of those; keeps the fastest configuration on the context and reports it
- * (cvr_get_warp_shape, cvr_get_brick_size and cvr_get_volume_layout report
- * the rest).  best_ms may be NULL. */
+ * of those, then the persistent ray-refill marcher at every register variant
+ * (plain, extinction, cone, ground truth); keeps the fastest configuration on
+ * the context and reports it (cvr_get_warp_shape, cvr_get_brick_size,
+ * cvr_get_volume_layout and cvr_get_ray_refill report the rest).  best_ms may
+ * be NULL. */
 cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
                         const void* params, size_t params_size, int w, int h, int reps,
                         int* best_tile_w, int* best_tile_h, int* best_variant, float* best_ms);
@@ -565,11 +576,16 @@ cvr_status cvr_mlp_load(cvr_ctx* ctx, const char* path);
  * Network inputs at a shading point (texture-space position p, primary ray
  * direction dir), in the frame n = -dir, r = normalize(dir x (0,1,0)),
  * u = normalize(-dir x r) of the ground-truth occlusion kernel:
- *   x[7l+k], l = 0..5, k = 0..6: 1 - exp(-sigma_l(p + o_k d_l) d_l), with
- *     d_l = 2^(l+1) voxels, o = {0, L, 3L, n, 3n, r, u}, sigma_l pyramid level l
- *     (0 outside the volume), L the direction towards the light; except
- *     x[35]: 1 - exp(-sum_j sigma_5(p + L s_j) d_5), s_j = (4+j) d_5, j < 8,
- *     over the s_j within sdw_distance and the volume (the far light path);
+ *   x[7l+k], l = 0..5, k = 0..6: 1 - exp(-sigma_l(p + o_k) d_l), with
+ *     d_l = 2^(l+1) voxels, sigma_l pyramid level l (0 outside the volume),
+ *     L the direction towards the light and offsets o_0 = 0,
+ *     o_1 = L (2.5 d_l - 4), o_2 = L (3.5 d_l - 4) (voxels: the centres of
+ *     two consecutive light-ray segments of length d_l; the twelve partition
+ *     the light ray over [0, 252] voxels), o_3 = n d_l, o_4 = 3 n d_l,
+ *     o_5 = r d_l, o_6 = u d_l; except
+ *     x[35]: 1 - exp(-sum_j sigma_5(p + L s_j) d_5), s_j = (4.5+j) d_5 - 4,
+ *     j < 8 (the rest of the light ray, 252 ... 764 voxels), over the s_j
+ *     within sdw_distance and the volume;
  *   x[42..44] = L in (r, u, n); x[45..47] = gradient of pyramid level 0
  *     (central differences at +-1 voxel, times the voxel length) in (r, u, n).
  * Outputs: (ambient occlusion, shadow) as the ground-truth integrator defines

@@ -537,10 +537,11 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
     if (q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) return T(0);
     return T(1) - std::exp(-pyr_level(f, d, l, q) * dl);
   };
-  auto far = [&](T d5) -> T {  // the far light path of x[35]
+  const T unit = T((s.sx + s.sy + s.sz) / 3.0);
+  auto far = [&](T d5) -> T {  // the rest of the light path, x[35]
     T tau = 0;
     for (int j = 0; j < 8; ++j) {
-      T sj = (T(4) + T(j)) * d5;
+      T sj = (T(4.5) + T(j)) * d5 - T(4) * unit;
       V3<T> q = tx + L * sj;
       if (sj > sdw_dist || q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) break;
       tau += pyr_level(f, d, 5, q) * d5;
@@ -550,8 +551,9 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
   T dl = T((s.sx + s.sy + s.sz) / 3.0) * T(2);
   for (int l = 0; l < 6; ++l) {
     x[7 * l + 0] = l == 5 ? far(dl) : tap(l, tx, dl);
-    x[7 * l + 1] = tap(l, tx + L * dl, dl);
-    x[7 * l + 2] = tap(l, tx + L * (T(3) * dl), dl);
+    // two consecutive light-ray segments of length dl (the twelve partition [0, 252 unit])
+    x[7 * l + 1] = tap(l, tx + L * (T(2.5) * dl - T(4) * unit), dl);
+    x[7 * l + 2] = tap(l, tx + L * (T(3.5) * dl - T(4) * unit), dl);
     x[7 * l + 3] = tap(l, tx + n * dl, dl);
     x[7 * l + 4] = tap(l, tx + n * (T(3) * dl), dl);
     x[7 * l + 5] = tap(l, tx + r * dl, dl);

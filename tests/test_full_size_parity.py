@@ -36,6 +36,7 @@ def reset(ctx):
     abi.check(ctx.lib.cvr_set_brick_size(ctx.h, 0), ctx.h)
     abi.check(ctx.lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
     abi.check(ctx.lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
+    abi.check(ctx.lib.cvr_set_ray_refill(ctx.h, 0), ctx.h)
     ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
 
 

@@ -306,9 +306,21 @@ def test_tuning_does_not_change_results(ctx, name, n, image):
         img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
         images.append(img)
     abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
+    # the persistent ray-refill marchers (plain, extinction, cone, ground truth;
+    # the iso caster keeps its tiles), every register variant, both layouts
+    for quads in (abi.LAYOUT_PLAIN, abi.LAYOUT_QUADS):
+        abi.check(lib.cvr_set_volume_layout(ctx.h, quads), ctx.h)
+        for v in (0, 1, 2):
+            abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, v), ctx.h)
+            abi.check(lib.cvr_set_ray_refill(ctx.h, 1), ctx.h)
+            assert lib.cvr_get_ray_refill(ctx.h) == 1
+            img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+            images.append(img)
+    abi.check(lib.cvr_set_ray_refill(ctx.h, 0), ctx.h)
+    abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
     abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
-    for im in images[1:]:
-        assert np.array_equal(im, images[0])
+    for k, im in enumerate(images[1:]):
+        assert np.array_equal(im, images[0]), k + 1
     assert lib.cvr_set_tuning(ctx.h, 24, 8, 0) == abi.CVR_ERR_INVALID_ARG  # 6 warps
     assert lib.cvr_set_tuning(ctx.h, 12, 8, 0) == abi.CVR_ERR_INVALID_ARG  # not whole warps
     assert lib.cvr_set_brick_size(ctx.h, 12) == abi.CVR_ERR_INVALID_ARG
