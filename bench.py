@@ -693,49 +693,65 @@ def batch_section(ctx, lib, args, log=print):
     abi.check(lib.cvr_autotune(ctx.h, jb.method, C.byref(jb.camera), C.byref(jb.light), C.c_void_p(jb.params),
                                jb.params_size, W, W, 2, C.byref(tw), C.byref(th), C.byref(tv), C.byref(tms)), ctx.h)
     ctx.select_volume(0)
-    arr = (abi.Job * n)(*b.jobs)
-    bh = C.c_void_p()
-    abi.check(lib.cvr_batch_create(ctx.h, arr, n, C.byref(bh)), ctx.h)
-    try:
-        for _ in range(2):
-            abi.check(lib.cvr_batch_run(bh), ctx.h)
-        abi.check(lib.cvr_sync(ctx.h), ctx.h)
-        times = []
-        ms = C.c_float()
-        for _ in range(3):
-            abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
-            abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
-            abi.check(lib.cvr_batch_run(bh), ctx.h)
-            abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
-            times.append(ms.value)
-        samples = {abi.EXTINCTION: 0, abi.SURROGATE: 0}
-        for k in range(n):
-            st = abi.FrameStats()
-            abi.check(lib.cvr_batch_job_stats(bh, k, C.byref(st)), ctx.h)
-            samples[b.jobs[k].method] += st.samples
-    finally:
-        lib.cvr_batch_destroy(bh)
-    # the same jobs as single cvr_render calls (one pass, device-timed as a whole)
-    abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
-    abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
-    for k, j in enumerate(b.jobs):
-        abi.check(lib.cvr_select_volume(ctx.h, j.volume), ctx.h)
-        abi.check(lib.cvr_render(ctx.h, j.method, C.byref(j.camera), C.byref(j.light), C.c_void_p(j.params),
-                                 j.params_size, outs[k], W, W, None, None), ctx.h)
-    abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
-    seq_ms = ms.value
-    abi.check(lib.cvr_select_volume(ctx.h, 0), ctx.h)
-    med = statistics.median(times)
-    tot = samples[abi.EXTINCTION] + samples[abi.SURROGATE]
+    ms = C.c_float()
+
+    def run_batch(idx):
+        """Median device time of 3 replays of a batch of the jobs idx, and its samples."""
+        arr = (abi.Job * len(idx))(*[b.jobs[k] for k in idx])
+        bh = C.c_void_p()
+        abi.check(lib.cvr_batch_create(ctx.h, arr, len(idx), C.byref(bh)), ctx.h)
+        try:
+            for _ in range(2):
+                abi.check(lib.cvr_batch_run(bh), ctx.h)
+            abi.check(lib.cvr_sync(ctx.h), ctx.h)
+            times = []
+            for _ in range(3):
+                abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+                abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+                abi.check(lib.cvr_batch_run(bh), ctx.h)
+                abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+                times.append(ms.value)
+            smp = 0
+            for k in range(len(idx)):
+                st = abi.FrameStats()
+                abi.check(lib.cvr_batch_job_stats(bh, k, C.byref(st)), ctx.h)
+                smp += st.samples
+        finally:
+            lib.cvr_batch_destroy(bh)
+        return statistics.median(times), smp
+
+    def run_sequential(idx):
+        """The same jobs as single cvr_render calls (one pass, device-timed as a whole)."""
+        abi.check(lib.cvr_flush_l2(ctx.h), ctx.h)
+        abi.check(lib.cvr_timer_start(ctx.h), ctx.h)
+        for k in idx:
+            j = b.jobs[k]
+            abi.check(lib.cvr_select_volume(ctx.h, j.volume), ctx.h)
+            abi.check(lib.cvr_render(ctx.h, j.method, C.byref(j.camera), C.byref(j.light), C.c_void_p(j.params),
+                                     j.params_size, outs[k], W, W, None, None), ctx.h)
+        abi.check(lib.cvr_timer_stop(ctx.h, C.byref(ms)), ctx.h)
+        abi.check(lib.cvr_select_volume(ctx.h, 0), ctx.h)
+        return ms.value
+
+    every = list(range(n))
+    med, tot = run_batch(every)
+    seq_ms = run_sequential(every)
+    per_method = {}
+    for name, m in (("extinction", abi.EXTINCTION), ("surrogate", abi.SURROGATE)):
+        idx = [k for k in every if b.jobs[k].method == m]
+        bm, smp = run_batch(idx)
+        sm = run_sequential(idx)
+        per_method[name] = {"jobs": len(idx), "batch_ms": bm, "msamples_s": smp / (bm / 1000.0) / 1e6,
+                            "sequential_ms": sm, "sequential_msamples_s": smp / (sm / 1000.0) / 1e6,
+                            "speedup_vs_sequential": sm / bm}
     return {"workload": "4 volumes (128^3 u8, 192x256x160 u16, 256^3 u8, 384^3 u16 value noise) x 16 views x "
                         "4 directional lights x {extinction, surrogate} = 512 images of 512^2",
             "jobs": n, "batch_ms": med, "images_per_s": n / (med / 1000.0),
-            "msamples_s": tot / (med / 1000.0) / 1e6, "samples": {"extinction": samples[abi.EXTINCTION],
-                                                                  "surrogate": samples[abi.SURROGATE]},
+            "msamples_s": tot / (med / 1000.0) / 1e6, "by_method": per_method,
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
             "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
-                  "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
-              "refill": lib.cvr_get_ray_refill(ctx.h)},
+                       "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
+                       "refill": lib.cvr_get_ray_refill(ctx.h)},
             "prepare_s": t_prep,
             "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
 
@@ -761,10 +777,20 @@ def run_ours(args):
     out_ptr = C.cast(out, C.c_void_p)
     params = wl.params
     # autotuner (part of set-up, outside the timed region): tile shape x register variant
+    # x warp shape x layout x ray refill; --tuning fixes a configuration instead (profiling)
     tw, th, tv, tms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
-    abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
-                               C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th), C.byref(tv),
-                               C.byref(tms)), ctx.h)
+    if args.tuning:
+        t = [int(v) for v in args.tuning.split(",")]
+        abi.check(lib.cvr_set_tuning(ctx.h, t[0], t[1], t[2]), ctx.h)
+        abi.check(lib.cvr_set_warp_shape(ctx.h, t[3]), ctx.h)
+        abi.check(lib.cvr_set_volume_layout(ctx.h, t[4]), ctx.h)
+        abi.check(lib.cvr_set_ray_refill(ctx.h, t[5]), ctx.h)
+        abi.check(lib.cvr_set_brick_size(ctx.h, t[6] if len(t) > 6 else 0), ctx.h)
+        tw.value, th.value, tv.value = t[0], t[1], t[2]
+    else:
+        abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
+                                   C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th),
+                                   C.byref(tv), C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
               "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
               "refill": lib.cvr_get_ray_refill(ctx.h)}
@@ -919,6 +945,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--size", type=int, default=None, help="volume side override (profiling / small cases)")
     ap.add_argument("--image", type=int, default=None, help="image side override (profiling / small cases)")
+    ap.add_argument("--tuning", default=None,
+                    help="tile_w,tile_h,variant,warp_w,layout,refill[,brick edge]: skip the autotuner (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -16,16 +16,16 @@
 //          sigma_l is level l of the Gaussian extinction pyramid (trilinear
 //          within the level) and 0 outside the volume box, with offsets
 //            k = 0: 0 (the centre)
-//            k = 1, 2: L * (2.5 d_l - 4 unit), L * (3.5 d_l - 4 unit): the
-//                   centres of two consecutive segments of length d_l, so the
-//                   twelve light taps partition the light ray over
-//                   [0, 252 unit] into segments of doubling length
 //            k = 3, 4: n * d_l, n * 3 d_l;  k = 5: r * d_l;  k = 6: u * d_l
-//          except x[35] (level 5, centre): the rest of the light path,
-//          1 - exp(-sum_j sigma_5(tx + L s_j) d_5) over the segments of length
-//          d_5 centred at s_j = (4.5 + j) d_5 - 4 unit, j = 0..7 (252 ... 764
-//          unit), while s_j <= the shadow-ray length and tx + L s_j is inside
-//          the box
+//          except the light taps k = 1, 2: the segments [2 d_l - 4 unit,
+//          3 d_l - 4 unit] and [3 d_l - 4 unit, 4 d_l - 4 unit] of the light ray
+//          tx + L s (the twelve partition [0, 252 unit] into segments of
+//          doubling length), each clipped to the ray's end t_end = min(box exit,
+//          shadow-ray length): 1 - exp(-sigma_l(midpoint) * clipped length), 0
+//          when nothing is left; and x[35] (level 5, centre): the rest of the
+//          light ray, 1 - exp(-sum_j sigma_5(midpoint_j) * length_j) over the
+//          segments [(4 + j) d_5 - 4 unit, (5 + j) d_5 - 4 unit], j = 0..7
+//          (252 ... 764 unit), clipped the same way
 //   x[42..44] = (L.r, L.u, L.n)
 //   x[45..47] = (g.r, g.u, g.n), g = central differences of pyramid level 0
 //               at +-1 voxel, times the voxel length (the level-0 taps are
@@ -85,16 +85,38 @@ __device__ __forceinline__ float sur_tap(const SurArgs& a, int l, float3 q, floa
   return 1.0f - __expf(-sur_sigma<TEX>(a, l, q) * d);
 }
 
-// Far light path: level-5 optical depth of the shadow ray beyond the taps.
+// Length of the light ray tx + L s inside the box [0, S] (tx inside) and
+// within the shadow-ray length: the end of the light path the taps cover.
+__device__ __forceinline__ float sur_ray_end(const SurArgs& a, float3 tx, float3 L, float3 S) {
+  float t = a.sdw_dist;
+  if (L.x > 0.0f) t = fminf(t, (S.x - tx.x) / L.x); else if (L.x < 0.0f) t = fminf(t, -tx.x / L.x);
+  if (L.y > 0.0f) t = fminf(t, (S.y - tx.y) / L.y); else if (L.y < 0.0f) t = fminf(t, -tx.y / L.y);
+  if (L.z > 0.0f) t = fminf(t, (S.z - tx.z) / L.z); else if (L.z < 0.0f) t = fminf(t, -tx.z / L.z);
+  return fmaxf(t, 0.0f);
+}
+
+// Optical depth sigma_l(midpoint) * length of the light-ray segment [s0, s1]
+// clipped to [0, t_end] (0 when nothing is left).
 template <bool TEX>
-__device__ __forceinline__ float sur_far(const SurArgs& a, float3 tx, float3 L, float d5, float3 S) {
+__device__ __forceinline__ float sur_seg_tau(const SurArgs& a, int l, float3 tx, float3 L, float s0, float s1,
+                                             float t_end) {
+  s0 = fmaxf(s0, 0.0f);
+  s1 = fminf(s1, t_end);
+  if (!(s1 > s0)) return 0.0f;
+  return sur_sigma<TEX>(a, l, tx + L * (0.5f * (s0 + s1))) * (s1 - s0);
+}
+
+// The rest of the light path: level-5 optical depth of the eight segments
+// beyond the twelve light taps.
+template <bool TEX>
+__device__ __forceinline__ float sur_far(const SurArgs& a, float3 tx, float3 L, float d5, float t_end) {
   float tau = 0.0f;
+  const float s0 = fmaf(4.0f, d5, -4.0f * a.unit);
 #pragma unroll 1
   for (int j = 0; j < 8; ++j) {
-    float s = fmaf(4.5f + (float)j, d5, -4.0f * a.unit);
-    float3 q = tx + L * s;
-    if (s > a.sdw_dist || q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) break;
-    tau += sur_sigma<TEX>(a, kSurLevels - 1, q) * d5;
+    const float lo = fmaf((float)j, d5, s0);
+    if (!(lo < t_end)) break;
+    tau += sur_seg_tau<TEX>(a, kSurLevels - 1, tx, L, lo, lo + d5, t_end);
   }
   return 1.0f - __expf(-tau);
 }
@@ -106,12 +128,15 @@ __device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView&
                                              float3 tx, float3 dir, Sink& out) {
   const float3 S = vol.grid;
   SurFrame F = sur_frame(a, tx, dir, S);
+  const float t_end = sur_ray_end(a, tx, F.L, S);
+  const float u4 = 4.0f * a.unit;
   float d = a.unit * 2.0f;
 #pragma unroll
   for (int l = 0; l < kSurLevels; ++l) {
-    out(7 * l + 0, l == kSurLevels - 1 ? sur_far<TEX>(a, tx, F.L, d, S) : sur_tap<TEX>(a, l, tx, d, S));
-    out(7 * l + 1, sur_tap<TEX>(a, l, tx + F.L * fmaf(2.5f, d, -4.0f * a.unit), d, S));
-    out(7 * l + 2, sur_tap<TEX>(a, l, tx + F.L * fmaf(3.5f, d, -4.0f * a.unit), d, S));
+    out(7 * l + 0, l == kSurLevels - 1 ? sur_far<TEX>(a, tx, F.L, d, t_end) : sur_tap<TEX>(a, l, tx, d, S));
+    const float s0 = fmaf(2.0f, d, -u4), s1 = fmaf(3.0f, d, -u4), s2 = fmaf(4.0f, d, -u4);
+    out(7 * l + 1, 1.0f - __expf(-sur_seg_tau<TEX>(a, l, tx, F.L, s0, s1, t_end)));
+    out(7 * l + 2, 1.0f - __expf(-sur_seg_tau<TEX>(a, l, tx, F.L, s1, s2, t_end)));
     out(7 * l + 3, sur_tap<TEX>(a, l, tx + F.n * d, d, S));
     out(7 * l + 4, sur_tap<TEX>(a, l, tx + F.n * (3.0f * d), d, S));
     out(7 * l + 5, sur_tap<TEX>(a, l, tx + F.r * d, d, S));

@@ -578,14 +578,14 @@ cvr_status cvr_mlp_load(cvr_ctx* ctx, const char* path);
  * u = normalize(-dir x r) of the ground-truth occlusion kernel:
  *   x[7l+k], l = 0..5, k = 0..6: 1 - exp(-sigma_l(p + o_k) d_l), with
  *     d_l = 2^(l+1) voxels, sigma_l pyramid level l (0 outside the volume),
- *     L the direction towards the light and offsets o_0 = 0,
- *     o_1 = L (2.5 d_l - 4), o_2 = L (3.5 d_l - 4) (voxels: the centres of
- *     two consecutive light-ray segments of length d_l; the twelve partition
- *     the light ray over [0, 252] voxels), o_3 = n d_l, o_4 = 3 n d_l,
- *     o_5 = r d_l, o_6 = u d_l; except
- *     x[35]: 1 - exp(-sum_j sigma_5(p + L s_j) d_5), s_j = (4.5+j) d_5 - 4,
- *     j < 8 (the rest of the light ray, 252 ... 764 voxels), over the s_j
- *     within sdw_distance and the volume;
+ *     L the direction towards the light and offsets o_0 = 0, o_3 = n d_l,
+ *     o_4 = 3 n d_l, o_5 = r d_l, o_6 = u d_l; except the light taps k = 1,
+ *     2: the segments [2 d_l - 4, 3 d_l - 4] and [3 d_l - 4, 4 d_l - 4]
+ *     (voxels) of the light ray p + L s (the twelve partition [0, 252]),
+ *     clipped to t_end = min(box exit, sdw_distance):
+ *     1 - exp(-sigma_l(midpoint) * clipped length), 0 when empty; and
+ *     x[35]: the same over the rest of the ray, the eight level-5 segments
+ *     [(4+j) d_5 - 4, (5+j) d_5 - 4], j < 8 (252 ... 764 voxels), summed;
  *   x[42..44] = L in (r, u, n); x[45..47] = gradient of pyramid level 0
  *     (central differences at +-1 voxel, times the voxel length) in (r, u, n).
  * Outputs: (ambient occlusion, shadow) as the ground-truth integrator defines

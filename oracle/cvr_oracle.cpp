@@ -538,22 +538,38 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
     return T(1) - std::exp(-pyr_level(f, d, l, q) * dl);
   };
   const T unit = T((s.sx + s.sy + s.sz) / 3.0);
+  // the light ray's end: the box exit, at most the shadow-ray length
+  T t_end = sdw_dist;
+  const T Lc[3] = {L.x, L.y, L.z}, Tc[3] = {tx.x, tx.y, tx.z}, Sc[3] = {S.x, S.y, S.z};
+  for (int ax = 0; ax < 3; ++ax) {
+    if (Lc[ax] > 0) t_end = std::min(t_end, (Sc[ax] - Tc[ax]) / Lc[ax]);
+    else if (Lc[ax] < 0) t_end = std::min(t_end, -Tc[ax] / Lc[ax]);
+  }
+  t_end = std::max(t_end, T(0));
+  // optical depth of the light-ray segment [s0, s1] clipped to [0, t_end]
+  auto seg_tau = [&](int l, T s0, T s1) -> T {
+    s0 = std::max(s0, T(0));
+    s1 = std::min(s1, t_end);
+    if (!(s1 > s0)) return T(0);
+    return pyr_level(f, d, l, tx + L * (T(0.5) * (s0 + s1))) * (s1 - s0);
+  };
   auto far = [&](T d5) -> T {  // the rest of the light path, x[35]
     T tau = 0;
+    const T s0 = T(4) * d5 - T(4) * unit;
     for (int j = 0; j < 8; ++j) {
-      T sj = (T(4.5) + T(j)) * d5 - T(4) * unit;
-      V3<T> q = tx + L * sj;
-      if (sj > sdw_dist || q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) break;
-      tau += pyr_level(f, d, 5, q) * d5;
+      const T lo = s0 + T(j) * d5;
+      if (!(lo < t_end)) break;
+      tau += seg_tau(5, lo, lo + d5);
     }
     return T(1) - std::exp(-tau);
   };
   T dl = T((s.sx + s.sy + s.sz) / 3.0) * T(2);
   for (int l = 0; l < 6; ++l) {
     x[7 * l + 0] = l == 5 ? far(dl) : tap(l, tx, dl);
-    // two consecutive light-ray segments of length dl (the twelve partition [0, 252 unit])
-    x[7 * l + 1] = tap(l, tx + L * (T(2.5) * dl - T(4) * unit), dl);
-    x[7 * l + 2] = tap(l, tx + L * (T(3.5) * dl - T(4) * unit), dl);
+    // two consecutive light-ray segments of length dl (the twelve partition
+    // [0, 252 unit]), clipped to the ray's end
+    x[7 * l + 1] = T(1) - std::exp(-seg_tau(l, T(2) * dl - T(4) * unit, T(3) * dl - T(4) * unit));
+    x[7 * l + 2] = T(1) - std::exp(-seg_tau(l, T(3) * dl - T(4) * unit, T(4) * dl - T(4) * unit));
     x[7 * l + 3] = tap(l, tx + n * dl, dl);
     x[7 * l + 4] = tap(l, tx + n * (T(3) * dl), dl);
     x[7 * l + 5] = tap(l, tx + r * dl, dl);
