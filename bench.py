@@ -219,7 +219,7 @@ def run_reference(args):
         return
     from cpp_volume_rendering_gb300 import scene
     import oracle
-    oracle.build()
+    oracle.build_lib()
     # the same workload, volume and tables built by the oracle alone
     wl = scene.workload(args.workload, n=args.size, image=args.image, gen=oracle.GEN)
     threads = os.cpu_count() or 1
@@ -329,7 +329,7 @@ def tuned_frames(ctx, lib, w2):
                       key + "tuning": {"tile": [tw.value, th.value], "variant": tv.value,
                                        "brick": lib.cvr_get_brick_size(ctx.h),
                   "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
-              "refill": lib.cvr_get_ray_refill(ctx.h)}})
+              "refill": lib.cvr_get_ray_refill(ctx.h), "staging": lib.cvr_get_brick_staging(ctx.h)}})
     ctx.set_sampling(abi.SAMPLING_TEX_FEATURES)
     return entry
 
@@ -614,7 +614,7 @@ def surrogate_section(ctx, lib, args, log=print):
             cfg = {"sampling": flags, "tile": [tw.value, th.value], "variant": tv.value,
                    "brick": lib.cvr_get_brick_size(ctx.h),
                   "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
-              "refill": lib.cvr_get_ray_refill(ctx.h)}
+              "refill": lib.cvr_get_ray_refill(ctx.h), "staging": lib.cvr_get_brick_staging(ctx.h)}
             wl.method = method
             t = time_frames(ctx, lib, wl, wl.params, optr, 2 if method == abi.GROUND_TRUTH else 3, 1)
             if best is None or statistics.median(t) < statistics.median(best[1]):
@@ -751,7 +751,7 @@ def batch_section(ctx, lib, args, log=print):
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
             "tuning": {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
                        "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
-                       "refill": lib.cvr_get_ray_refill(ctx.h)},
+                       "refill": lib.cvr_get_ray_refill(ctx.h), "staging": lib.cvr_get_brick_staging(ctx.h)},
             "prepare_s": t_prep,
             "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
 
@@ -793,7 +793,7 @@ def run_ours(args):
                                    C.byref(tv), C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
               "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
-              "refill": lib.cvr_get_ray_refill(ctx.h)}
+              "refill": lib.cvr_get_ray_refill(ctx.h), "staging": lib.cvr_get_brick_staging(ctx.h)}
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),
@@ -868,6 +868,7 @@ def run_ours(args):
             abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
             abi.check(lib.cvr_set_warp_shape(ctx.h, 8), ctx.h)
             abi.check(lib.cvr_set_ray_refill(ctx.h, 0), ctx.h)
+            abi.check(lib.cvr_set_brick_staging(ctx.h, 0), ctx.h)
         emit_here = rank == 0
         if surrogate is None and not args.no_surrogate:
             surrogate = surrogate_section(ctx, lib, args)

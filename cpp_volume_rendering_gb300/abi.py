@@ -203,6 +203,10 @@ SIGNATURES = {
     "cvr_get_warp_shape": (_I, [_P]),
     "cvr_set_ray_refill": (_I, [_P, _I]),
     "cvr_get_ray_refill": (_I, [_P]),
+    "cvr_set_brick_staging": (_I, [_P, _I]),
+    "cvr_get_brick_staging": (_I, [_P]),
+    "cvr_set_walk_tables": (_I, [_P, _I]),
+    "cvr_get_walk_tables": (_I, [_P]),
     "cvr_set_volume_layout": (_I, [_P, _I]),
     "cvr_get_volume_layout": (_I, [_P]),
     "cvr_set_compact_sat": (_I, [_P, _I]),

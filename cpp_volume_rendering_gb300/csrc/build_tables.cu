@@ -331,6 +331,36 @@ __global__ void k_sat_quads(const unsigned* __restrict__ s, uint4* __restrict__ 
   out[i] = make_uint4(s[i - dy - dx], s[i - dy], s[i - dx], s[i]);
 }
 
+// Walk table (WalkView) from the predecessor-quad table: D at the clamped
+// coordinates (x-1..x, y-1..y, z-1..z) of each cell, S read from the quads'
+// own-cell component.
+__global__ void k_sat_walk(const uint4* __restrict__ q, uint4* __restrict__ out, int sx, int sy, int sz, int axis,
+                           int w, long long cells) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cells) return;
+  const int x = (int)(i % sx), y = (int)((i / sx) % sy), z = (int)(i / ((long long)sx * sy));
+  const size_t sxy = (size_t)sx * sy;
+  auto S = [&](int X, int Y, int Z) {
+    X = min(max(X, 0), sx - 1); Y = min(max(Y, 0), sy - 1); Z = min(max(Z, 0), sz - 1);
+    return __ldg(&q[(size_t)X + (size_t)sx * Y + sxy * Z].w);
+  };
+  unsigned d[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int X = max(x - 1 + (c & 1), 0), Y = max(y - 1 + ((c >> 1) & 1), 0), Z = max(z - 1 + (c >> 2), 0);
+    d[c] = S(X + (axis == 0 ? w : 0), Y + (axis == 1 ? w : 0), Z + (axis == 2 ? w : 0)) - S(X, Y, Z);
+  }
+  out[2 * i] = make_uint4(d[0], d[1], d[2], d[3]);
+  out[2 * i + 1] = make_uint4(d[4], d[5], d[6], d[7]);
+}
+
+cudaError_t launch_sat_walk(const uint4* quads, uint4* out, int sx, int sy, int sz, int axis, int w,
+                            cudaStream_t st) {
+  const long long cells = (long long)sx * sy * sz;
+  k_sat_walk<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(quads, out, sx, sy, sz, axis, w, cells);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st) {
   const long long cells = (long long)sx * sy * sz;
   k_sat_quads<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(sat, out, sx, sy, cells);

@@ -13,6 +13,10 @@ cudaError_t launch_sat_build(const void* vox, int dtype, int nx, int ny, int nz,
 // scratch holds (nx+2)(ny+2)(nz+2) 32-bit values (the plane prefixes).
 cudaError_t launch_sat_build_quads(const void* vox, int dtype, int nx, int ny, int nz, const unsigned* lut,
                                    unsigned* scratch, uint4* out, cudaStream_t st);
+// The walk table of a directional shadow cone (WalkView: 32 bytes per cell)
+// along axis, box depth w, from the compact predecessor-quad table.
+cudaError_t launch_sat_walk(const uint4* quads, uint4* out, int sx, int sy, int sz, int axis, int w,
+                            cudaStream_t st);
 // The x-y predecessor-quad layout of a finished plain (sx, sy, sz) table.
 cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st);
 

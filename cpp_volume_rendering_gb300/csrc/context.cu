@@ -4,6 +4,7 @@
 // Clean(): the volume texture, transfer-function textures, SAT / pyramid /
 // cone-table / kernel-vector textures and the output frame.  Uploads happen
 // once (Init); each cvr_render is Update() + Redraw() of one frame.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -280,10 +281,41 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
       if (inv_scale32 > 0.0f) {
         a.sat.sat32 = c->d_sat32;
         a.sat.inv_scale32 = inv_scale32;
+        // every box of an aligned directional table has the walk depth of the
+        // sample interval: its queries read the walk table
+        if (*table && (*table)->aligned && c->walk_tables) {
+          cs = ensure_walk_table(c, (*table)->axis, (int)std::nearbyint(p->sdw_sample_interval), &a.walk);
+          if (cs != CVR_OK) return cs;
+        }
       }
     }
   }
   *eo = a;
+  return CVR_OK;
+}
+
+// The walk table of the current compact table for walk axis / depth w
+// (rebuilt when the compact table, the axis or the depth changes); without
+// room for it the frame's queries read the quads.
+cvr_status ensure_walk_table(cvr_ctx* c, int axis, int w, WalkView* out) {
+  *out = WalkView{nullptr, axis, w};
+  if (w < 1 || w > 1023 || !c->d_sat32) return CVR_OK;
+  if (!(c->d_walk && c->walk_gen == c->sat32_gen && c->walk_axis == axis && c->walk_w == w)) {
+    const int sx = c->nx + 2, sy = c->ny + 2, sz = c->nz + 2;
+    const size_t cells = (size_t)sx * sy * sz;
+    c->walk_gen = 0;
+    cudaError_t e = ensure(c->d_walk, c->walk_cap, cells * 2 * sizeof(uint4));
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      return CVR_OK;
+    }
+    if (e != cudaSuccess) return cuda_fail(c, e, "walk table");
+    CK(c, launch_sat_walk(c->d_sat32, c->d_walk, sx, sy, sz, axis, w, c->stream));
+    c->walk_gen = c->sat32_gen;
+    c->walk_axis = axis;
+    c->walk_w = w;
+  }
+  out->oct = c->d_walk;
   return CVR_OK;
 }
 
@@ -357,6 +389,8 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
     if (st == CVR_ERR_OUT_OF_MEMORY) return CVR_OK;
     if (st != CVR_OK) return st;
     c->sat32_F = F;
+    static std::atomic<unsigned long long> builds{0};  // distinct id of every compact build
+    c->sat32_gen = ++builds;
   }
   *inv_scale = (float)std::ldexp(1.0, -F);
   return CVR_OK;
@@ -447,7 +481,7 @@ void cvr_destroy(cvr_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
                   c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_probe, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
-                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq, c->d_satp};
+                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq, c->d_satp, c->d_walk};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -745,7 +779,7 @@ static cvr_status render_frame(cvr_ctx* c, int method, const cvr_camera* cam, co
       const cvr_plain_params* p = static_cast<const cvr_plain_params*>(params);
       if (!(p->step_size > 0.0f)) return fail(c, CVR_ERR_INVALID_ARG, "step_size must be > 0");
       f.step = p->step_size;
-      e = launch_plain(f, c->stream);
+      e = (c->staging && plain_staging_applies(f)) ? launch_plain_staged(f, c->stream) : launch_plain(f, c->stream);
       break;
     }
     case CVR_METHOD_EXTINCTION: {
@@ -893,6 +927,22 @@ static bool tile_ok(int tile_w, int tile_h) {
   const int warps = (tile_w / 8) * (tile_h / 4);
   return warps == 2 || warps == 4 || warps == 8;
 }
+
+cvr_status cvr_set_walk_tables(cvr_ctx* c, int on) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  c->walk_tables = on != 0;
+  return CVR_OK;
+}
+
+int cvr_get_walk_tables(const cvr_ctx* c) { return c && c->walk_tables ? 1 : 0; }
+
+cvr_status cvr_set_brick_staging(cvr_ctx* c, int on) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  c->staging = on != 0;
+  return CVR_OK;
+}
+
+int cvr_get_brick_staging(const cvr_ctx* c) { return c && c->staging ? 1 : 0; }
 
 cvr_status cvr_set_ray_refill(cvr_ctx* c, int on) {
   if (!c) return CVR_ERR_INVALID_ARG;
@@ -1080,7 +1130,28 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   }
   c->variant = bvar;
   c->refill = br;
+  // the plain marcher with shared-memory brick staging (plain layout, its own tile)
+  const bool keep_st = c->staging;
+  bool bst = false;
+  c->staging = false;
+  if (method == CVR_METHOD_PLAIN && s == CVR_OK && !(c->sampling & CVR_SAMPLING_TEX_VOLUME)) {
+    const int kb = c->brick_bs;
+    const bool kq = c->quads, kr = c->refill;
+    c->brick_bs = 0; c->quads = false; c->refill = false; c->staging = true;
+    float ms = 0.0f;
+    s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
+    if (s == CVR_OK && ms < best) {
+      best = ms;
+      bst = true;
+      bb = 0;
+      br = false;
+    } else {
+      c->brick_bs = kb; c->quads = kq; c->refill = kr;
+    }
+  }
+  c->staging = bst;
   if (s != CVR_OK) {
+    c->staging = keep_st;
     c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b; c->quads = keep_q;
     c->warp_w = keep_ww;
     c->refill = keep_r;

@@ -117,6 +117,7 @@ struct VolSlot {
   unsigned* d_lut32 = nullptr;
   size_t lut32_cap = 0;
   int sat32_F = kNoCompactSat;
+  unsigned long long sat32_gen = 0;  // which build of the compact table (walk tables follow it)
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;
   PyramidView pyr{};
@@ -186,9 +187,16 @@ struct cvr_ctx {
   unsigned* d_lut32 = nullptr;
   size_t lut32_cap = 0;
   int sat32_F = kNoCompactSat;
+  unsigned long long sat32_gen = 0;          // which build of the compact table (walk tables follow it)
   bool compact_sat = true;                   // cvr_set_compact_sat
+  bool walk_tables = true;                   // cvr_set_walk_tables
   unsigned* d_satp = nullptr;                // compact builds' plane-prefix scratch (any volume slot)
   size_t satp_cap = 0;
+  // the directional shadow's walk table (WalkView) of compact build walk_gen
+  uint4* d_walk = nullptr;
+  size_t walk_cap = 0;
+  unsigned long long walk_gen = 0;
+  int walk_axis = -1, walk_w = 0;
   // pyramid, and its x-y quad copy for FP32 taps (built with the first frame that needs it)
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;
@@ -219,6 +227,7 @@ struct cvr_ctx {
   int tile_w = 16, tile_h = 8, variant = 0;
   int warp_w = 8;                            // cvr_set_warp_shape (used where the tile holds whole warps)
   bool refill = false;                       // cvr_set_ray_refill: persistent ray-refill marchers
+  bool staging = false;                      // cvr_set_brick_staging: the plain marcher's staged variant
   std::unique_ptr<ShadowBoxTable> sdw_table;  // per-frame directional shadow boxes (host staging)
   std::unique_ptr<MlpState> mlp;             // surrogate network (created by cvr_mlp_init)
   std::unique_ptr<SurState> sur;             // surrogate shading points
@@ -274,6 +283,7 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->d_lut32, s.d_lut32);
   std::swap(c->lut32_cap, s.lut32_cap);
   std::swap(c->sat32_F, s.sat32_F);
+  std::swap(c->sat32_gen, s.sat32_gen);
   std::swap(c->d_pyr, s.d_pyr);
   std::swap(c->pyr_cap, s.pyr_cap);
   std::swap(c->pyr, s.pyr);
@@ -412,6 +422,7 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
 // cells, (re)built when its fixed point changes; *inv_scale = 2^-F32, or 0
 // when the frame keeps the int64 table.
 cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale);
+cvr_status ensure_walk_table(cvr_ctx* c, int axis, int w, WalkView* out);
 // The pieces of it: the fixed point (false: keep the int64 table) and the
 // build of the current volume's compact table into dst.
 bool compact_plan(const std::vector<double>& ext, double vmax, int* F, std::vector<unsigned>* q);

@@ -395,6 +395,64 @@ __device__ __forceinline__ float sat_box_aligned(const SatView& S, float3 u, int
   return fmaf(tx, y1v - y0v, y0v) * S.inv_scale32;
 }
 
+// Walk table of a directional light's shadow cone: the compact table's sums
+// differenced along the walk axis by the boxes' common depth w (texels),
+//   D(p) = S(clamp(p + w e_walk)) - S(p)   (p a clamped table coordinate),
+// stored as predecessor octs: cell (x, y, z) holds D at (x-1..x, y-1..y,
+// z-1..z), coordinates clamped, component dx + 2 dy + 4 dz (32 bytes).
+struct WalkView {
+  const uint4* oct;  // two uint4 per cell, or nullptr: no walk table
+  int axis;          // the walk axis (0, 1, 2)
+  int w;             // box depth along it, texels
+};
+
+__device__ __forceinline__ void load_oct(const uint4* p, unsigned (&v)[8]) {
+  asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+      : "l"(p));
+}
+
+// The equal-fraction query (sat_box_aligned) of a box of the walk, whose
+// depth along the walk axis is the table's w: the eight sub-box sums are
+// rectangle sums of D over the two lateral axes, four 32-byte loads (the
+// walk-axis differences are in the table).  The walk-axis taps of every box
+// of the walk lie inside the table (the walk stops where the next box would
+// leave the volume), where D of a clamped tap is the clamped difference;
+// a box reaching below the table on that axis takes sat_box_aligned.
+__device__ __forceinline__ float sat_box_walk(const SatView& S, const WalkView& Wk, float3 u, int wx, int wy,
+                                              int wz) {
+  const float fx = floorf(u.x), fy = floorf(u.y), fz = floorf(u.z);
+  const int ax = int(fx), ay = int(fy), az = int(fz);
+  const int aw = Wk.axis == 0 ? ax : (Wk.axis == 1 ? ay : az);
+  if (aw < 0) return sat_box_aligned(S, u, wx, wy, wz);
+  const float tx = u.x - fx, ty = u.y - fy, tz = u.z - fz;
+  const unsigned sx = (unsigned)S.sx, sxy = S.sxy;
+  const unsigned x0 = (unsigned)min(max(ax + 1, 0), S.sx - 1), x1 = (unsigned)min(max(ax + 1 + wx, 0), S.sx - 1);
+  const unsigned y0 = (unsigned)min(max(ay + 1, 0), S.sy - 1), y1 = (unsigned)min(max(ay + 1 + wy, 0), S.sy - 1);
+  const unsigned z0 = (unsigned)min(max(az + 1, 0), S.sz - 1), z1 = (unsigned)min(max(az + 1 + wz, 0), S.sz - 1);
+  // the walk axis contributes its low cell only; the lateral axes a (lower
+  // index) and b contribute a low and a high cell each
+  unsigned pw, pa0, pa1, pb0, pb1;
+  if (Wk.axis == 0) { pw = x0; pa0 = y0 * sx; pa1 = y1 * sx; pb0 = z0 * sxy; pb1 = z1 * sxy; }
+  else if (Wk.axis == 1) { pw = y0 * sx; pa0 = x0; pa1 = x1; pb0 = z0 * sxy; pb1 = z1 * sxy; }
+  else { pw = z0 * sxy; pa0 = x0; pa1 = x1; pb0 = y0 * sx; pb1 = y1 * sx; }
+  // 32-bit cell numbers (the compact table has fewer than 2^31 cells)
+  unsigned q00[8], q10[8], q01[8], q11[8];
+  load_oct(Wk.oct + 2u * (pw + pa0 + pb0), q00);
+  load_oct(Wk.oct + 2u * (pw + pa1 + pb0), q10);
+  load_oct(Wk.oct + 2u * (pw + pa0 + pb1), q01);
+  load_oct(Wk.oct + 2u * (pw + pa1 + pb1), q11);
+  float b[8];  // sub-box sums (below 2^31 by the compact table's fixed point)
+#pragma unroll
+  for (int c = 0; c < 8; ++c) b[c] = (float)(int)(q11[c] - q01[c] - q10[c] + q00[c]);
+  // component c = dx + 2 dy + 4 dz: trilinear weights of the fractions, in
+  // sat_box_aligned's order (z, y, x), so both queries give the same bits
+  const float z00 = fmaf(tz, b[4] - b[0], b[0]), z10 = fmaf(tz, b[5] - b[1], b[1]);
+  const float z01 = fmaf(tz, b[6] - b[2], b[2]), z11 = fmaf(tz, b[7] - b[3], b[3]);
+  const float y0v = fmaf(ty, z01 - z00, z00), y1v = fmaf(ty, z11 - z10, z10);
+  return fmaf(tx, y1v - y0v, y0v) * S.inv_scale32;
+}
+
 // ---------------------------------------------------------------- pyramid
 // Gaussian extinction pyramid, float32 levels concatenated, x fastest.
 #define CVR_MAX_LEVELS 16

@@ -56,6 +56,8 @@ struct ExtArgs {
   // every AO box has integer texel widths (2 r): the compact table's
   // equal-fraction query applies (sat_box_aligned)
   int ao_aligned;
+  // the directional shadow's walk table (walk.oct nullptr: none)
+  WalkView walk;
 };
 
 // Boxes of the SAT shadow cone of a directional light.  The cone direction is
@@ -173,6 +175,10 @@ cudaError_t launch_march_cached(const FrameArgs& f, const float2* cache, const i
                                 int apply_sdw, float ka, float kd, cudaStream_t st);
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st);
+// The plain marcher with shared-memory brick staging (staged.cu): plain
+// volume layout, FP32 samples only (plain_staging_applies).
+bool plain_staging_applies(const FrameArgs& f);
+cudaError_t launch_plain_staged(const FrameArgs& f, cudaStream_t st);
 cudaError_t launch_iso(const FrameArgs& f, const IsoArgs& a, cudaStream_t st);
 // table == nullptr: per-sample cone geometry (point lights, or too many boxes);
 // storage: any table object (the persistent variant's argument when table is null).

@@ -325,7 +325,9 @@ struct ExtShadeT {
           if (!(nxt > tvmin && nxt < tvmax)) break;
           const float4 o = ttx[k];
           const int w = __float_as_int(o.w);
-          const float b = sat_box_aligned(S, f3(g.x + o.x, g.y + o.y, g.z + o.z), w & 1023, (w >> 10) & 1023, w >> 20);
+          const float3 u = f3(g.x + o.x, g.y + o.y, g.z + o.z);
+          const float b = e->walk.oct ? sat_box_walk(S, e->walk, u, w & 1023, (w >> 10) & 1023, w >> 20)
+                                      : sat_box_aligned(S, u, w & 1023, (w >> 10) & 1023, w >> 20);
           st = fmaf(b, thi[k].w, st);
           ++aux;
         }

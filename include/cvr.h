@@ -314,6 +314,14 @@ int cvr_get_warp_shape(cvr_ctx* ctx);
  * not apply.  The autotuner tries it at every register variant. */
 cvr_status cvr_set_ray_refill(cvr_ctx* ctx, int enable);
 int cvr_get_ray_refill(const cvr_ctx* ctx);
+/* Shared-memory brick staging for CVR_METHOD_PLAIN (no reference counterpart;
+ * default off): 16x8-pixel tiles marched slab by slab along the ray, each
+ * slab's voxel box loaded into shared memory once and sampled from there.
+ * Plain volume layout, FP32 samples and transfer functions of at most 512
+ * entries only (otherwise ignored); same images.  The autotuner tries it for
+ * the plain method. */
+cvr_status cvr_set_brick_staging(cvr_ctx* ctx, int enable);
+int cvr_get_brick_staging(const cvr_ctx* ctx);
 #define CVR_LAYOUT_PLAIN 0
 #define CVR_LAYOUT_QUADS 1
 cvr_status cvr_set_volume_layout(cvr_ctx* ctx, int layout);
@@ -330,6 +338,16 @@ int cvr_get_volume_layout(cvr_ctx* ctx);
  * int64 table; batches build their own.  0 disables it. */
 cvr_status cvr_set_compact_sat(cvr_ctx* ctx, int enable);
 int cvr_get_compact_sat(cvr_ctx* ctx);
+/* Walk tables (no reference counterpart; default on): a frame on the compact
+ * SAT whose directional-shadow boxes all have integer widths (the sample
+ * interval along the walk axis, ceil-rounded cross-sections) reads a second
+ * table for its shadow queries: the compact sums differenced along the walk
+ * axis by the interval, 32 bytes per cell (8 x the volume's cells x 4 bytes),
+ * built on the first frame that needs it and kept until the SAT, the walk
+ * axis or the interval changes.  A shadow box is then four 32-byte loads
+ * instead of sixteen 16-byte ones; same images.  0 disables it. */
+cvr_status cvr_set_walk_tables(cvr_ctx* ctx, int enable);
+int cvr_get_walk_tables(const cvr_ctx* ctx);
 
 /* Object-space light cache (PreIlluminationStructuredVolume,
  * cppvolrend/utils/preillumination.h:15-47; reference default 32^3, off):
@@ -346,9 +364,10 @@ cvr_status cvr_download_light_cache(cvr_ctx* ctx, float* host_out, size_t n_floa
  * (reps timed frames each, CUDA events, L2 flushed before each), then the
  * 4x8 and 16x2 warp shapes, every brick size and the quad layout at the best
  * of those, then the persistent ray-refill marcher at every register variant
- * (plain, extinction, cone, ground truth); keeps the fastest configuration on
- * the context and reports it (cvr_get_warp_shape, cvr_get_brick_size,
- * cvr_get_volume_layout and cvr_get_ray_refill report the rest).  best_ms may
+ * (plain, extinction, cone, ground truth) and, for the plain method, brick
+ * staging; keeps the fastest configuration on the context and reports it
+ * (cvr_get_warp_shape, cvr_get_brick_size, cvr_get_volume_layout,
+ * cvr_get_ray_refill and cvr_get_brick_staging report the rest).  best_ms may
  * be NULL. */
 cvr_status cvr_autotune(cvr_ctx* ctx, int method, const cvr_camera* camera, const cvr_light* light,
                         const void* params, size_t params_size, int w, int h, int reps,

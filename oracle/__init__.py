@@ -29,7 +29,8 @@ _lib = None
 _ref = None
 
 
-def build():
+def build_lib():
+    """Compiles liboracle.so (oracle/build.py) when it is missing or stale."""
     import importlib
     return importlib.import_module("oracle.build").build()
 
@@ -38,7 +39,7 @@ def load():
     global _lib
     if _lib is None:
         if not LIB.exists():
-            build()
+            build_lib()
         lib = C.CDLL(str(LIB))
         P, I, D = C.c_void_p, C.c_int, C.c_double
         sig = {

@@ -23,7 +23,7 @@ def lib():
 @pytest.fixture(scope="session")
 def oracle_mod():
     import oracle
-    oracle.build()
+    oracle.build_lib()
     return oracle
 
 

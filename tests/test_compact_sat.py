@@ -61,3 +61,25 @@ def test_compact_table_follows_the_volume(ctx):
     ref, _, _ = orc.render(wl2.method, wl2.cam, wl2.light, wl2.params, 48, 48, precision=64)
     compare(b, ref, "extinction after a volume change")
     assert not np.array_equal(a, b)
+
+
+# directional lights whose walk runs along x, y or z, either way
+@pytest.mark.parametrize("direction", [(0.9, 0.3, 0.2), (-0.2, 0.85, 0.3), (0.25, -0.3, -0.9), (-0.8, -0.4, 0.3)])
+def test_walk_tables_equal_quads_and_match_oracle(ctx, direction):
+    """Shadow boxes read from the walk table (sums differenced along the walk
+    axis) give the bits of the quad-table query, and the oracle's image."""
+    wl = scene.workload("extinction", n=44, image=72)
+    f, u, r = scene.light_frame(direction)
+    wl.light = scene.light(abi.LIGHT_DIRECTIONAL, position=tuple(130.0 * np.array(f)), forward=f, up=u, right=r)
+    scene.prepare(ctx, wl)
+    imgs = {}
+    for on in (1, 0):
+        abi.check(ctx.lib.cvr_set_walk_tables(ctx.h, on), ctx.h)
+        assert ctx.lib.cvr_get_walk_tables(ctx.h) == on
+        imgs[on], _ = ctx.render(wl.method, wl.cam, wl.light, wl.params, 72, 72)
+    abi.check(ctx.lib.cvr_set_walk_tables(ctx.h, 1), ctx.h)
+    assert np.array_equal(imgs[1], imgs[0])
+    orc = oracle.Oracle()
+    oracle.prepare(orc, wl)
+    ref, _, _ = orc.render(wl.method, wl.cam, wl.light, wl.params, 72, 72, precision=64)
+    compare(imgs[1], ref, f"extinction walk table, light {direction}")

@@ -326,6 +326,12 @@ def test_tuning_does_not_change_results(ctx, name, n, image):
     abi.check(lib.cvr_set_ray_refill(ctx.h, 0), ctx.h)
     abi.check(lib.cvr_set_volume_layout(ctx.h, abi.LAYOUT_PLAIN), ctx.h)
     abi.check(lib.cvr_set_tuning(ctx.h, 16, 8, 0), ctx.h)
+    if name == "plain":  # shared-memory brick staging (plain layout)
+        abi.check(lib.cvr_set_brick_staging(ctx.h, 1), ctx.h)
+        assert lib.cvr_get_brick_staging(ctx.h) == 1
+        img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+        refill.append(img)
+        abi.check(lib.cvr_set_brick_staging(ctx.h, 0), ctx.h)
     for k, im in enumerate(refill):
         d = float(np.abs(im - images[0]).max())
         assert d <= 1e-5, (k, d)
