@@ -419,13 +419,16 @@ __device__ __forceinline__ void load_oct(const uint4* p, unsigned (&v)[8]) {
 // of the walk lie inside the table (the walk stops where the next box would
 // leave the volume), where D of a clamped tap is the clamped difference;
 // a box reaching below the table on that axis takes sat_box_aligned.
-__device__ __forceinline__ float sat_box_walk(const SatView& S, const WalkView& Wk, float3 u, int wx, int wy,
-                                              int wz) {
-  const float fx = floorf(u.x), fy = floorf(u.y), fz = floorf(u.z);
-  const int ax = int(fx), ay = int(fy), az = int(fz);
-  const int aw = Wk.axis == 0 ? ax : (Wk.axis == 1 ? ay : az);
-  if (aw < 0) return sat_box_aligned(S, u, wx, wy, wz);
-  const float tx = u.x - fx, ty = u.y - fy, tz = u.z - fz;
+// walk_fetch issues the four loads (always of clamped, valid cells) and
+// walk_sum turns them into the box value, so a caller can overlap the loads of
+// the next box with the sums of this one.
+struct WalkFetch {
+  unsigned q00[8], q10[8], q01[8], q11[8];
+};
+
+__device__ __forceinline__ void walk_fetch(const SatView& S, const WalkView& Wk, float3 u, int wx, int wy, int wz,
+                                           WalkFetch& F) {
+  const int ax = int(floorf(u.x)), ay = int(floorf(u.y)), az = int(floorf(u.z));
   const unsigned sx = (unsigned)S.sx, sxy = S.sxy;
   const unsigned x0 = (unsigned)min(max(ax + 1, 0), S.sx - 1), x1 = (unsigned)min(max(ax + 1 + wx, 0), S.sx - 1);
   const unsigned y0 = (unsigned)min(max(ay + 1, 0), S.sy - 1), y1 = (unsigned)min(max(ay + 1 + wy, 0), S.sy - 1);
@@ -437,20 +440,34 @@ __device__ __forceinline__ float sat_box_walk(const SatView& S, const WalkView& 
   else if (Wk.axis == 1) { pw = y0 * sx; pa0 = x0; pa1 = x1; pb0 = z0 * sxy; pb1 = z1 * sxy; }
   else { pw = z0 * sxy; pa0 = x0; pa1 = x1; pb0 = y0 * sx; pb1 = y1 * sx; }
   // 32-bit cell numbers (the compact table has fewer than 2^31 cells)
-  unsigned q00[8], q10[8], q01[8], q11[8];
-  load_oct(Wk.oct + 2u * (pw + pa0 + pb0), q00);
-  load_oct(Wk.oct + 2u * (pw + pa1 + pb0), q10);
-  load_oct(Wk.oct + 2u * (pw + pa0 + pb1), q01);
-  load_oct(Wk.oct + 2u * (pw + pa1 + pb1), q11);
+  load_oct(Wk.oct + 2u * (pw + pa0 + pb0), F.q00);
+  load_oct(Wk.oct + 2u * (pw + pa1 + pb0), F.q10);
+  load_oct(Wk.oct + 2u * (pw + pa0 + pb1), F.q01);
+  load_oct(Wk.oct + 2u * (pw + pa1 + pb1), F.q11);
+}
+
+__device__ __forceinline__ float walk_sum(const SatView& S, const WalkView& Wk, float3 u, int wx, int wy, int wz,
+                                          const WalkFetch& F) {
+  const float fx = floorf(u.x), fy = floorf(u.y), fz = floorf(u.z);
+  const int aw = Wk.axis == 0 ? int(fx) : (Wk.axis == 1 ? int(fy) : int(fz));
+  if (aw < 0) return sat_box_aligned(S, u, wx, wy, wz);
+  const float tx = u.x - fx, ty = u.y - fy, tz = u.z - fz;
   float b[8];  // sub-box sums (below 2^31 by the compact table's fixed point)
 #pragma unroll
-  for (int c = 0; c < 8; ++c) b[c] = (float)(int)(q11[c] - q01[c] - q10[c] + q00[c]);
+  for (int c = 0; c < 8; ++c) b[c] = (float)(int)(F.q11[c] - F.q01[c] - F.q10[c] + F.q00[c]);
   // component c = dx + 2 dy + 4 dz: trilinear weights of the fractions, in
   // sat_box_aligned's order (z, y, x), so both queries give the same bits
   const float z00 = fmaf(tz, b[4] - b[0], b[0]), z10 = fmaf(tz, b[5] - b[1], b[1]);
   const float z01 = fmaf(tz, b[6] - b[2], b[2]), z11 = fmaf(tz, b[7] - b[3], b[3]);
   const float y0v = fmaf(ty, z01 - z00, z00), y1v = fmaf(ty, z11 - z10, z10);
   return fmaf(tx, y1v - y0v, y0v) * S.inv_scale32;
+}
+
+__device__ __forceinline__ float sat_box_walk(const SatView& S, const WalkView& Wk, float3 u, int wx, int wy,
+                                              int wz) {
+  WalkFetch F;
+  walk_fetch(S, Wk, u, wx, wy, wz, F);
+  return walk_sum(S, Wk, u, wx, wy, wz, F);
 }
 
 // ---------------------------------------------------------------- pyramid

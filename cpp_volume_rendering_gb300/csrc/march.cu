@@ -272,7 +272,7 @@ static cudaError_t launch_batch_t(const BatchExtJob* jobs, int n_jobs, unsigned 
 // Register variants as minimum resident CTAs: caps of 128 and 80 registers.
 template <int NT>
 constexpr int minb_of(int variant) {
-  return variant == 1 ? 65536 / (NT * 128) : (variant == 2 ? 65536 / (NT * 80) : 1);
+  return variant == 1 ? 65536 / (NT * 128) : (variant == 2 ? 65536 / (NT * 80) : (variant == 3 ? 65536 / (NT * 96) : 1));
 }
 
 cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigned total_blocks, unsigned* counter,
