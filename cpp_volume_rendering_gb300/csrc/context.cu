@@ -954,9 +954,9 @@ int cvr_get_ray_refill(const cvr_ctx* c) { return c && c->refill ? 1 : 0; }
 
 cvr_status cvr_set_tuning(cvr_ctx* c, int tile_w, int tile_h, int variant) {
   if (!c) return CVR_ERR_INVALID_ARG;
-  if (!tile_ok(tile_w, tile_h) || variant < 0 || variant > 2)
+  if (!tile_ok(tile_w, tile_h) || variant < 0 || variant > 3)
     return fail(c, CVR_ERR_INVALID_ARG,
-                "cvr_set_tuning: tile must be 2, 4 or 8 warps of 8x4 pixels (8x8 ... 32x8), variant 0..2");
+                "cvr_set_tuning: tile must be 2, 4 or 8 warps of 8x4 pixels (8x8 ... 32x8), variant 0..3");
   c->tile_w = tile_w;
   c->tile_h = tile_h;
   c->variant = variant;
@@ -1064,11 +1064,13 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   const int keep_ww = c->warp_w;
   float best = 1e30f;
   int bw = keep_w, bh = keep_h, bvar = keep_v, bb = 0;
+  // register variants: the extinction marchers have a fourth (<= 96 registers)
+  const int n_variants = method == CVR_METHOD_EXTINCTION ? 4 : 3;
   c->brick_bs = 0;
   c->quads = false;
   c->warp_w = 8;
   for (int t = 0; t < 6 && s == CVR_OK; ++t) {
-    for (int v = 0; v < 3 && s == CVR_OK; ++v) {
+    for (int v = 0; v < n_variants && s == CVR_OK; ++v) {
       c->tile_w = tiles[t][0]; c->tile_h = tiles[t][1]; c->variant = v;
       float ms = 0.0f;
       s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
@@ -1116,7 +1118,7 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   c->refill = false;
   if (method == CVR_METHOD_PLAIN || method == CVR_METHOD_EXTINCTION || method == CVR_METHOD_CONE_DOS ||
       method == CVR_METHOD_GROUND_TRUTH) {
-    for (int v = 0; v < 3 && s == CVR_OK; ++v) {
+    for (int v = 0; v < n_variants && s == CVR_OK; ++v) {
       c->refill = true;
       c->variant = v;
       float ms = 0.0f;

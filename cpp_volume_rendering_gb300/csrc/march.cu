@@ -169,7 +169,7 @@ static int threads_of(const FrameArgs& f) { return (f.tile_w / 8) * (f.tile_h / 
 
 template <int V>
 constexpr int minb128() {
-  return V == 1 ? 65536 / (128 * 128) : (V == 2 ? 65536 / (128 * 80) : 1);
+  return V == 1 ? 65536 / (128 * 128) : (V == 2 ? 65536 / (128 * 80) : (V == 3 ? 65536 / (128 * 96) : 1));
 }
 
 cudaError_t launch_plain(const FrameArgs& f, cudaStream_t st) {
@@ -286,6 +286,8 @@ cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigne
       return launch_batch_t<NT, minb_of<NT>(1)>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st); \
     case 2:                                                                                                  \
       return launch_batch_t<NT, minb_of<NT>(2)>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st); \
+    case 3:                                                                                                  \
+      return launch_batch_t<NT, minb_of<NT>(3)>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st); \
     default: return launch_batch_t<NT, 1>(jobs, n_jobs, total_blocks, counter, smem, compact, aligned, st);      \
   }
   if (tile_threads == 64) { CVR_BATCH(64) }
@@ -315,6 +317,7 @@ static void launch_extinction_nt(const FrameArgs& f, const ExtArgs& e, const Sha
   switch (f.variant) {
     case 1: launch_extinction_t<NT, minb_of<NT>(1)>(f, e, table, st); break;
     case 2: launch_extinction_t<NT, minb_of<NT>(2)>(f, e, table, st); break;
+    case 3: launch_extinction_t<NT, minb_of<NT>(3)>(f, e, table, st); break;
     default: launch_extinction_t<NT, 1>(f, e, table, st); break;
   }
 }
@@ -339,6 +342,7 @@ cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const Shadow
     switch (f.variant) {
       case 1: return launch_extinction_refill<minb128<1>()>(f, e, table, storage, st);
       case 2: return launch_extinction_refill<minb128<2>()>(f, e, table, storage, st);
+      case 3: return launch_extinction_refill<minb128<3>()>(f, e, table, storage, st);
       default: return launch_extinction_refill<1>(f, e, table, storage, st);
     }
   }

@@ -281,10 +281,11 @@ cvr_status cvr_download_frame(cvr_ctx* ctx, const float* dev_frame, int w, int h
  * 2, 4 or 8 warps, each covering an 8x4 pixel block, arranged as
  * (tile_w/8) x (tile_h/4) warps: tiles 8x8, 16x8, 32x4, 8x16, 32x8 or 16x16.
  * variant selects the register budget of the kernel (0: compiler's choice,
- * 1: <= 128, 2: <= 80 registers per thread); for CVR_METHOD_SURROGATE, whose
- * persistent launch ignores the tile, it selects the CTAs per SM (0: 4,
- * 1: as many as fit, 2: 3), the rest of the SM's shared memory serving as
- * cache.  Results do not depend on the choice. */
+ * 1: <= 128, 2: <= 80, 3: <= 96 registers per thread; 3 only for the
+ * extinction marchers, the others treat it as 0); for CVR_METHOD_SURROGATE,
+ * whose persistent launch ignores the tile, it selects the CTAs per SM (0: 4,
+ * 1 and 3: as many as fit, 2: 3), the rest of the SM's shared memory serving
+ * as cache.  Results do not depend on the choice. */
 cvr_status cvr_set_tuning(cvr_ctx* ctx, int tile_w, int tile_h, int variant);
 cvr_status cvr_get_tuning(cvr_ctx* ctx, int* tile_w, int* tile_h, int* variant);
 /* Storage of the volume the marchers read: 0 = the plain x-fastest array,

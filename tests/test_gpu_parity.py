@@ -282,7 +282,7 @@ def test_tuning_does_not_change_results(ctx, name, n, image):
     scene.prepare(ctx, wl)
     images = []
     for tw, th in TILES:
-        for v in ((0, 1, 2) if name in ("extinction", "cone") else (0,)):
+        for v in ((0, 1, 2, 3) if name == "extinction" else ((0, 1, 2) if name == "cone" else (0,))):
             abi.check(lib.cvr_set_tuning(ctx.h, tw, th, v), ctx.h)
             img, st = ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
             images.append(img)
