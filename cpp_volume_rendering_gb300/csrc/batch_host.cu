@@ -29,6 +29,8 @@ struct cvr_batch {
   bool ext_compact = false;
   bool ext_aligned = false;  // every job: an aligned shadow table and aligned AO boxes (or AO off)
   std::vector<uint4*> sat32;              // the batch's own compact SATs, one per volume slot used
+  std::vector<uint4*> walks;              // their walk tables, one per (slot, walk axis, depth) in use
+  std::vector<long long> walk_keys;
   cudaGraphExec_t graph = nullptr;
   ~cvr_batch() {
     if (graph) cudaGraphExecDestroy(graph);
@@ -36,6 +38,8 @@ struct cvr_batch {
     for (void* p : bufs)
       if (p) cudaFree(p);
     for (uint4* p : sat32)
+      if (p) cudaFree(p);
+    for (uint4* p : walks)
       if (p) cudaFree(p);
   }
 };
@@ -185,6 +189,31 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
         ext[k].e.sat.inv_scale32 = inv[ext_slot[k]];
       }
       b->ext_compact = true;
+      // walk tables of these compact tables, one per (slot, walk axis, box
+      // depth) that the jobs with an aligned directional table use (a job's
+      // table holds its texel offsets after lo and hi when it is aligned)
+      for (size_t k = 0; k < ext.size() && st == CVR_OK && c->walk_tables; ++k) {
+        BatchExtJob& J = ext[k];
+        if (J.tn <= 0 || tables[k].size() != 3 * (size_t)J.tn) continue;
+        const int slot = ext_slot[k], axis = J.tax, w = (int)std::nearbyint(J.e.interval);
+        if (w < 1 || w > 1023) continue;
+        const long long key = ((long long)slot * 3 + axis) * 1024 + w;
+        uint4* d = nullptr;
+        for (size_t i = 0; i < b->walk_keys.size(); ++i)
+          if (b->walk_keys[i] == key) d = b->walks[i];
+        if (!d) {
+          select_slot(c, slot);
+          const int sx = c->nx + 2, sy = c->ny + 2, sz = c->nz + 2;
+          cudaError_t e = cudaMalloc((void**)&d, (size_t)sx * sy * sz * 2 * sizeof(uint4));
+          if (e == cudaErrorMemoryAllocation) { cudaGetLastError(); continue; }  // this job reads the quads
+          if (e != cudaSuccess) { st = cuda_fail(c, e, "cvr_batch_create: walk table"); break; }
+          b->walks.push_back(d);
+          b->walk_keys.push_back(key);
+          e = launch_sat_walk(tab[slot], d, sx, sy, sz, axis, w, c->stream);
+          if (e != cudaSuccess) { st = cuda_fail(c, e, "cvr_batch_create: walk table"); break; }
+        }
+        J.e.walk = WalkView{d, axis, w};
+      }
     }
   }
   select_slot(c, keep);
