@@ -182,8 +182,8 @@ def algorithmic_bytes(wl, st, abi):
     reference's R32F table, this library's compact table), 8 float32 pyramid
     texels (cone) or 8 voxel texels (ground truth), plus the image."""
     bvox = 1 if wl.dtype == abi.CVR_U8 else 2
-    if wl.method == abi.SURROGATE:  # per shaded sample: 42 pyramid taps (8 float32) + 6 volume taps
-        return st.samples * 8 * bvox + st.shaded_samples * (42 * 8 * 4 + 6 * 8 * bvox) + wl.width * wl.height * 16
+    if wl.method == abi.SURROGATE:  # per shaded sample: 67 pyramid taps of 8 float32 texels
+        return st.samples * 8 * bvox + st.shaded_samples * 67 * 8 * 4 + wl.width * wl.height * 16
     per_aux = {abi.PLAIN: 0, abi.EXTINCTION: 64 * 4, abi.CONE_DOS: 8 * 4, abi.GROUND_TRUTH: 8 * bvox,
                abi.ISO: 0}[wl.method]
     return st.samples * 8 * bvox + st.aux_fetches * per_aux + wl.width * wl.height * 16

@@ -319,53 +319,6 @@ struct ExtShadeT {
     if constexpr (ALIGNED) {
       const float3 g = f3(fmaf(tx.x, S.inv_spacing.x, 0.5f), fmaf(tx.y, S.inv_spacing.y, 0.5f),
                           fmaf(tx.z, S.inv_spacing.z, 0.5f));
-      if (e->walk.oct) {
-        // The boxes the walk visits before the CUT_WHEN_AWAY test first fails:
-        // the tested position moves monotonically with k, so when box 0 passes
-        // they are the boxes before the first failure on the side the walk
-        // heads for -- estimated from the linear position, then settled by
-        // the exact test.  Knowing the count, the loop fetches box k + 1 while
-        // it sums box k.
-        auto pass = [&](int k) {
-          const float nxt = pm + (tlo[k].w + tiw);
-          return nxt > tvmin && nxt < tvmax;
-        };
-        int K = 0;
-        if (tn > 0 && pass(0)) {
-          const float lim = tiw > 0.0f ? tvmax : tvmin;
-          const float est = ceilf((lim - pm - tlo[0].w - tiw) / tiw);
-          K = (int)fminf(fmaxf(est, 1.0f), (float)tn);
-          while (K < tn && pass(K)) ++K;
-          while (K > 1 && !pass(K - 1)) --K;
-        }
-        auto box = [&](int k, float3& u, int& w) {
-          const float4 o = ttx[k];
-          w = __float_as_int(o.w);
-          u = f3(g.x + o.x, g.y + o.y, g.z + o.z);
-        };
-        WalkFetch fa, fb;
-        float3 ua, ub;
-        int wa, wb;
-        if (K > 0) {
-          box(0, ua, wa);
-          walk_fetch(S, e->walk, ua, wa & 1023, (wa >> 10) & 1023, wa >> 20, fa);
-        }
-        for (int k = 0; k < K; k += 2) {
-          if (k + 1 < K) {
-            box(k + 1, ub, wb);
-            walk_fetch(S, e->walk, ub, wb & 1023, (wb >> 10) & 1023, wb >> 20, fb);
-          }
-          st = fmaf(walk_sum(S, e->walk, ua, wa & 1023, (wa >> 10) & 1023, wa >> 20, fa), thi[k].w, st);
-          if (k + 1 >= K) break;
-          if (k + 2 < K) {
-            box(k + 2, ua, wa);
-            walk_fetch(S, e->walk, ua, wa & 1023, (wa >> 10) & 1023, wa >> 20, fa);
-          }
-          st = fmaf(walk_sum(S, e->walk, ub, wb & 1023, (wb >> 10) & 1023, wb >> 20, fb), thi[k + 1].w, st);
-        }
-        aux += (unsigned)K;
-        return expf(-st);
-      }
       {  // every box has integer widths: the equal-fraction query
         for (int k = 0; k < tn; ++k) {
           const float nxt = pm + (tlo[k].w + tiw);
@@ -373,7 +326,8 @@ struct ExtShadeT {
           const float4 o = ttx[k];
           const int w = __float_as_int(o.w);
           const float3 u = f3(g.x + o.x, g.y + o.y, g.z + o.z);
-          const float b = sat_box_aligned(S, u, w & 1023, (w >> 10) & 1023, w >> 20);
+          const float b = e->walk.oct ? sat_box_walk(S, e->walk, u, w & 1023, (w >> 10) & 1023, w >> 20)
+                                      : sat_box_aligned(S, u, w & 1023, (w >> 10) & 1023, w >> 20);
           st = fmaf(b, thi[k].w, st);
           ++aux;
         }

@@ -203,7 +203,7 @@ struct SurCounts {
     if (job >= 0 && stats && (n | shaded)) {
       atomicAdd(stats + 0, (unsigned long long)n);
       atomicAdd(stats + 1, (unsigned long long)shaded);
-      atomicAdd(stats + 2, (unsigned long long)shaded * (unsigned long long)(kSurTapFeatures + 6));
+      atomicAdd(stats + 2, (unsigned long long)shaded * (unsigned long long)kSurPyramidTaps);
     }
     n = shaded = 0;
   }
@@ -353,7 +353,7 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
   if (BATCH) {
     cnt.flush(src_rays.f(cnt.job < 0 ? 0 : cnt.job).stats);
   } else {
-    add_stats(src_rays.f(0), cnt.n, cnt.shaded, cnt.shaded * (unsigned)(kSurTapFeatures + 6));
+    add_stats(src_rays.f(0), cnt.n, cnt.shaded, cnt.shaded * (unsigned)kSurPyramidTaps);
   }
   mlp_cta_end(ms.tmem, kSurTmemCols);
 }

@@ -16,7 +16,9 @@
 //          sigma_l is level l of the Gaussian extinction pyramid (trilinear
 //          within the level) and 0 outside the volume box, with offsets
 //            k = 0: 0 (the centre)
-//            k = 3, 4: n * d_l, n * 3 d_l;  k = 5: r * d_l;  k = 6: u * d_l
+//            k = 3, 4: n * d_l, n * 3 d_l;  k = 5: +-r * d_l and k = 6:
+//                   +-u * d_l, each the mean extinction of the two taps
+//                   (1 - exp(-(sigma_l(tx + o) + sigma_l(tx - o)) d_l / 2))
 //          except the light taps k = 1, 2: the segments [2 d_l - 4 unit,
 //          3 d_l - 4 unit] and [3 d_l - 4 unit, 4 d_l - 4 unit] of the light ray
 //          tx + L s (the twelve partition [0, 252 unit] into segments of
@@ -41,6 +43,10 @@ namespace cvr {
 constexpr int kSurLevels = 6;
 constexpr int kSurTaps = 7;
 constexpr int kSurTapFeatures = kSurLevels * kSurTaps;  // 42
+// Pyramid taps per shading point: 9 per level (centre, 2 light-ray segments,
+// 2 along n, the +-r and +-u pairs) on levels 0-4, the far path's 8 and 8 on
+// level 5, and the gradient's 6 on level 0.
+constexpr int kSurPyramidTaps = 5 * 9 + 8 + 8 + 6;  // 67
 
 struct SurArgs {
   PyramidView pyr;  // at least kSurLevels levels
@@ -78,11 +84,25 @@ __device__ __forceinline__ float sur_sigma(const SurArgs& a, int l, float3 q) {
   }
 }
 
+// Extinction of level l at q, 0 outside the box.
+template <bool TEX>
+__device__ __forceinline__ float sur_sigma_box(const SurArgs& a, int l, float3 q, float3 S) {
+  if (q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) return 0.0f;
+  return sur_sigma<TEX>(a, l, q);
+}
+
 // Segment opacity 1 - exp(-sigma_l(q) d) of one tap; 0 outside the box.
 template <bool TEX>
 __device__ __forceinline__ float sur_tap(const SurArgs& a, int l, float3 q, float d, float3 S) {
   if (q.x < 0.0f || q.x > S.x || q.y < 0.0f || q.y > S.y || q.z < 0.0f || q.z > S.z) return 0.0f;
   return 1.0f - __expf(-sur_sigma<TEX>(a, l, q) * d);
+}
+
+// The same for the mean extinction of the taps at c + o and c - o.
+template <bool TEX>
+__device__ __forceinline__ float sur_tap_pair(const SurArgs& a, int l, float3 c, float3 o, float d, float3 S) {
+  const float s2 = sur_sigma_box<TEX>(a, l, c + o, S) + sur_sigma_box<TEX>(a, l, c - o, S);
+  return 1.0f - __expf(-(0.5f * s2) * d);
 }
 
 // Length of the light ray tx + L s inside the box [0, S] (tx inside) and
@@ -139,8 +159,8 @@ __device__ __forceinline__ void sur_features(const SurArgs& a, const VolumeView&
     out(7 * l + 2, 1.0f - __expf(-sur_seg_tau<TEX>(a, l, tx, F.L, s1, s2, t_end)));
     out(7 * l + 3, sur_tap<TEX>(a, l, tx + F.n * d, d, S));
     out(7 * l + 4, sur_tap<TEX>(a, l, tx + F.n * (3.0f * d), d, S));
-    out(7 * l + 5, sur_tap<TEX>(a, l, tx + F.r * d, d, S));
-    out(7 * l + 6, sur_tap<TEX>(a, l, tx + F.u * d, d, S));
+    out(7 * l + 5, sur_tap_pair<TEX>(a, l, tx, F.r * d, d, S));
+    out(7 * l + 6, sur_tap_pair<TEX>(a, l, tx, F.u * d, d, S));
     d *= 2.0f;
   }
   out(42, dot3(F.L, F.r));

@@ -185,7 +185,8 @@ typedef struct cvr_frame_stats {
   uint64_t samples;         /* executed primary-ray steps (volume fetches) */
   uint64_t shaded_samples;  /* steps with extinction > 0 that went through ShadeSample */
   uint64_t aux_fetches;     /* secondary lookups: SAT box queries (extinction), pyramid
-                               taps (cone), light-ray volume samples (ground truth) */
+                               taps (cone; the surrogate: 67 per shaded sample),
+                               light-ray volume samples (ground truth) */
   float kernel_ms;          /* device time of the render kernel (CUDA events) */
 } cvr_frame_stats;
 
@@ -599,7 +600,8 @@ cvr_status cvr_mlp_load(cvr_ctx* ctx, const char* path);
  *   x[7l+k], l = 0..5, k = 0..6: 1 - exp(-sigma_l(p + o_k) d_l), with
  *     d_l = 2^(l+1) voxels, sigma_l pyramid level l (0 outside the volume),
  *     L the direction towards the light and offsets o_0 = 0, o_3 = n d_l,
- *     o_4 = 3 n d_l, o_5 = r d_l, o_6 = u d_l; except the light taps k = 1,
+ *     o_4 = 3 n d_l; k = 5 and 6 take the mean extinction of the taps at
+ *     +-r d_l and +-u d_l; and the light taps k = 1,
  *     2: the segments [2 d_l - 4, 3 d_l - 4] and [3 d_l - 4, 4 d_l - 4]
  *     (voxels) of the light ray p + L s (the twelve partition [0, 252]),
  *     clipped to t_end = min(box exit, sdw_distance):

@@ -9,8 +9,9 @@ Compiles the reference's own CPU table builders from its sources, in place
   libs/math_utils/utils.cpp,
   cppvolrend/structured/rc1pdosct/conegaussiansampler.cpp,
   libs/vis_utils/summedareatable.h (header only).
-The reference checkout must be present (it is, where fixtures are generated);
-without it this script does nothing and the tests that need the library skip.
+The reference checkout must be present ($CVR_REFERENCE_ROOT, or a `reference`
+directory beside this repository, where fixtures are generated); without it
+this script does nothing and the tests that need the library skip.
 Output goes only to oracle/_ref/.
 """
 from __future__ import annotations
@@ -26,7 +27,10 @@ LIB = OUT / "libcvr_ref.so"
 
 
 def reference_root() -> Path | None:
-    p = Path(os.environ.get("CVR_REFERENCE_ROOT", "/root/reference"))
+    """The reference checkout: $CVR_REFERENCE_ROOT, else a `reference`
+    directory beside this repository."""
+    env = os.environ.get("CVR_REFERENCE_ROOT")
+    p = Path(env) if env else HERE.parent.parent / "reference"
     return p if (p / "libs" / "vis_utils" / "summedareatable.h").exists() else None
 
 

@@ -537,6 +537,10 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
     if (q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) return T(0);
     return T(1) - std::exp(-pyr_level(f, d, l, q) * dl);
   };
+  auto sig = [&](int l, V3<T> q) -> T {  // extinction of level l, 0 outside the box
+    if (q.x < 0 || q.x > S.x || q.y < 0 || q.y > S.y || q.z < 0 || q.z > S.z) return T(0);
+    return pyr_level(f, d, l, q);
+  };
   const T unit = T((s.sx + s.sy + s.sz) / 3.0);
   // the light ray's end: the box exit, at most the shadow-ray length
   T t_end = sdw_dist;
@@ -572,8 +576,9 @@ void sur_features(const Frame<T>& f, const Scene& s, const std::vector<T>& pyr, 
     x[7 * l + 2] = T(1) - std::exp(-seg_tau(l, T(3) * dl - T(4) * unit, T(4) * dl - T(4) * unit));
     x[7 * l + 3] = tap(l, tx + n * dl, dl);
     x[7 * l + 4] = tap(l, tx + n * (T(3) * dl), dl);
-    x[7 * l + 5] = tap(l, tx + r * dl, dl);
-    x[7 * l + 6] = tap(l, tx + u * dl, dl);
+    // the mean extinction of the taps at +- r dl (k = 5) and +- u dl (k = 6)
+    x[7 * l + 5] = T(1) - std::exp(-(T(0.5) * (sig(l, tx + r * dl) + sig(l, tx - r * dl))) * dl);
+    x[7 * l + 6] = T(1) - std::exp(-(T(0.5) * (sig(l, tx + u * dl) + sig(l, tx - u * dl))) * dl);
     dl = dl * T(2);
   }
   x[42] = dot(L, r);
