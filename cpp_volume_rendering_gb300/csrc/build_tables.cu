@@ -8,6 +8,7 @@
 #include "build_tables.cuh"
 
 #include <algorithm>
+#include <cmath>
 
 namespace cvr {
 
@@ -453,22 +454,166 @@ __global__ void k_pyr_backtotau(float* data, long long n) {
   if (i < n) data[i] = -1.0f * logf(1.0f - data[i]);
 }
 
+// ---- separable form of the two level builders
+// Where a level's cells and taps fall on one lattice of input texel
+// coordinates with a constant fraction on every axis -- m input texels per
+// output cell and t per tap step, both whole numbers (the reference's base
+// 128^3 of a 256^3 volume with S0 = 1 voxel; every level from the one below it
+// when the dimensions halve) -- the Gaussian weights factor per axis
+// (exp(-|k|^2 / 2) = product of exp(-k_a^2 / 2)), so a level is one pass that
+// takes every lattice sample once (the TF opacity of the trilinear volume for
+// the base, the trilinear level below for the others; 0 outside the box, as
+// in_grid) and three 7-tap passes, instead of 343 samples per cell.  Cell i,
+// tap k reads lattice point i m + (k + 3) t, at texel coordinate j0 + q + f.
+struct PyrAxis {
+  int m, t;   // texels per cell, per tap step
+  int j0, g;  // lattice start (integer part) and size
+  int n_out;  // cells
+  float f;    // the constant fraction
+};
+struct PyrWeights { float w[7]; };
+
+static bool pyr_axis(int n_in, int n_out, double tap_texels, PyrAxis* a) {
+  if (n_out < 1 || n_in % n_out) return false;
+  const double t = std::nearbyint(tap_texels);
+  if (!(t >= 1.0) || std::fabs(tap_texels - t) > 1e-9 * t) return false;
+  a->m = n_in / n_out;
+  a->t = (int)t;
+  const double c0 = 0.5 * a->m - 0.5;  // texel coordinate of cell 0, tap 0
+  a->f = (float)(c0 - std::floor(c0));
+  a->j0 = (int)std::floor(c0) - 3 * a->t;
+  a->g = (n_out - 1) * a->m + 6 * a->t + 1;
+  a->n_out = n_out;
+  return true;
+}
+
+// The plan of level l (l = 0: from the volume): false when it has no separable form.
+static bool pyr_plan(const VolumeView& vol, const PyramidView& P, int l, float s0, PyrAxis ax[3]) {
+  const int in[3] = {l == 0 ? vol.nx : P.dims[l - 1][0], l == 0 ? vol.ny : P.dims[l - 1][1],
+                     l == 0 ? vol.nz : P.dims[l - 1][2]};
+  const double grid[3] = {P.grid.x, P.grid.y, P.grid.z};
+  const double sigma = (double)s0 * std::ldexp(1.0, l);
+  for (int a = 0; a < 3; ++a)
+    if (!pyr_axis(in[a], P.dims[l][a], sigma * in[a] / grid[a], &ax[a])) return false;
+  return true;
+}
+
+static long long pyr_scratch(const PyrAxis ax[3]) {
+  return (long long)ax[0].g * ax[1].g * ax[2].g + (long long)ax[0].n_out * ax[1].g * ax[2].g +
+         (long long)ax[0].n_out * ax[1].n_out * ax[2].g;
+}
+
+long long pyramid_scratch_floats(const VolumeView& vol, const PyramidView& P, float s0) {
+  long long need = 0;
+  PyrAxis ax[3];
+  for (int l = 0; l < P.n_levels; ++l)
+    if (pyr_plan(vol, P, l, s0, ax)) need = std::max(need, pyr_scratch(ax));
+  return need;
+}
+
+__device__ __forceinline__ bool pyr_lattice_point(const PyrAxis* A, const int n_in[3], long long idx, float3& u) {
+  const int qx = (int)(idx % A[0].g), qy = (int)((idx / A[0].g) % A[1].g), qz = (int)(idx / ((long long)A[0].g * A[1].g));
+  u = f3((float)(A[0].j0 + qx) + A[0].f, (float)(A[1].j0 + qy) + A[1].f, (float)(A[2].j0 + qz) + A[2].f);
+  // inside the box [0, S]: texel coordinates in [-0.5, n - 0.5]
+  return u.x >= -0.5f && u.y >= -0.5f && u.z >= -0.5f && u.x <= (float)n_in[0] - 0.5f &&
+         u.y <= (float)n_in[1] - 0.5f && u.z <= (float)n_in[2] - 0.5f;
+}
+
+struct PyrAxes { PyrAxis a[3]; };
+
+__global__ void k_pyr_lattice_base(VolumeView vol, const float4* __restrict__ tf_rgba, int tf_n, PyrAxes A,
+                                   float* __restrict__ G, long long total) {
+  extern __shared__ float4 sm_tf[];
+  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tf[i] = tf_rgba[i];
+  __syncthreads();
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int n_in[3] = {vol.nx, vol.ny, vol.nz};
+  float3 u;
+  const bool inside = pyr_lattice_point(A.a, n_in, idx, u);
+  const float3 p = f3((u.x + 0.5f) * vol.spacing.x, (u.y + 0.5f) * vol.spacing.y, (u.z + 0.5f) * vol.spacing.z);
+  G[idx] = inside ? tf_alpha(sm_tf, tf_n, sample_volume(vol, p)) : 0.0f;
+}
+
+__global__ void k_pyr_lattice_level(PyramidView P, int l_in, PyrAxes A, float* __restrict__ G, long long total) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int* n_in = P.dims[l_in];
+  float3 u;
+  const bool inside = pyr_lattice_point(A.a, n_in, idx, u);
+  const float3 p = f3((u.x + 0.5f) * (P.grid.x / (float)n_in[0]), (u.y + 0.5f) * (P.grid.y / (float)n_in[1]),
+                      (u.z + 0.5f) * (P.grid.z / (float)n_in[2]));
+  G[idx] = inside ? pyr_sample_level(P, l_in, p) : 0.0f;
+}
+
+// One 7-tap pass along axis ax of an (nx, ny, nz) array: out has n_out cells
+// along that axis, out[i] = sum_k w[k] in[i m + (k + 3) t].
+__global__ void k_pyr_pass(const float* __restrict__ in, int nx, int ny, int nz, int ax, PyrAxis a, PyrWeights w,
+                           float* __restrict__ out, long long total) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= total) return;
+  const int ox = ax == 0 ? a.n_out : nx, oy = ax == 1 ? a.n_out : ny;
+  const int x = (int)(idx % ox), y = (int)((idx / ox) % oy), z = (int)(idx / ((long long)ox * oy));
+  const int i = ax == 0 ? x : (ax == 1 ? y : z);
+  const long long stride = ax == 0 ? 1 : (ax == 1 ? (long long)nx : (long long)nx * ny);
+  const long long base = (ax == 0 ? 0 : x) + (ax == 1 ? 0 : (long long)y * nx) + (ax == 2 ? 0 : (long long)z * nx * ny);
+  float acc = 0.0f;
+#pragma unroll
+  for (int k = 0; k < 7; ++k) acc = fmaf(w.w[k], __ldg(in + base + (long long)(i * a.m + k * a.t) * stride), acc);
+  out[idx] = acc;
+}
+
+static cudaError_t pyr_separable(const PyrAxis A[3], float* G, float* T1, float* T2, float* out, cudaStream_t st) {
+  PyrWeights w;
+  double sum = 0.0;
+  for (int k = -3; k <= 3; ++k) sum += std::exp(-0.5 * k * k);
+  for (int k = -3; k <= 3; ++k) w.w[k + 3] = (float)(std::exp(-0.5 * k * k) / sum);
+  const long long n1 = (long long)A[0].n_out * A[1].g * A[2].g, n2 = (long long)A[0].n_out * A[1].n_out * A[2].g;
+  const long long n3 = (long long)A[0].n_out * A[1].n_out * A[2].n_out;
+  k_pyr_pass<<<(unsigned)((n1 + 255) / 256), 256, 0, st>>>(G, A[0].g, A[1].g, A[2].g, 0, A[0], w, T1, n1);
+  k_pyr_pass<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(T1, A[0].n_out, A[1].g, A[2].g, 1, A[1], w, T2, n2);
+  k_pyr_pass<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(T2, A[0].n_out, A[1].n_out, A[2].g, 2, A[2], w, out, n3);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, int tf_n, float s0,
-                                 PyramidView& P, float* data, cudaStream_t st) {
+                                 PyramidView& P, float* data, float* scratch, long long scratch_floats,
+                                 cudaStream_t st) {
   const int threads = 128;
   long long n0 = (long long)P.dims[0][0] * P.dims[0][1] * P.dims[0][2];
   size_t sm = sizeof(float4) * tf_n;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_pyr_base, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_pyr_lattice_base, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
-  k_pyr_base<<<(unsigned)((n0 + threads - 1) / threads), threads, sm, st>>>(
-      vol, tf_rgba, tf_n, P.dims[0][0], P.dims[0][1], P.dims[0][2], s0, data + P.offset[0]);
+  PyrAxes A;
+  if (scratch && pyr_plan(vol, P, 0, s0, A.a) && pyr_scratch(A.a) <= scratch_floats) {
+    const long long g = (long long)A.a[0].g * A.a[1].g * A.a[2].g;
+    float* T1 = scratch + g;
+    float* T2 = T1 + (long long)A.a[0].n_out * A.a[1].g * A.a[2].g;
+    k_pyr_lattice_base<<<(unsigned)((g + 255) / 256), 256, sm, st>>>(vol, tf_rgba, tf_n, A, scratch, g);
+    cudaError_t e = pyr_separable(A.a, scratch, T1, T2, data + P.offset[0], st);
+    if (e != cudaSuccess) return e;
+  } else {
+    k_pyr_base<<<(unsigned)((n0 + threads - 1) / threads), threads, sm, st>>>(
+        vol, tf_rgba, tf_n, P.dims[0][0], P.dims[0][1], P.dims[0][2], s0, data + P.offset[0]);
+  }
   P.data = data;
   for (int l = 1; l < P.n_levels; ++l) {
     long long nl = (long long)P.dims[l][0] * P.dims[l][1] * P.dims[l][2];
     float si = s0 * powf(2.0f, float(l));
-    k_pyr_level<<<(unsigned)((nl + threads - 1) / threads), threads, 0, st>>>(P, l, si, data + P.offset[l]);
+    if (scratch && pyr_plan(vol, P, l, s0, A.a) && pyr_scratch(A.a) <= scratch_floats) {
+      const long long g = (long long)A.a[0].g * A.a[1].g * A.a[2].g;
+      float* T1 = scratch + g;
+      float* T2 = T1 + (long long)A.a[0].n_out * A.a[1].g * A.a[2].g;
+      k_pyr_lattice_level<<<(unsigned)((g + 255) / 256), 256, 0, st>>>(P, l - 1, A, scratch, g);
+      cudaError_t e = pyr_separable(A.a, scratch, T1, T2, data + P.offset[l], st);
+      if (e != cudaSuccess) return e;
+    } else {
+      k_pyr_level<<<(unsigned)((nl + threads - 1) / threads), threads, 0, st>>>(P, l, si, data + P.offset[l]);
+    }
   }
   long long total = P.offset[P.n_levels - 1] +
                     (long long)P.dims[P.n_levels - 1][0] * P.dims[P.n_levels - 1][1] * P.dims[P.n_levels - 1][2];

@@ -20,9 +20,14 @@ cudaError_t launch_sat_walk(const uint4* quads, uint4* out, int sx, int sy, int 
 // The x-y predecessor-quad layout of a finished plain (sx, sy, sz) table.
 cudaError_t launch_sat_quads(const unsigned* sat, uint4* out, int sx, int sy, int sz, cudaStream_t st);
 
-// Builds every level of P (dims/offsets/grid filled by the caller) into data.
+// Builds every level of P (dims/offsets/grid filled by the caller) into data;
+// levels with a separable form use scratch (scratch_floats floats; see
+// pyramid_scratch_floats), the others the direct 343-tap kernels.
 cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, int tf_n, float s0,
-                                 PyramidView& P, float* data, cudaStream_t st);
+                                 PyramidView& P, float* data, float* scratch, long long scratch_floats,
+                                 cudaStream_t st);
+// Floats of scratch the separable levels of P need (0: none is separable).
+long long pyramid_scratch_floats(const VolumeView& vol, const PyramidView& P, float s0);
 
 // Grid-stride fill of a device buffer (used to flush L2 between timed frames).
 cudaError_t launch_fill(void* p, size_t bytes, unsigned int v, cudaStream_t st);

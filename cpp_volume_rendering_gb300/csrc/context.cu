@@ -481,7 +481,7 @@ void cvr_destroy(cvr_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->d_vol, c->d_rgbt, c->d_rgba, c->d_sat, c->d_lut, c->d_pyr, c->d_occ_sec, c->d_sdw_sec,
                   c->d_occ_vec, c->d_sdw_vec, c->d_stats, c->d_out, c->d_flush, c->d_probe, c->d_vbrick, c->d_lcache, c->d_grad, c->d_ms, c->d_msf,
-                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq, c->d_satp, c->d_walk};
+                  c->d_sat32, c->d_lut32, c->d_kerr, c->d_pyrq, c->d_satp, c->d_walk, c->d_pyrs};
   for (void* p : bufs)
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
@@ -648,7 +648,17 @@ cvr_status cvr_build_ext_pyramid(cvr_ctx* c, const cvr_pyramid_params* p) {
   P.grid = v.grid;
   P.inv_grid = f3(1.0f / v.grid.x, 1.0f / v.grid.y, 1.0f / v.grid.z);
   CK(c, ensure(c->d_pyr, c->pyr_cap, (size_t)off * sizeof(float)));
-  CK(c, launch_pyramid_build(v, c->d_rgba, c->tf_n, p->sigma0, P, c->d_pyr, c->stream));
+  // scratch of the separable levels (lattice samples and two pass results);
+  // without room for it every level takes the direct kernels
+  const long long sf = pyramid_scratch_floats(v, P, p->sigma0);
+  float* scratch = nullptr;
+  if (sf > 0) {
+    cudaError_t e = ensure(c->d_pyrs, c->pyrs_cap, (size_t)sf * sizeof(float));
+    if (e == cudaErrorMemoryAllocation) cudaGetLastError();
+    else if (e != cudaSuccess) return cuda_fail(c, e, "pyramid scratch");
+    else scratch = c->d_pyrs;
+  }
+  CK(c, launch_pyramid_build(v, c->d_rgba, c->tf_n, p->sigma0, P, c->d_pyr, scratch, scratch ? sf : 0, c->stream));
   c->pyr = P;
   c->pyr_ready = true;
   c->pyrq_ready = false;

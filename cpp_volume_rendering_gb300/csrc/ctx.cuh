@@ -192,6 +192,8 @@ struct cvr_ctx {
   bool walk_tables = true;                   // cvr_set_walk_tables
   unsigned* d_satp = nullptr;                // compact builds' plane-prefix scratch (any volume slot)
   size_t satp_cap = 0;
+  float* d_pyrs = nullptr;                   // separable pyramid builds' scratch (any volume slot)
+  size_t pyrs_cap = 0;
   // the directional shadow's walk table (WalkView) of compact build walk_gen
   uint4* d_walk = nullptr;
   size_t walk_cap = 0;

@@ -139,13 +139,24 @@ def test_sat_bit_exact_and_relative_error(ctx):
     assert np.abs(got - ref).max() / ref.max() <= 1e-9
 
 
-def test_pyramid_levels_match_oracle(ctx):
+# (volume dims, base dims, sigma0): the reference geometry (base = half the
+# volume, S0 = 1 voxel), where every level has the separable form; an odd
+# volume over a half base (separable, odd-sized lattices); a base that does
+# not divide the volume and a non-integer sigma (the direct 343-tap kernels);
+# a flat base whose levels collapse to 1 cell on one axis
+@pytest.mark.parametrize("dims,base,s0", [((32, 32, 32), (16, 16, 16), 1.0), ((30, 22, 26), (15, 11, 13), 1.0),
+                                          ((32, 24, 20), (12, 9, 7), 1.0), ((32, 32, 32), (16, 16, 16), 1.5),
+                                          ((40, 8, 24), (20, 4, 12), 2.0)])
+def test_pyramid_levels_match_oracle(ctx, dims, base, s0):
     wl = scene.workload("cone", n=32, image=8)
+    w, h, d = dims
+    wl.volume = scene.synth_blobs(w, h, d, abi.CVR_U8, 8, seed=31, noise_max=20.0)
+    wl.pyramid = dict(base_dims=base, sigma0=s0, n_levels=5)
     scene.prepare(ctx, wl)
     levels = ctx.pyramid()
     orc = oracle.Oracle()
     oracle.prepare(orc, wl)
-    assert len(levels) == orc.n_levels == 5
+    assert len(levels) == orc.n_levels
     for l, lev in enumerate(levels):
         ref = orc.pyramid_level(l, 64)
         assert lev.shape == ref.shape
