@@ -107,23 +107,38 @@ __global__ void __launch_bounds__(kSatPlaneThreads) k_sat_planes(const void* vox
       const int y = y0 + r;
       const bool border_row = border_plane || y == 0 || y == sy - 1;
       const size_t vrow = border_row ? 0 : ((size_t)(z - 1) * ny + (y - 1)) * (size_t)nx;
+      // the row in segments of 32 cells x kSegs: every segment's voxels, then
+      // every segment's table values, are loaded before the scans, so a row
+      // costs two rounds of memory latency instead of two per segment
+      constexpr int kSegs = 8;
       W run = 0;
-      for (int base = 0; base < sx; base += 32) {
-        const int x = base + lane;
-        W v = 0;
-        if (!border_row && x > 0 && x < sx - 1) {
-          const unsigned q = dtype == 1 ? (unsigned)__ldg(static_cast<const uint8_t*>(vox) + vrow + (x - 1))
-                                        : (unsigned)__ldg(static_cast<const uint16_t*>(vox) + vrow + (x - 1));
-          v = __ldg(lut + q);
+      for (int base = 0; base < sx; base += 32 * kSegs) {
+        unsigned q[kSegs];
+        W v[kSegs];
+#pragma unroll
+        for (int g = 0; g < kSegs; ++g) {
+          const int x = base + 32 * g + lane;
+          q[g] = 0xffffffffu;
+          if (!border_row && x > 0 && x < sx - 1)
+            q[g] = dtype == 1 ? (unsigned)__ldg(static_cast<const uint8_t*>(vox) + vrow + (x - 1))
+                              : (unsigned)__ldg(static_cast<const uint16_t*>(vox) + vrow + (x - 1));
         }
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const W n = __shfl_up_sync(0xffffffffu, v, o);
-          if (lane >= o) v += n;
+        for (int g = 0; g < kSegs; ++g) v[g] = q[g] != 0xffffffffu ? __ldg(lut + q[g]) : W(0);
+#pragma unroll
+        for (int g = 0; g < kSegs; ++g) {
+          const int x = base + 32 * g + lane;
+          if (base + 32 * g >= sx) break;  // warp-uniform
+          W t = v[g];
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const W n = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += n;
+          }
+          t += run;
+          if (x < sx) chunk[(size_t)r * sx + x] = t;
+          run = __shfl_sync(0xffffffffu, t, 31);
         }
-        v += run;
-        if (x < sx) chunk[(size_t)r * sx + x] = v;
-        run = __shfl_sync(0xffffffffu, v, 31);
       }
     }
     __syncthreads();
@@ -332,27 +347,30 @@ __global__ void k_sat_quads(const unsigned* __restrict__ s, uint4* __restrict__ 
   out[i] = make_uint4(s[i - dy - dx], s[i - dy], s[i - dx], s[i]);
 }
 
-// Walk table (WalkView) from the predecessor-quad table: D at the clamped
-// coordinates (x-1..x, y-1..y, z-1..z) of each cell, S read from the quads'
-// own-cell component.
+// Walk table (WalkView) from the predecessor-quad table: the oct of cell
+// (x, y, z) is D = S(shifted) - S at the clamped coordinates (x-1..x, y-1..y,
+// z-1..z), read as four quads: planes z-1 and z of the cell (S at the x-y
+// pairs) and the same two shifted by w along the walk axis (clamped to the
+// table).  Along the walk axis this uses the predecessor of the shifted
+// coordinate, which equals the shift of the clamped predecessor except at
+// walk coordinate 0, a cell no query reads (a box reaching below the table
+// on the walk axis takes the quad query); past the high face S repeats.
 __global__ void k_sat_walk(const uint4* __restrict__ q, uint4* __restrict__ out, int sx, int sy, int sz, int axis,
                            int w, long long cells) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= cells) return;
   const int x = (int)(i % sx), y = (int)((i / sx) % sy), z = (int)(i / ((long long)sx * sy));
   const size_t sxy = (size_t)sx * sy;
-  auto S = [&](int X, int Y, int Z) {
+  auto Q = [&](int X, int Y, int Z) {
     X = min(max(X, 0), sx - 1); Y = min(max(Y, 0), sy - 1); Z = min(max(Z, 0), sz - 1);
-    return __ldg(&q[(size_t)X + (size_t)sx * Y + sxy * Z].w);
+    return __ldg(&q[(size_t)X + (size_t)sx * Y + sxy * Z]);
   };
-  unsigned d[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const int X = max(x - 1 + (c & 1), 0), Y = max(y - 1 + ((c >> 1) & 1), 0), Z = max(z - 1 + (c >> 2), 0);
-    d[c] = S(X + (axis == 0 ? w : 0), Y + (axis == 1 ? w : 0), Z + (axis == 2 ? w : 0)) - S(X, Y, Z);
-  }
-  out[2 * i] = make_uint4(d[0], d[1], d[2], d[3]);
-  out[2 * i + 1] = make_uint4(d[4], d[5], d[6], d[7]);
+  const int z0 = max(z - 1, 0);
+  const uint4 lo0 = Q(x, y, z0), lo1 = Q(x, y, z);
+  const int dx = axis == 0 ? w : 0, dy = axis == 1 ? w : 0;
+  const uint4 up0 = Q(x + dx, y + dy, axis == 2 ? z0 + w : z0), up1 = Q(x + dx, y + dy, axis == 2 ? z + w : z);
+  out[2 * i] = make_uint4(up0.x - lo0.x, up0.y - lo0.y, up0.z - lo0.z, up0.w - lo0.w);
+  out[2 * i + 1] = make_uint4(up1.x - lo1.x, up1.y - lo1.y, up1.z - lo1.z, up1.w - lo1.w);
 }
 
 cudaError_t launch_sat_walk(const uint4* quads, uint4* out, int sx, int sy, int sz, int axis, int w,
