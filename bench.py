@@ -824,7 +824,7 @@ def run_ours(args):
         tw.value, th.value, tv.value = t[0], t[1], t[2]
     else:
         abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
-                                   C.sizeof(params), wl.width, wl.height, 2, C.byref(tw), C.byref(th),
+                                   C.sizeof(params), wl.width, wl.height, 3, C.byref(tw), C.byref(th),
                                    C.byref(tv), C.byref(tms)), ctx.h)
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
               "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),

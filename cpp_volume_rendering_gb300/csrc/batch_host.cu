@@ -111,6 +111,7 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   bool all_compact = c->compact_sat;
   std::vector<std::vector<float4>> tables;
   std::vector<SurJob> sur;
+  unsigned long long sur_positions = 0;
   const int keep = c->cur_slot;
   cvr_status st = CVR_OK;
   for (int oi = 0; oi < n_jobs && st == CVR_OK; ++oi) {
@@ -154,9 +155,18 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
       if (!sur.empty() && tex != b->sur_tex) { st = fail(c, CVR_ERR_INVALID_ARG, "cvr_batch_create: mixed sampling"); break; }
       b->sur_tex = tex;
       J.f = f;
+      const SurSpiral o = sur_spiral(f);
+      J.cx = o.cx;
+      J.cy = o.cy;
       J.tiles_x = (j.width + 7) / 8;
-      J.first_tile = b->sur_rays / 32u;
-      b->sur_rays += (unsigned)J.tiles_x * (unsigned)((j.height + 3) / 4) * 32u;
+      J.tiles_y = (j.height + 3) / 4;
+      J.first_tile = (unsigned)sur_positions;
+      sur_positions += o.positions;
+      if (sur_positions * 32ull > 0xFFFFFFF0ull) {
+        st = fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: more than 2^32 surrogate rays");
+        break;
+      }
+      b->sur_rays = (unsigned)(sur_positions * 32ull);
       sur.push_back(J);
     }
   }

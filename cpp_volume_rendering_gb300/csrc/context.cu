@@ -1061,71 +1061,77 @@ static cvr_status time_config(cvr_ctx* c, int method, const cvr_camera* cam, con
 cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr_light* light, const void* params,
                         size_t params_size, int w, int h, int reps, int* btw, int* bth, int* bv, float* bms) {
   if (!c || reps <= 0 || reps > 100) return fail(c, CVR_ERR_INVALID_ARG, "cvr_autotune: bad arguments");
-  // ray tiles from 8x8 to 32x8 (2, 4 and 8 warps) x register variants, then
-  // the warp shape and the volume's layout at the best of those (plain,
-  // bricks of 8^3, 16^3, 32^3, x-y quads; -1 stands for the quads)
+  // Coordinate descent over three groups: ray tile (8x8 to 32x8: 2, 4 and 8
+  // warps) x register variant, warp shape (4x8, 8x4, 16x2 pixels), volume
+  // layout (plain, bricks of 8^3, 16^3, 32^3, x-y quads; -1 stands for the
+  // quads).  Each sweep times every member of a group with the other two
+  // fixed at the best so far; the search stops after a sweep that changes
+  // nothing (at most three).  Each configuration is timed once (memoised).
   static const int tiles[6][2] = {{8, 8}, {16, 8}, {32, 4}, {8, 16}, {32, 8}, {16, 16}};
   static const int bricks[5] = {0, 3, 4, 5, -1};
+  static const int warps[3] = {8, 4, 16};
   float* frame = nullptr;
   cvr_status s = cvr_get_frame_buffer(c, w, h, &frame);
   if (s != CVR_OK) return s;
   const int keep_w = c->tile_w, keep_h = c->tile_h, keep_v = c->variant, keep_b = c->brick_bs;
   const bool keep_q = c->quads;
   const int keep_ww = c->warp_w;
-  float best = 1e30f;
-  int bw = keep_w, bh = keep_h, bvar = keep_v, bb = 0;
+  const bool keep_r = c->refill, keep_st = c->staging;
+  c->refill = false;
+  c->staging = false;
   // register variants: the extinction marchers have a fourth (<= 96 registers)
   const int n_variants = method == CVR_METHOD_EXTINCTION ? 4 : 3;
-  c->brick_bs = 0;
-  c->quads = false;
-  c->warp_w = 8;
-  for (int t = 0; t < 6 && s == CVR_OK; ++t) {
-    for (int v = 0; v < n_variants && s == CVR_OK; ++v) {
+  float timed[6][4][3][5];
+  for (auto& a : timed)
+    for (auto& b : a)
+      for (auto& d : b)
+        for (float& x : d) x = -1.0f;
+  int bt = 1, bvar = 0, bw = 0, bb = 0;  // indices into tiles, variants, warps, bricks
+  float best = 1e30f;
+  auto trial = [&](int t, int v, int wi, int k) {
+    if (s != CVR_OK) return;
+    float& ms = timed[t][v][wi][k];
+    if (ms < 0.0f) {
       c->tile_w = tiles[t][0]; c->tile_h = tiles[t][1]; c->variant = v;
-      float ms = 0.0f;
-      s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
-      if (s == CVR_OK && ms < best) {
-        best = ms;
-        bw = tiles[t][0]; bh = tiles[t][1]; bvar = v;
-      }
+      c->warp_w = warps[wi];
+      c->brick_bs = bricks[k] > 0 ? bricks[k] : 0;
+      c->quads = bricks[k] < 0;
+      float m = 0.0f;
+      s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &m);
+      if (s != CVR_OK) return;
+      ms = m;
     }
-  }
-  c->tile_w = bw; c->tile_h = bh; c->variant = bvar;
-  // warp shapes of 4x8 and 16x2 pixels at that tile
-  int bww = 8;
-  for (int ww : {4, 16}) {
-    if (s != CVR_OK || !warp_fits(bw, bh, ww)) continue;
-    c->warp_w = ww;
-    float ms = 0.0f;
-    s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
-    if (s == CVR_OK && ms < best) {
+    if (ms < best) {
       best = ms;
-      bww = ww;
+      bt = t; bvar = v; bw = wi; bb = k;
     }
-  }
-  c->warp_w = bww;
-  for (int k = 1; k < 5 && s == CVR_OK; ++k) {
-    c->brick_bs = bricks[k] > 0 ? bricks[k] : 0;
-    c->quads = bricks[k] < 0;
-    float ms = 0.0f;
-    s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &ms);
-    if (s == CVR_OK && ms < best) {
-      best = ms;
-      bb = bricks[k];
+  };
+  for (int sweep = 0; sweep < 3 && s == CVR_OK; ++sweep) {
+    const int before[4] = {bt, bvar, bw, bb};
+    for (int t = 0; t < 6; ++t) {
+      const int wi = warp_fits(tiles[t][0], tiles[t][1], warps[bw]) ? bw : 0;
+      for (int v = 0; v < n_variants; ++v) trial(t, v, wi, bb);
     }
+    for (int wi = 0; wi < 3; ++wi)
+      if (warp_fits(tiles[bt][0], tiles[bt][1], warps[wi])) trial(bt, bvar, wi, bb);
+    for (int k = 0; k < 5; ++k) trial(bt, bvar, bw, k);
+    if (before[0] == bt && before[1] == bvar && before[2] == bw && before[3] == bb) break;
   }
   if (s != CVR_OK) {
     c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b; c->quads = keep_q;
     c->warp_w = keep_ww;
+    c->refill = keep_r;
+    c->staging = keep_st;
     return s;
   }
-  c->brick_bs = bb > 0 ? bb : 0;
-  c->quads = bb < 0;
+  c->tile_w = tiles[bt][0]; c->tile_h = tiles[bt][1]; c->variant = bvar;
+  c->warp_w = warps[bw];
+  c->brick_bs = bricks[bb] > 0 ? bricks[bb] : 0;
+  c->quads = bricks[bb] < 0;
+  const int bwt = tiles[bt][0], bht = tiles[bt][1];
   // the persistent ray-refill marcher at each register variant (the tile
   // shape does not apply to it)
-  const bool keep_r = c->refill;
   bool br = false;
-  c->refill = false;
   if (method == CVR_METHOD_PLAIN || method == CVR_METHOD_EXTINCTION || method == CVR_METHOD_CONE_DOS ||
       method == CVR_METHOD_GROUND_TRUTH) {
     for (int v = 0; v < n_variants && s == CVR_OK; ++v) {
@@ -1143,9 +1149,7 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   c->variant = bvar;
   c->refill = br;
   // the plain marcher with shared-memory brick staging (plain layout, its own tile)
-  const bool keep_st = c->staging;
   bool bst = false;
-  c->staging = false;
   if (method == CVR_METHOD_PLAIN && s == CVR_OK && !(c->sampling & CVR_SAMPLING_TEX_VOLUME)) {
     const int kb = c->brick_bs;
     const bool kq = c->quads, kr = c->refill;
@@ -1169,8 +1173,8 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
     c->refill = keep_r;
     return s;
   }
-  if (btw) *btw = bw;
-  if (bth) *bth = bh;
+  if (btw) *btw = bwt;
+  if (bth) *bth = bht;
   if (bv) *bv = bvar;
   if (bms) *bms = best;
   return CVR_OK;

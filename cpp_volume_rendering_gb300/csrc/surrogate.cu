@@ -178,19 +178,36 @@ struct BatchSource {
   unsigned total;
   __device__ __forceinline__ const FrameArgs& f(int j) const { return jobs[j].f; }
   __device__ __forceinline__ const SurArgs& a(int j) const { return jobs[j].a; }
+  __device__ __forceinline__ bool holds(int j, unsigned tile) const {
+    return jobs[j].first_tile <= tile && (j + 1 == n_jobs || jobs[j + 1].first_tile > tile);
+  }
+  // r.job on entry: the job of the thread's previous ray.  Rays are taken in
+  // increasing order, so the position is almost always in that job or the
+  // next; else a binary search for the last job whose first position is <= tile.
   __device__ __forceinline__ void locate(unsigned idx, SurRay& r) const {
     const unsigned tile = idx >> 5;
-    int lo = 0, hi = n_jobs - 1;  // last job whose first tile is <= tile
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (jobs[mid].first_tile <= tile) lo = mid;
-      else hi = mid - 1;
+    int j = r.job < 0 || r.job >= n_jobs ? 0 : r.job;
+    if (!holds(j, tile)) {
+      if (j + 1 < n_jobs && holds(j + 1, tile)) {
+        ++j;
+      } else {
+        int lo = 0, hi = n_jobs - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (jobs[mid].first_tile <= tile) lo = mid;
+          else hi = mid - 1;
+        }
+        j = lo;
+      }
     }
-    const unsigned local = tile - jobs[lo].first_tile;
-    const int tx = jobs[lo].tiles_x, within = (int)(idx & 31u);
-    r.job = lo;
-    r.px = (int)(local % (unsigned)tx) * 8 + (within & 7);
-    r.py = (int)(local / (unsigned)tx) * 4 + (within >> 3);
+    const SurJob& J = jobs[j];
+    int dx, dy;
+    spiral_tile(tile - J.first_tile, dx, dy);
+    const int tx = J.cx + dx, ty = J.cy + dy, within = (int)(idx & 31u);
+    r.job = j;
+    if (tx < 0 || ty < 0 || tx >= J.tiles_x || ty >= J.tiles_y) { r.px = -1; r.py = -1; return; }
+    r.px = tx * 8 + (within & 7);
+    r.py = ty * 4 + (within >> 3);
   }
 };
 
@@ -413,20 +430,39 @@ cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned tota
   return cudaGetLastError();
 }
 
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, int center_x, int center_y,
+SurSpiral sur_spiral(const FrameArgs& f) {
+  // pixel of the projected volume centre (the box is centred on the origin)
+  const float3 d = f3(0.0f, 0.0f, 0.0f) - f.cam.eye;
+  const float zf = dot3(d, f.cam.f);
+  int px = f.W / 2, py = f.H / 2;
+  if (zf > 1e-6f) {
+    const float xn = dot3(d, f.cam.s) / (zf * f.cam.tan_half_fovy * f.cam.aspect);
+    const float yn = dot3(d, f.cam.u) / (zf * f.cam.tan_half_fovy);
+    if (std::isfinite(xn) && std::isfinite(yn) && std::fabs(xn) < 4.0f && std::fabs(yn) < 4.0f) {
+      px = (int)((xn * 0.5f + 0.5f) * (float)f.W);
+      py = (int)((yn * 0.5f + 0.5f) * (float)f.H);
+    }
+  }
+  const int tiles_x = (f.W + 7) / 8, tiles_y = (f.H + 3) / 4;
+  SurSpiral o;
+  o.cx = std::min(std::max(px / 8, 0), tiles_x - 1);
+  o.cy = std::min(std::max(py / 4, 0), tiles_y - 1);
+  const int R = std::max(std::max(o.cx, tiles_x - 1 - o.cx), std::max(o.cy, tiles_y - 1 - o.cy));
+  o.positions = (unsigned long long)(2 * R + 1) * (unsigned long long)(2 * R + 1);
+  return o;
+}
+
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const SurSpiral& order,
                              unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
   auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
-  const int tiles_x = (f.W + 7) / 8, tiles_y = (f.H + 3) / 4;
-  const int cx = min(max(center_x / 8, 0), tiles_x - 1), cy = min(max(center_y / 4, 0), tiles_y - 1);
-  const int R = max(max(cx, tiles_x - 1 - cx), max(cy, tiles_y - 1 - cy));
-  const unsigned long long spiral = (unsigned long long)(2 * R + 1) * (unsigned long long)(2 * R + 1) * 32ull;
+  const unsigned long long spiral = order.positions * 32ull;
   if (spiral > 0xFFFFFFF0ull) return cudaErrorInvalidValue;
-  const unsigned rays = (unsigned)tiles_x * (unsigned)tiles_y * 32u;
+  const unsigned rays = (unsigned)((f.W + 7) / 8) * (unsigned)((f.H + 3) / 4) * 32u;
   unsigned ctas = 0;
   cudaError_t e = surrogate_grid(kern, smem, rays, f.variant, &ctas);
   if (e != cudaSuccess) return e;
-  kern<<<ctas, 128, smem, st>>>(f, a, cx, cy, (unsigned)spiral, work, err);
+  kern<<<ctas, 128, smem, st>>>(f, a, order.cx, order.cy, (unsigned)spiral, work, err);
   return cudaGetLastError();
 }
 

@@ -210,22 +210,33 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
 struct SurJob {
   FrameArgs f;
   SurArgs a;
-  unsigned first_tile;  // batch-wide index of the job's first 8x4-pixel tile
-  int tiles_x;
+  unsigned first_tile;  // batch-wide index of the job's first spiral position
+  int cx, cy;           // the job's spiral centre tile
+  int tiles_x, tiles_y;
 };
 
-// Persistent launch over all rays of all jobs (jobs ordered by first_tile;
-// total_rays = 32 x all tiles), rays taken from *work (zeroed before).
+// Ray order of a surrogate frame: 8x4-pixel tiles in the square spiral around
+// the tile of the projected volume centre (long rays first, neighbouring
+// tiles together); positions = the tiles of the spiral's bounding square
+// (those outside the image are skipped).
+struct SurSpiral {
+  int cx, cy;
+  unsigned long long positions;
+};
+SurSpiral sur_spiral(const FrameArgs& f);
+
+// Persistent launch over all rays of all jobs (jobs ordered by first_tile,
+// each job's rays in its spiral order; total_rays = 32 x all spiral
+// positions), rays taken from *work (zeroed before).
 cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
                                    int variant, unsigned int* work, int* err, cudaStream_t st);
 
 // The surrogate-shaded marcher: persistent CTAs take rays from *work (zeroed
-// before the launch) in 8x4-pixel tiles, in a square spiral around the tile
-// of pixel (center_x, center_y) (the projected volume centre: long rays
-// first, neighbouring tiles together); every round, each thread advances its
-// ray to the next shaded sample, the CTA evaluates the network for its 128
-// samples on the tensor cores, and each thread composites its sample.
-cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, int center_x, int center_y,
+// before the launch) in 8x4-pixel tiles in the frame's spiral order; every
+// round, each thread advances its ray to the next shaded sample, the CTA
+// evaluates the network for its 128 samples on the tensor cores, and each
+// thread composites its sample.
+cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const SurSpiral& order,
                              unsigned int* work, int* err, cudaStream_t st);
 
 }  // namespace cvr

@@ -209,20 +209,8 @@ cvr_status render_surrogate(cvr_ctx* c, const FrameArgs& f, const cvr_gt_params*
   bool tex = false;
   cvr_status st = sur_job_args(c, p, light, &a, &tex);
   if (st != CVR_OK) return st;
-  // pixel of the projected volume centre (the box is centred on the origin)
-  const float3 d = f3(0.0f, 0.0f, 0.0f) - f.cam.eye;
-  const float zf = dot3(d, f.cam.f);
-  int cx = f.W / 2, cy = f.H / 2;
-  if (zf > 1e-6f) {
-    const float xn = dot3(d, f.cam.s) / (zf * f.cam.tan_half_fovy * f.cam.aspect);
-    const float yn = dot3(d, f.cam.u) / (zf * f.cam.tan_half_fovy);
-    if (std::isfinite(xn) && std::isfinite(yn) && std::fabs(xn) < 4.0f && std::fabs(yn) < 4.0f) {
-      cx = (int)((xn * 0.5f + 0.5f) * (float)f.W);
-      cy = (int)((yn * 0.5f + 0.5f) * (float)f.H);
-    }
-  }
   CK(c, cudaMemsetAsync(c->sur->counter, 0, sizeof(unsigned int), c->stream));
-  CK(c, launch_surrogate(f, a, tex, cx, cy, c->sur->counter, c->mlp->err, c->stream));
+  CK(c, launch_surrogate(f, a, tex, sur_spiral(f), c->sur->counter, c->mlp->err, c->stream));
   return CVR_OK;
 }
 
