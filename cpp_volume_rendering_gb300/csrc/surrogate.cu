@@ -375,16 +375,19 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
   mlp_cta_end(ms.tmem, kSurTmemCols);
 }
 
-template <bool TEX>
-__global__ void __launch_bounds__(128, 5) k_march_surrogate(FrameArgs f, SurArgs a, int cx, int cy, unsigned total,
-                                                            unsigned int* work, int* err) {
+// MINB: resident CTAs per SM the register budget is cut for (5: at most 96
+// registers, for the variants that run as many CTAs as fit; 4: at most 128,
+// for the variants capped at 4 or 3 CTAs per SM).
+template <bool TEX, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_march_surrogate(FrameArgs f, SurArgs a, int cx, int cy, unsigned total,
+                                                               unsigned int* work, int* err) {
   SingleSource s{f, a, cx, cy, (f.W + 7) >> 3, (f.H + 3) >> 2, total};
   sur_march<TEX, false>(s, f.tf, f.tf_n, a.packed, work, err);
 }
 
-template <bool TEX>
-__global__ void __launch_bounds__(128, 5) k_batch_surrogate(const SurJob* __restrict__ jobs, int n_jobs,
-                                                            unsigned total_rays, unsigned int* work, int* err) {
+template <bool TEX, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_batch_surrogate(const SurJob* __restrict__ jobs, int n_jobs,
+                                                               unsigned total_rays, unsigned int* work, int* err) {
   BatchSource s{jobs, n_jobs, total_rays};
   sur_march<TEX, true>(s, jobs[0].f.tf, jobs[0].f.tf_n, jobs[0].a.packed, work, err);
 }
@@ -422,7 +425,9 @@ static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, int varian
 cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
                                    int variant, unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * tf_n + 16;
-  auto kern = tex ? k_batch_surrogate<true> : k_batch_surrogate<false>;
+  const bool wide = variant == 1 || variant == 3;
+  auto kern = tex ? (wide ? k_batch_surrogate<true, 5> : k_batch_surrogate<true, 4>)
+                  : (wide ? k_batch_surrogate<false, 5> : k_batch_surrogate<false, 4>);
   unsigned ctas = 0;
   cudaError_t e = surrogate_grid(kern, smem, total_rays, variant, &ctas);
   if (e != cudaSuccess) return e;
@@ -455,7 +460,9 @@ SurSpiral sur_spiral(const FrameArgs& f) {
 cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const SurSpiral& order,
                              unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
-  auto kern = tex ? k_march_surrogate<true> : k_march_surrogate<false>;
+  const bool wide = f.variant == 1 || f.variant == 3;
+  auto kern = tex ? (wide ? k_march_surrogate<true, 5> : k_march_surrogate<true, 4>)
+                  : (wide ? k_march_surrogate<false, 5> : k_march_surrogate<false, 4>);
   const unsigned long long spiral = order.positions * 32ull;
   if (spiral > 0xFFFFFFF0ull) return cudaErrorInvalidValue;
   const unsigned rays = (unsigned)((f.W + 7) / 8) * (unsigned)((f.H + 3) / 4) * 32u;
