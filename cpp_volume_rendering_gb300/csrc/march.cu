@@ -154,6 +154,7 @@ static cudaError_t launch_persistent(K kern, size_t smem, cudaStream_t st, Args.
   if (smem > 48 * 1024 &&
       (e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
     return e;
+  if ((e = carve_l1(kern, 128, smem)) != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
@@ -258,6 +259,7 @@ static cudaError_t launch_batch_t(const BatchExtJob* jobs, int n_jobs, unsigned 
                       : k_batch_extinction<NT, MINB, false, false>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
+  if ((e = carve_l1(kern, NT, smem)) != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
@@ -297,28 +299,35 @@ cudaError_t launch_batch_extinction(const BatchExtJob* jobs, int n_jobs, unsigne
 }
 
 template <int NT, int MINB>
-static void launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+static cudaError_t launch_extinction_t(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
+                                       cudaStream_t st) {
   const bool c = e.sat.sat32 != nullptr;
   if (table) {
     size_t sm = sizeof(float4) * (f.tf_n + 3 * table->n);
     const bool a = c && table->aligned && (e.ao_aligned || !e.apply_occ);
-    if (a) k_march_extinction_dir<NT, MINB, true, true><<<grid_of(f), NT, sm, st>>>(f, e, *table);
-    else if (c) k_march_extinction_dir<NT, MINB, true, false><<<grid_of(f), NT, sm, st>>>(f, e, *table);
-    else k_march_extinction_dir<NT, MINB, false, false><<<grid_of(f), NT, sm, st>>>(f, e, *table);
+    auto kern = a ? k_march_extinction_dir<NT, MINB, true, true>
+                  : (c ? k_march_extinction_dir<NT, MINB, true, false> : k_march_extinction_dir<NT, MINB, false, false>);
+    const cudaError_t err = carve_l1(kern, NT, sm);
+    if (err != cudaSuccess) return err;
+    kern<<<grid_of(f), NT, sm, st>>>(f, e, *table);
   } else {
     size_t sm = sizeof(float4) * f.tf_n;
-    if (c) k_march_extinction<NT, MINB, true><<<grid_of(f), NT, sm, st>>>(f, e);
-    else k_march_extinction<NT, MINB, false><<<grid_of(f), NT, sm, st>>>(f, e);
+    auto kern = c ? k_march_extinction<NT, MINB, true> : k_march_extinction<NT, MINB, false>;
+    const cudaError_t err = carve_l1(kern, NT, sm);
+    if (err != cudaSuccess) return err;
+    kern<<<grid_of(f), NT, sm, st>>>(f, e);
   }
+  return cudaGetLastError();
 }
 
 template <int NT>
-static void launch_extinction_nt(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table, cudaStream_t st) {
+static cudaError_t launch_extinction_nt(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
+                                        cudaStream_t st) {
   switch (f.variant) {
-    case 1: launch_extinction_t<NT, minb_of<NT>(1)>(f, e, table, st); break;
-    case 2: launch_extinction_t<NT, minb_of<NT>(2)>(f, e, table, st); break;
-    case 3: launch_extinction_t<NT, minb_of<NT>(3)>(f, e, table, st); break;
-    default: launch_extinction_t<NT, 1>(f, e, table, st); break;
+    case 1: return launch_extinction_t<NT, minb_of<NT>(1)>(f, e, table, st);
+    case 2: return launch_extinction_t<NT, minb_of<NT>(2)>(f, e, table, st);
+    case 3: return launch_extinction_t<NT, minb_of<NT>(3)>(f, e, table, st);
+    default: return launch_extinction_t<NT, 1>(f, e, table, st);
   }
 }
 
@@ -347,11 +356,10 @@ cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const Shadow
     }
   }
   switch (threads_of(f)) {
-    case 64: launch_extinction_nt<64>(f, e, table, st); break;
-    case 256: launch_extinction_nt<256>(f, e, table, st); break;
-    default: launch_extinction_nt<128>(f, e, table, st); break;
+    case 64: return launch_extinction_nt<64>(f, e, table, st);
+    case 256: return launch_extinction_nt<256>(f, e, table, st);
+    default: return launch_extinction_nt<128>(f, e, table, st);
   }
-  return cudaGetLastError();
 }
 
 static cudaError_t launch_dos_k(void (*kern)(DosArgs, FrameArgs), int nt, const FrameArgs& f, const DosArgs& d,
@@ -360,6 +368,8 @@ static cudaError_t launch_dos_k(void (*kern)(DosArgs, FrameArgs), int nt, const 
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
+  cudaError_t e = carve_l1(kern, nt, sm);
+  if (e != cudaSuccess) return e;
   kern<<<grid_of(f), nt, sm, st>>>(d, f);
   return cudaGetLastError();
 }
@@ -404,6 +414,8 @@ static cudaError_t launch_gt_t(const FrameArgs& f, const GtArgs& g, size_t sm, c
     cudaError_t e = cudaFuncSetAttribute(k_march_gt<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
   }
+  cudaError_t e = carve_l1(k_march_gt<NT>, NT, sm);
+  if (e != cudaSuccess) return e;
   k_march_gt<NT><<<grid_of(f), NT, sm, st>>>(g, f);
   return cudaGetLastError();
 }

@@ -3,6 +3,10 @@
 
 #include "cvr_device.cuh"
 
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 namespace cvr {
 
 #define CVR_MAX_GT_RAYS 256
@@ -139,6 +143,37 @@ cudaError_t resident_ctas(K kern, int threads, size_t dyn_smem, int* out) {
   if (regs_cta > 0) n = n < regs_sm / regs_cta ? n : regs_sm / regs_cta;
   n = n < threads_sm / threads ? n : threads_sm / threads;
   *out = n < 1 ? 1 : n;
+  return cudaSuccess;
+}
+
+// Shared-memory carveout of kern sized to the CTAs resident_ctas lets reside,
+// so that the rest of the SM's unified L1 / shared storage serves as L1 cache
+// (with no preference the driver reserves shared memory for as many CTAs as
+// the shared memory alone would allow, e.g. 100 KB where the registers let 4
+// CTAs of 11.6 KB reside).  Set once per device, kernel and size.
+template <class K>
+cudaError_t carve_l1(K kern, int threads, size_t dyn_smem) {
+  static std::mutex mu;
+  static std::vector<std::tuple<int, const void*, size_t>> done;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const auto key = std::make_tuple(dev, reinterpret_cast<const void*>(kern), dyn_smem);
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& k : done)
+    if (k == key) return cudaSuccess;
+  int n = 0, smem_sm = 0, reserved = 0;
+  if ((e = resident_ctas(kern, threads, dyn_smem, &n)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev)) != cudaSuccess) return e;
+  cudaFuncAttributes fa{};
+  if ((e = cudaFuncGetAttributes(&fa, kern)) != cudaSuccess) return e;
+  const size_t need = (size_t)n * (dyn_smem + fa.sharedSizeBytes + (size_t)reserved);
+  int pct = (int)((need * 100 + (size_t)smem_sm - 1) / (size_t)smem_sm);
+  pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+  if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, pct)) != cudaSuccess) return e;
+  if (done.size() >= 1024) done.clear();
+  done.push_back(key);
   return cudaSuccess;
 }
 

@@ -376,8 +376,10 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
 }
 
 // MINB: resident CTAs per SM the register budget is cut for (5: at most 96
-// registers, for the variants that run as many CTAs as fit; 4: at most 128,
-// for the variants capped at 4 or 3 CTAs per SM).
+// registers; 4: at most 128).  The single-frame marcher runs at 5 for every
+// variant (measured faster than 4 at the 4-CTA variant); the batch marcher,
+// which keeps its job's descriptor fields live, takes 4 where its variant
+// runs at most 4 CTAs per SM (at 5 it spills).
 template <bool TEX, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_march_surrogate(FrameArgs f, SurArgs a, int cx, int cy, unsigned total,
                                                                unsigned int* work, int* err) {
@@ -460,9 +462,7 @@ SurSpiral sur_spiral(const FrameArgs& f) {
 cudaError_t launch_surrogate(const FrameArgs& f, const SurArgs& a, bool tex, const SurSpiral& order,
                              unsigned int* work, int* err, cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * f.tf_n + 16;
-  const bool wide = f.variant == 1 || f.variant == 3;
-  auto kern = tex ? (wide ? k_march_surrogate<true, 5> : k_march_surrogate<true, 4>)
-                  : (wide ? k_march_surrogate<false, 5> : k_march_surrogate<false, 4>);
+  auto kern = tex ? k_march_surrogate<true, 5> : k_march_surrogate<false, 5>;
   const unsigned long long spiral = order.positions * 32ull;
   if (spiral > 0xFFFFFFF0ull) return cudaErrorInvalidValue;
   const unsigned rays = (unsigned)((f.W + 7) / 8) * (unsigned)((f.H + 3) / 4) * 32u;
