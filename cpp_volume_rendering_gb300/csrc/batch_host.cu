@@ -3,6 +3,7 @@
 // captured with the resets of its counters in one CUDA graph.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <vector>
 
@@ -20,11 +21,9 @@ struct cvr_batch {
   int ext_variant = 0;
   int ext_threads = 128;
   float4* d_tables = nullptr;
-  SurJob* d_sur = nullptr;
   int n_sur = 0;
-  unsigned sur_rays = 0;
   bool sur_tex = false;
-  unsigned int* d_counters = nullptr;  // [0] extinction tiles, [1] surrogate rays
+  unsigned int* d_counters = nullptr;  // [0] extinction tiles, [1 + k] surrogate rays of launch k
   unsigned long long* d_stats = nullptr;  // 3 per job, in the caller's job order
   bool ext_compact = false;
   bool ext_aligned = false;  // every job: an aligned shadow table and aligned AO boxes (or AO off)
@@ -34,7 +33,7 @@ struct cvr_batch {
   cudaGraphExec_t graph = nullptr;
   ~cvr_batch() {
     if (graph) cudaGraphExecDestroy(graph);
-    void* bufs[] = {d_ext, d_tables, d_sur, d_counters, d_stats};
+    void* bufs[] = {d_ext, d_tables, d_counters, d_stats};
     for (void* p : bufs)
       if (p) cudaFree(p);
     for (uint4* p : sat32)
@@ -104,13 +103,12 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   std::stable_sort(order.begin(), order.end(),
                    [&](int x, int y) { return job_cost(jobs[x], c) > job_cost(jobs[y], c); });
   CK(c, cudaMalloc((void**)&b->d_stats, sizeof(unsigned long long) * 3 * n_jobs));
-  CK(c, cudaMalloc((void**)&b->d_counters, sizeof(unsigned int) * 2));
   std::vector<BatchExtJob> ext;
   std::vector<int> ext_slot;
   double slot_vmax[CVR_MAX_VOLUMES] = {};
   bool all_compact = c->compact_sat;
   std::vector<std::vector<float4>> tables;
-  std::vector<SurJob> sur;
+  std::vector<SurLaunch> sur;  // the surrogate jobs in launches of up to kSurLaunchJobs
   unsigned long long sur_positions = 0;
   const int keep = c->cur_slot;
   cvr_status st = CVR_OK;
@@ -160,14 +158,21 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
       J.cy = o.cy;
       J.tiles_x = (j.width + 7) / 8;
       J.tiles_y = (j.height + 3) / 4;
+      if (sur.empty() || sur.back().n_jobs == kSurLaunchJobs) {
+        sur.emplace_back();
+        std::memset(&sur.back(), 0, sizeof(SurLaunch));
+        sur_positions = 0;
+      }
+      SurLaunch& L = sur.back();
       J.first_tile = (unsigned)sur_positions;
       sur_positions += o.positions;
       if (sur_positions * 32ull > 0xFFFFFFF0ull) {
-        st = fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: more than 2^32 surrogate rays");
+        st = fail(c, CVR_ERR_UNSUPPORTED, "cvr_batch_create: more than 2^32 surrogate rays in one launch");
         break;
       }
-      b->sur_rays = (unsigned)(sur_positions * 32ull);
-      sur.push_back(J);
+      L.total = (unsigned)(sur_positions * 32ull);
+      L.jobs[L.n_jobs++] = J;
+      ++b->n_sur;
     }
   }
   // Compact SATs owned by the batch (a later frame may rebuild the context's
@@ -232,7 +237,6 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   b->ext_variant = c->variant;
   b->ext_threads = (c->tile_w / 8) * (c->tile_h / 4) * 32;
   b->n_ext = (int)ext.size();
-  b->n_sur = (int)sur.size();
   if (b->n_ext) {
     // shadow tables: one region per job, pointers patched in
     size_t total = 0;
@@ -255,21 +259,19 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
     CK(c, cudaMalloc((void**)&b->d_ext, sizeof(BatchExtJob) * ext.size()));
     CK(c, cudaMemcpy(b->d_ext, ext.data(), sizeof(BatchExtJob) * ext.size(), cudaMemcpyHostToDevice));
   }
-  if (b->n_sur) {
-    CK(c, cudaMalloc((void**)&b->d_sur, sizeof(SurJob) * sur.size()));
-    CK(c, cudaMemcpy(b->d_sur, sur.data(), sizeof(SurJob) * sur.size(), cudaMemcpyHostToDevice));
-  }
+  const size_t n_counters = 1 + sur.size();
+  CK(c, cudaMalloc((void**)&b->d_counters, sizeof(unsigned int) * n_counters));
   // capture: counter and statistics resets, then the persistent launches
   cudaGraph_t g = nullptr;
   CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
-  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * 2, c->stream);
+  cudaError_t e = cudaMemsetAsync(b->d_counters, 0, sizeof(unsigned int) * n_counters, c->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(b->d_stats, 0, sizeof(unsigned long long) * 3 * n_jobs, c->stream);
   if (e == cudaSuccess && b->n_ext)
     e = launch_batch_extinction(b->d_ext, b->n_ext, b->ext_blocks, b->d_counters, c->tf_n, b->ext_max_table,
                                 b->ext_threads, b->ext_variant, b->ext_compact, b->ext_aligned, c->stream);
-  if (e == cudaSuccess && b->n_sur)
-    e = launch_batch_surrogate(b->d_sur, b->n_sur, b->sur_rays, c->tf_n, b->sur_tex, b->ext_variant,
-                               b->d_counters + 1, c->mlp->err, c->stream);
+  for (size_t k = 0; k < sur.size() && e == cudaSuccess; ++k)
+    e = launch_batch_surrogate(sur[k], c->tf_n, b->sur_tex, b->ext_variant, b->d_counters + 1 + k, c->mlp->err,
+                               c->stream);
   cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
   if (e != cudaSuccess || e2 != cudaSuccess) {
     if (g) cudaGraphDestroy(g);

@@ -388,10 +388,10 @@ __global__ void __launch_bounds__(128, MINB) k_march_surrogate(FrameArgs f, SurA
 }
 
 template <bool TEX, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_batch_surrogate(const SurJob* __restrict__ jobs, int n_jobs,
-                                                               unsigned total_rays, unsigned int* work, int* err) {
-  BatchSource s{jobs, n_jobs, total_rays};
-  sur_march<TEX, true>(s, jobs[0].f.tf, jobs[0].f.tf_n, jobs[0].a.packed, work, err);
+__global__ void __launch_bounds__(128, MINB) k_batch_surrogate(const __grid_constant__ SurLaunch L, unsigned int* work,
+                                                               int* err) {
+  BatchSource s{L.jobs, L.n_jobs, L.total};
+  sur_march<TEX, true>(s, L.jobs[0].f.tf, L.jobs[0].f.tf_n, L.jobs[0].a.packed, work, err);
 }
 
 // Persistent grid.  CTAs per SM: at most 4 for variant 0, the most that fit
@@ -424,16 +424,16 @@ static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, int varian
   return cudaSuccess;
 }
 
-cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
-                                   int variant, unsigned int* work, int* err, cudaStream_t st) {
+cudaError_t launch_batch_surrogate(const SurLaunch& L, int tf_n, bool tex, int variant, unsigned int* work, int* err,
+                                   cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * tf_n + 16;
   const bool wide = variant == 1 || variant == 3;
   auto kern = tex ? (wide ? k_batch_surrogate<true, 5> : k_batch_surrogate<true, 4>)
                   : (wide ? k_batch_surrogate<false, 5> : k_batch_surrogate<false, 4>);
   unsigned ctas = 0;
-  cudaError_t e = surrogate_grid(kern, smem, total_rays, variant, &ctas);
+  cudaError_t e = surrogate_grid(kern, smem, L.total, variant, &ctas);
   if (e != cudaSuccess) return e;
-  kern<<<ctas, 128, smem, st>>>(jobs, n_jobs, total_rays, work, err);
+  kern<<<ctas, 128, smem, st>>>(L, work, err);
   return cudaGetLastError();
 }
 

@@ -225,11 +225,22 @@ struct SurSpiral {
 };
 SurSpiral sur_spiral(const FrameArgs& f);
 
-// Persistent launch over all rays of all jobs (jobs ordered by first_tile,
-// each job's rays in its spiral order; total_rays = 32 x all spiral
-// positions), rays taken from *work (zeroed before).
-cudaError_t launch_batch_surrogate(const SurJob* jobs, int n_jobs, unsigned total_rays, int tf_n, bool tex,
-                                   int variant, unsigned int* work, int* err, cudaStream_t st);
+// One persistent launch of a batch's surrogate jobs: up to kSurLaunchJobs
+// jobs whose descriptors are the launch's parameters (the constant bank, read
+// as the single-frame marcher reads its own), ordered by first_tile (relative
+// to the launch), each job's rays in its spiral order; total = 32 x the
+// spiral positions of its jobs.
+constexpr int kSurLaunchJobs = 32;
+struct SurLaunch {
+  int n_jobs;
+  unsigned total;
+  SurJob jobs[kSurLaunchJobs];
+};
+static_assert(sizeof(SurLaunch) <= 32000, "kernel parameters are limited to 32764 bytes");
+
+// Rays taken from *work (zeroed before the launch).
+cudaError_t launch_batch_surrogate(const SurLaunch& L, int tf_n, bool tex, int variant, unsigned int* work, int* err,
+                                   cudaStream_t st);
 
 // The surrogate-shaded marcher: persistent CTAs take rays from *work (zeroed
 // before the launch) in 8x4-pixel tiles in the frame's spiral order; every
