@@ -144,6 +144,7 @@ SIGNATURES = {
     "cvr_set_volume_device": (_I, [_P, _P, _I, _I, _I, _I, _F, _F, _F]),
     "cvr_set_transfer_function": (_I, [_P, _FP, _FP, _I]),
     "cvr_build_sat": (_I, [_P, _D, _I]),
+    "cvr_prepare_sat": (_I, [_P]),
     "cvr_get_sat_info": (_I, [_P, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "cvr_download_sat": (_I, [_P, C.POINTER(C.c_int64)]),
     "cvr_build_ext_pyramid": (_I, [_P, C.POINTER(PyramidParams)]),

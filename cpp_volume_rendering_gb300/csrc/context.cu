@@ -290,6 +290,12 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
       }
     }
   }
+  // the int64 table serves frames without a compact table; the caller of
+  // vmax_out may fall back to it
+  if (vmax_out || !a.sat.sat32) {
+    cvr_status cs = ensure_sat(c);
+    if (cs != CVR_OK) return cs;
+  }
   *eo = a;
   return CVR_OK;
 }
@@ -432,6 +438,16 @@ cvr_status check_kernel_flag(cvr_ctx* c, const char* what) {
   return fail(c, CVR_ERR_TIMEOUT, what);
 }
 
+cvr_status ensure_sat(cvr_ctx* c) {
+  if (!c->sat_ready || !c->sat_pending) return CVR_OK;
+  CK(c, cudaSetDevice(c->device));
+  size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+  CK(c, ensure(c->d_sat, c->sat_cap, cells * sizeof(long long)));
+  CK(c, launch_sat_build(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut, c->d_sat, c->stream));
+  c->sat_pending = false;
+  return CVR_OK;
+}
+
 }  // namespace ctxutil
 }  // namespace cvr
 
@@ -515,6 +531,7 @@ static cvr_status set_volume_common(cvr_ctx* c, const void* src, bool src_device
   c->has_volume = true;
   // Derived tables belong to the previous volume.
   c->sat_ready = false;
+  c->sat_pending = false;
   c->sat32_F = kNoCompactSat;
   c->pyr_ready = false;
   c->tex.vol_valid = false;
@@ -582,20 +599,28 @@ cvr_status cvr_build_sat(cvr_ctx* c, const double* ext, int n_values) {
   F = std::min(52, std::max(0, F));
   std::vector<long long> q(n_values);
   double scale = std::ldexp(1.0, F);
-  for (int i = 0; i < n_values; ++i) q[i] = std::llround(ext[i] * scale);
+  // llround of a non-negative value: below 2^52, v + 0.5 is exact and its
+  // truncation rounds halves up; from 2^52 on, v is an integer already
+  for (int i = 0; i < n_values; ++i) {
+    const double v = ext[i] * scale;
+    q[i] = v < 4503599627370496.0 ? (long long)(v + 0.5) : (long long)v;
+  }
   CK(c, cudaSetDevice(c->device));
   // the table of every possible voxel value (65536 entries covers u8 and u16)
   if (!c->d_lut) CK(c, cudaMalloc((void**)&c->d_lut, sizeof(long long) * 65536));
   // pageable source: staged by the time the call returns, so q may go
   CK(c, cudaMemcpyAsync(c->d_lut, q.data(), sizeof(long long) * n_values, cudaMemcpyHostToDevice, c->stream));
-  size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
-  CK(c, ensure(c->d_sat, c->sat_cap, cells * sizeof(long long)));
-  CK(c, launch_sat_build(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut, c->d_sat, c->stream));
   c->sat_frac_bits = F;
   c->sat_ready = true;
+  c->sat_pending = true;
   c->sat_ext.assign(ext, ext + n_values);
   c->sat32_F = kNoCompactSat;
   return CVR_OK;
+}
+
+cvr_status cvr_prepare_sat(cvr_ctx* c) {
+  if (!c) return CVR_ERR_INVALID_ARG;
+  return ensure_sat(c);
 }
 
 cvr_status cvr_get_sat_info(cvr_ctx* c, int dims[3], int* frac_bits) {
@@ -609,6 +634,8 @@ cvr_status cvr_get_sat_info(cvr_ctx* c, int dims[3], int* frac_bits) {
 cvr_status cvr_download_sat(cvr_ctx* c, int64_t* host) {
   if (!c || !host) return CVR_ERR_INVALID_ARG;
   if (!c->sat_ready) return fail(c, CVR_ERR_NOT_READY, "SAT not built");
+  cvr_status st = ensure_sat(c);
+  if (st != CVR_OK) return st;
   size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
   CK(c, cudaMemcpyAsync(host, c->d_sat, cells * sizeof(long long), cudaMemcpyDeviceToHost, c->stream));
   CK(c, cudaStreamSynchronize(c->stream));

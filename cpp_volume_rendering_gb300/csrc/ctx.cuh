@@ -111,6 +111,7 @@ struct VolSlot {
   long long* d_lut = nullptr;
   int sat_frac_bits = 0;
   bool sat_ready = false;
+  bool sat_pending = false;
   std::vector<double> sat_ext;
   uint4* d_sat32 = nullptr;
   size_t sat32_cap = 0;
@@ -178,7 +179,8 @@ struct cvr_ctx {
   size_t sat_cap = 0;
   long long* d_lut = nullptr;
   int sat_frac_bits = 0;
-  bool sat_ready = false;
+  bool sat_ready = false;    // cvr_build_sat succeeded for the current volume
+  bool sat_pending = false;  // its int64 table is not built yet (ensure_sat)
   // compact SAT (32-bit prefix sums modulo 2^32 at F32 fractional bits) for
   // frames whose boxes are small enough; the extinction table it is built from
   std::vector<double> sat_ext;
@@ -279,6 +281,7 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->d_lut, s.d_lut);
   std::swap(c->sat_frac_bits, s.sat_frac_bits);
   std::swap(c->sat_ready, s.sat_ready);
+  std::swap(c->sat_pending, s.sat_pending);
   std::swap(c->sat_ext, s.sat_ext);
   std::swap(c->d_sat32, s.d_sat32);
   std::swap(c->sat32_cap, s.sat32_cap);
@@ -425,6 +428,8 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
 // when the frame keeps the int64 table.
 cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale);
 cvr_status ensure_walk_table(cvr_ctx* c, int axis, int w, WalkView* out);
+// Enqueues the current volume's pending int64 SAT build (cvr_build_sat defers it).
+cvr_status ensure_sat(cvr_ctx* c);
 // The pieces of it: the fixed point (false: keep the int64 table) and the
 // build of the current volume's compact table into dst.
 bool compact_plan(const std::vector<double>& ext, double vmax, int* F, std::vector<unsigned>* q);

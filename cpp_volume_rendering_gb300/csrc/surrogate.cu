@@ -378,8 +378,7 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
 // MINB: resident CTAs per SM the register budget is cut for (5: at most 96
 // registers; 4: at most 128).  The single-frame marcher runs at 5 for every
 // variant (measured faster than 4 at the 4-CTA variant); the batch marcher,
-// which keeps its job's descriptor fields live, takes 4 where its variant
-// runs at most 4 CTAs per SM (at 5 it spills).
+// which keeps its job's descriptor fields live, takes 4 where 5 would spill.
 template <bool TEX, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_march_surrogate(FrameArgs f, SurArgs a, int cx, int cy, unsigned total,
                                                                unsigned int* work, int* err) {
@@ -427,9 +426,10 @@ static cudaError_t surrogate_grid(K kern, size_t smem, unsigned rays, int varian
 cudaError_t launch_batch_surrogate(const SurLaunch& L, int tf_n, bool tex, int variant, unsigned int* work, int* err,
                                    cudaStream_t st) {
   const size_t smem = kPkFwdBytes + kRowTile + sizeof(float4) * tf_n + 16;
+  // texture-unit features: 124 registers without spills at MINB 4 (at 5 they
+  // spill and the launch ran at 0.7x the single frames), so every variant takes 4
   const bool wide = variant == 1 || variant == 3;
-  auto kern = tex ? (wide ? k_batch_surrogate<true, 5> : k_batch_surrogate<true, 4>)
-                  : (wide ? k_batch_surrogate<false, 5> : k_batch_surrogate<false, 4>);
+  auto kern = tex ? k_batch_surrogate<true, 4> : (wide ? k_batch_surrogate<false, 5> : k_batch_surrogate<false, 4>);
   unsigned ctas = 0;
   cudaError_t e = surrogate_grid(kern, smem, L.total, variant, &ctas);
   if (e != cudaSuccess) return e;

@@ -231,8 +231,14 @@ cvr_status cvr_set_transfer_function(cvr_ctx* ctx, const float* rgbt, const floa
  * ext_per_value[v] = extinction of voxel value v (TransferFunction1D::GetExtN of
  * the normalised value), n_values = 256 (u8) or 65536 (u16).  The SAT is
  * (W+2)(H+2)(D+2), zero border, built on the device by exact int64
- * fixed-point prefix sums. */
+ * fixed-point prefix sums.  The call validates the table and uploads its
+ * fixed-point values; the int64 table itself is built on the context's stream
+ * by the first call that reads it (a frame the compact 32-bit table does not
+ * serve, a batch, cvr_download_sat) or by cvr_prepare_sat.  Frames served by
+ * the compact table never wait for it. */
 cvr_status cvr_build_sat(cvr_ctx* ctx, const double* ext_per_value, int n_values);
+/* Enqueues the build of a pending int64 SAT now (no-op when none is pending). */
+cvr_status cvr_prepare_sat(cvr_ctx* ctx);
 /* Fixed-point scale of the SAT: entry = round(sum * 2^frac_bits). */
 cvr_status cvr_get_sat_info(cvr_ctx* ctx, int dims[3], int* frac_bits);
 /* Copies the SAT to host memory (dims[0]*dims[1]*dims[2] int64). Synchronous. */

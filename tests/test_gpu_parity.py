@@ -139,6 +139,26 @@ def test_sat_bit_exact_and_relative_error(ctx):
     assert np.abs(got - ref).max() / ref.max() <= 1e-9
 
 
+def test_int64_sat_is_built_when_first_read(ctx):
+    # cvr_build_sat defers the int64 table: a frame the compact table serves
+    # does not build it, a later download does, from the latest table; a
+    # volume upload drops the pending build with the table
+    wl = scene.workload("extinction", n=40, image=48)
+    scene.prepare(ctx, wl)
+    ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+    ext = wl.tf.ext_per_value(wl.dtype)
+    ctx.build_sat(ext * 0.5)
+    ctx.build_sat(ext)
+    ctx.render(wl.method, wl.cam, wl.light, wl.params, wl.width, wl.height)
+    sat, F = ctx.sat()
+    q = np.floor(ext * 2.0 ** F + 0.5).astype(np.int64)
+    assert np.array_equal(sat, oracle.sat_i64(wl.volume, q))
+    ctx.set_volume(wl.volume, wl.spacing)
+    with pytest.raises(abi.CvrError):
+        ctx.sat()
+    assert ctx.lib.cvr_prepare_sat(ctx.h) == abi.CVR_OK
+
+
 # (volume dims, base dims, sigma0): the reference geometry (base = half the
 # volume, S0 = 1 voxel), where every level has the separable form; an odd
 # volume over a half base (separable, odd-sized lattices); a base that does
