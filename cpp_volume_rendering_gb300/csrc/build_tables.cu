@@ -81,16 +81,21 @@ __global__ void k_sat_scan_lines(W* __restrict__ sat, int sx, int n_lines_inner,
 // z-scan (in place for the int64 table; fused with the quad layout for the
 // compact one).  Two passes over the table instead of three.
 
-// Pass 1: one CTA per z plane.  Chunks of R rows: a warp scans a row along x
-// (shuffles, carried across 32-cell segments) into shared memory, a thread
-// per column adds the chunk's rows to the running column sum (the y prefix of
-// the rows above), then the chunk is written out row by row (coalesced).
-// Interior cells take lut[voxel(x-1, y-1, z-1)]; the one-cell border is zero.
+// Pass 1: one CTA per z plane, in chunks of R <= kSatChunkRows rows.  Phase A: a
+// thread per column (or per few columns) carries the column's running
+// y-prefix from chunk to chunk (in shared memory); the voxel loads and table
+// lookups of the chunk's rows are issued before the adds, and each row's
+// prefix goes to shared memory.  Phase B: a warp per row
+// scans it along x (shuffles, carried across 32-cell segments) and writes
+// the plane's row out (coalesced).  The y-then-x order gives the same 2D
+// prefix sums (integer adds).  Interior cells take lut[voxel(x-1, y-1, z-1)];
+// the one-cell border is zero.
 constexpr int kSatPlaneThreads = 512;
+constexpr int kSatChunkRows = 16;
 template <class W>
-__global__ void __launch_bounds__(kSatPlaneThreads) k_sat_planes(const void* vox, int dtype, int nx, int ny, int nz,
-                                                                  const W* __restrict__ lut, W* __restrict__ out,
-                                                                  int R) {
+__global__ void __launch_bounds__(kSatPlaneThreads, 2) k_sat_planes(const void* vox, int dtype, int nx, int ny,
+                                                                     int nz, const W* __restrict__ lut,
+                                                                     W* __restrict__ out, int R) {
   extern __shared__ __align__(16) unsigned char sm_sat[];
   const int sx = nx + 2, sy = ny + 2, sz = nz + 2;
   W* chunk = reinterpret_cast<W*>(sm_sat);  // R x sx
@@ -102,57 +107,51 @@ __global__ void __launch_bounds__(kSatPlaneThreads) k_sat_planes(const void* vox
   for (int x = threadIdx.x; x < sx; x += blockDim.x) carry[x] = 0;
   for (int y0 = 0; y0 < sy; y0 += R) {
     const int rows = min(R, sy - y0);
-    __syncthreads();  // the previous chunk is written out; carry initialised
-    for (int r = warp; r < rows; r += warps) {
-      const int y = y0 + r;
-      const bool border_row = border_plane || y == 0 || y == sy - 1;
-      const size_t vrow = border_row ? 0 : ((size_t)(z - 1) * ny + (y - 1)) * (size_t)nx;
-      // the row in segments of 32 cells x kSegs: every segment's voxels, then
-      // every segment's table values, are loaded before the scans, so a row
-      // costs two rounds of memory latency instead of two per segment
-      constexpr int kSegs = 8;
-      W run = 0;
-      for (int base = 0; base < sx; base += 32 * kSegs) {
-        unsigned q[kSegs];
-        W v[kSegs];
-#pragma unroll
-        for (int g = 0; g < kSegs; ++g) {
-          const int x = base + 32 * g + lane;
-          q[g] = 0xffffffffu;
-          if (!border_row && x > 0 && x < sx - 1)
-            q[g] = dtype == 1 ? (unsigned)__ldg(static_cast<const uint8_t*>(vox) + vrow + (x - 1))
-                              : (unsigned)__ldg(static_cast<const uint16_t*>(vox) + vrow + (x - 1));
-        }
-#pragma unroll
-        for (int g = 0; g < kSegs; ++g) v[g] = q[g] != 0xffffffffu ? __ldg(lut + q[g]) : W(0);
-#pragma unroll
-        for (int g = 0; g < kSegs; ++g) {
-          const int x = base + 32 * g + lane;
-          if (base + 32 * g >= sx) break;  // warp-uniform
-          W t = v[g];
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const W n = __shfl_up_sync(0xffffffffu, t, o);
-            if (lane >= o) t += n;
-          }
-          t += run;
-          if (x < sx) chunk[(size_t)r * sx + x] = t;
-          run = __shfl_sync(0xffffffffu, t, 31);
-        }
-      }
-    }
-    __syncthreads();
+#pragma unroll 1
     for (int x = threadIdx.x; x < sx; x += blockDim.x) {
-      W c = carry[x];
-      for (int r = 0; r < rows; ++r) {
-        c += chunk[(size_t)r * sx + x];
-        chunk[(size_t)r * sx + x] = c;
+      const bool col = !border_plane && x > 0 && x < sx - 1;
+      unsigned q[kSatChunkRows];
+#pragma unroll
+      for (int r = 0; r < kSatChunkRows; ++r) {
+        const int y = y0 + r;
+        q[r] = 0xffffffffu;
+        if (col && r < rows && y > 0 && y < sy - 1) {
+          const size_t i = ((size_t)(z - 1) * ny + (y - 1)) * (size_t)nx + (x - 1);
+          q[r] = dtype == 1 ? (unsigned)__ldg(static_cast<const uint8_t*>(vox) + i)
+                            : (unsigned)__ldg(static_cast<const uint16_t*>(vox) + i);
+        }
       }
-      carry[x] = c;
+      W v[kSatChunkRows];
+#pragma unroll
+      for (int r = 0; r < kSatChunkRows; ++r) v[r] = q[r] != 0xffffffffu ? __ldg(lut + q[r]) : W(0);
+      W run = carry[x];
+#pragma unroll
+      for (int r = 0; r < kSatChunkRows; ++r) {
+        if (r >= rows) break;
+        run += v[r];
+        chunk[(size_t)r * sx + x] = run;
+      }
+      carry[x] = run;
     }
     __syncthreads();
-    for (int r = 0; r < rows; ++r)
-      for (int x = threadIdx.x; x < sx; x += blockDim.x) plane[(size_t)(y0 + r) * sx + x] = chunk[(size_t)r * sx + x];
+    for (int r = warp; r < rows; r += warps) {
+      W run = 0;
+      W* dst = plane + (size_t)(y0 + r) * sx;
+      const W* src = chunk + (size_t)r * sx;
+      for (int base = 0; base < sx; base += 32) {
+        const int x = base + lane;
+        W t = x < sx ? src[x] : W(0);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const W n = __shfl_up_sync(0xffffffffu, t, o);
+          if (lane >= o) t += n;
+        }
+        t += run;
+        if (x < sx) dst[x] = t;
+        run = __shfl_sync(0xffffffffu, t, 31);
+      }
+    }
+    __syncthreads();  // the chunk is read before the next one is written
   }
 }
 
@@ -218,20 +217,20 @@ __global__ void __launch_bounds__(kQuadThreads) k_sat_zscan_quads(const unsigned
   }
 }
 
-// Rows per chunk of k_sat_planes for a row of sx cells of type W (0: the
-// plane does not fit shared memory; the line-scan builder below is used).
+// Rows per chunk of k_sat_planes for rows of sx cells of type W: the chunk
+// and the column sums within 200 KB of shared memory (0: fewer than 4 rows
+// fit; the line-scan builder below is used).
 template <class W>
 static int sat_plane_rows(int sx) {
-  const size_t budget = 200 * 1024;
-  const long long r = (long long)(budget / sizeof(W) - (size_t)sx) / sx;
-  return r >= 4 ? (int)std::min<long long>(r, 32) : 0;
+  const long long r = (long long)(200 * 1024 / sizeof(W)) / sx - 1;
+  return r >= 4 ? (int)std::min<long long>(r, kSatChunkRows) : 0;
 }
 
 template <class W>
 static cudaError_t sat_planes(const void* vox, int dtype, int nx, int ny, int nz, const W* lut, W* out, int R,
                               cudaStream_t st) {
   const int sx = nx + 2, sz = nz + 2;
-  const size_t smem = sizeof(W) * ((size_t)R * sx + sx);
+  const size_t smem = sizeof(W) * (size_t)(R + 1) * sx;
   cudaError_t e = cudaFuncSetAttribute(k_sat_planes<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   k_sat_planes<W><<<sz, kSatPlaneThreads, smem, st>>>(vox, dtype, nx, ny, nz, lut, out, R);
