@@ -180,12 +180,16 @@ __global__ void __launch_bounds__(256) k_sat_zscan(W* __restrict__ sat, long lon
 // Pass 2 (compact table): the z-scan of 32 x 8 columns and of their low halo
 // (x0 - 1, y0 - 1) per CTA, writing the predecessor quads of each plane
 // (S at (x-1, y-1), (x, y-1), (x-1, y), (x, y), coordinates clamped to the
-// table) from a shared-memory tile of the plane's running sums.
+// table) from shared-memory tiles of the planes' running sums.  Two groups of
+// kQuadGroup tiles alternate, so one barrier serves kQuadGroup planes: a
+// group is rewritten only after the barrier that follows the reads of its
+// previous planes.
 constexpr int kQuadTileX = 32, kQuadTileY = 8, kQuadHaloCols = (kQuadTileX + 1) * (kQuadTileY + 1);
 constexpr int kQuadThreads = ((kQuadHaloCols + 31) / 32) * 32;
+constexpr int kQuadGroup = 4;
 __global__ void __launch_bounds__(kQuadThreads) k_sat_zscan_quads(const unsigned* __restrict__ P, uint4* __restrict__ out,
                                                                   int sx, int sy, int sz) {
-  __shared__ unsigned tile[kQuadTileY + 1][kQuadTileX + 1];
+  __shared__ unsigned tile[2][kQuadGroup][kQuadTileY + 1][kQuadTileX + 1];
   const int x0 = blockIdx.x * kQuadTileX, y0 = blockIdx.y * kQuadTileY;
   const int t = threadIdx.x;
   const bool owner = t < kQuadHaloCols;
@@ -198,21 +202,31 @@ __global__ void __launch_bounds__(kQuadThreads) k_sat_zscan_quads(const unsigned
   const bool writer = t < kQuadTileX * kQuadTileY && ox < sx && oy < sy;
   uint4* dst = out + (size_t)oy * sx + ox;
   unsigned run = 0;
-  constexpr int B = 16;
+  constexpr int B = 16;  // planes loaded per round (a multiple of kQuadGroup)
+  int grp = 0;
   for (int z0 = 0; z0 < sz; z0 += B) {
     unsigned v[B];
 #pragma unroll
     for (int k = 0; k < B; ++k) v[k] = (owner && z0 + k < sz) ? __ldg(col + (size_t)(z0 + k) * sxy) : 0u;
 #pragma unroll
-    for (int k = 0; k < B; ++k) {
-      if (z0 + k >= sz) break;
-      run += v[k];
-      __syncthreads();  // the previous plane's quads are read
-      if (owner) tile[hy][hx] = run;
+    for (int k0 = 0; k0 < B; k0 += kQuadGroup) {
+      if (z0 + k0 >= sz) break;
+#pragma unroll
+      for (int j = 0; j < kQuadGroup; ++j) {
+        run += v[k0 + j];
+        if (owner) tile[grp][j][hy][hx] = run;
+      }
       __syncthreads();
-      if (writer)
-        dst[(size_t)(z0 + k) * sxy] =
-            make_uint4(tile[ly][lx], tile[ly][lx + 1], tile[ly + 1][lx], tile[ly + 1][lx + 1]);
+      if (writer) {
+#pragma unroll
+        for (int j = 0; j < kQuadGroup; ++j) {
+          const int z = z0 + k0 + j;
+          if (z < sz)
+            dst[(size_t)z * sxy] = make_uint4(tile[grp][j][ly][lx], tile[grp][j][ly][lx + 1], tile[grp][j][ly + 1][lx],
+                                              tile[grp][j][ly + 1][lx + 1]);
+        }
+      }
+      grp ^= 1;
     }
   }
 }
