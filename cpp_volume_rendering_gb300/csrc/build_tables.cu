@@ -515,7 +515,7 @@ static bool pyr_axis(int n_in, int n_out, double tap_texels, PyrAxis* a) {
   a->j0 = (int)std::floor(c0) - 3 * a->t;
   a->g = (n_out - 1) * a->m + 6 * a->t + 1;
   a->n_out = n_out;
-  return true;
+  return a->g <= 65535;  // a grid dimension of the lattice and pass launches
 }
 
 // The plan of level l (l = 0: from the volume): false when it has no separable form.
@@ -542,8 +542,9 @@ long long pyramid_scratch_floats(const VolumeView& vol, const PyramidView& P, fl
   return need;
 }
 
-__device__ __forceinline__ bool pyr_lattice_point(const PyrAxis* A, const int n_in[3], long long idx, float3& u) {
-  const int qx = (int)(idx % A[0].g), qy = (int)((idx / A[0].g) % A[1].g), qz = (int)(idx / ((long long)A[0].g * A[1].g));
+// Lattice point (qx, qy, qz) of a launch whose grid is (x blocks, g_y, g_z).
+__device__ __forceinline__ bool pyr_lattice_point(const PyrAxis* A, const int n_in[3], int qx, int qy, int qz,
+                                                  float3& u) {
   u = f3((float)(A[0].j0 + qx) + A[0].f, (float)(A[1].j0 + qy) + A[1].f, (float)(A[2].j0 + qz) + A[2].f);
   // inside the box [0, S]: texel coordinates in [-0.5, n - 0.5]
   return u.x >= -0.5f && u.y >= -0.5f && u.z >= -0.5f && u.x <= (float)n_in[0] - 0.5f &&
@@ -552,39 +553,44 @@ __device__ __forceinline__ bool pyr_lattice_point(const PyrAxis* A, const int n_
 
 struct PyrAxes { PyrAxis a[3]; };
 
+// The lattice and pass kernels run on (x blocks, y, z) grids: no division of
+// a flat index per element.
 __global__ void k_pyr_lattice_base(VolumeView vol, const float4* __restrict__ tf_rgba, int tf_n, PyrAxes A,
-                                   float* __restrict__ G, long long total) {
+                                   float* __restrict__ G) {
   extern __shared__ float4 sm_tf[];
   for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tf[i] = tf_rgba[i];
   __syncthreads();
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= total) return;
+  const int qx = blockIdx.x * blockDim.x + threadIdx.x, qy = blockIdx.y, qz = blockIdx.z;
+  if (qx >= A.a[0].g) return;
+  const size_t idx = ((size_t)qz * A.a[1].g + qy) * A.a[0].g + qx;
   const int n_in[3] = {vol.nx, vol.ny, vol.nz};
   float3 u;
-  const bool inside = pyr_lattice_point(A.a, n_in, idx, u);
+  const bool inside = pyr_lattice_point(A.a, n_in, qx, qy, qz, u);
   const float3 p = f3((u.x + 0.5f) * vol.spacing.x, (u.y + 0.5f) * vol.spacing.y, (u.z + 0.5f) * vol.spacing.z);
   G[idx] = inside ? tf_alpha(sm_tf, tf_n, sample_volume(vol, p)) : 0.0f;
 }
 
-__global__ void k_pyr_lattice_level(PyramidView P, int l_in, PyrAxes A, float* __restrict__ G, long long total) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= total) return;
+__global__ void k_pyr_lattice_level(PyramidView P, int l_in, PyrAxes A, float* __restrict__ G) {
+  const int qx = blockIdx.x * blockDim.x + threadIdx.x, qy = blockIdx.y, qz = blockIdx.z;
+  if (qx >= A.a[0].g) return;
+  const size_t idx = ((size_t)qz * A.a[1].g + qy) * A.a[0].g + qx;
   const int* n_in = P.dims[l_in];
   float3 u;
-  const bool inside = pyr_lattice_point(A.a, n_in, idx, u);
+  const bool inside = pyr_lattice_point(A.a, n_in, qx, qy, qz, u);
   const float3 p = f3((u.x + 0.5f) * (P.grid.x / (float)n_in[0]), (u.y + 0.5f) * (P.grid.y / (float)n_in[1]),
                       (u.z + 0.5f) * (P.grid.z / (float)n_in[2]));
   G[idx] = inside ? pyr_sample_level(P, l_in, p) : 0.0f;
 }
 
 // One 7-tap pass along axis ax of an (nx, ny, nz) array: out has n_out cells
-// along that axis, out[i] = sum_k w[k] in[i m + (k + 3) t].
+// along that axis, out[i] = sum_k w[k] in[i m + (k + 3) t].  Grid: (x blocks
+// of the output's x extent, its y extent, its z extent).
 __global__ void k_pyr_pass(const float* __restrict__ in, int nx, int ny, int nz, int ax, PyrAxis a, PyrWeights w,
-                           float* __restrict__ out, long long total) {
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (idx >= total) return;
+                           float* __restrict__ out) {
   const int ox = ax == 0 ? a.n_out : nx, oy = ax == 1 ? a.n_out : ny;
-  const int x = (int)(idx % ox), y = (int)((idx / ox) % oy), z = (int)(idx / ((long long)ox * oy));
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if (x >= ox) return;
+  const size_t idx = ((size_t)z * oy + y) * ox + x;
   const int i = ax == 0 ? x : (ax == 1 ? y : z);
   const long long stride = ax == 0 ? 1 : (ax == 1 ? (long long)nx : (long long)nx * ny);
   const long long base = (ax == 0 ? 0 : x) + (ax == 1 ? 0 : (long long)y * nx) + (ax == 2 ? 0 : (long long)z * nx * ny);
@@ -599,11 +605,10 @@ static cudaError_t pyr_separable(const PyrAxis A[3], float* G, float* T1, float*
   double sum = 0.0;
   for (int k = -3; k <= 3; ++k) sum += std::exp(-0.5 * k * k);
   for (int k = -3; k <= 3; ++k) w.w[k + 3] = (float)(std::exp(-0.5 * k * k) / sum);
-  const long long n1 = (long long)A[0].n_out * A[1].g * A[2].g, n2 = (long long)A[0].n_out * A[1].n_out * A[2].g;
-  const long long n3 = (long long)A[0].n_out * A[1].n_out * A[2].n_out;
-  k_pyr_pass<<<(unsigned)((n1 + 255) / 256), 256, 0, st>>>(G, A[0].g, A[1].g, A[2].g, 0, A[0], w, T1, n1);
-  k_pyr_pass<<<(unsigned)((n2 + 255) / 256), 256, 0, st>>>(T1, A[0].n_out, A[1].g, A[2].g, 1, A[1], w, T2, n2);
-  k_pyr_pass<<<(unsigned)((n3 + 255) / 256), 256, 0, st>>>(T2, A[0].n_out, A[1].n_out, A[2].g, 2, A[2], w, out, n3);
+  const unsigned bx_n = (unsigned)(A[0].n_out + 127) / 128;  // every pass's output has n_out along x
+  k_pyr_pass<<<dim3(bx_n, A[1].g, A[2].g), 128, 0, st>>>(G, A[0].g, A[1].g, A[2].g, 0, A[0], w, T1);
+  k_pyr_pass<<<dim3(bx_n, A[1].n_out, A[2].g), 128, 0, st>>>(T1, A[0].n_out, A[1].g, A[2].g, 1, A[1], w, T2);
+  k_pyr_pass<<<dim3(bx_n, A[1].n_out, A[2].n_out), 128, 0, st>>>(T2, A[0].n_out, A[1].n_out, A[2].g, 2, A[2], w, out);
   return cudaGetLastError();
 }
 
@@ -624,7 +629,8 @@ cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, i
     const long long g = (long long)A.a[0].g * A.a[1].g * A.a[2].g;
     float* T1 = scratch + g;
     float* T2 = T1 + (long long)A.a[0].n_out * A.a[1].g * A.a[2].g;
-    k_pyr_lattice_base<<<(unsigned)((g + 255) / 256), 256, sm, st>>>(vol, tf_rgba, tf_n, A, scratch, g);
+    k_pyr_lattice_base<<<dim3((A.a[0].g + 127) / 128, A.a[1].g, A.a[2].g), 128, sm, st>>>(vol, tf_rgba, tf_n, A,
+                                                                                          scratch);
     cudaError_t e = pyr_separable(A.a, scratch, T1, T2, data + P.offset[0], st);
     if (e != cudaSuccess) return e;
   } else {
@@ -639,7 +645,7 @@ cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, i
       const long long g = (long long)A.a[0].g * A.a[1].g * A.a[2].g;
       float* T1 = scratch + g;
       float* T2 = T1 + (long long)A.a[0].n_out * A.a[1].g * A.a[2].g;
-      k_pyr_lattice_level<<<(unsigned)((g + 255) / 256), 256, 0, st>>>(P, l - 1, A, scratch, g);
+      k_pyr_lattice_level<<<dim3((A.a[0].g + 127) / 128, A.a[1].g, A.a[2].g), 128, 0, st>>>(P, l - 1, A, scratch);
       cudaError_t e = pyr_separable(A.a, scratch, T1, T2, data + P.offset[l], st);
       if (e != cudaSuccess) return e;
     } else {
