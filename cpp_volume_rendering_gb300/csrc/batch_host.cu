@@ -253,6 +253,8 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
         off += tables[k].size();
       }
     }
+    for (const BatchExtJob& J : ext)
+      if (!J.e.sat.sat32 && !J.e.sat.sat) return fail(c, CVR_ERR_NOT_READY, "cvr_batch_create: a job without a SAT");
     b->ext_aligned = true;
     for (const BatchExtJob& J : ext)
       if (!J.ttx || !(J.e.ao_aligned || !J.e.apply_occ)) b->ext_aligned = false;

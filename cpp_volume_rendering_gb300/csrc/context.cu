@@ -196,7 +196,6 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
   if (p->apply_shadow && !(p->sdw_sample_interval >= 1.0e-3f))
     return fail(c, CVR_ERR_INVALID_ARG, "sdw_sample_interval must be >= 1e-3 voxels");
   ExtArgs a{};
-  a.sat.sat = c->d_sat;
   a.sat.sx = c->nx + 2; a.sat.sy = c->ny + 2; a.sat.sz = c->nz + 2;
   a.sat.sxy = (unsigned)a.sat.sx * (unsigned)a.sat.sy;
   a.sat.inv_scale = (float)std::ldexp(1.0, -c->sat_frac_bits);
@@ -291,11 +290,13 @@ cvr_status ext_args(cvr_ctx* c, const cvr_ext_params* p, const cvr_light* light,
     }
   }
   // the int64 table serves frames without a compact table; the caller of
-  // vmax_out may fall back to it
+  // vmax_out may fall back to it.  Its pointer is taken after the build,
+  // which allocates it the first time.
   if (vmax_out || !a.sat.sat32) {
     cvr_status cs = ensure_sat(c);
     if (cs != CVR_OK) return cs;
   }
+  a.sat.sat = c->d_sat;
   *eo = a;
   return CVR_OK;
 }

@@ -347,6 +347,7 @@ static cudaError_t launch_extinction_refill(const FrameArgs& f, const ExtArgs& e
 
 cudaError_t launch_extinction(const FrameArgs& f, const ExtArgs& e, const ShadowBoxTable* table,
                               const ShadowBoxTable& storage, cudaStream_t st) {
+  if (!e.sat.sat32 && !e.sat.sat) return cudaErrorInvalidValue;  // no table to read
   if (f.work) {
     switch (f.variant) {
       case 1: return launch_extinction_refill<minb128<1>()>(f, e, table, storage, st);
