@@ -377,6 +377,12 @@ cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint4* 
 // the frame keeps the int64 table.
 cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
   *inv_scale = 0.0f;
+  // the table planned for this extent is current (cvr_build_sat and a new
+  // volume reset sat32_F): no per-frame pass over the extinction table
+  if (c->d_sat32 && c->sat32_F != kNoCompactSat && c->sat32_vmax == vmax) {
+    *inv_scale = (float)std::ldexp(1.0, -c->sat32_F);
+    return CVR_OK;
+  }
   int F;
   std::vector<unsigned> q;
   if (!compact_plan(c->sat_ext, vmax, &F, &q)) return CVR_OK;
@@ -399,6 +405,7 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale) {
     static std::atomic<unsigned long long> builds{0};  // distinct id of every compact build
     c->sat32_gen = ++builds;
   }
+  c->sat32_vmax = vmax;
   *inv_scale = (float)std::ldexp(1.0, -F);
   return CVR_OK;
 }

@@ -118,6 +118,7 @@ struct VolSlot {
   unsigned* d_lut32 = nullptr;
   size_t lut32_cap = 0;
   int sat32_F = kNoCompactSat;
+  double sat32_vmax = 0.0;
   unsigned long long sat32_gen = 0;  // which build of the compact table (walk tables follow it)
   float* d_pyr = nullptr;
   size_t pyr_cap = 0;
@@ -189,6 +190,7 @@ struct cvr_ctx {
   unsigned* d_lut32 = nullptr;
   size_t lut32_cap = 0;
   int sat32_F = kNoCompactSat;
+  double sat32_vmax = 0.0;  // the query extent the current compact table was planned for
   unsigned long long sat32_gen = 0;          // which build of the compact table (walk tables follow it)
   bool compact_sat = true;                   // cvr_set_compact_sat
   bool walk_tables = true;                   // cvr_set_walk_tables
@@ -288,6 +290,7 @@ inline void swap_volume(cvr_ctx* c, VolSlot& s) {
   std::swap(c->d_lut32, s.d_lut32);
   std::swap(c->lut32_cap, s.lut32_cap);
   std::swap(c->sat32_F, s.sat32_F);
+  std::swap(c->sat32_vmax, s.sat32_vmax);
   std::swap(c->sat32_gen, s.sat32_gen);
   std::swap(c->d_pyr, s.d_pyr);
   std::swap(c->pyr_cap, s.pyr_cap);
