@@ -816,7 +816,12 @@ def run_ours(args):
     lib = abi.load()
     ctx = scene.Context(local)
     surrogate = None
-    if args.workload == "surrogate":
+    if args.workload == "surrogate" and args.no_surrogate:
+        # profiling the frame alone: an untrained network of the same shape (the
+        # network scales the samples' colour; opacity, and so every ray's
+        # samples and the frame's work, come from the transfer function)
+        ctx.mlp_init(7)
+    elif args.workload == "surrogate":
         surrogate = surrogate_section(ctx, lib, args)
     wl = scene.workload(args.workload, n=args.size, image=args.image)
     scene.prepare(ctx, wl)
@@ -1008,7 +1013,9 @@ def main():
     ap.add_argument("--workload", default="extinction", choices=list(WORKLOAD_DESC))
     ap.add_argument("--quick", action="store_true", help="skip the per-renderer table")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-surrogate", action="store_true", help="skip training / evaluating the surrogate")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip training / evaluating the surrogate (with --workload surrogate: time the frame "
+                         "with an untrained network)")
     ap.add_argument("--surrogate-points", type=int, default=4_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient Blinn-Phong section")
