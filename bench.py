@@ -711,36 +711,56 @@ def surrogate_section(ctx, lib, args, log=print):
     }
 
 
+def apply_tuning(lib, ctx, tuning):
+    """--tuning tile_w,tile_h,variant,warp_w,layout,refill[,brick edge] on ctx; returns the fields."""
+    from cpp_volume_rendering_gb300 import abi
+    t = [int(v) for v in tuning.split(",")]
+    abi.check(lib.cvr_set_tuning(ctx.h, t[0], t[1], t[2]), ctx.h)
+    abi.check(lib.cvr_set_warp_shape(ctx.h, t[3]), ctx.h)
+    abi.check(lib.cvr_set_volume_layout(ctx.h, t[4]), ctx.h)
+    abi.check(lib.cvr_set_ray_refill(ctx.h, t[5]), ctx.h)
+    abi.check(lib.cvr_set_brick_size(ctx.h, t[6] if len(t) > 6 else 0), ctx.h)
+    return t
+
+
 def batch_section(ctx, lib, args, log=print):
-    """The batched workload: 4 volumes of uneven size x 16 views x 4 directional
-    lights at 512^2, extinction and surrogate shading (512 images), one CUDA
-    graph of two persistent launches; against the same jobs as 512 cvr_render
-    calls.  Uses the network on ctx (trained by the surrogate section when it ran)."""
+    """The batched workload: 4 volumes of uneven size x 16 views (--batch-views)
+    x 4 directional lights at 512^2, extinction and surrogate shading (512
+    images), one CUDA graph of persistent launches; against the same jobs as
+    512 cvr_render calls.  Uses the network on ctx (trained by the surrogate
+    section when it ran).  --tuning fixes the marchers' configuration instead
+    of tuning it on the largest extinction job."""
     import ctypes as C
     from cpp_volume_rendering_gb300 import abi, scene
     t0 = time.perf_counter()
-    vols = scene.batch_volumes(1.0)
+    vols = scene.batch_volumes(args.batch_scale)
     scene.prepare_batch_volumes(ctx, vols)
     t_prep = time.perf_counter() - t0
     if not ctx.lib.cvr_mlp_training_size(ctx.h):  # no trained network on ctx: timing only
         ctx.mlp_init(7)
     W = 512
-    probe = scene.batch_jobs(vols, image=W)
+    views = args.batch_views
+    probe = scene.batch_jobs(vols, n_views=views, image=W)
     n = len(probe.jobs)
     frames = C.POINTER(C.c_float)()
     fb_w = 32768  # one library-owned buffer holding all n frames
     abi.check(lib.cvr_get_frame_buffer(ctx.h, fb_w, (n * W * W + fb_w - 1) // fb_w, C.byref(frames)), ctx.h)
     base = C.cast(frames, C.c_void_p).value
     outs = [C.c_void_p(base + k * W * W * 16) for k in range(n)]
-    b = scene.batch_jobs(vols, image=W, out_ptrs=outs)
-    # tuner: tile shape x register variant on the largest volume's first extinction job
-    big = max(range(n), key=lambda k: (b.jobs[k].method == abi.EXTINCTION, vols[b.jobs[k].volume].size))
-    jb = b.jobs[big]
-    ctx.select_volume(jb.volume)
+    b = scene.batch_jobs(vols, n_views=views, image=W, out_ptrs=outs)
     tw, th, tv, tms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
-    abi.check(lib.cvr_autotune(ctx.h, jb.method, C.byref(jb.camera), C.byref(jb.light), C.c_void_p(jb.params),
-                               jb.params_size, W, W, 2, C.byref(tw), C.byref(th), C.byref(tv), C.byref(tms)), ctx.h)
-    ctx.select_volume(0)
+    if args.tuning:
+        apply_tuning(lib, ctx, args.tuning)
+        abi.check(lib.cvr_get_tuning(ctx.h, C.byref(tw), C.byref(th), C.byref(tv)), ctx.h)
+    else:
+        # tuner: tile shape x register variant on the largest volume's first extinction job
+        big = max(range(n), key=lambda k: (b.jobs[k].method == abi.EXTINCTION, vols[b.jobs[k].volume].size))
+        jb = b.jobs[big]
+        ctx.select_volume(jb.volume)
+        abi.check(lib.cvr_autotune(ctx.h, jb.method, C.byref(jb.camera), C.byref(jb.light), C.c_void_p(jb.params),
+                                   jb.params_size, W, W, 2, C.byref(tw), C.byref(th), C.byref(tv), C.byref(tms)),
+                  ctx.h)
+        ctx.select_volume(0)
     ms = C.c_float()
 
     def run_batch(idx):
@@ -792,8 +812,9 @@ def batch_section(ctx, lib, args, log=print):
         per_method[name] = {"jobs": len(idx), "batch_ms": bm, "msamples_s": smp / (bm / 1000.0) / 1e6,
                             "sequential_ms": sm, "sequential_msamples_s": smp / (sm / 1000.0) / 1e6,
                             "speedup_vs_sequential": sm / bm}
-    return {"workload": "4 volumes (128^3 u8, 192x256x160 u16, 256^3 u8, 384^3 u16 value noise) x 16 views x "
-                        "4 directional lights x {extinction, surrogate} = 512 images of 512^2",
+    dims = ", ".join("x".join(str(e) for e in v.shape[::-1]) for v in vols)
+    return {"workload": f"4 volumes ({dims}; u8, u16, u8, u16 value noise) x {views} views x "
+                        f"4 directional lights x {{extinction, surrogate}} = {n} images of 512^2",
             "jobs": n, "batch_ms": med, "images_per_s": n / (med / 1000.0),
             "msamples_s": tot / (med / 1000.0) / 1e6, "by_method": per_method,
             "sequential_ms": seq_ms, "speedup_vs_sequential": seq_ms / med,
@@ -801,7 +822,8 @@ def batch_section(ctx, lib, args, log=print):
                        "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
                        "refill": lib.cvr_get_ray_refill(ctx.h), "staging": lib.cvr_get_brick_staging(ctx.h)},
             "prepare_s": t_prep,
-            "launch": "one CUDA graph: 2 memsets + persistent extinction launch + persistent surrogate launch"}
+            "launch": "one CUDA graph: 2 memsets + the persistent extinction launch + persistent surrogate launches "
+                      "of up to 32 jobs each (their descriptors as kernel parameters)"}
 
 
 def run_ours(args):
@@ -815,6 +837,11 @@ def run_ours(args):
     build.build()
     lib = abi.load()
     ctx = scene.Context(local)
+    if args.batch_only:
+        if rank == 0:
+            emit("batch", batch_section(ctx, lib, args))
+        ctx.close()
+        return
     surrogate = None
     if args.workload == "surrogate" and args.no_surrogate:
         # profiling the frame alone: an untrained network of the same shape (the
@@ -833,12 +860,7 @@ def run_ours(args):
     # x warp shape x layout x ray refill; --tuning fixes a configuration instead (profiling)
     tw, th, tv, tms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
     if args.tuning:
-        t = [int(v) for v in args.tuning.split(",")]
-        abi.check(lib.cvr_set_tuning(ctx.h, t[0], t[1], t[2]), ctx.h)
-        abi.check(lib.cvr_set_warp_shape(ctx.h, t[3]), ctx.h)
-        abi.check(lib.cvr_set_volume_layout(ctx.h, t[4]), ctx.h)
-        abi.check(lib.cvr_set_ray_refill(ctx.h, t[5]), ctx.h)
-        abi.check(lib.cvr_set_brick_size(ctx.h, t[6] if len(t) > 6 else 0), ctx.h)
+        t = apply_tuning(lib, ctx, args.tuning)
         tw.value, th.value, tv.value = t[0], t[1], t[2]
     else:
         abi.check(lib.cvr_autotune(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params),
@@ -1018,6 +1040,10 @@ def main():
                          "with an untrained network)")
     ap.add_argument("--surrogate-points", type=int, default=4_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
+    ap.add_argument("--batch-views", type=int, default=16, help="views per volume and light of the batch")
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="edge scale of the batch's volumes (profiling)")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="run the batched-rendering section alone (profiling; no headline line)")
     ap.add_argument("--no-gradient", action="store_true", help="skip the gradient Blinn-Phong section")
     ap.add_argument("--no-postpass", action="store_true", help="skip the pixel-multiscaling section")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
