@@ -56,6 +56,15 @@ int select_slot(cvr_ctx* c, int s) {
   return prev;
 }
 
+// Dominant axis of a job's directional light (the walk axis of its shadow
+// table), 3 for other lights: jobs that share a volume and this axis read
+// the same walk table.
+int job_walk_axis(const cvr_job& j) {
+  if (j.light.type != CVR_LIGHT_DIRECTIONAL) return 3;
+  const float a[3] = {std::fabs(j.light.forward[0]), std::fabs(j.light.forward[1]), std::fabs(j.light.forward[2])};
+  return (a[2] > a[0] && a[2] > a[1]) ? 2 : (a[1] > a[0] ? 1 : 0);
+}
+
 double job_cost(const cvr_job& j, const cvr_ctx* c) {
   const VolSlot& v = c->slots[j.volume];
   int nx = j.volume == c->cur_slot ? c->nx : v.nx, ny = j.volume == c->cur_slot ? c->ny : v.ny,
@@ -100,8 +109,15 @@ cvr_status cvr_batch_create(cvr_ctx* c, const cvr_job* jobs, int n_jobs, cvr_bat
   // longest jobs first within each method group
   std::vector<int> order(n_jobs);
   std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int x, int y) { return job_cost(jobs[x], c) > job_cost(jobs[y], c); });
+  // longest jobs first; among equal costs, jobs of one volume, method and
+  // walk axis together, so that consecutive jobs share their tables in L2
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    const double cx = job_cost(jobs[x], c), cy = job_cost(jobs[y], c);
+    if (cx != cy) return cx > cy;
+    if (jobs[x].volume != jobs[y].volume) return jobs[x].volume < jobs[y].volume;
+    if (jobs[x].method != jobs[y].method) return jobs[x].method < jobs[y].method;
+    return job_walk_axis(jobs[x]) < job_walk_axis(jobs[y]);
+  });
   CK(c, cudaMalloc((void**)&b->d_stats, sizeof(unsigned long long) * 3 * n_jobs));
   std::vector<BatchExtJob> ext;
   std::vector<int> ext_slot;

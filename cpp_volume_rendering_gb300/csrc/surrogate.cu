@@ -331,12 +331,13 @@ __device__ __forceinline__ void sur_march(const Src& src_rays, const float4* tf_
       }
     }
     if (!__syncthreads_or(pending)) break;
+    // A row's outputs depend on that row's inputs alone, so the rows of
+    // threads without a pending sample keep whatever the tile holds (their
+    // outputs are not used): only the threads with a sample store features,
+    // which halves the partial-warp stores of every chunk.
     if (pending) {
       TileSink out{xt, (int)threadIdx.x};
       sur_features<TEX>(src_rays.a(ray.job), src_rays.f(ray.job).vol, tf, tf_n, p, ray.dir, out);
-    } else {
-#pragma unroll
-      for (int c = 0; c < 6; ++c) store_chunk(xt, threadIdx.x, c, 0u, 0u, 0u, 0u);
     }
     // K padding (inputs 48..63): the previous round's hidden layers wrote there
     store_chunk(xt, threadIdx.x, 6, 0u, 0u, 0u, 0u);
