@@ -343,7 +343,7 @@ bool compact_plan(const std::vector<double>& ext, double vmax, int* F_out, std::
     const double scale = std::ldexp(1.0, F);
     double qmax = 0.0;
     for (size_t i = 0; i < q->size(); ++i) {
-      const double r = std::nearbyint(ext[i] * scale);
+      const double r = std::rint(ext[i] * scale);  // nearbyint's value without its FP-environment save
       qmax = std::max(qmax, r);
       (*q)[i] = (unsigned)r;
     }
