@@ -152,8 +152,9 @@ struct SurRay {
 
 // Where a marcher thread's rays come from.  SingleSource: one frame, tiles
 // in the square spiral around (cx, cy) (positions outside the image are
-// skipped: px = -1).  BatchSource: the jobs of a batch, each a run of
-// 8x4-pixel tiles of one counter (jobs ordered by first tile).
+// skipped: px = -1).  BatchSource: the jobs of one batch launch, each a run
+// of spiral positions of one counter (jobs ordered by first position), each
+// in the square spiral around its own centre tile.
 struct SingleSource {
   const FrameArgs& f0;
   const SurArgs& a0;

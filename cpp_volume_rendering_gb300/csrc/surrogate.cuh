@@ -206,7 +206,8 @@ cudaError_t launch_sur_label(const float4* pts, int n, const FrameArgs& f, const
                              cudaStream_t st);
 
 // One job of a batch of surrogate frames (device table entry).  f.stats points
-// at the job's three counters; f.tf / f.tf_n and a.packed of job 0 serve all.
+// at the job's three counters; f.tf / f.tf_n and a.packed of a launch's first
+// job serve all its jobs (one transfer function and network per batch).
 struct SurJob {
   FrameArgs f;
   SurArgs a;
