@@ -59,7 +59,7 @@ WORKLOAD_DESC = {
             "occlusion + point-light shadow cones",
     "ground_truth": "ground truth: 256^3 u8 32 blobs + U[0,20] noise -> 512^2, 16 occlusion rays of 32 voxels + "
                     "1 shadow ray to a point light, 1-voxel light steps",
-    "surrogate": "learned occlusion/shadow surrogate: MLP 48-64-64-2 (BF16 tcgen05) trained on 4M GT-labelled "
+    "surrogate": "learned occlusion/shadow surrogate: MLP 48-64-64-2 (BF16 tcgen05) trained on up to 8M GT-labelled "
                  "points of 20 seeded blob volumes (160^3..448^3); held-out 512^3 u8 blobs -> 1024^2, point light",
 }
 
@@ -613,8 +613,8 @@ def measured_peak_bf16():
 
 
 def surrogate_section(ctx, lib, args, log=print):
-    """Trains the surrogate from scratch (cfg: 4M GT-labelled points of 20
-    seeded 256^3 blob volumes), then on the held-out 512^3 volume at 1024^2
+    """Trains the surrogate from scratch (cfg: up to 8M GT-labelled points of
+    20 seeded blob volumes of 160^3..448^3, 60 epochs), then on the held-out 512^3 volume at 1024^2
     measures its RMSE and the cone method's against the ground-truth
     integrator, and the GT and surrogate frame times.  Leaves the surrogate
     workload prepared on ctx."""
@@ -1038,7 +1038,7 @@ def main():
     ap.add_argument("--no-surrogate", action="store_true",
                     help="skip training / evaluating the surrogate (with --workload surrogate: time the frame "
                          "with an untrained network)")
-    ap.add_argument("--surrogate-points", type=int, default=4_000_000)
+    ap.add_argument("--surrogate-points", type=int, default=8_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-rendering section")
     ap.add_argument("--batch-views", type=int, default=16, help="views per volume and light of the batch")
     ap.add_argument("--batch-scale", type=float, default=1.0, help="edge scale of the batch's volumes (profiling)")

@@ -603,7 +603,7 @@ def shaded_sample_count(ctx: Context, cam, w, h, step) -> int:
     return int(st.shaded_samples)
 
 
-def build_surrogate_training_set(ctx: Context, n_volumes=SURROGATE_VOLUMES, size=None, points=4_000_000,
+def build_surrogate_training_set(ctx: Context, n_volumes=SURROGATE_VOLUMES, size=None, points=8_000_000,
                                  views=4, image=256, seed=SURROGATE_SEED, log=None) -> int:
     """Appends ~points labelled shading points to the context's training set
     (the network must exist: cvr_mlp_init first).  size=None cycles through
@@ -636,7 +636,7 @@ def build_surrogate_training_set(ctx: Context, n_volumes=SURROGATE_VOLUMES, size
 
 
 # Adam schedule: (epochs, learning rate) phases.
-SURROGATE_SCHEDULE = ((12, 2e-3), (8, 7e-4), (6, 2e-4), (4, 5e-5))
+SURROGATE_SCHEDULE = ((24, 2e-3), (16, 7e-4), (12, 2e-4), (8, 5e-5))
 
 
 def train_surrogate(ctx: Context, batch=4096, schedule=SURROGATE_SCHEDULE, seed=SURROGATE_SEED) -> list:
