@@ -4,6 +4,7 @@
 // Clean(): the volume texture, transfer-function textures, SAT / pyramid /
 // cone-table / kernel-vector textures and the output frame.  Uploads happen
 // once (Init); each cvr_render is Update() + Redraw() of one frame.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -1151,6 +1152,36 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
       if (warp_fits(tiles[bt][0], tiles[bt][1], warps[wi])) trial(bt, bvar, wi, bb);
     for (int k = 0; k < 5; ++k) trial(bt, bvar, bw, k);
     if (before[0] == bt && before[1] == bvar && before[2] == bw && before[3] == bb) break;
+  }
+  // Single timings of configurations a few percent apart are within the
+  // frames' noise: the four fastest are timed again with twice the frames,
+  // and the fastest of those wins.
+  if (s == CVR_OK) {
+    struct Cand { float ms; int t, v, wi, k; };
+    std::vector<Cand> cands;
+    for (int t = 0; t < 6; ++t)
+      for (int v = 0; v < n_variants; ++v)
+        for (int wi = 0; wi < 3; ++wi)
+          for (int k = 0; k < 5; ++k)
+            if (timed[t][v][wi][k] >= 0.0f) cands.push_back({timed[t][v][wi][k], t, v, wi, k});
+    std::sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) { return a.ms < b.ms; });
+    if (cands.size() > 4) cands.resize(4);
+    if (cands.size() > 1) {
+      best = 1e30f;
+      for (const Cand& cd : cands) {
+        c->tile_w = tiles[cd.t][0]; c->tile_h = tiles[cd.t][1]; c->variant = cd.v;
+        c->warp_w = warps[cd.wi];
+        c->brick_bs = bricks[cd.k] > 0 ? bricks[cd.k] : 0;
+        c->quads = bricks[cd.k] < 0;
+        float m = 0.0f;
+        s = time_config(c, method, cam, light, params, params_size, frame, w, h, std::min(2 * reps, 100), &m);
+        if (s != CVR_OK) break;
+        if (m < best) {
+          best = m;
+          bt = cd.t; bvar = cd.v; bw = cd.wi; bb = cd.k;
+        }
+      }
+    }
   }
   if (s != CVR_OK) {
     c->tile_w = keep_w; c->tile_h = keep_h; c->variant = keep_v; c->brick_bs = keep_b; c->quads = keep_q;
