@@ -383,12 +383,21 @@ __device__ __forceinline__ float sat_box_aligned(const SatView& S, float3 u, int
     const uint4 c = __ldg(q + (zo + c10)), d = __ldg(q + (zo + c11));
     return make_uint4(d.x - c.x - b.x + a.x, d.y - c.y - b.y + a.y, d.z - c.z - b.z + a.z, d.w - c.w - b.w + a.w);
   };
-  const uint4 r0 = rect(az), r1 = rect(az + 1), r2 = rect(az + wz), r3 = rect(az + wz + 1);
+  // z-offset 0 (planes az, az + wz) and 1 (az + 1, az + wz + 1), one pair at a
+  // time: eight 16-byte loads in flight instead of sixteen
+  uint4 d0 = make_uint4(0u, 0u, 0u, 0u), d1 = d0;
+#pragma unroll 1
+  for (int o = 0; o < 2; ++o) {
+    const uint4 lo = rect(az + o), hi = rect(az + wz + o);
+    const uint4 dz = make_uint4(hi.x - lo.x, hi.y - lo.y, hi.z - lo.z, hi.w - lo.w);
+    if (o == 0) d0 = dz;
+    else d1 = dz;
+  }
   // sub-box sums (below 2^31 by the compact table's fixed point): z-offset 0 and 1
-  const float b00 = (float)(int)(r2.x - r0.x), b10 = (float)(int)(r2.y - r0.y);
-  const float b01 = (float)(int)(r2.z - r0.z), b11 = (float)(int)(r2.w - r0.w);
-  const float e00 = (float)(int)(r3.x - r1.x), e10 = (float)(int)(r3.y - r1.y);
-  const float e01 = (float)(int)(r3.z - r1.z), e11 = (float)(int)(r3.w - r1.w);
+  const float b00 = (float)(int)d0.x, b10 = (float)(int)d0.y;
+  const float b01 = (float)(int)d0.z, b11 = (float)(int)d0.w;
+  const float e00 = (float)(int)d1.x, e10 = (float)(int)d1.y;
+  const float e01 = (float)(int)d1.z, e11 = (float)(int)d1.w;
   const float z00 = fmaf(tz, e00 - b00, b00), z10 = fmaf(tz, e10 - b10, b10);
   const float z01 = fmaf(tz, e01 - b01, b01), z11 = fmaf(tz, e11 - b11, b11);
   const float y0v = fmaf(ty, z01 - z00, z00), y1v = fmaf(ty, z11 - z10, z10);
