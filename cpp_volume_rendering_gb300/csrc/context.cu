@@ -360,12 +360,17 @@ bool compact_plan(const std::vector<double>& ext, double vmax, int* F_out, std::
 // Builds the compact table of the current volume from q into dst, in x-y
 // quad layout, asynchronously on the context stream: the plane prefixes go
 // to the context's persistent scratch (grown only when a larger volume needs
-// it), and q is copied from pageable memory, which the copy call has staged
-// by the time it returns.
+// it), and q goes through the pinned staging region 1 (q may go when the
+// call returns).
 cvr_status build_compact_sat(cvr_ctx* c, const std::vector<unsigned>& q, uint4* dst) {
   const size_t cells = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
   CK(c, ensure(c->d_lut32, c->lut32_cap, sizeof(unsigned) * q.size()));
-  CK(c, cudaMemcpyAsync(c->d_lut32, q.data(), sizeof(unsigned) * q.size(), cudaMemcpyHostToDevice, c->stream));
+  void* stage = nullptr;
+  cvr_status st = stage_region(c, 1, &stage);
+  if (st != CVR_OK) return st;
+  std::memcpy(stage, q.data(), sizeof(unsigned) * q.size());
+  st = stage_upload(c, 1, c->d_lut32, sizeof(unsigned) * q.size());
+  if (st != CVR_OK) return st;
   CK(c, ensure(c->d_satp, c->satp_cap, sizeof(unsigned) * cells));
   cudaError_t e = launch_sat_build_quads(c->d_vol, c->dtype, c->nx, c->ny, c->nz, c->d_lut32, c->d_satp, dst,
                                          c->stream);
@@ -447,6 +452,25 @@ cvr_status check_kernel_flag(cvr_ctx* c, const char* what) {
   return fail(c, CVR_ERR_TIMEOUT, what);
 }
 
+cvr_status stage_region(cvr_ctx* c, int r, void** out) {
+  constexpr size_t kRegion = sizeof(long long) * 65536;
+  if (!c->h_stage) {
+    CK(c, cudaHostAlloc(&c->h_stage, 2 * kRegion, cudaHostAllocDefault));
+    for (cudaEvent_t& e : c->stage_ev) CK(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  CK(c, cudaEventSynchronize(c->stage_ev[r]));  // an event never recorded is complete
+  *out = static_cast<char*>(c->h_stage) + (size_t)r * kRegion;
+  return CVR_OK;
+}
+
+cvr_status stage_upload(cvr_ctx* c, int r, void* dev, size_t n) {
+  constexpr size_t kRegion = sizeof(long long) * 65536;
+  CK(c, cudaMemcpyAsync(dev, static_cast<char*>(c->h_stage) + (size_t)r * kRegion, n, cudaMemcpyHostToDevice,
+                        c->stream));
+  CK(c, cudaEventRecord(c->stage_ev[r], c->stream));
+  return CVR_OK;
+}
+
 cvr_status ensure_sat(cvr_ctx* c) {
   if (!c->sat_ready || !c->sat_pending) return CVR_OK;
   CK(c, cudaSetDevice(c->device));
@@ -511,6 +535,9 @@ void cvr_destroy(cvr_ctx* c) {
     if (p) cudaFree(p);
   for (int i = 0; i < 4; ++i)
     if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+  for (cudaEvent_t e : c->stage_ev)
+    if (e) cudaEventDestroy(e);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -606,7 +633,11 @@ cvr_status cvr_build_sat(cvr_ctx* c, const double* ext, int n_values) {
   int F = 52;
   if (maxv > 0.0) F = (int)std::floor(62.0 - std::log2(nvox * maxv));
   F = std::min(52, std::max(0, F));
-  std::vector<long long> q(n_values);
+  CK(c, cudaSetDevice(c->device));
+  void* stage = nullptr;
+  cvr_status st = stage_region(c, 0, &stage);
+  if (st != CVR_OK) return st;
+  long long* q = static_cast<long long*>(stage);
   double scale = std::ldexp(1.0, F);
   // llround of a non-negative value: below 2^52, v + 0.5 is exact and its
   // truncation rounds halves up; from 2^52 on, v is an integer already
@@ -614,11 +645,10 @@ cvr_status cvr_build_sat(cvr_ctx* c, const double* ext, int n_values) {
     const double v = ext[i] * scale;
     q[i] = v < 4503599627370496.0 ? (long long)(v + 0.5) : (long long)v;
   }
-  CK(c, cudaSetDevice(c->device));
   // the table of every possible voxel value (65536 entries covers u8 and u16)
   if (!c->d_lut) CK(c, cudaMalloc((void**)&c->d_lut, sizeof(long long) * 65536));
-  // pageable source: staged by the time the call returns, so q may go
-  CK(c, cudaMemcpyAsync(c->d_lut, q.data(), sizeof(long long) * n_values, cudaMemcpyHostToDevice, c->stream));
+  st = stage_upload(c, 0, c->d_lut, sizeof(long long) * n_values);
+  if (st != CVR_OK) return st;
   c->sat_frac_bits = F;
   c->sat_ready = true;
   c->sat_pending = true;

@@ -230,6 +230,11 @@ struct cvr_ctx {
   void* d_probe = nullptr;  // cvr_measure_l1_bandwidth's buffer
   size_t probe_cap = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Pinned staging of the fixed-point tables cvr_build_sat (int64, 65536
+  // entries) and the compact rebuild (32-bit) upload, so that the copies are
+  // asynchronous; each region is rewritten only after its last copy completed.
+  void* h_stage = nullptr;
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
   int tile_w = 16, tile_h = 8, variant = 0;
   int warp_w = 8;                            // cvr_set_warp_shape (used where the tile holds whole warps)
   bool refill = false;                       // cvr_set_ray_refill: persistent ray-refill marchers
@@ -433,6 +438,11 @@ cvr_status ensure_compact_sat(cvr_ctx* c, double vmax, float* inv_scale);
 cvr_status ensure_walk_table(cvr_ctx* c, int axis, int w, WalkView* out);
 // Enqueues the current volume's pending int64 SAT build (cvr_build_sat defers it).
 cvr_status ensure_sat(cvr_ctx* c);
+// Staging region r of the pinned table buffer (0: 65536 int64 values, 1:
+// 65536 32-bit values), free to write: the region's previous copy has completed.
+cvr_status stage_region(cvr_ctx* c, int r, void** out);
+// Enqueues the copy of n bytes of staging region r to dev and marks the region busy.
+cvr_status stage_upload(cvr_ctx* c, int r, void* dev, size_t n);
 // The pieces of it: the fixed point (false: keep the int64 table) and the
 // build of the current volume's compact table into dst.
 bool compact_plan(const std::vector<double>& ext, double vmax, int* F, std::vector<unsigned>* q);
