@@ -492,9 +492,10 @@ cvr_status cvr_get_blinn_phong(cvr_ctx* ctx, cvr_blinn_phong* out);
 /* ---- batched rendering ------------------------------------------------------
  * No reference counterpart (the reference renders one view per Redraw()).
  * A batch is a fixed list of frames over the resident volumes, views and
- * lights, rendered by one persistent launch per method (CVR_METHOD_EXTINCTION
- * and CVR_METHOD_SURROGATE; other methods are rejected) whose CTAs take
- * ray tiles of all jobs from one work counter, longest jobs first.  The
+ * lights, rendered by persistent launches (CVR_METHOD_EXTINCTION: one over
+ * all its jobs; CVR_METHOD_SURROGATE: one per 32 jobs, their descriptors the
+ * launch's parameters; other methods are rejected) whose CTAs take ray tiles
+ * of their jobs from one work counter per launch, longest jobs first.  The
  * launches, with the resets of their counters, are captured in one CUDA
  * graph at creation; cvr_batch_run replays it.  Every image equals the image
  * of the same job rendered alone by cvr_render with the context's tuning at
