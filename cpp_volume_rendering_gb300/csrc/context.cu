@@ -1184,31 +1184,38 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
     if (before[0] == bt && before[1] == bvar && before[2] == bw && before[3] == bb) break;
   }
   // Single timings of configurations a few percent apart are within the
-  // frames' noise: the four fastest are timed again with twice the frames,
-  // and the fastest of those wins.
+  // frames' noise: the five fastest are timed again in three interleaved
+  // rounds (so that a drift of the clocks or caches hits all of them), and
+  // the lowest median wins.
   if (s == CVR_OK) {
-    struct Cand { float ms; int t, v, wi, k; };
+    struct Cand { float ms; int t, v, wi, k; float runs[3]; };
     std::vector<Cand> cands;
     for (int t = 0; t < 6; ++t)
       for (int v = 0; v < n_variants; ++v)
         for (int wi = 0; wi < 3; ++wi)
           for (int k = 0; k < 5; ++k)
-            if (timed[t][v][wi][k] >= 0.0f) cands.push_back({timed[t][v][wi][k], t, v, wi, k});
+            if (timed[t][v][wi][k] >= 0.0f) cands.push_back({timed[t][v][wi][k], t, v, wi, k, {0, 0, 0}});
     std::sort(cands.begin(), cands.end(), [](const Cand& a, const Cand& b) { return a.ms < b.ms; });
-    if (cands.size() > 4) cands.resize(4);
+    if (cands.size() > 5) cands.resize(5);
     if (cands.size() > 1) {
-      best = 1e30f;
-      for (const Cand& cd : cands) {
-        c->tile_w = tiles[cd.t][0]; c->tile_h = tiles[cd.t][1]; c->variant = cd.v;
-        c->warp_w = warps[cd.wi];
-        c->brick_bs = bricks[cd.k] > 0 ? bricks[cd.k] : 0;
-        c->quads = bricks[cd.k] < 0;
-        float m = 0.0f;
-        s = time_config(c, method, cam, light, params, params_size, frame, w, h, std::min(2 * reps, 100), &m);
-        if (s != CVR_OK) break;
-        if (m < best) {
-          best = m;
-          bt = cd.t; bvar = cd.v; bw = cd.wi; bb = cd.k;
+      for (int round = 0; round < 3 && s == CVR_OK; ++round) {
+        for (Cand& cd : cands) {
+          c->tile_w = tiles[cd.t][0]; c->tile_h = tiles[cd.t][1]; c->variant = cd.v;
+          c->warp_w = warps[cd.wi];
+          c->brick_bs = bricks[cd.k] > 0 ? bricks[cd.k] : 0;
+          c->quads = bricks[cd.k] < 0;
+          s = time_config(c, method, cam, light, params, params_size, frame, w, h, reps, &cd.runs[round]);
+          if (s != CVR_OK) break;
+        }
+      }
+      if (s == CVR_OK) {
+        best = 1e30f;
+        for (Cand& cd : cands) {
+          std::sort(cd.runs, cd.runs + 3);
+          if (cd.runs[1] < best) {
+            best = cd.runs[1];
+            bt = cd.t; bvar = cd.v; bw = cd.wi; bb = cd.k;
+          }
         }
       }
     }
