@@ -869,6 +869,8 @@ def run_ours(args):
     tuning = {"tile": [tw.value, th.value], "variant": tv.value, "brick": lib.cvr_get_brick_size(ctx.h),
               "quads": lib.cvr_get_volume_layout(ctx.h), "warp_w": lib.cvr_get_warp_shape(ctx.h),
               "refill": lib.cvr_get_ray_refill(ctx.h), "staging": lib.cvr_get_brick_staging(ctx.h)}
+    if not args.tuning:
+        tuning["autotune_ms"] = round(tms.value, 4)  # the winner's time as the tuner measured it
     # one stats frame: sample counts are deterministic for a fixed frame
     st = abi.FrameStats()
     abi.check(lib.cvr_render(ctx.h, wl.method, C.byref(wl.cam), C.byref(wl.light), C.byref(params), C.sizeof(params),
