@@ -428,8 +428,8 @@ __device__ __forceinline__ bool in_grid(float3 p, float3 g) {
 __global__ void k_pyr_base(VolumeView vol, const float4* __restrict__ tf_rgba, int tf_n, int bx, int by, int bz,
                            float s0, float* __restrict__ out) {
   __shared__ float sm_w[343];
-  extern __shared__ float sm_tfa[];  // the transfer function's opacity channel
-  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tfa[i] = tf_rgba[i].w;
+  extern __shared__ float4 sm_tf[];
+  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tf[i] = tf_rgba[i];
   const float sum_w = stage_gauss(s0, sm_w);
   long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long total = (long long)bx * by * bz;
@@ -444,7 +444,7 @@ __global__ void k_pyr_base(VolumeView vol, const float4* __restrict__ tf_rgba, i
       for (int ptz = -3; ptz < 4; ++ptz, ++k) {
         const float3 p = gp + f3(float(ptx) * s0, float(pty) * s0, float(ptz) * s0);
         float ck = 0.0f;
-        if (in_grid(p, vol.grid)) ck = tf_scalar(sm_tfa, tf_n, sample_volume(vol, p));
+        if (in_grid(p, vol.grid)) ck = tf_alpha(sm_tf, tf_n, sample_volume(vol, p));
         sum_wc += sm_w[k] * ck;
       }
     }
@@ -557,8 +557,8 @@ struct PyrAxes { PyrAxis a[3]; };
 // a flat index per element.
 __global__ void k_pyr_lattice_base(VolumeView vol, const float4* __restrict__ tf_rgba, int tf_n, PyrAxes A,
                                    float* __restrict__ G) {
-  extern __shared__ float sm_tfa[];  // the transfer function's opacity channel
-  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tfa[i] = tf_rgba[i].w;
+  extern __shared__ float4 sm_tf[];
+  for (int i = threadIdx.x; i < tf_n; i += blockDim.x) sm_tf[i] = tf_rgba[i];
   __syncthreads();
   const int qx = blockIdx.x * blockDim.x + threadIdx.x, qy = blockIdx.y, qz = blockIdx.z;
   if (qx >= A.a[0].g) return;
@@ -567,7 +567,7 @@ __global__ void k_pyr_lattice_base(VolumeView vol, const float4* __restrict__ tf
   float3 u;
   const bool inside = pyr_lattice_point(A.a, n_in, qx, qy, qz, u);
   const float3 p = f3((u.x + 0.5f) * vol.spacing.x, (u.y + 0.5f) * vol.spacing.y, (u.z + 0.5f) * vol.spacing.z);
-  G[idx] = inside ? tf_scalar(sm_tfa, tf_n, sample_volume(vol, p)) : 0.0f;
+  G[idx] = inside ? tf_alpha(sm_tf, tf_n, sample_volume(vol, p)) : 0.0f;
 }
 
 __global__ void k_pyr_lattice_level(PyramidView P, int l_in, PyrAxes A, float* __restrict__ G) {
@@ -617,7 +617,7 @@ cudaError_t launch_pyramid_build(const VolumeView& vol, const float4* tf_rgba, i
                                  cudaStream_t st) {
   const int threads = 128;
   long long n0 = (long long)P.dims[0][0] * P.dims[0][1] * P.dims[0][2];
-  size_t sm = sizeof(float) * tf_n;
+  size_t sm = sizeof(float4) * tf_n;
   if (sm > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_pyr_base, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e == cudaSuccess)

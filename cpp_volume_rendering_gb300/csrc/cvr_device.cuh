@@ -188,15 +188,6 @@ __device__ __forceinline__ float tf_alpha(const float4* tf, int n, float density
   return fmaf(t.t, b - a, a);
 }
 
-// The same lookup from a table of the alpha channel alone (4-byte entries:
-// neighbouring entries in neighbouring shared-memory banks, where the .w of
-// 16-byte entries spreads a warp's gathers over 8 banks).
-__device__ __forceinline__ float tf_scalar(const float* tf_a, int n, float density) {
-  Tap t = axis_tap(fmaf(density, float(n), -0.5f), n);
-  float a = tf_a[t.i0], b = tf_a[t.i1];
-  return fmaf(t.t, b - a, a);
-}
-
 // ---------------------------------------------------------------- SAT query
 // The extinction SAT is stored as exact int64 fixed point (value * 2^F).
 // The reference evaluates a box as V1-V2-V3+V4-V5+V6+V7-V8 over eight

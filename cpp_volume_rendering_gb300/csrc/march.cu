@@ -76,16 +76,11 @@ __global__ void __launch_bounds__(NT) k_march_gt(GtArgs g, FrameArgs f) {
   float4* tf = sm;
   float3* ov = reinterpret_cast<float3*>(sm + f.tf_n);
   float3* sv = ov + g.n_occ;
-  float* te = reinterpret_cast<float*>(sv + g.n_sdw);
-  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) {
-    const float4 e = f.tf[i];
-    tf[i] = e;
-    te[i] = e.w;
-  }
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
   for (int i = threadIdx.x; i < g.n_occ; i += blockDim.x) ov[i] = g.occ_vec[i];
   for (int i = threadIdx.x; i < g.n_sdw; i += blockDim.x) sv[i] = g.sdw_vec[i];
   __syncthreads();
-  GtShade sh{&g, tf, f.tf_n, ov, sv, te};
+  GtShade sh{&g, tf, f.tf_n, ov, sv};
   march_pixel(f, tf, sh);
 }
 
@@ -144,16 +139,11 @@ __global__ void __launch_bounds__(128, MINB) k_march_gt_refill(GtArgs g, FrameAr
   float4* tf = sm;
   float3* ov = reinterpret_cast<float3*>(sm + f.tf_n);
   float3* sv = ov + g.n_occ;
-  float* te = reinterpret_cast<float*>(sv + g.n_sdw);
-  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) {
-    const float4 e = f.tf[i];
-    tf[i] = e;
-    te[i] = e.w;
-  }
+  for (int i = threadIdx.x; i < f.tf_n; i += blockDim.x) tf[i] = f.tf[i];
   for (int i = threadIdx.x; i < g.n_occ; i += blockDim.x) ov[i] = g.occ_vec[i];
   for (int i = threadIdx.x; i < g.n_sdw; i += blockDim.x) sv[i] = g.sdw_vec[i];
   __syncthreads();
-  GtShade sh{&g, tf, f.tf_n, ov, sv, te};
+  GtShade sh{&g, tf, f.tf_n, ov, sv};
   march_refill(f, tf, sh, f.work, o);
 }
 
@@ -432,8 +422,7 @@ static cudaError_t launch_gt_t(const FrameArgs& f, const GtArgs& g, size_t sm, c
 }
 
 cudaError_t launch_gt(const FrameArgs& f, const GtArgs& g, cudaStream_t st) {
-  // transfer function, kernel vectors, the transfer function's extinction channel
-  size_t sm = sizeof(float4) * f.tf_n + sizeof(float3) * (g.n_occ + g.n_sdw) + sizeof(float) * f.tf_n;
+  size_t sm = sizeof(float4) * f.tf_n + sizeof(float3) * (g.n_occ + g.n_sdw);
   if (f.work) {
     const RayOrder o = ray_order(f);
     switch (f.variant) {

@@ -536,12 +536,7 @@ struct GtShade {
   int tf_n;
   const float3* occ_vec;  // shared-memory copies
   const float3* sdw_vec;
-  const float* tf_ext = nullptr;  // shared-memory copy of tf's extinction channel, or nullptr
   struct Ray { float3 dir, v_up, v_right; };
-
-  __device__ __forceinline__ float extinction(float density) const {
-    return tf_ext ? tf_scalar(tf_ext, tf_n, density) : tf_alpha(tf, tf_n, density);
-  }
 
   // main(), gt_ray_marching.comp:396-399.
   __device__ __forceinline__ void begin(Ray& r, float3 dir) const {
@@ -557,12 +552,12 @@ struct GtShade {
     ++aux;
     float s = g->gap;
     float3 S = f.vol.grid;
-    float st0 = extinction(sample_volume(f.vol, tx + w * s));
+    float st0 = tf_alpha(tf, tf_n, sample_volume(f.vol, tx + w * s));
     for (int guard = 0; guard < kMaxLightSteps && s < dist; ++guard) {
       float h = fminf(g->lstep, dist - s);
       float3 at = tx + w * (s + h);
       if (at.x < 0.0f || at.x > S.x || at.y < 0.0f || at.y > S.y || at.z < 0.0f || at.z > S.z) break;
-      float st1 = extinction(sample_volume(f.vol, at));
+      float st1 = tf_alpha(tf, tf_n, sample_volume(f.vol, at));
       ++aux;
       vt *= expf(-((st0 + st1) * 0.5f) * h);
       if ((1.0f - vt) > 0.99f) break;
