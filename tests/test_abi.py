@@ -34,6 +34,9 @@ def test_null_and_bad_arguments_are_errors(lib):
     assert lib.cvr_create(None, 0) == abi.CVR_ERR_INVALID_ARG
     assert lib.cvr_sync(None) == abi.CVR_ERR_INVALID_ARG
     assert lib.cvr_set_volume(None, None, 1, 1, 1, 1, 1.0, 1.0, 1.0) == abi.CVR_ERR_INVALID_ARG
+    assert lib.cvr_prepare_sat(None) == abi.CVR_ERR_INVALID_ARG
+    assert lib.cvr_build_sat(None, None, 256) == abi.CVR_ERR_INVALID_ARG
+    assert lib.cvr_batch_create(None, None, 0, None) == abi.CVR_ERR_INVALID_ARG
     lib.cvr_destroy(None)  # no-op
     rgb = np.zeros((1, 4))
     assert lib.cvr_tf_build_linear(0, 0, abi.dptr(rgb), 0, abi.dptr(rgb), 0, None, None) == abi.CVR_ERR_INVALID_ARG
