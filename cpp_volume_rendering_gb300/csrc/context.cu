@@ -1128,11 +1128,12 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
                         size_t params_size, int w, int h, int reps, int* btw, int* bth, int* bv, float* bms) {
   if (!c || reps <= 0 || reps > 100) return fail(c, CVR_ERR_INVALID_ARG, "cvr_autotune: bad arguments");
   // Coordinate descent over three groups: ray tile (8x8 to 32x8: 2, 4 and 8
-  // warps) x register variant, warp shape (4x8, 8x4, 16x2 pixels), volume
-  // layout (plain, bricks of 8^3, 16^3, 32^3, x-y quads; -1 stands for the
-  // quads).  Each sweep times every member of a group with the other two
-  // fixed at the best so far; the search stops after a sweep that changes
-  // nothing (at most three).  Each configuration is timed once (memoised).
+  // warps) x warp shape (4x8, 8x4, 16x2 pixels; the two interact: a warp
+  // shape fits some tiles only), register variant, volume layout (plain,
+  // bricks of 8^3, 16^3, 32^3, x-y quads; -1 stands for the quads).  Each
+  // sweep times every member of a group with the other two fixed at the best
+  // so far; the search stops after a sweep that changes nothing (at most
+  // three).  Each configuration is timed once (memoised).
   static const int tiles[6][2] = {{8, 8}, {16, 8}, {32, 4}, {8, 16}, {32, 8}, {16, 16}};
   static const int bricks[5] = {0, 3, 4, 5, -1};
   static const int warps[3] = {8, 4, 16};
@@ -1174,12 +1175,10 @@ cvr_status cvr_autotune(cvr_ctx* c, int method, const cvr_camera* cam, const cvr
   };
   for (int sweep = 0; sweep < 3 && s == CVR_OK; ++sweep) {
     const int before[4] = {bt, bvar, bw, bb};
-    for (int t = 0; t < 6; ++t) {
-      const int wi = warp_fits(tiles[t][0], tiles[t][1], warps[bw]) ? bw : 0;
-      for (int v = 0; v < n_variants; ++v) trial(t, v, wi, bb);
-    }
-    for (int wi = 0; wi < 3; ++wi)
-      if (warp_fits(tiles[bt][0], tiles[bt][1], warps[wi])) trial(bt, bvar, wi, bb);
+    for (int t = 0; t < 6; ++t)
+      for (int wi = 0; wi < 3; ++wi)
+        if (warp_fits(tiles[t][0], tiles[t][1], warps[wi])) trial(t, bvar, wi, bb);
+    for (int v = 0; v < n_variants; ++v) trial(bt, v, bw, bb);
     for (int k = 0; k < 5; ++k) trial(bt, bvar, bw, k);
     if (before[0] == bt && before[1] == bvar && before[2] == bw && before[3] == bb) break;
   }
